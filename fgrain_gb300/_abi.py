@@ -1,0 +1,153 @@
+"""ctypes view of include/fgrain_cuda.h.
+
+The structures below mirror the C declarations field for field; every function prototype is
+declared so that ctypes checks argument types.  Loading fails loudly when the shared library has
+not been built: there is no Python or CPU fallback for the path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libfgrain_cuda.so"
+
+FG_OK = 0
+STATUS_NAMES = {
+    0: "FG_OK",
+    1: "FG_ERR_ADAPTER_NOT_FOUND",
+    2: "FG_ERR_DEVICE_REQUEST_FAILED",
+    3: "FG_ERR_CHANNEL",
+    4: "FG_ERR_BUFFER_MAP",
+    5: "FG_ERR_BUFFER_RANGE",
+    6: "FG_ERR_PIPELINE",
+    16: "FG_ERR_INVALID_ARG",
+    17: "FG_ERR_OOM",
+    18: "FG_ERR_DEVICE_TIMEOUT",
+    19: "FG_ERR_DEVICE_OVERFLOW",
+}
+
+
+class fg_optics(C.Structure):
+    _fields_ = [("refractive_index", C.c_double), ("absorption_coeff", C.c_double),
+                ("scattering_coeff", C.c_double), ("anisotropy_g", C.c_double),
+                ("antihalation_reflectance", C.c_double), ("antihalation_density", C.c_double)]
+
+
+class fg_emulsion_cfg(C.Structure):
+    _fields_ = [("width", C.c_double), ("height", C.c_double), ("depth", C.c_double),
+                ("r_min", C.c_double), ("mean_crystal_radius", C.c_double),
+                ("size_variance", C.c_double), ("morphology", C.c_int32), ("_pad", C.c_int32),
+                ("tabular_aspect_ratio", C.c_double), ("optics", fg_optics),
+                ("base_sensitivity", C.c_double)]
+
+
+class fg_exposure_cfg(C.Structure):
+    _fields_ = [("photons_per_sq_um", C.c_double), ("illumination_angle_rad", C.c_double),
+                ("crystal_absorption_coeff", C.c_double), ("max_bounces", C.c_uint32),
+                ("_pad", C.c_uint32)]
+
+
+class fg_dev_cfg(C.Structure):
+    _fields_ = [("threshold_photons", C.c_uint32), ("_pad", C.c_uint32),
+                ("filament_expansion", C.c_double), ("clumping_proximity_factor", C.c_double),
+                ("developer_contrast", C.c_double)]
+
+
+class fg_dev_report(C.Structure):
+    _fields_ = [("total_crystals", C.c_uint64), ("developed_crystals", C.c_uint64),
+                ("fixed_crystals", C.c_uint64), ("total_clumps", C.c_uint64),
+                ("max_clump_size", C.c_uint64), ("avg_clump_size", C.c_double)]
+
+
+class fg_scan_cfg(C.Structure):
+    _fields_ = [("width_px", C.c_uint32), ("height_px", C.c_uint32),
+                ("samples_per_pixel", C.c_uint32), ("mode", C.c_int32),
+                ("silver_opacity", C.c_double)]
+
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+
+
+class fg_crystals_host(C.Structure):
+    _fields_ = [("pos", _dp), ("dims", _dp), ("quat", _dp), ("sensitivity", _dp),
+                ("morphology", _ip)]
+
+
+class fg_crystals_out(C.Structure):
+    _fields_ = [("pos", _dp), ("dims", _dp), ("quat", _dp), ("sensitivity", _dp),
+                ("morphology", _ip)]
+
+
+class fg_segment(C.Structure):
+    _fields_ = [("origin", C.c_double * 3), ("dir", C.c_double * 3), ("step", C.c_double),
+                ("energy", C.c_double), ("photon", C.c_uint32), ("bounce", C.c_uint32)]
+
+
+class fg_timings(C.Structure):
+    _fields_ = [("synth_ms", C.c_double), ("bvh_ms", C.c_double), ("transport_ms", C.c_double),
+                ("develop_ms", C.c_double), ("scan_ms", C.c_double), ("post_ms", C.c_double),
+                ("total_ms", C.c_double), ("crystals", C.c_uint64), ("photons", C.c_uint64),
+                ("hits", C.c_uint64), ("rays", C.c_uint64), ("developed", C.c_uint64),
+                ("fallbacks", C.c_uint64), ("kernel_launches", C.c_uint32),
+                ("error_word", C.c_uint32)]
+
+
+_vp = C.c_void_p
+_st = C.c_int
+_u32p = C.POINTER(C.c_uint32)
+_u8p = C.POINTER(C.c_uint8)
+_u16p = C.POINTER(C.c_uint16)
+_i64p = C.POINTER(C.c_int64)
+_fp = C.POINTER(C.c_float)
+_szp = C.POINTER(C.c_size_t)
+
+# name -> (restype, argtypes); the complete list of entry points in include/fgrain_cuda.h.
+PROTOTYPES = {
+    "fg_engine_create": (_st, [C.c_int, C.POINTER(_vp)]),
+    "fg_engine_destroy": (_st, [_vp]),
+    "fg_last_error": (C.c_char_p, [_vp]),
+    "fg_engine_device_name": (C.c_char_p, [_vp]),
+    "fg_engine_timings": (_st, [_vp, C.POINTER(fg_timings)]),
+    "fg_status_string": (C.c_char_p, [_st]),
+    "fg_emulsion_preset": (_st, [C.c_char_p, C.c_double, C.c_double, C.POINTER(fg_emulsion_cfg)]),
+    "fg_emulsion_upload": (_st, [_vp, C.POINTER(fg_emulsion_cfg), C.POINTER(fg_crystals_host),
+                                 C.c_size_t, C.POINTER(_vp)]),
+    "fg_emulsion_destroy": (_st, [_vp, _vp]),
+    "fg_emulsion_count": (_st, [_vp, _szp]),
+    "fg_emulsion_download": (_st, [_vp, _vp, C.POINTER(fg_crystals_out)]),
+    "fg_emulsion_get_counts": (_st, [_vp, _vp, _u32p]),
+    "fg_emulsion_set_counts": (_st, [_vp, _vp, _u32p]),
+    "fg_emulsion_get_development": (_st, [_vp, _vp, _u8p, _i64p, _dp]),
+    "fg_emulsion_set_development": (_st, [_vp, _vp, _u8p, _dp]),
+    "fg_expose_emulsion": (_st, [_vp, _vp, _fp, C.c_uint32, C.c_uint32,
+                                 C.POINTER(fg_exposure_cfg), C.c_uint64]),
+    "fg_develop_emulsion": (_st, [_vp, _vp, C.POINTER(fg_dev_cfg), C.POINTER(fg_dev_report)]),
+    "fg_scan_emulsion": (_st, [_vp, _vp, C.POINTER(fg_scan_cfg), C.c_uint64, _fp, _fp, _u8p]),
+    "fg_replay_segments": (_st, [_vp, _vp, C.POINTER(fg_exposure_cfg), C.c_uint64,
+                                 C.POINTER(fg_segment), C.c_size_t, _u32p, _u32p, C.c_size_t,
+                                 _szp]),
+    "fg_replay_rays": (_st, [_vp, _vp, _dp, _dp, C.c_size_t, C.c_int, _u32p, _u32p,
+                             C.c_size_t, _szp, _dp]),
+    "fg_scan_ray_hits": (_st, [_vp, _vp, C.POINTER(fg_scan_cfg), C.c_uint64, _u16p]),
+}
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Loads libfgrain_cuda.so (built by fgrain_gb300.build) and declares every prototype."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise ImportError(
+            f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+            "(the fgrain GB300 path has no CPU fallback)")
+    lib = C.CDLL(str(LIB_PATH))
+    for name, (res, args) in PROTOTYPES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib

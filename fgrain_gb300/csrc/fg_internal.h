@@ -1,0 +1,183 @@
+// Host-side internals shared by the translation units of libfgrain_cuda.so.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/fgrain_cuda.h"
+#include "fg_device.cuh"
+
+namespace fg {
+
+// A failed CUDA call or a rejected argument, carried to the C boundary as (status, message).
+struct Error {
+  fg_status st;
+  std::string msg;
+};
+
+#define FG_CUDA(call)                                                                     \
+  do {                                                                                    \
+    cudaError_t e__ = (call);                                                             \
+    if (e__ != cudaSuccess) throw ::fg::Error{::fg::status_of(e__), std::string(#call) + \
+                                              ": " + cudaGetErrorString(e__)};            \
+  } while (0)
+
+#define FG_REQUIRE(cond, msg)                                                   \
+  do {                                                                          \
+    if (!(cond)) throw ::fg::Error{FG_ERR_INVALID_ARG, std::string(msg)};       \
+  } while (0)
+
+inline fg_status status_of(cudaError_t e) {
+  switch (e) {
+    case cudaErrorMemoryAllocation: return FG_ERR_OOM;
+    case cudaErrorInvalidDevice:
+    case cudaErrorNoDevice:
+    case cudaErrorInsufficientDriver: return FG_ERR_ADAPTER_NOT_FOUND;
+    case cudaErrorInvalidValue: return FG_ERR_INVALID_ARG;
+    default: return FG_ERR_PIPELINE;
+  }
+}
+
+// Device buffer owned by RAII; stream-ordered allocation on the engine stream.
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaStream_t s = nullptr;
+  DBuf() = default;
+  DBuf(size_t count, cudaStream_t st) { alloc(count, st); }
+  void alloc(size_t count, cudaStream_t st) {
+    release();
+    s = st;
+    n = count;
+    if (count) FG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&p), count * sizeof(T), st));
+  }
+  void release() {
+    if (p) cudaFreeAsync(p, s);
+    p = nullptr;
+    n = 0;
+  }
+  ~DBuf() { release(); }
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n), s(o.s) { o.p = nullptr; o.n = 0; }
+  DBuf& operator=(DBuf&& o) noexcept {
+    if (this != &o) { release(); p = o.p; n = o.n; s = o.s; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+};
+
+// Stage timer: events recorded on the engine stream around each stage.
+struct StageTimer {
+  cudaEvent_t ev[2 * 8];
+  int used = 0;
+  bool made = false;
+  void init() {
+    if (made) return;
+    for (auto& e : ev) FG_CUDA(cudaEventCreate(&e));
+    made = true;
+  }
+  void destroy() {
+    if (!made) return;
+    for (auto& e : ev) cudaEventDestroy(e);
+    made = false;
+  }
+};
+
+}  // namespace fg
+
+struct fg_engine {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::recursive_mutex mu;
+  std::string err;
+  std::string name;
+  uint32_t* d_err = nullptr;                    // device error word
+  unsigned long long* d_stats = nullptr;        // device counters (hits, fallbacks, ...)
+  fg_timings timings{};
+  int sm_count = 0;
+  fg::StageTimer timer;
+};
+
+struct fg_emulsion {
+  fg_emulsion_cfg cfg{};
+  uint32_t n = 0;
+  cudaStream_t stream = nullptr;
+  // Hot crystal records in Morton order.
+  fg::DBuf<float4> a, q, d;
+  // FP64 copies (uploaded sets only).
+  fg::DBuf<double> pos64, dims64, quat64, sens64;
+  fg::DBuf<uint32_t> sorted_to_id, id_to_sorted;
+  // LBVH over undeveloped geometry.
+  fg::DBuf<fg::Node> nodes;
+  fg::DBuf<int> leaf_parent;
+  // Mutable per-crystal state (Morton order).
+  fg::DBuf<uint32_t> counts;
+  fg::DBuf<uint8_t> developed;
+  fg::DBuf<float> exp32;
+  fg::DBuf<double> exp64;
+  fg::DBuf<int64_t> clump;  // by crystal id
+  bool has64 = false;
+  double extent = 0.0;             // largest coordinate magnitude (sets the box padding)
+  std::vector<uint32_t> h_s2id;    // host copy of sorted_to_id (empty: identity)
+
+  fg::CrystalsView view() const {
+    fg::CrystalsView v;
+    v.a = a.p; v.q = q.p; v.d = d.p;
+    v.pos64 = has64 ? pos64.p : nullptr;
+    v.dims64 = has64 ? dims64.p : nullptr;
+    v.quat64 = has64 ? quat64.p : nullptr;
+    v.sens64 = has64 ? sens64.p : nullptr;
+    v.n = n;
+    return v;
+  }
+};
+
+namespace fg {
+
+// fg_bvh.cu
+// Builds (or refits) the LBVH of an emulsion whose crystals are already in Morton order.
+// keys: sorted 64-bit Morton keys (device).  developed_geometry: leaf boxes of developed crystals
+// with their expansion (undeveloped leaves get empty boxes) instead of the raw geometry.
+void build_lbvh(fg_emulsion* em, const uint64_t* keys, Node* nodes, int* leaf_parent,
+                bool developed_geometry, cudaStream_t st);
+void refit_lbvh(fg_emulsion* em, Node* nodes, const int* leaf_parent, bool developed_geometry,
+                cudaStream_t st);
+// Sorts crystals by Morton code and fills the hot arrays; returns the sorted keys.
+// pos_host / pos_dev: id-ordered FP64 positions on the host and on the device.
+void morton_order(fg_emulsion* em, const double* pos_host, const double* pos_dev, cudaStream_t st,
+                  DBuf<uint64_t>& keys, DBuf<uint32_t>& order);
+void gather_sorted(fg_emulsion* em, const uint32_t* order, const double* pos, const double* dims,
+                   const double* quat, const double* sens, const int32_t* morph, int32_t morph_all,
+                   cudaStream_t st);
+
+// fg_develop.cu
+void develop(fg_engine* e, fg_emulsion* em, const fg_dev_cfg& cfg, fg_dev_report* rep);
+
+// fg_scan.cu
+struct ScanOut {
+  float* out = nullptr;      // mode-mapped value per pixel
+  uint8_t* image8 = nullptr; // 8-bit image
+  float* d_neg = nullptr;    // -log10(clamp(T)) + 0.05
+  uint16_t* ray_hits = nullptr;
+};
+void scan(fg_engine* e, const fg_emulsion* em, const fg_scan_cfg& cfg, uint64_t seed,
+          const float* sigma_sorted, const ScanOut& out);
+
+// fg_transport.cu
+void expose(fg_engine* e, fg_emulsion* em, const float* tile_dev, uint32_t tw, uint32_t th,
+            const fg_exposure_cfg& cfg, uint64_t seed, unsigned long long* photons_out);
+
+// Exclusive prefix sum on the device (CUB).
+void exclusive_scan_u32(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t st);
+
+// Raises an Error when a kernel reported one through the engine's error word.
+void check_error_word(fg_engine* e);
+
+inline unsigned grid_for(size_t n, unsigned block) {
+  return static_cast<unsigned>((n + block - 1) / block);
+}
+
+}  // namespace fg

@@ -1,0 +1,310 @@
+// Monte-Carlo photon transport (transport.rs:48-188 and optics.rs:75-196) as a persistent,
+// warp-scheduled kernel over one or many tiles, plus the exact replay of recorded segments.
+//
+// Work: photon ids of all tiles form one index space; each warp takes 32 ids at a time from a
+// global counter.  Every draw is a Philox block named by (photon, bounce, slot, tag), so results
+// do not depend on which warp or SM traces a photon.  Hits of one segment are collected, ordered
+// by (t_enter, crystal id) and absorbed in that order (Beer-Lambert, Bernoulli rounding of
+// 5 E p s latent photons, energy *= max(1 - 0.9 p, 0.05)).  Counts reach HBM as warp-aggregated
+// atomics.
+#include "fg_internal.h"
+#include "fg_transport.cuh"
+
+namespace fg {
+
+// ---------------------------------------------------------------------------------------------
+// Production (FP32) kernel.
+__global__ void __launch_bounds__(256) k_transport(const TileDesc* __restrict__ tiles, int ntiles,
+                                                  unsigned long long total,
+                                                  unsigned long long* next, uint32_t* err,
+                                                  unsigned long long* stats) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long my_hits = 0;
+  for (;;) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(next, 32ull);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= total) break;
+    const unsigned long long gid = base + lane;
+    if (gid < total) {
+      int lo = 0, hi = ntiles - 1;
+      while (lo < hi) {  // last tile whose first photon is <= gid
+        const int mid = (lo + hi + 1) >> 1;
+        if (tiles[mid].photon_base <= gid) lo = mid; else hi = mid - 1;
+      }
+      const TileDesc& t = tiles[lo];
+      my_hits += trace_photon(t, static_cast<uint32_t>(gid - t.photon_base), err);
+    }
+  }
+  if (stats) {
+    for (int o = 16; o > 0; o >>= 1) my_hits += __shfl_down_sync(0xffffffffu, my_hits, o);
+    if (lane == 0 && my_hits) atomicAdd(&stats[0], my_hits);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Exact replay of recorded segments: FP32 LBVH walk for candidates, the reference predicate and
+// per-hit arithmetic in FP64.  pass 0 counts hits per segment; pass 1 writes hit ids and adds the
+// latent photons.
+struct Hit64 {
+  double t0, t1;
+  uint32_t id, s;
+};
+
+__global__ void k_replay_segments(const fg_segment* __restrict__ segs, uint32_t nseg,
+                                  CrystalsView cv, const Node* __restrict__ nodes,
+                                  const uint32_t* __restrict__ s2id, uint32_t n, double alpha,
+                                  uint32_t k0, uint32_t k1, int pass, uint32_t* seg_count,
+                                  const uint32_t* offsets, uint32_t* ids, uint32_t id_cap,
+                                  uint32_t* counts, uint32_t* err) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nseg || n == 0) return;
+  const fg_segment g = segs[i];
+  const D3 o = d3(g.origin[0], g.origin[1], g.origin[2]);
+  const D3 d = d3(g.dir[0], g.dir[1], g.dir[2]);
+  const D3 inv = d3(__ddiv_rn(1.0, d.x), __ddiv_rn(1.0, d.y), __ddiv_rn(1.0, d.z));
+  const float3 of = make_float3((float)o.x, (float)o.y, (float)o.z);
+  const float3 invf = make_float3(1.0f / (float)d.x, 1.0f / (float)d.y, 1.0f / (float)d.z);
+  const float tlim = (float)g.step * 1.00001f + 1e-3f;
+  Hit64 hits[HMAX];
+  int nh = 0;
+  walk_lbvh(nodes, of, invf, tlim, err, [&](uint32_t s) {
+    const Crystal64 k = load64(cv, s);
+    double t0, t1;
+    if (!dcanonical_hit(k, 1.0, o, d, inv, t0, t1)) return;
+    if (!(t0 < g.step)) return;
+    const double path = fmax(__dsub_rn(fmin(t1, g.step), t0), 0.0);
+    if (!(path > 0.0)) return;
+    const uint32_t id = s2id ? s2id[s] : s;
+    if (nh == HMAX) { atomicOr(err, ERR_HIT_OVERFLOW); return; }
+    int j = nh++;
+    while (j > 0 && (hits[j - 1].t0 > t0 || (hits[j - 1].t0 == t0 && hits[j - 1].id > id))) {
+      hits[j] = hits[j - 1];
+      --j;
+    }
+    hits[j] = Hit64{t0, t1, id, s};
+  });
+  if (pass == 0) {
+    seg_count[i] = static_cast<uint32_t>(nh);
+    return;
+  }
+  double E = g.energy;
+  const uint32_t base = offsets[i];
+  P4 r{};
+  for (int h = 0; h < nh; ++h) {
+    if ((h & 3) == 0) r = philox(g.photon, g.bounce, static_cast<uint32_t>(h) >> 2, TAG_HIT, k0, k1);
+    const double u = ud(word(r, h & 3));
+    const double path = fmax(__dsub_rn(fmin(hits[h].t1, g.step), hits[h].t0), 0.0);
+    const double sens = cv.sens64 ? cv.sens64[hits[h].s] : (double)cv.a[hits[h].s].w;
+    uint32_t cnt;
+    E = absorb64(E, path, alpha, sens, u, &cnt);
+    if (cnt) atomicAdd(&counts[hits[h].s], cnt);
+    if (base + h < id_cap) ids[base + h] = hits[h].id;
+  }
+}
+
+// Hits of arbitrary rays (no step limit), exact rule; e is the expansion of developed crystals.
+__global__ void k_replay_rays(const double* __restrict__ org, const double* __restrict__ dir,
+                              uint32_t nrays, CrystalsView cv, const Node* __restrict__ nodes,
+                              const uint32_t* __restrict__ s2id, uint32_t n,
+                              const uint8_t* developed, const double* exp64, int developed_only,
+                              int pass, uint32_t* ray_count, const uint32_t* offsets,
+                              uint32_t* ids, uint32_t id_cap, double* chord_sum, uint32_t* err) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrays) return;
+  const D3 o = d3(org[3 * i], org[3 * i + 1], org[3 * i + 2]);
+  const D3 d = d3(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]);
+  const D3 inv = d3(__ddiv_rn(1.0, d.x), __ddiv_rn(1.0, d.y), __ddiv_rn(1.0, d.z));
+  const float3 of = make_float3((float)o.x, (float)o.y, (float)o.z);
+  const float3 invf = make_float3(1.0f / (float)d.x, 1.0f / (float)d.y, 1.0f / (float)d.z);
+  Hit64 hits[HMAX];
+  int nh = 0;
+  if (n > 0) {
+    walk_lbvh(nodes, of, invf, INFINITY, err, [&](uint32_t s) {
+      if (developed_only && !developed[s]) return;
+      const double e = developed_only ? exp64[s] : 1.0;
+      const Crystal64 k = load64(cv, s);
+      double t0, t1;
+      if (!dcanonical_hit(k, e, o, d, inv, t0, t1)) return;
+      const uint32_t id = s2id ? s2id[s] : s;
+      if (nh == HMAX) { atomicOr(err, ERR_HIT_OVERFLOW); return; }
+      int j = nh++;
+      while (j > 0 && (hits[j - 1].t0 > t0 || (hits[j - 1].t0 == t0 && hits[j - 1].id > id))) {
+        hits[j] = hits[j - 1];
+        --j;
+      }
+      hits[j] = Hit64{t0, t1, id, s};
+    });
+  }
+  if (pass == 0) {
+    ray_count[i] = static_cast<uint32_t>(nh);
+    return;
+  }
+  const uint32_t base = offsets[i];
+  double L = 0.0;
+  for (int h = 0; h < nh; ++h) {
+    L = __dadd_rn(L, fmax(__dsub_rn(hits[h].t1, hits[h].t0), 0.0));
+    if (base + h < id_cap) ids[base + h] = hits[h].id;
+  }
+  if (chord_sum) chord_sum[i] = L;
+}
+
+// ---------------------------------------------------------------------------------------------
+TileDesc make_tile_desc(const fg_emulsion* em, const float* tile_dev, uint32_t tw, uint32_t th,
+                        const fg_exposure_cfg& cfg, uint64_t seed, uint32_t* counts) {
+  TileDesc t{};
+  t.a = em->a.p;
+  t.q = em->q.p;
+  t.d = em->d.p;
+  t.nodes = em->nodes.p;
+  t.s2id = em->sorted_to_id.p;
+  t.n = em->n;
+  t.counts = counts;
+  t.tile = tile_dev;
+  t.tw = tw;
+  t.th = th;
+  t.W = (float)em->cfg.width;
+  t.H = (float)em->cfg.height;
+  t.D = (float)em->cfg.depth;
+  const double P = std::round(em->cfg.width * em->cfg.height * cfg.photons_per_sq_um);
+  t.P = P > 0 ? static_cast<uint32_t>(P) : 0u;
+  t.k0 = static_cast<uint32_t>(seed);
+  t.k1 = static_cast<uint32_t>(seed >> 32);
+  const fg_optics& o = em->cfg.optics;
+  const double mu_t = o.absorption_coeff + o.scattering_coeff;
+  t.mu_t = (float)mu_t;
+  t.albedo = (float)(mu_t > 0.0 ? o.scattering_coeff / mu_t : 0.0);
+  t.g = (float)o.anisotropy_g;
+  const double r = (1.0 - o.refractive_index) / (1.0 + o.refractive_index);
+  t.r0 = (float)(r * r);
+  t.eff_r = (float)(o.antihalation_reflectance * std::pow(10.0, -2.0 * o.antihalation_density));
+  t.theta_max = (float)cfg.illumination_angle_rad;
+  t.alpha = (float)cfg.crystal_absorption_coeff;
+  t.max_bounces = cfg.max_bounces;
+  return t;
+}
+
+void launch_transport(const TileDesc* tiles_dev, int ntiles, unsigned long long total,
+                      unsigned long long* counter, uint32_t* err, unsigned long long* stats,
+                      int sm_count, cudaStream_t st) {
+  if (total == 0) return;
+  FG_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
+  const unsigned long long warps = (total + 31) / 32;
+  unsigned blocks = static_cast<unsigned>(std::min<unsigned long long>((warps + 7) / 8, (unsigned long long)sm_count * 8));
+  blocks = std::max(blocks, 1u);
+  k_transport<<<blocks, 256, 0, st>>>(tiles_dev, ntiles, total, counter, err, stats);
+  FG_CUDA(cudaGetLastError());
+}
+
+void expose(fg_engine* e, fg_emulsion* em, const float* tile_dev, uint32_t tw, uint32_t th,
+            const fg_exposure_cfg& cfg, uint64_t seed, unsigned long long* photons_out) {
+  cudaStream_t st = e->stream;
+  const TileDesc t = make_tile_desc(em, tile_dev, tw, th, cfg, seed, em->counts.p);
+  if (photons_out) *photons_out = t.P;
+  if (t.P == 0 || em->n == 0) return;
+  DBuf<TileDesc> td(1, st);
+  DBuf<unsigned long long> ctr(1, st);
+  FG_CUDA(cudaMemcpyAsync(td.p, &t, sizeof(TileDesc), cudaMemcpyHostToDevice, st));
+  launch_transport(td.p, 1, t.P, ctr.p, e->d_err, e->d_stats, e->sm_count, st);
+}
+
+void replay_segments(fg_engine* e, fg_emulsion* em, const fg_exposure_cfg& cfg, uint64_t seed,
+                     const fg_segment* segs_host, size_t nseg, uint32_t* offsets_host,
+                     uint32_t* ids_host, size_t id_cap, size_t* nhits) {
+  cudaStream_t st = e->stream;
+  FG_REQUIRE(nseg < 0x7fffffffu, "too many segments");
+  DBuf<fg_segment> segs(std::max<size_t>(nseg, 1), st);
+  DBuf<uint32_t> cnt(nseg + 1, st), off(nseg + 1, st);
+  if (nseg) FG_CUDA(cudaMemcpyAsync(segs.p, segs_host, nseg * sizeof(fg_segment), cudaMemcpyHostToDevice, st));
+  const uint32_t k0 = static_cast<uint32_t>(seed), k1 = static_cast<uint32_t>(seed >> 32);
+  const unsigned grid = grid_for(std::max<size_t>(nseg, 1), 128);
+  k_replay_segments<<<grid, 128, 0, st>>>(segs.p, (uint32_t)nseg, em->view(), em->nodes.p,
+                                          em->sorted_to_id.p, em->n, cfg.crystal_absorption_coeff,
+                                          k0, k1, 0, cnt.p, nullptr, nullptr, 0, em->counts.p,
+                                          e->d_err);
+  FG_CUDA(cudaGetLastError());
+  std::vector<uint32_t> hc(nseg + 1, 0);
+  if (nseg) FG_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, nseg * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  FG_CUDA(cudaStreamSynchronize(st));
+  std::vector<uint32_t> ho(nseg + 1, 0);
+  uint64_t acc = 0;
+  for (size_t i = 0; i < nseg; ++i) {
+    ho[i] = static_cast<uint32_t>(acc);
+    acc += hc[i];
+  }
+  ho[nseg] = static_cast<uint32_t>(acc);
+  FG_REQUIRE(acc < 0xffffffffull, "too many hits");
+  if (nhits) *nhits = acc;
+  FG_CUDA(cudaMemcpyAsync(off.p, ho.data(), (nseg + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+  DBuf<uint32_t> ids(std::max<uint64_t>(std::min<uint64_t>(acc, id_cap), 1), st);
+  k_replay_segments<<<grid, 128, 0, st>>>(segs.p, (uint32_t)nseg, em->view(), em->nodes.p,
+                                          em->sorted_to_id.p, em->n, cfg.crystal_absorption_coeff,
+                                          k0, k1, 1, nullptr, off.p, ids.p,
+                                          static_cast<uint32_t>(std::min<uint64_t>(acc, id_cap)),
+                                          em->counts.p, e->d_err);
+  FG_CUDA(cudaGetLastError());
+  if (ids_host && acc) {
+    FG_CUDA(cudaMemcpyAsync(ids_host, ids.p, std::min<uint64_t>(acc, id_cap) * sizeof(uint32_t),
+                            cudaMemcpyDeviceToHost, st));
+  }
+  FG_CUDA(cudaStreamSynchronize(st));
+  if (offsets_host) std::copy(ho.begin(), ho.end(), offsets_host);
+}
+
+void replay_rays(fg_engine* e, const fg_emulsion* em, const double* org_host,
+                 const double* dir_host, size_t nrays, int developed_only, uint32_t* offsets_host,
+                 uint32_t* ids_host, size_t id_cap, size_t* nhits, double* chord_host) {
+  cudaStream_t st = e->stream;
+  FG_REQUIRE(nrays < 0x7fffffffu, "too many rays");
+  DBuf<double> org(std::max<size_t>(3 * nrays, 1), st), dir(std::max<size_t>(3 * nrays, 1), st);
+  DBuf<uint32_t> cnt(nrays + 1, st), off(nrays + 1, st);
+  DBuf<double> chord(std::max<size_t>(nrays, 1), st);
+  if (nrays) {
+    FG_CUDA(cudaMemcpyAsync(org.p, org_host, 3 * nrays * sizeof(double), cudaMemcpyHostToDevice, st));
+    FG_CUDA(cudaMemcpyAsync(dir.p, dir_host, 3 * nrays * sizeof(double), cudaMemcpyHostToDevice, st));
+  }
+  // Developed crystals are tested with their expansion: walk a refitted copy of the tree.
+  const Node* nodes = em->nodes.p;
+  DBuf<Node> dev_nodes;
+  if (developed_only && em->n > 0) {
+    dev_nodes.alloc(em->nodes.n, st);
+    FG_CUDA(cudaMemcpyAsync(dev_nodes.p, em->nodes.p, em->nodes.n * sizeof(Node), cudaMemcpyDeviceToDevice, st));
+    refit_lbvh(const_cast<fg_emulsion*>(em), dev_nodes.p, em->leaf_parent.p, true, st);
+    nodes = dev_nodes.p;
+  }
+  const unsigned grid = grid_for(std::max<size_t>(nrays, 1), 128);
+  k_replay_rays<<<grid, 128, 0, st>>>(org.p, dir.p, (uint32_t)nrays, em->view(), nodes,
+                                      em->sorted_to_id.p, em->n, em->developed.p, em->exp64.p,
+                                      developed_only, 0, cnt.p, nullptr, nullptr, 0, nullptr,
+                                      e->d_err);
+  FG_CUDA(cudaGetLastError());
+  std::vector<uint32_t> hc(nrays + 1, 0);
+  if (nrays) FG_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, nrays * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  FG_CUDA(cudaStreamSynchronize(st));
+  std::vector<uint32_t> ho(nrays + 1, 0);
+  uint64_t acc = 0;
+  for (size_t i = 0; i < nrays; ++i) {
+    ho[i] = static_cast<uint32_t>(acc);
+    acc += hc[i];
+  }
+  ho[nrays] = static_cast<uint32_t>(acc);
+  FG_REQUIRE(acc < 0xffffffffull, "too many hits");
+  if (nhits) *nhits = acc;
+  FG_CUDA(cudaMemcpyAsync(off.p, ho.data(), (nrays + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+  DBuf<uint32_t> ids(std::max<uint64_t>(std::min<uint64_t>(acc, id_cap), 1), st);
+  k_replay_rays<<<grid, 128, 0, st>>>(org.p, dir.p, (uint32_t)nrays, em->view(), nodes,
+                                      em->sorted_to_id.p, em->n, em->developed.p, em->exp64.p,
+                                      developed_only, 1, nullptr, off.p, ids.p,
+                                      static_cast<uint32_t>(std::min<uint64_t>(acc, id_cap)),
+                                      chord.p, e->d_err);
+  FG_CUDA(cudaGetLastError());
+  if (ids_host && acc)
+    FG_CUDA(cudaMemcpyAsync(ids_host, ids.p, std::min<uint64_t>(acc, id_cap) * sizeof(uint32_t),
+                            cudaMemcpyDeviceToHost, st));
+  if (chord_host && nrays)
+    FG_CUDA(cudaMemcpyAsync(chord_host, chord.p, nrays * sizeof(double), cudaMemcpyDeviceToHost, st));
+  FG_CUDA(cudaStreamSynchronize(st));
+  if (offsets_host) std::copy(ho.begin(), ho.end(), offsets_host);
+}
+
+}  // namespace fg

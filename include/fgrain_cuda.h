@@ -1,0 +1,216 @@
+/* fgrain_cuda.h - C ABI of the GB300-native fgrain photon-transport and scan path.
+ *
+ * The library replaces, behind the reference's --gpu switch, the per-tile chain of the Rust
+ * crate fgrain (paths are relative to that project):
+ *   VirtualEmulsionLayer::synthesize   src/emulsion.rs:155
+ *   expose_emulsion                    src/transport.rs:48   (re-exported src/lib.rs:34)
+ *   develop_emulsion                   src/development.rs:59 (re-exported src/lib.rs:24)
+ *   scan_emulsion                      src/transmittance.rs:65 (re-exported src/lib.rs:33)
+ *   GpuEngine::render_tile_all_gpu     src/gpu.rs:491 (engine singleton src/gpu.rs:9-14)
+ * with CPU-path physics (the reference's wgpu shaders run a different model).
+ *
+ * Conventions: plain C types, host pointers unless a name says "device", every entry point
+ * returns fg_status.  An engine is safe to call from several threads: calls are serialised on
+ * the engine's stream, like the reference's dispatch_lock (src/gpu.rs:169,503).  There is no
+ * CPU fallback: on an error the caller decides (the reference falls back to its CPU chain,
+ * src/image_pipeline.rs:535-558).  fg_last_error() returns the message of the last failure.
+ */
+#ifndef FGRAIN_CUDA_H
+#define FGRAIN_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  1-6 mirror GpuError (src/error.rs:9-33) one to one. */
+typedef enum fg_status {
+  FG_OK = 0,
+  FG_ERR_ADAPTER_NOT_FOUND = 1,     /* GpuError::AdapterNotFound: no CUDA device / bad index */
+  FG_ERR_DEVICE_REQUEST_FAILED = 2, /* GpuError::DeviceRequestFailed: context / stream setup */
+  FG_ERR_CHANNEL = 3,               /* GpuError::ChannelError: asynchronous completion failed */
+  FG_ERR_BUFFER_MAP = 4,            /* GpuError::BufferMapError: host<->device copy failed */
+  FG_ERR_BUFFER_RANGE = 5,          /* GpuError::BufferRangeError: size / capacity mismatch */
+  FG_ERR_PIPELINE = 6,              /* GpuError::PipelineError: kernel launch or fault */
+  FG_ERR_INVALID_ARG = 16,          /* bad pointer, size or configuration value */
+  FG_ERR_OOM = 17,                  /* device allocation failed */
+  FG_ERR_DEVICE_TIMEOUT = 18,       /* a bounded device wait gave up (error word set) */
+  FG_ERR_DEVICE_OVERFLOW = 19       /* a fixed device capacity was exceeded (error word set) */
+} fg_status;
+
+typedef struct fg_engine fg_engine;
+typedef struct fg_emulsion fg_emulsion;
+
+typedef enum fg_morphology { FG_CUBIC = 0, FG_TABULAR = 1, FG_OCTAHEDRAL = 2 } fg_morphology;
+
+/* GelatinOptics, src/optics.rs:41-60 */
+typedef struct fg_optics {
+  double refractive_index;
+  double absorption_coeff;
+  double scattering_coeff;
+  double anisotropy_g;
+  double antihalation_reflectance;
+  double antihalation_density;
+} fg_optics;
+
+/* EmulsionConfig, src/emulsion.rs:14-37 (dimensions = width, height, depth in micrometres) */
+typedef struct fg_emulsion_cfg {
+  double width, height, depth;
+  double r_min;
+  double mean_crystal_radius;
+  double size_variance;
+  int32_t morphology; /* fg_morphology */
+  int32_t _pad;
+  double tabular_aspect_ratio;
+  fg_optics optics;
+  double base_sensitivity;
+} fg_emulsion_cfg;
+
+/* ExposureConfig, src/transport.rs:15-28 */
+typedef struct fg_exposure_cfg {
+  double photons_per_sq_um;
+  double illumination_angle_rad;
+  double crystal_absorption_coeff;
+  uint32_t max_bounces;
+  uint32_t _pad;
+} fg_exposure_cfg;
+
+/* DevelopmentConfig, src/development.rs:12-27 */
+typedef struct fg_dev_cfg {
+  uint32_t threshold_photons;
+  uint32_t _pad;
+  double filament_expansion;
+  double clumping_proximity_factor;
+  double developer_contrast;
+} fg_dev_cfg;
+
+/* DevelopmentReport, src/development.rs:42-56 */
+typedef struct fg_dev_report {
+  uint64_t total_crystals;
+  uint64_t developed_crystals;
+  uint64_t fixed_crystals;
+  uint64_t total_clumps;
+  uint64_t max_clump_size;
+  double avg_clump_size;
+} fg_dev_report;
+
+/* ScanMode / ScanConfig, src/transmittance.rs:17-48 */
+typedef enum fg_scan_mode { FG_SCAN_NEGATIVE = 0, FG_SCAN_POSITIVE = 1, FG_SCAN_OPTICAL_DENSITY = 2 } fg_scan_mode;
+typedef struct fg_scan_cfg {
+  uint32_t width_px;
+  uint32_t height_px;
+  uint32_t samples_per_pixel;
+  int32_t mode; /* fg_scan_mode */
+  double silver_opacity;
+} fg_scan_cfg;
+
+/* A crystal set on the host, structure of arrays in crystal-index order (HalideCrystal,
+ * src/crystal.rs:21-50).  pos/dims: 3 doubles per crystal; quat: (i, j, k, w); morphology may be
+ * NULL (then cfg->morphology applies to all). */
+typedef struct fg_crystals_host {
+  const double* pos;
+  const double* dims;
+  const double* quat;
+  const double* sensitivity;
+  const int32_t* morphology;
+} fg_crystals_host;
+
+/* Same layout for downloads (any pointer may be NULL). */
+typedef struct fg_crystals_out {
+  double* pos;
+  double* dims;
+  double* quat;
+  double* sensitivity;
+  int32_t* morphology;
+} fg_crystals_out;
+
+/* One photon segment as the reference's bounce loop sees it (src/transport.rs:101-185): the
+ * position and direction a bounce starts from, its step length and the packet energy. */
+typedef struct fg_segment {
+  double origin[3];
+  double dir[3];
+  double step;
+  double energy;
+  uint32_t photon;
+  uint32_t bounce;
+} fg_segment;
+
+/* Device time of the stages of the last call on an engine (CUDA events, milliseconds) and the
+ * work it did.  Fields a call does not touch are zero. */
+typedef struct fg_timings {
+  double synth_ms, bvh_ms, transport_ms, develop_ms, scan_ms, post_ms, total_ms;
+  uint64_t crystals, photons, hits, rays, developed, fallbacks;
+  uint32_t kernel_launches;
+  uint32_t error_word;
+} fg_timings;
+
+/* ---- engine (GpuEngine::new / get_gpu_engine, src/gpu.rs:9-14,174) ---- */
+fg_status fg_engine_create(int device, fg_engine** out);
+fg_status fg_engine_destroy(fg_engine* e);
+const char* fg_last_error(const fg_engine* e);           /* message of the last failure */
+const char* fg_engine_device_name(const fg_engine* e);   /* GpuEngine::adapter_name, gpu.rs:484 */
+fg_status fg_engine_timings(const fg_engine* e, fg_timings* out);
+const char* fg_status_string(fg_status s);
+
+/* ---- presets (EmulsionConfig::tri_x_400 / tri_x_1600 / t_max_100 / hp5_plus,
+ *      src/emulsion.rs:46-136); name: "tri-x", "tri-x-1600", "t-max", "hp5" ---- */
+fg_status fg_emulsion_preset(const char* name, double width, double height, fg_emulsion_cfg* out);
+
+/* ---- emulsions ---- */
+/* Upload a crystal set (for parity runs on exactly the oracle's crystals).  The device keeps the
+ * FP64 values for exact predicates and builds the Morton-ordered LBVH. */
+fg_status fg_emulsion_upload(fg_engine* e, const fg_emulsion_cfg* cfg, const fg_crystals_host* c,
+                             size_t n, fg_emulsion** out);
+fg_status fg_emulsion_destroy(fg_engine* e, fg_emulsion* em);
+fg_status fg_emulsion_count(const fg_emulsion* em, size_t* n);
+fg_status fg_emulsion_download(fg_engine* e, const fg_emulsion* em, fg_crystals_out* out);
+/* Latent counts (HalideCrystal::latent_photons, src/crystal.rs:41), crystal-index order. */
+fg_status fg_emulsion_get_counts(fg_engine* e, const fg_emulsion* em, uint32_t* counts);
+fg_status fg_emulsion_set_counts(fg_engine* e, fg_emulsion* em, const uint32_t* counts);
+/* Developed flag, clump id (-1 when none) and filament expansion per crystal (any may be NULL). */
+fg_status fg_emulsion_get_development(fg_engine* e, const fg_emulsion* em, uint8_t* developed,
+                                      int64_t* clump, double* expansion);
+/* Fix the developed mask and expansions (a scan with a fixed developed mask). */
+fg_status fg_emulsion_set_development(fg_engine* e, fg_emulsion* em, const uint8_t* developed,
+                                      const double* expansion);
+
+/* ---- stages ---- */
+/* expose_emulsion (src/transport.rs:48-188) with the tile worker's exposure closure: tile is
+ * tw*th row-major float, sampled at the nearest pixel (src/image_pipeline.rs:949-958).  Counts
+ * are added to the emulsion's latent counts, like record_absorption (src/crystal.rs:221). */
+fg_status fg_expose_emulsion(fg_engine* e, fg_emulsion* em, const float* tile, uint32_t tw,
+                             uint32_t th, const fg_exposure_cfg* cfg, uint64_t seed);
+
+/* develop_emulsion (src/development.rs:59-188).  report may be NULL. */
+fg_status fg_develop_emulsion(fg_engine* e, fg_emulsion* em, const fg_dev_cfg* cfg,
+                              fg_dev_report* report);
+
+/* scan_emulsion (src/transmittance.rs:65-171).  out: width*height mode-mapped floats;
+ * image8 (may be NULL): the 8-bit image.  sigma_per_crystal (may be NULL): per-crystal silver
+ * opacity in crystal-index order, replacing cfg->silver_opacity. */
+fg_status fg_scan_emulsion(fg_engine* e, const fg_emulsion* em, const fg_scan_cfg* cfg,
+                           uint64_t seed, const float* sigma_per_crystal, float* out,
+                           uint8_t* image8);
+
+/* ---- replay (parity) ---- */
+/* Replays recorded segments with the exact hit rule and FP64 per-hit arithmetic.  Latent counts
+ * are added to the emulsion.  Hit lists are returned CSR style: offsets[nseg+1], ids (crystal
+ * indices in canonical order); *nhits receives the total even when it exceeds id_cap. */
+fg_status fg_replay_segments(fg_engine* e, fg_emulsion* em, const fg_exposure_cfg* cfg,
+                             uint64_t seed, const fg_segment* segs, size_t nseg,
+                             uint32_t* offsets, uint32_t* ids, size_t id_cap, size_t* nhits);
+/* Hits of arbitrary rays against the developed crystals (exact rule), CSR style, plus the
+ * per-ray sum of chord lengths (may be NULL). */
+fg_status fg_replay_rays(fg_engine* e, const fg_emulsion* em, const double* origins,
+                         const double* dirs, size_t nrays, int developed_only, uint32_t* offsets,
+                         uint32_t* ids, size_t id_cap, size_t* nhits, double* chord_sum);
+/* Per-ray hit counts of the production scan kernel (pixel-major, stratum-minor). */
+fg_status fg_scan_ray_hits(fg_engine* e, const fg_emulsion* em, const fg_scan_cfg* cfg,
+                           uint64_t seed, uint16_t* ray_hits);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FGRAIN_CUDA_H */

@@ -1,0 +1,209 @@
+/* CPU oracle for the fgrain photon-transport and transmittance-scan path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library restates the reference's Rust CPU path in C++ so
+ * that tests can check the CUDA library against it, and so that bench.py can time it as the
+ * CPU baseline.  Nothing in the product links or calls it.
+ *
+ * Parity status: the geometric and development stages are pinned to the reference's own
+ * inline known-answer tests (crystal.rs:238-282, bvh.rs:412-462, development.rs:197-265,
+ * poisson.rs:141-165, optics.rs:206-245, transport.rs:195-237, transmittance.rs:181-221).
+ * The random streams are NOT pinned: the reference draws from rand 0.8.8 StdRng (ChaCha12),
+ * which cannot be built here; the oracle draws from Philox-4x32-10 instead (philox.h).
+ */
+#ifndef FG_ORACLE_H
+#define FG_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* GelatinOptics, optics.rs:41-60 */
+typedef struct or_optics {
+  double refractive_index;
+  double absorption_coeff;
+  double scattering_coeff;
+  double anisotropy_g;
+  double antihalation_reflectance;
+  double antihalation_density;
+} or_optics;
+
+/* EmulsionConfig, emulsion.rs:14-37 (morphology: 0 cubic, 1 tabular, 2 octahedral) */
+typedef struct or_emulsion_cfg {
+  double width, height, depth;
+  double r_min;
+  double mean_crystal_radius;
+  double size_variance;
+  int32_t morphology;
+  int32_t _pad;
+  double tabular_aspect_ratio;
+  or_optics optics;
+  double base_sensitivity;
+} or_emulsion_cfg;
+
+/* ExposureConfig, transport.rs:15-28 */
+typedef struct or_exposure_cfg {
+  double photons_per_sq_um;
+  double illumination_angle_rad;
+  double crystal_absorption_coeff;
+  uint32_t max_bounces;
+  uint32_t _pad;
+} or_exposure_cfg;
+
+/* DevelopmentConfig, development.rs:12-27 */
+typedef struct or_dev_cfg {
+  uint32_t threshold_photons;
+  uint32_t _pad;
+  double filament_expansion;
+  double clumping_proximity_factor;
+  double developer_contrast;
+} or_dev_cfg;
+
+/* DevelopmentReport, development.rs:42-56 */
+typedef struct or_dev_report {
+  uint64_t total_crystals;
+  uint64_t developed_crystals;
+  uint64_t fixed_crystals;
+  uint64_t total_clumps;
+  uint64_t max_clump_size;
+  double avg_clump_size;
+} or_dev_report;
+
+/* ScanConfig, transmittance.rs:32-48 (mode: 0 negative T, 1 positive 1-T, 2 optical density) */
+typedef struct or_scan_cfg {
+  uint32_t width_px;
+  uint32_t height_px;
+  uint32_t samples_per_pixel;
+  int32_t mode;
+  double silver_opacity;
+} or_scan_cfg;
+
+/* A crystal set in structure-of-arrays form (HalideCrystal, crystal.rs:21-50).  pos and dims
+ * hold 3 doubles per crystal, quat holds (i, j, k, w).  The mutable fields (latent counts,
+ * developed flag, clump id, filament expansion) live in the same struct so that the stages
+ * can be chained exactly like the reference chains them. */
+typedef struct or_crystals {
+  size_t n;
+  double* pos;
+  double* dims;
+  double* quat;
+  double* sens;
+  int32_t* morph;
+  uint32_t* latent;
+  uint8_t* developed;
+  int64_t* clump;
+  double* expansion;
+} or_crystals;
+
+/* Hit-selection rule.  FAITHFUL walks the reference's spatial-median BVH (bvh.rs:157-347) and
+ * reports hits in its traversal order; a crystal counts when its geometry is hit and the
+ * enclosing LEAF box is hit.  CANONICAL counts a crystal when its geometry is hit and its OWN
+ * max_dim box (crystal.rs:106-133) is hit, and orders hits by (t_enter, crystal index); it does
+ * not depend on how a BVH groups crystals, so a device LBVH can reproduce it exactly. */
+enum { OR_FAITHFUL = 0, OR_CANONICAL = 1 };
+
+/* One recorded photon segment: the state a bounce starts from. */
+typedef struct or_segment {
+  double origin[3];
+  double dir[3];
+  double step;
+  double energy;
+  uint32_t photon;
+  uint32_t bounce;
+} or_segment;
+
+/* ---- known-answer entry points ---- */
+int or_philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
+              uint32_t out[4]);
+/* HalideCrystal::intersect_ray (crystal.rs:140-217); returns 1 on hit. */
+int or_intersect_crystal(const double pos[3], const double dims[3], const double quat[4],
+                         int32_t morph, double expansion, const double origin[3],
+                         const double dir[3], double* t_enter, double* t_exit);
+/* Builds the reference BVH over the set and returns the hits of one ray (faithful or
+ * canonical).  Returns the number of hits (<= cap). */
+int64_t or_ray_hits(const or_crystals* c, const double origin[3], const double dir[3], int mode,
+                    uint32_t* idx_out, double* t0_out, double* t1_out, int64_t cap);
+/* BVH::query_radius (bvh.rs:350-402); returns the number of results (<= cap). */
+int64_t or_query_radius(const or_crystals* c, const double center[3], double radius,
+                        uint32_t* out, int64_t cap);
+/* Statistics of the reference BVH over the set: node count, depth, and stack drops. */
+int or_bvh_stats(const or_crystals* c, int64_t* nodes, int64_t* depth);
+
+/* GelatinOptics::sample_free_path (optics.rs:100-107) for one uniform xi. */
+double or_free_path(const or_optics* o, double xi);
+/* GelatinOptics::handle_antihalation_reflection (optics.rs:160-196) with its uniforms u[0..3]
+ * (roulette, diffuse choice, u1, u2).  Returns 1 while the packet is alive. */
+int or_antihalation(const or_optics* o, double* energy, double dir[3], const double u[4]);
+/* Hits of many rays against the set (one BVH build): CSR offsets[n+1], ids, per-ray chord sums.
+ * developed_only: test only developed crystals, with their expansion.  Returns total hits. */
+int64_t or_rays_hits(const or_crystals* c, const double* origins, const double* dirs, int64_t n,
+                     int mode, int developed_only, uint32_t* offsets, uint32_t* ids,
+                     int64_t id_cap, double* chord_sum);
+
+/* ---- stages ---- */
+/* sample_poisson_3d (poisson.rs:14-132): returns the point count; writes at most cap points. */
+int64_t or_sample_poisson(const double bounds[3], double r_min, uint32_t k, uint64_t seed,
+                          double* pts, int64_t cap);
+/* VirtualEmulsionLayer::synthesize (emulsion.rs:155-220).  Pass out->n = capacity. */
+int64_t or_synthesize(const or_emulsion_cfg* cfg, uint64_t seed, or_crystals* out);
+
+/* expose_emulsion (transport.rs:48-188) with the tile worker's nearest-pixel exposure closure
+ * (image_pipeline.rs:949-958).  Counts are ADDED to c->latent.  When seg_out is not NULL the
+ * segments are recorded (sorted by photon, bounce); *seg_n receives the total count even if it
+ * exceeds seg_cap.  Returns the number of photons launched. */
+int64_t or_expose(or_crystals* c, const or_emulsion_cfg* cfg, const float* tile, uint32_t tw,
+                  uint32_t th, const or_exposure_cfg* ecfg, uint64_t seed, int mode,
+                  int threads, or_segment* seg_out, int64_t seg_cap, int64_t* seg_n,
+                  uint64_t* hits_out);
+
+/* Replays recorded segments with the per-hit arithmetic of expose (canonical hits only);
+ * counts are added to c->latent; hit lists are written CSR-style when offsets != NULL. */
+int64_t or_replay_segments(or_crystals* c, const or_exposure_cfg* ecfg, uint64_t seed,
+                           const or_segment* segs, int64_t nseg, uint32_t* offsets,
+                           uint32_t* ids, int64_t id_cap);
+
+/* develop_emulsion (development.rs:59-188): fills developed / clump / expansion. */
+int or_develop(or_crystals* c, const or_dev_cfg* cfg, or_dev_report* rep);
+
+/* scan_emulsion (transmittance.rs:65-171).  out receives the mode-mapped f32 buffer; image8
+ * (optional) the 8-bit image.  sigma_c (optional) gives a per-crystal opacity in place of
+ * cfg->silver_opacity.  T64 (optional) receives the FP64 pixel means.  ray_hits (optional)
+ * receives, per ray (pixel-major, stratum-minor), the number of canonical/faithful hits. */
+int or_scan(const or_crystals* c, const or_emulsion_cfg* ecfg, const or_scan_cfg* scfg,
+            uint64_t seed, int mode, int threads, const double* sigma_c, float* out,
+            uint8_t* image8, double* T64, uint16_t* ray_hits);
+
+/* Scan ray origins exactly as or_scan forms them (pixel-major, stratum-minor). */
+int or_scan_ray_origins(const or_emulsion_cfg* ecfg, const or_scan_cfg* scfg, uint64_t seed,
+                        double* origins);
+
+/* render_tile_cpu_full (image_pipeline.rs:924-987) + render_tile_cpu_density (:990-1014).
+ * preset: 0 tri-x, 1 tri-x-1600, 2 t-max, 3 hp5.  tile is tw*th row-major exposure. */
+typedef struct or_tile_report {
+  uint64_t crystals;
+  uint64_t developed;
+  uint64_t clumps;
+  uint64_t photons;
+  uint64_t hits;
+} or_tile_report;
+int or_render_tile(int preset, double pixel_size_um, const float* tile, uint32_t tw, uint32_t th,
+                   double exposure, double push, uint64_t tile_seed, int mode, int threads,
+                   float* d_neg, or_tile_report* rep);
+
+/* Scanner OTF, image_pipeline.rs:825-855 (3-tap, clamp to edge), on a float field. */
+int or_scanner_otf(const float* in, uint32_t w, uint32_t h, const float taps[3], float* out);
+/* Triangle-filter resize of a float field (the supersample downsample, image_pipeline.rs:
+ * 315-330; separable tent filter whose support scales with the ratio). */
+int or_resize_triangle(const float* in, uint32_t w, uint32_t h, uint32_t ow, uint32_t oh,
+                       float* out);
+/* Hann overlap blend of tiles into an image (image_pipeline.rs:593-649): returns d_norm. */
+int or_blend_tiles(uint32_t out_w, uint32_t out_h, uint32_t tile_step, uint32_t pad,
+                   uint32_t ntiles, const uint32_t* desc /* ntiles x (tx,ty,x0,y0,tw,th) */,
+                   const float* const* tiles, float* d_norm);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

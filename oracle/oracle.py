@@ -1,0 +1,372 @@
+"""ctypes wrapper of the CPU oracle (oracle/fg_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and bench.py's CPU baseline use this
+module as the checker.  It restates the reference's Rust CPU path; the product never calls it.
+Parity status: geometry, BVH and development are pinned to the reference's inline known-answer
+tests; the random streams are not pinned (Philox replaces rand 0.8.8's ChaCha12).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "build" / "liboracle.so"
+
+FAITHFUL = 0
+CANONICAL = 1
+PRESETS = {"tri-x": 0, "tri-x-1600": 1, "t-max": 2, "hp5": 3}
+
+
+class or_optics(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("refractive_index", "absorption_coeff", "scattering_coeff",
+                                          "anisotropy_g", "antihalation_reflectance",
+                                          "antihalation_density")]
+
+
+class or_emulsion_cfg(C.Structure):
+    _fields_ = [("width", C.c_double), ("height", C.c_double), ("depth", C.c_double),
+                ("r_min", C.c_double), ("mean_crystal_radius", C.c_double),
+                ("size_variance", C.c_double), ("morphology", C.c_int32), ("_pad", C.c_int32),
+                ("tabular_aspect_ratio", C.c_double), ("optics", or_optics),
+                ("base_sensitivity", C.c_double)]
+
+
+class or_exposure_cfg(C.Structure):
+    _fields_ = [("photons_per_sq_um", C.c_double), ("illumination_angle_rad", C.c_double),
+                ("crystal_absorption_coeff", C.c_double), ("max_bounces", C.c_uint32),
+                ("_pad", C.c_uint32)]
+
+
+class or_dev_cfg(C.Structure):
+    _fields_ = [("threshold_photons", C.c_uint32), ("_pad", C.c_uint32),
+                ("filament_expansion", C.c_double), ("clumping_proximity_factor", C.c_double),
+                ("developer_contrast", C.c_double)]
+
+
+class or_dev_report(C.Structure):
+    _fields_ = [("total_crystals", C.c_uint64), ("developed_crystals", C.c_uint64),
+                ("fixed_crystals", C.c_uint64), ("total_clumps", C.c_uint64),
+                ("max_clump_size", C.c_uint64), ("avg_clump_size", C.c_double)]
+
+
+class or_scan_cfg(C.Structure):
+    _fields_ = [("width_px", C.c_uint32), ("height_px", C.c_uint32),
+                ("samples_per_pixel", C.c_uint32), ("mode", C.c_int32),
+                ("silver_opacity", C.c_double)]
+
+
+class or_crystals(C.Structure):
+    _fields_ = [("n", C.c_size_t), ("pos", C.POINTER(C.c_double)), ("dims", C.POINTER(C.c_double)),
+                ("quat", C.POINTER(C.c_double)), ("sens", C.POINTER(C.c_double)),
+                ("morph", C.POINTER(C.c_int32)), ("latent", C.POINTER(C.c_uint32)),
+                ("developed", C.POINTER(C.c_uint8)), ("clump", C.POINTER(C.c_int64)),
+                ("expansion", C.POINTER(C.c_double))]
+
+
+class or_tile_report(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("crystals", "developed", "clumps", "photons", "hits")]
+
+
+SEGMENT_DTYPE = np.dtype([("origin", "<f8", 3), ("dir", "<f8", 3), ("step", "<f8"),
+                          ("energy", "<f8"), ("photon", "<u4"), ("bounce", "<u4")])
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("oracle_build", HERE / "build.py")
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()  # no-op when up to date
+        _lib = C.CDLL(str(LIB))
+        _lib.or_free_path.restype = C.c_double
+        _lib.or_rays_hits.restype = C.c_int64
+    return _lib
+
+
+def _p(a, t):
+    return None if a is None else a.ctypes.data_as(C.POINTER(t))
+
+
+class Crystals:
+    """Mutable crystal set in crystal-index order (HalideCrystal fields as arrays)."""
+
+    def __init__(self, pos, dims, quat, sens, morph):
+        n = len(pos)
+        self.pos = np.ascontiguousarray(pos, np.float64).reshape(n, 3)
+        self.dims = np.ascontiguousarray(dims, np.float64).reshape(n, 3)
+        self.quat = np.ascontiguousarray(quat, np.float64).reshape(n, 4)
+        self.sens = np.ascontiguousarray(sens, np.float64).reshape(n)
+        self.morph = np.ascontiguousarray(morph, np.int32).reshape(n)
+        self.latent = np.zeros(n, np.uint32)
+        self.developed = np.zeros(n, np.uint8)
+        self.clump = np.full(n, -1, np.int64)
+        self.expansion = np.ones(n, np.float64)
+
+    def __len__(self):
+        return self.pos.shape[0]
+
+    def struct(self) -> or_crystals:
+        return or_crystals(len(self), _p(self.pos, C.c_double), _p(self.dims, C.c_double),
+                           _p(self.quat, C.c_double), _p(self.sens, C.c_double),
+                           _p(self.morph, C.c_int32), _p(self.latent, C.c_uint32),
+                           _p(self.developed, C.c_uint8), _p(self.clump, C.c_int64),
+                           _p(self.expansion, C.c_double))
+
+    def copy(self) -> "Crystals":
+        c = Crystals(self.pos.copy(), self.dims.copy(), self.quat.copy(), self.sens.copy(), self.morph.copy())
+        c.latent = self.latent.copy()
+        c.developed = self.developed.copy()
+        c.clump = self.clump.copy()
+        c.expansion = self.expansion.copy()
+        return c
+
+
+def emulsion_cfg(cfg) -> or_emulsion_cfg:
+    """From any object with EmulsionConfig's fields (dimensions tuple + the rest)."""
+    o = cfg.optics
+    return or_emulsion_cfg(float(cfg.dimensions[0]), float(cfg.dimensions[1]), float(cfg.dimensions[2]),
+                           cfg.r_min, cfg.mean_crystal_radius, cfg.size_variance, int(cfg.morphology), 0,
+                           cfg.tabular_aspect_ratio,
+                           or_optics(o.refractive_index, o.absorption_coeff, o.scattering_coeff,
+                                     o.anisotropy_g, o.antihalation_reflectance, o.antihalation_density),
+                           cfg.base_sensitivity)
+
+
+def exposure_cfg(c) -> or_exposure_cfg:
+    return or_exposure_cfg(c.photons_per_sq_um, c.illumination_angle_rad, c.crystal_absorption_coeff,
+                           int(c.max_bounces), 0)
+
+
+def dev_cfg(c) -> or_dev_cfg:
+    return or_dev_cfg(int(c.threshold_photons), 0, c.filament_expansion, c.clumping_proximity_factor,
+                      c.developer_contrast)
+
+
+def scan_cfg(c) -> or_scan_cfg:
+    return or_scan_cfg(int(c.width_px), int(c.height_px), int(c.samples_per_pixel), int(c.mode),
+                       c.silver_opacity)
+
+
+def philox(ctr, key):
+    out = (C.c_uint32 * 4)()
+    lib().or_philox(*[C.c_uint32(v) for v in ctr], *[C.c_uint32(v) for v in key], out)
+    return list(out)
+
+
+def intersect_crystal(pos, dims, quat, morph, expansion, origin, direction):
+    a = lambda v: (C.c_double * len(v))(*v)  # noqa: E731
+    t0, t1 = C.c_double(), C.c_double()
+    hit = lib().or_intersect_crystal(a(pos), a(dims), a(quat), C.c_int32(morph), C.c_double(expansion),
+                                     a(origin), a(direction), C.byref(t0), C.byref(t1))
+    return (t0.value, t1.value) if hit else None
+
+
+def ray_hits(cr: Crystals, origin, direction, mode=CANONICAL):
+    L = lib()
+    L.or_ray_hits.restype = C.c_int64
+    cap = len(cr) + 1
+    idx = np.zeros(cap, np.uint32)
+    t0 = np.zeros(cap)
+    t1 = np.zeros(cap)
+    s = cr.struct()
+    a = lambda v: (C.c_double * 3)(*v)  # noqa: E731
+    n = L.or_ray_hits(C.byref(s), a(origin), a(direction), mode, _p(idx, C.c_uint32),
+                      _p(t0, C.c_double), _p(t1, C.c_double), C.c_int64(cap))
+    return idx[:n], t0[:n], t1[:n]
+
+
+def free_path(optics, xi):
+    o = or_optics(optics.refractive_index, optics.absorption_coeff, optics.scattering_coeff,
+                  optics.anisotropy_g, optics.antihalation_reflectance, optics.antihalation_density)
+    return lib().or_free_path(C.byref(o), C.c_double(xi))
+
+
+def antihalation(optics, energy, direction, u):
+    o = or_optics(optics.refractive_index, optics.absorption_coeff, optics.scattering_coeff,
+                  optics.anisotropy_g, optics.antihalation_reflectance, optics.antihalation_density)
+    E = C.c_double(energy)
+    d = (C.c_double * 3)(*direction)
+    alive = lib().or_antihalation(C.byref(o), C.byref(E), d, (C.c_double * 4)(*u))
+    return bool(alive), E.value, list(d)
+
+
+def rays_hits(cr: Crystals, origins, dirs, mode=CANONICAL, developed_only=False):
+    """Hit lists of many rays: (offsets, ids, chord sums)."""
+    o = np.ascontiguousarray(origins, np.float64).reshape(-1, 3)
+    d = np.ascontiguousarray(dirs, np.float64).reshape(-1, 3)
+    n = o.shape[0]
+    offsets = np.zeros(n + 1, np.uint32)
+    chord = np.zeros(n)
+    s = cr.struct()
+    total = lib().or_rays_hits(C.byref(s), _p(o, C.c_double), _p(d, C.c_double), C.c_int64(n), mode,
+                               int(developed_only), _p(offsets, C.c_uint32), None, C.c_int64(0),
+                               _p(chord, C.c_double))
+    ids = np.zeros(max(total, 1), np.uint32)
+    lib().or_rays_hits(C.byref(s), _p(o, C.c_double), _p(d, C.c_double), C.c_int64(n), mode,
+                       int(developed_only), _p(offsets, C.c_uint32), _p(ids, C.c_uint32),
+                       C.c_int64(total), _p(chord, C.c_double))
+    return offsets, ids[:total], chord
+
+
+def query_radius(cr: Crystals, center, radius):
+    L = lib()
+    L.or_query_radius.restype = C.c_int64
+    out = np.zeros(len(cr) + 1, np.uint32)
+    s = cr.struct()
+    n = L.or_query_radius(C.byref(s), (C.c_double * 3)(*center), C.c_double(radius),
+                          _p(out, C.c_uint32), C.c_int64(len(out)))
+    return sorted(out[:n].tolist())
+
+
+def bvh_stats(cr: Crystals):
+    nodes, depth = C.c_int64(), C.c_int64()
+    s = cr.struct()
+    lib().or_bvh_stats(C.byref(s), C.byref(nodes), C.byref(depth))
+    return nodes.value, depth.value
+
+
+def sample_poisson(bounds, r_min, k, seed):
+    L = lib()
+    L.or_sample_poisson.restype = C.c_int64
+    vol = bounds[0] * bounds[1] * bounds[2]
+    cap = int(vol / r_min ** 3 * 1.5) + 64
+    pts = np.zeros((cap, 3))
+    n = L.or_sample_poisson((C.c_double * 3)(*bounds), C.c_double(r_min), C.c_uint32(k),
+                            C.c_uint64(seed), _p(pts, C.c_double), C.c_int64(cap))
+    assert n <= cap
+    return pts[:n].copy()
+
+
+def synthesize(cfg, seed) -> Crystals:
+    L = lib()
+    L.or_synthesize.restype = C.c_int64
+    ec = emulsion_cfg(cfg)
+    vol = ec.width * ec.height * ec.depth
+    cap = int(vol / ec.r_min ** 3 * 1.5) + 64
+    while True:
+        cr = Crystals(np.zeros((cap, 3)), np.zeros((cap, 3)), np.zeros((cap, 4)), np.zeros(cap),
+                      np.zeros(cap, np.int32))
+        s = cr.struct()
+        n = L.or_synthesize(C.byref(ec), C.c_uint64(seed), C.byref(s))
+        if n <= cap:
+            break
+        cap = n
+    out = Crystals(cr.pos[:n], cr.dims[:n], cr.quat[:n], cr.sens[:n], cr.morph[:n])
+    return out
+
+
+def expose(cr: Crystals, cfg, tile, ecfg, seed, mode=CANONICAL, threads=0, record=False):
+    """Adds counts into cr.latent; returns (photons, segments or None, absorbing hits)."""
+    L = lib()
+    L.or_expose.restype = C.c_int64
+    tile = np.ascontiguousarray(tile, np.float32)
+    th, tw = tile.shape
+    ec, xc = emulsion_cfg(cfg), exposure_cfg(ecfg)
+    s = cr.struct()
+    nseg = C.c_int64()
+    hits = C.c_uint64()
+    if not record:
+        P = L.or_expose(C.byref(s), C.byref(ec), _p(tile, C.c_float), tw, th, C.byref(xc),
+                        C.c_uint64(seed), mode, threads, None, C.c_int64(0), None, C.byref(hits))
+        return P, None, hits.value
+    # Record: first pass sizes the buffer on a copy of the counts.
+    saved = cr.latent.copy()
+    L.or_expose(C.byref(s), C.byref(ec), _p(tile, C.c_float), tw, th, C.byref(xc), C.c_uint64(seed),
+                mode, threads, None, C.c_int64(0), C.byref(nseg), C.byref(hits))
+    cr.latent[:] = saved
+    segs = np.zeros(nseg.value, SEGMENT_DTYPE)
+    s = cr.struct()
+    P = L.or_expose(C.byref(s), C.byref(ec), _p(tile, C.c_float), tw, th, C.byref(xc), C.c_uint64(seed),
+                    mode, threads, segs.ctypes.data_as(C.c_void_p), C.c_int64(len(segs)),
+                    C.byref(nseg), C.byref(hits))
+    return P, segs, hits.value
+
+
+def replay_segments(cr: Crystals, ecfg, seed, segs):
+    L = lib()
+    L.or_replay_segments.restype = C.c_int64
+    segs = np.ascontiguousarray(segs, SEGMENT_DTYPE)
+    offsets = np.zeros(len(segs) + 1, np.uint32)
+    cap = max(len(segs) * 64, 1)
+    ids = np.zeros(cap, np.uint32)
+    xc = exposure_cfg(ecfg)
+    s = cr.struct()
+    n = L.or_replay_segments(C.byref(s), C.byref(xc), C.c_uint64(seed), segs.ctypes.data_as(C.c_void_p),
+                             C.c_int64(len(segs)), _p(offsets, C.c_uint32), _p(ids, C.c_uint32),
+                             C.c_int64(cap))
+    return offsets, ids[:n].copy()
+
+
+def develop(cr: Crystals, dcfg):
+    rep = or_dev_report()
+    dc = dev_cfg(dcfg)
+    s = cr.struct()
+    lib().or_develop(C.byref(s), C.byref(dc), C.byref(rep))
+    return {k: getattr(rep, k) for k, _ in rep._fields_}
+
+
+def scan(cr: Crystals, cfg, scfg, seed, mode=CANONICAL, threads=0, sigma_c=None, want_hits=False):
+    """Returns dict(out, image8, T64[, ray_hits])."""
+    sc = scan_cfg(scfg)
+    ec = emulsion_cfg(cfg)
+    h, w = sc.height_px, sc.width_px
+    g = int(round(np.sqrt(max(sc.samples_per_pixel, 1))))
+    a = max(g * g, 1)
+    out = np.zeros((h, w), np.float32)
+    img = np.zeros((h, w), np.uint8)
+    T64 = np.zeros((h, w), np.float64)
+    rh = np.zeros(h * w * a, np.uint16) if want_hits else None
+    sig = None if sigma_c is None else np.ascontiguousarray(sigma_c, np.float64)
+    s = cr.struct()
+    lib().or_scan(C.byref(s), C.byref(ec), C.byref(sc), C.c_uint64(seed), mode, threads,
+                  _p(sig, C.c_double), _p(out, C.c_float), _p(img, C.c_uint8), _p(T64, C.c_double),
+                  _p(rh, C.c_uint16))
+    r = {"out": out, "image8": img, "T64": T64}
+    if want_hits:
+        r["ray_hits"] = rh
+    return r
+
+
+def scan_ray_origins(cfg, scfg, seed):
+    sc = scan_cfg(scfg)
+    ec = emulsion_cfg(cfg)
+    g = int(round(np.sqrt(max(sc.samples_per_pixel, 1))))
+    a = max(g * g, 1)
+    o = np.zeros((sc.width_px * sc.height_px * a, 3))
+    lib().or_scan_ray_origins(C.byref(ec), C.byref(sc), C.c_uint64(seed), _p(o, C.c_double))
+    return o
+
+
+def render_tile(preset, pixel_size_um, tile, exposure, push, tile_seed, mode=CANONICAL, threads=0):
+    tile = np.ascontiguousarray(tile, np.float32)
+    th, tw = tile.shape
+    d = np.zeros((th, tw), np.float32)
+    rep = or_tile_report()
+    lib().or_render_tile(PRESETS[preset] if isinstance(preset, str) else int(preset),
+                         C.c_double(pixel_size_um), _p(tile, C.c_float), tw, th, C.c_double(exposure),
+                         C.c_double(push), C.c_uint64(tile_seed), mode, threads, _p(d, C.c_float),
+                         C.byref(rep))
+    return d, {k: getattr(rep, k) for k, _ in rep._fields_}
+
+
+def scanner_otf(field, taps=(0.035, 0.93, 0.035)):
+    f = np.ascontiguousarray(field, np.float32)
+    h, w = f.shape
+    out = np.zeros_like(f)
+    lib().or_scanner_otf(_p(f, C.c_float), w, h, (C.c_float * 3)(*taps), _p(out, C.c_float))
+    return out
+
+
+def resize_triangle(field, ow, oh):
+    f = np.ascontiguousarray(field, np.float32)
+    h, w = f.shape
+    out = np.zeros((oh, ow), np.float32)
+    lib().or_resize_triangle(_p(f, C.c_float), w, h, ow, oh, _p(out, C.c_float))
+    return out

@@ -1,0 +1,92 @@
+"""The C ABI without a GPU: the library loads, exports every entry point include/fgrain_cuda.h
+declares, its structs have the layouts ctypes assumes, and the preset table matches the
+reference's presets (emulsion.rs:46-136)."""
+import ctypes as C
+import re
+import subprocess
+import textwrap
+from pathlib import Path
+
+import pytest
+
+import fgrain_gb300 as fg
+from fgrain_gb300 import _abi
+from tests.helpers import REFERENCE_PRESETS
+
+ROOT = Path(__file__).resolve().parents[1]
+HEADER = ROOT / "include" / "fgrain_cuda.h"
+
+
+def declared_functions():
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    return sorted(set(re.findall(r"\b(fg_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_every_declared_symbol_is_exported_and_bound():
+    lib = _abi.load()
+    names = declared_functions()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), f"{n} declared in the header but not exported"
+        assert n in _abi.PROTOTYPES, f"{n} has no ctypes prototype"
+    assert set(_abi.PROTOTYPES) == set(names)
+
+
+STRUCTS = ["fg_optics", "fg_emulsion_cfg", "fg_exposure_cfg", "fg_dev_cfg", "fg_dev_report",
+           "fg_scan_cfg", "fg_crystals_host", "fg_crystals_out", "fg_segment", "fg_timings"]
+
+
+def test_struct_layouts_match_ctypes(tmp_path):
+    lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void){"]
+    for s in STRUCTS:
+        lines.append(f'printf("{s} %zu\\n", sizeof({s}));')
+        for f, _ in getattr(_abi, s)._fields_:
+            lines.append(f'printf("{s}.{f} %zu\\n", offsetof({s}, {f}));')
+    lines.append("return 0;}")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", str(src), "-o", str(exe)], check=True)
+    got = dict(l.split() for l in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines())
+    for s in STRUCTS:
+        ct = getattr(_abi, s)
+        assert int(got[s]) == C.sizeof(ct), s
+        for f, _ in ct._fields_:
+            assert int(got[f"{s}.{f}"]) == getattr(ct, f).offset, f"{s}.{f}"
+
+
+@pytest.mark.parametrize("name", list(REFERENCE_PRESETS))
+def test_preset_table_matches_reference(name):
+    cfg = fg.EmulsionConfig.preset(name, 33.0, 44.0)
+    d, r, m, v, mo, ar, o, s = REFERENCE_PRESETS[name]
+    assert cfg.dimensions == (33.0, 44.0, d)
+    assert (cfg.r_min, cfg.mean_crystal_radius, cfg.size_variance, int(cfg.morphology), cfg.tabular_aspect_ratio,
+            cfg.base_sensitivity) == (r, m, v, mo, ar, s)
+    oo = cfg.optics
+    assert (oo.refractive_index, oo.absorption_coeff, oo.scattering_coeff, oo.anisotropy_g,
+            oo.antihalation_reflectance, oo.antihalation_density) == o
+
+
+def test_unknown_preset_is_invalid_argument():
+    with pytest.raises(fg.GpuError) as ei:
+        fg.EmulsionConfig.preset("portra", 1.0, 1.0)
+    assert ei.value.status == 16
+
+
+def test_status_strings_mirror_gpu_error():
+    lib = _abi.load()
+    # error.rs:9-33 messages for the six GpuError variants.
+    assert lib.fg_status_string(1).decode().startswith("Failed to find suitable GPU adapter")
+    assert lib.fg_status_string(6).decode() == "GPU pipeline error"
+    assert lib.fg_status_string(0).decode() == "ok"
+
+
+def test_engine_creation_reports_status_without_crashing():
+    lib = _abi.load()
+    h = C.c_void_p()
+    st = lib.fg_engine_create(0, C.byref(h))
+    assert st in (0, 1)
+    if st == 0:
+        assert lib.fg_engine_destroy(h) == 0
+    assert lib.fg_engine_create(-1, C.byref(h)) == 1
+    assert lib.fg_engine_destroy(None) == 16
