@@ -106,8 +106,10 @@ __global__ void k_karras(const uint64_t* keys, uint32_t n, Node* nodes, int* lea
   if (i == 0) nodes[0].d.z = -1;
 }
 
-// Leaf box: the crystal shape (oriented cube or ellipsoid) cut by its own max_dim box, padded
-// outward by pad.  An empty box is NaN (never hit: every comparison with NaN is false).
+// Leaf box: the bounding box of the crystal shape (oriented cube or ellipsoid), padded outward by
+// pad.  It is not cut by the crystal's own max_dim box: a canonical hit tests that box on the
+// whole ray, while its entry distance is the shape's, so culling by entry distance needs the
+// full shape.  An empty box is NaN (never hit: every comparison with NaN is false).
 __device__ __forceinline__ void leaf_box(const float4 a, const float4 q, const float4 d, float e,
                                          float pad, float* lo, float* hi) {
   const float x = q.x, y = q.y, z = q.z, w = q.w;
@@ -115,7 +117,6 @@ __device__ __forceinline__ void leaf_box(const float4 a, const float4 q, const f
                          {2.f * (x * y + z * w), 1.f - 2.f * (x * x + z * z), 2.f * (y * z - x * w)},
                          {2.f * (x * z - y * w), 2.f * (y * z + x * w), 1.f - 2.f * (x * x + y * y)}};
   const float dm[3] = {d.x * e, d.y * e, d.z * e};
-  const float m = fmaxf(fmaxf(dm[0], dm[1]), dm[2]);
   const bool cubic = __float_as_int(d.w) == 0;
   const float p[3] = {a.x, a.y, a.z};
 #pragma unroll
@@ -127,7 +128,7 @@ __device__ __forceinline__ void leaf_box(const float4 a, const float4 q, const f
       const float u = R[i][0] * dm[0], v = R[i][1] * dm[1], t = R[i][2] * dm[2];
       ext = sqrtf(u * u + v * v + t * t);
     }
-    const float h = fminf(ext * 1.0001f, m) + pad;
+    const float h = ext * 1.0001f + pad;
     lo[i] = p[i] - h;
     hi[i] = p[i] + h;
   }

@@ -147,9 +147,10 @@ __global__ void k_flags(uint32_t n, const uint8_t* developed, const int* parent,
                         DevCounters* dc) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
-  const uint32_t id = s2id ? s2id[s] : s;
+  // Clumps are numbered by their smallest crystal index (the reference's BFS start order), so
+  // each component flags its minimum id; a prefix sum over ids then ranks them.
   const bool root = developed[s] && parent[s] == static_cast<int>(s);
-  flag_by_id[id] = root ? 1u : 0u;
+  if (root) flag_by_id[minid[s]] = 1u;
   const unsigned act = __activemask();
   const unsigned ball = __ballot_sync(act, root);
   const unsigned mx = __reduce_max_sync(act, root ? size[s] : 0u);
@@ -157,7 +158,7 @@ __global__ void k_flags(uint32_t n, const uint8_t* developed, const int* parent,
     atomicAdd(&dc->clumps, static_cast<unsigned long long>(__popc(ball)));
     atomicMax(&dc->max_size, static_cast<unsigned long long>(mx));
   }
-  (void)minid;
+  (void)s2id;
 }
 
 __global__ void k_finalize(uint32_t n, const uint8_t* developed, const int* parent,
@@ -216,6 +217,7 @@ void develop(fg_engine* e, fg_emulsion* em, const fg_dev_cfg& cfg, fg_dev_report
   FG_CUDA(cudaMemsetAsync(dc.p, 0, sizeof(DevCounters), st));
   FG_CUDA(cudaMemsetAsync(size.p, 0, n * sizeof(uint32_t), st));
   FG_CUDA(cudaMemsetAsync(minid.p, 0xff, n * sizeof(uint32_t), st));
+  FG_CUDA(cudaMemsetAsync(flag.p, 0, n * sizeof(uint32_t), st));
   FG_CUDA(cudaMemsetAsync(mb.p, 0, sizeof(unsigned long long), st));
   const unsigned G = grid_for(n, 256);
   const uint32_t* s2id = em->h_s2id.empty() ? nullptr : em->sorted_to_id.p;

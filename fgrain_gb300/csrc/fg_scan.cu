@@ -46,83 +46,109 @@ __global__ void k_bin_fill(ScanTile t, const uint32_t* off, uint32_t* cursor, ui
     }
 }
 
-// Shared-memory image of a staged crystal (index c of the current chunk).
+// Error-free transformations on floats (Knuth's two-sum, FMA two-product).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  e = b - (s - a);
+}
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
+  p = a * b;
+  e = fmaf(a, b, -p);
+}
+__device__ __forceinline__ void split64(double v, float& hi, float& lo) {
+  hi = static_cast<float>(v);
+  lo = static_cast<float>(v - static_cast<double>(hi));
+}
+
+// Crystal kinds in shared memory.
+enum : int { K_CUBE = 0, K_CUBE_DF = 1, K_ELLIPSOID = 2, K_FP64 = 3 };
+
+// Shared-memory image of a staged crystal (index c of the current chunk).  Coordinates are
+// relative to the bin corner and carried as float pairs (hi + lo) so that ray-minus-crystal
+// offsets are accurate to ~1e-8 um.
 struct ScanSmem {
-  float cx[SCAN_CH], cy[SCAN_CH], m[SCAN_CH], delta[SCAN_CH], err[SCAN_CH], sig[SCAN_CH];
-  float g[12][SCAN_CH];
+  float cxh[SCAN_CH], cxl[SCAN_CH], cyh[SCAN_CH], cyl[SCAN_CH];
+  float m[SCAN_CH], delta[SCAN_CH], err[SCAN_CH], sig[SCAN_CH];
+  float g[21][SCAN_CH];
   int s[SCAN_CH];
-  int type[SCAN_CH];
+  int kind[SCAN_CH];
   double T[SCAN_THREADS];
 };
 
-// Stages crystal s for vertical rays relative to the bin corner (bx0, by0) (FP64 corner).
+constexpr float EPS32 = 5.9604645e-8f;  // 2^-24
+
+// Stages crystal s for vertical rays relative to the bin corner (bx0, by0).  Everything is
+// derived in FP64 once per crystal and CTA, then rounded:
+//   cubes:      rows 0 and 1 of R as float pairs, 1 / (-R_2i), half-sizes as float pairs;
+//   ellipsoids: R_0i / D_i, R_1i / D_i, e_i = -R_2i / D_i, A = |e|^2, 1 / A.
+// Cubes whose faces are nearly parallel to the ray (|1/R_2i| > 15) evaluate their local origin in
+// float-pair arithmetic; cubes with an exactly parallel face decide in FP64.
 __device__ __forceinline__ void stage_crystal(const ScanTile& t, ScanSmem& sm, int c, uint32_t s,
                                               double bx0, double by0) {
-  const float4 a = t.a[s], q = t.q[s], d = t.d[s];
-  double px, py, pz, mdim;
-  if (t.pos64) {
-    px = t.pos64[3 * s];
-    py = t.pos64[3 * s + 1];
-    pz = t.pos64[3 * s + 2];
-    mdim = fmax(fmax(t.dims64[3 * s], t.dims64[3 * s + 1]), t.dims64[3 * s + 2]);
-  } else {
-    px = a.x; py = a.y; pz = a.z;
-    mdim = (double)fmaxf(fmaxf(d.x, d.y), d.z);
-  }
+  const Crystal64 k = load64_parts(t, s);
   const double e64 = t.exp64[s];
-  const float e = (float)e64;
-  const float m = (float)__dmul_rn(mdim, e64);
-  sm.cx[c] = (float)(px - bx0);
-  sm.cy[c] = (float)(py - by0);
+  const double mdim = fmax(fmax(k.dims.x, k.dims.y), k.dims.z);
+  const double m64 = __dmul_rn(mdim, e64);
+  const float m = static_cast<float>(m64);
+  split64(k.pos.x - bx0, sm.cxh[c], sm.cxl[c]);
+  split64(k.pos.y - by0, sm.cyh[c], sm.cyl[c]);
   sm.m[c] = m;
-  sm.delta[c] = (float)(t.z0 - pz);
+  sm.delta[c] = static_cast<float>(t.z0 - k.pos.z);
   sm.sig[c] = t.sigma_c ? t.sigma_c[s] : t.sigma;
   sm.s[c] = static_cast<int>(s);
-  const float x = q.x, y = q.y, z = q.z, w = q.w;
+  const double x = k.q[0], y = k.q[1], z = k.q[2], w = k.q[3];
   // world = R local + p, so local_i = R_0i dx + R_1i dy + R_2i dz: rows 0..2 of R.
-  const float R0[3] = {1.f - 2.f * (y * y + z * z), 2.f * (x * y - z * w), 2.f * (x * z + y * w)};
-  const float R1[3] = {2.f * (x * y + z * w), 1.f - 2.f * (x * x + z * z), 2.f * (y * z - x * w)};
-  const float R2[3] = {2.f * (x * z - y * w), 2.f * (y * z + x * w), 1.f - 2.f * (x * x + y * y)};
-  const float D[3] = {d.x * e, d.y * e, d.z * e};
-  const float eps = 5.9604645e-8f;
-  const float dlt = SCAN_DELTA;
-  if (morph_of(d) == 0) {
-    sm.type[c] = 0;
-    float invmax = 0.0f, Dmax = fmaxf(fmaxf(D[0], D[1]), D[2]);
+  const double R0[3] = {1.0 - 2.0 * (y * y + z * z), 2.0 * (x * y - z * w), 2.0 * (x * z + y * w)};
+  const double R1[3] = {2.0 * (x * y + z * w), 1.0 - 2.0 * (x * x + z * z), 2.0 * (y * z - x * w)};
+  const double R2[3] = {2.0 * (x * z - y * w), 2.0 * (y * z + x * w), 1.0 - 2.0 * (x * x + y * y)};
+  const double D[3] = {k.dims.x * e64, k.dims.y * e64, k.dims.z * e64};
+  if (k.morph == 0) {
+    float invmax = 0.0f;
+    const float Dmax = static_cast<float>(fmax(fmax(D[0], D[1]), D[2]));
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-      sm.g[i][c] = R0[i];
-      sm.g[3 + i][c] = R1[i];
-      const float inv = 1.0f / (-R2[i]);
-      sm.g[6 + i][c] = inv;
-      sm.g[9 + i][c] = D[i];
+      split64(R0[i], sm.g[i][c], sm.g[3 + i][c]);
+      split64(R1[i], sm.g[6 + i][c], sm.g[9 + i][c]);
+      const float inv = static_cast<float>(1.0 / (-R2[i]));
+      sm.g[12 + i][c] = inv;
+      split64(D[i], sm.g[15 + i][c], sm.g[18 + i][c]);
       invmax = fmaxf(invmax, fabsf(inv));
     }
-    const float Tmax = (Dmax + 2.0f * m) * invmax;
-    float E = 4.0f * ((24.0f * eps * m + 2.0f * dlt + 2.0f * eps * Dmax) * invmax +
-                      eps * Tmax * (12.0f * invmax + 2.0f));
-    if (!(E < 1e30f)) E = INFINITY;  // axis-parallel faces: always decide in FP64
-    sm.err[c] = E;
+    if (!(invmax < 1e30f)) {
+      sm.kind[c] = K_FP64;
+      sm.err[c] = INFINITY;
+    } else if (invmax > 15.0f) {
+      sm.kind[c] = K_CUBE_DF;
+      sm.err[c] = 0.0f;  // bounds are formed per ray from the t values
+    } else {
+      sm.kind[c] = K_CUBE;
+      // |d local| <= 4e-7 m + 1e-7 (rounded rows, offsets); |d D| <= eps D; each t = (+-D - lo)
+      // * inv carries (d lo + d D) |inv| + 2 eps |t|, with |t| <= (D + 2m) invmax.
+      sm.err[c] = 4.0f * ((4e-7f * m + 1e-7f + EPS32 * Dmax) * invmax + 2.0f * EPS32 * (Dmax + 2.0f * m) * invmax);
+    }
   } else {
-    sm.type[c] = 1;
-    float A = 0.0f, Dmin = fminf(fminf(D[0], D[1]), D[2]);
+    sm.kind[c] = K_ELLIPSOID;
+    double A = 0.0;
+    const double Dmin = fmin(fmin(D[0], D[1]), D[2]);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-      sm.g[i][c] = R0[i] / D[i];
-      sm.g[3 + i][c] = R1[i] / D[i];
-      const float ei = -R2[i] / D[i];
-      sm.g[6 + i][c] = ei;
+      sm.g[i][c] = static_cast<float>(R0[i] / D[i]);
+      sm.g[3 + i][c] = static_cast<float>(R1[i] / D[i]);
+      const double ei = -R2[i] / D[i];
+      sm.g[6 + i][c] = static_cast<float>(ei);
       A += ei * ei;
     }
-    sm.g[9][c] = A;
-    sm.g[10][c] = 1.0f / A;
-    sm.g[11][c] = 0.0f;
-    const float Pmax = 1.4142136f * m / Dmin;
-    const float dP = 1.7320508f * (28.0f * eps * m + 2.0f * dlt) / Dmin;
-    const float de = 1.7320508f * 14.0f * eps / Dmin;
-    const float sA = sqrtf(A);
-    sm.err[c] = 2.0f * (4.0f * A * Pmax * dP + 4.0f * sA * (Pmax * Pmax + 1.0f) * de +
-                        6.0f * eps * A * (2.0f * Pmax * Pmax + 1.0f));
+    sm.g[9][c] = static_cast<float>(A);
+    sm.g[10][c] = static_cast<float>(1.0 / A);
+    // h = 1 - |P_perp|^2; P (|P| <= sqrt(2) m / Dmin) and P_perp = P + tc e carry ~8 eps |P|
+    // each, so |d h| <= 2 |P_perp| 8 eps sqrt(3) Pmax + 4 eps; four times that as the bound.
+    const float Pmax = static_cast<float>(1.4142135623730951 * m64 / Dmin);
+    sm.err[c] = 4.0f * (2.0f * 1.05f * 8.0f * EPS32 * 1.7320508f * Pmax + 4.0f * EPS32) + 1e-9f;
   }
 }
 
@@ -149,21 +175,31 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const ScanTile* __restric
   const uint32_t sx = st % t.g, sy = st / t.g;
   const double bx0 = __dmul_rn(static_cast<double>(bx * t.bin_px), t.pw);
   const double by0 = __dmul_rn(static_cast<double>(by * t.bin_px), t.ph);
-  // FP32 ray position relative to the bin corner.
-  float ox = 0.0f, oy = 0.0f;
-  P4 r{};
+  // Ray position relative to the bin corner as a float pair.  The offset in units of the
+  // 24-bit jitter is an exact integer X = (l g + s) 2^24 + u, so x = X * pw / (g 2^24).
+  float oxh = 0.0f, oxl = 0.0f, oyh = 0.0f, oyl = 0.0f;
   if (active) {
     const uint64_t ps = t.seed + static_cast<uint64_t>(px) * 0x9E3779B97F4A7C15ull +
                         static_cast<uint64_t>(py) * 0xC6A4A7935BD1E995ull;
-    r = philox(sy * t.g + sx, 0, 0, TAG_SCAN, static_cast<uint32_t>(ps), static_cast<uint32_t>(ps >> 32));
-    const float gf = (float)t.g;
-    ox = ((float)lx + ((float)sx + uf(r.x)) / gf) * (float)t.pw;
-    oy = ((float)ly + ((float)sy + uf(r.y)) / gf) * (float)t.ph;
+    const P4 r = philox(sy * t.g + sx, 0, 0, TAG_SCAN, static_cast<uint32_t>(ps), static_cast<uint32_t>(ps >> 32));
+    const double scale = 1.0 / (static_cast<double>(t.g) * 16777216.0);
+    float cxh, cxl, cyh, cyl;
+    split64(t.pw * scale, cxh, cxl);
+    split64(t.ph * scale, cyh, cyl);
+    const uint32_t X = ((lx * t.g + sx) << 24) + (r.x >> 8);
+    const uint32_t Y = ((ly * t.g + sy) << 24) + (r.y >> 8);
+    const float Xh = static_cast<float>(X), Yh = static_cast<float>(Y);
+    const float Xl = static_cast<float>(static_cast<long long>(X) - static_cast<long long>(Xh));
+    const float Yl = static_cast<float>(static_cast<long long>(Y) - static_cast<long long>(Yh));
+    float p, e;
+    two_prod(Xh, cxh, p, e);
+    fast_two_sum(p, e + (Xh * cxl + Xl * cxh), oxh, oxl);
+    two_prod(Yh, cyh, p, e);
+    fast_two_sum(p, e + (Yh * cyl + Yl * cyh), oyh, oyl);
   }
-  long long Lfix = 0;  // sum of sigma-weighted chords, 2^-40 um units (sigma folded in when per-crystal)
+  long long Lfix = 0;  // chord sum (sigma-weighted when per crystal), 2^-40 um units
   uint32_t nh = 0, nfb = 0;
   const uint32_t b0 = t.bin_off[bin], b1 = t.bin_off[bin + 1];
-  const float EB = 2.0f * SCAN_DELTA;
   const bool per_crystal = t.sigma_c != nullptr;
   for (uint32_t base = b0; base < b1; base += SCAN_CH) {
     const uint32_t cnt = min(static_cast<uint32_t>(SCAN_CH), b1 - base);
@@ -172,51 +208,84 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const ScanTile* __restric
     __syncthreads();
     if (!active) continue;
     for (uint32_t c = 0; c < cnt; ++c) {
-      const float dx = ox - sm.cx[c], dy = oy - sm.cy[c];
-      const float m = sm.m[c];
-      const float mx = m - fabsf(dx), my = m - fabsf(dy), mz = sm.delta[c] + m;
-      if (mx < -EB || my < -EB || mz < -EB) continue;
-      bool amb = mx <= EB || my <= EB || mz <= EB;
+      // Ray minus crystal centre, x and y, as float pairs.
+      float dh, dl, dx, dxl, dy, dyl;
+      two_sum(oxh, -sm.cxh[c], dh, dl);
+      fast_two_sum(dh, dl + (oxl - sm.cxl[c]), dx, dxl);
+      two_sum(oyh, -sm.cyh[c], dh, dl);
+      fast_two_sum(dh, dl + (oyl - sm.cyl[c]), dy, dyl);
+      const float m = sm.m[c], delta = sm.delta[c];
+      // Own box (strict containment in x and y, entry below the origin in z): exact margins
+      // up to ~2 eps m.
+      const float mx = m - fabsf(dx), my = m - fabsf(dy), mz = delta + m;
+      const float EB = 7.2e-7f * m + 1e-9f, EBz = 1e-6f + 2.4e-7f * m;
+      if (mx < -EB || my < -EB || mz < -EBz) continue;
+      const int kind = sm.kind[c];
+      bool amb = mx <= EB || my <= EB || mz <= EBz || kind == K_FP64;
       bool hit = false;
       float chord = 0.0f;
       if (!amb) {
-        const float E = sm.err[c];
-        const float delta = sm.delta[c];
-        if (sm.type[c] == 0) {
+        if (kind != K_ELLIPSOID) {
           float tmin = -INFINITY, tmax = INFINITY;
 #pragma unroll
           for (int i = 0; i < 3; ++i) {
-            const float lo_i = sm.g[i][c] * dx + sm.g[3 + i][c] * dy;
-            const float inv = sm.g[6 + i][c], D = sm.g[9 + i][c];
-            const float t1 = (-D - lo_i) * inv, t2 = (D - lo_i) * inv;
+            const float inv = sm.g[12 + i][c], Dh = sm.g[15 + i][c];
+            float a1, a2;
+            if (kind == K_CUBE) {
+              const float lo_i = fmaf(sm.g[i][c], dx, sm.g[6 + i][c] * dy);
+              a1 = -Dh - lo_i;
+              a2 = Dh - lo_i;
+            } else {
+              // Local origin as a float pair, then the two face offsets exactly rounded.
+              const float R0h = sm.g[i][c], R0l = sm.g[3 + i][c], R1h = sm.g[6 + i][c], R1l = sm.g[9 + i][c];
+              const float Dl = sm.g[18 + i][c];
+              float p0, e0, p1, e1, sh, sl;
+              two_prod(R0h, dx, p0, e0);
+              two_prod(R1h, dy, p1, e1);
+              two_sum(p0, p1, sh, sl);
+              sl += (e0 + e1) + ((R0h * dxl + R1h * dyl) + (R0l * dx + R1l * dy));
+              float v, wv;
+              two_sum(-Dh, -sh, v, wv);
+              a1 = v + ((wv - Dl) - sl);
+              two_sum(Dh, -sh, v, wv);
+              a2 = v + ((wv + Dl) - sl);
+            }
+            const float t1 = a1 * inv, t2 = a2 * inv;
             tmin = fmaxf(tmin, fminf(t1, t2));
             tmax = fminf(tmax, fmaxf(t1, t2));
           }
+          const float E = kind == K_CUBE ? sm.err[c] : 4.0f * 3.0f * EPS32 * (fabsf(tmin) + fabsf(tmax)) + 1e-9f;
           const float m1 = tmax - tmin, m2 = tmax + delta;
-          if (m1 > 2.0f * E && m2 > E + 1e-6f) {
+          const float E2 = E + 4.0f * 3.0f * EPS32 * fabsf(delta) + 2e-6f;
+          if (m1 > 2.0f * E && m2 > E2) {
             hit = true;
             chord = tmax - fmaxf(tmin, -delta);
-          } else if (!(m1 < -2.0f * E || m2 < -E - 1e-6f)) {
+          } else if (!(m1 < -2.0f * E || m2 < -E2)) {
             amb = true;
           }
         } else {
           float P[3];
 #pragma unroll
-          for (int i = 0; i < 3; ++i) P[i] = sm.g[i][c] * dx + sm.g[3 + i][c] * dy;
-          const float A = sm.g[9][c], iA = sm.g[10][c];
-          const float qd = P[0] * sm.g[6][c] + P[1] * sm.g[7][c] + P[2] * sm.g[8][c];
-          const float C = P[0] * P[0] + P[1] * P[1] + P[2] * P[2] - 1.0f;
-          const float wv = qd * qd - A * C;
-          if (wv > E) {
-            const float sq = sqrtf(wv);
-            const float t0 = (-qd - sq) * iA, t1 = (-qd + sq) * iA;
-            if (t1 + delta > 1e-4f) {
+          for (int i = 0; i < 3; ++i) P[i] = fmaf(sm.g[i][c], dx, sm.g[3 + i][c] * dy);
+          const float e0 = sm.g[6][c], e1 = sm.g[7][c], e2 = sm.g[8][c];
+          const float iA = sm.g[10][c];
+          // Closest approach along the ray (t' = tc) and the offset there: h = 1 - |P_perp|^2
+          // has the sign of the reference's discriminant.
+          const float tc = -(P[0] * e0 + P[1] * e1 + P[2] * e2) * iA;
+          const float q0 = fmaf(tc, e0, P[0]), q1 = fmaf(tc, e1, P[1]), q2 = fmaf(tc, e2, P[2]);
+          const float hh = 1.0f - (q0 * q0 + q1 * q1 + q2 * q2);
+          const float E = sm.err[c];
+          if (hh > E) {
+            const float sq = sqrtf(hh * iA);
+            const float t0 = tc - sq, t1 = tc + sq;
+            const float E2 = 4.0f * 3.0f * EPS32 * (fabsf(t1) + fabsf(delta)) + 2e-6f;
+            if (t1 + delta > E2) {
               hit = true;
               chord = t1 - fmaxf(t0, -delta);
             } else {
-              amb = true;  // crystal at or above the scanner origin: let FP64 decide
+              amb = true;
             }
-          } else if (!(wv < -E)) {
+          } else if (!(hh < -E)) {
             amb = true;
           }
         }
@@ -340,7 +409,9 @@ void scan(fg_engine* e, const fg_emulsion* em, const fg_scan_cfg& cfg, uint64_t 
   t.bin_items = items.p;
   DBuf<ScanTile> td(1, st);
   FG_CUDA(cudaMemcpyAsync(td.p, &t, sizeof(ScanTile), cudaMemcpyHostToDevice, st));
-  k_scan<<<static_cast<unsigned>(nbins), t.bin_px * t.bin_px * a, 0, st>>>(td.p, 1, e->d_err, e->d_stats);
+  // Whole warps only: the closing reductions shuffle across all 32 lanes.
+  const unsigned threads = ((t.bin_px * t.bin_px * a + 31) / 32) * 32;
+  k_scan<<<static_cast<unsigned>(nbins), threads, 0, st>>>(td.p, 1, e->d_err, e->d_stats);
   FG_CUDA(cudaGetLastError());
   FG_CUDA(cudaStreamSynchronize(st));
 }

@@ -19,7 +19,6 @@ namespace fg {
 
 constexpr int SCAN_CH = 128;        // crystals staged per pass
 constexpr int SCAN_THREADS = 256;   // rays per CTA (bin_px^2 * strata)
-constexpr float SCAN_DELTA = 4e-6f; // bound on the FP32 error of a bin-relative coordinate (um)
 
 struct ScanTile {
   const float4* a;

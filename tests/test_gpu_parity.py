@@ -260,7 +260,8 @@ def test_empty_single_and_zero_opacity(engine):
     assert rep.total_crystals == 0
     buf, img = fg.scan_emulsion(empty, fg.ScanConfig(8, 8, 4, 0, 0.25), 1)
     assert (buf == 1.0).all() and (img == 255).all()
-    one = fg.VirtualEmulsionLayer.from_crystals(cfg, [[4.0, 4.0, 7.0]], [[0.5, 0.5, 0.5]], identity_quats(1),
+    # A unit cube filling pixel (4, 4) exactly: chord 1 for all four strata.
+    one = fg.VirtualEmulsionLayer.from_crystals(cfg, [[4.5, 4.5, 7.0]], [[0.5, 0.5, 0.5]], identity_quats(1),
                                                 [1.0], None, engine)
     one.set_development([1], [1.0])
     buf, _ = fg.scan_emulsion(one, fg.ScanConfig(8, 8, 4, 0, 0.25), 1)
