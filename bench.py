@@ -1,0 +1,359 @@
+#!/usr/bin/env python
+"""Benchmark of the fgrain photon-transport and transmittance-scan path on GB300.
+
+Workload (one "step"): the 1024 x 1024 black-and-white image of configuration C2 rendered at
+supersample 2 (2048 x 2048 internal, tri-x cubic grains, grain 2.4 px, push 0, seed 42): 49
+overlapping tiles of up to 384 x 384 px, each synthesized, exposed, developed and scanned to
+negative density by the batched graph path.  Inputs: blurred uniform noise (sigma 16 px, seed 1,
+gamma 2.2) upsampled x2 by linear interpolation (synthetic; no dataset is involved).
+
+Reported:
+  value      output Mpx/s (1024^2 output pixels per step / device time per step), inputs resident
+             in HBM; the working set (crystals, LBVH, grids) is several GB, far larger than L2.
+  e2e        the same through the public API with page-locked host buffers: host->device copy of
+             the exposure tiles, run, device->host copy of the density tiles, every step.
+  roofline   the transport kernel against the measured HBM copy bandwidth.
+  cpu_baseline  the CPU oracle (a C++ restatement of the reference's Rayon CPU path, faithful
+             hit rule) on a bounded sample of the same tiles, all host threads.
+
+`--impl reference` times that CPU restatement alone (the reference itself is Rust and cannot be
+built here) on the same workload, metric and unit.  With torchrun (N > 1) every rank renders its
+own replica of the image (replicas only: no collective is involved), and rank 0 reports the sum.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mpx/s and photons/s on 1 GB300, batched vs plain at <=0.5% mean-T error"
+OUT_W = OUT_H = 1024
+SS = 2
+GRAIN = 2.4
+SEED = 42
+
+
+def c2_inputs():
+    from scipy.ndimage import gaussian_filter, zoom
+
+    a = np.random.default_rng(1).random((OUT_H, OUT_W))
+    lum = np.clip(gaussian_filter(a, 16.0, mode="reflect"), 0.0, None) ** 2.2
+    exposure = zoom(lum, SS, order=1, mode="nearest").astype(np.float32)
+    return exposure
+
+
+def c2_tiles(exposure):
+    import fgrain_gb300 as fg
+    from fgrain_gb300.image import tile_grid, tile_seed
+
+    H, W = exposure.shape
+    grid, step, pad = tile_grid(W, H, GRAIN)
+    params, tiles = [], []
+    for t in grid:
+        params.append(fg.tile_params("tri-x", 1.0 / GRAIN, t.tw, t.th, 1.0, 0.0, tile_seed(SEED, t)))
+        tiles.append(np.ascontiguousarray(exposure[t.y_start:t.y_start + t.th, t.x_start:t.x_start + t.tw]))
+    return grid, params, tiles
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100", "-f", self.path],
+                                         stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in Path(self.path).read_text().splitlines():
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9:
+                    rows.append(f)
+        except OSError:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except OSError:
+                pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = max((num(r[2]) for r in rows if num(r[2]) is not None), default=None)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        loaded = sorted(sm)[len(sm) // 2:] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows), "power_w_max": max((num(r[3]) or 0 for r in rows), default=None)}
+
+
+def dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0, None
+    import torch.distributed as td
+
+    td.init_process_group("gloo")
+    return td.get_rank(), td.get_world_size(), int(os.environ.get("LOCAL_RANK", "0")), td
+
+
+def reduce_max(td, v):
+    if td is None:
+        return v
+    import torch
+
+    t = torch.tensor([v], dtype=torch.float64)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+def oracle_sample(params, tiles, ntiles, threads):
+    """Renders `ntiles` tiles with the CPU oracle (faithful hit rule), tiles in parallel the way the
+    reference's rayon map does (image_pipeline.rs:427); returns (seconds, tile pixels)."""
+    from oracle import oracle as orc
+
+    idx = list(range(min(ntiles, len(params))))
+
+    def one(i):
+        p = params[i]
+        orc.render_tile("tri-x", 1.0 / GRAIN, tiles[i], p.exposure, 0.0, p.seed, orc.FAITHFUL, 1)
+        return p.width_px * p.height_px
+
+    orc.lib()
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        px = sum(ex.map(one, idx))
+    return time.perf_counter() - t0, px
+
+
+def measured_peak():
+    try:
+        d = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """dram bytes per transport launch from the committed ncu summary, or None."""
+    f = ROOT / "profiles" / "k_transport_c2.md"
+    try:
+        for line in f.read_text().splitlines():
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].strip().split()[0])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
+def run_ours(args):
+    import fgrain_gb300 as fg
+
+    rank, world, local, td = dist()
+    exposure = c2_inputs()
+    grid, params, tiles = c2_tiles(exposure)
+    engine = fg.GpuEngine(local)
+    batch = fg.Batch(params, engine, use_graph=True, autotune=True)
+    batch.set_exposure(tiles)
+    for _ in range(max(args.warmup, 0)):
+        batch.run()
+        stats = batch.wait()
+    batch.run()
+    stats = batch.wait()
+    d_batched = batch.density()
+    if td:
+        td.barrier()
+    with Clocks(local) as clk:
+        ms = batch.time(args.steps)
+    if td:
+        td.barrier()
+    clocks = clk.summary()
+    ms_max = reduce_max(td, ms)
+    per_step = ms_max / args.steps
+    out_px = OUT_W * OUT_H
+    value = world * out_px / (per_step / 1e3) / 1e6
+
+    # End to end through the public API: pinned host exposure in, pinned density out, per step.
+    pin_in = [fg.PinnedArray(t.shape) for t in tiles]
+    pin_out = [fg.PinnedArray(t.shape) for t in tiles]
+    for pi, t in zip(pin_in, tiles):
+        pi.array[...] = t
+    def e2e_step():
+        batch.set_exposure([p.array for p in pin_in])
+        batch.run()
+        batch.wait()
+        ptrs = [p.array for p in pin_out]
+        import ctypes as C
+        arr = (C.POINTER(C.c_float) * len(ptrs))(*[a.ctypes.data_as(C.POINTER(C.c_float)) for a in ptrs])
+        st = engine._lib.fg_batch_get_density(batch._h, arr)
+        if st != 0:
+            raise RuntimeError("density copy failed")
+    e2e_step()
+    if td:
+        td.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = reduce_max(td, time.perf_counter() - t0) / args.steps
+    h2d = sum(t.nbytes for t in tiles)
+    d2h = h2d
+    e2e_value = world * out_px / e2e_s / 1e6
+
+    # Plain per-tile path (one render_tile call per tile, each making and freeing its buffers).
+    t0 = time.perf_counter()
+    d_plain = [fg.render_tile(t, p, engine) for t, p in zip(tiles, params)]
+    plain_s = time.perf_counter() - t0
+    plain_value = out_px / plain_s / 1e6
+    Tb = np.concatenate([(10.0 ** -(d.astype(np.float64) - 0.05)).ravel() for d in d_batched])
+    Tp = np.concatenate([(10.0 ** -(d.astype(np.float64) - 0.05)).ravel() for d in d_plain])
+    mean_t_err = abs(Tb.mean() - Tp.mean()) / Tp.mean()
+    bit_identical = all(np.array_equal(a, b) for a, b in zip(d_batched, d_plain))
+
+    # Roofline of the transport kernel: algorithmic bytes per launch = 4 B exposure gather per
+    # photon + 8 B count read-modify-write per hit + 116 B per crystal (48 B record, 64 B node,
+    # 4 B count zero) read once.
+    P, H, N = stats["photons"], stats["hits"], stats["crystals"]
+    alg_bytes = 4.0 * P + 8.0 * H + 116.0 * N
+    peak, peak_kind = measured_peak()
+    achieved = alg_bytes / (stats["transport_ms"] / 1e3) / 1e9
+    photons_per_s = P / (stats["transport_ms"] / 1e3)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        secs, px = oracle_sample(params, tiles, max(threads, 4), threads)
+        total_px = sum(p.width_px * p.height_px for p in params)
+        cpu_value = out_px * (px / total_px) / secs / 1e6
+        cpu = {"value": cpu_value, "unit": "Mpx/s", "cores": threads, "kind": "port",
+               "sample": f"{max(threads, 4)} of the 49 C2 tiles rendered by the C++ restatement of the "
+                         f"reference CPU path (faithful hit rule), tiles in parallel; scaled by tile pixels"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Mpx/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "C2: 1024x1024 blurred-noise luminance (sigma 16, seed 1, gamma 2.2), tri-x, "
+                                   "grain 2.4 px, push 0, supersample 2 (2048^2 internal, 49 tiles), batched "
+                                   "graph path", "tiles": len(params), "internal_px": int(exposure.size),
+                       "output_px": out_px, "l2": "working set (crystals, LBVH, grids) exceeds L2; no flush",
+                       "parallelism": f"replicas x{world}"},
+            "photons_per_s": photons_per_s,
+            "plain_mpx_s": plain_value,
+            "batched_over_plain": value / world / plain_value,
+            "mean_T_rel_err_batched_vs_plain": mean_t_err,
+            "batched_equals_plain_bitwise": bit_identical,
+            "stage_ms": {k: stats[k] for k in ("synth_ms", "bvh_ms", "transport_ms", "develop_ms", "scan_ms",
+                                               "total_ms")},
+            "work": {k: stats[k] for k in ("crystals", "photons", "hits", "rays", "scan_hits", "scan_fallbacks")},
+            "launch_shape": {"transport_threads": stats["transport_threads"],
+                             "transport_blocks": stats["transport_blocks"], "scan_bin_px": stats["scan_bin_px"]},
+            "e2e": {"value": e2e_value, "unit": "Mpx/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": stats["kernel_launches"] * args.steps,
+            "roofline": {"bound": "hbm", "kernel": "k_transport", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                         "traffic": profile_traffic(),
+                         "alg_bytes_per_launch": alg_bytes},
+            "clocks": clocks,
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line))
+    for p in pin_in + pin_out:
+        p.free()
+    batch.close()
+    if td:
+        td.destroy_process_group()
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    exposure = c2_inputs()
+    grid, params, tiles = c2_tiles(exposure)
+    threads = os.cpu_count() or 1
+    n = max(threads, 4)
+    for _ in range(max(args.warmup, 0) and 1):
+        oracle_sample(params, tiles, min(n, 4), threads)
+    secs, px = 0.0, 0
+    for _ in range(args.steps):
+        s, p = oracle_sample(params, tiles, n, threads)
+        secs += s
+        px += p
+    total_px = sum(p.width_px * p.height_px for p in params)
+    value = OUT_W * OUT_H * (px / args.steps / total_px) / (secs / args.steps) / 1e6
+    sample = (f"each step renders {n} of the 49 C2 tiles with the C++ restatement of the reference CPU path "
+              f"(faithful hit rule; the Rust reference cannot be built here), tiles in parallel on {threads} "
+              f"threads; output Mpx/s scaled by tile pixels")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mpx/s", "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "C2 (see ours)", "tiles_per_step": n},
+        "cpu_baseline": {"value": value, "unit": "Mpx/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "Mpx/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -8,5 +8,6 @@ from .api import (  # noqa: F401
     DevelopmentConfig, DevelopmentReport, EmulsionConfig, ExposureConfig, GelatinOptics,
     GpuEngine, GpuError, Morphology, ScanConfig, ScanMode, VirtualEmulsionLayer,
     develop_emulsion, expose_emulsion, get_gpu_engine, replay_rays, replay_segments,
-    scan_emulsion, scan_ray_hits, SEGMENT_DTYPE,
+    scan_emulsion, scan_ray_hits, SEGMENT_DTYPE, Batch, render_tile, tile_params,
+    PinnedArray,
 )

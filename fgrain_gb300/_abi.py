@@ -93,6 +93,36 @@ class fg_timings(C.Structure):
                 ("error_word", C.c_uint32)]
 
 
+class fg_tile_params(C.Structure):
+    _fields_ = [("film_w", C.c_double), ("film_h", C.c_double), ("film_d", C.c_double),
+                ("width_px", C.c_uint32), ("height_px", C.c_uint32),
+                ("samples_per_pixel", C.c_uint32), ("threshold_photons", C.c_uint32),
+                ("silver_opacity", C.c_double), ("seed", C.c_uint64),
+                ("r_min", C.c_double), ("mean_crystal_radius", C.c_double), ("size_variance", C.c_double),
+                ("morphology", C.c_int32), ("_pad0", C.c_int32),
+                ("tabular_aspect_ratio", C.c_double), ("base_sensitivity", C.c_double),
+                ("exposure", C.c_double), ("filament_expansion", C.c_double),
+                ("clumping_proximity_factor", C.c_double), ("optics", fg_optics),
+                ("photons_per_sq_um", C.c_double), ("illumination_angle_rad", C.c_double),
+                ("crystal_absorption_coeff", C.c_double), ("max_bounces", C.c_uint32),
+                ("_pad1", C.c_uint32)]
+
+
+class fg_batch_options(C.Structure):
+    _fields_ = [("use_graph", C.c_int32), ("autotune", C.c_int32), ("transport_threads", C.c_uint32),
+                ("transport_blocks", C.c_uint32), ("scan_bin_px", C.c_uint32), ("_pad", C.c_uint32)]
+
+
+class fg_batch_stats(C.Structure):
+    _fields_ = [("synth_ms", C.c_double), ("bvh_ms", C.c_double), ("transport_ms", C.c_double),
+                ("develop_ms", C.c_double), ("scan_ms", C.c_double), ("total_ms", C.c_double),
+                ("crystals", C.c_uint64), ("photons", C.c_uint64), ("rays", C.c_uint64),
+                ("pixels", C.c_uint64), ("hits", C.c_uint64), ("scan_hits", C.c_uint64),
+                ("scan_fallbacks", C.c_uint64), ("transport_threads", C.c_uint32),
+                ("transport_blocks", C.c_uint32), ("scan_bin_px", C.c_uint32), ("graph", C.c_uint32),
+                ("kernel_launches", C.c_uint32), ("_pad", C.c_uint32)]
+
+
 _vp = C.c_void_p
 _st = C.c_int
 _u32p = C.POINTER(C.c_uint32)
@@ -130,6 +160,24 @@ PROTOTYPES = {
     "fg_replay_rays": (_st, [_vp, _vp, _dp, _dp, C.c_size_t, C.c_int, _u32p, _u32p,
                              C.c_size_t, _szp, _dp]),
     "fg_scan_ray_hits": (_st, [_vp, _vp, C.POINTER(fg_scan_cfg), C.c_uint64, _u16p]),
+    "fg_tile_params_preset": (_st, [C.c_char_p, C.c_double, C.c_uint32, C.c_uint32, C.c_double,
+                                    C.c_double, C.c_uint64, C.POINTER(fg_tile_params)]),
+    "fg_render_tile": (_st, [_vp, _fp, C.POINTER(fg_tile_params), _fp]),
+    "fg_batch_create": (_st, [_vp, C.POINTER(fg_tile_params), C.c_uint32, C.POINTER(fg_batch_options),
+                              C.POINTER(_vp)]),
+    "fg_batch_destroy": (_st, [_vp]),
+    "fg_batch_set_exposure": (_st, [_vp, C.POINTER(_fp)]),
+    "fg_batch_exposure_device": (_st, [_vp, C.c_uint32, C.POINTER(_fp)]),
+    "fg_batch_density_device": (_st, [_vp, C.c_uint32, C.POINTER(_fp)]),
+    "fg_batch_run": (_st, [_vp]),
+    "fg_batch_wait": (_st, [_vp, C.POINTER(fg_batch_stats)]),
+    "fg_batch_get_density": (_st, [_vp, C.POINTER(_fp)]),
+    "fg_batch_tile_crystals": (_st, [_vp, C.c_uint32, C.POINTER(fg_crystals_out), _u32p, _u8p, _dp,
+                                     C.c_size_t, _szp]),
+    "fg_batch_time": (_st, [_vp, C.c_uint32, _dp]),
+    "fg_host_alloc": (_st, [C.c_size_t, C.POINTER(_vp)]),
+    "fg_host_free": (_st, [_vp]),
+    "fg_render_batch": (_st, [_vp, C.POINTER(fg_tile_params), C.c_uint32, C.POINTER(_fp), C.POINTER(_fp)]),
 }
 
 _lib = None

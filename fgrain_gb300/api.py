@@ -392,3 +392,127 @@ def scan_ray_hits(emulsion: VirtualEmulsionLayer, config: ScanConfig, seed: int)
     e = emulsion.engine
     _check(e, e._lib.fg_scan_ray_hits(e._h, emulsion._h, C.byref(cfg), seed, _ptr(out, C.c_uint16)))
     return out
+
+
+# ------------------------------------------------------------------------------------------------
+# Tiles and batches (the drop-in for GpuEngine::render_tile_all_gpu, gpu.rs:491-938, with the CPU
+# tile worker's physics, image_pipeline.rs:924-1014).
+
+def tile_params(preset: str, pixel_size_um: float, tw: int, th: int, exposure: float = 1.0,
+                push: float = 0.0, tile_seed: int = 0) -> _abi.fg_tile_params:
+    """The parameters the reference's CPU tile worker uses for one tile."""
+    p = _abi.fg_tile_params()
+    _check(None, _abi.load().fg_tile_params_preset(preset.encode(), pixel_size_um, tw, th, exposure, push,
+                                                   tile_seed & 0xFFFFFFFFFFFFFFFF, C.byref(p)))
+    return p
+
+
+def render_tile(exposure_tile, params: _abi.fg_tile_params, engine: GpuEngine | None = None) -> np.ndarray:
+    """Plain per-tile path: exposure tile -> negative density tile (blocking)."""
+    e = _engine(engine)
+    tile = np.ascontiguousarray(exposure_tile, np.float32)
+    assert tile.shape == (params.height_px, params.width_px)
+    out = np.zeros_like(tile)
+    _check(e, e._lib.fg_render_tile(e._h, _ptr(tile, C.c_float), C.byref(params), _ptr(out, C.c_float)))
+    return out
+
+
+class Batch:
+    """Many tiles rendered by one graph-captured sequence of launches."""
+
+    def __init__(self, params, engine: GpuEngine | None = None, use_graph=True, autotune=False,
+                 transport_threads=0, transport_blocks=0, scan_bin_px=0):
+        self.engine = _engine(engine)
+        self.params = list(params)
+        arr = (_abi.fg_tile_params * len(self.params))(*self.params)
+        opt = _abi.fg_batch_options(int(use_graph), int(autotune), transport_threads, transport_blocks,
+                                    scan_bin_px, 0)
+        h = C.c_void_p()
+        e = self.engine
+        _check(e, e._lib.fg_batch_create(e._h, arr, len(self.params), C.byref(opt), C.byref(h)))
+        self._h = h
+
+    def set_exposure(self, tiles):
+        tiles = [np.ascontiguousarray(t, np.float32) for t in tiles]
+        for t, p in zip(tiles, self.params):
+            assert t.shape == (p.height_px, p.width_px)
+        ptrs = (C.POINTER(C.c_float) * len(tiles))(*[_ptr(t, C.c_float) for t in tiles])
+        e = self.engine
+        _check(e, e._lib.fg_batch_set_exposure(self._h, ptrs))
+        self._keep = tiles
+
+    def run(self):
+        e = self.engine
+        _check(e, e._lib.fg_batch_run(self._h))
+
+    def wait(self) -> dict:
+        s = _abi.fg_batch_stats()
+        e = self.engine
+        _check(e, e._lib.fg_batch_wait(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def time(self, steps: int) -> float:
+        """Device milliseconds of `steps` back-to-back replays (CUDA events on the engine stream)."""
+        ms = C.c_double()
+        e = self.engine
+        _check(e, e._lib.fg_batch_time(self._h, steps, C.byref(ms)))
+        return ms.value
+
+    def density(self):
+        outs = [np.zeros((p.height_px, p.width_px), np.float32) for p in self.params]
+        ptrs = (C.POINTER(C.c_float) * len(outs))(*[_ptr(o, C.c_float) for o in outs])
+        e = self.engine
+        _check(e, e._lib.fg_batch_get_density(self._h, ptrs))
+        return outs
+
+    def tile_crystals(self, tile: int) -> dict:
+        e = self.engine
+        n = C.c_size_t()
+        _check(e, e._lib.fg_batch_tile_crystals(self._h, tile, None, None, None, None, 0, C.byref(n)))
+        k = n.value
+        out = {"pos": np.zeros((k, 3)), "dims": np.zeros((k, 3)), "quat": np.zeros((k, 4)),
+               "sensitivity": np.zeros(k), "morphology": np.zeros(k, np.int32),
+               "counts": np.zeros(k, np.uint32), "developed": np.zeros(k, np.uint8), "expansion": np.zeros(k)}
+        o = _abi.fg_crystals_out(_ptr(out["pos"], C.c_double), _ptr(out["dims"], C.c_double),
+                                 _ptr(out["quat"], C.c_double), _ptr(out["sensitivity"], C.c_double),
+                                 _ptr(out["morphology"], C.c_int32))
+        _check(e, e._lib.fg_batch_tile_crystals(self._h, tile, C.byref(o), _ptr(out["counts"], C.c_uint32),
+                                                _ptr(out["developed"], C.c_uint8),
+                                                _ptr(out["expansion"], C.c_double), k, C.byref(n)))
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.engine._lib.fg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PinnedArray:
+    """A numpy view of page-locked host memory (fg_host_alloc)."""
+
+    def __init__(self, shape, dtype=np.float32):
+        self._lib = _abi.load()
+        self.nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        p = C.c_void_p()
+        _check(None, self._lib.fg_host_alloc(self.nbytes, C.byref(p)))
+        self._p = p
+        buf = (C.c_byte * self.nbytes).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=dtype).reshape(shape)
+
+    def free(self):
+        if getattr(self, "_p", None):
+            self.array = None
+            self._lib.fg_host_free(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

@@ -1,0 +1,1103 @@
+// Batched tile pipeline: many exposure tiles (uneven sizes, stocks, push, seeds) rendered to
+// negative density in one sequence of launches:
+//   synthesis (column Bridson, 4 colour classes) -> thinning -> Morton compaction -> LBVH
+//   -> persistent transport over all tiles' photons -> development -> bins -> binned scan.
+// Every kernel covers all tiles at once (per-tile descriptors in HBM, tile found by binary search
+// on a prefix of work items), every buffer is allocated when the plan is made, and nothing waits
+// on the host, so the sequence is captured once into a CUDA graph and replayed.  An autotuner
+// picks the transport launch shape and the scan bin edge when the plan is made.
+//
+// The plain per-tile path (fg_render_tile, the drop-in for GpuEngine::render_tile_all_gpu,
+// gpu.rs:491-938) is the same plan for one tile, made, run and freed per call.
+#include <cub/device/device_scan.cuh>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+
+#include "fg_internal.h"
+#include "fg_scan.cuh"
+#include "fg_synth.cuh"
+#include "fg_transport.cuh"
+
+namespace fg {
+
+void launch_bridson(const SynthTile* tiles, int ntiles, int color, unsigned ncols, int gdmax, uint32_t* cells,
+                    uint32_t* err, cudaStream_t st);
+size_t bridson_smem(int gdmax);
+void launch_synth_post(const SynthTile* tiles, int ntiles, unsigned long long ncells, unsigned long long nslots,
+                       uint32_t* cells, uint32_t* npts, uint32_t* flags, cudaStream_t st);
+void launch_emit(const SynthTile* tiles, int ntiles, unsigned long long nslots, const uint32_t* cells,
+                 const uint32_t* scan, float4* A, float4* Q, float4* D, uint64_t* keys, uint32_t* err,
+                 cudaStream_t st);
+void launch_transport(const TileDesc* tiles_dev, int ntiles, unsigned long long total, unsigned long long* counter,
+                      uint32_t* err, unsigned long long* stats, int sm_count, cudaStream_t st);
+void launch_transport_shape(const TileDesc* tiles_dev, int ntiles, unsigned long long total,
+                            unsigned long long* counter, uint32_t* err, unsigned long long* stats,
+                            unsigned blocks, unsigned threads, cudaStream_t st);
+void launch_scan(const ScanTile* tiles, int ntiles, unsigned long long nbins, unsigned threads, uint32_t* err,
+                 unsigned long long* stats, cudaStream_t st);
+uint32_t scan_bin_px(uint32_t spp);
+
+// Per-tile state for the batched LBVH, development and binning kernels.
+struct __align__(16) BTile {
+  unsigned long long cbase;   // first crystal slot
+  unsigned long long bin_base;
+  double fe, prox;            // filament expansion, clumping proximity (development.rs:12-27)
+  double max_base;            // largest undeveloped max_dim (device-written)
+  uint32_t n;                 // crystals (device-written)
+  uint32_t thr;               // threshold photons
+  uint32_t nbx, nby;
+  float binw_x, binw_y;
+  float pad;                  // leaf box padding
+  uint32_t _pad;
+};
+
+__device__ __forceinline__ int btile_of(const BTile* tiles, int ntiles, unsigned long long g) {
+  int lo = 0, hi = ntiles - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tiles[mid].cbase <= g) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void k_set_n(const SynthTile* syn, int ntiles, const uint32_t* slot_scan, BTile* bt, TileDesc* td,
+                        ScanTile* sc, uint32_t* ncrys) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  const uint32_t n = slot_scan[syn[t].slot_base + syn[t].slots] - slot_scan[syn[t].slot_base];
+  const uint32_t nn = min(n, syn[t].ccap);
+  bt[t].n = nn;
+  bt[t].max_base = 0.0;
+  td[t].n = nn;
+  sc[t].n = nn;
+  ncrys[t] = nn;
+}
+
+__device__ __forceinline__ int kdelta_b(const uint64_t* keys, long long n, long long i, long long j) {
+  if (j < 0 || j >= n) return -1;
+  const uint64_t ki = keys[i], kj = keys[j];
+  if (ki == kj) return 64 + __clz(static_cast<uint32_t>(i ^ j));
+  return __clzll(ki ^ kj);
+}
+
+// Karras internal nodes of every tile (node array and keys offset by the tile's crystal base).
+__global__ void k_karras_b(const BTile* __restrict__ bt, int ntiles, unsigned long long ncap,
+                           const uint64_t* __restrict__ keys_all, Node* nodes_all, int* leaf_parent_all,
+                           int* visit_all) {
+  const unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+  if (g >= ncap) return;
+  const BTile& t = bt[btile_of(bt, ntiles, g)];
+  const long long i = static_cast<long long>(g - t.cbase);
+  const long long n = t.n;
+  Node* nodes = nodes_all + t.cbase;
+  int* leaf_parent = leaf_parent_all + t.cbase;
+  if (n == 1) {
+    if (i == 0) {
+      const float q = __int_as_float(0x7fc00000);
+      nodes[0].a = make_float4(q, q, q, q);
+      nodes[0].b = make_float4(q, q, q, q);
+      nodes[0].c = make_float4(q, q, q, q);
+      nodes[0].d = make_int4(~0, INT32_MIN, -1, 0);
+      leaf_parent[0] = 0;
+      visit_all[t.cbase] = 1;  // the lone leaf must climb past its root
+    }
+    return;
+  }
+  if (i >= n - 1) return;
+  const uint64_t* keys = keys_all + t.cbase;
+  const int dir = (kdelta_b(keys, n, i, i + 1) - kdelta_b(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+  const int dmin = kdelta_b(keys, n, i, i - dir);
+  long long lmax = 2;
+  while (kdelta_b(keys, n, i, i + lmax * dir) > dmin) lmax <<= 1;
+  long long l = 0;
+  for (long long s = lmax >> 1; s >= 1; s >>= 1)
+    if (kdelta_b(keys, n, i, i + (l + s) * dir) > dmin) l += s;
+  const long long j = i + l * dir;
+  const int dnode = kdelta_b(keys, n, i, j);
+  long long s = 0, st = l;
+  do {
+    st = (st + 1) >> 1;
+    if (kdelta_b(keys, n, i, i + (s + st) * dir) > dnode) s += st;
+  } while (st > 1);
+  const long long gamma = i + s * dir + (dir < 0 ? -1 : 0);
+  const long long lo = i < j ? i : j, hi = i < j ? j : i;
+  int left, right;
+  if (lo == gamma) {
+    left = ~static_cast<int>(gamma);
+    leaf_parent[gamma] = static_cast<int>(i);
+  } else {
+    left = static_cast<int>(gamma);
+    nodes[gamma].d.z = static_cast<int>(i);
+  }
+  if (hi == gamma + 1) {
+    right = ~static_cast<int>(gamma + 1);
+    leaf_parent[gamma + 1] = static_cast<int>(i);
+  } else {
+    right = static_cast<int>(gamma + 1);
+    nodes[gamma + 1].d.z = static_cast<int>(i);
+  }
+  nodes[i].d.x = left;
+  nodes[i].d.y = right;
+  if (i == 0) nodes[0].d.z = -1;
+}
+
+// Bottom-up fit of every tile's tree (leaf boxes bound the whole crystal shape, padded).
+__global__ void k_fit_b(const BTile* __restrict__ bt, int ntiles, unsigned long long ncap,
+                        const float4* __restrict__ A, const float4* __restrict__ Q, const float4* __restrict__ D,
+                        Node* nodes_all, const int* leaf_parent_all, int* visit_all) {
+  const unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+  if (g >= ncap) return;
+  const BTile& t = bt[btile_of(bt, ntiles, g)];
+  const uint32_t s = static_cast<uint32_t>(g - t.cbase);
+  if (s >= t.n) return;
+  Node* nodes = nodes_all + t.cbase;
+  int* visit = visit_all + t.cbase;
+  const float4 a = A[g], q = Q[g], d = D[g];
+  float lo[3], hi[3];
+  {
+    const float x = q.x, y = q.y, z = q.z, w = q.w;
+    const float R[3][3] = {{1.f - 2.f * (y * y + z * z), 2.f * (x * y - z * w), 2.f * (x * z + y * w)},
+                           {2.f * (x * y + z * w), 1.f - 2.f * (x * x + z * z), 2.f * (y * z - x * w)},
+                           {2.f * (x * z - y * w), 2.f * (y * z + x * w), 1.f - 2.f * (x * x + y * y)}};
+    const float dm[3] = {d.x, d.y, d.z};
+    const bool cubic = __float_as_int(d.w) == 0;
+    const float p[3] = {a.x, a.y, a.z};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      float ext;
+      if (cubic) {
+        ext = fabsf(R[i][0]) * dm[0] + fabsf(R[i][1]) * dm[1] + fabsf(R[i][2]) * dm[2];
+      } else {
+        const float u = R[i][0] * dm[0], v = R[i][1] * dm[1], tt = R[i][2] * dm[2];
+        ext = sqrtf(u * u + v * v + tt * tt);
+      }
+      const float h = ext * 1.0001f + t.pad;
+      lo[i] = p[i] - h;
+      hi[i] = p[i] + h;
+    }
+  }
+  int code = ~static_cast<int>(s);
+  int p = leaf_parent_all[g];
+  while (p >= 0) {
+    float* f = reinterpret_cast<float*>(&nodes[p]);
+    const int off = (nodes[p].d.x == code) ? 0 : 6;
+    __stcg(f + off + 0, lo[0]);
+    __stcg(f + off + 1, lo[1]);
+    __stcg(f + off + 2, lo[2]);
+    __stcg(f + off + 3, hi[0]);
+    __stcg(f + off + 4, hi[1]);
+    __stcg(f + off + 5, hi[2]);
+    __threadfence();
+    if (atomicAdd(&visit[p], 1) == 0) return;
+    __threadfence();
+    float v[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) v[k] = __ldcg(f + k);
+    lo[0] = fminf(v[0], v[6]);
+    lo[1] = fminf(v[1], v[7]);
+    lo[2] = fminf(v[2], v[8]);
+    hi[0] = fmaxf(v[3], v[9]);
+    hi[1] = fmaxf(v[4], v[10]);
+    hi[2] = fmaxf(v[5], v[11]);
+    code = p;
+    p = __ldcg(&nodes[p].d.z);
+  }
+}
+
+// ---- development (development.rs:59-188), batched; see fg_develop.cu for the reasoning ----
+
+__global__ void k_maxdim_b(BTile* bt, int ntiles, unsigned long long ncap, const float4* __restrict__ D) {
+  const unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+  int tile = -1;
+  float m = 0.0f;
+  if (g < ncap) {
+    tile = btile_of(bt, ntiles, g);
+    if (g - bt[tile].cbase < bt[tile].n) {
+      const float4 d = D[g];
+      m = fmaxf(fmaxf(d.x, d.y), d.z);
+    } else {
+      tile = -1;
+    }
+  }
+  const unsigned act = __activemask();
+  const unsigned grp = __match_any_sync(act, tile);
+  float mm = m;
+  for (unsigned k = grp; k; k &= k - 1) mm = fmaxf(mm, __shfl_sync(grp, m, __ffs(k) - 1));
+  if (tile >= 0 && (threadIdx.x & 31) == static_cast<unsigned>(__ffs(grp) - 1))
+    atomicMax(reinterpret_cast<unsigned long long*>(&bt[tile].max_base),
+              static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(mm))));
+}
+
+__global__ void k_threshold_b(const BTile* __restrict__ bt, int ntiles, unsigned long long ncap,
+                              const uint32_t* counts, uint8_t* developed, int* parent) {
+  const unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+  if (g >= ncap) return;
+  const BTile& t = bt[btile_of(bt, ntiles, g)];
+  const bool in = g - t.cbase < t.n;
+  developed[g] = (in && counts[g] >= t.thr) ? 1 : 0;
+  parent[g] = static_cast<int>(g);
+}
+
+__device__ __forceinline__ int uf_find_b(int* parent, int x, uint32_t* err) {
+  for (int it = 0; it < (1 << 22); ++it) {
+    const int p = __ldcg(&parent[x]);
+    if (p == x) return x;
+    const int gp = __ldcg(&parent[p]);
+    if (gp != p) atomicCAS(&parent[x], p, gp);
+    x = gp;
+  }
+  atomicOr(err, ERR_SPIN_LIMIT);
+  return x;
+}
+
+__device__ __forceinline__ void uf_unite_b(int* parent, int a, int b, uint32_t* err) {
+  for (int it = 0; it < (1 << 20); ++it) {
+    a = uf_find_b(parent, a, err);
+    b = uf_find_b(parent, b, err);
+    if (a == b) return;
+    if (a > b) { const int tmp = a; a = b; b = tmp; }
+    const int old = atomicCAS(&parent[b], b, a);
+    if (old == b) return;
+    b = old;
+  }
+  atomicOr(err, ERR_SPIN_LIMIT);
+}
+
+__global__ void k_link_b(const BTile* __restrict__ bt, int ntiles, unsigned long long ncap,
+                         const float4* __restrict__ A, const float4* __restrict__ D, const Node* __restrict__ nodes_all,
+                         const uint8_t* __restrict__ developed, int* parent, uint32_t* err) {
+  const unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+  if (g >= ncap || !developed[g]) return;
+  const BTile& t = bt[btile_of(bt, ntiles, g)];
+  const uint32_t s = static_cast<uint32_t>(g - t.cbase);
+  const Node* nodes = nodes_all + t.cbase;
+  const float4* Ab = A + t.cbase;
+  const float4* Db = D + t.cbase;
+  const uint8_t* dev = developed + t.cbase;
+  const float4 a = Ab[s], d = Db[s];
+  // Synthesized crystals are exactly their FP32 values, so the reference's FP64 expressions can
+  // be evaluated from them directly when the FP32 margin is too thin.
+  const double rc = __dmul_rn(static_cast<double>(fmaxf(fmaxf(d.x, d.y), d.z)), t.fe);
+  const double search = __dmul_rn(__dadd_rn(rc, __dmul_rn(t.max_base, t.fe)), t.prox);
+  const float R = static_cast<float>(search) * 1.0001f + 1e-3f;
+  const float3 lo = make_float3(a.x - R, a.y - R, a.z - R), hi = make_float3(a.x + R, a.y + R, a.z + R);
+  const float fef = static_cast<float>(t.fe), proxf = static_cast<float>(t.prox);
+  const float rcf = fmaxf(fmaxf(d.x, d.y), d.z) * fef;
+  int stack[64];
+  int sp = 0, cur = 0;
+  if (t.n < 2) return;
+  for (;;) {
+    const float4 na = __ldg(&nodes[cur].a), nb = __ldg(&nodes[cur].b), nc = __ldg(&nodes[cur].c);
+    const int4 nd = __ldg(&nodes[cur].d);
+    bool hl = na.x <= hi.x && na.w >= lo.x && na.y <= hi.y && nb.x >= lo.y && na.z <= hi.z && nb.y >= lo.z;
+    bool hr = nb.z <= hi.x && nc.y >= lo.x && nb.w <= hi.y && nc.z >= lo.y && nc.x <= hi.z && nc.w >= lo.z &&
+              nd.y != INT32_MIN;
+    for (int side = 0; side < 2; ++side) {
+      const bool h = side == 0 ? hl : hr;
+      const int c = side == 0 ? nd.x : nd.y;
+      if (!h || c >= 0) continue;
+      const uint32_t j = static_cast<uint32_t>(~c);
+      if (j <= s || !dev[j]) continue;
+      const float4 aj = Ab[j], dj = Db[j];
+      const float dx = aj.x - a.x, dy = aj.y - a.y, dz = aj.z - a.z;
+      const float d2 = dx * dx + dy * dy + dz * dz;
+      const float touch = (rcf + fmaxf(fmaxf(dj.x, dj.y), dj.z) * fef) * proxf;
+      const float t2 = touch * touch;
+      const float margin = 1e-5f * t2 + 1e-6f;
+      bool hit;
+      if (d2 < t2 - margin) {
+        hit = true;
+      } else if (d2 > t2 + margin) {
+        hit = false;
+      } else {
+        const double rn = __dmul_rn(static_cast<double>(fmaxf(fmaxf(dj.x, dj.y), dj.z)), t.fe);
+        const double tt = __dmul_rn(__dadd_rn(rc, rn), t.prox);
+        const double ex = __dsub_rn(static_cast<double>(aj.x), static_cast<double>(a.x));
+        const double ey = __dsub_rn(static_cast<double>(aj.y), static_cast<double>(a.y));
+        const double ez = __dsub_rn(static_cast<double>(aj.z), static_cast<double>(a.z));
+        hit = __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez)) <= __dmul_rn(tt, tt);
+      }
+      if (hit) uf_unite_b(parent, static_cast<int>(g), static_cast<int>(t.cbase + j), err);
+    }
+    if (hl && nd.x < 0) hl = false;
+    if (hr && nd.y < 0) hr = false;
+    if (hl && hr) {
+      if (sp < 64) stack[sp++] = nd.y; else atomicOr(err, ERR_STACK_OVERFLOW);
+      cur = nd.x;
+    } else if (hl) {
+      cur = nd.x;
+    } else if (hr) {
+      cur = nd.y;
+    } else {
+      if (sp == 0) break;
+      cur = stack[--sp];
+    }
+  }
+}
+
+__global__ void k_roots_b(unsigned long long ncap, const uint8_t* developed, int* parent, uint32_t* size,
+                          uint32_t* err) {
+  const unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+  if (g >= ncap || !developed[g]) return;
+  const int r = uf_find_b(parent, static_cast<int>(g), err);
+  parent[g] = r;
+  atomicAdd(&size[r], 1u);
+}
+
+__global__ void k_finalize_b(const BTile* __restrict__ bt, int ntiles, unsigned long long ncap,
+                             const uint8_t* developed, const int* parent, const uint32_t* size, double* exp64) {
+  const unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+  if (g >= ncap) return;
+  if (!developed[g]) {
+    exp64[g] = 0.0;
+    return;
+  }
+  const BTile& t = bt[btile_of(bt, ntiles, g)];
+  const uint32_t sz = size[parent[g]];
+  double e = t.fe;
+  if (sz > 1) e = __dmul_rn(t.fe, __dadd_rn(1.15, __dmul_rn(0.18, static_cast<double>((sz < 6 ? sz : 6) - 1))));
+  exp64[g] = e;
+}
+
+// ---- scan bins (per tile grid of bin_px x bin_px pixels) ----
+
+__device__ __forceinline__ void bin_span(float c, float m, float binw, uint32_t nb, uint32_t& b0, uint32_t& b1) {
+  const float lo = (c - m - 1e-3f) / binw, hi = (c + m + 1e-3f) / binw;
+  b0 = static_cast<uint32_t>(fminf(fmaxf(floorf(lo), 0.0f), static_cast<float>(nb - 1)));
+  b1 = static_cast<uint32_t>(fminf(fmaxf(floorf(hi), 0.0f), static_cast<float>(nb - 1)));
+}
+
+__global__ void k_bin_b(const BTile* __restrict__ bt, int ntiles, unsigned long long ncap, const float4* __restrict__ A,
+                        const float4* __restrict__ D, const uint8_t* __restrict__ developed,
+                        const double* __restrict__ exp64, uint32_t* cnt, const uint32_t* off, uint32_t* cursor,
+                        uint32_t* items, unsigned long long item_cap, uint32_t* err) {
+  const unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+  if (g >= ncap || !developed[g]) return;
+  const BTile& t = bt[btile_of(bt, ntiles, g)];
+  const float4 a = A[g], d = D[g];
+  const float m = fmaxf(fmaxf(d.x, d.y), d.z) * static_cast<float>(exp64[g]) * 1.0001f;
+  uint32_t x0, x1, y0, y1;
+  bin_span(a.x, m, t.binw_x, t.nbx, x0, x1);
+  bin_span(a.y, m, t.binw_y, t.nby, y0, y1);
+  const uint32_t s = static_cast<uint32_t>(g - t.cbase);
+  for (uint32_t by = y0; by <= y1; ++by)
+    for (uint32_t bx = x0; bx <= x1; ++bx) {
+      const unsigned long long b = t.bin_base + by * t.nbx + bx;
+      if (!off) {
+        atomicAdd(&cnt[b], 1u);
+      } else {
+        const unsigned long long k = off[b] + atomicAdd(&cursor[b], 1u);
+        if (k < item_cap) items[k] = s; else atomicOr(err, ERR_LIST_OVERFLOW);
+      }
+    }
+}
+
+}  // namespace fg
+
+using namespace fg;
+
+// ---------------------------------------------------------------------------------------------
+struct fg_batch {
+  fg_engine* e = nullptr;
+  uint32_t ntiles = 0;
+  std::vector<fg_tile_params> params;
+  std::vector<SynthTile> syn;
+  std::vector<TileDesc> td;
+  std::vector<ScanTile> sc;
+  std::vector<BTile> bt;
+  std::vector<unsigned long long> exp_off, out_off;
+  DBuf<SynthTile> d_syn;
+  DBuf<TileDesc> d_td;
+  DBuf<ScanTile> d_sc;
+  DBuf<BTile> d_bt;
+  DBuf<uint32_t> cells, npts, flags, slot_scan, ncrys;
+  DBuf<float4> A, Q, D;
+  DBuf<uint64_t> keys;
+  DBuf<Node> nodes;
+  DBuf<int> leaf_parent, visit, parent;
+  DBuf<uint32_t> counts, size;
+  DBuf<uint8_t> developed;
+  DBuf<double> exp64;
+  DBuf<uint32_t> bin_cnt, bin_off, bin_cur, bin_items;
+  DBuf<float> exposure, d_neg;
+  DBuf<unsigned long long> counter;
+  DBuf<unsigned long long> dstats;  // [0] transport hits, [1] scan FP64 fallbacks, [2] scan hits
+  DBuf<unsigned char> cub_tmp;
+  size_t cub_bytes = 0;
+  unsigned long long ncells = 0, nslots = 0, ncap = 0, nbins = 0, item_cap = 0, photons = 0, rays = 0;
+  unsigned long long exp_total = 0, out_total = 0;
+  int gdmax = 0;
+  unsigned cols[4] = {0, 0, 0, 0};
+  unsigned tr_blocks = 0, tr_threads = 256, scan_threads = 256;
+  uint32_t bin_px = 8;
+  bool use_graph = true;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t ev[7] = {};
+  fg_batch_stats stats{};
+
+  ~fg_batch() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (auto& x : ev)
+      if (x) cudaEventDestroy(x);
+  }
+};
+
+namespace fg {
+
+static void derive_tile(const fg_tile_params& p, SynthTile& s, TileDesc& t, ScanTile& c, BTile& b) {
+  FG_REQUIRE(p.film_w > 0 && p.film_h > 0 && p.film_d > 0, "film dimensions must be positive");
+  FG_REQUIRE(p.width_px > 0 && p.height_px > 0, "tile size must be positive");
+  FG_REQUIRE(p.r_min > 0, "r_min must be positive");
+  FG_REQUIRE(p.morphology >= 0 && p.morphology <= 2, "morphology out of range");
+  const double W = p.film_w, H = p.film_h, Dd = p.film_d, r = p.r_min;
+  const double cell = r / std::sqrt(3.0);
+  s = SynthTile{};
+  s.cell = static_cast<float>(cell);
+  s.gw = static_cast<uint32_t>(std::ceil(W / cell));
+  s.gh = static_cast<uint32_t>(std::ceil(H / cell));
+  s.gd = static_cast<uint32_t>(std::ceil(Dd / cell));
+  FG_REQUIRE(s.gw <= 16000 && s.gh <= 16000 && s.gd <= 100, "tile too large for the synthesis grid");
+  s.nbx = (s.gw + SYN_B - 1) / SYN_B;
+  s.nby = (s.gh + SYN_B - 1) / SYN_B;
+  s.XW = static_cast<uint32_t>(std::ceil(W * SYN_Q / cell));
+  s.YW = static_cast<uint32_t>(std::ceil(H * SYN_Q / cell));
+  s.ZW = static_cast<uint32_t>(std::ceil(Dd * SYN_Q / cell));
+  uint32_t bits = 0;
+  while ((1u << bits) < std::max(s.gw, s.gh)) ++bits;
+  s.slot_bits = bits;
+  s.slots = (1u << (2 * bits)) * s.gd;
+  const double vol = W * H * Dd;
+  const double cap = std::min(0.8 * vol / (r * r * r) + 64.0, static_cast<double>(s.gw) * s.gh * s.gd);
+  s.ccap = static_cast<uint32_t>(cap);
+  s.target = static_cast<uint32_t>(std::llround(bridson_density(W, H, Dd, r) * vol));
+  s.k0 = static_cast<uint32_t>(p.seed);
+  s.k1 = static_cast<uint32_t>(p.seed >> 32);
+  double mu = std::log(p.mean_crystal_radius), sg = p.size_variance;
+  if (!(sg >= 0.0) || !std::isfinite(mu) || !std::isfinite(sg)) {  // LogNormal::new fallback
+    mu = 0.0;
+    sg = 0.2;
+  }
+  s.mu = static_cast<float>(mu);
+  s.sg = static_cast<float>(sg);
+  s.rmax = static_cast<float>(r * 0.48);
+  s.base_sens = static_cast<float>(p.base_sensitivity);
+  s.aspect = static_cast<float>(p.tabular_aspect_ratio);
+  s.morph = p.morphology;
+  // Transport (seed + 1) and scan (seed + 2) as the tile worker derives them.
+  t = TileDesc{};
+  t.tw = p.width_px;
+  t.th = p.height_px;
+  t.stride = p.width_px;
+  t.W = static_cast<float>(W);
+  t.H = static_cast<float>(H);
+  t.D = static_cast<float>(Dd);
+  const double pps = p.photons_per_sq_um * std::max(p.exposure, 0.05);
+  const double P = std::round(W * H * pps);
+  FG_REQUIRE(P < 4e9, "too many photons in one tile");
+  t.P = P > 0 ? static_cast<uint32_t>(P) : 0u;
+  const uint64_t es = p.seed + 1, ss = p.seed + 2;
+  t.k0 = static_cast<uint32_t>(es);
+  t.k1 = static_cast<uint32_t>(es >> 32);
+  const fg_optics& o = p.optics;
+  const double mu_t = o.absorption_coeff + o.scattering_coeff;
+  t.mu_t = static_cast<float>(mu_t);
+  t.albedo = static_cast<float>(mu_t > 0 ? o.scattering_coeff / mu_t : 0.0);
+  t.g = static_cast<float>(o.anisotropy_g);
+  const double rr = (1.0 - o.refractive_index) / (1.0 + o.refractive_index);
+  t.r0 = static_cast<float>(rr * rr);
+  t.eff_r = static_cast<float>(o.antihalation_reflectance * std::pow(10.0, -2.0 * o.antihalation_density));
+  t.theta_max = static_cast<float>(p.illumination_angle_rad);
+  t.alpha = static_cast<float>(p.crystal_absorption_coeff);
+  t.max_bounces = p.max_bounces;
+  c = ScanTile{};
+  const uint32_t spp = std::max<uint32_t>(p.samples_per_pixel, 1);
+  const uint32_t g = static_cast<uint32_t>(std::lround(std::sqrt(static_cast<double>(spp))));
+  c.g = g;
+  c.spp = std::max<uint32_t>(g * g, 1);
+  FG_REQUIRE(c.spp <= SCAN_THREADS, "samples_per_pixel too large");
+  c.w = p.width_px;
+  c.h = p.height_px;
+  c.pw = W / p.width_px;
+  c.ph = H / p.height_px;
+  c.z0 = Dd + 0.1;
+  c.seed = ss;
+  c.sigma = static_cast<float>(p.silver_opacity);
+  c.mode = 0;
+  b = BTile{};
+  b.fe = p.filament_expansion;
+  b.prox = p.clumping_proximity_factor;
+  b.thr = p.threshold_photons;
+  b.pad = static_cast<float>(std::max(std::max(W, H), Dd) * 2e-6 + 1e-5);
+}
+
+// Places the per-tile bins for a bin edge and refreshes the scan / bin descriptors.
+static void layout_bins(fg_batch* B, uint32_t bin_px) {
+  unsigned long long base = 0;
+  for (uint32_t i = 0; i < B->ntiles; ++i) {
+    ScanTile& c = B->sc[i];
+    BTile& b = B->bt[i];
+    const uint32_t bp = std::min<uint32_t>(bin_px, scan_bin_px(c.spp));
+    c.bin_px = bp;
+    c.nbx = (c.w + bp - 1) / bp;
+    c.nby = (c.h + bp - 1) / bp;
+    c.bin_base = base;
+    b.bin_base = base;
+    b.nbx = c.nbx;
+    b.nby = c.nby;
+    b.binw_x = static_cast<float>(bp * c.pw);
+    b.binw_y = static_cast<float>(bp * c.ph);
+    base += static_cast<unsigned long long>(c.nbx) * c.nby;
+  }
+  B->nbins = base;
+  unsigned mx = 32;
+  for (uint32_t i = 0; i < B->ntiles; ++i)
+    mx = std::max(mx, ((B->sc[i].bin_px * B->sc[i].bin_px * B->sc[i].spp + 31) / 32) * 32);
+  B->scan_threads = mx;
+  B->bin_px = bin_px;
+}
+
+static void upload_descriptors(fg_batch* B, cudaStream_t st) {
+  // Device pointers inside the descriptors depend on the buffers; n stays as the device wrote it
+  // (the copy of bt/td/sc happens before the run that sets it).
+  for (uint32_t i = 0; i < B->ntiles; ++i) {
+    const unsigned long long cb = B->syn[i].cbase;
+    TileDesc& t = B->td[i];
+    t.a = B->A.p + cb;
+    t.q = B->Q.p + cb;
+    t.d = B->D.p + cb;
+    t.nodes = B->nodes.p + cb;
+    t.s2id = nullptr;
+    t.counts = B->counts.p + cb;
+    t.tile = B->exposure.p + B->exp_off[i];
+    ScanTile& c = B->sc[i];
+    c.a = B->A.p + cb;
+    c.q = B->Q.p + cb;
+    c.d = B->D.p + cb;
+    c.pos64 = c.dims64 = c.quat64 = nullptr;
+    c.developed = B->developed.p + cb;
+    c.exp64 = B->exp64.p + cb;
+    c.sigma_c = nullptr;
+    c.bin_off = B->bin_off.p + c.bin_base;
+    c.bin_items = B->bin_items.p;
+    c.out = nullptr;
+    c.image8 = nullptr;
+    c.d_neg = B->d_neg.p + B->out_off[i];
+    c.ray_hits = nullptr;
+    B->bt[i].cbase = cb;
+  }
+  FG_CUDA(cudaMemcpyAsync(B->d_syn.p, B->syn.data(), B->ntiles * sizeof(SynthTile), cudaMemcpyHostToDevice, st));
+  FG_CUDA(cudaMemcpyAsync(B->d_td.p, B->td.data(), B->ntiles * sizeof(TileDesc), cudaMemcpyHostToDevice, st));
+  FG_CUDA(cudaMemcpyAsync(B->d_sc.p, B->sc.data(), B->ntiles * sizeof(ScanTile), cudaMemcpyHostToDevice, st));
+  FG_CUDA(cudaMemcpyAsync(B->d_bt.p, B->bt.data(), B->ntiles * sizeof(BTile), cudaMemcpyHostToDevice, st));
+}
+
+static void cub_scan(fg_batch* B, const uint32_t* in, uint32_t* out, unsigned long long n, cudaStream_t st) {
+  size_t bytes = B->cub_bytes;
+  FG_CUDA(cub::DeviceScan::ExclusiveSum(B->cub_tmp.p, bytes, in, out, static_cast<int64_t>(n), st));
+}
+
+// Stages; each only enqueues work on `st`.
+static void stage_synth(fg_batch* B, cudaStream_t st) {
+  fg_engine* e = B->e;
+  const int nt = static_cast<int>(B->ntiles);
+  FG_CUDA(cudaMemsetAsync(B->dstats.p, 0, 4 * sizeof(unsigned long long), st));
+  FG_CUDA(cudaMemsetAsync(B->cells.p, 0, B->ncells * sizeof(uint32_t), st));
+  FG_CUDA(cudaMemsetAsync(B->npts.p, 0, B->ntiles * sizeof(uint32_t), st));
+  for (int c = 0; c < 4; ++c) launch_bridson(B->d_syn.p, nt, c, B->cols[c], B->gdmax, B->cells.p, e->d_err, st);
+  FG_CUDA(cudaMemsetAsync(B->flags.p + B->nslots, 0, sizeof(uint32_t), st));
+  launch_synth_post(B->d_syn.p, nt, B->ncells, B->nslots, B->cells.p, B->npts.p, B->flags.p, st);
+  cub_scan(B, B->flags.p, B->slot_scan.p, B->nslots + 1, st);
+  launch_emit(B->d_syn.p, nt, B->nslots, B->cells.p, B->slot_scan.p, B->A.p, B->Q.p, B->D.p, B->keys.p, e->d_err, st);
+  k_set_n<<<grid_for(B->ntiles, 128), 128, 0, st>>>(B->d_syn.p, nt, B->slot_scan.p, B->d_bt.p, B->d_td.p, B->d_sc.p,
+                                                    B->ncrys.p);
+  FG_CUDA(cudaGetLastError());
+}
+
+static void stage_bvh(fg_batch* B, cudaStream_t st) {
+  const int nt = static_cast<int>(B->ntiles);
+  FG_CUDA(cudaMemsetAsync(B->visit.p, 0, B->ncap * sizeof(int), st));
+  k_karras_b<<<grid_for(B->ncap, 256), 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->keys.p, B->nodes.p, B->leaf_parent.p,
+                                                     B->visit.p);
+  k_fit_b<<<grid_for(B->ncap, 256), 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->A.p, B->Q.p, B->D.p, B->nodes.p,
+                                                  B->leaf_parent.p, B->visit.p);
+  FG_CUDA(cudaGetLastError());
+}
+
+static void stage_transport(fg_batch* B, cudaStream_t st) {
+  FG_CUDA(cudaMemsetAsync(B->counts.p, 0, B->ncap * sizeof(uint32_t), st));
+  launch_transport_shape(B->d_td.p, static_cast<int>(B->ntiles), B->photons, B->counter.p, B->e->d_err,
+                         B->dstats.p, B->tr_blocks, B->tr_threads, st);
+}
+
+static void stage_develop(fg_batch* B, cudaStream_t st) {
+  const int nt = static_cast<int>(B->ntiles);
+  fg_engine* e = B->e;
+  const unsigned G = grid_for(B->ncap, 256);
+  k_maxdim_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->D.p);
+  k_threshold_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->counts.p, B->developed.p, B->parent.p);
+  k_link_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->A.p, B->D.p, B->nodes.p, B->developed.p, B->parent.p,
+                              e->d_err);
+  FG_CUDA(cudaMemsetAsync(B->size.p, 0, B->ncap * sizeof(uint32_t), st));
+  k_roots_b<<<G, 256, 0, st>>>(B->ncap, B->developed.p, B->parent.p, B->size.p, e->d_err);
+  k_finalize_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->developed.p, B->parent.p, B->size.p, B->exp64.p);
+  FG_CUDA(cudaGetLastError());
+}
+
+static void stage_scan(fg_batch* B, cudaStream_t st) {
+  const int nt = static_cast<int>(B->ntiles);
+  fg_engine* e = B->e;
+  const unsigned G = grid_for(B->ncap, 256);
+  FG_CUDA(cudaMemsetAsync(B->bin_cnt.p, 0, (B->nbins + 1) * sizeof(uint32_t), st));
+  FG_CUDA(cudaMemsetAsync(B->bin_cur.p, 0, (B->nbins + 1) * sizeof(uint32_t), st));
+  k_bin_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->A.p, B->D.p, B->developed.p, B->exp64.p, B->bin_cnt.p, nullptr,
+                             nullptr, nullptr, 0, e->d_err);
+  cub_scan(B, B->bin_cnt.p, B->bin_off.p, B->nbins + 1, st);
+  k_bin_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->A.p, B->D.p, B->developed.p, B->exp64.p, nullptr,
+                             B->bin_off.p, B->bin_cur.p, B->bin_items.p, B->item_cap, e->d_err);
+  FG_CUDA(cudaGetLastError());
+  launch_scan(B->d_sc.p, nt, B->nbins, B->scan_threads, e->d_err, B->dstats.p, st);
+}
+
+// Stage events: inside a graph capture they must be external records so that every replay
+// records them again (a plain record would become an internal dependency only).
+static void mark(cudaEvent_t ev, cudaStream_t st, bool capturing) {
+  FG_CUDA(cudaEventRecordWithFlags(ev, st, capturing ? cudaEventRecordExternal : cudaEventRecordDefault));
+}
+
+static void enqueue_all(fg_batch* B, cudaStream_t st, bool capturing = false) {
+  mark(B->ev[0], st, capturing);
+  stage_synth(B, st);
+  mark(B->ev[1], st, capturing);
+  stage_bvh(B, st);
+  mark(B->ev[2], st, capturing);
+  stage_transport(B, st);
+  mark(B->ev[3], st, capturing);
+  stage_develop(B, st);
+  mark(B->ev[4], st, capturing);
+  stage_scan(B, st);
+  mark(B->ev[5], st, capturing);
+}
+
+static float ev_ms(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0;
+  FG_CUDA(cudaEventElapsedTime(&ms, a, b));
+  return ms;
+}
+
+// Picks the transport launch shape and the scan bin edge by timing candidates on this batch.
+static void autotune(fg_batch* B, cudaStream_t st) {
+  fg_engine* e = B->e;
+  enqueue_all(B, st);  // warm-up; leaves a developed emulsion for the scan trials
+  FG_CUDA(cudaStreamSynchronize(st));
+  check_error_word(e);
+  float best = 1e30f;
+  unsigned bb = B->tr_blocks, bt_ = B->tr_threads;
+  for (unsigned threads : {128u, 256u}) {
+    for (unsigned per_sm : {2u, 4u, 8u, 16u}) {
+      const unsigned blocks = static_cast<unsigned>(e->sm_count) * per_sm * 256u / threads;
+      B->tr_blocks = blocks;
+      B->tr_threads = threads;
+      FG_CUDA(cudaEventRecord(B->ev[2], st));
+      stage_transport(B, st);
+      FG_CUDA(cudaEventRecord(B->ev[3], st));
+      FG_CUDA(cudaStreamSynchronize(st));
+      const float ms = ev_ms(B->ev[2], B->ev[3]);
+      if (ms < best) {
+        best = ms;
+        bb = blocks;
+        bt_ = threads;
+      }
+    }
+  }
+  B->tr_blocks = bb;
+  B->tr_threads = bt_;
+  // Recreate the transport result of the chosen shape (counts are identical for every shape).
+  stage_transport(B, st);
+  stage_develop(B, st);
+  best = 1e30f;
+  uint32_t bp_best = B->bin_px;
+  for (uint32_t bp : {4u, 8u}) {
+    layout_bins(B, bp);
+    upload_descriptors(B, st);
+    FG_CUDA(cudaEventRecord(B->ev[4], st));
+    stage_scan(B, st);
+    FG_CUDA(cudaEventRecord(B->ev[5], st));
+    FG_CUDA(cudaStreamSynchronize(st));
+    const float ms = ev_ms(B->ev[4], B->ev[5]);
+    if (ms < best) {
+      best = ms;
+      bp_best = bp;
+    }
+  }
+  layout_bins(B, bp_best);
+  upload_descriptors(B, st);
+  FG_CUDA(cudaStreamSynchronize(st));
+  check_error_word(e);
+}
+
+static void plan(fg_batch* B, const fg_batch_options* opt) {
+  fg_engine* e = B->e;
+  cudaStream_t st = e->stream;
+  (void)cudaGetLastError();  // start from a clean runtime error state (library queries check it)
+  const uint32_t n = B->ntiles;
+  B->syn.resize(n);
+  B->td.resize(n);
+  B->sc.resize(n);
+  B->bt.resize(n);
+  B->exp_off.resize(n);
+  B->out_off.resize(n);
+  unsigned long long cb = 0, sb = 0, cap = 0, pb = 0, eo = 0, oo = 0;
+  unsigned colc[4] = {0, 0, 0, 0};
+  for (uint32_t i = 0; i < n; ++i) {
+    derive_tile(B->params[i], B->syn[i], B->td[i], B->sc[i], B->bt[i]);
+    SynthTile& s = B->syn[i];
+    s.cell_base = cb;
+    s.slot_base = sb;
+    s.cbase = cap;
+    for (int c = 0; c < 4; ++c) {
+      s.col_base[c] = colc[c];
+      const uint32_t cxn = (s.nbx + 1 - (c & 1)) / 2, cyn = (s.nby + 1 - (c >> 1)) / 2;
+      colc[c] += cxn * cyn;
+    }
+    cb += static_cast<unsigned long long>(s.gw) * s.gh * s.gd;
+    sb += s.slots;
+    cap += s.ccap;
+    B->td[i].photon_base = pb;
+    pb += B->td[i].P;
+    B->exp_off[i] = eo;
+    eo += static_cast<unsigned long long>(B->params[i].width_px) * B->params[i].height_px;
+    B->out_off[i] = oo;
+    oo += static_cast<unsigned long long>(B->params[i].width_px) * B->params[i].height_px;
+    B->gdmax = std::max<int>(B->gdmax, static_cast<int>(s.gd));
+    B->rays += static_cast<unsigned long long>(B->sc[i].w) * B->sc[i].h * B->sc[i].spp;
+  }
+  for (int c = 0; c < 4; ++c) B->cols[c] = colc[c];
+  FG_REQUIRE(cap < 0x7fffffffull, "batch too large: more than 2^31 crystal slots");
+  FG_REQUIRE(bridson_smem(B->gdmax) <= 220 * 1024, "emulsion too deep for the synthesis column");
+  B->ncells = cb;
+  B->nslots = sb;
+  B->ncap = cap;
+  B->photons = pb;
+  B->exp_total = eo;
+  B->out_total = oo;
+  B->tr_threads = opt && opt->transport_threads ? opt->transport_threads : 256;
+  B->tr_blocks = opt && opt->transport_blocks ? opt->transport_blocks : static_cast<unsigned>(e->sm_count) * 8;
+  const uint32_t bin0 = opt && opt->scan_bin_px ? opt->scan_bin_px : 8;
+  B->use_graph = !opt || opt->use_graph;
+  // Buffers (bins sized for the smallest bin edge the tuner tries).
+  layout_bins(B, 4);
+  const unsigned long long nbins_max = B->nbins;
+  B->d_syn.alloc(n, st);
+  B->d_td.alloc(n, st);
+  B->d_sc.alloc(n, st);
+  B->d_bt.alloc(n, st);
+  B->cells.alloc(std::max<unsigned long long>(cb, 1), st);
+  B->npts.alloc(n, st);
+  B->ncrys.alloc(n, st);
+  B->flags.alloc(sb + 1, st);
+  B->slot_scan.alloc(sb + 1, st);
+  B->A.alloc(std::max<unsigned long long>(cap, 1), st);
+  B->Q.alloc(std::max<unsigned long long>(cap, 1), st);
+  B->D.alloc(std::max<unsigned long long>(cap, 1), st);
+  B->keys.alloc(std::max<unsigned long long>(cap, 1), st);
+  B->nodes.alloc(std::max<unsigned long long>(cap, 1), st);
+  B->leaf_parent.alloc(std::max<unsigned long long>(cap, 1), st);
+  B->visit.alloc(std::max<unsigned long long>(cap, 1), st);
+  B->parent.alloc(std::max<unsigned long long>(cap, 1), st);
+  B->counts.alloc(std::max<unsigned long long>(cap, 1), st);
+  B->size.alloc(std::max<unsigned long long>(cap, 1), st);
+  B->developed.alloc(std::max<unsigned long long>(cap, 1), st);
+  B->exp64.alloc(std::max<unsigned long long>(cap, 1), st);
+  B->bin_cnt.alloc(nbins_max + 1, st);
+  B->bin_off.alloc(nbins_max + 1, st);
+  B->bin_cur.alloc(nbins_max + 1, st);
+  B->item_cap = std::max<unsigned long long>(cap * 6, 1);
+  B->bin_items.alloc(B->item_cap, st);
+  B->exposure.alloc(std::max<unsigned long long>(eo, 1), st);
+  B->d_neg.alloc(std::max<unsigned long long>(oo, 1), st);
+  B->counter.alloc(1, st);
+  B->dstats.alloc(4, st);
+  FG_CUDA(cudaMemsetAsync(B->exposure.p, 0, B->exposure.n * sizeof(float), st));
+  size_t b1 = 0, b2 = 0;
+  FG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, b1, B->flags.p, B->slot_scan.p, static_cast<int64_t>(sb + 1), st));
+  FG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, b2, B->bin_cnt.p, B->bin_off.p, static_cast<int64_t>(nbins_max + 1), st));
+  B->cub_bytes = std::max(b1, b2);
+  B->cub_tmp.alloc(std::max<size_t>(B->cub_bytes, 1), st);
+  for (auto& x : B->ev) FG_CUDA(cudaEventCreate(&x));
+  layout_bins(B, bin0);
+  upload_descriptors(B, st);
+  FG_CUDA(cudaStreamSynchronize(st));
+}
+
+static void capture(fg_batch* B) {
+  cudaStream_t st = B->e->stream;
+  FG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  try {
+    enqueue_all(B, st, true);
+  } catch (...) {
+    cudaGraph_t g = nullptr;
+    cudaStreamEndCapture(st, &g);
+    if (g) cudaGraphDestroy(g);
+    throw;
+  }
+  FG_CUDA(cudaStreamEndCapture(st, &B->graph));
+  FG_CUDA(cudaGraphInstantiate(&B->exec, B->graph, 0));
+}
+
+}  // namespace fg
+
+extern "C" {
+
+fg_status fg_tile_params_preset(const char* preset, double pixel_size_um, uint32_t tw, uint32_t th,
+                                double exposure, double push, uint64_t tile_seed, fg_tile_params* out) {
+  if (!preset || !out || !(pixel_size_um > 0) || tw == 0 || th == 0) return FG_ERR_INVALID_ARG;
+  std::string s(preset);
+  for (auto& ch : s) ch = static_cast<char>(std::tolower(static_cast<unsigned char>(ch)));
+  const bool is1600 = s.find("1600") != std::string::npos || s == "caffenol";
+  const double eff_push = is1600 ? std::max(push, 2.0) : std::max(push, 0.0);  // image_pipeline.rs:369-375
+  // Emulsion stock of the tile worker (image_pipeline.rs:925-938): tri-x at push >= 1.5 uses 1600.
+  std::string stock;
+  if (s == "t-max" || s == "tmax") stock = "t-max";
+  else if (s == "hp5" || s == "hp5-plus") stock = "hp5";
+  else if (is1600) stock = "tri-x-1600";
+  else stock = eff_push >= 1.5 ? "tri-x-1600" : "tri-x";
+  fg_emulsion_cfg ec;
+  const fg_status st = fg_emulsion_preset(stock.c_str(), tw * pixel_size_um, th * pixel_size_um, &ec);
+  if (st != FG_OK) return st;
+  *out = fg_tile_params{};
+  out->film_w = ec.width;
+  out->film_h = ec.height;
+  out->film_d = ec.depth;
+  out->width_px = tw;
+  out->height_px = th;
+  out->samples_per_pixel = 4;       // render_tile_cpu_density, image_pipeline.rs:996-1002
+  out->threshold_photons = 4;       // image_pipeline.rs:964
+  out->silver_opacity = 0.25;
+  out->seed = tile_seed;
+  out->r_min = ec.r_min;
+  out->mean_crystal_radius = ec.mean_crystal_radius;
+  out->size_variance = ec.size_variance;
+  out->morphology = ec.morphology;
+  out->tabular_aspect_ratio = ec.tabular_aspect_ratio;
+  out->base_sensitivity = ec.base_sensitivity;
+  out->exposure = exposure;
+  if (s == "t-max" || s == "tmax") {
+    out->filament_expansion = 1.10 + 0.04 * eff_push;
+    out->clumping_proximity_factor = 1.10 + 0.03 * eff_push;
+  } else if (s == "hp5" || s == "hp5-plus") {
+    out->filament_expansion = 1.15 + 0.05 * eff_push;
+    out->clumping_proximity_factor = 1.18 + 0.04 * eff_push;
+  } else {
+    out->filament_expansion = 1.20 + 0.06 * eff_push;
+    out->clumping_proximity_factor = 1.25 + 0.05 * eff_push;
+  }
+  out->optics = ec.optics;
+  out->photons_per_sq_um = 6.0;     // image_pipeline.rs:943
+  out->illumination_angle_rad = 0.12;
+  out->crystal_absorption_coeff = 1.3;
+  out->max_bounces = 48;
+  return FG_OK;
+}
+
+fg_status fg_batch_create(fg_engine* e, const fg_tile_params* tiles, uint32_t ntiles,
+                          const fg_batch_options* opt, fg_batch** out) {
+  if (!out) return FG_ERR_INVALID_ARG;
+  *out = nullptr;
+  return guard(e, [&] {
+    FG_REQUIRE(tiles && ntiles > 0, "no tiles");
+    std::unique_ptr<fg_batch> B(new fg_batch());
+    B->e = e;
+    B->ntiles = ntiles;
+    B->params.assign(tiles, tiles + ntiles);
+    plan(B.get(), opt);
+    if (opt && opt->autotune) autotune(B.get(), e->stream);
+    if (B->use_graph) capture(B.get());
+    *out = B.release();
+  });
+}
+
+fg_status fg_batch_destroy(fg_batch* b) {
+  if (!b) return FG_ERR_INVALID_ARG;
+  fg_engine* e = b->e;
+  return guard(e, [&] {
+    FG_CUDA(cudaStreamSynchronize(e->stream));
+    delete b;
+    FG_CUDA(cudaStreamSynchronize(e->stream));
+  });
+}
+
+fg_status fg_batch_set_exposure(fg_batch* b, const float* const* tiles) {
+  if (!b) return FG_ERR_INVALID_ARG;
+  return guard(b->e, [&] {
+    FG_REQUIRE(tiles, "null tile list");
+    for (uint32_t i = 0; i < b->ntiles; ++i) {
+      FG_REQUIRE(tiles[i], "null exposure tile");
+      const size_t n = static_cast<size_t>(b->params[i].width_px) * b->params[i].height_px;
+      FG_CUDA(cudaMemcpyAsync(b->exposure.p + b->exp_off[i], tiles[i], n * sizeof(float), cudaMemcpyHostToDevice,
+                              b->e->stream));
+    }
+  });
+}
+
+fg_status fg_batch_exposure_device(fg_batch* b, uint32_t tile, float** ptr) {
+  if (!b || !ptr || tile >= b->ntiles) return FG_ERR_INVALID_ARG;
+  *ptr = b->exposure.p + b->exp_off[tile];
+  return FG_OK;
+}
+
+fg_status fg_batch_density_device(fg_batch* b, uint32_t tile, const float** ptr) {
+  if (!b || !ptr || tile >= b->ntiles) return FG_ERR_INVALID_ARG;
+  *ptr = b->d_neg.p + b->out_off[tile];
+  return FG_OK;
+}
+
+fg_status fg_batch_run(fg_batch* b) {
+  if (!b) return FG_ERR_INVALID_ARG;
+  return guard(b->e, [&] {
+    cudaStream_t st = b->e->stream;
+    if (b->exec) {
+      FG_CUDA(cudaGraphLaunch(b->exec, st));
+    } else {
+      enqueue_all(b, st);
+    }
+  });
+}
+
+fg_status fg_batch_wait(fg_batch* b, fg_batch_stats* stats) {
+  if (!b) return FG_ERR_INVALID_ARG;
+  return guard(b->e, [&] {
+    cudaStream_t st = b->e->stream;
+    FG_CUDA(cudaStreamSynchronize(st));
+    check_error_word(b->e);
+    fg_batch_stats s{};
+    s.synth_ms = ev_ms(b->ev[0], b->ev[1]);
+    s.bvh_ms = ev_ms(b->ev[1], b->ev[2]);
+    s.transport_ms = ev_ms(b->ev[2], b->ev[3]);
+    s.develop_ms = ev_ms(b->ev[3], b->ev[4]);
+    s.scan_ms = ev_ms(b->ev[4], b->ev[5]);
+    s.total_ms = ev_ms(b->ev[0], b->ev[5]);
+    std::vector<uint32_t> nc(b->ntiles);
+    FG_CUDA(cudaMemcpy(nc.data(), b->ncrys.p, b->ntiles * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    for (uint32_t v : nc) s.crystals += v;
+    s.photons = b->photons;
+    unsigned long long ds[4];
+    FG_CUDA(cudaMemcpy(ds, b->dstats.p, sizeof(ds), cudaMemcpyDeviceToHost));
+    s.hits = ds[0];
+    s.scan_fallbacks = ds[1];
+    s.scan_hits = ds[2];
+    s.rays = b->rays;
+    s.pixels = b->out_total;
+    s.transport_threads = b->tr_threads;
+    s.transport_blocks = b->tr_blocks;
+    s.scan_bin_px = b->bin_px;
+    s.graph = b->exec ? 1u : 0u;
+    // Own kernels per run: Bridson x4, count + thin + flags, emit, set_n, Karras + fit, transport,
+    // maxdim + threshold + link + roots + finalize, two bin passes, scan (CUB scans not counted).
+    s.kernel_launches = 4 + 3 + 1 + 1 + 2 + 1 + 5 + 2 + 1;
+    b->stats = s;
+    if (stats) *stats = s;
+  });
+}
+
+fg_status fg_batch_get_density(fg_batch* b, float* const* outs) {
+  if (!b) return FG_ERR_INVALID_ARG;
+  return guard(b->e, [&] {
+    FG_REQUIRE(outs, "null output list");
+    for (uint32_t i = 0; i < b->ntiles; ++i) {
+      FG_REQUIRE(outs[i], "null output tile");
+      const size_t n = static_cast<size_t>(b->params[i].width_px) * b->params[i].height_px;
+      FG_CUDA(cudaMemcpyAsync(outs[i], b->d_neg.p + b->out_off[i], n * sizeof(float), cudaMemcpyDeviceToHost,
+                              b->e->stream));
+    }
+    FG_CUDA(cudaStreamSynchronize(b->e->stream));
+  });
+}
+
+fg_status fg_batch_tile_crystals(fg_batch* b, uint32_t tile, fg_crystals_out* out, uint32_t* counts,
+                                 uint8_t* developed, double* expansion, size_t cap, size_t* n) {
+  if (!b || tile >= b->ntiles || !n) return FG_ERR_INVALID_ARG;
+  return guard(b->e, [&] {
+    cudaStream_t st = b->e->stream;
+    uint32_t nc = 0;
+    FG_CUDA(cudaMemcpyAsync(&nc, b->ncrys.p + tile, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    FG_CUDA(cudaStreamSynchronize(st));
+    *n = nc;
+    const size_t k = std::min<size_t>(nc, cap);
+    if (!k) return;
+    const unsigned long long cb = b->syn[tile].cbase;
+    std::vector<float4> A(k), Q(k), D(k);
+    FG_CUDA(cudaMemcpyAsync(A.data(), b->A.p + cb, k * sizeof(float4), cudaMemcpyDeviceToHost, st));
+    FG_CUDA(cudaMemcpyAsync(Q.data(), b->Q.p + cb, k * sizeof(float4), cudaMemcpyDeviceToHost, st));
+    FG_CUDA(cudaMemcpyAsync(D.data(), b->D.p + cb, k * sizeof(float4), cudaMemcpyDeviceToHost, st));
+    if (counts) FG_CUDA(cudaMemcpyAsync(counts, b->counts.p + cb, k * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    if (developed) FG_CUDA(cudaMemcpyAsync(developed, b->developed.p + cb, k, cudaMemcpyDeviceToHost, st));
+    if (expansion) FG_CUDA(cudaMemcpyAsync(expansion, b->exp64.p + cb, k * sizeof(double), cudaMemcpyDeviceToHost, st));
+    FG_CUDA(cudaStreamSynchronize(st));
+    for (size_t i = 0; i < k; ++i) {
+      if (out && out->pos) { out->pos[3 * i] = A[i].x; out->pos[3 * i + 1] = A[i].y; out->pos[3 * i + 2] = A[i].z; }
+      if (out && out->dims) { out->dims[3 * i] = D[i].x; out->dims[3 * i + 1] = D[i].y; out->dims[3 * i + 2] = D[i].z; }
+      if (out && out->quat) { out->quat[4 * i] = Q[i].x; out->quat[4 * i + 1] = Q[i].y; out->quat[4 * i + 2] = Q[i].z; out->quat[4 * i + 3] = Q[i].w; }
+      if (out && out->sensitivity) out->sensitivity[i] = A[i].w;
+      if (out && out->morphology) { int32_t m; std::memcpy(&m, &D[i].w, 4); out->morphology[i] = m; }
+    }
+  });
+}
+
+fg_status fg_batch_time(fg_batch* b, uint32_t steps, double* ms) {
+  if (!b || !ms || steps == 0) return FG_ERR_INVALID_ARG;
+  return guard(b->e, [&] {
+    cudaStream_t st = b->e->stream;
+    FG_CUDA(cudaStreamSynchronize(st));
+    FG_CUDA(cudaEventRecord(b->ev[6], st));
+    for (uint32_t i = 0; i < steps; ++i) {
+      if (b->exec) {
+        FG_CUDA(cudaGraphLaunch(b->exec, st));
+      } else {
+        enqueue_all(b, st);
+      }
+    }
+    FG_CUDA(cudaEventRecord(b->ev[5], st));
+    FG_CUDA(cudaStreamSynchronize(st));
+    check_error_word(b->e);
+    *ms = ev_ms(b->ev[6], b->ev[5]);
+  });
+}
+
+fg_status fg_host_alloc(size_t bytes, void** ptr) {
+  if (!ptr) return FG_ERR_INVALID_ARG;
+  *ptr = nullptr;
+  if (cudaMallocHost(ptr, bytes ? bytes : 1) != cudaSuccess) return FG_ERR_OOM;
+  return FG_OK;
+}
+
+fg_status fg_host_free(void* ptr) {
+  if (ptr && cudaFreeHost(ptr) != cudaSuccess) return FG_ERR_INVALID_ARG;
+  return FG_OK;
+}
+
+fg_status fg_render_batch(fg_engine* e, const fg_tile_params* tiles, uint32_t ntiles, const float* const* exposure,
+                          float* const* d_neg) {
+  fg_batch* b = nullptr;
+  fg_batch_options opt{};
+  opt.use_graph = 0;
+  fg_status s = fg_batch_create(e, tiles, ntiles, &opt, &b);
+  if (s != FG_OK) return s;
+  s = fg_batch_set_exposure(b, exposure);
+  if (s == FG_OK) s = fg_batch_run(b);
+  if (s == FG_OK) s = fg_batch_wait(b, nullptr);
+  if (s == FG_OK) s = fg_batch_get_density(b, d_neg);
+  const fg_status d = fg_batch_destroy(b);
+  return s != FG_OK ? s : d;
+}
+
+fg_status fg_render_tile(fg_engine* e, const float* tile, const fg_tile_params* p, float* d_neg) {
+  if (!p || !tile || !d_neg) return FG_ERR_INVALID_ARG;
+  return fg_render_batch(e, p, 1, &tile, &d_neg);
+}
+
+}  // extern "C"

@@ -33,27 +33,6 @@ void check_error_word(fg_engine* e) {
   throw Error{FG_ERR_DEVICE_OVERFLOW, m};
 }
 
-// Runs f under the engine lock with the device current; converts failures to a status.
-template <class F>
-fg_status guard(fg_engine* e, F&& f) {
-  if (!e) return FG_ERR_INVALID_ARG;
-  std::lock_guard<std::recursive_mutex> lk(e->mu);
-  try {
-    FG_CUDA(cudaSetDevice(e->device));
-    f();
-    return FG_OK;
-  } catch (const Error& x) {
-    e->err = x.msg;
-    return x.st;
-  } catch (const std::bad_alloc&) {
-    e->err = "host allocation failed";
-    return FG_ERR_OOM;
-  } catch (const std::exception& x) {
-    e->err = x.what();
-    return FG_ERR_PIPELINE;
-  }
-}
-
 // Starts a call: zeroes the per-call timings and device counters.
 void begin_call(fg_engine* e) {
   e->timings = fg_timings{};

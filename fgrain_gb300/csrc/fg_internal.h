@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 
 #include <mutex>
+#include <new>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -175,6 +177,27 @@ void exclusive_scan_u32(const uint32_t* in, uint32_t* out, size_t n, cudaStream_
 
 // Raises an Error when a kernel reported one through the engine's error word.
 void check_error_word(fg_engine* e);
+
+// Runs f under the engine lock with the device current; converts failures to a status.
+template <class F>
+fg_status guard(fg_engine* e, F&& f) {
+  if (!e) return FG_ERR_INVALID_ARG;
+  std::lock_guard<std::recursive_mutex> lk(e->mu);
+  try {
+    FG_CUDA(cudaSetDevice(e->device));
+    f();
+    return FG_OK;
+  } catch (const Error& x) {
+    e->err = x.msg;
+    return x.st;
+  } catch (const std::bad_alloc&) {
+    e->err = "host allocation failed";
+    return FG_ERR_OOM;
+  } catch (const std::exception& x) {
+    e->err = x.what();
+    return FG_ERR_PIPELINE;
+  }
+}
 
 inline unsigned grid_for(size_t n, unsigned block) {
   return static_cast<unsigned>((n + block - 1) / block);

@@ -173,10 +173,15 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const ScanTile* __restric
   const uint32_t px = bx * t.bin_px + lx, py = by * t.bin_px + ly;
   const bool active = pix < t.bin_px * t.bin_px && px < t.w && py < t.h;
   const uint32_t sx = st % t.g, sy = st / t.g;
-  const double bx0 = __dmul_rn(static_cast<double>(bx * t.bin_px), t.pw);
-  const double by0 = __dmul_rn(static_cast<double>(by * t.bin_px), t.ph);
-  // Ray position relative to the bin corner as a float pair.  The offset in units of the
-  // 24-bit jitter is an exact integer X = (l g + s) 2^24 + u, so x = X * pw / (g 2^24).
+  // Coordinates are taken relative to the corner of the 16-pixel square holding this bin, not to
+  // the bin itself, so that every bin edge rounds identically and results do not depend on the
+  // launch shape.
+  const uint32_t ox_px = (bx * t.bin_px) & ~15u, oy_px = (by * t.bin_px) & ~15u;
+  const double bx0 = __dmul_rn(static_cast<double>(ox_px), t.pw);
+  const double by0 = __dmul_rn(static_cast<double>(oy_px), t.ph);
+  const uint32_t rlx = px - ox_px, rly = py - oy_px;  // < 16 + bin_px
+  // Ray position relative to that corner as a float pair.  The offset in units of the 24-bit
+  // jitter is an exact integer X = (l g + s) 2^24 + u, so x = X * pw / (g 2^24).
   float oxh = 0.0f, oxl = 0.0f, oyh = 0.0f, oyl = 0.0f;
   if (active) {
     const uint64_t ps = t.seed + static_cast<uint64_t>(px) * 0x9E3779B97F4A7C15ull +
@@ -186,8 +191,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const ScanTile* __restric
     float cxh, cxl, cyh, cyl;
     split64(t.pw * scale, cxh, cxl);
     split64(t.ph * scale, cyh, cyl);
-    const uint32_t X = ((lx * t.g + sx) << 24) + (r.x >> 8);
-    const uint32_t Y = ((ly * t.g + sy) << 24) + (r.y >> 8);
+    const uint32_t X = ((rlx * t.g + sx) << 24) + (r.x >> 8);
+    const uint32_t Y = ((rly * t.g + sy) << 24) + (r.y >> 8);
     const float Xh = static_cast<float>(X), Yh = static_cast<float>(Y);
     const float Xl = static_cast<float>(static_cast<long long>(X) - static_cast<long long>(Xh));
     const float Yl = static_cast<float>(static_cast<long long>(Y) - static_cast<long long>(Yh));
@@ -348,6 +353,13 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const ScanTile* __restric
       if (hsum) atomicAdd(&stats[2], hsum);
     }
   }
+}
+
+void launch_scan(const ScanTile* tiles, int ntiles, unsigned long long nbins, unsigned threads, uint32_t* err,
+                 unsigned long long* stats, cudaStream_t st) {
+  if (nbins == 0) return;
+  k_scan<<<static_cast<unsigned>(nbins), threads, 0, st>>>(tiles, ntiles, err, stats);
+  FG_CUDA(cudaGetLastError());
 }
 
 // Chooses the bin edge so one CTA holds bin_px^2 pixels of `spp` strata.

@@ -77,7 +77,7 @@ __device__ __forceinline__ Crystal64 load64_parts(const ScanTile& t, uint32_t s)
 }
 
 // Exact FP64 chord of a vertical scan ray through crystal s (0 when it misses).
-__device__ __noinline__ double scan_chord64(const ScanTile& t, uint32_t s, double ox, double oy,
+static __device__ __noinline__ double scan_chord64(const ScanTile& t, uint32_t s, double ox, double oy,
                                             bool& hit) {
   const Crystal64 k = load64_parts(t, s);
   const double e = t.exp64[s];

@@ -1,0 +1,373 @@
+// Device crystal synthesis: column-parallel Bridson, thinning to the reference density, Morton
+// compaction and crystal attributes.  See fg_synth.cuh for the scheme.
+#include "fg_internal.h"
+#include "fg_synth.cuh"
+
+namespace fg {
+
+enum : uint32_t {
+  TAG_PICK = 0x50490000u,
+  TAG_CAND = 0x43410000u,
+  TAG_SEED = 0x53450000u,
+  TAG_THIN = 0x54480000u,
+};
+
+__device__ __forceinline__ int find_tile_ull(const SynthTile* tiles, int ntiles, unsigned long long v,
+                                             int which) {
+  int lo = 0, hi = ntiles - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    const unsigned long long b = which == 0 ? tiles[mid].cell_base : (which == 1 ? tiles[mid].slot_base : tiles[mid].cbase);
+    if (b <= v) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Exact test of a fixed-point candidate against the staged grid (5x5x5 cells, corners skipped:
+// their nearest point is sqrt(3) cells = r away or more).
+__device__ __forceinline__ bool syn_free(const uint32_t* grid, int rx, int ry, int rz, int X, int Y,
+                                         int Z, int cx, int cy, int cz) {
+#pragma unroll 1
+  for (int dz = -2; dz <= 2; ++dz)
+#pragma unroll
+    for (int dy = -2; dy <= 2; ++dy)
+#pragma unroll
+      for (int dx = -2; dx <= 2; ++dx) {
+        if ((dx == -2 || dx == 2) && (dy == -2 || dy == 2) && (dz == -2 || dz == 2)) continue;
+        const uint32_t w = grid[((rz + dz) * SYN_R + (ry + dy)) * SYN_R + (rx + dx)];
+        if (w & OCC) {
+          const int ex = (cx + dx) * SYN_Q + static_cast<int>(w & 1023u) - X;
+          const int ey = (cy + dy) * SYN_Q + static_cast<int>((w >> 10) & 1023u) - Y;
+          const int ez = (cz + dz) * SYN_Q + static_cast<int>((w >> 20) & 1023u) - Z;
+          if (ex * ex + ey * ey + ez * ez < SYN_R2) return false;
+        }
+      }
+  return true;
+}
+
+__global__ void __launch_bounds__(SYN_WARPS * 32) k_bridson(const SynthTile* __restrict__ tiles,
+                                                            int ntiles, int color, int nz,
+                                                            uint32_t* __restrict__ cells,
+                                                            uint32_t* err) {
+  extern __shared__ uint32_t syn_sm[];
+  uint32_t* grid = syn_sm;                                             // SYN_R^2 * nz
+  uint16_t* active = reinterpret_cast<uint16_t*>(grid + SYN_R * SYN_R * nz);  // SYN_B^2 * (nz-4)
+  __shared__ int s_nact, s_nrem, s_wsum[SYN_WARPS];
+  __shared__ int s_pick[SYN_WARPS];
+  __shared__ unsigned s_vmask[SYN_WARPS];
+  __shared__ int s_cand[SYN_WARPS][SYN_K][3];
+  __shared__ int s_rem[SYN_WARPS];
+
+  // Column of this CTA: tile, then the j-th column of this colour class in that tile.
+  int lo = 0, hi = ntiles - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tiles[mid].col_base[color] <= blockIdx.x) lo = mid; else hi = mid - 1;
+  }
+  const SynthTile& t = tiles[lo];
+  const uint32_t j = blockIdx.x - t.col_base[color];
+  const uint32_t cxn = (t.nbx - (color & 1) + 1) / 2;
+  const uint32_t bx = 2 * (j % cxn) + (color & 1), by = 2 * (j / cxn) + (color >> 1);
+  const int x0 = static_cast<int>(bx) * SYN_B, y0 = static_cast<int>(by) * SYN_B;
+  const int x1 = min(x0 + SYN_B, static_cast<int>(t.gw)), y1 = min(y0 + SYN_B, static_cast<int>(t.gh));
+  const int gd = static_cast<int>(t.gd);
+  const int ox = x0 - SYN_HALO, oy = y0 - SYN_HALO;
+  const uint32_t colkey = by * t.nbx + bx;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ncell = SYN_R * SYN_R * nz;
+  uint32_t* tc = cells + t.cell_base;
+
+  // Stage the region (column + halo) of the cell grid.
+  for (int i = tid; i < ncell; i += blockDim.x) {
+    const int rx = i % SYN_R, ry = (i / SYN_R) % SYN_R, rz = i / (SYN_R * SYN_R);
+    const int gx = ox + rx, gy = oy + ry, gz = rz - 2;
+    uint32_t w = 0;
+    if (gx >= 0 && gy >= 0 && gz >= 0 && gx < static_cast<int>(t.gw) && gy < static_cast<int>(t.gh) && gz < gd)
+      w = tc[(static_cast<size_t>(gz) * t.gh + gy) * t.gw + gx];
+    grid[i] = w;
+  }
+  if (tid == 0) s_nact = 0;
+  __syncthreads();
+  // Active list: the column's points in cell order (deterministic block-wide compaction).
+  const int bw = x1 - x0, bh = y1 - y0;
+  const int bcells = bw * bh * gd;
+  for (int base = 0; base < bcells; base += blockDim.x) {
+    const int i = base + tid;
+    int ridx = 0;
+    bool occ = false;
+    if (i < bcells) {
+      const int lx = i % bw, ly = (i / bw) % bh, lz = i / (bw * bh);
+      ridx = ((lz + 2) * SYN_R + (ly + SYN_HALO)) * SYN_R + (lx + SYN_HALO);
+      occ = (grid[ridx] & OCC) != 0;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, occ);
+    if (lane == 0) s_wsum[warp] = __popc(m);
+    __syncthreads();
+    int off = s_nact;
+    for (int w = 0; w < warp; ++w) off += s_wsum[w];
+    if (occ) active[off + __popc(m & ((1u << lane) - 1u))] = static_cast<uint16_t>(ridx);
+    __syncthreads();
+    if (tid == 0)
+      for (int w = 0; w < SYN_WARPS; ++w) s_nact += s_wsum[w];
+    __syncthreads();
+  }
+  // An empty column starts from one random point (poisson.rs:46-57), up to 30 tries.
+  if (tid == 0 && s_nact == 0 && bw > 0 && bh > 0) {
+    for (int k = 0; k < SYN_K; ++k) {
+      const P4 r = philox(static_cast<uint32_t>(k), 0, colkey, TAG_SEED, t.k0, t.k1);
+      const int X = x0 * SYN_Q + static_cast<int>(uf(r.x) * static_cast<float>(bw * SYN_Q));
+      const int Y = y0 * SYN_Q + static_cast<int>(uf(r.y) * static_cast<float>(bh * SYN_Q));
+      const int Z = static_cast<int>(uf(r.z) * static_cast<float>(t.ZW));
+      if (X >= static_cast<int>(t.XW) || Y >= static_cast<int>(t.YW) || Z >= static_cast<int>(t.ZW)) continue;
+      const int cx = X >> 10, cy = Y >> 10, cz = Z >> 10;
+      const int rx = cx - ox, ry = cy - oy, rz = cz + 2;
+      if (!syn_free(grid, rx, ry, rz, X, Y, Z, cx, cy, cz)) continue;
+      const int ridx = (rz * SYN_R + ry) * SYN_R + rx;
+      grid[ridx] = OCC | (static_cast<uint32_t>(Z & 1023) << 20) | (static_cast<uint32_t>(Y & 1023) << 10) |
+                   static_cast<uint32_t>(X & 1023);
+      active[s_nact++] = static_cast<uint16_t>(ridx);
+      break;
+    }
+  }
+  const int max_iter = 16 * SYN_B * SYN_B * gd + 64;
+  for (int iter = 0;; ++iter) {
+    __syncthreads();
+    const int nact = s_nact;
+    if (nact == 0) break;
+    if (iter >= max_iter) {
+      if (tid == 0) atomicOr(err, ERR_SPIN_LIMIT);
+      break;
+    }
+    // One Bridson step per warp on a random active point (poisson.rs:59-129).
+    if (lane == 0) {
+      const P4 r = philox(static_cast<uint32_t>(iter), static_cast<uint32_t>(warp), colkey, TAG_PICK, t.k0, t.k1);
+      s_pick[warp] = static_cast<int>((static_cast<unsigned long long>(r.x) * static_cast<unsigned>(nact)) >> 32);
+    }
+    __syncwarp();
+    const int pick = s_pick[warp];
+    const int pr = active[pick];
+    const uint32_t pw = grid[pr];
+    const int prx = pr % SYN_R, pry = (pr / SYN_R) % SYN_R, prz = pr / (SYN_R * SYN_R);
+    const int BX = (prx + ox) * SYN_Q + static_cast<int>(pw & 1023u);
+    const int BY = (pry + oy) * SYN_Q + static_cast<int>((pw >> 10) & 1023u);
+    const int BZ = (prz - 2) * SYN_Q + static_cast<int>((pw >> 20) & 1023u);
+    bool valid = false;
+    int X = 0, Y = 0, Z = 0;
+    if (lane < SYN_K) {
+      const P4 r = philox(static_cast<uint32_t>(iter), static_cast<uint32_t>(warp * 32 + lane), colkey, TAG_CAND,
+                          t.k0, t.k1);
+      const float u = uf(r.x);
+      const float ct = uf(r.y) * 2.0f - 1.0f;
+      const float st = sqrtf(fmaxf(1.0f - ct * ct, 0.0f));
+      float sp, cp;
+      sincospif(uf(r.z) * 2.0f, &sp, &cp);
+      const float rad = cbrtf(7.0f * u + 1.0f) * 1.7320508075688772f;  // r = sqrt(3) cells
+      const float fx = static_cast<float>(BX) * (1.0f / SYN_Q) + rad * st * cp;
+      const float fy = static_cast<float>(BY) * (1.0f / SYN_Q) + rad * st * sp;
+      const float fz = static_cast<float>(BZ) * (1.0f / SYN_Q) + rad * ct;
+      if (fx >= 0.0f && fy >= 0.0f && fz >= 0.0f) {
+        X = static_cast<int>(floorf(fx * SYN_Q));
+        Y = static_cast<int>(floorf(fy * SYN_Q));
+        Z = static_cast<int>(floorf(fz * SYN_Q));
+        if (X < static_cast<int>(t.XW) && Y < static_cast<int>(t.YW) && Z < static_cast<int>(t.ZW)) {
+          const int cx = X >> 10, cy = Y >> 10, cz = Z >> 10;
+          valid = syn_free(grid, cx - ox, cy - oy, cz + 2, X, Y, Z, cx, cy, cz);
+        }
+      }
+      s_cand[warp][lane][0] = X;
+      s_cand[warp][lane][1] = Y;
+      s_cand[warp][lane][2] = Z;
+    }
+    const unsigned vm = __ballot_sync(0xffffffffu, valid);
+    if (lane == 0) s_vmask[warp] = vm;
+    __syncthreads();
+    if (tid == 0) {
+      int cx_[SYN_WARPS], cy_[SYN_WARPS], cz_[SYN_WARPS];
+      int ncom = 0, nrem = 0;
+      for (int w = 0; w < SYN_WARPS; ++w) {
+        unsigned m = s_vmask[w];
+        if (m == 0) {
+          s_rem[nrem++] = s_pick[w];  // 30 misses: the point retires
+          continue;
+        }
+        while (m) {
+          const int l = __ffs(m) - 1;
+          m &= m - 1;
+          const int CX = s_cand[w][l][0], CY = s_cand[w][l][1], CZ = s_cand[w][l][2];
+          bool ok = true;
+          for (int k = 0; k < ncom && ok; ++k) {
+            const int ex = CX - cx_[k], ey = CY - cy_[k], ez = CZ - cz_[k];
+            ok = ex * ex + ey * ey + ez * ez >= SYN_R2;
+          }
+          if (!ok) continue;
+          const int ccx = CX >> 10, ccy = CY >> 10, ccz = CZ >> 10;
+          const int ridx = ((ccz + 2) * SYN_R + (ccy - oy)) * SYN_R + (ccx - ox);
+          grid[ridx] = OCC | (static_cast<uint32_t>(CZ & 1023) << 20) | (static_cast<uint32_t>(CY & 1023) << 10) |
+                       static_cast<uint32_t>(CX & 1023);
+          cx_[ncom] = CX; cy_[ncom] = CY; cz_[ncom] = CZ;
+          ++ncom;
+          if (ccx >= x0 && ccx < x1 && ccy >= y0 && ccy < y1) active[s_nact++] = static_cast<uint16_t>(ridx);
+          break;
+        }
+      }
+      // Retire in descending index order (swap-remove keeps lower indices valid); skip repeats.
+      for (int a = 1; a < nrem; ++a)
+        for (int b = a; b > 0 && s_rem[b] > s_rem[b - 1]; --b) {
+          const int tmp = s_rem[b]; s_rem[b] = s_rem[b - 1]; s_rem[b - 1] = tmp;
+        }
+      for (int a = 0; a < nrem; ++a) {
+        if (a > 0 && s_rem[a] == s_rem[a - 1]) continue;
+        active[s_rem[a]] = active[--s_nact];
+      }
+    }
+  }
+  __syncthreads();
+  // Write back the column and its spill zone.
+  for (int i = tid; i < ncell; i += blockDim.x) {
+    const int rx = i % SYN_R, ry = (i / SYN_R) % SYN_R, rz = i / (SYN_R * SYN_R);
+    if (rx < 2 || ry < 2 || rx >= SYN_R - 2 || ry >= SYN_R - 2) continue;
+    const int gx = ox + rx, gy = oy + ry, gz = rz - 2;
+    if (gx >= 0 && gy >= 0 && gz >= 0 && gx < static_cast<int>(t.gw) && gy < static_cast<int>(t.gh) && gz < gd)
+      tc[(static_cast<size_t>(gz) * t.gh + gy) * t.gw + gx] = grid[i];
+  }
+}
+
+// Points per tile.
+__global__ void k_count_points(const SynthTile* __restrict__ tiles, int ntiles, unsigned long long ncells,
+                               const uint32_t* __restrict__ cells, uint32_t* npts) {
+  const unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+  const bool occ = i < ncells && (cells[i] & OCC);
+  const unsigned act = __activemask();
+  int tile = -1;
+  if (occ) tile = find_tile_ull(tiles, ntiles, i, 0);
+  const unsigned grp = __match_any_sync(act, tile);
+  if (occ && (threadIdx.x & 31) == static_cast<unsigned>(__ffs(grp) - 1)) atomicAdd(&npts[tile], __popc(grp));
+}
+
+// Independent deletion down to the Bridson-expected count.
+__global__ void k_thin(const SynthTile* __restrict__ tiles, int ntiles, unsigned long long ncells,
+                       uint32_t* __restrict__ cells, const uint32_t* npts) {
+  const unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+  if (i >= ncells || !(cells[i] & OCC)) return;
+  const int tile = find_tile_ull(tiles, ntiles, i, 0);
+  const SynthTile& t = tiles[tile];
+  const uint32_t n = npts[tile];
+  if (n <= t.target) return;
+  const float p = 1.0f - static_cast<float>(t.target) / static_cast<float>(n);
+  const uint32_t lin = static_cast<uint32_t>(i - t.cell_base);
+  if (uf(philox(lin, 0, 0, TAG_THIN, t.k0, t.k1).x) < p) cells[i] = 0;
+}
+
+// Occupancy of each compaction slot: slot = morton2(x, y) * gd + z.
+__global__ void k_slot_flags(const SynthTile* __restrict__ tiles, int ntiles, unsigned long long nslots,
+                             const uint32_t* __restrict__ cells, uint32_t* flags) {
+  const unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+  if (i >= nslots) return;
+  const SynthTile& t = tiles[find_tile_ull(tiles, ntiles, i, 1)];
+  const uint32_t sl = static_cast<uint32_t>(i - t.slot_base);
+  uint32_t f = 0;
+  if (sl < t.slots) {
+    const uint32_t m2 = sl / t.gd, z = sl % t.gd;
+    const uint32_t x = morton2_compact(m2), y = morton2_compact(m2 >> 1);
+    if (x < t.gw && y < t.gh) f = (cells[t.cell_base + (static_cast<size_t>(z) * t.gh + y) * t.gw + x] & OCC) ? 1u : 0u;
+  }
+  flags[i] = f;
+}
+
+// Crystal k of a tile from its slot: position from the fixed-point cell word, attributes from the
+// tile's Philox stream keyed by the cell (emulsion.rs:162-200).
+__global__ void k_emit(const SynthTile* __restrict__ tiles, int ntiles, unsigned long long nslots,
+                       const uint32_t* __restrict__ cells, const uint32_t* __restrict__ scan,
+                       float4* A, float4* Q, float4* D, uint64_t* keys, uint32_t* err) {
+  const unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+  if (i >= nslots) return;
+  const SynthTile& t = tiles[find_tile_ull(tiles, ntiles, i, 1)];
+  const uint32_t sl = static_cast<uint32_t>(i - t.slot_base);
+  if (sl >= t.slots || scan[i + 1] == scan[i]) return;
+  const uint32_t k = scan[i] - scan[t.slot_base];
+  if (k >= t.ccap) {
+    atomicOr(err, ERR_LIST_OVERFLOW);
+    return;
+  }
+  const uint32_t m2 = sl / t.gd, z = sl % t.gd;
+  const uint32_t x = morton2_compact(m2), y = morton2_compact(m2 >> 1);
+  const uint32_t lin = (z * t.gh + y) * t.gw + x;
+  const uint32_t w = cells[t.cell_base + lin];
+  const float px = static_cast<float>(static_cast<int>(x) * SYN_Q + static_cast<int>(w & 1023u)) * (t.cell / SYN_Q);
+  const float py = static_cast<float>(static_cast<int>(y) * SYN_Q + static_cast<int>((w >> 10) & 1023u)) * (t.cell / SYN_Q);
+  const float pz = static_cast<float>(static_cast<int>(z) * SYN_Q + static_cast<int>((w >> 20) & 1023u)) * (t.cell / SYN_Q);
+  const P4 r0 = philox(lin, 0, 0, TAG_ATTR, t.k0, t.k1);
+  const P4 r1 = philox(lin, 1, 0, TAG_ATTR, t.k0, t.k1);
+  // Two normals from one Box-Muller pair: radius (log-normal) and sensitivity.
+  const float bm = sqrtf(-2.0f * logf(1.0f - uf(r0.x)));
+  float s2, c2;
+  sincospif(2.0f * uf(r0.y), &s2, &c2);
+  const float radius = fminf(fmaxf(expf(t.mu + t.sg * bm * c2), 0.15f), t.rmax);
+  const float sens = fmaxf(t.base_sens + 0.15f * bm * s2, 0.1f);
+  float4 q, d;
+  if (t.morph == 1) {
+    // Tabular: thickness r / AR (>= 0.05), tilt +-0.17 rad about a random in-plane axis.
+    const float ht = fmaxf(radius / t.aspect, 0.05f);
+    const float tilt = uf(r0.z) * 0.34f - 0.17f;
+    float ax = uf(r0.w) * 2.0f - 1.0f, ay = uf(r1.x) * 2.0f - 1.0f;
+    const float n = rsqrtf(fmaxf(ax * ax + ay * ay, 1e-30f));
+    ax *= n;
+    ay *= n;
+    float sh, ch;
+    sincosf(0.5f * tilt, &sh, &ch);
+    q = make_float4(ax * sh, ay * sh, 0.0f, ch);
+    d = make_float4(radius, radius, ht, __int_as_float(1));
+  } else {
+    // Cubic / octahedral: UnitQuaternion::from_euler_angles(2 pi u1, pi u2, 2 pi u3).
+    float sr, cr, sp, cp, sy, cy;
+    sincospif(uf(r0.z), &sr, &cr);        // roll / 2 = pi u1
+    sincospif(0.5f * uf(r0.w), &sp, &cp); // pitch / 2 = pi u2 / 2
+    sincospif(uf(r1.x), &sy, &cy);        // yaw / 2 = pi u3
+    q = make_float4(sr * cp * cy - cr * sp * sy, cr * sp * cy + sr * cp * sy, cr * cp * sy - sr * sp * cy,
+                    cr * cp * cy + sr * sp * sy);
+    d = make_float4(radius, radius, radius, __int_as_float(t.morph));
+  }
+  const unsigned long long o = t.cbase + k;
+  A[o] = make_float4(px, py, pz, sens);
+  Q[o] = q;
+  D[o] = d;
+  keys[o] = sl;
+}
+
+}  // namespace fg
+
+namespace fg {
+
+// Host wrappers (launch on `st`; all buffers preallocated so the sequence can be graph-captured).
+void launch_bridson(const SynthTile* tiles, int ntiles, int color, unsigned ncols, int gdmax,
+                    uint32_t* cells, uint32_t* err, cudaStream_t st) {
+  if (ncols == 0) return;
+  const int nz = gdmax + 4;
+  const size_t smem = static_cast<size_t>(SYN_R) * SYN_R * nz * sizeof(uint32_t) +
+                      static_cast<size_t>(SYN_B) * SYN_B * gdmax * sizeof(uint16_t);
+  FG_CUDA(cudaFuncSetAttribute(k_bridson, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  k_bridson<<<ncols, SYN_WARPS * 32, smem, st>>>(tiles, ntiles, color, nz, cells, err);
+  FG_CUDA(cudaGetLastError());
+}
+
+size_t bridson_smem(int gdmax) {
+  return static_cast<size_t>(SYN_R) * SYN_R * (gdmax + 4) * sizeof(uint32_t) +
+         static_cast<size_t>(SYN_B) * SYN_B * gdmax * sizeof(uint16_t);
+}
+
+void launch_synth_post(const SynthTile* tiles, int ntiles, unsigned long long ncells, unsigned long long nslots,
+                       uint32_t* cells, uint32_t* npts, uint32_t* flags, cudaStream_t st) {
+  k_count_points<<<grid_for(ncells, 256), 256, 0, st>>>(tiles, ntiles, ncells, cells, npts);
+  k_thin<<<grid_for(ncells, 256), 256, 0, st>>>(tiles, ntiles, ncells, cells, npts);
+  k_slot_flags<<<grid_for(nslots, 256), 256, 0, st>>>(tiles, ntiles, nslots, cells, flags);
+  FG_CUDA(cudaGetLastError());
+}
+
+void launch_emit(const SynthTile* tiles, int ntiles, unsigned long long nslots, const uint32_t* cells,
+                 const uint32_t* scan, float4* A, float4* Q, float4* D, uint64_t* keys, uint32_t* err,
+                 cudaStream_t st) {
+  k_emit<<<grid_for(nslots, 256), 256, 0, st>>>(tiles, ntiles, nslots, cells, scan, A, Q, D, keys, err);
+  FG_CUDA(cudaGetLastError());
+}
+
+}  // namespace fg

@@ -163,6 +163,7 @@ TileDesc make_tile_desc(const fg_emulsion* em, const float* tile_dev, uint32_t t
   t.tile = tile_dev;
   t.tw = tw;
   t.th = th;
+  t.stride = tw;
   t.W = (float)em->cfg.width;
   t.H = (float)em->cfg.height;
   t.D = (float)em->cfg.depth;
@@ -193,6 +194,18 @@ void launch_transport(const TileDesc* tiles_dev, int ntiles, unsigned long long 
   unsigned blocks = static_cast<unsigned>(std::min<unsigned long long>((warps + 7) / 8, (unsigned long long)sm_count * 8));
   blocks = std::max(blocks, 1u);
   k_transport<<<blocks, 256, 0, st>>>(tiles_dev, ntiles, total, counter, err, stats);
+  FG_CUDA(cudaGetLastError());
+}
+
+void launch_transport_shape(const TileDesc* tiles_dev, int ntiles, unsigned long long total,
+                            unsigned long long* counter, uint32_t* err, unsigned long long* stats,
+                            unsigned blocks, unsigned threads, cudaStream_t st) {
+  if (total == 0) return;
+  FG_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
+  const unsigned long long warps = (total + 31) / 32;
+  const unsigned long long need = (warps * 32 + threads - 1) / threads;
+  blocks = static_cast<unsigned>(std::max<unsigned long long>(std::min<unsigned long long>(blocks, need), 1));
+  k_transport<<<blocks, threads, 0, st>>>(tiles_dev, ntiles, total, counter, err, stats);
   FG_CUDA(cudaGetLastError());
 }
 

@@ -18,6 +18,7 @@ struct __align__(16) TileDesc {
   const float* tile;
   unsigned long long photon_base;
   uint32_t n, tw, th, P;
+  uint32_t stride;  // exposure row stride (floats); tiles may be windows of one image
   float W, H, D;
   uint32_t k0, k1;
   float mu_t, albedo, g, r0, eff_r, theta_max, alpha;
@@ -98,7 +99,7 @@ __device__ __forceinline__ void add_counts(uint32_t* counts, uint32_t s, uint32_
 }
 
 // One photon packet from emission to death (transport.rs:72-185).  Returns its absorbing hits.
-__device__ __noinline__ uint32_t trace_photon(const TileDesc& t, uint32_t id, uint32_t* err) {
+static __device__ __noinline__ uint32_t trace_photon(const TileDesc& t, uint32_t id, uint32_t* err) {
   const float PI2 = 6.283185307179586f;
   const P4 e0 = philox(id, 0, 0, TAG_EMIT, t.k0, t.k1);
   const float x = uf(e0.x) * t.W;
@@ -107,7 +108,7 @@ __device__ __noinline__ uint32_t trace_photon(const TileDesc& t, uint32_t id, ui
   const float uu = fminf(fmaxf(x / t.W, 0.0f), 1.0f), vv = fminf(fmaxf(y / t.H, 0.0f), 1.0f);
   const uint32_t px = min(static_cast<uint32_t>(roundf(uu * (float)(t.tw - 1))), t.tw - 1);
   const uint32_t py = min(static_cast<uint32_t>(roundf(vv * (float)(t.th - 1))), t.th - 1);
-  float E = fmaxf(__ldg(&t.tile[static_cast<size_t>(py) * t.tw + px]), 0.0f);
+  float E = fmaxf(__ldg(&t.tile[static_cast<size_t>(py) * t.stride + px]), 0.0f);
   if (!(E > 0.0f)) return 0;
   const float theta = uf(e0.z) * t.theta_max;
   const float phi = uf(e0.w) * PI2;

@@ -210,6 +210,89 @@ fg_status fg_replay_rays(fg_engine* e, const fg_emulsion* em, const double* orig
 fg_status fg_scan_ray_hits(fg_engine* e, const fg_emulsion* em, const fg_scan_cfg* cfg,
                            uint64_t seed, uint16_t* ray_hits);
 
+/* ---- tiles: the drop-in for GpuEngine::render_tile_all_gpu (src/gpu.rs:491-938) ---- */
+
+/* Per-tile parameters: GpuTileParams (src/gpu.rs:18-37) with the same meaning, followed by the
+ * CPU-path physics of the reference's tile worker (src/image_pipeline.rs:924-1014) that
+ * GpuTileParams does not carry.  Seeds follow the tile worker: synthesis `seed`, exposure
+ * `seed + 1`, scan `seed + 2`; photons per um^2 = photons_per_sq_um * max(exposure, 0.05). */
+typedef struct fg_tile_params {
+  double film_w, film_h, film_d;
+  uint32_t width_px, height_px;
+  uint32_t samples_per_pixel;
+  uint32_t threshold_photons;
+  double silver_opacity;
+  uint64_t seed;
+  double r_min, mean_crystal_radius, size_variance;
+  int32_t morphology;
+  int32_t _pad0;
+  double tabular_aspect_ratio, base_sensitivity, exposure;
+  double filament_expansion, clumping_proximity_factor;
+  fg_optics optics;
+  double photons_per_sq_um;
+  double illumination_angle_rad;
+  double crystal_absorption_coeff;
+  uint32_t max_bounces;
+  uint32_t _pad1;
+} fg_tile_params;
+
+/* Fills the parameters the reference's CPU tile worker would use for a tile of tw x th pixels of
+ * pixel_size_um micrometres (stock selection image_pipeline.rs:925-938, exposure config :942-947,
+ * development :963-976 with the effective push of :369-375, scan :996-1002). */
+fg_status fg_tile_params_preset(const char* preset, double pixel_size_um, uint32_t tw, uint32_t th,
+                                double exposure, double push, uint64_t tile_seed, fg_tile_params* out);
+
+/* Plain per-tile path: one tile from exposure (tw*th floats) to negative density
+ * d = -log10(clamp(T, 1e-4, 1)) + 0.05 (src/image_pipeline.rs:1007-1011); blocking; device
+ * buffers are made and freed inside the call, like the reference engine's per-call buffers. */
+fg_status fg_render_tile(fg_engine* e, const float* tile, const fg_tile_params* params, float* d_neg);
+
+/* ---- batches: many tiles in one graph-captured sequence of launches ---- */
+typedef struct fg_batch fg_batch;
+typedef struct fg_batch_options {
+  int32_t use_graph;              /* capture the run into a CUDA graph (default in NULL options) */
+  int32_t autotune;               /* time launch shapes when the plan is made */
+  uint32_t transport_threads;     /* 0: default */
+  uint32_t transport_blocks;      /* 0: default */
+  uint32_t scan_bin_px;           /* 0: default */
+  uint32_t _pad;
+} fg_batch_options;
+
+typedef struct fg_batch_stats {
+  double synth_ms, bvh_ms, transport_ms, develop_ms, scan_ms, total_ms;
+  uint64_t crystals, photons, rays, pixels;
+  uint64_t hits;            /* absorbing photon-crystal hits in transport */
+  uint64_t scan_hits;       /* scanner ray-crystal hits */
+  uint64_t scan_fallbacks;  /* scanner decisions taken in FP64 */
+  uint32_t transport_threads, transport_blocks, scan_bin_px, graph, kernel_launches, _pad;
+} fg_batch_stats;
+
+fg_status fg_batch_create(fg_engine* e, const fg_tile_params* tiles, uint32_t ntiles,
+                          const fg_batch_options* options, fg_batch** out);
+fg_status fg_batch_destroy(fg_batch* b);
+/* Copies every tile's exposure (width_px * height_px floats each) from the host. */
+fg_status fg_batch_set_exposure(fg_batch* b, const float* const* tiles);
+/* Device addresses of a tile's exposure input and density output (valid for the batch's life). */
+fg_status fg_batch_exposure_device(fg_batch* b, uint32_t tile, float** ptr);
+fg_status fg_batch_density_device(fg_batch* b, uint32_t tile, const float** ptr);
+/* Enqueues one run on the engine stream (returns at once); wait for it with fg_batch_wait. */
+fg_status fg_batch_run(fg_batch* b);
+fg_status fg_batch_wait(fg_batch* b, fg_batch_stats* stats);
+fg_status fg_batch_get_density(fg_batch* b, float* const* outs);
+/* The synthesized crystals of one tile after a run, with their latent counts, developed flags and
+ * expansions (any pointer may be NULL); *n receives the tile's crystal count. */
+fg_status fg_batch_tile_crystals(fg_batch* b, uint32_t tile, fg_crystals_out* out, uint32_t* counts,
+                                 uint8_t* developed, double* expansion, size_t cap, size_t* n);
+/* Replays the batch `steps` times back to back on the engine stream; *ms receives the device time
+ * between CUDA events recorded before the first and after the last replay. */
+fg_status fg_batch_time(fg_batch* b, uint32_t steps, double* ms);
+/* Page-locked host memory for fast host<->device copies of exposure and density tiles. */
+fg_status fg_host_alloc(size_t bytes, void** ptr);
+fg_status fg_host_free(void* ptr);
+/* Convenience: plan, copy in, run, copy out and free (no graph). */
+fg_status fg_render_batch(fg_engine* e, const fg_tile_params* tiles, uint32_t ntiles,
+                          const float* const* exposure, float* const* d_neg);
+
 #ifdef __cplusplus
 }
 #endif

@@ -33,7 +33,8 @@ def test_every_declared_symbol_is_exported_and_bound():
 
 
 STRUCTS = ["fg_optics", "fg_emulsion_cfg", "fg_exposure_cfg", "fg_dev_cfg", "fg_dev_report",
-           "fg_scan_cfg", "fg_crystals_host", "fg_crystals_out", "fg_segment", "fg_timings"]
+           "fg_scan_cfg", "fg_crystals_host", "fg_crystals_out", "fg_segment", "fg_timings",
+           "fg_tile_params", "fg_batch_options", "fg_batch_stats"]
 
 
 def test_struct_layouts_match_ctypes(tmp_path):
@@ -90,3 +91,26 @@ def test_engine_creation_reports_status_without_crashing():
         assert lib.fg_engine_destroy(h) == 0
     assert lib.fg_engine_create(-1, C.byref(h)) == 1
     assert lib.fg_engine_destroy(None) == 16
+
+
+@pytest.mark.parametrize("preset,push", [("tri-x", 0.0), ("tri-x", 2.0), ("t-max", 1.0), ("hp5", 0.5),
+                                         ("tri-x-1600", 0.0)])
+def test_tile_params_follow_the_cpu_tile_worker(preset, push):
+    """fg_tile_params_preset reproduces render_tile_cpu_full's configuration
+    (image_pipeline.rs:925-1002) for every stock and push."""
+    from tests.helpers import tile_worker_dev_cfg, REFERENCE_PRESETS
+    px = 0.5
+    p = fg.tile_params(preset, px, 100, 80, 0.7, push, 99)
+    eff = max(push, 2.0) if "1600" in preset else max(push, 0.0)
+    stock = preset if preset in ("t-max", "hp5", "tri-x-1600") else ("tri-x-1600" if eff >= 1.5 else "tri-x")
+    d, r, m, v, mo, ar, o, sens = REFERENCE_PRESETS[stock]
+    assert (p.film_w, p.film_h, p.film_d) == (50.0, 40.0, d)
+    assert (p.r_min, p.mean_crystal_radius, p.size_variance, p.morphology, p.base_sensitivity) == (r, m, v, mo, sens)
+    base = preset if preset in ("t-max", "hp5") else "tri-x"
+    dc = tile_worker_dev_cfg(base, eff)
+    assert p.threshold_photons == 4
+    assert abs(p.filament_expansion - dc.filament_expansion) < 1e-15
+    assert abs(p.clumping_proximity_factor - dc.clumping_proximity_factor) < 1e-15
+    assert (p.samples_per_pixel, p.silver_opacity, p.seed) == (4, 0.25, 99)
+    assert (p.photons_per_sq_um, p.illumination_angle_rad, p.crystal_absorption_coeff, p.max_bounces) == (6.0, 0.12, 1.3, 48)
+    assert p.exposure == 0.7
