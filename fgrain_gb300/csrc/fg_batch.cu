@@ -31,11 +31,12 @@ void launch_synth_post(const SynthTile* tiles, int ntiles, unsigned long long nc
 void launch_emit(const SynthTile* tiles, int ntiles, unsigned long long nslots, const uint32_t* cells,
                  const uint32_t* scan, float4* A, float4* Q, float4* D, uint64_t* keys, uint32_t* err,
                  cudaStream_t st);
-void launch_transport(const TileDesc* tiles_dev, int ntiles, unsigned long long total, unsigned long long* counter,
-                      uint32_t* err, unsigned long long* stats, int sm_count, cudaStream_t st);
 void launch_transport_shape(const TileDesc* tiles_dev, int ntiles, unsigned long long total,
-                            unsigned long long* counter, uint32_t* err, unsigned long long* stats,
-                            unsigned blocks, unsigned threads, cudaStream_t st);
+                            const uint32_t* order, unsigned long long* counter, uint32_t* err,
+                            unsigned long long* stats, unsigned blocks, unsigned threads, cudaStream_t st);
+void launch_photon_sort(const TileDesc* tiles_dev, int ntiles, unsigned long long total, unsigned long long ncells,
+                        uint32_t* cnt, const uint32_t* off, uint32_t* cur, uint32_t* order, uint32_t* err,
+                        cudaStream_t st);
 void launch_scan(const ScanTile* tiles, int ntiles, unsigned long long nbins, unsigned threads, uint32_t* err,
                  unsigned long long* stats, cudaStream_t st);
 uint32_t scan_bin_px(uint32_t spp);
@@ -422,6 +423,8 @@ struct fg_batch {
   DBuf<uint8_t> developed;
   DBuf<double> exp64;
   DBuf<uint32_t> bin_cnt, bin_off, bin_cur, bin_items;
+  DBuf<uint32_t> pcnt, poff, pcur, porder;  // photon ordering by emission cell
+  unsigned long long npcells = 0;
   DBuf<float> exposure, d_neg;
   DBuf<unsigned long long> counter;
   DBuf<unsigned long long> dstats;  // [0] transport hits, [1] scan FP64 fallbacks, [2] scan hits
@@ -434,6 +437,7 @@ struct fg_batch {
   unsigned tr_blocks = 0, tr_threads = 256, scan_threads = 256;
   uint32_t bin_px = 8;
   bool use_graph = true;
+  bool tune_pending = false;  // autotune (and capture) at the first run, once exposure is set
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t ev[7] = {};
@@ -562,8 +566,9 @@ static void layout_bins(fg_batch* B, uint32_t bin_px) {
 }
 
 static void upload_descriptors(fg_batch* B, cudaStream_t st) {
-  // Device pointers inside the descriptors depend on the buffers; n stays as the device wrote it
-  // (the copy of bt/td/sc happens before the run that sets it).
+  // Device pointers inside the descriptors depend on the buffers.  The per-tile crystal counts n
+  // are device-written (k_set_n from the compaction scan); the host copies hold 0, so they are
+  // re-derived on the device right after the copy.
   for (uint32_t i = 0; i < B->ntiles; ++i) {
     const unsigned long long cb = B->syn[i].cbase;
     TileDesc& t = B->td[i];
@@ -584,6 +589,7 @@ static void upload_descriptors(fg_batch* B, cudaStream_t st) {
     c.sigma_c = nullptr;
     c.bin_off = B->bin_off.p + c.bin_base;
     c.bin_items = B->bin_items.p;
+    c.items_cap = static_cast<uint32_t>(std::min<unsigned long long>(B->item_cap, 0xffffffffull));
     c.out = nullptr;
     c.image8 = nullptr;
     c.d_neg = B->d_neg.p + B->out_off[i];
@@ -594,6 +600,9 @@ static void upload_descriptors(fg_batch* B, cudaStream_t st) {
   FG_CUDA(cudaMemcpyAsync(B->d_td.p, B->td.data(), B->ntiles * sizeof(TileDesc), cudaMemcpyHostToDevice, st));
   FG_CUDA(cudaMemcpyAsync(B->d_sc.p, B->sc.data(), B->ntiles * sizeof(ScanTile), cudaMemcpyHostToDevice, st));
   FG_CUDA(cudaMemcpyAsync(B->d_bt.p, B->bt.data(), B->ntiles * sizeof(BTile), cudaMemcpyHostToDevice, st));
+  k_set_n<<<grid_for(B->ntiles, 128), 128, 0, st>>>(B->d_syn.p, static_cast<int>(B->ntiles), B->slot_scan.p, B->d_bt.p,
+                                                    B->d_td.p, B->d_sc.p, B->ncrys.p);
+  FG_CUDA(cudaGetLastError());
 }
 
 static void cub_scan(fg_batch* B, const uint32_t* in, uint32_t* out, unsigned long long n, cudaStream_t st) {
@@ -630,8 +639,19 @@ static void stage_bvh(fg_batch* B, cudaStream_t st) {
 
 static void stage_transport(fg_batch* B, cudaStream_t st) {
   FG_CUDA(cudaMemsetAsync(B->counts.p, 0, B->ncap * sizeof(uint32_t), st));
-  launch_transport_shape(B->d_td.p, static_cast<int>(B->ntiles), B->photons, B->counter.p, B->e->d_err,
-                         B->dstats.p, B->tr_blocks, B->tr_threads, st);
+  launch_transport_shape(B->d_td.p, static_cast<int>(B->ntiles), B->photons, B->porder.p, B->counter.p,
+                         B->e->d_err, B->dstats.p, B->tr_blocks, B->tr_threads, st);
+}
+
+// Orders photon ids by emission cell (independent of the crystals: runs with synthesis).
+static void stage_photon_order(fg_batch* B, cudaStream_t st) {
+  const int nt = static_cast<int>(B->ntiles);
+  FG_CUDA(cudaMemsetAsync(B->pcnt.p, 0, (B->npcells + 1) * sizeof(uint32_t), st));
+  FG_CUDA(cudaMemsetAsync(B->pcur.p, 0, (B->npcells + 1) * sizeof(uint32_t), st));
+  launch_photon_sort(B->d_td.p, nt, B->photons, B->npcells, B->pcnt.p, nullptr, nullptr, nullptr, B->e->d_err, st);
+  cub_scan(B, B->pcnt.p, B->poff.p, B->npcells + 1, st);
+  launch_photon_sort(B->d_td.p, nt, B->photons, B->npcells, nullptr, B->poff.p, B->pcur.p, B->porder.p, B->e->d_err,
+                     st);
 }
 
 static void stage_develop(fg_batch* B, cudaStream_t st) {
@@ -672,6 +692,7 @@ static void mark(cudaEvent_t ev, cudaStream_t st, bool capturing) {
 static void enqueue_all(fg_batch* B, cudaStream_t st, bool capturing = false) {
   mark(B->ev[0], st, capturing);
   stage_synth(B, st);
+  stage_photon_order(B, st);
   mark(B->ev[1], st, capturing);
   stage_bvh(B, st);
   mark(B->ev[2], st, capturing);
@@ -769,6 +790,14 @@ static void plan(fg_batch* B, const fg_batch_options* opt) {
     cap += s.ccap;
     B->td[i].photon_base = pb;
     pb += B->td[i].P;
+    {
+      const double side = std::max(B->params[i].film_w, B->params[i].film_h) / PHOTON_CELL_UM;
+      uint32_t bits = 0;
+      while ((1u << bits) < static_cast<uint32_t>(std::ceil(side))) ++bits;
+      B->td[i].pcell_bits = bits;
+      B->td[i].pcell_base = static_cast<uint32_t>(B->npcells);
+      B->npcells += 1ull << (2 * bits);
+    }
     B->exp_off[i] = eo;
     eo += static_cast<unsigned long long>(B->params[i].width_px) * B->params[i].height_px;
     B->out_off[i] = oo;
@@ -801,6 +830,7 @@ static void plan(fg_batch* B, const fg_batch_options* opt) {
   B->ncrys.alloc(n, st);
   B->flags.alloc(sb + 1, st);
   B->slot_scan.alloc(sb + 1, st);
+  FG_CUDA(cudaMemsetAsync(B->slot_scan.p, 0, (sb + 1) * sizeof(uint32_t), st));  // n = 0 until the first run
   B->A.alloc(std::max<unsigned long long>(cap, 1), st);
   B->Q.alloc(std::max<unsigned long long>(cap, 1), st);
   B->D.alloc(std::max<unsigned long long>(cap, 1), st);
@@ -816,17 +846,24 @@ static void plan(fg_batch* B, const fg_batch_options* opt) {
   B->bin_cnt.alloc(nbins_max + 1, st);
   B->bin_off.alloc(nbins_max + 1, st);
   B->bin_cur.alloc(nbins_max + 1, st);
-  B->item_cap = std::max<unsigned long long>(cap * 6, 1);
+  B->item_cap = std::max<unsigned long long>(cap * 8, 1);
   B->bin_items.alloc(B->item_cap, st);
   B->exposure.alloc(std::max<unsigned long long>(eo, 1), st);
   B->d_neg.alloc(std::max<unsigned long long>(oo, 1), st);
   B->counter.alloc(1, st);
+  FG_REQUIRE(pb < 0xffffffffull && B->npcells < 0xffffffffull, "batch too large: photon count");
+  B->pcnt.alloc(B->npcells + 1, st);
+  B->poff.alloc(B->npcells + 1, st);
+  B->pcur.alloc(B->npcells + 1, st);
+  B->porder.alloc(std::max<unsigned long long>(pb, 1), st);
   B->dstats.alloc(4, st);
   FG_CUDA(cudaMemsetAsync(B->exposure.p, 0, B->exposure.n * sizeof(float), st));
   size_t b1 = 0, b2 = 0;
   FG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, b1, B->flags.p, B->slot_scan.p, static_cast<int64_t>(sb + 1), st));
   FG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, b2, B->bin_cnt.p, B->bin_off.p, static_cast<int64_t>(nbins_max + 1), st));
-  B->cub_bytes = std::max(b1, b2);
+  size_t b3 = 0;
+  FG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, b3, B->pcnt.p, B->poff.p, static_cast<int64_t>(B->npcells + 1), st));
+  B->cub_bytes = std::max(std::max(b1, b2), b3);
   B->cub_tmp.alloc(std::max<size_t>(B->cub_bytes, 1), st);
   for (auto& x : B->ev) FG_CUDA(cudaEventCreate(&x));
   layout_bins(B, bin0);
@@ -915,8 +952,11 @@ fg_status fg_batch_create(fg_engine* e, const fg_tile_params* tiles, uint32_t nt
     B->ntiles = ntiles;
     B->params.assign(tiles, tiles + ntiles);
     plan(B.get(), opt);
-    if (opt && opt->autotune) autotune(B.get(), e->stream);
-    if (B->use_graph) capture(B.get());
+    if (opt && opt->autotune) {
+      B->tune_pending = true;  // tuned on the first run's exposure, then captured
+    } else if (B->use_graph) {
+      capture(B.get());
+    }
     *out = B.release();
   });
 }
@@ -956,10 +996,19 @@ fg_status fg_batch_density_device(fg_batch* b, uint32_t tile, const float** ptr)
   return FG_OK;
 }
 
+// First run of an autotuned batch: time the candidates on the exposure now set, then capture.
+static void finish_setup(fg_batch* B) {
+  if (!B->tune_pending) return;
+  autotune(B, B->e->stream);
+  if (B->use_graph) capture(B);
+  B->tune_pending = false;
+}
+
 fg_status fg_batch_run(fg_batch* b) {
   if (!b) return FG_ERR_INVALID_ARG;
   return guard(b->e, [&] {
     cudaStream_t st = b->e->stream;
+    finish_setup(b);
     if (b->exec) {
       FG_CUDA(cudaGraphLaunch(b->exec, st));
     } else {
@@ -996,9 +1045,9 @@ fg_status fg_batch_wait(fg_batch* b, fg_batch_stats* stats) {
     s.transport_blocks = b->tr_blocks;
     s.scan_bin_px = b->bin_px;
     s.graph = b->exec ? 1u : 0u;
-    // Own kernels per run: Bridson x4, count + thin + flags, emit, set_n, Karras + fit, transport,
+    // Own kernels per run: Bridson x4, count + thin + flags, emit, set_n, Karras + fit, photon order x2, transport,
     // maxdim + threshold + link + roots + finalize, two bin passes, scan (CUB scans not counted).
-    s.kernel_launches = 4 + 3 + 1 + 1 + 2 + 1 + 5 + 2 + 1;
+    s.kernel_launches = 4 + 3 + 1 + 1 + 2 + 2 + 1 + 5 + 2 + 1;
     b->stats = s;
     if (stats) *stats = s;
   });
@@ -1052,6 +1101,7 @@ fg_status fg_batch_time(fg_batch* b, uint32_t steps, double* ms) {
   if (!b || !ms || steps == 0) return FG_ERR_INVALID_ARG;
   return guard(b->e, [&] {
     cudaStream_t st = b->e->stream;
+    finish_setup(b);
     FG_CUDA(cudaStreamSynchronize(st));
     FG_CUDA(cudaEventRecord(b->ev[6], st));
     for (uint32_t i = 0; i < steps; ++i) {

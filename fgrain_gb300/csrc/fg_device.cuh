@@ -72,8 +72,8 @@ struct CrystalsView {
 };
 
 // LBVH node, 64 bytes: the boxes of both children plus their indices.  A child index >= 0 is an
-// internal node; a negative index ~s is crystal s.  Leaf boxes bound the region where a crystal
-// can be hit (its shape cut by its own max_dim box), rounded outward.
+// internal node; a negative index ~s is crystal s.  Leaf boxes bound the crystal's shape (oriented
+// cube or ellipsoid), rounded outward.
 struct __align__(16) Node {
   float4 a;  // l.lo.x l.lo.y l.lo.z l.hi.x
   float4 b;  // l.hi.y l.hi.z r.lo.x r.lo.y
@@ -269,13 +269,62 @@ __device__ __forceinline__ bool fcanonical_hit(float4 a, float4 q, float4 d, flo
   return false;
 }
 
-// Error word bits written by kernels (read back by the host after each call).
+// 2D Morton interleave of 16-bit coordinates.
+__host__ __device__ inline uint32_t morton2_spread(uint32_t v) {
+  v &= 0xffffu;
+  v = (v | (v << 8)) & 0x00ff00ffu;
+  v = (v | (v << 4)) & 0x0f0f0f0fu;
+  v = (v | (v << 2)) & 0x33333333u;
+  v = (v | (v << 1)) & 0x55555555u;
+  return v;
+}
+__host__ __device__ inline uint32_t morton2_compact(uint32_t v) {
+  v &= 0x55555555u;
+  v = (v | (v >> 1)) & 0x33333333u;
+  v = (v | (v >> 2)) & 0x0f0f0f0fu;
+  v = (v | (v >> 4)) & 0x00ff00ffu;
+  v = (v | (v >> 8)) & 0x0000ffffu;
+  return v;
+}
+
+// Error word bits written by kernels (read back by the host after each call).  The error record
+// is four words: the bits, then (for ERR_BAD_INDEX) the site and two values of the first failed
+// index check.
 enum : uint32_t {
   ERR_HIT_OVERFLOW = 1u << 0,
   ERR_STACK_OVERFLOW = 1u << 1,
   ERR_SPIN_LIMIT = 1u << 2,
   ERR_LIST_OVERFLOW = 1u << 3,
   ERR_BAD_INPUT = 1u << 4,
+  ERR_BAD_INDEX = 1u << 5,
 };
+constexpr int ERR_WORDS = 4;
+
+// Sites of index checks (the second word of the error record).
+enum : uint32_t {
+  SITE_SYN_REGION = 1,   // synthesis: candidate neighbourhood outside the staged region
+  SITE_SYN_COMMIT = 2,   // synthesis: accepted point outside the staged region
+  SITE_SYN_ACTIVE = 3,   // synthesis: active list full
+  SITE_PHOTON_CELL = 4,  // photon ordering: emission cell out of range
+  SITE_PHOTON_SLOT = 5,  // photon ordering: slot past the photon count
+  SITE_PHOTON_ID = 6,    // transport: ordered photon id past the photon count
+  SITE_NODE = 7,         // LBVH walk: internal node index out of range
+  SITE_LEAF = 8,         // LBVH walk: crystal index out of range
+};
+
+__device__ __noinline__ static void record_bad_index(uint32_t* err, uint32_t site, uint32_t a, uint32_t b) {
+  atomicOr(err, ERR_BAD_INDEX);
+  if (atomicCAS(err + 1, 0u, site) == 0u) {
+    err[2] = a;
+    err[3] = b;
+  }
+}
+
+// Guard of an index computed from data: on failure the access is to be skipped and the failure is
+// recorded in the error record.
+__device__ __forceinline__ bool index_ok(bool ok, uint32_t* err, uint32_t site, uint32_t a, uint32_t b) {
+  if (!ok) record_bad_index(err, site, a, b);
+  return ok;
+}
 
 }  // namespace fg

@@ -17,14 +17,18 @@ void replay_rays(fg_engine* e, const fg_emulsion* em, const double* org_host,
                  uint32_t* ids_host, size_t id_cap, size_t* nhits, double* chord_host);
 
 void check_error_word(fg_engine* e) {
-  uint32_t w = 0;
-  FG_CUDA(cudaMemcpyAsync(&w, e->d_err, sizeof(w), cudaMemcpyDeviceToHost, e->stream));
+  uint32_t rec[ERR_WORDS] = {};
+  FG_CUDA(cudaMemcpyAsync(rec, e->d_err, sizeof(rec), cudaMemcpyDeviceToHost, e->stream));
   FG_CUDA(cudaStreamSynchronize(e->stream));
+  const uint32_t w = rec[0];
   e->timings.error_word = w;
   if (!w) return;
-  FG_CUDA(cudaMemsetAsync(e->d_err, 0, sizeof(uint32_t), e->stream));
+  FG_CUDA(cudaMemsetAsync(e->d_err, 0, sizeof(rec), e->stream));
   FG_CUDA(cudaStreamSynchronize(e->stream));
-  std::string m = "device error word 0x" + std::to_string(w) + ":";
+  std::string m = "device error word " + std::to_string(w) + ":";
+  if (w & ERR_BAD_INDEX)
+    m += " index check failed at site " + std::to_string(rec[1]) + " (values " + std::to_string(rec[2]) + ", " +
+         std::to_string(rec[3]) + "), access skipped;";
   if (w & ERR_HIT_OVERFLOW) m += " hit list overflow;";
   if (w & ERR_STACK_OVERFLOW) m += " traversal stack overflow;";
   if (w & ERR_LIST_OVERFLOW) m += " work list overflow;";
@@ -130,9 +134,9 @@ fg_status fg_engine_create(int device, fg_engine** out) {
     FG_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
     uint64_t thr = UINT64_MAX;
     FG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
-    FG_CUDA(cudaMalloc(&e->d_err, sizeof(uint32_t)));
+    FG_CUDA(cudaMalloc(&e->d_err, ERR_WORDS * sizeof(uint32_t)));
     FG_CUDA(cudaMalloc(&e->d_stats, 8 * sizeof(unsigned long long)));
-    FG_CUDA(cudaMemset(e->d_err, 0, sizeof(uint32_t)));
+    FG_CUDA(cudaMemset(e->d_err, 0, ERR_WORDS * sizeof(uint32_t)));
     FG_CUDA(cudaMemset(e->d_stats, 0, 8 * sizeof(unsigned long long)));
     e->timer.init();
   } catch (const Error& x) {

@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const ScanTile* __restric
   }
   long long Lfix = 0;  // chord sum (sigma-weighted when per crystal), 2^-40 um units
   uint32_t nh = 0, nfb = 0;
-  const uint32_t b0 = t.bin_off[bin], b1 = t.bin_off[bin + 1];
+  const uint32_t b0 = min(t.bin_off[bin], t.items_cap), b1 = min(t.bin_off[bin + 1], t.items_cap);
   const bool per_crystal = t.sigma_c != nullptr;
   for (uint32_t base = b0; base < b1; base += SCAN_CH) {
     const uint32_t cnt = min(static_cast<uint32_t>(SCAN_CH), b1 - base);
@@ -419,6 +419,7 @@ void scan(fg_engine* e, const fg_emulsion* em, const fg_scan_cfg& cfg, uint64_t 
   if (em->n) k_bin_fill<<<grid_for(em->n, 256), 256, 0, st>>>(t, off.p, cur.p, items.p);
   t.bin_off = off.p;
   t.bin_items = items.p;
+  t.items_cap = total;
   DBuf<ScanTile> td(1, st);
   FG_CUDA(cudaMemcpyAsync(td.p, &t, sizeof(ScanTile), cudaMemcpyHostToDevice, st));
   // Whole warps only: the closing reductions shuffle across all 32 lanes.

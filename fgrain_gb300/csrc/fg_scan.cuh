@@ -42,6 +42,7 @@ struct ScanTile {
   uint32_t w, h, g, spp, bin_px, nbx, nby, n;
   float sigma;
   int mode;
+  uint32_t items_cap;  // entries of bin_items; lists past it were dropped (overflow flagged)
 };
 
 // Stratum ray origin in FP64 exactly as the reference forms it (transmittance.rs:102-120).

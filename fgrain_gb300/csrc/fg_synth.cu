@@ -23,26 +23,43 @@ __device__ __forceinline__ int find_tile_ull(const SynthTile* tiles, int ntiles,
   return lo;
 }
 
-// Exact test of a fixed-point candidate against the staged grid (5x5x5 cells, corners skipped:
-// their nearest point is sqrt(3) cells = r away or more).
-__device__ __forceinline__ bool syn_free(const uint32_t* grid, int rx, int ry, int rz, int X, int Y,
-                                         int Z, int cx, int cy, int cz) {
-#pragma unroll 1
-  for (int dz = -2; dz <= 2; ++dz)
+// Exact test of a fixed-point candidate against the staged grid: every point within r.  Rows of
+// the 5x5x5 neighbourhood are scanned through occupancy bitmasks (one 32-bit word per (y, z) row
+// of the staged region), so only occupied cells are loaded; on the four (y, z) corner rows only
+// the middle three cells can hold a point within r = sqrt(3) cells.
+__device__ __forceinline__ bool syn_free(const uint32_t* grid, const uint32_t* occ, int nz, int rx, int ry,
+                                         int rz, int X, int Y, int Z, int cx, int cy, int cz, uint32_t* err) {
+  // The neighbourhood must lie inside the staged region (it does for candidates within 2r of a
+  // point of the column); a candidate that fails the check is rejected.
+  if (!index_ok(rx >= 2 && rx <= SYN_R - 3 && ry >= 2 && ry <= SYN_R - 3 && rz >= 2 && rz <= nz - 3, err,
+                SITE_SYN_REGION, static_cast<uint32_t>(rx | (ry << 8) | (rz << 16)), blockIdx.x))
+    return false;
 #pragma unroll
-    for (int dy = -2; dy <= 2; ++dy)
+  for (int dz = -2; dz <= 2; ++dz) {
 #pragma unroll
-      for (int dx = -2; dx <= 2; ++dx) {
-        if ((dx == -2 || dx == 2) && (dy == -2 || dy == 2) && (dz == -2 || dz == 2)) continue;
+    for (int dy = -2; dy <= 2; ++dy) {
+      const bool corner = (dy == -2 || dy == 2) && (dz == -2 || dz == 2);
+      const int lo = corner ? rx - 1 : rx - 2;
+      const uint32_t width = corner ? 3u : 5u;
+      uint32_t bits = (occ[(rz + dz) * SYN_R + (ry + dy)] >> lo) & ((1u << width) - 1u);
+      while (bits) {
+        const int k = __ffs(bits) - 1;
+        bits &= bits - 1;
+        const int dx = lo + k - rx;
         const uint32_t w = grid[((rz + dz) * SYN_R + (ry + dy)) * SYN_R + (rx + dx)];
-        if (w & OCC) {
-          const int ex = (cx + dx) * SYN_Q + static_cast<int>(w & 1023u) - X;
-          const int ey = (cy + dy) * SYN_Q + static_cast<int>((w >> 10) & 1023u) - Y;
-          const int ez = (cz + dz) * SYN_Q + static_cast<int>((w >> 20) & 1023u) - Z;
-          if (ex * ex + ey * ey + ez * ez < SYN_R2) return false;
-        }
+        const int ex = (cx + dx) * SYN_Q + static_cast<int>(w & 1023u) - X;
+        const int ey = (cy + dy) * SYN_Q + static_cast<int>((w >> 10) & 1023u) - Y;
+        const int ez = (cz + dz) * SYN_Q + static_cast<int>((w >> 20) & 1023u) - Z;
+        if (ex * ex + ey * ey + ez * ez < SYN_R2) return false;
       }
+    }
+  }
   return true;
+}
+
+__device__ __forceinline__ uint32_t syn_word(int X, int Y, int Z) {
+  return OCC | (static_cast<uint32_t>(Z & 1023) << 20) | (static_cast<uint32_t>(Y & 1023) << 10) |
+         static_cast<uint32_t>(X & 1023);
 }
 
 __global__ void __launch_bounds__(SYN_WARPS * 32) k_bridson(const SynthTile* __restrict__ tiles,
@@ -50,13 +67,14 @@ __global__ void __launch_bounds__(SYN_WARPS * 32) k_bridson(const SynthTile* __r
                                                             uint32_t* __restrict__ cells,
                                                             uint32_t* err) {
   extern __shared__ uint32_t syn_sm[];
-  uint32_t* grid = syn_sm;                                             // SYN_R^2 * nz
-  uint16_t* active = reinterpret_cast<uint16_t*>(grid + SYN_R * SYN_R * nz);  // SYN_B^2 * (nz-4)
-  __shared__ int s_nact, s_nrem, s_wsum[SYN_WARPS];
+  uint32_t* grid = syn_sm;                                   // SYN_R^2 * nz cell words
+  uint32_t* occ = grid + SYN_R * SYN_R * nz;                 // SYN_R * nz row masks
+  uint16_t* active = reinterpret_cast<uint16_t*>(occ + SYN_R * nz);  // SYN_B^2 * (nz - 4)
+  __shared__ int s_nact, s_wsum[SYN_WARPS];
   __shared__ int s_pick[SYN_WARPS];
   __shared__ unsigned s_vmask[SYN_WARPS];
-  __shared__ int s_cand[SYN_WARPS][SYN_K][3];
-  __shared__ int s_rem[SYN_WARPS];
+  __shared__ int s_win[SYN_WARPS][3];
+  __shared__ int s_ok[SYN_WARPS];
 
   // Column of this CTA: tile, then the j-th column of this colour class in that tile.
   int lo = 0, hi = ntiles - 1;
@@ -75,9 +93,10 @@ __global__ void __launch_bounds__(SYN_WARPS * 32) k_bridson(const SynthTile* __r
   const uint32_t colkey = by * t.nbx + bx;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int ncell = SYN_R * SYN_R * nz;
+  const int acap = SYN_B * SYN_B * (nz - 4);  // active list capacity: one entry per column cell
   uint32_t* tc = cells + t.cell_base;
 
-  // Stage the region (column + halo) of the cell grid.
+  // Stage the region (column + halo) of the cell grid, then its row masks.
   for (int i = tid; i < ncell; i += blockDim.x) {
     const int rx = i % SYN_R, ry = (i / SYN_R) % SYN_R, rz = i / (SYN_R * SYN_R);
     const int gx = ox + rx, gy = oy + ry, gz = rz - 2;
@@ -88,24 +107,29 @@ __global__ void __launch_bounds__(SYN_WARPS * 32) k_bridson(const SynthTile* __r
   }
   if (tid == 0) s_nact = 0;
   __syncthreads();
+  for (int r = tid; r < SYN_R * nz; r += blockDim.x) {
+    uint32_t m = 0;
+    for (int x = 0; x < SYN_R; ++x) m |= (grid[r * SYN_R + x] & OCC) ? (1u << x) : 0u;
+    occ[r] = m;
+  }
   // Active list: the column's points in cell order (deterministic block-wide compaction).
   const int bw = x1 - x0, bh = y1 - y0;
   const int bcells = bw * bh * gd;
   for (int base = 0; base < bcells; base += blockDim.x) {
     const int i = base + tid;
     int ridx = 0;
-    bool occ = false;
+    bool o = false;
     if (i < bcells) {
       const int lx = i % bw, ly = (i / bw) % bh, lz = i / (bw * bh);
       ridx = ((lz + 2) * SYN_R + (ly + SYN_HALO)) * SYN_R + (lx + SYN_HALO);
-      occ = (grid[ridx] & OCC) != 0;
+      o = (grid[ridx] & OCC) != 0;
     }
-    const unsigned m = __ballot_sync(0xffffffffu, occ);
+    const unsigned m = __ballot_sync(0xffffffffu, o);
     if (lane == 0) s_wsum[warp] = __popc(m);
     __syncthreads();
     int off = s_nact;
     for (int w = 0; w < warp; ++w) off += s_wsum[w];
-    if (occ) active[off + __popc(m & ((1u << lane) - 1u))] = static_cast<uint16_t>(ridx);
+    if (o) active[off + __popc(m & ((1u << lane) - 1u))] = static_cast<uint16_t>(ridx);
     __syncthreads();
     if (tid == 0)
       for (int w = 0; w < SYN_WARPS; ++w) s_nact += s_wsum[w];
@@ -121,11 +145,11 @@ __global__ void __launch_bounds__(SYN_WARPS * 32) k_bridson(const SynthTile* __r
       if (X >= static_cast<int>(t.XW) || Y >= static_cast<int>(t.YW) || Z >= static_cast<int>(t.ZW)) continue;
       const int cx = X >> 10, cy = Y >> 10, cz = Z >> 10;
       const int rx = cx - ox, ry = cy - oy, rz = cz + 2;
-      if (!syn_free(grid, rx, ry, rz, X, Y, Z, cx, cy, cz)) continue;
+      if (!syn_free(grid, occ, nz, rx, ry, rz, X, Y, Z, cx, cy, cz, err)) continue;
       const int ridx = (rz * SYN_R + ry) * SYN_R + rx;
-      grid[ridx] = OCC | (static_cast<uint32_t>(Z & 1023) << 20) | (static_cast<uint32_t>(Y & 1023) << 10) |
-                   static_cast<uint32_t>(X & 1023);
-      active[s_nact++] = static_cast<uint16_t>(ridx);
+      grid[ridx] = syn_word(X, Y, Z);
+      occ[rz * SYN_R + ry] |= 1u << rx;
+      if (index_ok(s_nact < acap, err, SITE_SYN_ACTIVE, s_nact, blockIdx.x)) active[s_nact++] = static_cast<uint16_t>(ridx);
       break;
     }
   }
@@ -138,7 +162,8 @@ __global__ void __launch_bounds__(SYN_WARPS * 32) k_bridson(const SynthTile* __r
       if (tid == 0) atomicOr(err, ERR_SPIN_LIMIT);
       break;
     }
-    // One Bridson step per warp on a random active point (poisson.rs:59-129).
+    // One Bridson step per warp on a random active point (poisson.rs:59-129): 30 candidates in
+    // the shell [r, 2r], one per lane; the lowest valid lane is the step's winner.
     if (lane == 0) {
       const P4 r = philox(static_cast<uint32_t>(iter), static_cast<uint32_t>(warp), colkey, TAG_PICK, t.k0, t.k1);
       s_pick[warp] = static_cast<int>((static_cast<unsigned long long>(r.x) * static_cast<unsigned>(nact)) >> 32);
@@ -171,53 +196,60 @@ __global__ void __launch_bounds__(SYN_WARPS * 32) k_bridson(const SynthTile* __r
         Z = static_cast<int>(floorf(fz * SYN_Q));
         if (X < static_cast<int>(t.XW) && Y < static_cast<int>(t.YW) && Z < static_cast<int>(t.ZW)) {
           const int cx = X >> 10, cy = Y >> 10, cz = Z >> 10;
-          valid = syn_free(grid, cx - ox, cy - oy, cz + 2, X, Y, Z, cx, cy, cz);
+          valid = syn_free(grid, occ, nz, cx - ox, cy - oy, cz + 2, X, Y, Z, cx, cy, cz, err);
         }
       }
-      s_cand[warp][lane][0] = X;
-      s_cand[warp][lane][1] = Y;
-      s_cand[warp][lane][2] = Z;
     }
     const unsigned vm = __ballot_sync(0xffffffffu, valid);
+    if (vm && lane == __ffs(vm) - 1) {
+      s_win[warp][0] = X;
+      s_win[warp][1] = Y;
+      s_win[warp][2] = Z;
+    }
     if (lane == 0) s_vmask[warp] = vm;
     __syncthreads();
+    // A winner commits unless it lies within r of the winner of an earlier warp of this round
+    // (then its point simply stays active for a later step).
+    if (tid < SYN_WARPS) {
+      bool ok = s_vmask[tid] != 0;
+      for (int w = 0; w < tid && ok; ++w) {
+        if (!s_vmask[w]) continue;
+        const int ex = s_win[tid][0] - s_win[w][0], ey = s_win[tid][1] - s_win[w][1], ez = s_win[tid][2] - s_win[w][2];
+        ok = ex * ex + ey * ey + ez * ez >= SYN_R2;
+      }
+      s_ok[tid] = ok;
+    }
+    __syncthreads();
     if (tid == 0) {
-      int cx_[SYN_WARPS], cy_[SYN_WARPS], cz_[SYN_WARPS];
-      int ncom = 0, nrem = 0;
+      int rem[SYN_WARPS];
+      int nrem = 0;
       for (int w = 0; w < SYN_WARPS; ++w) {
-        unsigned m = s_vmask[w];
-        if (m == 0) {
-          s_rem[nrem++] = s_pick[w];  // 30 misses: the point retires
+        if (!s_vmask[w]) {
+          rem[nrem++] = s_pick[w];  // 30 misses: the point retires
           continue;
         }
-        while (m) {
-          const int l = __ffs(m) - 1;
-          m &= m - 1;
-          const int CX = s_cand[w][l][0], CY = s_cand[w][l][1], CZ = s_cand[w][l][2];
-          bool ok = true;
-          for (int k = 0; k < ncom && ok; ++k) {
-            const int ex = CX - cx_[k], ey = CY - cy_[k], ez = CZ - cz_[k];
-            ok = ex * ex + ey * ey + ez * ez >= SYN_R2;
-          }
-          if (!ok) continue;
-          const int ccx = CX >> 10, ccy = CY >> 10, ccz = CZ >> 10;
-          const int ridx = ((ccz + 2) * SYN_R + (ccy - oy)) * SYN_R + (ccx - ox);
-          grid[ridx] = OCC | (static_cast<uint32_t>(CZ & 1023) << 20) | (static_cast<uint32_t>(CY & 1023) << 10) |
-                       static_cast<uint32_t>(CX & 1023);
-          cx_[ncom] = CX; cy_[ncom] = CY; cz_[ncom] = CZ;
-          ++ncom;
-          if (ccx >= x0 && ccx < x1 && ccy >= y0 && ccy < y1) active[s_nact++] = static_cast<uint16_t>(ridx);
-          break;
-        }
+        if (!s_ok[w]) continue;
+        const int CX = s_win[w][0], CY = s_win[w][1], CZ = s_win[w][2];
+        const int ccx = CX >> 10, ccy = CY >> 10, ccz = CZ >> 10;
+        const int rx = ccx - ox, ry = ccy - oy, rz = ccz + 2;
+        if (!index_ok(rx >= 0 && rx < SYN_R && ry >= 0 && ry < SYN_R && rz >= 0 && rz < nz, err, SITE_SYN_COMMIT,
+                      static_cast<uint32_t>(rx | (ry << 8) | (rz << 16)), blockIdx.x))
+          continue;
+        const int ridx = (rz * SYN_R + ry) * SYN_R + rx;
+        grid[ridx] = syn_word(CX, CY, CZ);
+        occ[rz * SYN_R + ry] |= 1u << rx;
+        if (ccx >= x0 && ccx < x1 && ccy >= y0 && ccy < y1 &&
+            index_ok(s_nact < acap, err, SITE_SYN_ACTIVE, s_nact, blockIdx.x))
+          active[s_nact++] = static_cast<uint16_t>(ridx);
       }
       // Retire in descending index order (swap-remove keeps lower indices valid); skip repeats.
       for (int a = 1; a < nrem; ++a)
-        for (int b = a; b > 0 && s_rem[b] > s_rem[b - 1]; --b) {
-          const int tmp = s_rem[b]; s_rem[b] = s_rem[b - 1]; s_rem[b - 1] = tmp;
+        for (int b = a; b > 0 && rem[b] > rem[b - 1]; --b) {
+          const int tmp = rem[b]; rem[b] = rem[b - 1]; rem[b - 1] = tmp;
         }
       for (int a = 0; a < nrem; ++a) {
-        if (a > 0 && s_rem[a] == s_rem[a - 1]) continue;
-        active[s_rem[a]] = active[--s_nact];
+        if (a > 0 && rem[a] == rem[a - 1]) continue;
+        active[rem[a]] = active[--s_nact];
       }
     }
   }
@@ -338,13 +370,14 @@ __global__ void k_emit(const SynthTile* __restrict__ tiles, int ntiles, unsigned
 
 namespace fg {
 
+size_t bridson_smem(int gdmax);
+
 // Host wrappers (launch on `st`; all buffers preallocated so the sequence can be graph-captured).
 void launch_bridson(const SynthTile* tiles, int ntiles, int color, unsigned ncols, int gdmax,
                     uint32_t* cells, uint32_t* err, cudaStream_t st) {
   if (ncols == 0) return;
   const int nz = gdmax + 4;
-  const size_t smem = static_cast<size_t>(SYN_R) * SYN_R * nz * sizeof(uint32_t) +
-                      static_cast<size_t>(SYN_B) * SYN_B * gdmax * sizeof(uint16_t);
+  const size_t smem = bridson_smem(gdmax);
   FG_CUDA(cudaFuncSetAttribute(k_bridson, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   k_bridson<<<ncols, SYN_WARPS * 32, smem, st>>>(tiles, ntiles, color, nz, cells, err);
   FG_CUDA(cudaGetLastError());
@@ -352,6 +385,7 @@ void launch_bridson(const SynthTile* tiles, int ntiles, int color, unsigned ncol
 
 size_t bridson_smem(int gdmax) {
   return static_cast<size_t>(SYN_R) * SYN_R * (gdmax + 4) * sizeof(uint32_t) +
+         static_cast<size_t>(SYN_R) * (gdmax + 4) * sizeof(uint32_t) +
          static_cast<size_t>(SYN_B) * SYN_B * gdmax * sizeof(uint16_t);
 }
 

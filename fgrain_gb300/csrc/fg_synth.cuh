@@ -6,9 +6,9 @@
 // of one class are a column apart, so they never touch the same cells.  Each column runs Bridson
 // (k = 30 candidates in the shell [r, 2r], first valid candidate wins) from the points already
 // inside it (spilled in by earlier classes) or from one random seed; candidates may spill up to
-// 2r out of the column.  Eight warps per column each take a Bridson step on a randomly picked
-// active point; one thread then commits the steps in warp order, re-checking each winner
-// against the winners committed before it.  Positions are fixed point (1/1024 of a cell) so
+// 2r out of the column.  Sixteen warps per column each take a Bridson step on a randomly picked
+// active point; a step's winner commits unless it lies within r of an earlier warp's winner of
+// the same round (its point then stays active for a later step).  Positions are fixed point (1/1024 of a cell) so
 // every distance test is exact integer arithmetic.
 //
 // Bridson started from many seeds packs ~0.3-0.6 % denser than from one, so each tile is then
@@ -23,7 +23,7 @@ namespace fg {
 constexpr int SYN_B = 12;        // column edge in cells
 constexpr int SYN_HALO = 6;      // spill (4) + check reach (2)
 constexpr int SYN_R = SYN_B + 2 * SYN_HALO;  // staged region edge (24)
-constexpr int SYN_WARPS = 8;
+constexpr int SYN_WARPS = 16;
 constexpr int SYN_K = 30;        // Bridson's k
 constexpr int32_t SYN_Q = 1024;  // fixed-point steps per cell
 constexpr int32_t SYN_R2 = 3 * SYN_Q * SYN_Q;  // r^2 with r = sqrt(3) cells
@@ -53,22 +53,5 @@ struct __align__(16) SynthTile {
   float aspect;                  // tabular aspect ratio
   int morph;
 };
-
-__host__ __device__ inline uint32_t morton2_spread(uint32_t v) {
-  v &= 0xffffu;
-  v = (v | (v << 8)) & 0x00ff00ffu;
-  v = (v | (v << 4)) & 0x0f0f0f0fu;
-  v = (v | (v << 2)) & 0x33333333u;
-  v = (v | (v << 1)) & 0x55555555u;
-  return v;
-}
-__host__ __device__ inline uint32_t morton2_compact(uint32_t v) {
-  v &= 0x55555555u;
-  v = (v | (v >> 1)) & 0x33333333u;
-  v = (v | (v >> 2)) & 0x0f0f0f0fu;
-  v = (v | (v >> 4)) & 0x00ff00ffu;
-  v = (v | (v >> 8)) & 0x0000ffffu;
-  return v;
-}
 
 }  // namespace fg

@@ -13,33 +13,94 @@
 namespace fg {
 
 // ---------------------------------------------------------------------------------------------
-// Production (FP32) kernel.
-__global__ void __launch_bounds__(256) k_transport(const TileDesc* __restrict__ tiles, int ntiles,
-                                                  unsigned long long total,
-                                                  unsigned long long* next, uint32_t* err,
-                                                  unsigned long long* stats) {
+// Production kernel with lane refill: each loop turn every live lane runs one bounce; lanes whose
+// packet died take the next photon of the (optionally position-ordered) queue, so the warp stays
+// full until the queue is empty.
+__global__ void __launch_bounds__(256) k_transport_refill(const TileDesc* __restrict__ tiles, int ntiles,
+                                                         unsigned long long total,
+                                                         const uint32_t* __restrict__ order,
+                                                         unsigned long long* next, uint32_t* err,
+                                                         unsigned long long* stats) {
   const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  HitS hits[HMAX];
+  Photon ph;
+  int tile = 0;
+  bool alive = false, done = false;
   unsigned long long my_hits = 0;
   for (;;) {
-    unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(next, 32ull);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (base >= total) break;
-    const unsigned long long gid = base + lane;
-    if (gid < total) {
-      int lo = 0, hi = ntiles - 1;
-      while (lo < hi) {  // last tile whose first photon is <= gid
-        const int mid = (lo + hi + 1) >> 1;
-        if (tiles[mid].photon_base <= gid) lo = mid; else hi = mid - 1;
+    unsigned need = __ballot_sync(0xffffffffu, !alive && !done);
+    while (need) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(next, static_cast<unsigned long long>(__popc(need)));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (!alive && !done) {
+        const unsigned long long g = base + __popc(need & lt);
+        if (g >= total) {
+          done = true;
+        } else {
+          unsigned long long gid = order ? order[g] : g;
+          if (!index_ok(gid < total, err, SITE_PHOTON_ID, static_cast<uint32_t>(gid), static_cast<uint32_t>(g)))
+            gid = g;
+          int lo = 0, hi = ntiles - 1;
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (tiles[mid].photon_base <= gid) lo = mid; else hi = mid - 1;
+          }
+          tile = lo;
+          alive = emit_photon(tiles[lo], static_cast<uint32_t>(gid - tiles[lo].photon_base), ph);
+        }
       }
-      const TileDesc& t = tiles[lo];
-      my_hits += trace_photon(t, static_cast<uint32_t>(gid - t.photon_base), err);
+      need = __ballot_sync(0xffffffffu, !alive && !done);
+    }
+    if (!__any_sync(0xffffffffu, alive)) break;
+    if (alive) {
+      uint32_t nh = 0;
+      alive = photon_bounce(tiles[tile], ph, hits, err, nh);
+      my_hits += nh;
     }
   }
   if (stats) {
     for (int o = 16; o > 0; o >>= 1) my_hits += __shfl_down_sync(0xffffffffu, my_hits, o);
     if (lane == 0 && my_hits) atomicAdd(&stats[0], my_hits);
   }
+}
+
+// Photon ordering: a counting sort of photon ids by the coarse emission cell (Morton order inside
+// each tile), so neighbouring lanes trace neighbouring packets.  Pass 1 (off == null) counts,
+// pass 2 scatters.  The order only changes which lane traces a photon, never its result.
+__global__ void k_photon_sort(const TileDesc* __restrict__ tiles, int ntiles, unsigned long long total,
+                              unsigned long long ncells, uint32_t* cnt, const uint32_t* off, uint32_t* cur,
+                              uint32_t* order, uint32_t* err) {
+  const unsigned long long gid = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+  if (gid >= total) return;
+  int lo = 0, hi = ntiles - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tiles[mid].photon_base <= gid) lo = mid; else hi = mid - 1;
+  }
+  const TileDesc& t = tiles[lo];
+  const uint32_t id = static_cast<uint32_t>(gid - t.photon_base);
+  const P4 e0 = philox(id, 0, 0, TAG_EMIT, t.k0, t.k1);
+  const uint32_t mx = (1u << t.pcell_bits) - 1u;
+  const uint32_t cx = min(static_cast<uint32_t>(uf(e0.x) * t.W * (1.0f / PHOTON_CELL_UM)), mx);
+  const uint32_t cy = min(static_cast<uint32_t>(uf(e0.y) * t.H * (1.0f / PHOTON_CELL_UM)), mx);
+  const uint32_t cell = t.pcell_base + (morton2_spread(cx) | (morton2_spread(cy) << 1));
+  if (!index_ok(cell < ncells, err, SITE_PHOTON_CELL, cell, static_cast<uint32_t>(gid))) return;
+  if (!off) {
+    atomicAdd(&cnt[cell], 1u);
+  } else {
+    const unsigned long long k = off[cell] + atomicAdd(&cur[cell], 1u);
+    if (index_ok(k < total, err, SITE_PHOTON_SLOT, static_cast<uint32_t>(k), cell)) order[k] = static_cast<uint32_t>(gid);
+  }
+}
+
+void launch_photon_sort(const TileDesc* tiles_dev, int ntiles, unsigned long long total, unsigned long long ncells,
+                        uint32_t* cnt, const uint32_t* off, uint32_t* cur, uint32_t* order, uint32_t* err,
+                        cudaStream_t st) {
+  if (total == 0) return;
+  k_photon_sort<<<grid_for(total, 256), 256, 0, st>>>(tiles_dev, ntiles, total, ncells, cnt, off, cur, order, err);
+  FG_CUDA(cudaGetLastError());
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -185,27 +246,15 @@ TileDesc make_tile_desc(const fg_emulsion* em, const float* tile_dev, uint32_t t
   return t;
 }
 
-void launch_transport(const TileDesc* tiles_dev, int ntiles, unsigned long long total,
-                      unsigned long long* counter, uint32_t* err, unsigned long long* stats,
-                      int sm_count, cudaStream_t st) {
-  if (total == 0) return;
-  FG_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
-  const unsigned long long warps = (total + 31) / 32;
-  unsigned blocks = static_cast<unsigned>(std::min<unsigned long long>((warps + 7) / 8, (unsigned long long)sm_count * 8));
-  blocks = std::max(blocks, 1u);
-  k_transport<<<blocks, 256, 0, st>>>(tiles_dev, ntiles, total, counter, err, stats);
-  FG_CUDA(cudaGetLastError());
-}
-
 void launch_transport_shape(const TileDesc* tiles_dev, int ntiles, unsigned long long total,
-                            unsigned long long* counter, uint32_t* err, unsigned long long* stats,
-                            unsigned blocks, unsigned threads, cudaStream_t st) {
+                            const uint32_t* order, unsigned long long* counter, uint32_t* err,
+                            unsigned long long* stats, unsigned blocks, unsigned threads, cudaStream_t st) {
   if (total == 0) return;
   FG_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
   const unsigned long long warps = (total + 31) / 32;
   const unsigned long long need = (warps * 32 + threads - 1) / threads;
   blocks = static_cast<unsigned>(std::max<unsigned long long>(std::min<unsigned long long>(blocks, need), 1));
-  k_transport<<<blocks, threads, 0, st>>>(tiles_dev, ntiles, total, counter, err, stats);
+  k_transport_refill<<<blocks, threads, 0, st>>>(tiles_dev, ntiles, total, order, counter, err, stats);
   FG_CUDA(cudaGetLastError());
 }
 
@@ -218,7 +267,8 @@ void expose(fg_engine* e, fg_emulsion* em, const float* tile_dev, uint32_t tw, u
   DBuf<TileDesc> td(1, st);
   DBuf<unsigned long long> ctr(1, st);
   FG_CUDA(cudaMemcpyAsync(td.p, &t, sizeof(TileDesc), cudaMemcpyHostToDevice, st));
-  launch_transport(td.p, 1, t.P, ctr.p, e->d_err, e->d_stats, e->sm_count, st);
+  launch_transport_shape(td.p, 1, t.P, nullptr, ctr.p, e->d_err, e->d_stats,
+                         static_cast<unsigned>(e->sm_count) * 4, 256, st);
 }
 
 void replay_segments(fg_engine* e, fg_emulsion* em, const fg_exposure_cfg& cfg, uint64_t seed,

@@ -19,6 +19,8 @@ struct __align__(16) TileDesc {
   unsigned long long photon_base;
   uint32_t n, tw, th, P;
   uint32_t stride;  // exposure row stride (floats); tiles may be windows of one image
+  uint32_t pcell_base;  // first photon-sort cell of this tile
+  uint32_t pcell_bits;  // photon-sort cells per axis = 2^bits (Morton order)
   float W, H, D;
   uint32_t k0, k1;
   float mu_t, albedo, g, r0, eff_r, theta_max, alpha;
@@ -27,13 +29,17 @@ struct __align__(16) TileDesc {
 
 // Stack walk of the LBVH: fn(s) is called for every crystal whose padded leaf box the ray
 // enters before tlim.  Both child boxes come with the parent, so each step is one node load.
+// With n > 0 the node and crystal indices read from the tree are checked against the n - 1
+// internal nodes and n crystals of an n-crystal tree (n = 0: unchecked).
 template <class F>
 __device__ __forceinline__ void walk_lbvh(const Node* __restrict__ nodes, float3 o, float3 inv,
-                                          float tlim, uint32_t* err, F&& fn) {
+                                          float tlim, uint32_t* err, F&& fn, uint32_t n = 0) {
+  const int nint = n > 1 ? static_cast<int>(n - 1) : 1;
   int stack[64];
   int sp = 0;
   int cur = 0;
   for (;;) {
+    if (n && !index_ok(cur >= 0 && cur < nint, err, SITE_NODE, static_cast<uint32_t>(cur), n)) break;
     const float4 na = __ldg(&nodes[cur].a);
     const float4 nb = __ldg(&nodes[cur].b);
     const float4 nc = __ldg(&nodes[cur].c);
@@ -44,11 +50,13 @@ __device__ __forceinline__ void walk_lbvh(const Node* __restrict__ nodes, float3
     slab(o, inv, nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, te, tx);
     bool hr = tx >= te && tx >= 0.0f && te <= tlim && nd.y != INT32_MIN;
     if (hl && nd.x < 0) {
-      fn(static_cast<uint32_t>(~nd.x));
+      const uint32_t s = static_cast<uint32_t>(~nd.x);
+      if (!n || index_ok(s < n, err, SITE_LEAF, s, n)) fn(s);
       hl = false;
     }
     if (hr && nd.y < 0) {
-      fn(static_cast<uint32_t>(~nd.y));
+      const uint32_t s = static_cast<uint32_t>(~nd.y);
+      if (!n || index_ok(s < n, err, SITE_LEAF, s, n)) fn(s);
       hr = false;
     }
     if (hl && hr) {
@@ -83,11 +91,6 @@ __device__ __forceinline__ double absorb64(double E, double path, double alpha, 
   return __dmul_rn(E, fmax(__dsub_rn(1.0, __dmul_rn(p, 0.9)), 0.05));
 }
 
-struct HitF {
-  float t0, t1;
-  uint32_t id, s;
-};
-
 // Adds n latent photons to crystal s, one atomic per distinct crystal among the active lanes.
 __device__ __forceinline__ void add_counts(uint32_t* counts, uint32_t s, uint32_t n) {
   const unsigned act = __activemask();
@@ -98,131 +101,156 @@ __device__ __forceinline__ void add_counts(uint32_t* counts, uint32_t s, uint32_
   if ((threadIdx.x & 31) == leader && sum) atomicAdd(&counts[s], sum);
 }
 
-// One photon packet from emission to death (transport.rs:72-185).  Returns its absorbing hits.
-static __device__ __noinline__ uint32_t trace_photon(const TileDesc& t, uint32_t id, uint32_t* err) {
+// ---------------------------------------------------------------------------------------------
+// Photon state for the lane-refilling transport kernel: one bounce of the reference's loop per
+// call, so a lane whose packet dies takes a new photon while the rest of the warp carries on.
+struct Photon {
+  float3 pos, dir;
+  float E;
+  uint32_t id, b;
+};
+
+constexpr float PHOTON_CELL_UM = 4.0f;  // coarse emission cells used to order photons
+
+// Emission of photon `id` (transport.rs:72-97 with the tile worker's exposure closure).  Returns
+// false when the packet never enters the gelatin (zero exposure, Fresnel reflection).
+__device__ __forceinline__ bool emit_photon(const TileDesc& t, uint32_t id, Photon& ph) {
   const float PI2 = 6.283185307179586f;
   const P4 e0 = philox(id, 0, 0, TAG_EMIT, t.k0, t.k1);
   const float x = uf(e0.x) * t.W;
   const float y = uf(e0.y) * t.H;
-  // Nearest-pixel exposure closure (image_pipeline.rs:949-958).
   const float uu = fminf(fmaxf(x / t.W, 0.0f), 1.0f), vv = fminf(fmaxf(y / t.H, 0.0f), 1.0f);
   const uint32_t px = min(static_cast<uint32_t>(roundf(uu * (float)(t.tw - 1))), t.tw - 1);
   const uint32_t py = min(static_cast<uint32_t>(roundf(vv * (float)(t.th - 1))), t.th - 1);
-  float E = fmaxf(__ldg(&t.tile[static_cast<size_t>(py) * t.stride + px]), 0.0f);
-  if (!(E > 0.0f)) return 0;
+  const float E = fmaxf(__ldg(&t.tile[static_cast<size_t>(py) * t.stride + px]), 0.0f);
+  if (!(E > 0.0f)) return false;
   const float theta = uf(e0.z) * t.theta_max;
-  const float phi = uf(e0.w) * PI2;
   float st, ct, sp, cp;
   sincosf(theta, &st, &ct);
-  sincosf(phi, &sp, &cp);
+  sincosf(uf(e0.w) * PI2, &sp, &cp);
   float3 dir = make_float3(st * cp, st * sp, ct);
-  {
-    const float n = rsqrtf(dir.x * dir.x + dir.y * dir.y + dir.z * dir.z);
-    dir = make_float3(dir.x * n, dir.y * n, dir.z * n);
-  }
-  // Schlick reflectance at the air-gelatin interface (optics.rs:147-154).
+  const float n = rsqrtf(dir.x * dir.x + dir.y * dir.y + dir.z * dir.z);
+  dir = make_float3(dir.x * n, dir.y * n, dir.z * n);
   const float c = fminf(fabsf(dir.z), 1.0f), m = 1.0f - c, m2 = m * m;
   const float R = t.r0 + (1.0f - t.r0) * (m2 * m2 * m);
-  const P4 e1 = philox(id, 0, 1, TAG_EMIT, t.k0, t.k1);
-  if (uf(e1.x) < R) return 0;
-  float3 pos = make_float3(x, y, 0.001f);
-  uint32_t nhits_total = 0;
-  HitF hits[HMAX];
-  for (uint32_t b = 0; b < t.max_bounces; ++b) {
-    const P4 rb = philox(id, b, 0, TAG_BOUNCE, t.k0, t.k1);
-    const float fp = t.mu_t > 0.0f ? -__logf(fmaxf(1.0f - uf(rb.x), 1.17549435e-38f)) / t.mu_t : 1e6f;
-    const float step = fminf(fp, t.D * 1.5f);
-    const float3 inv = make_float3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
-    int nh = 0;
-    if (t.n > 0) {
-      walk_lbvh(t.nodes, pos, inv, step * 1.00001f + 1e-3f, err, [&](uint32_t s) {
-        const float4 a = __ldg(&t.a[s]), q = __ldg(&t.q[s]), d = __ldg(&t.d[s]);
-        float t0, t1;
-        if (!fcanonical_hit(a, q, d, 1.0f, pos, dir, inv, t0, t1)) return;
-        if (!(t0 < step)) return;
-        if (!(fmaxf(fminf(t1, step) - t0, 0.0f) > 0.0f)) return;
-        const uint32_t cid = t.s2id ? __ldg(&t.s2id[s]) : s;
-        if (nh == HMAX) { atomicOr(err, ERR_HIT_OVERFLOW); return; }
-        int j = nh++;
-        while (j > 0 && (hits[j - 1].t0 > t0 || (hits[j - 1].t0 == t0 && hits[j - 1].id > cid))) {
-          hits[j] = hits[j - 1];
-          --j;
-        }
-        hits[j] = HitF{t0, t1, cid, s};
-      });
-    }
-    P4 r{};
-    for (int h = 0; h < nh; ++h) {
-      if ((h & 3) == 0) r = philox(id, b, static_cast<uint32_t>(h) >> 2, TAG_HIT, t.k0, t.k1);
-      const float path = fmaxf(fminf(hits[h].t1, step) - hits[h].t0, 0.0f);
-      const float p = 1.0f - __expf(-t.alpha * path);
-      const float expected = E * p * __ldg(&t.a[hits[h].s].w) * 5.0f;
-      const float fl = floorf(expected);
-      const float frac = expected - fl;
-      const uint32_t cnt = static_cast<uint32_t>(fl) + (uf(word(r, h & 3)) < frac ? 1u : 0u);
-      if (cnt) add_counts(t.counts, hits[h].s, cnt);
-      E *= fmaxf(1.0f - p * 0.9f, 0.05f);
-    }
-    nhits_total += nh;
-    const float3 np = make_float3(pos.x + dir.x * step, pos.y + dir.y * step, pos.z + dir.z * step);
-    if (np.x < 0.0f || np.x >= t.W || np.y < 0.0f || np.y >= t.H) break;
-    if (np.z <= 0.0f) break;
-    if (np.z >= t.D) {
-      // Anti-halation backing (optics.rs:160-196).
-      pos = make_float3(np.x, np.y, t.D - 0.001f);
-      const P4 ra = philox(id, b, 0, TAG_AH, t.k0, t.k1);
-      E *= t.eff_r;
-      if (E < 1e-4f) {
-        if (uf(ra.x) < 0.1f) E /= 0.1f; else break;
+  if (uf(philox(id, 0, 1, TAG_EMIT, t.k0, t.k1).x) < R) return false;
+  ph.pos = make_float3(x, y, 0.001f);
+  ph.dir = dir;
+  ph.E = E;
+  ph.id = id;
+  ph.b = 0;
+  return true;
+}
+
+struct HitS {
+  float t0, t1;
+  uint32_t s;
+};
+
+// Canonical hit order (t_enter, crystal index); the index is the crystal id, which for crystal
+// sets without an id map is the Morton slot itself.
+__device__ __forceinline__ bool hit_before(const TileDesc& t, float ta, uint32_t sa, float tb, uint32_t sb) {
+  if (ta != tb) return ta < tb;
+  const uint32_t ia = t.s2id ? __ldg(&t.s2id[sa]) : sa, ib = t.s2id ? __ldg(&t.s2id[sb]) : sb;
+  return ia < ib;
+}
+
+// One bounce (transport.rs:101-185).  Returns whether the packet is still alive.
+__device__ __forceinline__ bool photon_bounce(const TileDesc& t, Photon& ph, HitS* hits, uint32_t* err,
+                                              uint32_t& nhit) {
+  const float PI2 = 6.283185307179586f;
+  nhit = 0;
+  if (ph.b >= t.max_bounces) return false;
+  const uint32_t b = ph.b++;
+  const P4 rb = philox(ph.id, b, 0, TAG_BOUNCE, t.k0, t.k1);
+  const float fp = t.mu_t > 0.0f ? -__logf(fmaxf(1.0f - uf(rb.x), 1.17549435e-38f)) / t.mu_t : 1e6f;
+  const float step = fminf(fp, t.D * 1.5f);
+  const float3 pos = ph.pos, dir = ph.dir;
+  const float3 inv = make_float3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
+  int nh = 0;
+  if (t.n > 0) {
+    walk_lbvh(t.nodes, pos, inv, step * 1.00001f + 1e-3f, err, [&](uint32_t s) {
+      const float4 a = __ldg(&t.a[s]), q = __ldg(&t.q[s]), d = __ldg(&t.d[s]);
+      float t0, t1;
+      if (!fcanonical_hit(a, q, d, 1.0f, pos, dir, inv, t0, t1)) return;
+      if (!(t0 < step)) return;
+      if (!(fmaxf(fminf(t1, step) - t0, 0.0f) > 0.0f)) return;
+      if (nh == HMAX) { atomicOr(err, ERR_HIT_OVERFLOW); return; }
+      int j = nh++;
+      while (j > 0 && hit_before(t, t0, s, hits[j - 1].t0, hits[j - 1].s)) {
+        hits[j] = hits[j - 1];
+        --j;
       }
-      if (uf(ra.y) < 0.4f) {
-        const float u1 = uf(ra.z), u2 = uf(ra.w);
-        const float r = sqrtf(u1);
-        float s2, c2;
-        sincosf(PI2 * u2, &s2, &c2);
-        dir = make_float3(r * c2, r * s2, -sqrtf(fmaxf(1.0f - u1, 0.0f)));
-      } else {
-        dir.z = -fabsf(dir.z);
-      }
-      const float n = rsqrtf(dir.x * dir.x + dir.y * dir.y + dir.z * dir.z);
-      dir = make_float3(dir.x * n, dir.y * n, dir.z * n);
-      continue;
-    }
-    pos = np;
-    // Henyey-Greenstein scattering (optics.rs:113-143).
-    float cth;
-    if (fabsf(t.g) < 1e-4f) {
-      cth = 2.0f * uf(rb.y) - 1.0f;
-    } else {
-      const float term = (1.0f - t.g * t.g) / (1.0f - t.g + 2.0f * t.g * uf(rb.y));
-      cth = (1.0f + t.g * t.g - term * term) / (2.0f * t.g);
-    }
-    cth = fminf(fmaxf(cth, -1.0f), 1.0f);
-    const float sth = sqrtf(fmaxf(1.0f - cth * cth, 0.0f));
-    float sph, cph;
-    sincosf(PI2 * uf(rb.z), &sph, &cph);
-    float3 u;
-    if (fabsf(dir.x) > 0.1f) {
-      u = make_float3(dir.z, 0.0f, -dir.x);  // (0,1,0) x w
-    } else {
-      u = make_float3(0.0f, -dir.z, dir.y);  // (1,0,0) x w
-    }
-    {
-      const float n = rsqrtf(u.x * u.x + u.y * u.y + u.z * u.z);
-      u = make_float3(u.x * n, u.y * n, u.z * n);
-    }
-    const float3 v = make_float3(dir.y * u.z - dir.z * u.y, dir.z * u.x - dir.x * u.z, dir.x * u.y - dir.y * u.x);
-    float3 nd = make_float3(u.x * sth * cph + v.x * sth * sph + dir.x * cth,
-                            u.y * sth * cph + v.y * sth * sph + dir.y * cth,
-                            u.z * sth * cph + v.z * sth * sph + dir.z * cth);
-    const float n = rsqrtf(nd.x * nd.x + nd.y * nd.y + nd.z * nd.z);
-    dir = make_float3(nd.x * n, nd.y * n, nd.z * n);
-    E *= t.albedo;
-    if (E < 1e-3f) {
-      if (uf(rb.w) < 0.1f) E /= 0.1f; else break;
-    }
+      hits[j] = HitS{t0, t1, s};
+    }, t.n);
   }
-  return nhits_total;
+  float E = ph.E;
+  P4 r{};
+  for (int h = 0; h < nh; ++h) {
+    if ((h & 3) == 0) r = philox(ph.id, b, static_cast<uint32_t>(h) >> 2, TAG_HIT, t.k0, t.k1);
+    const float path = fmaxf(fminf(hits[h].t1, step) - hits[h].t0, 0.0f);
+    const float p = 1.0f - __expf(-t.alpha * path);
+    const float expected = E * p * __ldg(&t.a[hits[h].s].w) * 5.0f;
+    const float fl = floorf(expected);
+    const uint32_t cnt = static_cast<uint32_t>(fl) + (uf(word(r, h & 3)) < expected - fl ? 1u : 0u);
+    if (cnt) add_counts(t.counts, hits[h].s, cnt);
+    E *= fmaxf(1.0f - p * 0.9f, 0.05f);
+  }
+  nhit = static_cast<uint32_t>(nh);
+  const float3 np = make_float3(pos.x + dir.x * step, pos.y + dir.y * step, pos.z + dir.z * step);
+  if (np.x < 0.0f || np.x >= t.W || np.y < 0.0f || np.y >= t.H) return false;
+  if (np.z <= 0.0f) return false;
+  if (np.z >= t.D) {
+    ph.pos = make_float3(np.x, np.y, t.D - 0.001f);
+    const P4 ra = philox(ph.id, b, 0, TAG_AH, t.k0, t.k1);
+    E *= t.eff_r;
+    if (E < 1e-4f) {
+      if (uf(ra.x) < 0.1f) E /= 0.1f; else return false;
+    }
+    float3 d2;
+    if (uf(ra.y) < 0.4f) {
+      const float u1 = uf(ra.z), u2 = uf(ra.w);
+      const float rr = sqrtf(u1);
+      float s2, c2;
+      sincosf(PI2 * u2, &s2, &c2);
+      d2 = make_float3(rr * c2, rr * s2, -sqrtf(fmaxf(1.0f - u1, 0.0f)));
+    } else {
+      d2 = make_float3(dir.x, dir.y, -fabsf(dir.z));
+    }
+    const float n = rsqrtf(d2.x * d2.x + d2.y * d2.y + d2.z * d2.z);
+    ph.dir = make_float3(d2.x * n, d2.y * n, d2.z * n);
+    ph.E = E;
+    return true;
+  }
+  ph.pos = np;
+  float cth;
+  if (fabsf(t.g) < 1e-4f) {
+    cth = 2.0f * uf(rb.y) - 1.0f;
+  } else {
+    const float term = (1.0f - t.g * t.g) / (1.0f - t.g + 2.0f * t.g * uf(rb.y));
+    cth = (1.0f + t.g * t.g - term * term) / (2.0f * t.g);
+  }
+  cth = fminf(fmaxf(cth, -1.0f), 1.0f);
+  const float sth = sqrtf(fmaxf(1.0f - cth * cth, 0.0f));
+  float sph, cph;
+  sincosf(PI2 * uf(rb.z), &sph, &cph);
+  float3 u = fabsf(dir.x) > 0.1f ? make_float3(dir.z, 0.0f, -dir.x) : make_float3(0.0f, -dir.z, dir.y);
+  {
+    const float n = rsqrtf(u.x * u.x + u.y * u.y + u.z * u.z);
+    u = make_float3(u.x * n, u.y * n, u.z * n);
+  }
+  const float3 v = make_float3(dir.y * u.z - dir.z * u.y, dir.z * u.x - dir.x * u.z, dir.x * u.y - dir.y * u.x);
+  const float3 nd = make_float3(u.x * sth * cph + v.x * sth * sph + dir.x * cth,
+                                u.y * sth * cph + v.y * sth * sph + dir.y * cth,
+                                u.z * sth * cph + v.z * sth * sph + dir.z * cth);
+  const float n = rsqrtf(nd.x * nd.x + nd.y * nd.y + nd.z * nd.z);
+  ph.dir = make_float3(nd.x * n, nd.y * n, nd.z * n);
+  E *= t.albedo;
+  if (E < 1e-3f) {
+    if (uf(rb.w) < 0.1f) E /= 0.1f; else return false;
+  }
+  ph.E = E;
+  return true;
 }
 
 }  // namespace fg
