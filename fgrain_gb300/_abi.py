@@ -123,6 +123,12 @@ class fg_batch_stats(C.Structure):
                 ("kernel_launches", C.c_uint32), ("_pad", C.c_uint32)]
 
 
+class fg_device_crystals(C.Structure):
+    _fields_ = [("a", C.c_void_p), ("q", C.c_void_p), ("d", C.c_void_p), ("pos64", C.c_void_p),
+                ("dims64", C.c_void_p), ("quat64", C.c_void_p), ("developed", C.c_void_p),
+                ("expansion", C.c_void_p), ("n", C.c_uint64)]
+
+
 _vp = C.c_void_p
 _st = C.c_int
 _u32p = C.POINTER(C.c_uint32)
@@ -178,6 +184,9 @@ PROTOTYPES = {
     "fg_host_alloc": (_st, [C.c_size_t, C.POINTER(_vp)]),
     "fg_host_free": (_st, [_vp]),
     "fg_render_batch": (_st, [_vp, C.POINTER(fg_tile_params), C.c_uint32, C.POINTER(_fp), C.POINTER(_fp)]),
+    "fg_scan_crystals_static": (_st, [C.POINTER(fg_device_crystals), C.POINTER(fg_emulsion_cfg),
+                                      C.POINTER(fg_scan_cfg), C.c_uint64, _vp, _vp, _vp, C.c_char_p,
+                                      C.c_size_t]),
 }
 
 _lib = None

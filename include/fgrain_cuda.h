@@ -293,6 +293,45 @@ fg_status fg_host_free(void* ptr);
 fg_status fg_render_batch(fg_engine* e, const fg_tile_params* tiles, uint32_t ntiles,
                           const float* const* exposure, float* const* d_neg);
 
+/* ---- Scan without device allocation ---------------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot let this library allocate device
+ * memory (a host that runs under a fixed device-memory budget or its own pool allocator, a plugin
+ * inside such a host, code that must avoid the device-wide synchronisation of cudaMalloc /
+ * cudaFree): the scan of fg_scan_emulsion over a crystal set and into an image that the caller
+ * already holds in device memory.  It calls no cudaMalloc, cudaFree or allocating library
+ * routine; its scratch is one file-scope device array of FG_STATIC_SCAN_SCRATCH_BYTES that every
+ * GPU loading this library holds until the process exits, shared by all calls on that device. */
+#define FG_STATIC_SCAN_MAX_BINS 16384u     /* scan bins (bin_px x bin_px pixels each) per call */
+#define FG_STATIC_SCAN_MAX_ITEMS 1048576u  /* (developed crystal, bin) entries per call */
+#define FG_STATIC_SCAN_SCRATCH_BYTES 4392192u
+
+/* A crystal set in device memory, in crystal-index order (any order gives the same image). */
+typedef struct fg_device_crystals {
+  const float* a;           /* n x 4, 16-byte aligned: position x, y, z (um), sensitivity */
+  const float* q;           /* n x 4, 16-byte aligned: unit quaternion i, j, k, w */
+  const float* d;           /* n x 4, 16-byte aligned: dims x, y, z (um), morphology (int32 bits) */
+  const double* pos64;      /* n x 3 FP64 positions, or NULL to decide ties from the floats */
+  const double* dims64;     /* n x 3, given together with pos64 */
+  const double* quat64;     /* n x 4, given together with pos64 */
+  const uint8_t* developed; /* n development flags */
+  const double* expansion;  /* n development expansions (development.rs:156-168) */
+  uint64_t n;
+} fg_device_crystals;
+
+/* Scans `crystals` like fg_scan_emulsion over a film of film->width x film->height x film->depth
+ * um (the other fields of film are ignored).  out (width*height floats) and image8 (width*height
+ * bytes, may be NULL) are device pointers; work runs on `stream` (a cudaStream_t; NULL is the
+ * legacy default stream) and the call returns when it has finished.  Requests needing more than
+ * FG_STATIC_SCAN_MAX_BINS bins or FG_STATIC_SCAN_MAX_ITEMS entries fail with FG_ERR_INVALID_ARG
+ * before any output is written.  On failure a message is copied to `message` (message_len bytes,
+ * may be NULL).  The first call on a device looks up the scratch's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.  Every call on a device
+ * shares the scratch, which keeps the last call's contents; each call clears what must start at
+ * zero.  Calls whose GPU work overlaps race on the scratch: serialise them. */
+fg_status fg_scan_crystals_static(const fg_device_crystals* crystals, const fg_emulsion_cfg* film,
+                                  const fg_scan_cfg* cfg, uint64_t seed, float* out, uint8_t* image8,
+                                  void* stream, char* message, size_t message_len);
+
 #ifdef __cplusplus
 }
 #endif
