@@ -55,17 +55,25 @@ def c2_inputs():
     return exposure
 
 
-def c2_tiles(exposure):
+def c2_tiles(exposure, ntiles=None):
     import fgrain_gb300 as fg
     from fgrain_gb300.image import tile_grid, tile_seed
 
     H, W = exposure.shape
     grid, step, pad = tile_grid(W, H, GRAIN)
+    if ntiles:
+        grid = grid[:ntiles]
     params, tiles = [], []
     for t in grid:
         params.append(fg.tile_params("tri-x", 1.0 / GRAIN, t.tw, t.th, 1.0, 0.0, tile_seed(SEED, t)))
         tiles.append(np.ascontiguousarray(exposure[t.y_start:t.y_start + t.th, t.x_start:t.x_start + t.tw]))
     return grid, params, tiles
+
+
+def c2_tiles_grid(exposure):
+    from fgrain_gb300.image import tile_grid
+
+    return tile_grid(exposure.shape[1], exposure.shape[0], GRAIN)[0]
 
 
 class Clocks:
@@ -196,7 +204,7 @@ def run_ours(args):
 
     rank, world, local, td = dist()
     exposure = c2_inputs()
-    grid, params, tiles = c2_tiles(exposure)
+    grid, params, tiles = c2_tiles(exposure, args.tiles)
     engine = fg.GpuEngine(local)
     batch = fg.Batch(params, engine, use_graph=True, autotune=True)
     batch.set_exposure(tiles)
@@ -208,14 +216,23 @@ def run_ours(args):
     d_batched = batch.density()
     if td:
         td.barrier()
+    prof = None
+    if args.profile_region:  # limits an `ncu --profile-from-start off` capture to the timed replays
+        import torch.cuda.profiler as prof
+        prof.start()
     with Clocks(local) as clk:
         ms = batch.time(args.steps)
+    if prof:
+        prof.stop()
+    stats = batch.wait()  # stage times of the last timed replay (CUDA events on the engine stream)
     if td:
         td.barrier()
     clocks = clk.summary()
     ms_max = reduce_max(td, ms)
     per_step = ms_max / args.steps
-    out_px = OUT_W * OUT_H
+    full = not args.tiles or args.tiles >= 49
+    out_px = OUT_W * OUT_H if full else int(round(OUT_W * OUT_H * sum(p.width_px * p.height_px for p in params)
+                                                  / sum(t.tw * t.th for t in c2_tiles_grid(exposure))))
     value = world * out_px / (per_step / 1e3) / 1e6
 
     # End to end through the public API: pinned host exposure in, pinned density out, per step.
@@ -278,7 +295,8 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": "Mpx/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "C2: 1024x1024 blurred-noise luminance (sigma 16, seed 1, gamma 2.2), tri-x, "
+            "config": {"workload": ("" if full else f"first {len(params)} tiles of ") +
+                                   "C2: 1024x1024 blurred-noise luminance (sigma 16, seed 1, gamma 2.2), tri-x, "
                                    "grain 2.4 px, push 0, supersample 2 (2048^2 internal, 49 tiles), batched "
                                    "graph path", "tiles": len(params), "internal_px": int(exposure.size),
                        "output_px": out_px, "l2": "working set (crystals, LBVH, grids) exceeds L2; no flush",
@@ -348,6 +366,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--tiles", type=int, default=0, help="render only the first N tiles of C2 (profiling)")
+    ap.add_argument("--profile-region", action="store_true",
+                    help="bracket the timed replays with cudaProfilerStart/Stop")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -9,5 +9,5 @@ from .api import (  # noqa: F401
     GpuEngine, GpuError, Morphology, ScanConfig, ScanMode, VirtualEmulsionLayer,
     develop_emulsion, expose_emulsion, get_gpu_engine, replay_rays, replay_segments,
     scan_emulsion, scan_ray_hits, SEGMENT_DTYPE, Batch, render_tile, tile_params,
-    PinnedArray,
+    PinnedArray, scan_signal, scan_backward, OTF_SIGMA_REFERENCE,
 )

@@ -149,6 +149,7 @@ PROTOTYPES = {
     "fg_emulsion_preset": (_st, [C.c_char_p, C.c_double, C.c_double, C.POINTER(fg_emulsion_cfg)]),
     "fg_emulsion_upload": (_st, [_vp, C.POINTER(fg_emulsion_cfg), C.POINTER(fg_crystals_host),
                                  C.c_size_t, C.POINTER(_vp)]),
+    "fg_emulsion_synthesize": (_st, [_vp, C.POINTER(fg_emulsion_cfg), C.c_uint64, C.POINTER(_vp)]),
     "fg_emulsion_destroy": (_st, [_vp, _vp]),
     "fg_emulsion_count": (_st, [_vp, _szp]),
     "fg_emulsion_download": (_st, [_vp, _vp, C.POINTER(fg_crystals_out)]),
@@ -166,6 +167,13 @@ PROTOTYPES = {
     "fg_replay_rays": (_st, [_vp, _vp, _dp, _dp, C.c_size_t, C.c_int, _u32p, _u32p,
                              C.c_size_t, _szp, _dp]),
     "fg_scan_ray_hits": (_st, [_vp, _vp, C.POINTER(fg_scan_cfg), C.c_uint64, _u16p]),
+    "fg_blend_tiles": (_st, [_vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _u32p,
+                             C.POINTER(_fp), _fp]),
+    "fg_scanner_otf": (_st, [_vp, _fp, C.c_uint32, C.c_uint32, _fp, _fp]),
+    "fg_resize_triangle": (_st, [_vp, _fp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _fp]),
+    "fg_scan_signal": (_st, [_vp, _vp, C.POINTER(fg_scan_cfg), C.c_uint64, _fp, C.c_double, C.c_double, _fp, _fp]),
+    "fg_scan_backward": (_st, [_vp, _vp, C.POINTER(fg_scan_cfg), C.c_uint64, _fp, C.c_double, C.c_double, _fp, _fp,
+                               _dp, _dp]),
     "fg_tile_params_preset": (_st, [C.c_char_p, C.c_double, C.c_uint32, C.c_uint32, C.c_double,
                                     C.c_double, C.c_uint64, C.POINTER(fg_tile_params)]),
     "fg_render_tile": (_st, [_vp, _fp, C.POINTER(fg_tile_params), _fp]),

@@ -228,6 +228,15 @@ class VirtualEmulsionLayer:
         self._h = handle
 
     @classmethod
+    def synthesize(cls, config: EmulsionConfig, seed: int, engine: GpuEngine | None = None) -> "VirtualEmulsionLayer":
+        """VirtualEmulsionLayer::synthesize (emulsion.rs:155-220), on the device."""
+        e = _engine(engine)
+        cfg = config.to_c()
+        h = C.c_void_p()
+        _check(e, e._lib.fg_emulsion_synthesize(e._h, C.byref(cfg), seed & 0xFFFFFFFFFFFFFFFF, C.byref(h)))
+        return cls(e, config, h.value)
+
+    @classmethod
     def from_crystals(cls, config: EmulsionConfig, pos, dims, quat, sensitivity, morphology=None,
                       engine: GpuEngine | None = None) -> "VirtualEmulsionLayer":
         e = _engine(engine)
@@ -335,6 +344,39 @@ def scan_emulsion(emulsion: VirtualEmulsionLayer, config: ScanConfig, seed: int,
                                       _ptr(sig, C.c_float), _ptr(out, C.c_float),
                                       _ptr(img, C.c_uint8)))
     return out, img
+
+
+OTF_SIGMA_REFERENCE = 0.3904441347190481  # OTF width whose taps are the reference's (0.035, 0.93, 0.035)
+
+
+def scan_signal(emulsion: VirtualEmulsionLayer, config: ScanConfig, seed: int, sigma_per_crystal=None,
+                exposure: float = 1.0, otf_sigma: float = OTF_SIGMA_REFERENCE):
+    """Differentiable scan: (signal = OTF_s(exposure * T), T), float32 [h, w] each."""
+    cfg = config.to_c()
+    S = np.zeros((config.height_px, config.width_px), np.float32)
+    T = np.zeros_like(S)
+    sig = None if sigma_per_crystal is None else np.ascontiguousarray(sigma_per_crystal, np.float32)
+    e = emulsion.engine
+    _check(e, e._lib.fg_scan_signal(e._h, emulsion._h, C.byref(cfg), seed & 0xFFFFFFFFFFFFFFFF,
+                                    _ptr(sig, C.c_float), float(exposure), float(otf_sigma),
+                                    _ptr(S, C.c_float), _ptr(T, C.c_float)))
+    return S, T
+
+
+def scan_backward(emulsion: VirtualEmulsionLayer, config: ScanConfig, seed: int, dL_dsignal,
+                  sigma_per_crystal=None, exposure: float = 1.0, otf_sigma: float = OTF_SIGMA_REFERENCE):
+    """Adjoint of scan_signal: (dL/dsigma per crystal [float32], dL/dexposure, dL/dotf_sigma)."""
+    cfg = config.to_c()
+    g = np.ascontiguousarray(dL_dsignal, np.float32).reshape(config.height_px, config.width_px)
+    gs = np.zeros(len(emulsion), np.float32)
+    ge = C.c_double()
+    go = C.c_double()
+    sig = None if sigma_per_crystal is None else np.ascontiguousarray(sigma_per_crystal, np.float32)
+    e = emulsion.engine
+    _check(e, e._lib.fg_scan_backward(e._h, emulsion._h, C.byref(cfg), seed & 0xFFFFFFFFFFFFFFFF,
+                                      _ptr(sig, C.c_float), float(exposure), float(otf_sigma), _ptr(g, C.c_float),
+                                      _ptr(gs, C.c_float), C.byref(ge), C.byref(go)))
+    return gs, ge.value, go.value
 
 
 SEGMENT_DTYPE = np.dtype([("origin", "<f8", 3), ("dir", "<f8", 3), ("step", "<f8"),

@@ -18,7 +18,7 @@ BUILD = HERE / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "--extended-lambda",
-    "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xptxas", "-warn-spills",
+    "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-warn-spills",
 ]
 
 

@@ -39,6 +39,8 @@ void launch_photon_sort(const TileDesc* tiles_dev, int ntiles, unsigned long lon
                         cudaStream_t st);
 void launch_scan(const ScanTile* tiles, int ntiles, unsigned long long nbins, unsigned threads, uint32_t* err,
                  unsigned long long* stats, cudaStream_t st);
+void launch_scan_prep(const ScanTile* tiles, int ntiles, unsigned long long nslots, ScanPrep* prep,
+                      cudaStream_t st);
 uint32_t scan_bin_px(uint32_t spp);
 
 // Per-tile state for the batched LBVH, development and binning kernels.
@@ -422,6 +424,7 @@ struct fg_batch {
   DBuf<uint32_t> counts, size;
   DBuf<uint8_t> developed;
   DBuf<double> exp64;
+  DBuf<ScanPrep> prep;  // staging terms of developed crystals for the scan
   DBuf<uint32_t> bin_cnt, bin_off, bin_cur, bin_items;
   DBuf<uint32_t> pcnt, poff, pcur, porder;  // photon ordering by emission cell
   unsigned long long npcells = 0;
@@ -580,6 +583,8 @@ static void upload_descriptors(fg_batch* B, cudaStream_t st) {
     t.counts = B->counts.p + cb;
     t.tile = B->exposure.p + B->exp_off[i];
     ScanTile& c = B->sc[i];
+    c.prep = B->prep.p + cb;
+    c.slot_base = cb;
     c.a = B->A.p + cb;
     c.q = B->Q.p + cb;
     c.d = B->D.p + cb;
@@ -672,6 +677,7 @@ static void stage_scan(fg_batch* B, cudaStream_t st) {
   const int nt = static_cast<int>(B->ntiles);
   fg_engine* e = B->e;
   const unsigned G = grid_for(B->ncap, 256);
+  launch_scan_prep(B->d_sc.p, nt, B->ncap, B->prep.p, st);
   FG_CUDA(cudaMemsetAsync(B->bin_cnt.p, 0, (B->nbins + 1) * sizeof(uint32_t), st));
   FG_CUDA(cudaMemsetAsync(B->bin_cur.p, 0, (B->nbins + 1) * sizeof(uint32_t), st));
   k_bin_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->A.p, B->D.p, B->developed.p, B->exp64.p, B->bin_cnt.p, nullptr,
@@ -843,6 +849,7 @@ static void plan(fg_batch* B, const fg_batch_options* opt) {
   B->size.alloc(std::max<unsigned long long>(cap, 1), st);
   B->developed.alloc(std::max<unsigned long long>(cap, 1), st);
   B->exp64.alloc(std::max<unsigned long long>(cap, 1), st);
+  B->prep.alloc(std::max<unsigned long long>(cap, 1), st);
   B->bin_cnt.alloc(nbins_max + 1, st);
   B->bin_off.alloc(nbins_max + 1, st);
   B->bin_cur.alloc(nbins_max + 1, st);
@@ -889,6 +896,85 @@ static void capture(fg_batch* B) {
 }  // namespace fg
 
 extern "C" {
+
+// VirtualEmulsionLayer::synthesize (emulsion.rs:155-220) on the device: the tile synthesis of this
+// file over the whole emulsion as one tile, then the LBVH.  Crystal ids are the Morton slot order
+// of the synthesis (the reference numbers crystals in its sampler's output order, which the random
+// streams do not pin either).
+fg_status fg_emulsion_synthesize(fg_engine* e, const fg_emulsion_cfg* cfg, uint64_t seed, fg_emulsion** out) {
+  if (!out) return FG_ERR_INVALID_ARG;
+  *out = nullptr;
+  return guard(e, [&] {
+    FG_REQUIRE(cfg, "null config");
+    cudaStream_t st = e->stream;
+    begin_call(e);
+    (void)cudaGetLastError();
+    fg_tile_params p{};
+    p.film_w = cfg->width;
+    p.film_h = cfg->height;
+    p.film_d = cfg->depth;
+    p.width_px = p.height_px = 1;
+    p.seed = seed;
+    p.r_min = cfg->r_min;
+    p.mean_crystal_radius = cfg->mean_crystal_radius;
+    p.size_variance = cfg->size_variance;
+    p.morphology = cfg->morphology;
+    p.tabular_aspect_ratio = cfg->tabular_aspect_ratio;
+    p.base_sensitivity = cfg->base_sensitivity;
+    SynthTile s;
+    TileDesc td;
+    ScanTile sc;
+    BTile bt;
+    derive_tile(p, s, td, sc, bt);
+    const unsigned long long ncells = static_cast<unsigned long long>(s.gw) * s.gh * s.gd;
+    FG_REQUIRE(s.ccap < 0x7ffffff0u, "emulsion too large");
+    unsigned cols[4];
+    for (int c = 0; c < 4; ++c) {
+      s.col_base[c] = 0;
+      cols[c] = ((s.nbx + 1 - (c & 1)) / 2) * ((s.nby + 1 - (c >> 1)) / 2);
+    }
+    const int gdmax = static_cast<int>(s.gd);
+    FG_REQUIRE(bridson_smem(gdmax) <= 220 * 1024, "emulsion too deep for the synthesis column");
+    FG_CUDA(cudaEventRecord(e->timer.ev[0], st));
+    DBuf<SynthTile> d_syn(1, st);
+    FG_CUDA(cudaMemcpyAsync(d_syn.p, &s, sizeof(SynthTile), cudaMemcpyHostToDevice, st));
+    DBuf<uint32_t> cells(ncells, st), npts(1, st), flags(s.slots + 1ull, st), scan(s.slots + 1ull, st);
+    DBuf<float4> A(s.ccap, st), Q(s.ccap, st), D(s.ccap, st);
+    DBuf<uint64_t> keys(s.ccap, st);
+    FG_CUDA(cudaMemsetAsync(cells.p, 0, ncells * sizeof(uint32_t), st));
+    FG_CUDA(cudaMemsetAsync(npts.p, 0, sizeof(uint32_t), st));
+    for (int c = 0; c < 4; ++c) launch_bridson(d_syn.p, 1, c, cols[c], gdmax, cells.p, e->d_err, st);
+    FG_CUDA(cudaMemsetAsync(flags.p + s.slots, 0, sizeof(uint32_t), st));
+    launch_synth_post(d_syn.p, 1, ncells, s.slots, cells.p, npts.p, flags.p, st);
+    exclusive_scan_u32(flags.p, scan.p, s.slots + 1ull, st);
+    launch_emit(d_syn.p, 1, s.slots, cells.p, scan.p, A.p, Q.p, D.p, keys.p, e->d_err, st);
+    uint32_t n = 0;
+    FG_CUDA(cudaMemcpyAsync(&n, scan.p + s.slots, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    FG_CUDA(cudaStreamSynchronize(st));
+    check_error_word(e);
+    n = std::min(n, s.ccap);
+    std::unique_ptr<fg_emulsion> em(new fg_emulsion());
+    em->cfg = *cfg;
+    em->n = n;
+    em->stream = st;
+    em->has64 = false;
+    em->extent = std::max(std::max(cfg->width, cfg->height), cfg->depth);
+    em->a = std::move(A);
+    em->q = std::move(Q);
+    em->d = std::move(D);
+    em->nodes.alloc(std::max<uint32_t>(n > 0 ? n - 1 : 0, 1), st);
+    em->leaf_parent.alloc(std::max<uint32_t>(n, 1), st);
+    alloc_state(em.get(), st);
+    if (n) build_lbvh(em.get(), keys.p, em->nodes.p, em->leaf_parent.p, false, st);
+    FG_CUDA(cudaEventRecord(e->timer.ev[1], st));
+    FG_CUDA(cudaStreamSynchronize(st));
+    e->timings.synth_ms = elapsed(e->timer.ev[0], e->timer.ev[1]);
+    e->timings.total_ms = e->timings.synth_ms;
+    e->timings.crystals = n;
+    end_call(e);
+    *out = em.release();
+  });
+}
 
 fg_status fg_tile_params_preset(const char* preset, double pixel_size_um, uint32_t tw, uint32_t th,
                                 double exposure, double push, uint64_t tile_seed, fg_tile_params* out) {
@@ -1046,8 +1132,9 @@ fg_status fg_batch_wait(fg_batch* b, fg_batch_stats* stats) {
     s.scan_bin_px = b->bin_px;
     s.graph = b->exec ? 1u : 0u;
     // Own kernels per run: Bridson x4, count + thin + flags, emit, set_n, Karras + fit, photon order x2, transport,
-    // maxdim + threshold + link + roots + finalize, two bin passes, scan (CUB scans not counted).
-    s.kernel_launches = 4 + 3 + 1 + 1 + 2 + 2 + 1 + 5 + 2 + 1;
+    // maxdim + threshold + link + roots + finalize, scan prep, two bin passes, scan (CUB scans not
+    // counted).
+    s.kernel_launches = 4 + 3 + 1 + 1 + 2 + 2 + 1 + 5 + 1 + 2 + 1;
     b->stats = s;
     if (stats) *stats = s;
   });

@@ -64,18 +64,6 @@ void to_device(DBuf<T>& d, const T* h, size_t n, cudaStream_t st) {
   if (n) FG_CUDA(cudaMemcpyAsync(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice, st));
 }
 
-// Host permutation helpers between crystal id order and Morton order.
-template <class T>
-std::vector<T> to_sorted(const fg_emulsion* em, const T* by_id) {
-  std::vector<T> v(em->n);
-  for (uint32_t s = 0; s < em->n; ++s) v[s] = by_id[em->h_s2id.empty() ? s : em->h_s2id[s]];
-  return v;
-}
-template <class T>
-void from_sorted(const fg_emulsion* em, const std::vector<T>& sorted, T* by_id) {
-  for (uint32_t s = 0; s < em->n; ++s) by_id[em->h_s2id.empty() ? s : em->h_s2id[s]] = sorted[s];
-}
-
 void alloc_state(fg_emulsion* em, cudaStream_t st) {
   const uint32_t n = em->n;
   em->counts.alloc(std::max<uint32_t>(n, 1), st);

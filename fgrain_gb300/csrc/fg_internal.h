@@ -165,8 +165,38 @@ struct ScanOut {
   float* d_neg = nullptr;    // -log10(clamp(T)) + 0.05
   uint16_t* ray_hits = nullptr;
 };
+// Host permutation helpers between crystal id order and Morton order.
+template <class T>
+std::vector<T> to_sorted(const fg_emulsion* em, const T* by_id) {
+  std::vector<T> v(em->n);
+  for (uint32_t s = 0; s < em->n; ++s) v[s] = by_id[em->h_s2id.empty() ? s : em->h_s2id[s]];
+  return v;
+}
+template <class T>
+void from_sorted(const fg_emulsion* em, const std::vector<T>& sorted, T* by_id) {
+  for (uint32_t s = 0; s < em->n; ++s) by_id[em->h_s2id.empty() ? s : em->h_s2id[s]] = sorted[s];
+}
+
+// fg_image.cu: the separable 3-tap clamp-to-edge filter (two passes through tmp), in the
+// reference's FP32 operation order, the second pass scaled by `scale`.
+void launch_otf(const float* in, float* tmp, float* out, uint32_t w, uint32_t h, const float k[3], float scale,
+                cudaStream_t st);
+
+// Device state of a new emulsion (counts, development, clumps), zeroed (fg_engine.cu).
+void alloc_state(fg_emulsion* em, cudaStream_t st);
+
+// Per-call bookkeeping of the engine entry points (fg_engine.cu): zero the timings and device
+// counters; read the counters back, synchronise and raise the device error word.
+void begin_call(fg_engine* e);
+void end_call(fg_engine* e);
+float elapsed(cudaEvent_t a, cudaEvent_t b);
+
 void scan(fg_engine* e, const fg_emulsion* em, const fg_scan_cfg& cfg, uint64_t seed,
           const float* sigma_sorted, const ScanOut& out);
+// g_sorted[s] += sum over the rays of each pixel p of wpx[p] / spp * T_ray * chord_s (device
+// arrays; wpx has one weight per pixel, g_sorted one FP64 sum per crystal in Morton order).
+void scan_adjoint(fg_engine* e, const fg_emulsion* em, const fg_scan_cfg& cfg, uint64_t seed,
+                  const float* sigma_sorted, const float* wpx, double* g_sorted);
 
 // fg_transport.cu
 void expose(fg_engine* e, fg_emulsion* em, const float* tile_dev, uint32_t tw, uint32_t th,

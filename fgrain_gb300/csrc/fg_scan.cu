@@ -88,86 +88,230 @@ constexpr float EPS32 = 5.9604645e-8f;  // 2^-24
 //   ellipsoids: R_0i / D_i, R_1i / D_i, e_i = -R_2i / D_i, A = |e|^2, 1 / A.
 // Cubes whose faces are nearly parallel to the ray (|1/R_2i| > 15) evaluate their local origin in
 // float-pair arithmetic; cubes with an exactly parallel face decide in FP64.
-__device__ __forceinline__ void stage_crystal(const ScanTile& t, ScanSmem& sm, int c, uint32_t s,
-                                              double bx0, double by0) {
+__device__ __forceinline__ void prep_crystal(const ScanTile& t, uint32_t s, ScanPrep& P) {
   const Crystal64 k = load64_parts(t, s);
   const double e64 = t.exp64[s];
   const double mdim = fmax(fmax(k.dims.x, k.dims.y), k.dims.z);
   const double m64 = __dmul_rn(mdim, e64);
   const float m = static_cast<float>(m64);
-  split64(k.pos.x - bx0, sm.cxh[c], sm.cxl[c]);
-  split64(k.pos.y - by0, sm.cyh[c], sm.cyl[c]);
-  sm.m[c] = m;
-  sm.delta[c] = static_cast<float>(t.z0 - k.pos.z);
-  sm.sig[c] = t.sigma_c ? t.sigma_c[s] : t.sigma;
-  sm.s[c] = static_cast<int>(s);
+  P.px = k.pos.x;
+  P.py = k.pos.y;
+  P.m = m;
+  P.delta = static_cast<float>(t.z0 - k.pos.z);
+  P.sig = t.sigma_c ? t.sigma_c[s] : t.sigma;
   const double x = k.q[0], y = k.q[1], z = k.q[2], w = k.q[3];
   // world = R local + p, so local_i = R_0i dx + R_1i dy + R_2i dz: rows 0..2 of R.
   const double R0[3] = {1.0 - 2.0 * (y * y + z * z), 2.0 * (x * y - z * w), 2.0 * (x * z + y * w)};
   const double R1[3] = {2.0 * (x * y + z * w), 1.0 - 2.0 * (x * x + z * z), 2.0 * (y * z - x * w)};
   const double R2[3] = {2.0 * (x * z - y * w), 2.0 * (y * z + x * w), 1.0 - 2.0 * (x * x + y * y)};
   const double D[3] = {k.dims.x * e64, k.dims.y * e64, k.dims.z * e64};
+#pragma unroll
+  for (int i = 0; i < 21; ++i) P.g[i] = 0.0f;
   if (k.morph == 0) {
     float invmax = 0.0f;
     const float Dmax = static_cast<float>(fmax(fmax(D[0], D[1]), D[2]));
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-      split64(R0[i], sm.g[i][c], sm.g[3 + i][c]);
-      split64(R1[i], sm.g[6 + i][c], sm.g[9 + i][c]);
+      split64(R0[i], P.g[i], P.g[3 + i]);
+      split64(R1[i], P.g[6 + i], P.g[9 + i]);
       const float inv = static_cast<float>(1.0 / (-R2[i]));
-      sm.g[12 + i][c] = inv;
-      split64(D[i], sm.g[15 + i][c], sm.g[18 + i][c]);
+      P.g[12 + i] = inv;
+      split64(D[i], P.g[15 + i], P.g[18 + i]);
       invmax = fmaxf(invmax, fabsf(inv));
     }
     if (!(invmax < 1e30f)) {
-      sm.kind[c] = K_FP64;
-      sm.err[c] = INFINITY;
+      P.kind = K_FP64;
+      P.err = INFINITY;
     } else if (invmax > 15.0f) {
-      sm.kind[c] = K_CUBE_DF;
-      sm.err[c] = 0.0f;  // bounds are formed per ray from the t values
+      P.kind = K_CUBE_DF;
+      P.err = 0.0f;  // bounds are formed per ray from the t values
     } else {
-      sm.kind[c] = K_CUBE;
+      P.kind = K_CUBE;
       // |d local| <= 4e-7 m + 1e-7 (rounded rows, offsets); |d D| <= eps D; each t = (+-D - lo)
       // * inv carries (d lo + d D) |inv| + 2 eps |t|, with |t| <= (D + 2m) invmax.
-      sm.err[c] = 4.0f * ((4e-7f * m + 1e-7f + EPS32 * Dmax) * invmax + 2.0f * EPS32 * (Dmax + 2.0f * m) * invmax);
+      P.err = 4.0f * ((4e-7f * m + 1e-7f + EPS32 * Dmax) * invmax + 2.0f * EPS32 * (Dmax + 2.0f * m) * invmax);
     }
   } else {
-    sm.kind[c] = K_ELLIPSOID;
+    P.kind = K_ELLIPSOID;
     double A = 0.0;
     const double Dmin = fmin(fmin(D[0], D[1]), D[2]);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-      sm.g[i][c] = static_cast<float>(R0[i] / D[i]);
-      sm.g[3 + i][c] = static_cast<float>(R1[i] / D[i]);
+      P.g[i] = static_cast<float>(R0[i] / D[i]);
+      P.g[3 + i] = static_cast<float>(R1[i] / D[i]);
       const double ei = -R2[i] / D[i];
-      sm.g[6 + i][c] = static_cast<float>(ei);
+      P.g[6 + i] = static_cast<float>(ei);
       A += ei * ei;
     }
-    sm.g[9][c] = static_cast<float>(A);
-    sm.g[10][c] = static_cast<float>(1.0 / A);
+    P.g[9] = static_cast<float>(A);
+    P.g[10] = static_cast<float>(1.0 / A);
     // h = 1 - |P_perp|^2; P (|P| <= sqrt(2) m / Dmin) and P_perp = P + tc e carry ~8 eps |P|
     // each, so |d h| <= 2 |P_perp| 8 eps sqrt(3) Pmax + 4 eps; four times that as the bound.
     const float Pmax = static_cast<float>(1.4142135623730951 * m64 / Dmin);
-    sm.err[c] = 4.0f * (2.0f * 1.05f * 8.0f * EPS32 * 1.7320508f * Pmax + 4.0f * EPS32) + 1e-9f;
+    P.err = 4.0f * (2.0f * 1.05f * 8.0f * EPS32 * 1.7320508f * Pmax + 4.0f * EPS32) + 1e-9f;
   }
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan(const ScanTile* __restrict__ tiles,
-                                                       int ntiles, uint32_t* err,
-                                                       unsigned long long* stats) {
-  __shared__ ScanSmem sm;
-  // Tile of this bin (last tile whose first bin <= blockIdx.x).
+// Stages crystal s for the bin whose 16-px-square corner is (bx0, by0): the bin-independent terms
+// (from t.prep, or derived here), and the centre relative to the corner as float pairs.
+__device__ __forceinline__ void stage_crystal(const ScanTile& t, ScanSmem& sm, int c, uint32_t s,
+                                              double bx0, double by0) {
+  ScanPrep P;
+  if (t.prep) {
+    P = t.prep[s];
+  } else {
+    prep_crystal(t, s, P);
+  }
+  split64(P.px - bx0, sm.cxh[c], sm.cxl[c]);
+  split64(P.py - by0, sm.cyh[c], sm.cyl[c]);
+  sm.m[c] = P.m;
+  sm.delta[c] = P.delta;
+  sm.err[c] = P.err;
+  sm.sig[c] = P.sig;
+  sm.kind[c] = P.kind;
+  sm.s[c] = static_cast<int>(s);
+#pragma unroll
+  for (int i = 0; i < 21; ++i) sm.g[i][c] = P.g[i];
+}
+
+// Staging terms of every developed crystal of every tile, once per crystal (k_scan reads them).
+__global__ void k_scan_prep(const ScanTile* __restrict__ tiles, int ntiles, unsigned long long nslots,
+                            ScanPrep* __restrict__ prep) {
+  const unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+  if (g >= nslots) return;
   int lo = 0, hi = ntiles - 1;
-  const unsigned long long gb = blockIdx.x;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (tiles[mid].bin_base <= gb) lo = mid; else hi = mid - 1;
+    if (tiles[mid].slot_base <= g) lo = mid; else hi = mid - 1;
   }
   const ScanTile& t = tiles[lo];
-  const uint32_t bin = static_cast<uint32_t>(gb - t.bin_base);
+  const unsigned long long s = g - t.slot_base;
+  if (s >= t.n || !t.developed[s]) return;
+  ScanPrep P;
+  prep_crystal(t, static_cast<uint32_t>(s), P);
+  prep[g] = P;
+}
+
+void launch_scan_prep(const ScanTile* tiles, int ntiles, unsigned long long nslots, ScanPrep* prep,
+                      cudaStream_t st) {
+  if (nslots == 0) return;
+  k_scan_prep<<<grid_for(nslots, 128), 128, 0, st>>>(tiles, ntiles, nslots, prep);
+  FG_CUDA(cudaGetLastError());
+}
+
+// Decision and chord of one scanner ray against staged crystal c.  The ray's origin is a float pair
+// relative to the bin's 16-px corner; a pair whose decision falls inside its error bound is
+// decided with the reference's FP64 expressions (counted in nfb).
+__device__ __forceinline__ bool scan_pair(const ScanTile& t, const ScanSmem& sm, uint32_t c, float oxh, float oxl,
+                                          float oyh, float oyl, uint32_t px, uint32_t py, uint32_t sx, uint32_t sy,
+                                          float& chord, uint32_t& nfb) {
+  // Ray minus crystal centre, x and y, as float pairs.
+  float dh, dl, dx, dxl, dy, dyl;
+  two_sum(oxh, -sm.cxh[c], dh, dl);
+  fast_two_sum(dh, dl + (oxl - sm.cxl[c]), dx, dxl);
+  two_sum(oyh, -sm.cyh[c], dh, dl);
+  fast_two_sum(dh, dl + (oyl - sm.cyl[c]), dy, dyl);
+  const float m = sm.m[c], delta = sm.delta[c];
+  // Own box (strict containment in x and y, entry below the origin in z): exact margins
+  // up to ~2 eps m.
+  const float mx = m - fabsf(dx), my = m - fabsf(dy), mz = delta + m;
+  const float EB = 7.2e-7f * m + 1e-9f, EBz = 1e-6f + 2.4e-7f * m;
+  if (mx < -EB || my < -EB || mz < -EBz) return false;
+  const int kind = sm.kind[c];
+  bool amb = mx <= EB || my <= EB || mz <= EBz || kind == K_FP64;
+  bool hit = false;
+  chord = 0.0f;
+  if (!amb) {
+    if (kind != K_ELLIPSOID) {
+      float tmin = -INFINITY, tmax = INFINITY;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const float inv = sm.g[12 + i][c], Dh = sm.g[15 + i][c];
+        float a1, a2;
+        if (kind == K_CUBE) {
+          const float lo_i = fmaf(sm.g[i][c], dx, sm.g[6 + i][c] * dy);
+          a1 = -Dh - lo_i;
+          a2 = Dh - lo_i;
+        } else {
+          // Local origin as a float pair, then the two face offsets exactly rounded.
+          const float R0h = sm.g[i][c], R0l = sm.g[3 + i][c], R1h = sm.g[6 + i][c], R1l = sm.g[9 + i][c];
+          const float Dl = sm.g[18 + i][c];
+          float p0, e0, p1, e1, sh, sl;
+          two_prod(R0h, dx, p0, e0);
+          two_prod(R1h, dy, p1, e1);
+          two_sum(p0, p1, sh, sl);
+          sl += (e0 + e1) + ((R0h * dxl + R1h * dyl) + (R0l * dx + R1l * dy));
+          float v, wv;
+          two_sum(-Dh, -sh, v, wv);
+          a1 = v + ((wv - Dl) - sl);
+          two_sum(Dh, -sh, v, wv);
+          a2 = v + ((wv + Dl) - sl);
+        }
+        const float t1 = a1 * inv, t2 = a2 * inv;
+        tmin = fmaxf(tmin, fminf(t1, t2));
+        tmax = fminf(tmax, fmaxf(t1, t2));
+      }
+      const float E = kind == K_CUBE ? sm.err[c] : 4.0f * 3.0f * EPS32 * (fabsf(tmin) + fabsf(tmax)) + 1e-9f;
+      const float m1 = tmax - tmin, m2 = tmax + delta;
+      const float E2 = E + 4.0f * 3.0f * EPS32 * fabsf(delta) + 2e-6f;
+      if (m1 > 2.0f * E && m2 > E2) {
+        hit = true;
+        chord = tmax - fmaxf(tmin, -delta);
+      } else if (!(m1 < -2.0f * E || m2 < -E2)) {
+        amb = true;
+      }
+    } else {
+      float P[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) P[i] = fmaf(sm.g[i][c], dx, sm.g[3 + i][c] * dy);
+      const float e0 = sm.g[6][c], e1 = sm.g[7][c], e2 = sm.g[8][c];
+      const float iA = sm.g[10][c];
+      // Closest approach along the ray (t' = tc) and the offset there: h = 1 - |P_perp|^2
+      // has the sign of the reference's discriminant.
+      const float tc = -(P[0] * e0 + P[1] * e1 + P[2] * e2) * iA;
+      const float q0 = fmaf(tc, e0, P[0]), q1 = fmaf(tc, e1, P[1]), q2 = fmaf(tc, e2, P[2]);
+      const float hh = 1.0f - (q0 * q0 + q1 * q1 + q2 * q2);
+      const float E = sm.err[c];
+      if (hh > E) {
+        const float sq = sqrtf(hh * iA);
+        const float t0 = tc - sq, t1 = tc + sq;
+        const float E2 = 4.0f * 3.0f * EPS32 * (fabsf(t1) + fabsf(delta)) + 2e-6f;
+        if (t1 + delta > E2) {
+          hit = true;
+          chord = t1 - fmaxf(t0, -delta);
+        } else {
+          amb = true;
+        }
+      } else if (!(hh < -E)) {
+        amb = true;
+      }
+    }
+  }
+  if (amb) {
+    ++nfb;
+    double ox64, oy64;
+    scan_origin64(t, px, py, sx, sy, ox64, oy64);
+    bool h64;
+    const double c64 = scan_chord64(t, static_cast<uint32_t>(sm.s[c]), ox64, oy64, h64);
+    hit = h64;
+    chord = static_cast<float>(c64);
+  }
+  return hit;
+}
+
+// One thread's scanner ray in a bin: pixel, stratum and the ray origin relative to the corner of
+// the 16-pixel square holding the bin (float pairs), shared by the forward scan and its adjoint.
+struct ScanRay {
+  uint32_t px, py, sx, sy, st;
+  bool active;
+  double bx0, by0;
+  float oxh, oxl, oyh, oyl;
+};
+
+__device__ __forceinline__ ScanRay scan_ray(const ScanTile& t, uint32_t bin, uint32_t tid) {
+  ScanRay R;
   const uint32_t bx = bin % t.nbx, by = bin / t.nbx;
   const uint32_t a = t.spp;
-  const uint32_t tid = threadIdx.x;
   const uint32_t pix = tid / a, st = tid % a;
   const uint32_t lx = pix % t.bin_px, ly = pix / t.bin_px;
   const uint32_t px = bx * t.bin_px + lx, py = by * t.bin_px + ly;
@@ -177,8 +321,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const ScanTile* __restric
   // the bin itself, so that every bin edge rounds identically and results do not depend on the
   // launch shape.
   const uint32_t ox_px = (bx * t.bin_px) & ~15u, oy_px = (by * t.bin_px) & ~15u;
-  const double bx0 = __dmul_rn(static_cast<double>(ox_px), t.pw);
-  const double by0 = __dmul_rn(static_cast<double>(oy_px), t.ph);
+  R.bx0 = __dmul_rn(static_cast<double>(ox_px), t.pw);
+  R.by0 = __dmul_rn(static_cast<double>(oy_px), t.ph);
   const uint32_t rlx = px - ox_px, rly = py - oy_px;  // < 16 + bin_px
   // Ray position relative to that corner as a float pair.  The offset in units of the 24-bit
   // jitter is an exact integer X = (l g + s) 2^24 + u, so x = X * pw / (g 2^24).
@@ -202,6 +346,43 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const ScanTile* __restric
     two_prod(Yh, cyh, p, e);
     fast_two_sum(p, e + (Yh * cyl + Yl * cyh), oyh, oyl);
   }
+  R.px = px;
+  R.py = py;
+  R.sx = sx;
+  R.sy = sy;
+  R.st = st;
+  R.active = active;
+  R.oxh = oxh;
+  R.oxl = oxl;
+  R.oyh = oyh;
+  R.oyl = oyl;
+  return R;
+}
+
+// Tile of global bin gb (last tile whose first bin <= gb).
+__device__ __forceinline__ int scan_tile_of(const ScanTile* tiles, int ntiles, unsigned long long gb) {
+  int lo = 0, hi = ntiles - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tiles[mid].bin_base <= gb) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan(const ScanTile* __restrict__ tiles,
+                                                       int ntiles, uint32_t* err,
+                                                       unsigned long long* stats) {
+  __shared__ ScanSmem sm;
+  const unsigned long long gb = blockIdx.x;
+  const ScanTile& t = tiles[scan_tile_of(tiles, ntiles, gb)];
+  const uint32_t bin = static_cast<uint32_t>(gb - t.bin_base);
+  const uint32_t a = t.spp;
+  const uint32_t tid = threadIdx.x;
+  const ScanRay R = scan_ray(t, bin, tid);
+  const uint32_t px = R.px, py = R.py, sx = R.sx, sy = R.sy, st = R.st;
+  const bool active = R.active;
+  const double bx0 = R.bx0, by0 = R.by0;
+  const float oxh = R.oxh, oxl = R.oxl, oyh = R.oyh, oyl = R.oyl;
   long long Lfix = 0;  // chord sum (sigma-weighted when per crystal), 2^-40 um units
   uint32_t nh = 0, nfb = 0;
   const uint32_t b0 = min(t.bin_off[bin], t.items_cap), b1 = min(t.bin_off[bin + 1], t.items_cap);
@@ -213,97 +394,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const ScanTile* __restric
     __syncthreads();
     if (!active) continue;
     for (uint32_t c = 0; c < cnt; ++c) {
-      // Ray minus crystal centre, x and y, as float pairs.
-      float dh, dl, dx, dxl, dy, dyl;
-      two_sum(oxh, -sm.cxh[c], dh, dl);
-      fast_two_sum(dh, dl + (oxl - sm.cxl[c]), dx, dxl);
-      two_sum(oyh, -sm.cyh[c], dh, dl);
-      fast_two_sum(dh, dl + (oyl - sm.cyl[c]), dy, dyl);
-      const float m = sm.m[c], delta = sm.delta[c];
-      // Own box (strict containment in x and y, entry below the origin in z): exact margins
-      // up to ~2 eps m.
-      const float mx = m - fabsf(dx), my = m - fabsf(dy), mz = delta + m;
-      const float EB = 7.2e-7f * m + 1e-9f, EBz = 1e-6f + 2.4e-7f * m;
-      if (mx < -EB || my < -EB || mz < -EBz) continue;
-      const int kind = sm.kind[c];
-      bool amb = mx <= EB || my <= EB || mz <= EBz || kind == K_FP64;
-      bool hit = false;
-      float chord = 0.0f;
-      if (!amb) {
-        if (kind != K_ELLIPSOID) {
-          float tmin = -INFINITY, tmax = INFINITY;
-#pragma unroll
-          for (int i = 0; i < 3; ++i) {
-            const float inv = sm.g[12 + i][c], Dh = sm.g[15 + i][c];
-            float a1, a2;
-            if (kind == K_CUBE) {
-              const float lo_i = fmaf(sm.g[i][c], dx, sm.g[6 + i][c] * dy);
-              a1 = -Dh - lo_i;
-              a2 = Dh - lo_i;
-            } else {
-              // Local origin as a float pair, then the two face offsets exactly rounded.
-              const float R0h = sm.g[i][c], R0l = sm.g[3 + i][c], R1h = sm.g[6 + i][c], R1l = sm.g[9 + i][c];
-              const float Dl = sm.g[18 + i][c];
-              float p0, e0, p1, e1, sh, sl;
-              two_prod(R0h, dx, p0, e0);
-              two_prod(R1h, dy, p1, e1);
-              two_sum(p0, p1, sh, sl);
-              sl += (e0 + e1) + ((R0h * dxl + R1h * dyl) + (R0l * dx + R1l * dy));
-              float v, wv;
-              two_sum(-Dh, -sh, v, wv);
-              a1 = v + ((wv - Dl) - sl);
-              two_sum(Dh, -sh, v, wv);
-              a2 = v + ((wv + Dl) - sl);
-            }
-            const float t1 = a1 * inv, t2 = a2 * inv;
-            tmin = fmaxf(tmin, fminf(t1, t2));
-            tmax = fminf(tmax, fmaxf(t1, t2));
-          }
-          const float E = kind == K_CUBE ? sm.err[c] : 4.0f * 3.0f * EPS32 * (fabsf(tmin) + fabsf(tmax)) + 1e-9f;
-          const float m1 = tmax - tmin, m2 = tmax + delta;
-          const float E2 = E + 4.0f * 3.0f * EPS32 * fabsf(delta) + 2e-6f;
-          if (m1 > 2.0f * E && m2 > E2) {
-            hit = true;
-            chord = tmax - fmaxf(tmin, -delta);
-          } else if (!(m1 < -2.0f * E || m2 < -E2)) {
-            amb = true;
-          }
-        } else {
-          float P[3];
-#pragma unroll
-          for (int i = 0; i < 3; ++i) P[i] = fmaf(sm.g[i][c], dx, sm.g[3 + i][c] * dy);
-          const float e0 = sm.g[6][c], e1 = sm.g[7][c], e2 = sm.g[8][c];
-          const float iA = sm.g[10][c];
-          // Closest approach along the ray (t' = tc) and the offset there: h = 1 - |P_perp|^2
-          // has the sign of the reference's discriminant.
-          const float tc = -(P[0] * e0 + P[1] * e1 + P[2] * e2) * iA;
-          const float q0 = fmaf(tc, e0, P[0]), q1 = fmaf(tc, e1, P[1]), q2 = fmaf(tc, e2, P[2]);
-          const float hh = 1.0f - (q0 * q0 + q1 * q1 + q2 * q2);
-          const float E = sm.err[c];
-          if (hh > E) {
-            const float sq = sqrtf(hh * iA);
-            const float t0 = tc - sq, t1 = tc + sq;
-            const float E2 = 4.0f * 3.0f * EPS32 * (fabsf(t1) + fabsf(delta)) + 2e-6f;
-            if (t1 + delta > E2) {
-              hit = true;
-              chord = t1 - fmaxf(t0, -delta);
-            } else {
-              amb = true;
-            }
-          } else if (!(hh < -E)) {
-            amb = true;
-          }
-        }
-      }
-      if (amb) {
-        ++nfb;
-        double ox64, oy64;
-        scan_origin64(t, px, py, sx, sy, ox64, oy64);
-        bool h64;
-        const double c64 = scan_chord64(t, static_cast<uint32_t>(sm.s[c]), ox64, oy64, h64);
-        hit = h64;
-        chord = static_cast<float>(c64);
-      }
+      float chord;
+      const bool hit = scan_pair(t, sm, c, oxh, oxl, oyh, oyl, px, py, sx, sy, chord, nfb);
       if (hit) {
         ++nh;
         const float v = per_crystal ? sm.sig[c] * fmaxf(chord, 0.0f) : fmaxf(chord, 0.0f);
@@ -355,6 +447,65 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const ScanTile* __restric
   }
 }
 
+// Adjoint of k_scan with respect to the per-crystal opacities (single tile).  The forward is
+// recomputed from the developed mask: pass 1 forms each ray's optical depth exactly as k_scan
+// does, pass 2 re-stages the bin's crystals and adds w[p] / spp * T_ray * chord_s for every hit to
+// a per-crystal FP64 sum in shared memory, flushed with one global atomic per staged crystal.
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_adjoint(const ScanTile* __restrict__ tiles,
+                                                               const float* __restrict__ wpx,
+                                                               double* __restrict__ g) {
+  __shared__ ScanSmem sm;
+  __shared__ double gsum[SCAN_CH];
+  const ScanTile& t = tiles[0];
+  const uint32_t bin = blockIdx.x;
+  const uint32_t a = t.spp;
+  const uint32_t tid = threadIdx.x;
+  const ScanRay R = scan_ray(t, bin, tid);
+  const uint32_t b0 = min(t.bin_off[bin], t.items_cap), b1 = min(t.bin_off[bin + 1], t.items_cap);
+  const bool per_crystal = t.sigma_c != nullptr;
+  uint32_t nfb = 0;
+  long long Lfix = 0;
+  for (uint32_t base = b0; base < b1; base += SCAN_CH) {
+    const uint32_t cnt = min(static_cast<uint32_t>(SCAN_CH), b1 - base);
+    __syncthreads();
+    for (uint32_t c = tid; c < cnt; c += blockDim.x) stage_crystal(t, sm, c, t.bin_items[base + c], R.bx0, R.by0);
+    __syncthreads();
+    if (!R.active) continue;
+    for (uint32_t c = 0; c < cnt; ++c) {
+      float chord;
+      if (scan_pair(t, sm, c, R.oxh, R.oxl, R.oyh, R.oyl, R.px, R.py, R.sx, R.sy, chord, nfb)) {
+        const float v = per_crystal ? sm.sig[c] * fmaxf(chord, 0.0f) : fmaxf(chord, 0.0f);
+        Lfix += __float2ll_rn(v * 1099511627776.0f);
+      }
+    }
+  }
+  float coef = 0.0f;
+  if (R.active) {
+    const float L = (float)((double)Lfix * 9.094947017729282e-13);
+    const float T = per_crystal ? expf(-L) : expf(-t.sigma * L);
+    coef = wpx[static_cast<size_t>(R.py) * t.w + R.px] / static_cast<float>(a) * T;
+  }
+  for (uint32_t base = b0; base < b1; base += SCAN_CH) {
+    const uint32_t cnt = min(static_cast<uint32_t>(SCAN_CH), b1 - base);
+    __syncthreads();
+    for (uint32_t c = tid; c < cnt; c += blockDim.x) {
+      stage_crystal(t, sm, c, t.bin_items[base + c], R.bx0, R.by0);
+      gsum[c] = 0.0;
+    }
+    __syncthreads();
+    if (R.active && coef != 0.0f) {
+      for (uint32_t c = 0; c < cnt; ++c) {
+        float chord;
+        if (scan_pair(t, sm, c, R.oxh, R.oxl, R.oyh, R.oyl, R.px, R.py, R.sx, R.sy, chord, nfb))
+          atomicAdd(&gsum[c], static_cast<double>(coef) * static_cast<double>(fmaxf(chord, 0.0f)));
+      }
+    }
+    __syncthreads();
+    for (uint32_t c = tid; c < cnt; c += blockDim.x)
+      if (gsum[c] != 0.0) atomicAdd(&g[sm.s[c]], gsum[c]);
+  }
+}
+
 void launch_scan(const ScanTile* tiles, int ntiles, unsigned long long nbins, unsigned threads, uint32_t* err,
                  unsigned long long* stats, cudaStream_t st) {
   if (nbins == 0) return;
@@ -369,15 +520,26 @@ uint32_t scan_bin_px(uint32_t spp) {
   return b;
 }
 
-void scan(fg_engine* e, const fg_emulsion* em, const fg_scan_cfg& cfg, uint64_t seed,
-          const float* sigma_sorted, const ScanOut& out) {
+// Bins the developed crystals of an emulsion for a scan: descriptor, bin offsets and lists on the
+// device (shared by the forward scan and its adjoint).
+struct ScanPlan {
+  ScanTile t{};
+  DBuf<ScanPrep> prep;
+  DBuf<uint32_t> cnt, off, cur, items;
+  DBuf<ScanTile> td;
+  unsigned nbins = 0, threads = 0;
+};
+
+static void plan_scan(fg_engine* e, const fg_emulsion* em, const fg_scan_cfg& cfg, uint64_t seed,
+                      const float* sigma_sorted, const ScanOut& out, ScanPlan& P) {
   cudaStream_t st = e->stream;
   const uint32_t spp_req = std::max<uint32_t>(cfg.samples_per_pixel, 1);
   const uint32_t g = static_cast<uint32_t>(std::lround(std::sqrt(static_cast<double>(spp_req))));
   const uint32_t a = std::max<uint32_t>(g * g, 1);
   FG_REQUIRE(a <= SCAN_THREADS, "samples_per_pixel too large (at most 256 strata)");
   FG_REQUIRE(cfg.width_px > 0 && cfg.height_px > 0, "scan size must be positive");
-  ScanTile t{};
+  ScanTile& t = P.t;
+  t = ScanTile{};
   t.a = em->a.p;
   t.q = em->q.p;
   t.d = em->d.p;
@@ -407,26 +569,51 @@ void scan(fg_engine* e, const fg_emulsion* em, const fg_scan_cfg& cfg, uint64_t 
   t.sigma = static_cast<float>(cfg.silver_opacity);
   t.mode = cfg.mode;
   const size_t nbins = static_cast<size_t>(t.nbx) * t.nby;
-  DBuf<uint32_t> cnt(nbins + 1, st), off(nbins + 1, st), cur(nbins, st);
-  FG_CUDA(cudaMemsetAsync(cnt.p, 0, (nbins + 1) * sizeof(uint32_t), st));
-  FG_CUDA(cudaMemsetAsync(cur.p, 0, nbins * sizeof(uint32_t), st));
-  if (em->n) k_bin_count<<<grid_for(em->n, 256), 256, 0, st>>>(t, cnt.p);
-  exclusive_scan_u32(cnt.p, off.p, nbins + 1, st);
+  FG_REQUIRE(nbins < 0x80000000ull, "scan too large");
+  P.nbins = static_cast<unsigned>(nbins);
+  P.cnt.alloc(nbins + 1, st);
+  P.off.alloc(nbins + 1, st);
+  P.cur.alloc(nbins, st);
+  FG_CUDA(cudaMemsetAsync(P.cnt.p, 0, (nbins + 1) * sizeof(uint32_t), st));
+  FG_CUDA(cudaMemsetAsync(P.cur.p, 0, nbins * sizeof(uint32_t), st));
+  if (em->n) k_bin_count<<<grid_for(em->n, 256), 256, 0, st>>>(t, P.cnt.p);
+  exclusive_scan_u32(P.cnt.p, P.off.p, nbins + 1, st);
   uint32_t total = 0;
-  FG_CUDA(cudaMemcpyAsync(&total, off.p + nbins, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  FG_CUDA(cudaMemcpyAsync(&total, P.off.p + nbins, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   FG_CUDA(cudaStreamSynchronize(st));
-  DBuf<uint32_t> items(std::max<uint32_t>(total, 1), st);
-  if (em->n) k_bin_fill<<<grid_for(em->n, 256), 256, 0, st>>>(t, off.p, cur.p, items.p);
-  t.bin_off = off.p;
-  t.bin_items = items.p;
+  P.items.alloc(std::max<uint32_t>(total, 1), st);
+  if (em->n) k_bin_fill<<<grid_for(em->n, 256), 256, 0, st>>>(t, P.off.p, P.cur.p, P.items.p);
+  t.bin_off = P.off.p;
+  t.bin_items = P.items.p;
   t.items_cap = total;
-  DBuf<ScanTile> td(1, st);
-  FG_CUDA(cudaMemcpyAsync(td.p, &t, sizeof(ScanTile), cudaMemcpyHostToDevice, st));
+  t.slot_base = 0;
+  P.prep.alloc(std::max<uint32_t>(em->n, 1), st);
+  t.prep = P.prep.p;
+  P.td.alloc(1, st);
+  FG_CUDA(cudaMemcpyAsync(P.td.p, &t, sizeof(ScanTile), cudaMemcpyHostToDevice, st));
+  launch_scan_prep(P.td.p, 1, em->n, P.prep.p, st);
   // Whole warps only: the closing reductions shuffle across all 32 lanes.
-  const unsigned threads = ((t.bin_px * t.bin_px * a + 31) / 32) * 32;
-  k_scan<<<static_cast<unsigned>(nbins), threads, 0, st>>>(td.p, 1, e->d_err, e->d_stats);
+  P.threads = ((t.bin_px * t.bin_px * a + 31) / 32) * 32;
+}
+
+void scan(fg_engine* e, const fg_emulsion* em, const fg_scan_cfg& cfg, uint64_t seed,
+          const float* sigma_sorted, const ScanOut& out) {
+  ScanPlan P;
+  plan_scan(e, em, cfg, seed, sigma_sorted, out, P);
+  k_scan<<<P.nbins, P.threads, 0, e->stream>>>(P.td.p, 1, e->d_err, e->d_stats);
   FG_CUDA(cudaGetLastError());
-  FG_CUDA(cudaStreamSynchronize(st));
+  FG_CUDA(cudaStreamSynchronize(e->stream));
+}
+
+// Adjoint of the scan with respect to the per-crystal opacities: g[s] += sum over the rays of
+// pixel p of w[p] / spp * T_ray * chord_s (w = dL/dT of the pixel, T_ray the ray's transmittance).
+void scan_adjoint(fg_engine* e, const fg_emulsion* em, const fg_scan_cfg& cfg, uint64_t seed,
+                  const float* sigma_sorted, const float* wpx, double* g_sorted) {
+  ScanPlan P;
+  plan_scan(e, em, cfg, seed, sigma_sorted, ScanOut{}, P);
+  k_scan_adjoint<<<P.nbins, P.threads, 0, e->stream>>>(P.td.p, wpx, g_sorted);
+  FG_CUDA(cudaGetLastError());
+  FG_CUDA(cudaStreamSynchronize(e->stream));
 }
 
 }  // namespace fg

@@ -20,7 +20,21 @@ namespace fg {
 constexpr int SCAN_CH = 128;        // crystals staged per pass
 constexpr int SCAN_THREADS = 256;   // rays per CTA (bin_px^2 * strata)
 
+// Bin-independent part of a developed crystal's staging, derived once per crystal in FP64 and
+// rounded (k_scan_prep): each bin that lists the crystal only adds its centre relative to the
+// bin's corner.  128 bytes, read with vector loads.
+struct __align__(16) ScanPrep {
+  double px, py;   // centre x, y (um) as the scan sees it
+  float g[21];     // per-kind terms (see stage_crystal)
+  float m, delta, err, sig;
+  int kind;
+  int pad_[2];
+};
+static_assert(sizeof(ScanPrep) == 128, "ScanPrep layout");
+
 struct ScanTile {
+  const ScanPrep* prep;  // staging of developed crystals (null: derived in each bin)
+  unsigned long long slot_base;  // first crystal slot of this tile in a batch
   const float4* a;
   const float4* q;
   const float4* d;

@@ -23,34 +23,32 @@ __device__ __forceinline__ int find_tile_ull(const SynthTile* tiles, int ntiles,
   return lo;
 }
 
-// Exact test of a fixed-point candidate against the staged grid: every point within r.  Rows of
-// the 5x5x5 neighbourhood are scanned through occupancy bitmasks (one 32-bit word per (y, z) row
-// of the staged region), so only occupied cells are loaded; on the four (y, z) corner rows only
-// the middle three cells can hold a point within r = sqrt(3) cells.
-__device__ __forceinline__ bool syn_free(const uint32_t* grid, const uint32_t* occ, int nz, int rx, int ry,
-                                         int rz, int X, int Y, int Z, int cx, int cy, int cz, uint32_t* err) {
+// Exact test of a fixed-point candidate against the staged grid: every point within r.  The eight
+// corner cells of the 5x5x5 neighbourhood cannot hold a point within r = sqrt(3) cells.  The
+// outer loop stays rolled (small code), the first point within r ends the test.
+__device__ __forceinline__ bool syn_free(const uint32_t* grid, int nz, int rx, int ry, int rz, int X, int Y, int Z,
+                                         int cx, int cy, int cz, uint32_t* err) {
   // The neighbourhood must lie inside the staged region (it does for candidates within 2r of a
   // point of the column); a candidate that fails the check is rejected.
   if (!index_ok(rx >= 2 && rx <= SYN_R - 3 && ry >= 2 && ry <= SYN_R - 3 && rz >= 2 && rz <= nz - 3, err,
                 SITE_SYN_REGION, static_cast<uint32_t>(rx | (ry << 8) | (rz << 16)), blockIdx.x))
     return false;
-#pragma unroll
+#pragma unroll 1
   for (int dz = -2; dz <= 2; ++dz) {
+    const bool zedge = dz == -2 || dz == 2;
 #pragma unroll
     for (int dy = -2; dy <= 2; ++dy) {
-      const bool corner = (dy == -2 || dy == 2) && (dz == -2 || dz == 2);
-      const int lo = corner ? rx - 1 : rx - 2;
-      const uint32_t width = corner ? 3u : 5u;
-      uint32_t bits = (occ[(rz + dz) * SYN_R + (ry + dy)] >> lo) & ((1u << width) - 1u);
-      while (bits) {
-        const int k = __ffs(bits) - 1;
-        bits &= bits - 1;
-        const int dx = lo + k - rx;
-        const uint32_t w = grid[((rz + dz) * SYN_R + (ry + dy)) * SYN_R + (rx + dx)];
-        const int ex = (cx + dx) * SYN_Q + static_cast<int>(w & 1023u) - X;
-        const int ey = (cy + dy) * SYN_Q + static_cast<int>((w >> 10) & 1023u) - Y;
-        const int ez = (cz + dz) * SYN_Q + static_cast<int>((w >> 20) & 1023u) - Z;
-        if (ex * ex + ey * ey + ez * ez < SYN_R2) return false;
+      const int row = ((rz + dz) * SYN_R + (ry + dy)) * SYN_R + rx;
+#pragma unroll
+      for (int dx = -2; dx <= 2; ++dx) {
+        if (zedge && (dx == -2 || dx == 2) && (dy == -2 || dy == 2)) continue;
+        const uint32_t w = grid[row + dx];
+        if (w & OCC) {
+          const int ex = (cx + dx) * SYN_Q + static_cast<int>(w & 1023u) - X;
+          const int ey = (cy + dy) * SYN_Q + static_cast<int>((w >> 10) & 1023u) - Y;
+          const int ez = (cz + dz) * SYN_Q + static_cast<int>((w >> 20) & 1023u) - Z;
+          if (ex * ex + ey * ey + ez * ez < SYN_R2X) return false;
+        }
       }
     }
   }
@@ -68,13 +66,12 @@ __global__ void __launch_bounds__(SYN_WARPS * 32) k_bridson(const SynthTile* __r
                                                             uint32_t* err) {
   extern __shared__ uint32_t syn_sm[];
   uint32_t* grid = syn_sm;                                   // SYN_R^2 * nz cell words
-  uint32_t* occ = grid + SYN_R * SYN_R * nz;                 // SYN_R * nz row masks
-  uint16_t* active = reinterpret_cast<uint16_t*>(occ + SYN_R * nz);  // SYN_B^2 * (nz - 4)
+  uint16_t* active = reinterpret_cast<uint16_t*>(grid + SYN_R * SYN_R * nz);  // SYN_B^2 * (nz - 4)
   __shared__ int s_nact, s_wsum[SYN_WARPS];
   __shared__ int s_pick[SYN_WARPS];
   __shared__ unsigned s_vmask[SYN_WARPS];
-  __shared__ int s_win[SYN_WARPS][3];
-  __shared__ int s_ok[SYN_WARPS];
+  __shared__ int s_cx[SYN_WARPS][32], s_cy[SYN_WARPS][32], s_cz[SYN_WARPS][32];  // valid candidates
+  __shared__ int s_wx[SYN_WARPS], s_wy[SYN_WARPS], s_wz[SYN_WARPS];             // accepted this round
 
   // Column of this CTA: tile, then the j-th column of this colour class in that tile.
   int lo = 0, hi = ntiles - 1;
@@ -96,7 +93,7 @@ __global__ void __launch_bounds__(SYN_WARPS * 32) k_bridson(const SynthTile* __r
   const int acap = SYN_B * SYN_B * (nz - 4);  // active list capacity: one entry per column cell
   uint32_t* tc = cells + t.cell_base;
 
-  // Stage the region (column + halo) of the cell grid, then its row masks.
+  // Stage the region (column + halo) of the cell grid.
   for (int i = tid; i < ncell; i += blockDim.x) {
     const int rx = i % SYN_R, ry = (i / SYN_R) % SYN_R, rz = i / (SYN_R * SYN_R);
     const int gx = ox + rx, gy = oy + ry, gz = rz - 2;
@@ -107,11 +104,6 @@ __global__ void __launch_bounds__(SYN_WARPS * 32) k_bridson(const SynthTile* __r
   }
   if (tid == 0) s_nact = 0;
   __syncthreads();
-  for (int r = tid; r < SYN_R * nz; r += blockDim.x) {
-    uint32_t m = 0;
-    for (int x = 0; x < SYN_R; ++x) m |= (grid[r * SYN_R + x] & OCC) ? (1u << x) : 0u;
-    occ[r] = m;
-  }
   // Active list: the column's points in cell order (deterministic block-wide compaction).
   const int bw = x1 - x0, bh = y1 - y0;
   const int bcells = bw * bh * gd;
@@ -145,10 +137,9 @@ __global__ void __launch_bounds__(SYN_WARPS * 32) k_bridson(const SynthTile* __r
       if (X >= static_cast<int>(t.XW) || Y >= static_cast<int>(t.YW) || Z >= static_cast<int>(t.ZW)) continue;
       const int cx = X >> 10, cy = Y >> 10, cz = Z >> 10;
       const int rx = cx - ox, ry = cy - oy, rz = cz + 2;
-      if (!syn_free(grid, occ, nz, rx, ry, rz, X, Y, Z, cx, cy, cz, err)) continue;
+      if (!syn_free(grid, nz, rx, ry, rz, X, Y, Z, cx, cy, cz, err)) continue;
       const int ridx = (rz * SYN_R + ry) * SYN_R + rx;
       grid[ridx] = syn_word(X, Y, Z);
-      occ[rz * SYN_R + ry] |= 1u << rx;
       if (index_ok(s_nact < acap, err, SITE_SYN_ACTIVE, s_nact, blockIdx.x)) active[s_nact++] = static_cast<uint16_t>(ridx);
       break;
     }
@@ -196,60 +187,85 @@ __global__ void __launch_bounds__(SYN_WARPS * 32) k_bridson(const SynthTile* __r
         Z = static_cast<int>(floorf(fz * SYN_Q));
         if (X < static_cast<int>(t.XW) && Y < static_cast<int>(t.YW) && Z < static_cast<int>(t.ZW)) {
           const int cx = X >> 10, cy = Y >> 10, cz = Z >> 10;
-          valid = syn_free(grid, occ, nz, cx - ox, cy - oy, cz + 2, X, Y, Z, cx, cy, cz, err);
+          if (cx >= x0 - SYN_SPILL && cx < x1 + SYN_SPILL && cy >= y0 - SYN_SPILL && cy < y1 + SYN_SPILL)
+            valid = syn_free(grid, nz, cx - ox, cy - oy, cz + 2, X, Y, Z, cx, cy, cz, err);
         }
       }
     }
     const unsigned vm = __ballot_sync(0xffffffffu, valid);
-    if (vm && lane == __ffs(vm) - 1) {
-      s_win[warp][0] = X;
-      s_win[warp][1] = Y;
-      s_win[warp][2] = Z;
+    if (valid) {
+      s_cx[warp][lane] = X;
+      s_cy[warp][lane] = Y;
+      s_cz[warp][lane] = Z;
     }
     if (lane == 0) s_vmask[warp] = vm;
     __syncthreads();
-    // A winner commits unless it lies within r of the winner of an earlier warp of this round
-    // (then its point simply stays active for a later step).
-    if (tid < SYN_WARPS) {
-      bool ok = s_vmask[tid] != 0;
-      for (int w = 0; w < tid && ok; ++w) {
-        if (!s_vmask[w]) continue;
-        const int ex = s_win[tid][0] - s_win[w][0], ey = s_win[tid][1] - s_win[w][1], ez = s_win[tid][2] - s_win[w][2];
-        ok = ex * ex + ey * ey + ez * ez >= SYN_R2;
-      }
-      s_ok[tid] = ok;
-    }
-    __syncthreads();
-    if (tid == 0) {
-      int rem[SYN_WARPS];
-      int nrem = 0;
+    if (warp == 0) {
+      // The round's steps in warp order, exactly as if they ran one after another: warp w keeps its
+      // first candidate (lane order) that is free in the grid and at least r from the points
+      // accepted for warps < w; with none left, its point retires.  One lane per candidate.
+      int ncom = 0;
+      unsigned retire = 0;
       for (int w = 0; w < SYN_WARPS; ++w) {
-        if (!s_vmask[w]) {
-          rem[nrem++] = s_pick[w];  // 30 misses: the point retires
+        const unsigned m = s_vmask[w];
+        bool ok = false;
+        int X = 0, Y = 0, Z = 0;
+        if ((m >> lane) & 1u) {
+          X = s_cx[w][lane];
+          Y = s_cy[w][lane];
+          Z = s_cz[w][lane];
+          ok = true;
+          for (int j = 0; j < ncom; ++j) {
+            const int ex = X - s_wx[j], ey = Y - s_wy[j], ez = Z - s_wz[j];
+            if (ex * ex + ey * ey + ez * ez < SYN_R2X) {
+              ok = false;
+              break;
+            }
+          }
+        }
+        const unsigned okm = __ballot_sync(0xffffffffu, ok);
+        if (okm == 0) {
+          retire |= 1u << w;
           continue;
         }
-        if (!s_ok[w]) continue;
-        const int CX = s_win[w][0], CY = s_win[w][1], CZ = s_win[w][2];
-        const int ccx = CX >> 10, ccy = CY >> 10, ccz = CZ >> 10;
-        const int rx = ccx - ox, ry = ccy - oy, rz = ccz + 2;
-        if (!index_ok(rx >= 0 && rx < SYN_R && ry >= 0 && ry < SYN_R && rz >= 0 && rz < nz, err, SITE_SYN_COMMIT,
-                      static_cast<uint32_t>(rx | (ry << 8) | (rz << 16)), blockIdx.x))
-          continue;
-        const int ridx = (rz * SYN_R + ry) * SYN_R + rx;
-        grid[ridx] = syn_word(CX, CY, CZ);
-        occ[rz * SYN_R + ry] |= 1u << rx;
-        if (ccx >= x0 && ccx < x1 && ccy >= y0 && ccy < y1 &&
-            index_ok(s_nact < acap, err, SITE_SYN_ACTIVE, s_nact, blockIdx.x))
-          active[s_nact++] = static_cast<uint16_t>(ridx);
+        if (lane == __ffs(okm) - 1) {
+          s_wx[ncom] = X;
+          s_wy[ncom] = Y;
+          s_wz[ncom] = Z;
+          const int ccx = X >> 10, ccy = Y >> 10, ccz = Z >> 10;
+          const int rx = ccx - ox, ry = ccy - oy, rz = ccz + 2;
+          if (index_ok(rx >= 0 && rx < SYN_R && ry >= 0 && ry < SYN_R && rz >= 0 && rz < nz, err, SITE_SYN_COMMIT,
+                       static_cast<uint32_t>(rx | (ry << 8) | (rz << 16)), blockIdx.x)) {
+            const int ridx = (rz * SYN_R + ry) * SYN_R + rx;
+            grid[ridx] = syn_word(X, Y, Z);
+            if (ccx >= x0 && ccx < x1 && ccy >= y0 && ccy < y1 &&
+                index_ok(s_nact < acap, err, SITE_SYN_ACTIVE, s_nact, blockIdx.x))
+              active[s_nact++] = static_cast<uint16_t>(ridx);
+          }
+        }
+        ++ncom;
+        __syncwarp();
       }
-      // Retire in descending index order (swap-remove keeps lower indices valid); skip repeats.
-      for (int a = 1; a < nrem; ++a)
-        for (int b = a; b > 0 && rem[b] > rem[b - 1]; --b) {
-          const int tmp = rem[b]; rem[b] = rem[b - 1]; rem[b - 1] = tmp;
+      // Retire the points of failed steps, each once, in descending list order (swap-remove keeps
+      // the lower indices valid): lane w speaks for warp w.
+      const bool mine = lane < SYN_WARPS && ((retire >> lane) & 1u);
+      const int mypick = mine ? s_pick[lane] : -1;
+      bool first = mine;
+      for (int w2 = 0; w2 < lane && first; ++w2)
+        if (((retire >> w2) & 1u) && s_pick[w2] == mypick) first = false;
+      const unsigned dm = __ballot_sync(0xffffffffu, first);
+      int rank = 0;
+      if (first)
+        for (int w2 = 0; w2 < SYN_WARPS; ++w2)
+          if (((dm >> w2) & 1u) && s_pick[w2] > mypick) ++rank;
+      const int K = __popc(dm);
+      for (int k = 0; k < K; ++k) {
+        if (first && rank == k) {
+          const int last = s_nact - 1;
+          active[mypick] = active[last];
+          s_nact = last;
         }
-      for (int a = 0; a < nrem; ++a) {
-        if (a > 0 && rem[a] == rem[a - 1]) continue;
-        active[rem[a]] = active[--s_nact];
+        __syncwarp();
       }
     }
   }
@@ -385,7 +401,6 @@ void launch_bridson(const SynthTile* tiles, int ntiles, int color, unsigned ncol
 
 size_t bridson_smem(int gdmax) {
   return static_cast<size_t>(SYN_R) * SYN_R * (gdmax + 4) * sizeof(uint32_t) +
-         static_cast<size_t>(SYN_R) * (gdmax + 4) * sizeof(uint32_t) +
          static_cast<size_t>(SYN_B) * SYN_B * gdmax * sizeof(uint16_t);
 }
 

@@ -1,15 +1,17 @@
 // Device crystal synthesis (emulsion.rs:155-220, poisson.rs:14-132).
 //
 // Bridson's sampler is sequential.  On the device the tile's cell grid (cell = r_min / sqrt(3),
-// at most one point per cell, as poisson.rs:25-31) is cut into columns of 12 x 12 cells that span
-// the full depth.  Columns are processed in four colour classes (column x and y parity); columns
-// of one class are a column apart, so they never touch the same cells.  Each column runs Bridson
-// (k = 30 candidates in the shell [r, 2r], first valid candidate wins) from the points already
-// inside it (spilled in by earlier classes) or from one random seed; candidates may spill up to
-// 2r out of the column.  Sixteen warps per column each take a Bridson step on a randomly picked
-// active point; a step's winner commits unless it lies within r of an earlier warp's winner of
-// the same round (its point then stays active for a later step).  Positions are fixed point (1/1024 of a cell) so
-// every distance test is exact integer arithmetic.
+// at most one point per cell, as poisson.rs:25-31) is cut into columns of SYN_B x SYN_B cells that
+// span the full depth.  Columns are processed in four colour classes (column x and y parity);
+// columns of one class are a column apart, so they never touch the same cells.  Each column runs
+// Bridson (k = 30 candidates in the shell [r, 2r], first valid candidate wins) from the points
+// already inside it (spilled in by earlier classes) or from one random seed; accepted points may
+// lie up to SYN_SPILL cells outside the column (the rest of the shell is left to the neighbouring
+// columns of later classes).  Each round, every warp of the column's CTA takes a Bridson step on a
+// randomly picked active point, one candidate per lane; then one warp resolves the steps in warp
+// order exactly as if they had run one after another (a step keeps its first candidate that is
+// also at least r from the points accepted for earlier warps, else its point retires).
+// Positions are fixed point (1/1024 of a cell) so every distance test is exact integer arithmetic.
 //
 // Bridson started from many seeds packs ~0.3-0.6 % denser than from one, so each tile is then
 // thinned (independent deletion) to the count Bridson yields on the same box:
@@ -20,13 +22,21 @@
 
 namespace fg {
 
-constexpr int SYN_B = 12;        // column edge in cells
-constexpr int SYN_HALO = 6;      // spill (4) + check reach (2)
-constexpr int SYN_R = SYN_B + 2 * SYN_HALO;  // staged region edge (24)
-constexpr int SYN_WARPS = 16;
+constexpr int SYN_B = 8;         // column edge in cells
+constexpr int SYN_SPILL = 2;     // cells an accepted point may lie outside its column
+constexpr int SYN_HALO = SYN_SPILL + 2;      // + the reach of the neighbourhood test
+constexpr int SYN_R = SYN_B + 2 * SYN_HALO;  // staged region edge
+// Columns of one colour class are one column apart: what one writes (its spill zone) must not
+// reach what another reads (its halo).
+static_assert(SYN_SPILL + SYN_HALO <= SYN_B, "colour classes would overlap");
+constexpr int SYN_WARPS = 8;
 constexpr int SYN_K = 30;        // Bridson's k
 constexpr int32_t SYN_Q = 1024;  // fixed-point steps per cell
 constexpr int32_t SYN_R2 = 3 * SYN_Q * SYN_Q;  // r^2 with r = sqrt(3) cells
+// Exclusion radius squared of the sampler: r^2 plus 128 units^2 (2e-5 r), so that two points kept
+// at the smallest allowed distance are still r_min apart after their positions are rounded to
+// float (about 1e-5 um at 100 um).
+constexpr int32_t SYN_R2X = SYN_R2 + 128;
 constexpr uint32_t OCC = 0x80000000u;
 
 __host__ __device__ inline double bridson_density(double W, double H, double D, double r) {

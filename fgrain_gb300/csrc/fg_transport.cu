@@ -13,14 +13,13 @@
 namespace fg {
 
 // ---------------------------------------------------------------------------------------------
-// Production kernel with lane refill: each loop turn every live lane runs one bounce; lanes whose
-// packet died take the next photon of the (optionally position-ordered) queue, so the warp stays
-// full until the queue is empty.
-__global__ void __launch_bounds__(256) k_transport_refill(const TileDesc* __restrict__ tiles, int ntiles,
-                                                         unsigned long long total,
-                                                         const uint32_t* __restrict__ order,
-                                                         unsigned long long* next, uint32_t* err,
-                                                         unsigned long long* stats) {
+// Production kernel with lane refill: each loop turn every lane with a live packet runs one bounce
+// (its LBVH walk, then absorption and the move or scatter); lanes whose packet died take the next
+// photon of the position-ordered queue, so the warp stays full until the queue is empty.
+__global__ void __launch_bounds__(256, 4) k_transport(const TileDesc* __restrict__ tiles, int ntiles,
+                                                     unsigned long long total, const uint32_t* __restrict__ order,
+                                                     unsigned long long* next, uint32_t* err,
+                                                     unsigned long long* stats) {
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   HitS hits[HMAX];
@@ -254,7 +253,7 @@ void launch_transport_shape(const TileDesc* tiles_dev, int ntiles, unsigned long
   const unsigned long long warps = (total + 31) / 32;
   const unsigned long long need = (warps * 32 + threads - 1) / threads;
   blocks = static_cast<unsigned>(std::max<unsigned long long>(std::min<unsigned long long>(blocks, need), 1));
-  k_transport_refill<<<blocks, threads, 0, st>>>(tiles_dev, ntiles, total, order, counter, err, stats);
+  k_transport<<<blocks, threads, 0, st>>>(tiles_dev, ntiles, total, order, counter, err, stats);
   FG_CUDA(cudaGetLastError());
 }
 

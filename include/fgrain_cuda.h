@@ -159,6 +159,11 @@ const char* fg_status_string(fg_status s);
 fg_status fg_emulsion_preset(const char* name, double width, double height, fg_emulsion_cfg* out);
 
 /* ---- emulsions ---- */
+/* VirtualEmulsionLayer::synthesize (src/emulsion.rs:155-220) on the device: Poisson-disk
+ * positions (src/poisson.rs:14-132, column-parallel Bridson thinned to the reference sampler's
+ * density) and crystal attributes, then the LBVH.  Crystal ids follow the Morton order of the
+ * synthesis grid. */
+fg_status fg_emulsion_synthesize(fg_engine* e, const fg_emulsion_cfg* cfg, uint64_t seed, fg_emulsion** out);
 /* Upload a crystal set (for parity runs on exactly the oracle's crystals).  The device keeps the
  * FP64 values for exact predicates and builds the Morton-ordered LBVH. */
 fg_status fg_emulsion_upload(fg_engine* e, const fg_emulsion_cfg* cfg, const fg_crystals_host* c,
@@ -195,6 +200,39 @@ fg_status fg_scan_emulsion(fg_engine* e, const fg_emulsion* em, const fg_scan_cf
                            uint8_t* image8);
 
 /* ---- replay (parity) ---- */
+/* Differentiable scan (scan_emulsion, src/transmittance.rs:65-171, followed by the scanner OTF of
+ * src/image_pipeline.rs:825-855).  signal = OTF_s(exposure * T) per pixel, where T is the scanned
+ * transmittance (Negative mode; cfg->mode is ignored) with per-crystal opacities sigma_per_crystal
+ * (crystal-index order; NULL: cfg->silver_opacity for all) and OTF_s the separable 3-tap
+ * clamp-to-edge filter with taps (g, 1, g) / (1 + 2 g), g = exp(-1 / (2 s^2));
+ * s = 0.3904441347190481 reproduces the reference's taps (0.035, 0.93, 0.035).  signal and
+ * transmittance (width*height floats each) may be NULL, not both. */
+fg_status fg_scan_signal(fg_engine* e, const fg_emulsion* em, const fg_scan_cfg* cfg, uint64_t seed,
+                         const float* sigma_per_crystal, double exposure, double otf_sigma, float* signal,
+                         float* transmittance);
+/* Hand-written adjoint of fg_scan_signal (no counterpart in the reference): for the upstream
+ * gradient dL_dsignal (width*height) returns dL/dsigma per crystal (crystal-index order; 0 for
+ * undeveloped crystals), dL/dexposure and dL/dotf_sigma.  Any output may be NULL.  The forward is
+ * recomputed from the developed mask; no intermediate of an earlier call is kept. */
+fg_status fg_scan_backward(fg_engine* e, const fg_emulsion* em, const fg_scan_cfg* cfg, uint64_t seed,
+                           const float* sigma_per_crystal, double exposure, double otf_sigma,
+                           const float* dL_dsignal, float* dL_dsigma, double* dL_dexposure,
+                           double* dL_dotf_sigma);
+
+/* ---- image stages around the tile path (host arrays, row-major floats) ---- */
+/* Hann overlap blend of tile densities into d_norm (src/image_pipeline.rs:593-649): desc holds
+ * (tx, ty, x_start, y_start, tw, th) per tile in grid order (index ty * ntx + tx, the order of
+ * src/image_pipeline.rs:377-424); tiles[t] is tile t's tw*th density. */
+fg_status fg_blend_tiles(fg_engine* e, uint32_t out_w, uint32_t out_h, uint32_t tile_step, uint32_t pad,
+                         uint32_t ntiles, const uint32_t* desc, const float* const* tiles, float* d_norm);
+/* Scanner OTF (src/image_pipeline.rs:825-855): separable 3-tap clamp-to-edge filter; taps NULL
+ * means the reference's (0.035, 0.93, 0.035). */
+fg_status fg_scanner_otf(fg_engine* e, const float* in, uint32_t w, uint32_t h, const float* taps, float* out);
+/* Supersample downsample (src/image_pipeline.rs:315-330): Triangle filter of the image crate,
+ * vertical pass then horizontal, w x h -> ow x oh. */
+fg_status fg_resize_triangle(fg_engine* e, const float* in, uint32_t w, uint32_t h, uint32_t ow, uint32_t oh,
+                             float* out);
+
 /* Replays recorded segments with the exact hit rule and FP64 per-hit arithmetic.  Latent counts
  * are added to the emulsion.  Hit lists are returned CSR style: offsets[nseg+1], ids (crystal
  * indices in canonical order); *nhits receives the total even when it exceeds id_cap. */

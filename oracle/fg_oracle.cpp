@@ -1032,6 +1032,151 @@ int or_scan(const or_crystals* c, const or_emulsion_cfg* ecfg, const or_scan_cfg
   return 0;
 }
 
+// ---- differentiable scan and its adjoint (FP64) ----
+
+void or_otf_taps(double s, double taps[3], double dtaps[3]) {
+  // g = exp(-1 / (2 s^2)); taps = (g, 1, g) / (1 + 2 g); dg/ds = g / s^3.
+  const double g = std::exp(-1.0 / (2.0 * s * s));
+  const double n = 1.0 + 2.0 * g;
+  taps[0] = taps[2] = g / n;
+  taps[1] = 1.0 / n;
+  const double dg = g / (s * s * s);
+  dtaps[0] = dtaps[2] = dg / (n * n);
+  dtaps[1] = -2.0 * dg / (n * n);
+}
+
+// One separable clamp-to-edge 3-tap pass (image_pipeline.rs:833-853) along x (axis 0) or y.
+static void otf_pass(const double* in, uint32_t w, uint32_t h, const double k[3], int axis, double* out) {
+  for (uint32_t y = 0; y < h; ++y)
+    for (uint32_t x = 0; x < w; ++x) {
+      const size_t i = static_cast<size_t>(y) * w + x;
+      size_t im, ip;
+      if (axis == 0) {
+        im = static_cast<size_t>(y) * w + (x > 0 ? x - 1 : 0);
+        ip = static_cast<size_t>(y) * w + std::min(x + 1, w - 1);
+      } else {
+        im = static_cast<size_t>(y > 0 ? y - 1 : 0) * w + x;
+        ip = static_cast<size_t>(std::min(y + 1, h - 1)) * w + x;
+      }
+      out[i] = in[im] * k[0] + in[i] * k[1] + in[ip] * k[2];
+    }
+}
+
+// Transpose of otf_pass: scatters each output's weights back onto the pixels it read.
+static void otf_pass_t(const double* g, uint32_t w, uint32_t h, const double k[3], int axis, double* out) {
+  std::fill(out, out + static_cast<size_t>(w) * h, 0.0);
+  for (uint32_t y = 0; y < h; ++y)
+    for (uint32_t x = 0; x < w; ++x) {
+      const size_t i = static_cast<size_t>(y) * w + x;
+      size_t im, ip;
+      if (axis == 0) {
+        im = static_cast<size_t>(y) * w + (x > 0 ? x - 1 : 0);
+        ip = static_cast<size_t>(y) * w + std::min(x + 1, w - 1);
+      } else {
+        im = static_cast<size_t>(y > 0 ? y - 1 : 0) * w + x;
+        ip = static_cast<size_t>(std::min(y + 1, h - 1)) * w + x;
+      }
+      out[im] += k[0] * g[i];
+      out[i] += k[1] * g[i];
+      out[ip] += k[2] * g[i];
+    }
+}
+
+int or_scan_signal(const or_crystals* c, const or_emulsion_cfg* ecfg, const or_scan_cfg* scfg,
+                   uint64_t seed, int mode, int threads, const double* sigma_c, double exposure,
+                   double otf_sigma, double* S, double* T) {
+  const uint32_t w = scfg->width_px, h = scfg->height_px;
+  const size_t np = static_cast<size_t>(w) * h;
+  std::vector<float> out(np);
+  std::vector<double> t64(np), tmp(np);
+  or_scan_cfg cfg = *scfg;
+  cfg.mode = 0;
+  or_scan(c, ecfg, &cfg, seed, mode, threads, sigma_c, out.data(), nullptr, t64.data(), nullptr);
+  double k[3], dk[3];
+  or_otf_taps(otf_sigma, k, dk);
+  otf_pass(t64.data(), w, h, k, 0, tmp.data());
+  otf_pass(tmp.data(), w, h, k, 1, S);
+  for (size_t i = 0; i < np; ++i) S[i] *= exposure;
+  if (T) std::copy(t64.begin(), t64.end(), T);
+  return 0;
+}
+
+int or_scan_backward(const or_crystals* c, const or_emulsion_cfg* ecfg, const or_scan_cfg* scfg,
+                     uint64_t seed, int mode, int threads, const double* sigma_c, double exposure,
+                     double otf_sigma, const double* dL_dS, double* g_sigma, double* g_exposure,
+                     double* g_otf) {
+  const uint32_t w = scfg->width_px, h = scfg->height_px;
+  const size_t np = static_cast<size_t>(w) * h;
+  const uint32_t spp = std::max<uint32_t>(scfg->samples_per_pixel, 1);
+  const uint32_t g = static_cast<uint32_t>(std::round(std::sqrt(static_cast<double>(spp))));
+  const uint32_t a = std::max<uint32_t>(g * g, 1);
+  const double pw = ecfg->width / static_cast<double>(w), ph = ecfg->height / static_cast<double>(h);
+  // Forward T, recomputed from the developed mask.
+  std::vector<float> out(np);
+  std::vector<double> T(np), H(np), dH(np), O(np), dO1(np), dO2(np), A1(np), A(np);
+  or_scan_cfg cfg = *scfg;
+  cfg.mode = 0;
+  or_scan(c, ecfg, &cfg, seed, mode, threads, sigma_c, out.data(), nullptr, T.data(), nullptr);
+  double k[3], dk[3];
+  or_otf_taps(otf_sigma, k, dk);
+  // S = e V(H(T)); dS/ds = e (V'(H(T)) + V(H'(T))); dS/de = V(H(T)).
+  otf_pass(T.data(), w, h, k, 0, H.data());
+  otf_pass(T.data(), w, h, dk, 0, dH.data());
+  otf_pass(H.data(), w, h, k, 1, O.data());
+  otf_pass(H.data(), w, h, dk, 1, dO1.data());
+  otf_pass(dH.data(), w, h, k, 1, dO2.data());
+  double ge = 0.0, gs = 0.0;
+  for (size_t i = 0; i < np; ++i) {
+    ge += dL_dS[i] * O[i];
+    gs += dL_dS[i] * (dO1[i] + dO2[i]);
+  }
+  if (g_exposure) *g_exposure = ge;
+  if (g_otf) *g_otf = exposure * gs;
+  if (!g_sigma) return 0;
+  // dL/dT = e H^T(V^T(dL/dS)); dT/dsigma_c = mean over the pixel's rays of -T_ray L_c.
+  otf_pass_t(dL_dS, w, h, k, 1, A1.data());
+  otf_pass_t(A1.data(), w, h, k, 0, A.data());
+  std::fill(g_sigma, g_sigma + c->n, 0.0);
+  std::vector<Crystal> dev;
+  std::vector<size_t> orig;
+  for (size_t i = 0; i < c->n; ++i) {
+    Crystal kk = load_crystal(c, i);
+    if (kk.developed) {
+      dev.push_back(kk);
+      orig.push_back(i);
+    }
+  }
+  if (dev.empty()) return 0;
+  RefBvh bvh;
+  bvh.build(dev);
+  const int nt = threads > 0 ? threads : omp_get_max_threads();
+  std::vector<std::vector<double>> part(nt, std::vector<double>(c->n, 0.0));
+#pragma omp parallel num_threads(nt)
+  {
+    std::vector<Hit> hits;
+    std::vector<double>& gp = part[omp_get_thread_num()];
+#pragma omp for schedule(static)
+    for (int64_t py = 0; py < static_cast<int64_t>(h); ++py)
+      for (uint32_t px = 0; px < w; ++px) {
+        const double coef = -exposure * A[static_cast<size_t>(py) * w + px] / static_cast<double>(a);
+        if (coef == 0.0) continue;
+        for (uint32_t sy = 0; sy < g; ++sy)
+          for (uint32_t sx = 0; sx < g; ++sx) {
+            const V3 o = scan_origin(seed, px, static_cast<uint32_t>(py), sx, sy, g, pw, ph, ecfg->depth + 0.1);
+            ray_hits(bvh, dev, o, v3(0.0, 0.0, -1.0), mode, hits);
+            double tau = 0.0;
+            for (const Hit& hh : hits)
+              tau += (sigma_c ? sigma_c[orig[hh.idx]] : scfg->silver_opacity) * rmax(hh.t1 - hh.t0, 0.0);
+            const double tr = std::exp(-tau);
+            for (const Hit& hh : hits) gp[orig[hh.idx]] += coef * tr * rmax(hh.t1 - hh.t0, 0.0);
+          }
+      }
+  }
+  for (int t = 0; t < nt; ++t)
+    for (size_t i = 0; i < c->n; ++i) g_sigma[i] += part[t][i];
+  return 0;
+}
+
 // Preset tables for the tile worker (emulsion.rs:46-136, image_pipeline.rs:925-976).
 static or_emulsion_cfg preset_cfg(int preset, double w, double h) {
   or_emulsion_cfg c{};

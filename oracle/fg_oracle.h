@@ -175,6 +175,24 @@ int or_scan(const or_crystals* c, const or_emulsion_cfg* ecfg, const or_scan_cfg
             uint64_t seed, int mode, int threads, const double* sigma_c, float* out,
             uint8_t* image8, double* T64, uint16_t* ray_hits);
 
+/* The differentiable scan (the adjoint asked of this build; the reference scans with one opacity
+ * and filters with fixed taps).  S = OTF_s(e T): T is or_scan's FP64 stratified mean
+ * transmittance with per-crystal opacities sigma_c (NULL: scfg->silver_opacity for all), e an
+ * exposure multiplier and OTF_s the scanner's separable 3-tap clamp-to-edge filter
+ * (image_pipeline.rs:825-855) with taps (g, 1, g) / (1 + 2 g), g = exp(-1 / (2 s^2)); the
+ * reference's taps (0.035, 0.93, 0.035) are s = 0.3904441347190481.  FP64 throughout. */
+void or_otf_taps(double s, double taps[3], double dtaps[3]);
+int or_scan_signal(const or_crystals* c, const or_emulsion_cfg* ecfg, const or_scan_cfg* scfg,
+                   uint64_t seed, int mode, int threads, const double* sigma_c, double exposure,
+                   double otf_sigma, double* S, double* T);
+/* Adjoint of or_scan_signal for an upstream gradient dL_dS (w*h): gradients with respect to the
+ * per-crystal opacities (crystal-index order; undeveloped crystals get 0), the exposure
+ * multiplier and the OTF width.  The forward is recomputed from the developed mask. */
+int or_scan_backward(const or_crystals* c, const or_emulsion_cfg* ecfg, const or_scan_cfg* scfg,
+                     uint64_t seed, int mode, int threads, const double* sigma_c, double exposure,
+                     double otf_sigma, const double* dL_dS, double* g_sigma, double* g_exposure,
+                     double* g_otf);
+
 /* Scan ray origins exactly as or_scan forms them (pixel-major, stratum-minor). */
 int or_scan_ray_origins(const or_emulsion_cfg* ecfg, const or_scan_cfg* scfg, uint64_t seed,
                         double* origins);

@@ -334,6 +334,47 @@ def scan(cr: Crystals, cfg, scfg, seed, mode=CANONICAL, threads=0, sigma_c=None,
     return r
 
 
+OTF_SIGMA_REFERENCE = 0.3904441347190481  # otf_taps(s) = (0.035, 0.93, 0.035), the reference's scanner taps
+
+
+def otf_taps(s):
+    k = (C.c_double * 3)()
+    dk = (C.c_double * 3)()
+    lib().or_otf_taps(C.c_double(s), k, dk)
+    return list(k), list(dk)
+
+
+def scan_signal(cr: Crystals, cfg, scfg, seed, sigma_c=None, exposure=1.0, otf_sigma=OTF_SIGMA_REFERENCE,
+                mode=CANONICAL, threads=0):
+    """Differentiable scan S = OTF_s(e T) in FP64; returns (S, T)."""
+    sc = scan_cfg(scfg)
+    ec = emulsion_cfg(cfg)
+    S = np.zeros((sc.height_px, sc.width_px))
+    T = np.zeros_like(S)
+    sig = None if sigma_c is None else np.ascontiguousarray(sigma_c, np.float64)
+    s = cr.struct()
+    lib().or_scan_signal(C.byref(s), C.byref(ec), C.byref(sc), C.c_uint64(seed), mode, threads, _p(sig, C.c_double),
+                         C.c_double(exposure), C.c_double(otf_sigma), _p(S, C.c_double), _p(T, C.c_double))
+    return S, T
+
+
+def scan_backward(cr: Crystals, cfg, scfg, seed, dL_dS, sigma_c=None, exposure=1.0,
+                  otf_sigma=OTF_SIGMA_REFERENCE, mode=CANONICAL, threads=0):
+    """FP64 adjoint of scan_signal: (dL/dsigma per crystal, dL/dexposure, dL/dotf_sigma)."""
+    sc = scan_cfg(scfg)
+    ec = emulsion_cfg(cfg)
+    g = np.ascontiguousarray(dL_dS, np.float64).reshape(sc.height_px, sc.width_px)
+    gs = np.zeros(len(cr))
+    ge = C.c_double()
+    go = C.c_double()
+    sig = None if sigma_c is None else np.ascontiguousarray(sigma_c, np.float64)
+    s = cr.struct()
+    lib().or_scan_backward(C.byref(s), C.byref(ec), C.byref(sc), C.c_uint64(seed), mode, threads,
+                           _p(sig, C.c_double), C.c_double(exposure), C.c_double(otf_sigma), _p(g, C.c_double),
+                           _p(gs, C.c_double), C.byref(ge), C.byref(go))
+    return gs, ge.value, go.value
+
+
 def scan_ray_origins(cfg, scfg, seed):
     sc = scan_cfg(scfg)
     ec = emulsion_cfg(cfg)
@@ -361,6 +402,15 @@ def scanner_otf(field, taps=(0.035, 0.93, 0.035)):
     h, w = f.shape
     out = np.zeros_like(f)
     lib().or_scanner_otf(_p(f, C.c_float), w, h, (C.c_float * 3)(*taps), _p(out, C.c_float))
+    return out
+
+
+def blend_tiles(out_w, out_h, grid, step, pad, densities):
+    desc = np.array([[t.tx, t.ty, t.x_start, t.y_start, t.tw, t.th] for t in grid], np.uint32).ravel()
+    ds = [np.ascontiguousarray(d, np.float32) for d in densities]
+    ptrs = (C.POINTER(C.c_float) * len(ds))(*[_p(d, C.c_float) for d in ds])
+    out = np.zeros((out_h, out_w), np.float32)
+    lib().or_blend_tiles(out_w, out_h, step, pad, len(ds), _p(desc, C.c_uint32), ptrs, _p(out, C.c_float))
     return out
 
 
