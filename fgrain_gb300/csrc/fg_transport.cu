@@ -10,6 +10,10 @@
 #include "fg_internal.h"
 #include "fg_transport.cuh"
 
+#ifndef FG_DEFERRED_LEAVES
+#define FG_DEFERRED_LEAVES 1
+#endif
+
 namespace fg {
 
 // ---------------------------------------------------------------------------------------------
@@ -53,10 +57,17 @@ __global__ void __launch_bounds__(256, 4) k_transport(const TileDesc* __restrict
       need = __ballot_sync(0xffffffffu, !alive && !done);
     }
     if (!__any_sync(0xffffffffu, alive)) break;
+    // The lanes with a bounce to run walk together (deferred leaf tests need the full set).
+    const bool go = alive && ph.b < tiles[tile].max_bounces;
+    const unsigned amask = __ballot_sync(0xffffffffu, go);
     if (alive) {
-      uint32_t nh = 0;
-      alive = photon_bounce(tiles[tile], ph, hits, err, nh);
-      my_hits += nh;
+      if (!go) {
+        alive = false;
+      } else {
+        uint32_t nh = 0;
+        alive = photon_bounce(tiles[tile], ph, hits, err, nh, FG_DEFERRED_LEAVES ? amask : 0u);
+        my_hits += nh;
+      }
     }
   }
   if (stats) {

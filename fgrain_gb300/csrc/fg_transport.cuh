@@ -77,6 +77,72 @@ __device__ __forceinline__ void walk_lbvh(const Node* __restrict__ nodes, float3
   }
 }
 
+// The same walk with the leaf tests deferred to warp-wide rounds: each lane of `amask` visits nodes
+// until it holds a leaf (or its walk ends) and waits while the others find theirs; then the lanes
+// test their leaves together.  The expensive crystal test runs with many lanes active instead of
+// one or two, and the set of leaves tested is the same as walk_lbvh's.
+template <class F>
+__device__ __forceinline__ void walk_lbvh_deferred(const Node* __restrict__ nodes, float3 o, float3 inv,
+                                                   float tlim, uint32_t* err, F&& fn, uint32_t n, unsigned amask) {
+  const int nint = n > 1 ? static_cast<int>(n - 1) : 1;
+  constexpr uint32_t NONE = 0xffffffffu;
+  int stack[64];
+  int sp = 0;
+  int cur = n ? 0 : -1;
+  uint32_t p0 = NONE, p1 = NONE;
+  for (;;) {
+    for (;;) {
+      const bool want = cur >= 0 && p0 == NONE;
+      if (!__any_sync(amask, want)) break;
+      if (!want) continue;
+      if (!index_ok(cur < nint, err, SITE_NODE, static_cast<uint32_t>(cur), n)) {
+        cur = -1;
+        continue;
+      }
+      const float4 na = __ldg(&nodes[cur].a);
+      const float4 nb = __ldg(&nodes[cur].b);
+      const float4 nc = __ldg(&nodes[cur].c);
+      const int4 nd = __ldg(&nodes[cur].d);
+      float te, tx;
+      slab(o, inv, na.x, na.y, na.z, na.w, nb.x, nb.y, te, tx);
+      bool hl = tx >= te && tx >= 0.0f && te <= tlim;
+      slab(o, inv, nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, te, tx);
+      bool hr = tx >= te && tx >= 0.0f && te <= tlim && nd.y != INT32_MIN;
+      if (hl && nd.x < 0) {
+        p0 = static_cast<uint32_t>(~nd.x);
+        hl = false;
+      }
+      if (hr && nd.y < 0) {
+        if (p0 == NONE) p0 = static_cast<uint32_t>(~nd.y); else p1 = static_cast<uint32_t>(~nd.y);
+        hr = false;
+      }
+      if (hl && hr) {
+        if (sp < 64) {
+          stack[sp++] = nd.y;
+        } else {
+          atomicOr(err, ERR_STACK_OVERFLOW);
+        }
+        cur = nd.x;
+      } else if (hl) {
+        cur = nd.x;
+      } else if (hr) {
+        cur = nd.y;
+      } else {
+        cur = sp > 0 ? stack[--sp] : -1;
+      }
+    }
+    if (!__any_sync(amask, p0 != NONE)) break;
+    if (p0 != NONE) {
+      if (index_ok(p0 < n, err, SITE_LEAF, p0, n)) fn(p0);
+      p0 = NONE;
+      if (p1 != NONE) {
+        if (index_ok(p1 < n, err, SITE_LEAF, p1, n)) fn(p1);
+        p1 = NONE;
+      }
+    }
+  }
+}
+
 // Beer-Lambert absorption of one hit and Bernoulli rounding of the latent photons
 // (transport.rs:359-381), in exactly rounded FP64.
 __device__ __forceinline__ double absorb64(double E, double path, double alpha, double sens,
@@ -91,14 +157,17 @@ __device__ __forceinline__ double absorb64(double E, double path, double alpha, 
   return __dmul_rn(E, fmax(__dsub_rn(1.0, __dmul_rn(p, 0.9)), 0.05));
 }
 
-// Adds n latent photons to crystal s, one atomic per distinct crystal among the active lanes.
+// Adds n latent photons to crystal s, one atomic per distinct counter among the active lanes.
+// Lanes are grouped by the counter's address, not by s: the lanes of a warp may trace photons of
+// different tiles, whose crystals share local indices.
 __device__ __forceinline__ void add_counts(uint32_t* counts, uint32_t s, uint32_t n) {
+  uint32_t* const ctr = counts + s;
   const unsigned act = __activemask();
-  const unsigned grp = __match_any_sync(act, s);
+  const unsigned grp = __match_any_sync(act, reinterpret_cast<unsigned long long>(ctr));
   const int leader = __ffs(grp) - 1;
   uint32_t sum = 0;
   for (unsigned m = grp; m; m &= m - 1) sum += __shfl_sync(grp, n, __ffs(m) - 1);
-  if ((threadIdx.x & 31) == leader && sum) atomicAdd(&counts[s], sum);
+  if ((threadIdx.x & 31) == leader && sum) atomicAdd(ctr, sum);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -157,7 +226,7 @@ __device__ __forceinline__ bool hit_before(const TileDesc& t, float ta, uint32_t
 
 // One bounce (transport.rs:101-185).  Returns whether the packet is still alive.
 __device__ __forceinline__ bool photon_bounce(const TileDesc& t, Photon& ph, HitS* hits, uint32_t* err,
-                                              uint32_t& nhit) {
+                                              uint32_t& nhit, unsigned amask = 0) {
   const float PI2 = 6.283185307179586f;
   nhit = 0;
   if (ph.b >= t.max_bounces) return false;
@@ -168,8 +237,7 @@ __device__ __forceinline__ bool photon_bounce(const TileDesc& t, Photon& ph, Hit
   const float3 pos = ph.pos, dir = ph.dir;
   const float3 inv = make_float3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
   int nh = 0;
-  if (t.n > 0) {
-    walk_lbvh(t.nodes, pos, inv, step * 1.00001f + 1e-3f, err, [&](uint32_t s) {
+  auto leaf = [&](uint32_t s) {
       const float4 a = __ldg(&t.a[s]), q = __ldg(&t.q[s]), d = __ldg(&t.d[s]);
       float t0, t1;
       if (!fcanonical_hit(a, q, d, 1.0f, pos, dir, inv, t0, t1)) return;
@@ -182,7 +250,11 @@ __device__ __forceinline__ bool photon_bounce(const TileDesc& t, Photon& ph, Hit
         --j;
       }
       hits[j] = HitS{t0, t1, s};
-    }, t.n);
+  };
+  if (amask) {
+    walk_lbvh_deferred(t.nodes, pos, inv, step * 1.00001f + 1e-3f, err, leaf, t.n, amask);
+  } else if (t.n > 0) {
+    walk_lbvh(t.nodes, pos, inv, step * 1.00001f + 1e-3f, err, leaf, t.n);
   }
   float E = ph.E;
   P4 r{};

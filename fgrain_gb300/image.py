@@ -108,3 +108,57 @@ def resize_triangle(field, ow: int, oh: int) -> np.ndarray:
     out = np.zeros((oh, ow), np.float32)
     _run("fg_resize_triangle", _fptr(f), f.shape[1], f.shape[0], ow, oh, _fptr(out))
     return out
+
+
+# ---- whole images through the batched tile path ----
+
+COLOR_SEED_OFFSETS = (0, 10007, 20011)  # R, G, B layer seeds (image_pipeline.rs:1048-1061, wrapping adds)
+
+
+def image_tile_params(preset: str, grain_px: float, grid: list[Tile], exposure: float = 1.0, push: float = 0.0,
+                      seed: int = 0) -> list:
+    """Tile-worker parameters of every tile of one black-and-white image (pixel = 1 / grain_px um)."""
+    from .api import tile_params
+
+    return [tile_params(preset, 1.0 / grain_px, t.tw, t.th, exposure, push, tile_seed(seed, t)) for t in grid]
+
+
+def render_tiles(params: list, tiles: list, engine=None, batch=None):
+    """Renders exposure tiles (one batch, one graph launch) and returns their densities."""
+    from .api import Batch
+
+    b = batch or Batch(params, engine, use_graph=True, autotune=False)
+    b.set_exposure(tiles)
+    b.run()
+    b.wait()
+    out = b.density()
+    if batch is None:
+        b.close()
+    return out
+
+
+def render_bw_image(exposure, preset: str, grain_px: float, push: float = 0.0, seed: int = 0, engine=None):
+    """render_film_black_and_white_tiled's tile path (image_pipeline.rs:377-649): tiles of the
+    exposure image rendered in one batch and Hann-blended into the image's d_norm."""
+    exposure = np.ascontiguousarray(exposure, np.float32)
+    H, W = exposure.shape
+    grid, step, pad = tile_grid(W, H, grain_px)
+    params = image_tile_params(preset, grain_px, grid, 1.0, push, seed)
+    tiles = [exposure[t.y_start:t.y_start + t.th, t.x_start:t.x_start + t.tw] for t in grid]
+    return blend_tiles(W, H, grid, step, pad, render_tiles(params, tiles, engine))
+
+
+def render_color_image(rgb, preset: str, grain_px: float, push: float = 0.0, seed: int = 0, engine=None):
+    """render_film_color_tiled (image_pipeline.rs:1017-1085): the R, G and B layers are independent
+    black-and-white runs with seeds seed, seed + 10007 and seed + 20011; here all three channels'
+    tiles share one batch.  Returns d_norm per channel, shape (3, H, W)."""
+    rgb = np.ascontiguousarray(rgb, np.float32)
+    H, W = rgb.shape[1:]
+    grid, step, pad = tile_grid(W, H, grain_px)
+    params, tiles = [], []
+    for c, off in enumerate(COLOR_SEED_OFFSETS):
+        params += image_tile_params(preset, grain_px, grid, 1.0, push, (seed + off) & M64)
+        tiles += [np.ascontiguousarray(rgb[c, t.y_start:t.y_start + t.th, t.x_start:t.x_start + t.tw]) for t in grid]
+    d = render_tiles(params, tiles, engine)
+    n = len(grid)
+    return np.stack([blend_tiles(W, H, grid, step, pad, d[c * n:(c + 1) * n]) for c in range(3)])

@@ -145,3 +145,19 @@ def test_statistical_parity_with_oracle_renders(engine):
         diff = fd.mean() - fo.mean()
         sig = np.sqrt(fd.var(ddof=1) / len(fd) + fo.var(ddof=1) / len(fo))
         assert abs(diff) <= 3 * sig, (name, fd.mean(), fo.mean(), sig)
+
+
+def test_identical_tiles_in_one_batch_stay_identical(engine):
+    """Copies of one tile share warps in the transport (the photon queue interleaves tiles at its
+    boundaries) and hit crystals with the same local indices: every copy must still get exactly
+    its own counts, so all copies equal the plain render."""
+    p = fg.tile_params("tri-x", 1 / 2.4, 96, 96, 1.0, 0.0, 77)
+    tile = np.random.default_rng(77).random((96, 96)).astype(np.float32)
+    plain = fg.render_tile(tile, p, engine)
+    b = fg.Batch([p] * 12, engine)
+    b.set_exposure([tile] * 12)
+    b.run()
+    b.wait()
+    for d in b.density():
+        np.testing.assert_array_equal(d, plain)
+    b.close()
