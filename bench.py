@@ -70,6 +70,41 @@ def c2_tiles(exposure, ntiles=None):
     return grid, params, tiles
 
 
+C3_STOCKS = ("tri-x", "t-max", "hp5")
+
+
+def c3_tiles():
+    """Configuration C3: 64 square images, sides exp(U[ln 64, ln 512]) rounded, stock uniform over
+    tri-x / t-max / hp5, push U[0, 3] stops, supersample uniform over 1-4 (master seed 0); image k
+    is blurred uniform noise (seed k, sigma side / 32 px, gamma 2.2) zoomed by its supersample
+    factor.  All tiles of all images form one batch.  Returns (params, tiles, output px, internal
+    px)."""
+    import fgrain_gb300 as fg
+    from scipy.ndimage import gaussian_filter, zoom
+    from fgrain_gb300.image import default_grain_px, effective_push, tile_grid, tile_seed
+
+    rng = np.random.default_rng(0)
+    params, tiles, out_px, int_px = [], [], 0, 0
+    for k in range(64):
+        side = int(round(float(np.exp(rng.uniform(np.log(64.0), np.log(512.0))))))
+        stock = C3_STOCKS[int(rng.integers(0, 3))]
+        push = float(rng.uniform(0.0, 3.0))
+        ss = int(rng.integers(1, 5))
+        a = np.random.default_rng(k).random((side, side))
+        lum = np.clip(gaussian_filter(a, max(side / 32.0, 2.0), mode="reflect"), 0.0, None) ** 2.2
+        exposure = (zoom(lum, ss, order=1, mode="nearest") if ss > 1 else lum).astype(np.float32)
+        grain = default_grain_px(stock, push)
+        H, W = exposure.shape
+        grid, _, _ = tile_grid(W, H, grain)
+        for t in grid:
+            params.append(fg.tile_params(stock, 1.0 / grain, t.tw, t.th, 1.0, effective_push(stock, push),
+                                         tile_seed(k, t)))
+            tiles.append(np.ascontiguousarray(exposure[t.y_start:t.y_start + t.th, t.x_start:t.x_start + t.tw]))
+        out_px += side * side
+        int_px += W * H
+    return params, tiles, out_px, int_px
+
+
 def c2_tiles_grid(exposure):
     from fgrain_gb300.image import tile_grid
 
@@ -203,8 +238,12 @@ def run_ours(args):
     import fgrain_gb300 as fg
 
     rank, world, local, td = dist()
-    exposure = c2_inputs()
-    grid, params, tiles = c2_tiles(exposure, args.tiles)
+    if args.workload == "c3":
+        params, tiles, c3_out_px, c3_int_px = c3_tiles()
+        exposure = None
+    else:
+        exposure = c2_inputs()
+        grid, params, tiles = c2_tiles(exposure, args.tiles)
     engine = fg.GpuEngine(local)
     batch = fg.Batch(params, engine, use_graph=True, autotune=True)
     batch.set_exposure(tiles)
@@ -231,8 +270,11 @@ def run_ours(args):
     ms_max = reduce_max(td, ms)
     per_step = ms_max / args.steps
     full = not args.tiles or args.tiles >= 49
-    out_px = OUT_W * OUT_H if full else int(round(OUT_W * OUT_H * sum(p.width_px * p.height_px for p in params)
-                                                  / sum(t.tw * t.th for t in c2_tiles_grid(exposure))))
+    if args.workload == "c3":
+        out_px = c3_out_px
+    else:
+        out_px = OUT_W * OUT_H if full else int(round(OUT_W * OUT_H * sum(p.width_px * p.height_px for p in params)
+                                                      / sum(t.tw * t.th for t in c2_tiles_grid(exposure))))
     value = world * out_px / (per_step / 1e3) / 1e6
 
     # End to end through the public API: pinned host exposure in, pinned density out, per step.
@@ -281,7 +323,7 @@ def run_ours(args):
     photons_per_s = P / (stats["transport_ms"] / 1e3)
 
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
+    if rank == 0 and world == 1 and not args.no_cpu and args.workload == "c2":
         threads = os.cpu_count() or 1
         secs, px = oracle_sample(params, tiles, max(threads, 4), threads)
         total_px = sum(p.width_px * p.height_px for p in params)
@@ -295,10 +337,14 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": "Mpx/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": ("" if full else f"first {len(params)} tiles of ") +
-                                   "C2: 1024x1024 blurred-noise luminance (sigma 16, seed 1, gamma 2.2), tri-x, "
-                                   "grain 2.4 px, push 0, supersample 2 (2048^2 internal, 49 tiles), batched "
-                                   "graph path", "tiles": len(params), "internal_px": int(exposure.size),
+            "config": {"workload": (("" if full else f"first {len(params)} tiles of ") +
+                                    "C2: 1024x1024 blurred-noise luminance (sigma 16, seed 1, gamma 2.2), tri-x, "
+                                    "grain 2.4 px, push 0, supersample 2 (2048^2 internal, 49 tiles), batched "
+                                    "graph path") if args.workload == "c2" else
+                                   "C3: 64 square images, sides log-uniform 64-512 px, tri-x / t-max / hp5, push "
+                                   "0-3, supersample 1-4 (master seed 0), all tiles in one autotuned batch",
+                       "tiles": len(params),
+                       "internal_px": int(exposure.size) if exposure is not None else int(c3_int_px),
                        "output_px": out_px, "l2": "working set (crystals, LBVH, grids) exceeds L2; no flush",
                        "parallelism": f"replicas x{world}"},
             "photons_per_s": photons_per_s,
@@ -367,6 +413,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--tiles", type=int, default=0, help="render only the first N tiles of C2 (profiling)")
+    ap.add_argument("--workload", choices=["c2", "c3"], default="c2",
+                    help="c2: the headline configuration; c3: the mixed batch (reported, not the headline)")
     ap.add_argument("--profile-region", action="store_true",
                     help="bracket the timed replays with cudaProfilerStart/Stop")
     args = ap.parse_args()

@@ -235,13 +235,24 @@ __global__ void k_maxdim_b(BTile* bt, int ntiles, unsigned long long ncap, const
 }
 
 __global__ void k_threshold_b(const BTile* __restrict__ bt, int ntiles, unsigned long long ncap,
-                              const uint32_t* counts, uint8_t* developed, int* parent) {
+                              const uint32_t* counts, uint8_t* developed, int* parent, uint32_t* devflag) {
   const unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
   if (g >= ncap) return;
   const BTile& t = bt[btile_of(bt, ntiles, g)];
   const bool in = g - t.cbase < t.n;
-  developed[g] = (in && counts[g] >= t.thr) ? 1 : 0;
+  const bool dv = in && counts[g] >= t.thr;
+  developed[g] = dv ? 1 : 0;
+  devflag[g] = dv ? 1u : 0u;
   parent[g] = static_cast<int>(g);
+}
+
+// Developed slots in slot order (from the exclusive scan of the flags), so that the touch queries
+// run in full, spatially coherent warps.
+__global__ void k_devlist_b(unsigned long long ncap, const uint32_t* __restrict__ devflag,
+                            const uint32_t* __restrict__ devscan, uint32_t* __restrict__ list) {
+  const unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+  if (g >= ncap || !devflag[g]) return;
+  list[devscan[g]] = static_cast<uint32_t>(g);
 }
 
 __device__ __forceinline__ int uf_find_b(int* parent, int x, uint32_t* err) {
@@ -271,9 +282,11 @@ __device__ __forceinline__ void uf_unite_b(int* parent, int a, int b, uint32_t* 
 
 __global__ void k_link_b(const BTile* __restrict__ bt, int ntiles, unsigned long long ncap,
                          const float4* __restrict__ A, const float4* __restrict__ D, const Node* __restrict__ nodes_all,
-                         const uint8_t* __restrict__ developed, int* parent, uint32_t* err) {
-  const unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
-  if (g >= ncap || !developed[g]) return;
+                         const uint8_t* __restrict__ developed, int* parent, const uint32_t* __restrict__ list,
+                         const uint32_t* __restrict__ ndev, uint32_t* err) {
+  const unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+  if (i >= ncap || i >= *ndev) return;
+  const unsigned long long g = list[i];
   const BTile& t = bt[btile_of(bt, ntiles, g)];
   const uint32_t s = static_cast<uint32_t>(g - t.cbase);
   const Node* nodes = nodes_all + t.cbase;
@@ -425,6 +438,7 @@ struct fg_batch {
   DBuf<uint8_t> developed;
   DBuf<double> exp64;
   DBuf<ScanPrep> prep;  // staging terms of developed crystals for the scan
+  DBuf<uint32_t> devflag, devscan, devlist;  // developed slots, compacted for the touch queries
   DBuf<uint32_t> bin_cnt, bin_off, bin_cur, bin_items;
   DBuf<uint32_t> pcnt, poff, pcur, porder;  // photon ordering by emission cell
   unsigned long long npcells = 0;
@@ -535,6 +549,7 @@ static void derive_tile(const fg_tile_params& p, SynthTile& s, TileDesc& t, Scan
   c.seed = ss;
   c.sigma = static_cast<float>(p.silver_opacity);
   c.mode = 0;
+  set_jitter_units(c);
   b = BTile{};
   b.fe = p.filament_expansion;
   b.prox = p.clumping_proximity_factor;
@@ -664,9 +679,12 @@ static void stage_develop(fg_batch* B, cudaStream_t st) {
   fg_engine* e = B->e;
   const unsigned G = grid_for(B->ncap, 256);
   k_maxdim_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->D.p);
-  k_threshold_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->counts.p, B->developed.p, B->parent.p);
+  k_threshold_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->counts.p, B->developed.p, B->parent.p, B->devflag.p);
+  FG_CUDA(cudaMemsetAsync(B->devflag.p + B->ncap, 0, sizeof(uint32_t), st));
+  cub_scan(B, B->devflag.p, B->devscan.p, B->ncap + 1, st);
+  k_devlist_b<<<G, 256, 0, st>>>(B->ncap, B->devflag.p, B->devscan.p, B->devlist.p);
   k_link_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->A.p, B->D.p, B->nodes.p, B->developed.p, B->parent.p,
-                              e->d_err);
+                              B->devlist.p, B->devscan.p + B->ncap, e->d_err);
   FG_CUDA(cudaMemsetAsync(B->size.p, 0, B->ncap * sizeof(uint32_t), st));
   k_roots_b<<<G, 256, 0, st>>>(B->ncap, B->developed.p, B->parent.p, B->size.p, e->d_err);
   k_finalize_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->developed.p, B->parent.p, B->size.p, B->exp64.p);
@@ -850,6 +868,9 @@ static void plan(fg_batch* B, const fg_batch_options* opt) {
   B->developed.alloc(std::max<unsigned long long>(cap, 1), st);
   B->exp64.alloc(std::max<unsigned long long>(cap, 1), st);
   B->prep.alloc(std::max<unsigned long long>(cap, 1), st);
+  B->devflag.alloc(cap + 1, st);
+  B->devscan.alloc(cap + 1, st);
+  B->devlist.alloc(std::max<unsigned long long>(cap, 1), st);
   B->bin_cnt.alloc(nbins_max + 1, st);
   B->bin_off.alloc(nbins_max + 1, st);
   B->bin_cur.alloc(nbins_max + 1, st);
@@ -870,7 +891,9 @@ static void plan(fg_batch* B, const fg_batch_options* opt) {
   FG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, b2, B->bin_cnt.p, B->bin_off.p, static_cast<int64_t>(nbins_max + 1), st));
   size_t b3 = 0;
   FG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, b3, B->pcnt.p, B->poff.p, static_cast<int64_t>(B->npcells + 1), st));
-  B->cub_bytes = std::max(std::max(b1, b2), b3);
+  size_t b4 = 0;
+  FG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, b4, B->devflag.p, B->devscan.p, static_cast<int64_t>(cap + 1), st));
+  B->cub_bytes = std::max(std::max(b1, b2), std::max(b3, b4));
   B->cub_tmp.alloc(std::max<size_t>(B->cub_bytes, 1), st);
   for (auto& x : B->ev) FG_CUDA(cudaEventCreate(&x));
   layout_bins(B, bin0);
@@ -1132,9 +1155,9 @@ fg_status fg_batch_wait(fg_batch* b, fg_batch_stats* stats) {
     s.scan_bin_px = b->bin_px;
     s.graph = b->exec ? 1u : 0u;
     // Own kernels per run: Bridson x4, count + thin + flags, emit, set_n, Karras + fit, photon order x2, transport,
-    // maxdim + threshold + link + roots + finalize, scan prep, two bin passes, scan (CUB scans not
-    // counted).
-    s.kernel_launches = 4 + 3 + 1 + 1 + 2 + 2 + 1 + 5 + 1 + 2 + 1;
+    // maxdim + threshold + developed list + link + roots + finalize, scan prep, two bin passes, scan
+    // (CUB scans not counted).
+    s.kernel_launches = 4 + 3 + 1 + 1 + 2 + 2 + 1 + 6 + 1 + 2 + 1;
     b->stats = s;
     if (stats) *stats = s;
   });

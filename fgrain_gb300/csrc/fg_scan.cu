@@ -331,10 +331,7 @@ __device__ __forceinline__ ScanRay scan_ray(const ScanTile& t, uint32_t bin, uin
     const uint64_t ps = t.seed + static_cast<uint64_t>(px) * 0x9E3779B97F4A7C15ull +
                         static_cast<uint64_t>(py) * 0xC6A4A7935BD1E995ull;
     const P4 r = philox(sy * t.g + sx, 0, 0, TAG_SCAN, static_cast<uint32_t>(ps), static_cast<uint32_t>(ps >> 32));
-    const double scale = 1.0 / (static_cast<double>(t.g) * 16777216.0);
-    float cxh, cxl, cyh, cyl;
-    split64(t.pw * scale, cxh, cxl);
-    split64(t.ph * scale, cyh, cyl);
+    const float cxh = t.jxh, cxl = t.jxl, cyh = t.jyh, cyl = t.jyl;
     const uint32_t X = ((rlx * t.g + sx) << 24) + (r.x >> 8);
     const uint32_t Y = ((rly * t.g + sy) << 24) + (r.y >> 8);
     const float Xh = static_cast<float>(X), Yh = static_cast<float>(Y);
@@ -568,6 +565,7 @@ static void plan_scan(fg_engine* e, const fg_emulsion* em, const fg_scan_cfg& cf
   t.n = em->n;
   t.sigma = static_cast<float>(cfg.silver_opacity);
   t.mode = cfg.mode;
+  set_jitter_units(t);
   const size_t nbins = static_cast<size_t>(t.nbx) * t.nby;
   FG_REQUIRE(nbins < 0x80000000ull, "scan too large");
   P.nbins = static_cast<unsigned>(nbins);

@@ -51,6 +51,7 @@ struct ScanTile {
   float* d_neg;
   uint16_t* ray_hits;
   double pw, ph, z0;
+  float jxh, jxl, jyh, jyl;  // pw / (g 2^24), ph / (g 2^24) as float pairs: one unit of the jitter
   uint64_t seed;
   unsigned long long bin_base;  // first global bin of this tile
   uint32_t w, h, g, spp, bin_px, nbx, nby, n;
@@ -58,6 +59,16 @@ struct ScanTile {
   int mode;
   uint32_t items_cap;  // entries of bin_items; lists past it were dropped (overflow flagged)
 };
+
+// Sets the jitter units of a tile whose pw, ph and g are set (host side, once per tile).
+inline void set_jitter_units(ScanTile& t) {
+  const double scale = 1.0 / (static_cast<double>(t.g) * 16777216.0);
+  const double ux = t.pw * scale, uy = t.ph * scale;
+  t.jxh = static_cast<float>(ux);
+  t.jxl = static_cast<float>(ux - static_cast<double>(t.jxh));
+  t.jyh = static_cast<float>(uy);
+  t.jyl = static_cast<float>(uy - static_cast<double>(t.jyh));
+}
 
 // Stratum ray origin in FP64 exactly as the reference forms it (transmittance.rs:102-120).
 __device__ __forceinline__ void scan_origin64(const ScanTile& t, uint32_t px, uint32_t py,

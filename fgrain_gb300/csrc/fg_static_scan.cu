@@ -173,6 +173,7 @@ void static_scan(const fg_device_crystals* c, const fg_emulsion_cfg* film, const
   t.sigma = static_cast<float>(cfg->silver_opacity);
   t.mode = cfg->mode;
   t.items_cap = FG_STATIC_SCAN_MAX_ITEMS;
+  set_jitter_units(t);
   const unsigned long long nbins = static_cast<unsigned long long>(t.nbx) * t.nby;
   if (nbins > FG_STATIC_SCAN_MAX_BINS)
     throw Error{FG_ERR_INVALID_ARG, "scan of " + std::to_string(t.w) + "x" + std::to_string(t.h) + " px needs " +

@@ -179,7 +179,7 @@ struct Photon {
   uint32_t id, b;
 };
 
-constexpr float PHOTON_CELL_UM = 4.0f;  // coarse emission cells used to order photons
+constexpr float PHOTON_CELL_UM = 1.0f;  // emission cells used to order photons
 
 // Emission of photon `id` (transport.rs:72-97 with the tile worker's exposure closure).  Returns
 // false when the packet never enters the gelatin (zero exposure, Fresnel reflection).
