@@ -23,6 +23,75 @@ __device__ __forceinline__ int find_tile_ull(const SynthTile* tiles, int ntiles,
   return lo;
 }
 
+// True when the cell word w holds a point closer than r to the candidate at (lx, ly, lz) (fixed
+// point, relative to the candidate's cell) from the cell at offset (dx, dy, dz).
+__device__ __forceinline__ bool syn_conflict(uint32_t w, int dx, int dy, int dz, int lx, int ly, int lz) {
+  if (!(w & OCC)) return false;
+  const int ex = dx * SYN_Q + static_cast<int>(w & 1023u) - lx;
+  const int ey = dy * SYN_Q + static_cast<int>((w >> 10) & 1023u) - ly;
+  const int ez = dz * SYN_Q + static_cast<int>((w >> 20) & 1023u) - lz;
+  return ex * ex + ey * ey + ez * ez < SYN_R2X;
+}
+
+// First half of the candidate test, one lane per candidate: the 27 cells of the inner 3x3x3 block
+// (the candidate's own cell first).  They reject about 87 % of Bridson candidates, so the lanes
+// that survive are few and the rest of the test runs warp-cooperatively (syn_outer_free).
+__device__ __forceinline__ bool syn_near_free(const uint32_t* grid, int rb, int lx, int ly, int lz) {
+  if (syn_conflict(grid[rb], 0, 0, 0, lx, ly, lz)) return false;
+#pragma unroll
+  for (int k = 0; k < 27; ++k) {
+    if (k == 13) continue;
+    const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
+    if (syn_conflict(grid[rb + (dz * SYN_R + dy) * SYN_R + dx], dx, dy, dz, lx, ly, lz)) return false;
+  }
+  return true;
+}
+
+// The 90 cells of the 5x5x5 neighbourhood outside the inner block (without its eight corners,
+// which cannot hold a point within r = sqrt(3) cells), as packed entries: region-index offset in
+// the low 16 bits (signed), dx + 2, dy + 2, dz + 2 in three bits each from bit 16.
+constexpr int SYN_OUTER = 90;
+
+__device__ void syn_outer_table(int* tbl) {
+  int j = 0;
+  for (int dz = -2; dz <= 2; ++dz)
+    for (int dy = -2; dy <= 2; ++dy)
+      for (int dx = -2; dx <= 2; ++dx) {
+        const int ax = dx < 0 ? -dx : dx, ay = dy < 0 ? -dy : dy, az = dz < 0 ? -dz : dz;
+        if (ax < 2 && ay < 2 && az < 2) continue;
+        if (ax == 2 && ay == 2 && az == 2) continue;
+        tbl[j++] = (((dz * SYN_R + dy) * SYN_R + dx) & 0xffff) | ((dx + 2) << 16) | ((dy + 2) << 19) | ((dz + 2) << 22);
+      }
+}
+
+// Second half of the test for the lanes whose candidates passed syn_near_free: the warp takes the
+// survivors one at a time and splits the 90 outer cells over its lanes.  Returns the lane's
+// updated verdict.  All 32 lanes must call it.
+__device__ __forceinline__ bool syn_outer_free(const uint32_t* grid, const int* tbl, bool valid, int rb, int lx,
+                                               int ly, int lz, int lane) {
+  unsigned sm = __ballot_sync(0xffffffffu, valid);
+  while (sm) {
+    const int c = __ffs(sm) - 1;
+    sm &= sm - 1;
+    const int cb = __shfl_sync(0xffffffffu, rb, c);
+    const int cx = __shfl_sync(0xffffffffu, lx, c);
+    const int cy = __shfl_sync(0xffffffffu, ly, c);
+    const int cz = __shfl_sync(0xffffffffu, lz, c);
+    bool hit = false;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int j = lane + 32 * k;
+      if (j < SYN_OUTER) {
+        const int e = tbl[j];
+        hit |= syn_conflict(grid[cb + static_cast<int16_t>(e & 0xffff)], ((e >> 16) & 7) - 2, ((e >> 19) & 7) - 2,
+                            ((e >> 22) & 7) - 2, cx, cy, cz);
+      }
+    }
+    if (__any_sync(0xffffffffu, hit) && lane == c) valid = false;
+  }
+  return valid;
+}
+
 // Exact test of a fixed-point candidate against the staged grid: every point within r.  The eight
 // corner cells of the 5x5x5 neighbourhood cannot hold a point within r = sqrt(3) cells.  The
 // outer loop stays rolled (small code), the first point within r ends the test.
@@ -74,6 +143,7 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* 
   __shared__ unsigned s_vmask[SYN_WARPS];
   __shared__ int s_cx[SYN_WARPS][32], s_cy[SYN_WARPS][32], s_cz[SYN_WARPS][32];  // valid candidates
   __shared__ int s_wx[SYN_WARPS], s_wy[SYN_WARPS], s_wz[SYN_WARPS];             // accepted this round
+  __shared__ int s_outer[SYN_OUTER];
 
   // Column of this CTA: tile, then the j-th column of this colour class in that tile.
   int lo = 0, hi = ntiles - 1;
@@ -104,7 +174,10 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* 
       w = tc[(static_cast<size_t>(gz) * t.gh + gy) * t.gw + gx];
     grid[i] = w;
   }
-  if (tid == 0) s_nact = 0;
+  if (tid == 0) {
+    s_nact = 0;
+    syn_outer_table(s_outer);
+  }
   __syncthreads();
   // Active list: the column's points in cell order (deterministic block-wide compaction).
   const int bw = x1 - x0, bh = y1 - y0;
@@ -170,7 +243,7 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* 
     const int BY = (pry + oy) * SYN_Q + static_cast<int>((pw >> 10) & 1023u);
     const int BZ = (prz - 2) * SYN_Q + static_cast<int>((pw >> 20) & 1023u);
     bool valid = false;
-    int X = 0, Y = 0, Z = 0;
+    int X = 0, Y = 0, Z = 0, rb = 0;
     if (lane < SYN_K) {
       const P4 r = philox(static_cast<uint32_t>(iter), static_cast<uint32_t>(warp * 32 + lane), colkey, TAG_CAND,
                           t.k0, t.k1);
@@ -189,11 +262,19 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* 
         Z = static_cast<int>(floorf(fz * SYN_Q));
         if (X < static_cast<int>(t.XW) && Y < static_cast<int>(t.YW) && Z < static_cast<int>(t.ZW)) {
           const int cx = X >> 10, cy = Y >> 10, cz = Z >> 10;
-          if (cx >= x0 - SYN_SPILL && cx < x1 + SYN_SPILL && cy >= y0 - SYN_SPILL && cy < y1 + SYN_SPILL)
-            valid = syn_free(grid, nz, cx - ox, cy - oy, cz + 2, X, Y, Z, cx, cy, cz, err);
+          const int rx = cx - ox, ry = cy - oy, rz = cz + 2;
+          // The neighbourhood must lie inside the staged region (it does for candidates within 2r
+          // of a point of the column); a candidate that fails the check is rejected.
+          if (cx >= x0 - SYN_SPILL && cx < x1 + SYN_SPILL && cy >= y0 - SYN_SPILL && cy < y1 + SYN_SPILL &&
+              index_ok(rx >= 2 && rx <= SYN_R - 3 && ry >= 2 && ry <= SYN_R - 3 && rz >= 2 && rz <= nz - 3, err,
+                       SITE_SYN_REGION, static_cast<uint32_t>(rx | (ry << 8) | (rz << 16)), blockIdx.x)) {
+            rb = (rz * SYN_R + ry) * SYN_R + rx;
+            valid = syn_near_free(grid, rb, X & 1023, Y & 1023, Z & 1023);
+          }
         }
       }
     }
+    valid = syn_outer_free(grid, s_outer, valid, rb, X & 1023, Y & 1023, Z & 1023, lane);
     const unsigned vm = __ballot_sync(0xffffffffu, valid);
     if (valid) {
       s_cx[warp][lane] = X;
