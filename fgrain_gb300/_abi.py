@@ -129,6 +129,25 @@ class fg_device_crystals(C.Structure):
                 ("expansion", C.c_void_p), ("n", C.c_uint64)]
 
 
+class fg_film_options(C.Structure):
+    _fields_ = [("preset", C.c_char_p), ("grain_size_px", C.c_double), ("grain_strength", C.c_double),
+                ("exposure", C.c_double), ("color", C.c_int32), ("out_w", C.c_uint32), ("out_h", C.c_uint32),
+                ("tile_size", C.c_uint32), ("seed", C.c_uint64), ("auto_scale", C.c_int32),
+                ("reference_res", C.c_uint32), ("scale", C.c_double), ("supersample", C.c_uint32),
+                ("scanner_otf", C.c_int32), ("push", C.c_double), ("eberhard", C.c_double)]
+
+
+class fg_film_report(C.Structure):
+    _fields_ = [("in_w", C.c_uint32), ("in_h", C.c_uint32), ("out_w", C.c_uint32), ("out_h", C.c_uint32),
+                ("total_tiles", C.c_uint64), ("total_crystals", C.c_uint64), ("photons", C.c_uint64),
+                ("elapsed_seconds", C.c_double)]
+
+
+class fg_finish_cfg(C.Structure):
+    _fields_ = [("preset", C.c_char_p), ("grain_size_px", C.c_double), ("grain_strength", C.c_double),
+                ("push", C.c_double), ("scanner_otf", C.c_int32), ("_pad", C.c_int32)]
+
+
 _vp = C.c_void_p
 _st = C.c_int
 _u32p = C.POINTER(C.c_uint32)
@@ -171,6 +190,15 @@ PROTOTYPES = {
                              C.POINTER(_fp), _fp]),
     "fg_scanner_otf": (_st, [_vp, _fp, C.c_uint32, C.c_uint32, _fp, _fp]),
     "fg_resize_triangle": (_st, [_vp, _fp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _fp]),
+    "fg_film_options_default": (None, [C.POINTER(fg_film_options)]),
+    "fg_film_output_size": (_st, [C.POINTER(fg_film_options), C.c_uint32, C.c_uint32, _u32p, _u32p]),
+    "fg_render_film": (_st, [_vp, _u8p, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(fg_film_options), _u8p,
+                             C.POINTER(fg_film_report)]),
+    "fg_panchromatic_luma": (_st, [_vp, _u8p, C.c_uint32, C.c_uint32, C.c_char_p, _u8p]),
+    "fg_resize_u8": (_st, [_vp, _u8p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int32, _u8p]),
+    "fg_gelatin_psf": (_st, [_vp, _u8p, C.c_uint32, C.c_uint32, _fp, _u32p]),
+    "fg_film_finish": (_st, [_vp, C.POINTER(fg_finish_cfg), C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                             C.c_uint32, _u32p, C.POINTER(_fp), _u8p, _fp, _u8p, _fp, _fp]),
     "fg_scan_signal": (_st, [_vp, _vp, C.POINTER(fg_scan_cfg), C.c_uint64, _fp, C.c_double, C.c_double, _fp, _fp]),
     "fg_scan_backward": (_st, [_vp, _vp, C.POINTER(fg_scan_cfg), C.c_uint64, _fp, C.c_double, C.c_double, _fp, _fp,
                                _dp, _dp]),

@@ -8,7 +8,7 @@
 #include <cmath>
 #include <vector>
 
-#include "fg_internal.h"
+#include "fg_image.cuh"
 
 namespace fg {
 
@@ -16,25 +16,6 @@ namespace {
 
 __device__ __forceinline__ uint32_t clamp_lo(uint32_t v) { return v > 0 ? v - 1 : 0; }
 __device__ __forceinline__ uint32_t clamp_hi(uint32_t v, uint32_t n) { return v + 1 < n ? v + 1 : n - 1; }
-
-// Hann weight of global coordinate g in tile t of nt along one axis (image_pipeline.rs:613-638).
-__device__ __forceinline__ float hann_weight(uint32_t t, uint32_t g, uint32_t nt, uint32_t o0, uint32_t step,
-                                            uint32_t pad) {
-  const float pad2 = static_cast<float>(2 * pad);
-  const float pi = 3.14159265358979323846f;
-  if (t > 0 && g < o0 + pad) {
-    const float u = __fdiv_rn(__fsub_rn(static_cast<float>(g), __fsub_rn(static_cast<float>(o0), static_cast<float>(pad))), pad2);
-    const float c = static_cast<float>(cos(static_cast<double>(__fmul_rn(pi, fminf(fmaxf(u, 0.0f), 1.0f)))));
-    return __fsub_rn(0.5f, __fmul_rn(0.5f, c));
-  }
-  if (t + 1 < nt && g >= o0 + step - pad) {
-    const float u = __fdiv_rn(__fsub_rn(static_cast<float>(g), __fsub_rn(static_cast<float>(o0 + step), static_cast<float>(pad))),
-                              pad2);
-    const float c = static_cast<float>(cos(static_cast<double>(__fmul_rn(pi, fminf(fmaxf(u, 0.0f), 1.0f)))));
-    return __fadd_rn(0.5f, __fmul_rn(0.5f, c));
-  }
-  return 1.0f;
-}
 
 struct BlendTile {
   uint32_t tx, ty, xs, ys, tw, th;
@@ -91,17 +72,28 @@ __global__ void k_tent_pass(const float* __restrict__ in, uint32_t w, uint32_t h
   out[i] = s;
 }
 
-// Tent-filter weights for resampling n samples to m (the image crate's Triangle filter: support
-// 1 scaled by the ratio when shrinking, weights normalised to sum 1).
-void tent_weights(uint32_t n, uint32_t m, std::vector<uint32_t>& left, std::vector<uint32_t>& cnt,
-                  std::vector<float>& wts, uint32_t& stride) {
+}  // namespace
+
+void resample_weights(uint32_t n, uint32_t m, int filter, std::vector<uint32_t>& left, std::vector<uint32_t>& cnt,
+                      std::vector<float>& wts, uint32_t& stride) {
   const float ratio = static_cast<float>(n) / static_cast<float>(m);
   const float sratio = ratio < 1.0f ? 1.0f : ratio;
-  const float support = sratio;
+  const float support = (filter == RESAMPLE_TRIANGLE ? 1.0f : 3.0f) * sratio;
   stride = static_cast<uint32_t>(std::ceil(support * 2.0f)) + 2;
   left.assign(m, 0);
   cnt.assign(m, 0);
   wts.assign(static_cast<size_t>(m) * stride, 0.0f);
+  auto kernel = [filter](float x) {
+    if (filter == RESAMPLE_TRIANGLE) {
+      const float a = std::fabs(x);
+      return a < 1.0f ? 1.0f - a : 0.0f;
+    }
+    auto sinc = [](float t) {
+      const float a = t * 3.14159265358979323846f;
+      return t == 0.0f ? 1.0f : std::sin(a) / a;
+    };
+    return std::fabs(x) < 3.0f ? sinc(x) * sinc(x / 3.0f) : 0.0f;
+  };
   for (uint32_t o = 0; o < m; ++o) {
     float c = (static_cast<float>(o) + 0.5f) * ratio;
     const int64_t l = std::clamp<int64_t>(static_cast<int64_t>(std::floor(c - support)), 0, static_cast<int64_t>(n) - 1);
@@ -110,9 +102,7 @@ void tent_weights(uint32_t n, uint32_t m, std::vector<uint32_t>& left, std::vect
     const uint32_t k = static_cast<uint32_t>(std::min<int64_t>(r - l, stride));
     float sum = 0.0f;
     for (uint32_t q = 0; q < k; ++q) {
-      const float x = (static_cast<float>(l + q) - c) / sratio;
-      const float ax = std::fabs(x);
-      const float wv = ax < 1.0f ? 1.0f - ax : 0.0f;
+      const float wv = kernel((static_cast<float>(l + q) - c) / sratio);
       wts[static_cast<size_t>(o) * stride + q] = wv;
       sum += wv;
     }
@@ -121,8 +111,6 @@ void tent_weights(uint32_t n, uint32_t m, std::vector<uint32_t>& left, std::vect
     cnt[o] = k;
   }
 }
-
-}  // namespace
 
 // Separable 3-tap clamp-to-edge pass in the reference's operation order (a k0 + b k1 + c k2),
 // optionally scaled: the scanner OTF (two passes) and the differentiable scan's forward.
@@ -181,8 +169,8 @@ fg_status fg_resize_triangle(fg_engine* e, const float* in, uint32_t w, uint32_t
     std::vector<uint32_t> ly, cy, lx, cx;
     std::vector<float> wy, wx;
     uint32_t sy = 0, sx = 0;
-    tent_weights(h, oh, ly, cy, wy, sy);
-    tent_weights(w, ow, lx, cx, wx, sx);
+    resample_weights(h, oh, RESAMPLE_TRIANGLE, ly, cy, wy, sy);
+    resample_weights(w, ow, RESAMPLE_TRIANGLE, lx, cx, wx, sx);
     DBuf<float> a(static_cast<size_t>(w) * h, st), t(static_cast<size_t>(w) * oh, st), o(static_cast<size_t>(ow) * oh, st);
     DBuf<uint32_t> dly(oh, st), dcy(oh, st), dlx(ow, st), dcx(ow, st);
     DBuf<float> dwy(wy.size(), st), dwx(wx.size(), st);

@@ -233,6 +233,75 @@ fg_status fg_scanner_otf(fg_engine* e, const float* in, uint32_t w, uint32_t h, 
 fg_status fg_resize_triangle(fg_engine* e, const float* in, uint32_t w, uint32_t h, uint32_t ow, uint32_t oh,
                              float* out);
 
+/* ---- whole photographs: the film renderer around the tile path ---- */
+/* FilmRenderOptions (src/image_pipeline.rs:18-101).  out_w = out_h = 0 keeps the input size; one
+ * of them 0 keeps the aspect ratio (output_resolution, src/image_pipeline.rs:306-313).  eberhard
+ * has no effect (the reference's halo term is zero, src/image_pipeline.rs:789). */
+typedef struct fg_film_options {
+  const char* preset;      /* "tri-x", "t-max", "hp5", "tri-x-1600", "caffenol", ... */
+  double grain_size_px;    /* 2.2 */
+  double grain_strength;   /* 1.0 */
+  double exposure;         /* 1.0 */
+  int32_t color;           /* 0: black and white; 1: three dye layers (needs 3 channels) */
+  uint32_t out_w, out_h;   /* 0, 0 */
+  uint32_t tile_size;      /* 320 */
+  uint64_t seed;           /* 42 */
+  int32_t auto_scale;      /* 0 */
+  uint32_t reference_res;  /* 6000 */
+  double scale;            /* 1.0 */
+  uint32_t supersample;    /* 1 (1 to 4) */
+  int32_t scanner_otf;     /* 1 */
+  double push;             /* 0 */
+  double eberhard;         /* 1.0 */
+} fg_film_options;
+
+typedef struct fg_film_report {  /* ImageProcessReport (src/image_pipeline.rs:103-113) */
+  uint32_t in_w, in_h, out_w, out_h;
+  uint64_t total_tiles, total_crystals, photons;
+  double elapsed_seconds;
+} fg_film_report;
+
+/* The reference's defaults (FilmRenderOptions::default, src/image_pipeline.rs:82-101). */
+void fg_film_options_default(fg_film_options* o);
+fg_status fg_film_output_size(const fg_film_options* o, uint32_t in_w, uint32_t in_h, uint32_t* out_w,
+                              uint32_t* out_h);
+/* render_film_black_and_white_tiled / render_film_color_tiled (src/image_pipeline.rs:299-891,
+ * 1017-1085) with every stage on the device: pixels is a u8 image of `channels` (1 gray, 3 RGB
+ * interleaved) channels, out receives out_w x out_h x (color ? 3 : 1) bytes.  A gray render of an
+ * RGB image takes the stock's panchromatic luma first.  All tiles of all layers run as one batch. */
+fg_status fg_render_film(fg_engine* e, const uint8_t* pixels, uint32_t w, uint32_t h, uint32_t channels,
+                         const fg_film_options* options, uint8_t* out, fg_film_report* report);
+
+/* Stages of the renderer, for parity checks and for callers that compose their own pipeline. */
+/* convert_to_panchromatic_luma (src/image_pipeline.rs:259-296) of an RGB8 image. */
+fg_status fg_panchromatic_luma(fg_engine* e, const uint8_t* rgb, uint32_t w, uint32_t h, const char* preset,
+                               uint8_t* out);
+/* image::imageops::resize of a u8 image (src/image_pipeline.rs:324-328, 333-342): the image
+ * crate's separable filter, vertical pass to f32 then horizontal pass, clamped and rounded. */
+#define FG_FILTER_TRIANGLE 0
+#define FG_FILTER_LANCZOS3 1
+fg_status fg_resize_u8(fg_engine* e, const uint8_t* in, uint32_t w, uint32_t h, uint32_t ow, uint32_t oh,
+                       int32_t filter, uint8_t* out);
+/* apply_camera_and_gelatin_optics (src/image_pipeline.rs:133-252): h_effective of a u8 image
+ * (zero outside the camera gate); gate (may be NULL) receives top, bottom, left, right. */
+fg_status fg_gelatin_psf(fg_engine* e, const uint8_t* src, uint32_t w, uint32_t h, float* h_eff, uint32_t* gate);
+/* Everything after the tiles (src/image_pipeline.rs:593-891): Hann blend with the weight sums,
+ * low-frequency split, grain statistics, sensitometric composite, scanner OTF and output gates.
+ * desc and tiles as in fg_blend_tiles; src is the u8 image at the render size, h_eff its PSF.
+ * fields (may be NULL) receives 5 planes of out_w x out_h floats: d_norm, d_low, grain, tone,
+ * scanned grain; stats (may be NULL) receives 4 floats: high_mean, high_std, norm_factor, 0. */
+typedef struct fg_finish_cfg {
+  const char* preset;      /* picks the grain amplitude (src/image_pipeline.rs:718-723) */
+  double grain_size_px;    /* after scaling (src/image_pipeline.rs:365) */
+  double grain_strength;   /* effective strength (src/image_pipeline.rs:366) */
+  double push;             /* effective push (src/image_pipeline.rs:369-375) */
+  int32_t scanner_otf;
+  int32_t _pad;
+} fg_finish_cfg;
+fg_status fg_film_finish(fg_engine* e, const fg_finish_cfg* cfg, uint32_t out_w, uint32_t out_h, uint32_t tile_step,
+                         uint32_t pad, uint32_t ntiles, const uint32_t* desc, const float* const* tiles,
+                         const uint8_t* src, const float* h_eff, uint8_t* out, float* fields, float* stats);
+
 /* Replays recorded segments with the exact hit rule and FP64 per-hit arithmetic.  Latent counts
  * are added to the emulsion.  Hit lists are returned CSR style: offsets[nseg+1], ids (crystal
  * indices in canonical order); *nhits receives the total even when it exceeds id_cap. */

@@ -221,6 +221,35 @@ int or_blend_tiles(uint32_t out_w, uint32_t out_h, uint32_t tile_step, uint32_t 
                    uint32_t ntiles, const uint32_t* desc /* ntiles x (tx,ty,x0,y0,tw,th) */,
                    const float* const* tiles, float* d_norm);
 
+/* ---- image stages either side of the tile path (fg_oracle_film.cpp) ---- */
+/* Panchromatic weights of a stock (image_pipeline.rs:265-284) and the luma of an RGB8 image
+ * (image_pipeline.rs:286-294: round(clamp(r wr + g wg + b wb, 0, 255))). */
+int or_luma_weights(const char* preset, float out[3]);
+int or_luma(const uint8_t* rgb, uint32_t w, uint32_t h, const float wts[3], uint8_t* out);
+/* The image crate's resize of a u8 image (filter 0 Triangle, 1 Lanczos3): vertical pass to f32,
+ * horizontal pass, clamp and round to u8; a copy when the size is unchanged. */
+int or_resize_u8(const uint8_t* in, uint32_t w, uint32_t h, uint32_t ow, uint32_t oh, int filter,
+                 uint8_t* out);
+/* Camera gate and gelatin PSF (image_pipeline.rs:133-252): h_effective, zero outside the gate;
+ * gate receives (top, bottom, left, right). */
+int or_gelatin_psf(const uint8_t* src, uint32_t w, uint32_t h, float* heff, uint32_t gate[4]);
+/* Grain amplitude of a stock (image_pipeline.rs:718-723). */
+float or_film_base_nominal(const char* preset);
+typedef struct or_finish_cfg {
+  double grain_size_px; /* after scaling (image_pipeline.rs:365) */
+  double strength;      /* effective strength (image_pipeline.rs:366) */
+  double push;          /* effective push (image_pipeline.rs:369-375) */
+  float base_nominal;
+  int32_t scanner_otf;
+} or_finish_cfg;
+/* Everything after the tiles (image_pipeline.rs:593-891): Hann blend with weights, DoG low-pass
+ * split, grain statistics, composite, scanner OTF and output gates, to a u8 image.  fields (may
+ * be NULL) receives 5 planes: d_norm, d_low, grain, tone, scanned grain; stats (may be NULL)
+ * receives high_mean, high_std, norm_factor. */
+int or_film_finish(const or_finish_cfg* cfg, uint32_t out_w, uint32_t out_h, uint32_t tile_step, uint32_t pad,
+                   uint32_t ntiles, const uint32_t* desc, const float* const* tiles, const uint8_t* src,
+                   const float* heff, uint8_t* out, float* fields, float* stats);
+
 #ifdef __cplusplus
 }
 #endif

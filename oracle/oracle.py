@@ -420,3 +420,161 @@ def resize_triangle(field, ow, oh):
     out = np.zeros((oh, ow), np.float32)
     lib().or_resize_triangle(_p(f, C.c_float), w, h, ow, oh, _p(out, C.c_float))
     return out
+
+
+# ---- image stages either side of the tile path (fg_oracle_film.cpp) ----
+
+class or_finish_cfg(C.Structure):
+    _fields_ = [("grain_size_px", C.c_double), ("strength", C.c_double), ("push", C.c_double),
+                ("base_nominal", C.c_float), ("scanner_otf", C.c_int32)]
+
+
+def luma_weights(preset):
+    w = (C.c_float * 3)()
+    lib().or_luma_weights(preset.encode(), w)
+    return np.array(list(w), np.float32)
+
+
+def luma(rgb, preset):
+    """Panchromatic luma of an RGB8 image (H, W, 3), image_pipeline.rs:259-296."""
+    a = np.ascontiguousarray(rgb, np.uint8)
+    h, w = a.shape[:2]
+    out = np.zeros((h, w), np.uint8)
+    lib().or_luma(_p(a, C.c_uint8), w, h, _p(luma_weights(preset), C.c_float), _p(out, C.c_uint8))
+    return out
+
+
+TRIANGLE, LANCZOS3 = 0, 1
+
+
+def resize_u8(img, ow, oh, filt):
+    a = np.ascontiguousarray(img, np.uint8)
+    h, w = a.shape
+    out = np.zeros((oh, ow), np.uint8)
+    lib().or_resize_u8(_p(a, C.c_uint8), w, h, ow, oh, filt, _p(out, C.c_uint8))
+    return out
+
+
+def gelatin_psf(img):
+    """h_effective of a u8 image and its camera gate (top, bottom, left, right)."""
+    a = np.ascontiguousarray(img, np.uint8)
+    h, w = a.shape
+    out = np.zeros((h, w), np.float32)
+    gate = (C.c_uint32 * 4)()
+    lib().or_gelatin_psf(_p(a, C.c_uint8), w, h, _p(out, C.c_float), gate)
+    return out, tuple(gate)
+
+
+def film_base_nominal(preset):
+    L = lib()
+    L.or_film_base_nominal.restype = C.c_float
+    return float(L.or_film_base_nominal(preset.encode()))
+
+
+def film_finish(preset, grain_px, strength, push, scanner_otf, out_w, out_h, grid, step, pad, densities, src, heff,
+                fields=False):
+    """image_pipeline.rs:593-891 on given tile densities: returns (u8 image, stats[, fields])."""
+    cfg = or_finish_cfg(grain_px, strength, push, film_base_nominal(preset), int(bool(scanner_otf)))
+    desc = np.array([[t.tx, t.ty, t.x_start, t.y_start, t.tw, t.th] for t in grid], np.uint32).ravel()
+    ds = [np.ascontiguousarray(d, np.float32) for d in densities]
+    ptrs = (C.POINTER(C.c_float) * len(ds))(*[_p(d, C.c_float) for d in ds])
+    s = np.ascontiguousarray(src, np.uint8)
+    he = np.ascontiguousarray(heff, np.float32)
+    out = np.zeros((out_h, out_w), np.uint8)
+    fl = np.zeros((5, out_h, out_w), np.float32) if fields else None
+    st = np.zeros(4, np.float32)
+    lib().or_film_finish(C.byref(cfg), out_w, out_h, step, pad, len(ds), _p(desc, C.c_uint32), ptrs,
+                         _p(s, C.c_uint8), _p(he, C.c_float), _p(out, C.c_uint8),
+                         _p(fl, C.c_float) if fields else None, _p(st, C.c_float))
+    return (out, st, fl) if fields else (out, st)
+
+
+class FilmTile:
+    """One overlapping tile of the image (image_pipeline.rs:400-424)."""
+
+    def __init__(self, idx, tx, ty, x_start, y_start, tw, th):
+        self.idx, self.tx, self.ty, self.x_start, self.y_start, self.tw, self.th = idx, tx, ty, x_start, y_start, tw, th
+
+
+def film_grid(out_w, out_h, grain_px, tile_size):
+    """Tile step, pad and tiles (image_pipeline.rs:377-424)."""
+    step = max(min(int(np.floor(384.0 * grain_px + 0.5)), tile_size), 48)
+    pad = min(max(step // 10, 12), 48)
+    ntx, nty = -(-out_w // step), -(-out_h // step)
+    tiles = []
+    for ty in range(nty):
+        for tx in range(ntx):
+            x0, y0 = tx * step, ty * step
+            xs, ys = max(x0 - pad, 0), max(y0 - pad, 0)
+            tiles.append(FilmTile(len(tiles), tx, ty, xs, ys, min(x0 + step + pad, out_w) - xs,
+                                  min(y0 + step + pad, out_h) - ys))
+    return tiles, step, pad
+
+
+def film_scaling(opts, out_w, out_h):
+    """(grain_size_px, effective_strength, effective_push) of image_pipeline.rs:347-375."""
+    user = opts["scale"] if opts["scale"] > 0 else 1.0
+    if opts["auto_scale"]:
+        ref = max(float(opts["reference_res"]), 512.0)
+        ratio = min(max(max(max(out_w, out_h), 1) / ref, 0.05), 5.0)
+        res, selwyn = ratio, float(np.sqrt(ratio))
+    else:
+        res, selwyn = 1.0, 1.0
+    grain = min(max(opts["grain_size_px"] * user * res, 0.05), 15.0)
+    strength = max(opts["grain_strength"] * float(np.sqrt(user)) * selwyn, 0.0)
+    p = opts["preset"].lower()
+    push = max(opts["push"], 2.0) if ("1600" in p or p == "caffenol") else max(opts["push"], 0.0)
+    return grain, strength, push
+
+
+FILM_DEFAULTS = dict(preset="tri-x", grain_size_px=2.2, grain_strength=1.0, exposure=1.0, output_resolution=None,
+                     tile_size=320, seed=42, auto_scale=False, scale=1.0, reference_res=6000, supersample=1, push=0.0,
+                     eberhard=1.0, scanner_otf=True)
+
+
+def _oracle_stock(preset, push):
+    p = preset.lower()
+    if p in ("t-max", "tmax"):
+        return 2
+    if p in ("hp5", "hp5-plus"):
+        return 3
+    if "1600" in p or p == "caffenol":
+        return 1
+    return 0
+
+
+def film_render_bw(image, threads=0, **kw):
+    """render_film_black_and_white_tiled (image_pipeline.rs:299-891) on the CPU: a u8 gray image
+    (H, W) or an RGB8 image (H, W, 3) to a u8 gray image, every tile through or_render_tile."""
+    opts = dict(FILM_DEFAULTS, **kw)
+    img = np.ascontiguousarray(image, np.uint8)
+    gray = img if img.ndim == 2 else luma(img, opts["preset"])
+    in_h, in_w = gray.shape
+    aspect = in_w / in_h
+    res = opts["output_resolution"]
+    if res is None:
+        out_w, out_h = in_w, in_h
+    elif res[1] == 0:
+        out_w, out_h = res[0], max(int(np.floor(res[0] / aspect + 0.5)), 1)
+    elif res[0] == 0:
+        out_w, out_h = max(int(np.floor(res[1] * aspect + 0.5)), 1), res[1]
+    else:
+        out_w, out_h = res
+    ss = min(max(opts["supersample"], 1), 4)
+    if ss > 1:
+        big = film_render_bw(image, threads, **dict(opts, supersample=1, output_resolution=(out_w * ss, out_h * ss)))
+        return resize_u8(big, out_w, out_h, TRIANGLE)
+    src = gray if (in_w, in_h) == (out_w, out_h) else resize_u8(gray, out_w, out_h, LANCZOS3)
+    heff, _ = gelatin_psf(src)
+    grain, strength, push = film_scaling(opts, out_w, out_h)
+    grid, step, pad = film_grid(out_w, out_h, grain, opts["tile_size"])
+    stock = _oracle_stock(opts["preset"], push)
+    dens = []
+    for t in grid:
+        seed = (opts["seed"] + t.idx * 73856093 + t.tx * 19349663 + t.ty * 83492791) & 0xFFFFFFFFFFFFFFFF
+        tile = np.ascontiguousarray(heff[t.y_start:t.y_start + t.th, t.x_start:t.x_start + t.tw])
+        d, _ = render_tile(stock, 1.0 / grain, tile, opts["exposure"], opts["push"], seed, FAITHFUL, threads)
+        dens.append(d)
+    out, _ = film_finish(opts["preset"], grain, strength, push, opts["scanner_otf"], out_w, out_h, grid, step, pad,
+                         dens, src, heff)
+    return out

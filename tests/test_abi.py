@@ -34,7 +34,8 @@ def test_every_declared_symbol_is_exported_and_bound():
 
 STRUCTS = ["fg_optics", "fg_emulsion_cfg", "fg_exposure_cfg", "fg_dev_cfg", "fg_dev_report",
            "fg_scan_cfg", "fg_crystals_host", "fg_crystals_out", "fg_segment", "fg_timings",
-           "fg_tile_params", "fg_batch_options", "fg_batch_stats", "fg_device_crystals"]
+           "fg_tile_params", "fg_batch_options", "fg_batch_stats", "fg_device_crystals", "fg_film_options",
+           "fg_film_report", "fg_finish_cfg"]
 
 
 def test_struct_layouts_match_ctypes(tmp_path):
