@@ -210,6 +210,18 @@ __global__ void k_fit_b(const BTile* __restrict__ bt, int ntiles, unsigned long 
   }
 }
 
+// Four-wide collapse of every tile's tree (the transport walk).
+__global__ void k_collapse4_b(const BTile* __restrict__ bt, int ntiles, unsigned long long ncap,
+                              const Node* __restrict__ nodes_all, Node4* __restrict__ out_all) {
+  const unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+  if (g >= ncap) return;
+  const BTile& t = bt[btile_of(bt, ntiles, g)];
+  const unsigned long long i = g - t.cbase;
+  const unsigned long long nint = t.n > 1 ? t.n - 1 : (t.n ? 1 : 0);
+  if (i >= nint) return;
+  collapse_node4(nodes_all + t.cbase, static_cast<int>(i), out_all + g);
+}
+
 // ---- development (development.rs:59-188), batched; see fg_develop.cu for the reasoning ----
 
 __global__ void k_maxdim_b(BTile* bt, int ntiles, unsigned long long ncap, const float4* __restrict__ D) {
@@ -433,6 +445,7 @@ struct fg_batch {
   DBuf<float4> A, Q, D;
   DBuf<uint64_t> keys;
   DBuf<Node> nodes;
+  DBuf<Node4> nodes4;
   DBuf<int> leaf_parent, visit, parent;
   DBuf<uint32_t> counts, size;
   DBuf<uint8_t> developed;
@@ -594,6 +607,7 @@ static void upload_descriptors(fg_batch* B, cudaStream_t st) {
     t.q = B->Q.p + cb;
     t.d = B->D.p + cb;
     t.nodes = B->nodes.p + cb;
+    t.nodes4 = B->nodes4.p + cb;
     t.s2id = nullptr;
     t.counts = B->counts.p + cb;
     t.tile = B->exposure.p + B->exp_off[i];
@@ -654,6 +668,7 @@ static void stage_bvh(fg_batch* B, cudaStream_t st) {
                                                      B->visit.p);
   k_fit_b<<<grid_for(B->ncap, 256), 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->A.p, B->Q.p, B->D.p, B->nodes.p,
                                                   B->leaf_parent.p, B->visit.p);
+  k_collapse4_b<<<grid_for(B->ncap, 256), 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->nodes.p, B->nodes4.p);
   FG_CUDA(cudaGetLastError());
 }
 
@@ -860,6 +875,7 @@ static void plan(fg_batch* B, const fg_batch_options* opt) {
   B->D.alloc(std::max<unsigned long long>(cap, 1), st);
   B->keys.alloc(std::max<unsigned long long>(cap, 1), st);
   B->nodes.alloc(std::max<unsigned long long>(cap, 1), st);
+  B->nodes4.alloc(std::max<unsigned long long>(cap, 1), st);
   B->leaf_parent.alloc(std::max<unsigned long long>(cap, 1), st);
   B->visit.alloc(std::max<unsigned long long>(cap, 1), st);
   B->parent.alloc(std::max<unsigned long long>(cap, 1), st);
@@ -1154,10 +1170,10 @@ fg_status fg_batch_wait(fg_batch* b, fg_batch_stats* stats) {
     s.transport_blocks = b->tr_blocks;
     s.scan_bin_px = b->bin_px;
     s.graph = b->exec ? 1u : 0u;
-    // Own kernels per run: Bridson x4, count + thin + flags, emit, set_n, Karras + fit, photon order x2, transport,
-    // maxdim + threshold + developed list + link + roots + finalize, scan prep, two bin passes, scan
-    // (CUB scans not counted).
-    s.kernel_launches = 4 + 3 + 1 + 1 + 2 + 2 + 1 + 6 + 1 + 2 + 1;
+    // Own kernels per run: Bridson x4, count + thin + flags, emit, set_n, Karras + fit + four-wide collapse,
+    // photon order x2, transport, maxdim + threshold + developed list + link + roots + finalize, scan prep,
+    // two bin passes, scan (CUB scans not counted).
+    s.kernel_launches = 4 + 3 + 1 + 1 + 3 + 2 + 1 + 6 + 1 + 2 + 1;
     b->stats = s;
     if (stats) *stats = s;
   });

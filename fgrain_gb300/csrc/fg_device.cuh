@@ -81,6 +81,55 @@ struct __align__(16) Node {
   int4 d;    // left, right, parent, unused
 };
 
+// Four-wide node collapsed from the binary LBVH (the transport walk): binary internal node i keeps
+// its grandchildren (or a child leaf in place of an internal child), so one step of a walk covers
+// two binary levels.  Child k's box is (lox[k], loy[k], loz[k]) - (hix[k], hiy[k], hiz[k]); ref[k]
+// is a collapsed node (the binary index, >= 0), a leaf (~crystal, < 0) or empty (INT32_MIN).
+struct __align__(16) Node4 {
+  float4 lox, loy, loz, hix, hiy, hiz;
+  int4 ref;
+  int4 pad;
+};
+
+// Node4 of binary internal node i.  Every child box is the same box its binary parent holds, so
+// the leaves a walk reaches are those of the binary walk: an ancestor box contains its
+// descendants' boxes, and the slab test is monotone in the box.
+__device__ __forceinline__ void collapse_node4(const Node* __restrict__ nodes, int i, Node4* __restrict__ out) {
+  float v[4][6];
+  int r[4];
+  int k = 0;
+  auto add = [&](int ref, float a0, float a1, float a2, float a3, float a4, float a5) {
+    v[k][0] = a0; v[k][1] = a1; v[k][2] = a2; v[k][3] = a3; v[k][4] = a4; v[k][5] = a5;
+    r[k] = ref;
+    ++k;
+  };
+  const Node nd = nodes[i];
+  auto expand = [&](int ref, float a0, float a1, float a2, float a3, float a4, float a5) {
+    if (ref == INT32_MIN) return;
+    if (ref < 0) {
+      add(ref, a0, a1, a2, a3, a4, a5);
+      return;
+    }
+    const Node ch = nodes[ref];
+    add(ch.d.x, ch.a.x, ch.a.y, ch.a.z, ch.a.w, ch.b.x, ch.b.y);
+    if (ch.d.y != INT32_MIN) add(ch.d.y, ch.b.z, ch.b.w, ch.c.x, ch.c.y, ch.c.z, ch.c.w);
+  };
+  expand(nd.d.x, nd.a.x, nd.a.y, nd.a.z, nd.a.w, nd.b.x, nd.b.y);
+  expand(nd.d.y, nd.b.z, nd.b.w, nd.c.x, nd.c.y, nd.c.z, nd.c.w);
+  for (; k < 4; ++k) {
+    for (int j = 0; j < 6; ++j) v[k][j] = 0.0f;
+    r[k] = INT32_MIN;
+  }
+  out->lox = make_float4(v[0][0], v[1][0], v[2][0], v[3][0]);
+  out->loy = make_float4(v[0][1], v[1][1], v[2][1], v[3][1]);
+  out->loz = make_float4(v[0][2], v[1][2], v[2][2], v[3][2]);
+  out->hix = make_float4(v[0][3], v[1][3], v[2][3], v[3][3]);
+  out->hiy = make_float4(v[0][4], v[1][4], v[2][4], v[3][4]);
+  out->hiz = make_float4(v[0][5], v[1][5], v[2][5], v[3][5]);
+  out->ref = make_int4(r[0], r[1], r[2], r[3]);
+  out->pad = make_int4(0, 0, 0, 0);
+}
+
 __device__ __forceinline__ int morph_of(const float4& d) { return __float_as_int(d.w); }
 
 // ---------------------------------------------------------------------------------------------

@@ -223,6 +223,12 @@ __global__ void k_replay_rays(const double* __restrict__ org, const double* __re
   if (chord_sum) chord_sum[i] = L;
 }
 
+// Four-wide collapse of a binary LBVH with n crystals (its max(n - 1, 1) internal nodes).
+__global__ void k_collapse4(const Node* __restrict__ nodes, uint32_t nint, Node4* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nint) collapse_node4(nodes, static_cast<int>(i), out + i);
+}
+
 // ---------------------------------------------------------------------------------------------
 TileDesc make_tile_desc(const fg_emulsion* em, const float* tile_dev, uint32_t tw, uint32_t th,
                         const fg_exposure_cfg& cfg, uint64_t seed, uint32_t* counts) {
@@ -274,9 +280,14 @@ void launch_transport_shape(const TileDesc* tiles_dev, int ntiles, unsigned long
 void expose(fg_engine* e, fg_emulsion* em, const float* tile_dev, uint32_t tw, uint32_t th,
             const fg_exposure_cfg& cfg, uint64_t seed, unsigned long long* photons_out) {
   cudaStream_t st = e->stream;
-  const TileDesc t = make_tile_desc(em, tile_dev, tw, th, cfg, seed, em->counts.p);
+  TileDesc t = make_tile_desc(em, tile_dev, tw, th, cfg, seed, em->counts.p);
   if (photons_out) *photons_out = t.P;
   if (t.P == 0 || em->n == 0) return;
+  const uint32_t nint = em->n > 1 ? em->n - 1 : 1;
+  DBuf<Node4> n4(nint, st);
+  k_collapse4<<<grid_for(nint, 256), 256, 0, st>>>(em->nodes.p, nint, n4.p);
+  FG_CUDA(cudaGetLastError());
+  t.nodes4 = n4.p;
   DBuf<TileDesc> td(1, st);
   DBuf<unsigned long long> ctr(1, st);
   FG_CUDA(cudaMemcpyAsync(td.p, &t, sizeof(TileDesc), cudaMemcpyHostToDevice, st));

@@ -13,6 +13,7 @@ struct __align__(16) TileDesc {
   const float4* q;
   const float4* d;
   const Node* nodes;
+  const Node4* nodes4;  // the same tree collapsed four-wide (the transport walk)
   const uint32_t* s2id;
   uint32_t* counts;
   const float* tile;
@@ -77,68 +78,62 @@ __device__ __forceinline__ void walk_lbvh(const Node* __restrict__ nodes, float3
   }
 }
 
-// The same walk with the leaf tests deferred to warp-wide rounds: each lane of `amask` visits nodes
-// until it holds a leaf (or its walk ends) and waits while the others find theirs; then the lanes
-// test their leaves together.  The expensive crystal test runs with many lanes active instead of
-// one or two, and the set of leaves tested is the same as walk_lbvh's.
+// The deferred walk over the four-wide tree: a hit child becomes the next node (the first one) or
+// goes on the stack; a leaf taken from the stack (or as the next node) is held until every lane of
+// `amask` holds one or has finished, then the lanes test their leaves together.  The leaves tested
+// are those of walk_lbvh on the binary tree.  With amask = the lane's own bit it is a plain walk.
 template <class F>
-__device__ __forceinline__ void walk_lbvh_deferred(const Node* __restrict__ nodes, float3 o, float3 inv,
-                                                   float tlim, uint32_t* err, F&& fn, uint32_t n, unsigned amask) {
+__device__ __forceinline__ void walk_bvh4_deferred(const Node4* __restrict__ nodes, float3 o, float3 inv, float tlim,
+                                                   uint32_t* err, F&& fn, uint32_t n, unsigned amask) {
   const int nint = n > 1 ? static_cast<int>(n - 1) : 1;
+  constexpr int EMPTY = INT32_MIN;
   constexpr uint32_t NONE = 0xffffffffu;
   int stack[64];
   int sp = 0;
-  int cur = n ? 0 : -1;
-  uint32_t p0 = NONE, p1 = NONE;
+  int cur = n ? 0 : EMPTY;
+  uint32_t leaf = NONE;
   for (;;) {
     for (;;) {
-      const bool want = cur >= 0 && p0 == NONE;
+      const bool want = cur != EMPTY && leaf == NONE;
       if (!__any_sync(amask, want)) break;
       if (!want) continue;
-      if (!index_ok(cur < nint, err, SITE_NODE, static_cast<uint32_t>(cur), n)) {
-        cur = -1;
+      if (cur < 0) {
+        leaf = static_cast<uint32_t>(~cur);
+        cur = sp > 0 ? stack[--sp] : EMPTY;
         continue;
       }
-      const float4 na = __ldg(&nodes[cur].a);
-      const float4 nb = __ldg(&nodes[cur].b);
-      const float4 nc = __ldg(&nodes[cur].c);
-      const int4 nd = __ldg(&nodes[cur].d);
-      float te, tx;
-      slab(o, inv, na.x, na.y, na.z, na.w, nb.x, nb.y, te, tx);
-      bool hl = tx >= te && tx >= 0.0f && te <= tlim;
-      slab(o, inv, nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, te, tx);
-      bool hr = tx >= te && tx >= 0.0f && te <= tlim && nd.y != INT32_MIN;
-      if (hl && nd.x < 0) {
-        p0 = static_cast<uint32_t>(~nd.x);
-        hl = false;
+      if (!index_ok(cur < nint, err, SITE_NODE, static_cast<uint32_t>(cur), n)) {
+        cur = EMPTY;
+        continue;
       }
-      if (hr && nd.y < 0) {
-        if (p0 == NONE) p0 = static_cast<uint32_t>(~nd.y); else p1 = static_cast<uint32_t>(~nd.y);
-        hr = false;
-      }
-      if (hl && hr) {
-        if (sp < 64) {
-          stack[sp++] = nd.y;
-        } else {
-          atomicOr(err, ERR_STACK_OVERFLOW);
+      const Node4* nd = nodes + cur;
+      const float4 lx = __ldg(&nd->lox), ly = __ldg(&nd->loy), lz = __ldg(&nd->loz);
+      const float4 hx = __ldg(&nd->hix), hy = __ldg(&nd->hiy), hz = __ldg(&nd->hiz);
+      const int4 rf = __ldg(&nd->ref);
+      int next = EMPTY;
+      auto child = [&](float a0, float a1, float a2, float a3, float a4, float a5, int r) {
+        float te, tx;
+        slab(o, inv, a0, a1, a2, a3, a4, a5, te, tx);
+        if (r != EMPTY && tx >= te && tx >= 0.0f && te <= tlim) {
+          if (next == EMPTY) {
+            next = r;
+          } else if (sp < 64) {
+            stack[sp++] = r;
+          } else {
+            atomicOr(err, ERR_STACK_OVERFLOW);
+          }
         }
-        cur = nd.x;
-      } else if (hl) {
-        cur = nd.x;
-      } else if (hr) {
-        cur = nd.y;
-      } else {
-        cur = sp > 0 ? stack[--sp] : -1;
-      }
+      };
+      child(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, rf.x);
+      child(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, rf.y);
+      child(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, rf.z);
+      child(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, rf.w);
+      cur = next != EMPTY ? next : (sp > 0 ? stack[--sp] : EMPTY);
     }
-    if (!__any_sync(amask, p0 != NONE)) break;
-    if (p0 != NONE) {
-      if (index_ok(p0 < n, err, SITE_LEAF, p0, n)) fn(p0);
-      p0 = NONE;
-      if (p1 != NONE) {
-        if (index_ok(p1 < n, err, SITE_LEAF, p1, n)) fn(p1);
-        p1 = NONE;
-      }
+    if (!__any_sync(amask, leaf != NONE)) break;
+    if (leaf != NONE) {
+      if (index_ok(leaf < n, err, SITE_LEAF, leaf, n)) fn(leaf);
+      leaf = NONE;
     }
   }
 }
@@ -251,11 +246,8 @@ __device__ __forceinline__ bool photon_bounce(const TileDesc& t, Photon& ph, Hit
       }
       hits[j] = HitS{t0, t1, s};
   };
-  if (amask) {
-    walk_lbvh_deferred(t.nodes, pos, inv, step * 1.00001f + 1e-3f, err, leaf, t.n, amask);
-  } else if (t.n > 0) {
-    walk_lbvh(t.nodes, pos, inv, step * 1.00001f + 1e-3f, err, leaf, t.n);
-  }
+  walk_bvh4_deferred(t.nodes4, pos, inv, step * 1.00001f + 1e-3f, err, leaf, t.n,
+                     amask ? amask : (1u << (threadIdx.x & 31)));
   float E = ph.E;
   P4 r{};
   for (int h = 0; h < nh; ++h) {
