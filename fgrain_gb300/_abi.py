@@ -190,6 +190,12 @@ PROTOTYPES = {
                              C.POINTER(_fp), _fp]),
     "fg_scanner_otf": (_st, [_vp, _fp, C.c_uint32, C.c_uint32, _fp, _fp]),
     "fg_resize_triangle": (_st, [_vp, _fp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _fp]),
+    "fg_tile_params_fast_preset": (_st, [C.c_char_p, C.c_double, C.c_uint32, C.c_uint32, C.c_double,
+                                         C.c_double, C.c_uint64, C.POINTER(fg_tile_params)]),
+    "fg_fast_grid": (_st, [C.POINTER(fg_tile_params), _u32p, _fp]),
+    "fg_render_tiles_fast": (_st, [_vp, C.POINTER(fg_tile_params), C.c_uint32, C.POINTER(_fp), C.POINTER(_fp),
+                                   C.POINTER(_vp)]),
+    "fg_render_tile_fast": (_st, [_vp, _fp, C.POINTER(fg_tile_params), _fp, _vp]),
     "fg_film_options_default": (None, [C.POINTER(fg_film_options)]),
     "fg_film_output_size": (_st, [C.POINTER(fg_film_options), C.c_uint32, C.c_uint32, _u32p, _u32p]),
     "fg_render_film": (_st, [_vp, _u8p, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(fg_film_options), _u8p,

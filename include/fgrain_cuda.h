@@ -400,6 +400,27 @@ fg_status fg_host_free(void* ptr);
 fg_status fg_render_batch(fg_engine* e, const fg_tile_params* tiles, uint32_t ntiles,
                           const float* const* exposure, float* const* d_neg);
 
+/* ---- fast approximation: the reference's wgpu tile model ---- */
+/* The compute shaders of GpuEngine::render_tile_all_gpu (src/gpu.rs:491-938,
+ * src/shaders/{poisson,develop,scan}.wgsl) as CUDA kernels: one jittered crystal per grid cell
+ * relaxed against its neighbours, a per-crystal Poisson photon count from the local pixel instead
+ * of photon transport, neighbour clumping, and a scan of the 5 x 5 cell columns around each ray.
+ * A different, cheaper model than fg_render_tile's CPU-path physics.  Uses of fg_tile_params:
+ * film size, pixels, samples per pixel, silver opacity, seed, r_min, radius distribution,
+ * morphology, aspect ratio, sensitivity, exposure, filament expansion and clumping factor. */
+/* GpuTileParams of the reference's GPU branch (src/image_pipeline.rs:455-518). */
+fg_status fg_tile_params_fast_preset(const char* preset, double pixel_size_um, uint32_t tw, uint32_t th,
+                                     double exposure, double push, uint64_t tile_seed, fg_tile_params* out);
+/* The tile's cell grid (src/gpu.rs:505-525): dims[3] = (w, h, d), cells of *cell_size um. */
+fg_status fg_fast_grid(const fg_tile_params* p, uint32_t* dims, float* cell_size);
+/* d_neg of ntiles tiles in one set of launches; cells (may be NULL, or hold NULL entries) receives
+ * each tile's final grid, 64 bytes per cell: position (4 floats), half-dimensions and expansion
+ * (4 floats), quaternion (4 floats), flags (occupied, morphology, developed, photons). */
+fg_status fg_render_tiles_fast(fg_engine* e, const fg_tile_params* params, uint32_t ntiles, const float* const* tiles,
+                               float* const* d_neg, void* const* cells);
+fg_status fg_render_tile_fast(fg_engine* e, const float* tile, const fg_tile_params* params, float* d_neg,
+                              void* cells);
+
 /* ---- Scan without device allocation ---------------------------------------------------------
  * No counterpart in the reference.  For callers that cannot let this library allocate device
  * memory (a host that runs under a fixed device-memory budget or its own pool allocator, a plugin

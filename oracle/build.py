@@ -16,7 +16,7 @@ OUT = HERE / "build" / "liboracle.so"
 
 def build(force: bool = False) -> Path:
     OUT.parent.mkdir(exist_ok=True)
-    srcs = [HERE / "fg_oracle.cpp", HERE / "fg_oracle_film.cpp"]
+    srcs = [HERE / "fg_oracle.cpp", HERE / "fg_oracle_film.cpp", HERE / "fg_oracle_fast.cpp"]
     deps = srcs + [HERE / "fg_oracle.h", HERE / "philox.h"]
     if not force and OUT.exists() and all(d.stat().st_mtime <= OUT.stat().st_mtime for d in deps):
         return OUT

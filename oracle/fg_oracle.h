@@ -250,6 +250,27 @@ int or_film_finish(const or_finish_cfg* cfg, uint32_t out_w, uint32_t out_h, uin
                    uint32_t ntiles, const uint32_t* desc, const float* const* tiles, const uint8_t* src,
                    const float* heff, uint8_t* out, float* fields, float* stats);
 
+/* ---- the reference's wgpu tile model (fg_oracle_fast.cpp) ---- */
+/* GpuTileParams (gpu.rs:18-37). */
+typedef struct or_fast_params {
+  double film_w, film_h, film_d;
+  uint32_t width_px, height_px, samples_per_pixel, _pad0;
+  double silver_opacity;
+  uint64_t seed;
+  double r_min, mean_crystal_radius, size_variance;
+  uint32_t morphology, threshold_photons;
+  double tabular_aspect_ratio, base_sensitivity, exposure, filament_expansion, clumping_proximity_factor;
+} or_fast_params;
+typedef struct or_fast_grid_t {
+  uint32_t w, h, d;
+  float cell_size;
+} or_fast_grid_t;
+/* The cell grid of a tile (gpu.rs:505-525). */
+int or_fast_grid(const or_fast_params* p, or_fast_grid_t* g);
+/* render_tile_all_gpu's shaders on the CPU: d_neg (width_px x height_px) and, when cells_out is not
+ * NULL, the final grid cells (64 bytes each: pos, dims and expansion, quaternion, flags). */
+int or_fast_tile(const or_fast_params* p, const float* tile, float* d_neg, void* cells_out);
+
 #ifdef __cplusplus
 }
 #endif

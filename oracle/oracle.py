@@ -578,3 +578,48 @@ def film_render_bw(image, threads=0, **kw):
     out, _ = film_finish(opts["preset"], grain, strength, push, opts["scanner_otf"], out_w, out_h, grid, step, pad,
                          dens, src, heff)
     return out
+
+
+# ---- the reference's wgpu tile model (fg_oracle_fast.cpp) ----
+
+class or_fast_params(C.Structure):
+    _fields_ = [("film_w", C.c_double), ("film_h", C.c_double), ("film_d", C.c_double),
+                ("width_px", C.c_uint32), ("height_px", C.c_uint32), ("samples_per_pixel", C.c_uint32),
+                ("_pad0", C.c_uint32), ("silver_opacity", C.c_double), ("seed", C.c_uint64),
+                ("r_min", C.c_double), ("mean_crystal_radius", C.c_double), ("size_variance", C.c_double),
+                ("morphology", C.c_uint32), ("threshold_photons", C.c_uint32),
+                ("tabular_aspect_ratio", C.c_double), ("base_sensitivity", C.c_double), ("exposure", C.c_double),
+                ("filament_expansion", C.c_double), ("clumping_proximity_factor", C.c_double)]
+
+
+class or_fast_grid_t(C.Structure):
+    _fields_ = [("w", C.c_uint32), ("h", C.c_uint32), ("d", C.c_uint32), ("cell_size", C.c_float)]
+
+
+FAST_CELL_DTYPE = np.dtype([("pos", "<f4", 4), ("dims_exp", "<f4", 4), ("rot", "<f4", 4), ("flags", "<u4", 4)])
+
+
+def fast_params(p):
+    """or_fast_params from any object with GpuTileParams' field names."""
+    q = or_fast_params()
+    for name, _ in or_fast_params._fields_:
+        if not name.startswith("_"):
+            setattr(q, name, getattr(p, name))
+    return q
+
+
+def fast_grid(p):
+    g = or_fast_grid_t()
+    lib().or_fast_grid(C.byref(fast_params(p)), C.byref(g))
+    return (g.w, g.h, g.d), g.cell_size
+
+
+def fast_tile(p, tile):
+    """render_tile_all_gpu's shaders on the CPU: (d_neg, cells as a (d, h, w) record array)."""
+    q = fast_params(p)
+    t = np.ascontiguousarray(tile, np.float32)
+    (w, h, d), _ = fast_grid(p)
+    out = np.zeros((q.height_px, q.width_px), np.float32)
+    cells = np.zeros((d, h, w), FAST_CELL_DTYPE)
+    lib().or_fast_tile(C.byref(q), _p(t, C.c_float), _p(out, C.c_float), C.c_void_p(cells.ctypes.data))
+    return out, cells
