@@ -286,10 +286,76 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* 
     if (warp == 0) {
       // The round's steps in warp order, exactly as if they ran one after another: warp w keeps its
       // first candidate (lane order) that is free in the grid and at least r from the points
-      // accepted for warps < w; with none left, its point retires.  One lane per candidate.
-      int ncom = 0;
-      unsigned retire = 0;
+      // accepted for warps < w; with none left, its point retires.
+      //
+      // Fast path: a warp's first grid-free candidate (its winner) is what that order keeps unless
+      // it lies within r of a point accepted for an earlier warp.  Lane w holds warp w's winner;
+      // the winners' pairwise conflicts come from shuffles, and warps are accepted in order, in
+      // registers, up to the first one whose winner conflicts with an accepted winner.
+      int fw = -1, WX = 0, WY = 0, WZ = 0;
+      if (lane < SYN_WARPS) {
+        const unsigned m = s_vmask[lane];
+        if (m) {
+          fw = __ffs(m) - 1;
+          WX = s_cx[lane][fw];
+          WY = s_cy[lane][fw];
+          WZ = s_cz[lane][fw];
+        }
+      }
+      unsigned cm = 0;  // bit u: this lane's winner conflicts with warp u's (u < lane)
+#pragma unroll
+      for (int u = 0; u < SYN_WARPS - 1; ++u) {
+        const int ux = __shfl_sync(0xffffffffu, WX, u), uy = __shfl_sync(0xffffffffu, WY, u);
+        const int uz = __shfl_sync(0xffffffffu, WZ, u), uf = __shfl_sync(0xffffffffu, fw, u);
+        if (u < lane && fw >= 0 && uf >= 0) {
+          const int ex = WX - ux, ey = WY - uy, ez = WZ - uz;
+          if (ex * ex + ey * ey + ez * ez < SYN_R2X) cm |= 1u << u;
+        }
+      }
+      unsigned acc = 0, retire = 0;
+      int wslow = SYN_WARPS;
       for (int w = 0; w < SYN_WARPS; ++w) {
+        const int f = __shfl_sync(0xffffffffu, fw, w);
+        const unsigned c = __shfl_sync(0xffffffffu, cm, w);
+        if (f < 0) {
+          retire |= 1u << w;
+          continue;
+        }
+        if (c & acc) {
+          wslow = w;
+          break;
+        }
+        acc |= 1u << w;
+      }
+      // Commit the accepted winners, appending to the active list in warp order.
+      bool inside = false;
+      int cridx = 0;
+      if (lane < SYN_WARPS && ((acc >> lane) & 1u)) {
+        const int slot = __popc(acc & ((1u << lane) - 1u));
+        s_wx[slot] = WX;
+        s_wy[slot] = WY;
+        s_wz[slot] = WZ;
+        const int ccx = WX >> 10, ccy = WY >> 10, ccz = WZ >> 10;
+        const int rx = ccx - ox, ry = ccy - oy, rz = ccz + 2;
+        if (index_ok(rx >= 0 && rx < SYN_R && ry >= 0 && ry < SYN_R && rz >= 0 && rz < nz, err, SITE_SYN_COMMIT,
+                     static_cast<uint32_t>(rx | (ry << 8) | (rz << 16)), blockIdx.x)) {
+          cridx = (rz * SYN_R + ry) * SYN_R + rx;
+          grid[cridx] = syn_word(WX, WY, WZ);
+          inside = ccx >= x0 && ccx < x1 && ccy >= y0 && ccy < y1;
+        }
+      }
+      const unsigned im = __ballot_sync(0xffffffffu, inside);
+      const int nbase = s_nact;
+      if (inside) {
+        const int pos = nbase + __popc(im & ((1u << lane) - 1u));
+        if (index_ok(pos < acap, err, SITE_SYN_ACTIVE, pos, blockIdx.x)) active[pos] = static_cast<uint16_t>(cridx);
+      }
+      __syncwarp();
+      if (lane == 0) s_nact = min(nbase + __popc(im), acap);
+      __syncwarp();
+      // Serial path from the first conflicting warp on.  One lane per candidate.
+      int ncom = __popc(acc);
+      for (int w = wslow; w < SYN_WARPS; ++w) {
         const unsigned m = s_vmask[w];
         bool ok = false;
         int X = 0, Y = 0, Z = 0;

@@ -92,6 +92,7 @@ __device__ __forceinline__ void walk_bvh4_deferred(const Node4* __restrict__ nod
   int sp = 0;
   int cur = n ? 0 : EMPTY;
   uint32_t leaf = NONE;
+  const float3 oi = make_float3(o.x * inv.x, o.y * inv.y, o.z * inv.z);
   for (;;) {
     for (;;) {
       const bool want = cur != EMPTY && leaf == NONE;
@@ -111,10 +112,16 @@ __device__ __forceinline__ void walk_bvh4_deferred(const Node4* __restrict__ nod
       const float4 hx = __ldg(&nd->hix), hy = __ldg(&nd->hiy), hz = __ldg(&nd->hiz);
       const int4 rf = __ldg(&nd->ref);
       int next = EMPTY;
+      // Slab test as lo * inv - o * inv (one FMA per plane).  Its rounding differs from the exact
+      // walk's (lo - o) * inv by about |o| * 2^-24 in box units, far inside the leaf padding, so
+      // every crystal the ray meets is still reached; the crystal test itself is unchanged.
       auto child = [&](float a0, float a1, float a2, float a3, float a4, float a5, int r) {
-        float te, tx;
-        slab(o, inv, a0, a1, a2, a3, a4, a5, te, tx);
-        if (r != EMPTY && tx >= te && tx >= 0.0f && te <= tlim) {
+        const float t1x = fmaf(a0, inv.x, -oi.x), t2x = fmaf(a3, inv.x, -oi.x);
+        const float t1y = fmaf(a1, inv.y, -oi.y), t2y = fmaf(a4, inv.y, -oi.y);
+        const float t1z = fmaf(a2, inv.z, -oi.z), t2z = fmaf(a5, inv.z, -oi.z);
+        const float te = fmaxf(fmaxf(fminf(t1x, t2x), fminf(t1y, t2y)), fmaxf(fminf(t1z, t2z), 0.0f));
+        const float tx = fminf(fminf(fmaxf(t1x, t2x), fmaxf(t1y, t2y)), fminf(fmaxf(t1z, t2z), tlim));
+        if (r != EMPTY && te <= tx) {
           if (next == EMPTY) {
             next = r;
           } else if (sp < 64) {
