@@ -80,7 +80,7 @@ __device__ __forceinline__ void walk_lbvh(const Node* __restrict__ nodes, float3
 
 // The deferred walk over the four-wide tree: a hit child becomes the next node (the first one) or
 // goes on the stack; a leaf taken from the stack (or as the next node) is held until every lane of
-// `amask` holds one or has finished, then the lanes test their leaves together.  The leaves tested
+// `amask` holds one or has finished, then the lanes test one leaf each together.  The leaves tested
 // are those of walk_lbvh on the binary tree.  With amask = the lane's own bit it is a plain walk.
 template <class F>
 __device__ __forceinline__ void walk_bvh4_deferred(const Node4* __restrict__ nodes, float3 o, float3 inv, float tlim,
@@ -91,15 +91,18 @@ __device__ __forceinline__ void walk_bvh4_deferred(const Node4* __restrict__ nod
   int stack[64];
   int sp = 0;
   int cur = n ? 0 : EMPTY;
-  uint32_t leaf = NONE;
+  uint32_t leaf = NONE, leaf2 = NONE;  // a pending leaf and one found speculatively
   const float3 oi = make_float3(o.x * inv.x, o.y * inv.y, o.z * inv.z);
   for (;;) {
     for (;;) {
-      const bool want = cur != EMPTY && leaf == NONE;
-      if (!__any_sync(amask, want)) break;
+      // Visit while some lane still has no leaf; a lane that holds one goes on walking until it
+      // finds a second (speculative traversal) instead of idling.
+      const bool need = cur != EMPTY && leaf == NONE;
+      if (!__any_sync(amask, need)) break;
+      const bool want = cur != EMPTY && leaf2 == NONE;
       if (!want) continue;
       if (cur < 0) {
-        leaf = static_cast<uint32_t>(~cur);
+        if (leaf == NONE) leaf = static_cast<uint32_t>(~cur); else leaf2 = static_cast<uint32_t>(~cur);
         cur = sp > 0 ? stack[--sp] : EMPTY;
         continue;
       }
@@ -140,7 +143,8 @@ __device__ __forceinline__ void walk_bvh4_deferred(const Node4* __restrict__ nod
     if (!__any_sync(amask, leaf != NONE)) break;
     if (leaf != NONE) {
       if (index_ok(leaf < n, err, SITE_LEAF, leaf, n)) fn(leaf);
-      leaf = NONE;
+      leaf = leaf2;
+      leaf2 = NONE;
     }
   }
 }
