@@ -134,7 +134,8 @@ class fg_film_options(C.Structure):
                 ("exposure", C.c_double), ("color", C.c_int32), ("out_w", C.c_uint32), ("out_h", C.c_uint32),
                 ("tile_size", C.c_uint32), ("seed", C.c_uint64), ("auto_scale", C.c_int32),
                 ("reference_res", C.c_uint32), ("scale", C.c_double), ("supersample", C.c_uint32),
-                ("scanner_otf", C.c_int32), ("push", C.c_double), ("eberhard", C.c_double)]
+                ("scanner_otf", C.c_int32), ("push", C.c_double), ("eberhard", C.c_double),
+                ("batch_bytes", C.c_uint64)]
 
 
 class fg_film_report(C.Structure):

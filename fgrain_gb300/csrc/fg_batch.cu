@@ -932,6 +932,24 @@ static void capture(fg_batch* B) {
   FG_CUDA(cudaGraphInstantiate(&B->exec, B->graph, 0));
 }
 
+unsigned long long tile_footprint(const fg_tile_params& p, unsigned long long* slots) {
+  SynthTile s;
+  TileDesc t;
+  ScanTile c;
+  BTile b;
+  derive_tile(p, s, t, c, b);
+  if (slots) *slots = s.ccap;
+  const double side = std::max(p.film_w, p.film_h) / PHOTON_CELL_UM;
+  uint32_t bits = 0;
+  while ((1u << bits) < static_cast<uint32_t>(std::ceil(side))) ++bits;
+  const unsigned long long px = static_cast<unsigned long long>(p.width_px) * p.height_px;
+  // Per crystal slot: records 48, key 8, nodes 64 + 128, links and flags 36, expansion 8, scan
+  // prep 128, bin entries 32 (plus slack); cells 4 B; Morton slots 8 B; photon order; images.
+  return static_cast<unsigned long long>(s.ccap) * 480ull + static_cast<unsigned long long>(s.gw) * s.gh * s.gd * 4ull +
+         static_cast<unsigned long long>(s.slots) * 8ull + static_cast<unsigned long long>(t.P) * 4ull +
+         (1ull << (2 * bits)) * 12ull + px * 8ull + 4096ull;
+}
+
 }  // namespace fg
 
 extern "C" {

@@ -40,8 +40,15 @@ struct FilmGate {
 };
 
 struct GatherTile {
+  const float* img;  // the layer's h_effective, W floats per row
   float* dst;
-  uint32_t xs, ys, tw, th;
+  uint32_t W, xs, ys, tw, th;
+};
+
+struct CopyTile {
+  const float* src;
+  float* dst;
+  unsigned long long n;
 };
 
 struct FilmTile {
@@ -239,14 +246,22 @@ __global__ void k_psf_v(const float* __restrict__ tn, const float* __restrict__ 
 }
 
 // h_effective -> the batch's exposure tiles; blockIdx.y is the tile.
-__global__ void k_gather_tiles(const float* __restrict__ img, uint32_t W, const GatherTile* __restrict__ tiles) {
+__global__ void k_gather_tiles(const GatherTile* __restrict__ tiles) {
   const GatherTile t = tiles[blockIdx.y];
   const size_t n = static_cast<size_t>(t.tw) * t.th;
   for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<size_t>(gridDim.x) * blockDim.x) {
     const uint32_t px = static_cast<uint32_t>(i % t.tw), py = static_cast<uint32_t>(i / t.tw);
-    t.dst[i] = img[static_cast<size_t>(t.ys + py) * W + t.xs + px];
+    t.dst[i] = t.img[static_cast<size_t>(t.ys + py) * t.W + t.xs + px];
   }
+}
+
+// Tile densities of a batch -> the image's density array; blockIdx.y is the tile.
+__global__ void k_copy_tiles(const CopyTile* __restrict__ tiles) {
+  const CopyTile t = tiles[blockIdx.y];
+  for (unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; i < t.n;
+       i += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
+    t.dst[i] = t.src[i];
 }
 
 // Hann overlap blend with the weight sums (image_pipeline.rs:593-655): d_norm and the
@@ -627,12 +642,15 @@ void prepare_layer(Layer& L, const uint8_t* gray, uint32_t in_w, uint32_t in_h, 
   L.grid = make_grid(L.rw, L.rh, L.grain, o.tile_size);
 }
 
-// Renders gray layers (device u8 images of in_w x in_h) into device u8 outputs, all tiles of all
-// layers in one batch.
+// Renders gray layers (device u8 images of in_w x in_h) into device u8 outputs.  The tiles of all
+// layers run as consecutive batches in tile order, each within the byte budget (one batch when
+// everything fits); their densities are gathered into one device array before the finish.
+// Tiles are independent, so the result does not depend on how they are grouped.
 void render_layers(fg_engine* e, std::vector<Layer>& layers, const std::vector<const uint8_t*>& gray, uint32_t in_w,
                    uint32_t in_h, const fg_film_options& o, const std::vector<uint8_t*>& out, fg_film_report* rep) {
   cudaStream_t st = e->stream;
   std::vector<fg_tile_params> params;
+  std::vector<GatherTile> src;  // where each tile's exposure comes from (dst filled per batch)
   for (size_t l = 0; l < layers.size(); ++l) {
     Layer& L = layers[l];
     prepare_layer(L, gray[l], in_w, in_h, o, st);
@@ -645,53 +663,85 @@ void render_layers(fg_engine* e, std::vector<Layer>& layers, const std::vector<c
       fg_tile_params tp;
       ok(e, fg_tile_params_preset(o.preset, 1.0 / L.grain, q[4], q[5], o.exposure, o.push, seed, &tp));
       params.push_back(tp);
+      src.push_back(GatherTile{L.heff.p, nullptr, L.rw, q[2], q[3], q[4], q[5]});
     }
   }
+  const size_t ntot = params.size();
+  std::vector<unsigned long long> doff(ntot);
+  unsigned long long dtot = 0;
+  for (size_t i = 0; i < ntot; ++i) {
+    doff[i] = dtot;
+    dtot += static_cast<unsigned long long>(params[i].width_px) * params[i].height_px;
+  }
+  DBuf<float> dens(std::max<unsigned long long>(dtot, 1), st);
+  size_t freeb = 0, totalb = 0;
+  FG_CUDA(cudaMemGetInfo(&freeb, &totalb));
+  const unsigned long long budget =
+      o.batch_bytes ? o.batch_bytes : static_cast<unsigned long long>(0.7 * static_cast<double>(freeb));
   fg_batch_options bo{};
   bo.use_graph = 0;
   bo.autotune = 0;
-  fg_batch* b = nullptr;
-  ok(e, fg_batch_create(e, params.data(), static_cast<uint32_t>(params.size()), &bo, &b));
-  struct BatchGuard {
-    fg_batch* b;
-    ~BatchGuard() { fg_batch_destroy(b); }
-  } guard_b{b};
-  for (Layer& L : layers) {
-    const uint32_t nt = static_cast<uint32_t>(L.grid.desc.size() / 6);
-    std::vector<GatherTile> gt(nt);
-    for (uint32_t t = 0; t < nt; ++t) {
-      const uint32_t* q = L.grid.desc.data() + 6 * t;
-      float* dst = nullptr;
-      ok(e, fg_batch_exposure_device(b, L.first_tile + t, &dst));
-      gt[t] = GatherTile{dst, q[2], q[3], q[4], q[5]};
+  for (size_t first = 0; first < ntot;) {
+    size_t last = first;
+    unsigned long long bytes = 0, slots = 0;
+    while (last < ntot) {
+      unsigned long long s = 0;
+      const unsigned long long b = tile_footprint(params[last], &s);
+      if (last > first && (bytes + b > budget || slots + s >= 0x7fffffffull)) break;
+      bytes += b;
+      slots += s;
+      ++last;
     }
-    DBuf<GatherTile> dgt(nt, st);
-    FG_CUDA(cudaMemcpyAsync(dgt.p, gt.data(), nt * sizeof(GatherTile), cudaMemcpyHostToDevice, st));
-    k_gather_tiles<<<dim3(64, nt), 256, 0, st>>>(L.heff.p, L.rw, dgt.p);
+    const uint32_t nb = static_cast<uint32_t>(last - first);
+    FG_REQUIRE(nb <= 65535, "too many tiles in one batch");
+    fg_batch* b = nullptr;
+    ok(e, fg_batch_create(e, params.data() + first, nb, &bo, &b));
+    struct BatchGuard {
+      fg_batch* b;
+      ~BatchGuard() { fg_batch_destroy(b); }
+    } guard_b{b};
+    std::vector<GatherTile> gt(nb);
+    std::vector<CopyTile> ct(nb);
+    for (uint32_t t = 0; t < nb; ++t) {
+      gt[t] = src[first + t];
+      ok(e, fg_batch_exposure_device(b, t, &gt[t].dst));
+      const float* d = nullptr;
+      ok(e, fg_batch_density_device(b, t, &d));
+      ct[t] = CopyTile{d, dens.p + doff[first + t],
+                       static_cast<unsigned long long>(params[first + t].width_px) * params[first + t].height_px};
+    }
+    DBuf<GatherTile> dgt(nb, st);
+    DBuf<CopyTile> dct(nb, st);
+    FG_CUDA(cudaMemcpyAsync(dgt.p, gt.data(), nb * sizeof(GatherTile), cudaMemcpyHostToDevice, st));
+    FG_CUDA(cudaMemcpyAsync(dct.p, ct.data(), nb * sizeof(CopyTile), cudaMemcpyHostToDevice, st));
+    k_gather_tiles<<<dim3(64, nb), 256, 0, st>>>(dgt.p);
     FG_CUDA(cudaGetLastError());
+    ok(e, fg_batch_run(b));
+    k_copy_tiles<<<dim3(64, nb), 256, 0, st>>>(dct.p);
+    FG_CUDA(cudaGetLastError());
+    fg_batch_stats bs{};
+    ok(e, fg_batch_wait(b, &bs));
+    if (rep) {
+      rep->total_crystals += bs.crystals;
+      rep->photons += bs.photons;
+    }
+    first = last;
   }
-  ok(e, fg_batch_run(b));
-  fg_batch_stats bs{};
-  ok(e, fg_batch_wait(b, &bs));
   for (size_t l = 0; l < layers.size(); ++l) {
     Layer& L = layers[l];
     const uint32_t nt = static_cast<uint32_t>(L.grid.desc.size() / 6);
-    std::vector<const float*> dens(nt);
-    for (uint32_t t = 0; t < nt; ++t) ok(e, fg_batch_density_device(b, L.first_tile + t, &dens[t]));
+    std::vector<const float*> dp(nt);
+    for (uint32_t t = 0; t < nt; ++t) dp[t] = dens.p + doff[L.first_tile + t];
     const FinishArgs fa{o.preset, L.grain, L.strength, L.push, o.scanner_otf};
     if (L.rw == L.ow && L.rh == L.oh) {
-      launch_finish(fa, L.rw, L.rh, L.grid, dens, L.src.p, L.heff.p, out[l], nullptr, nullptr, st);
+      launch_finish(fa, L.rw, L.rh, L.grid, dp, L.src.p, L.heff.p, out[l], nullptr, nullptr, st);
     } else {
       DBuf<uint8_t> big(static_cast<size_t>(L.rw) * L.rh, st);
-      launch_finish(fa, L.rw, L.rh, L.grid, dens, L.src.p, L.heff.p, big.p, nullptr, nullptr, st);
+      launch_finish(fa, L.rw, L.rh, L.grid, dp, L.src.p, L.heff.p, big.p, nullptr, nullptr, st);
       launch_resize_u8(big.p, L.rw, L.rh, L.ow, L.oh, RESAMPLE_TRIANGLE, out[l], st);
     }
   }
-  if (rep) {
-    rep->total_tiles += params.size();
-    rep->total_crystals += bs.crystals;
-    rep->photons += bs.photons;
-  }
+  if (rep) rep->total_tiles += ntot;
 }
 
 }  // namespace

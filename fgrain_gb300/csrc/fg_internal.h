@@ -182,6 +182,10 @@ void from_sorted(const fg_emulsion* em, const std::vector<T>& sorted, T* by_id) 
 void launch_otf(const float* in, float* tmp, float* out, uint32_t w, uint32_t h, const float k[3], float scale,
                 cudaStream_t st);
 
+// Device bytes a batch needs for one tile (fg_batch.cu), a little above what plan() allocates;
+// *slots (may be null) receives the tile's crystal slots.
+unsigned long long tile_footprint(const fg_tile_params& p, unsigned long long* slots);
+
 // Device state of a new emulsion (counts, development, clumps), zeroed (fg_engine.cu).
 void alloc_state(fg_emulsion* em, cudaStream_t st);
 

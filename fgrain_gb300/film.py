@@ -37,11 +37,11 @@ class FilmRenderOptions:
     push: float = 0.0
     eberhard: float = 1.0
     scanner_otf: bool = True
+    batch_bytes: int = 0  # device bytes one batch of tiles may use (0: 70 % of the free memory)
 
     def to_c(self) -> _abi.fg_film_options:
         o = _abi.fg_film_options()
-        self._preset = self.preset.encode()
-        o.preset = self._preset
+        o.preset = self.preset.encode()  # the structure keeps the bytes alive
         o.grain_size_px = self.grain_size_px
         o.grain_strength = self.grain_strength
         o.exposure = self.exposure
@@ -57,6 +57,7 @@ class FilmRenderOptions:
         o.scanner_otf = int(bool(self.scanner_otf))
         o.push = self.push
         o.eberhard = self.eberhard
+        o.batch_bytes = int(self.batch_bytes)
         return o
 
 

@@ -253,6 +253,8 @@ typedef struct fg_film_options {
   int32_t scanner_otf;     /* 1 */
   double push;             /* 0 */
   double eberhard;         /* 1.0 */
+  uint64_t batch_bytes;    /* device bytes one batch of tiles may use; 0: 70 % of the free memory.
+                              Larger images run as several batches, with identical results. */
 } fg_film_options;
 
 typedef struct fg_film_report {  /* ImageProcessReport (src/image_pipeline.rs:103-113) */
@@ -268,7 +270,8 @@ fg_status fg_film_output_size(const fg_film_options* o, uint32_t in_w, uint32_t 
 /* render_film_black_and_white_tiled / render_film_color_tiled (src/image_pipeline.rs:299-891,
  * 1017-1085) with every stage on the device: pixels is a u8 image of `channels` (1 gray, 3 RGB
  * interleaved) channels, out receives out_w x out_h x (color ? 3 : 1) bytes.  A gray render of an
- * RGB image takes the stock's panchromatic luma first.  All tiles of all layers run as one batch. */
+ * RGB image takes the stock's panchromatic luma first.  The tiles of all layers run as one batch,
+ * or as consecutive batches within options->batch_bytes. */
 fg_status fg_render_film(fg_engine* e, const uint8_t* pixels, uint32_t w, uint32_t h, uint32_t channels,
                          const fg_film_options* options, uint8_t* out, fg_film_report* report);
 

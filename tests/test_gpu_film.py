@@ -172,3 +172,16 @@ def test_render_rejects_bad_arguments(engine):
         film.render_film(np.zeros((8, 8), np.uint8), film.FilmRenderOptions(tile_size=16), engine)
     with pytest.raises(ValueError):
         film.render_film(np.zeros((8, 8, 2), np.uint8), None, engine)
+
+
+def test_render_in_several_batches_equals_one_batch(engine):
+    """With a small device budget the tiles run as consecutive batches; tiles are independent, so
+    the photograph is the same bit for bit."""
+    rgb = np.random.default_rng(8).integers(0, 256, (200, 260, 3), dtype=np.uint8)
+    opts = film.FilmRenderOptions(preset="hp5", grain_size_px=1.8, tile_size=64, color=True, seed=3)
+    rep1, one = film.render_film(rgb, opts, engine)
+    for budget in (64 << 20, 1):
+        small = film.FilmRenderOptions(**{**opts.__dict__, "batch_bytes": budget})
+        rep, many = film.render_film(rgb, small, engine)
+        np.testing.assert_array_equal(one, many)
+        assert rep.total_crystals == rep1.total_crystals and rep.total_tiles == rep1.total_tiles
