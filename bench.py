@@ -388,10 +388,12 @@ def run_c4(args):
 
     rank, world, local, td = dist()
     rng = np.random.default_rng(1)
-    img = np.stack([np.clip(gaussian_filter(rng.random((4096, 4096)), 16.0, mode="reflect"), 0.0, 1.0) ** 2.2
+    side = args.film_side
+    img = np.stack([np.clip(gaussian_filter(rng.random((side, side)), 16.0, mode="reflect"), 0.0, 1.0) ** 2.2
                     for _ in range(3)], -1)
     img = np.ascontiguousarray(np.round(img * 255.0).astype(np.uint8))
-    opts = film.FilmRenderOptions(preset="t-max", grain_size_px=1.1, supersample=4, color=True, seed=SEED)
+    opts = film.FilmRenderOptions(preset="t-max", grain_size_px=1.1, supersample=4, color=True, seed=SEED,
+                                  batch_bytes=int(args.batch_gb * 2**30))
     engine = fg.GpuEngine(local)
     for _ in range(max(args.warmup, 0)):
         film.render_film(img, opts, engine)
@@ -405,7 +407,7 @@ def run_c4(args):
             times.append(time.perf_counter() - t0)
             reps.append(rep)
     t = reduce_max(td, sum(times) / len(times))
-    px = 4096 * 4096 * 3
+    px = side * side * 3
     if rank == 0:
         value = px * world / t / 1e6
         rep = reps[-1]
@@ -413,10 +415,12 @@ def run_c4(args):
             "metric": METRIC, "value": value, "unit": "Mpx/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "C4: 4096x4096 RGB blurred-noise photograph, t-max, grain 1.1 px, supersample 4 "
-                                   "(16384^2 per channel), colour, whole photograph per fg_render_film call",
+            "config": {"workload": (f"C4: {side}x{side} RGB blurred-noise photograph, t-max, grain 1.1 px, supersample 4 "
+                                    f"({4 * side}^2 per channel), colour, whole photograph per fg_render_film call"
+                                    + ("" if side == 4096 else " (reduced size)")),
                        "tiles": rep.total_tiles, "output_px_channels": px, "crystals": rep.total_crystals,
-                       "photons": rep.photons, "parallelism": f"replicas x{world}"},
+                       "photons": rep.photons, "parallelism": f"replicas x{world}",
+                       "stage_ms": rep.extra},
             "e2e": {"value": value, "unit": "Mpx/s", "h2d_bytes_per_step": img.nbytes, "d2h_bytes_per_step": out.nbytes},
             "clocks": ck.summary()}))
 
@@ -462,6 +466,9 @@ def main():
     ap.add_argument("--workload", choices=["c2", "c3", "c4"], default="c2",
                     help="c2: the headline configuration; c3: the mixed batch; c4: a 4096^2 RGB photograph at "
                          "supersample 4 through the film renderer (c3 and c4 are reported, not the headline)")
+    ap.add_argument("--film-side", type=int, default=4096, help="c4: side of the RGB photograph (4096 for C4)")
+    ap.add_argument("--batch-gb", type=float, default=0.0,
+                    help="c4: device GiB one batch of tiles may use (0: 70 %% of the free memory)")
     ap.add_argument("--profile-region", action="store_true",
                     help="bracket the timed replays with cudaProfilerStart/Stop")
     args = ap.parse_args()

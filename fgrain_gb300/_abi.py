@@ -141,7 +141,8 @@ class fg_film_options(C.Structure):
 class fg_film_report(C.Structure):
     _fields_ = [("in_w", C.c_uint32), ("in_h", C.c_uint32), ("out_w", C.c_uint32), ("out_h", C.c_uint32),
                 ("total_tiles", C.c_uint64), ("total_crystals", C.c_uint64), ("photons", C.c_uint64),
-                ("elapsed_seconds", C.c_double)]
+                ("elapsed_seconds", C.c_double), ("prep_ms", C.c_double), ("tiles_ms", C.c_double),
+                ("finish_ms", C.c_double)]
 
 
 class fg_finish_cfg(C.Structure):

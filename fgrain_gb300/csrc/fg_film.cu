@@ -649,6 +649,17 @@ void prepare_layer(Layer& L, const uint8_t* gray, uint32_t in_w, uint32_t in_h, 
 void render_layers(fg_engine* e, std::vector<Layer>& layers, const std::vector<const uint8_t*>& gray, uint32_t in_w,
                    uint32_t in_h, const fg_film_options& o, const std::vector<uint8_t*>& out, fg_film_report* rep) {
   cudaStream_t st = e->stream;
+  struct Ev {
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    Ev() {
+      for (auto& x : ev) FG_CUDA(cudaEventCreate(&x));
+    }
+    ~Ev() {
+      for (auto& x : ev)
+        if (x) cudaEventDestroy(x);
+    }
+  } ev;
+  FG_CUDA(cudaEventRecord(ev.ev[0], st));
   std::vector<fg_tile_params> params;
   std::vector<GatherTile> src;  // where each tile's exposure comes from (dst filled per batch)
   for (size_t l = 0; l < layers.size(); ++l) {
@@ -666,6 +677,7 @@ void render_layers(fg_engine* e, std::vector<Layer>& layers, const std::vector<c
       src.push_back(GatherTile{L.heff.p, nullptr, L.rw, q[2], q[3], q[4], q[5]});
     }
   }
+  FG_CUDA(cudaEventRecord(ev.ev[1], st));
   const size_t ntot = params.size();
   std::vector<unsigned long long> doff(ntot);
   unsigned long long dtot = 0;
@@ -727,6 +739,7 @@ void render_layers(fg_engine* e, std::vector<Layer>& layers, const std::vector<c
     }
     first = last;
   }
+  FG_CUDA(cudaEventRecord(ev.ev[2], st));
   for (size_t l = 0; l < layers.size(); ++l) {
     Layer& L = layers[l];
     const uint32_t nt = static_cast<uint32_t>(L.grid.desc.size() / 6);
@@ -741,7 +754,18 @@ void render_layers(fg_engine* e, std::vector<Layer>& layers, const std::vector<c
       launch_resize_u8(big.p, L.rw, L.rh, L.ow, L.oh, RESAMPLE_TRIANGLE, out[l], st);
     }
   }
-  if (rep) rep->total_tiles += ntot;
+  FG_CUDA(cudaEventRecord(ev.ev[3], st));
+  FG_CUDA(cudaEventSynchronize(ev.ev[3]));
+  if (rep) {
+    rep->total_tiles += ntot;
+    float a = 0, b = 0, c = 0;
+    FG_CUDA(cudaEventElapsedTime(&a, ev.ev[0], ev.ev[1]));
+    FG_CUDA(cudaEventElapsedTime(&b, ev.ev[1], ev.ev[2]));
+    FG_CUDA(cudaEventElapsedTime(&c, ev.ev[2], ev.ev[3]));
+    rep->prep_ms += a;
+    rep->tiles_ms += b;
+    rep->finish_ms += c;
+  }
 }
 
 }  // namespace

@@ -111,7 +111,8 @@ def render_film(image, options: FilmRenderOptions | None = None, engine=None):
     rep = _abi.fg_film_report()
     _run(engine, "fg_render_film", _u8(img), w, h, ch, C.byref(co), _u8(out), C.byref(rep))
     return ImageProcessReport((rep.in_w, rep.in_h), (rep.out_w, rep.out_h), rep.total_tiles, rep.total_crystals,
-                              rep.photons, rep.elapsed_seconds), out
+                              rep.photons, rep.elapsed_seconds,
+                              {"prep_ms": rep.prep_ms, "tiles_ms": rep.tiles_ms, "finish_ms": rep.finish_ms}), out
 
 
 def render_film_black_and_white_tiled(image, options: FilmRenderOptions | None = None, engine=None):

@@ -261,6 +261,9 @@ typedef struct fg_film_report {  /* ImageProcessReport (src/image_pipeline.rs:10
   uint32_t in_w, in_h, out_w, out_h;
   uint64_t total_tiles, total_crystals, photons;
   double elapsed_seconds;
+  /* device time (CUDA events) of the image stages before the tiles (resize, gate, PSF), of the
+   * tile batches (gather, run, density copy) and of the finish (blend to u8, downscale) */
+  double prep_ms, tiles_ms, finish_ms;
 } fg_film_report;
 
 /* The reference's defaults (FilmRenderOptions::default, src/image_pipeline.rs:82-101). */
