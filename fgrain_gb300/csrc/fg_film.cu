@@ -20,9 +20,10 @@
 //   composite       k_grain                 image_pipeline.rs:725-808
 //   scanner OTF     k_otf_pass + k_film_out image_pipeline.rs:825-891 (with the output gates)
 //
-// The composite's powf and sinf are taken in FP64 and rounded once to FP32; the reference calls
-// the C library's single-precision functions, which may differ in the last place, so final
-// pixels may differ by one level where a value lies on a rounding boundary.
+// The composite calls CUDA's single-precision powf and sinf where the reference calls the C
+// library's; the two may differ in the last places, so final pixels may differ by one level where
+// a value lies on a rounding boundary.  (FP64 versions would cost the composite ten times more on
+// GB300's narrow FP64 pipe.)
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -69,10 +70,6 @@ __device__ __forceinline__ float gate_highlight(float v) {
   if (v >= 0.94f) return 0.0f;
   const float u = __fdiv_rn(__fsub_rn(v, 0.65f), __fsub_rn(0.94f, 0.65f));
   return __fsub_rn(1.0f, __fmul_rn(__fmul_rn(u, u), __fsub_rn(3.0f, __fmul_rn(2.0f, u))));
-}
-
-__device__ __forceinline__ float powf_cr(float x, float y) {
-  return static_cast<float>(pow(static_cast<double>(x), static_cast<double>(y)));
 }
 
 __global__ void k_luma(const uint8_t* __restrict__ rgb, size_t n, float rw, float gw, float bw,
@@ -264,11 +261,25 @@ __global__ void k_copy_tiles(const CopyTile* __restrict__ tiles) {
     t.dst[i] = t.src[i];
 }
 
+// Hann weights along one axis, once per image: tab[3 g + 1 + d] is the weight at coordinate g of
+// the tile in grid column (or row) g / step + d, d in -1..1 (0 where there is no such tile).
+__global__ void k_hann_table(uint32_t n, uint32_t nt, uint32_t step, uint32_t pad, float* __restrict__ tab) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n) return;
+  const int c = static_cast<int>(g / step);
+  for (int d = -1; d <= 1; ++d) {
+    const int t = c + d;
+    tab[3 * g + 1 + d] = (t >= 0 && t < static_cast<int>(nt))
+                             ? hann_weight(static_cast<uint32_t>(t), g, nt, static_cast<uint32_t>(t) * step, step, pad)
+                             : 0.0f;
+  }
+}
+
 // Hann overlap blend with the weight sums (image_pipeline.rs:593-655): d_norm and the
 // equal-power grain scale min(1 / sqrt(max(sum w^2 / max(sum w, 1e-5)^2, 0.05)), 1.45).
 __global__ void k_blend_film(const FilmTile* __restrict__ tiles, uint32_t ntiles, uint32_t ntx, uint32_t nty,
-                             uint32_t step, uint32_t pad, uint32_t out_w, uint32_t out_h, float* __restrict__ d_norm,
-                             float* __restrict__ gscale) {
+                             uint32_t step, const float* __restrict__ hx, const float* __restrict__ hy,
+                             uint32_t out_w, uint32_t out_h, float* __restrict__ d_norm, float* __restrict__ gscale) {
   const size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x;
   if (i >= static_cast<size_t>(out_w) * out_h) return;
   const uint32_t gx = static_cast<uint32_t>(i % out_w), gy = static_cast<uint32_t>(i / out_w);
@@ -284,8 +295,8 @@ __global__ void k_blend_film(const FilmTile* __restrict__ tiles, uint32_t ntiles
       if (k >= ntiles) continue;
       const FilmTile T = tiles[k];
       if (gx < T.xs || gx >= T.xs + T.tw || gy < T.ys || gy >= T.ys + T.th) continue;
-      const float wy = hann_weight(T.ty, gy, nty, T.ty * step, step, pad);
-      const float wx = hann_weight(T.tx, gx, ntx, T.tx * step, step, pad);
+      const float wy = hy[3 * gy + 1 + dy];
+      const float wx = hx[3 * gx + 1 + dx];
       const float wv = __fmul_rn(wx, wy);
       const float v = T.d[static_cast<size_t>(gy - T.ys) * T.tw + (gx - T.xs)];
       acc = __fadd_rn(acc, __fmul_rn(v, wv));
@@ -385,16 +396,15 @@ __global__ void k_grain(const uint8_t* __restrict__ src, const float* __restrict
   const float raw = __fdiv_rn(static_cast<float>(src[i]), 255.0f);
   const float base = raw <= 0.005f ? 0.0f : __fadd_rn(__fmul_rn(0.35f, raw), __fmul_rn(0.65f, heff[i]));
   const float mid =
-      fmaxf(static_cast<float>(sin(static_cast<double>(__fmul_rn(pi, powf_cr(fminf(fmaxf(base, 0.0f), 1.0f), 0.72f))))),
-            0.0f);
+      fmaxf(sinf(__fmul_rn(pi, powf(fminf(fmaxf(base, 0.0f), 1.0f), 0.72f))), 0.0f);
   const float vis = __fmul_rn(__fmul_rn(gate_shadow(base), gate_highlight(base)), mid);
   float tv = base;
   if (pushed) {
-    tv = base <= 0.5f ? __fmul_rn(0.5f, powf_cr(__fmul_rn(2.0f, base), gamma))
-                      : __fsub_rn(1.0f, __fmul_rn(0.5f, powf_cr(__fmul_rn(2.0f, __fsub_rn(1.0f, base)), gamma)));
+    tv = base <= 0.5f ? __fmul_rn(0.5f, powf(__fmul_rn(2.0f, base), gamma))
+                      : __fsub_rn(1.0f, __fmul_rn(0.5f, powf(__fmul_rn(2.0f, __fsub_rn(1.0f, base)), gamma)));
   }
   const float dd = __fsub_rn(__fsub_rn(dn[i], dl[i]), mean);
-  const float sharp = fabsf(dd) > 1e-6f ? copysignf(powf_cr(fabsf(dd), 0.85f), dd) : 0.0f;
+  const float sharp = fabsf(dd) > 1e-6f ? copysignf(powf(fabsf(dd), 0.85f), dd) : 0.0f;
   grain[i] = __fmul_rn(__fmul_rn(__fmul_rn(sharp, norm), gs[i]), vis);
   tone[i] = tv;
 }
@@ -560,7 +570,10 @@ void launch_finish(const FinishArgs& a, uint32_t out_w, uint32_t out_h, const Gr
   FG_CUDA(cudaMemsetAsync(S, 0, 4 * sizeof(float), st));
   FG_CUDA(cudaMemcpyAsync(dk.p, kern.data(), kern.size() * sizeof(float), cudaMemcpyHostToDevice, st));
   const unsigned G = grid_for(n, 256);
-  k_blend_film<<<G, 256, 0, st>>>(dft.p, ntiles, g.ntx, g.nty, g.step, g.pad, out_w, out_h, dn, gsc.p);
+  DBuf<float> hx(3 * static_cast<size_t>(out_w), st), hy(3 * static_cast<size_t>(out_h), st);
+  k_hann_table<<<grid_for(out_w, 256), 256, 0, st>>>(out_w, g.ntx, g.step, g.pad, hx.p);
+  k_hann_table<<<grid_for(out_h, 256), 256, 0, st>>>(out_h, g.nty, g.step, g.pad, hy.p);
+  k_blend_film<<<G, 256, 0, st>>>(dft.p, ntiles, g.ntx, g.nty, g.step, hx.p, hy.p, out_w, out_h, dn, gsc.p);
   k_gauss_pass<<<G, 256, 0, st>>>(dn, out_w, out_h, dk.p, krad, 0, tmp.p);
   k_gauss_pass<<<G, 256, 0, st>>>(tmp.p, out_w, out_h, dk.p, krad, 1, dl);
   const int nb = static_cast<int>(std::min<size_t>(STAT_BLOCKS, std::max<size_t>(grid_for(n, STAT_THREADS), 1)));
