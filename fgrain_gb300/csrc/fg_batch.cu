@@ -292,8 +292,12 @@ __device__ __forceinline__ void uf_unite_b(int* parent, int a, int b, uint32_t* 
   atomicOr(err, ERR_SPIN_LIMIT);
 }
 
+// Links each developed crystal to the developed crystals it touches (union-find), walking the
+// four-wide tree with the query box: a leaf is reached iff its box and its ancestors' boxes overlap
+// the query, as in the binary walk (ancestor boxes contain their descendants'), and the union-find
+// roots do not depend on the order of the unions.
 __global__ void k_link_b(const BTile* __restrict__ bt, int ntiles, unsigned long long ncap,
-                         const float4* __restrict__ A, const float4* __restrict__ D, const Node* __restrict__ nodes_all,
+                         const float4* __restrict__ A, const float4* __restrict__ D, const Node4* __restrict__ nodes_all,
                          const uint8_t* __restrict__ developed, int* parent, const uint32_t* __restrict__ list,
                          const uint32_t* __restrict__ ndev, uint32_t* err) {
   const unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
@@ -301,7 +305,7 @@ __global__ void k_link_b(const BTile* __restrict__ bt, int ntiles, unsigned long
   const unsigned long long g = list[i];
   const BTile& t = bt[btile_of(bt, ntiles, g)];
   const uint32_t s = static_cast<uint32_t>(g - t.cbase);
-  const Node* nodes = nodes_all + t.cbase;
+  const Node4* nodes = nodes_all + t.cbase;
   const float4* Ab = A + t.cbase;
   const float4* Db = D + t.cbase;
   const uint8_t* dev = developed + t.cbase;
@@ -314,51 +318,59 @@ __global__ void k_link_b(const BTile* __restrict__ bt, int ntiles, unsigned long
   const float3 lo = make_float3(a.x - R, a.y - R, a.z - R), hi = make_float3(a.x + R, a.y + R, a.z + R);
   const float fef = static_cast<float>(t.fe), proxf = static_cast<float>(t.prox);
   const float rcf = fmaxf(fmaxf(d.x, d.y), d.z) * fef;
+  if (t.n < 2) return;
+  const int nint = static_cast<int>(t.n) - 1;
+  auto leaf = [&](uint32_t j) {
+    if (j <= s || j >= t.n || !dev[j]) return;
+    const float4 aj = Ab[j], dj = Db[j];
+    const float dx = aj.x - a.x, dy = aj.y - a.y, dz = aj.z - a.z;
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    const float touch = (rcf + fmaxf(fmaxf(dj.x, dj.y), dj.z) * fef) * proxf;
+    const float t2 = touch * touch;
+    const float margin = 1e-5f * t2 + 1e-6f;
+    bool hit;
+    if (d2 < t2 - margin) {
+      hit = true;
+    } else if (d2 > t2 + margin) {
+      hit = false;
+    } else {
+      const double rn = __dmul_rn(static_cast<double>(fmaxf(fmaxf(dj.x, dj.y), dj.z)), t.fe);
+      const double tt = __dmul_rn(__dadd_rn(rc, rn), t.prox);
+      const double ex = __dsub_rn(static_cast<double>(aj.x), static_cast<double>(a.x));
+      const double ey = __dsub_rn(static_cast<double>(aj.y), static_cast<double>(a.y));
+      const double ez = __dsub_rn(static_cast<double>(aj.z), static_cast<double>(a.z));
+      hit = __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez)) <= __dmul_rn(tt, tt);
+    }
+    if (hit) uf_unite_b(parent, static_cast<int>(g), static_cast<int>(t.cbase + j), err);
+  };
   int stack[64];
   int sp = 0, cur = 0;
-  if (t.n < 2) return;
   for (;;) {
-    const float4 na = __ldg(&nodes[cur].a), nb = __ldg(&nodes[cur].b), nc = __ldg(&nodes[cur].c);
-    const int4 nd = __ldg(&nodes[cur].d);
-    bool hl = na.x <= hi.x && na.w >= lo.x && na.y <= hi.y && nb.x >= lo.y && na.z <= hi.z && nb.y >= lo.z;
-    bool hr = nb.z <= hi.x && nc.y >= lo.x && nb.w <= hi.y && nc.z >= lo.y && nc.x <= hi.z && nc.w >= lo.z &&
-              nd.y != INT32_MIN;
-    for (int side = 0; side < 2; ++side) {
-      const bool h = side == 0 ? hl : hr;
-      const int c = side == 0 ? nd.x : nd.y;
-      if (!h || c >= 0) continue;
-      const uint32_t j = static_cast<uint32_t>(~c);
-      if (j <= s || !dev[j]) continue;
-      const float4 aj = Ab[j], dj = Db[j];
-      const float dx = aj.x - a.x, dy = aj.y - a.y, dz = aj.z - a.z;
-      const float d2 = dx * dx + dy * dy + dz * dz;
-      const float touch = (rcf + fmaxf(fmaxf(dj.x, dj.y), dj.z) * fef) * proxf;
-      const float t2 = touch * touch;
-      const float margin = 1e-5f * t2 + 1e-6f;
-      bool hit;
-      if (d2 < t2 - margin) {
-        hit = true;
-      } else if (d2 > t2 + margin) {
-        hit = false;
+    if (!index_ok(cur >= 0 && cur < nint, err, SITE_NODE, static_cast<uint32_t>(cur), t.n)) break;
+    const Node4* nd = nodes + cur;
+    const float4 lx = __ldg(&nd->lox), ly = __ldg(&nd->loy), lz = __ldg(&nd->loz);
+    const float4 hx = __ldg(&nd->hix), hy = __ldg(&nd->hiy), hz = __ldg(&nd->hiz);
+    const int4 rf = __ldg(&nd->ref);
+    int next = -1;
+    auto child = [&](float a0, float a1, float a2, float a3, float a4, float a5, int r) {
+      if (r == INT32_MIN) return;
+      if (!(a0 <= hi.x && a3 >= lo.x && a1 <= hi.y && a4 >= lo.y && a2 <= hi.z && a5 >= lo.z)) return;
+      if (r < 0) {
+        leaf(static_cast<uint32_t>(~r));
+      } else if (next < 0) {
+        next = r;
+      } else if (sp < 64) {
+        stack[sp++] = r;
       } else {
-        const double rn = __dmul_rn(static_cast<double>(fmaxf(fmaxf(dj.x, dj.y), dj.z)), t.fe);
-        const double tt = __dmul_rn(__dadd_rn(rc, rn), t.prox);
-        const double ex = __dsub_rn(static_cast<double>(aj.x), static_cast<double>(a.x));
-        const double ey = __dsub_rn(static_cast<double>(aj.y), static_cast<double>(a.y));
-        const double ez = __dsub_rn(static_cast<double>(aj.z), static_cast<double>(a.z));
-        hit = __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez)) <= __dmul_rn(tt, tt);
+        atomicOr(err, ERR_STACK_OVERFLOW);
       }
-      if (hit) uf_unite_b(parent, static_cast<int>(g), static_cast<int>(t.cbase + j), err);
-    }
-    if (hl && nd.x < 0) hl = false;
-    if (hr && nd.y < 0) hr = false;
-    if (hl && hr) {
-      if (sp < 64) stack[sp++] = nd.y; else atomicOr(err, ERR_STACK_OVERFLOW);
-      cur = nd.x;
-    } else if (hl) {
-      cur = nd.x;
-    } else if (hr) {
-      cur = nd.y;
+    };
+    child(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, rf.x);
+    child(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, rf.y);
+    child(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, rf.z);
+    child(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, rf.w);
+    if (next >= 0) {
+      cur = next;
     } else {
       if (sp == 0) break;
       cur = stack[--sp];
@@ -698,7 +710,7 @@ static void stage_develop(fg_batch* B, cudaStream_t st) {
   FG_CUDA(cudaMemsetAsync(B->devflag.p + B->ncap, 0, sizeof(uint32_t), st));
   cub_scan(B, B->devflag.p, B->devscan.p, B->ncap + 1, st);
   k_devlist_b<<<G, 256, 0, st>>>(B->ncap, B->devflag.p, B->devscan.p, B->devlist.p);
-  k_link_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->A.p, B->D.p, B->nodes.p, B->developed.p, B->parent.p,
+  k_link_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->A.p, B->D.p, B->nodes4.p, B->developed.p, B->parent.p,
                               B->devlist.p, B->devscan.p + B->ncap, e->d_err);
   FG_CUDA(cudaMemsetAsync(B->size.p, 0, B->ncap * sizeof(uint32_t), st));
   k_roots_b<<<G, 256, 0, st>>>(B->ncap, B->developed.p, B->parent.p, B->size.p, e->d_err);
