@@ -404,7 +404,8 @@ __global__ void __launch_bounds__(SCAN_THREADS, 4) k_scan(const ScanTile* __rest
   }
   float T = 1.0f;
   if (active) {
-    const float L = (float)((double)Lfix * 9.094947017729282e-13);
+    // Lfix * 2^-40 rounded once to float (the conversion rounds, the power-of-two scale is exact).
+    const float L = __ll2float_rn(Lfix) * 0x1p-40f;
     T = per_crystal ? expf(-L) : expf(-t.sigma * L);
     if (t.ray_hits) t.ray_hits[(static_cast<size_t>(py) * t.w + px) * a + st] = static_cast<uint16_t>(min(nh, 65535u));
   }
@@ -414,7 +415,9 @@ __global__ void __launch_bounds__(SCAN_THREADS, 4) k_scan(const ScanTile* __rest
     // FP64 mean over strata in the reference's order (sy, sx), then f32 (transmittance.rs:142).
     double acc = 0.0;
     for (uint32_t k = 0; k < a; ++k) acc = __dadd_rn(acc, sm.T[tid + k]);
-    const float mean = (float)__ddiv_rn(acc, (double)a);
+    // Division by a power of two is the multiplication by its exact reciprocal.
+    const float mean = (float)((a & (a - 1)) == 0 ? __dmul_rn(acc, 1.0 / static_cast<double>(a))
+                                                   : __ddiv_rn(acc, static_cast<double>(a)));
     const size_t idx = static_cast<size_t>(py) * t.w + px;
     float v;
     if (t.mode == 0) {
@@ -480,7 +483,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_adjoint(const ScanTile* _
   }
   float coef = 0.0f;
   if (R.active) {
-    const float L = (float)((double)Lfix * 9.094947017729282e-13);
+    const float L = __ll2float_rn(Lfix) * 0x1p-40f;  // rounded once, as in k_scan
     const float T = per_crystal ? expf(-L) : expf(-t.sigma * L);
     coef = wpx[static_cast<size_t>(R.py) * t.w + R.px] / static_cast<float>(a) * T;
   }
