@@ -24,11 +24,11 @@
 namespace fg {
 
 void launch_bridson(const SynthTile* tiles, int ntiles, int color, unsigned ncols, int gdmax, uint32_t* cells,
-                    uint32_t* err, cudaStream_t st);
+                    uint32_t* npts, uint32_t* err, cudaStream_t st);
 size_t bridson_smem(int gdmax);
-void launch_synth_post(const SynthTile* tiles, int ntiles, unsigned long long ncells, unsigned long long nslots,
+void launch_synth_post(const SynthTile* tiles, int ntiles, unsigned long long max_cells, unsigned long long max_slots,
                        uint32_t* cells, uint32_t* npts, uint32_t* flags, cudaStream_t st);
-void launch_emit(const SynthTile* tiles, int ntiles, unsigned long long nslots, const uint32_t* cells,
+void launch_emit(const SynthTile* tiles, int ntiles, unsigned long long max_slots, const uint32_t* cells,
                  const uint32_t* scan, float4* A, float4* Q, float4* D, uint64_t* keys, uint32_t* err,
                  cudaStream_t st);
 void launch_transport_shape(const TileDesc* tiles_dev, int ntiles, unsigned long long total,
@@ -454,6 +454,7 @@ struct fg_batch {
   DBuf<ScanTile> d_sc;
   DBuf<BTile> d_bt;
   DBuf<uint32_t> cells, npts, flags, slot_scan, ncrys;
+  unsigned long long maxcells = 0, maxslots = 0;  // the largest tile's cells and Morton slots
   DBuf<float4> A, Q, D;
   DBuf<uint64_t> keys;
   DBuf<Node> nodes;
@@ -508,6 +509,7 @@ static void derive_tile(const fg_tile_params& p, SynthTile& s, TileDesc& t, Scan
   s.gh = static_cast<uint32_t>(std::ceil(H / cell));
   s.gd = static_cast<uint32_t>(std::ceil(Dd / cell));
   FG_REQUIRE(s.gw <= 16000 && s.gh <= 16000 && s.gd <= 100, "tile too large for the synthesis grid");
+  FG_REQUIRE(static_cast<unsigned long long>(s.gw) * s.gh * s.gd < (1ull << 31), "tile too large for the synthesis grid");
   s.nbx = (s.gw + SYN_B - 1) / SYN_B;
   s.nby = (s.gh + SYN_B - 1) / SYN_B;
   s.XW = static_cast<uint32_t>(std::ceil(W * SYN_Q / cell));
@@ -663,11 +665,13 @@ static void stage_synth(fg_batch* B, cudaStream_t st) {
   FG_CUDA(cudaMemsetAsync(B->dstats.p, 0, 4 * sizeof(unsigned long long), st));
   FG_CUDA(cudaMemsetAsync(B->cells.p, 0, B->ncells * sizeof(uint32_t), st));
   FG_CUDA(cudaMemsetAsync(B->npts.p, 0, B->ntiles * sizeof(uint32_t), st));
-  for (int c = 0; c < 4; ++c) launch_bridson(B->d_syn.p, nt, c, B->cols[c], B->gdmax, B->cells.p, e->d_err, st);
+  for (int c = 0; c < 4; ++c)
+    launch_bridson(B->d_syn.p, nt, c, B->cols[c], B->gdmax, B->cells.p, B->npts.p, e->d_err, st);
   FG_CUDA(cudaMemsetAsync(B->flags.p + B->nslots, 0, sizeof(uint32_t), st));
-  launch_synth_post(B->d_syn.p, nt, B->ncells, B->nslots, B->cells.p, B->npts.p, B->flags.p, st);
+  launch_synth_post(B->d_syn.p, nt, B->maxcells, B->maxslots, B->cells.p, B->npts.p, B->flags.p, st);
   cub_scan(B, B->flags.p, B->slot_scan.p, B->nslots + 1, st);
-  launch_emit(B->d_syn.p, nt, B->nslots, B->cells.p, B->slot_scan.p, B->A.p, B->Q.p, B->D.p, B->keys.p, e->d_err, st);
+  launch_emit(B->d_syn.p, nt, B->maxslots, B->cells.p, B->slot_scan.p, B->A.p, B->Q.p, B->D.p, B->keys.p, e->d_err,
+              st);
   k_set_n<<<grid_for(B->ntiles, 128), 128, 0, st>>>(B->d_syn.p, nt, B->slot_scan.p, B->d_bt.p, B->d_td.p, B->d_sc.p,
                                                     B->ncrys.p);
   FG_CUDA(cudaGetLastError());
@@ -838,6 +842,8 @@ static void plan(fg_batch* B, const fg_batch_options* opt) {
     }
     cb += static_cast<unsigned long long>(s.gw) * s.gh * s.gd;
     sb += s.slots;
+    B->maxcells = std::max<unsigned long long>(B->maxcells, static_cast<unsigned long long>(s.gw) * s.gh * s.gd);
+    B->maxslots = std::max<unsigned long long>(B->maxslots, s.slots);
     cap += s.ccap;
     B->td[i].photon_base = pb;
     pb += B->td[i].P;
@@ -1012,7 +1018,7 @@ fg_status fg_emulsion_synthesize(fg_engine* e, const fg_emulsion_cfg* cfg, uint6
     DBuf<uint64_t> keys(s.ccap, st);
     FG_CUDA(cudaMemsetAsync(cells.p, 0, ncells * sizeof(uint32_t), st));
     FG_CUDA(cudaMemsetAsync(npts.p, 0, sizeof(uint32_t), st));
-    for (int c = 0; c < 4; ++c) launch_bridson(d_syn.p, 1, c, cols[c], gdmax, cells.p, e->d_err, st);
+    for (int c = 0; c < 4; ++c) launch_bridson(d_syn.p, 1, c, cols[c], gdmax, cells.p, npts.p, e->d_err, st);
     FG_CUDA(cudaMemsetAsync(flags.p + s.slots, 0, sizeof(uint32_t), st));
     launch_synth_post(d_syn.p, 1, ncells, s.slots, cells.p, npts.p, flags.p, st);
     exclusive_scan_u32(flags.p, scan.p, s.slots + 1ull, st);
@@ -1200,10 +1206,10 @@ fg_status fg_batch_wait(fg_batch* b, fg_batch_stats* stats) {
     s.transport_blocks = b->tr_blocks;
     s.scan_bin_px = b->bin_px;
     s.graph = b->exec ? 1u : 0u;
-    // Own kernels per run: Bridson x4, count + thin + flags, emit, set_n, Karras + fit + four-wide collapse,
-    // photon order x2, transport, maxdim + threshold + developed list + link + roots + finalize, scan prep,
-    // two bin passes, scan (CUB scans not counted).
-    s.kernel_launches = 4 + 3 + 1 + 1 + 3 + 2 + 1 + 6 + 1 + 2 + 1;
+    // Own kernels per run: Bridson x4 (which also count the points), thin + flags, emit, set_n, Karras + fit +
+    // four-wide collapse, photon order x2, transport, maxdim + threshold + developed list + link + roots +
+    // finalize, scan prep, two bin passes, scan (CUB scans not counted).
+    s.kernel_launches = 4 + 2 + 1 + 1 + 3 + 2 + 1 + 6 + 1 + 2 + 1;
     b->stats = s;
     if (stats) *stats = s;
   });

@@ -1,5 +1,7 @@
 // Device crystal synthesis: column-parallel Bridson, thinning to the reference density, Morton
 // compaction and crystal attributes.  See fg_synth.cuh for the scheme.
+#include <algorithm>
+
 #include "fg_internal.h"
 #include "fg_synth.cuh"
 
@@ -134,11 +136,12 @@ __device__ __forceinline__ uint32_t syn_word(int X, int Y, int Z) {
 __global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* __restrict__ tiles,
                                                             int ntiles, int color, int nz,
                                                             uint32_t* __restrict__ cells,
-                                                            uint32_t* err) {
+                                                            uint32_t* __restrict__ npts, uint32_t* err) {
   extern __shared__ uint32_t syn_sm[];
   uint32_t* grid = syn_sm;                                   // SYN_R^2 * nz cell words
   uint16_t* active = reinterpret_cast<uint16_t*>(grid + SYN_R * SYN_R * nz);  // SYN_B^2 * (nz - 4)
   __shared__ int s_nact, s_wsum[SYN_WARPS];
+  __shared__ int s_ncom;  // points this column commits (each fills one empty cell of its tile)
   __shared__ int s_pick[SYN_WARPS];
   __shared__ unsigned s_vmask[SYN_WARPS];
   __shared__ int s_cx[SYN_WARPS][32], s_cy[SYN_WARPS][32], s_cz[SYN_WARPS][32];  // valid candidates
@@ -176,6 +179,7 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* 
   }
   if (tid == 0) {
     s_nact = 0;
+    s_ncom = 0;
     syn_outer_table(s_outer);
   }
   __syncthreads();
@@ -215,6 +219,7 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* 
       if (!syn_free(grid, nz, rx, ry, rz, X, Y, Z, cx, cy, cz, err)) continue;
       const int ridx = (rz * SYN_R + ry) * SYN_R + rx;
       grid[ridx] = syn_word(X, Y, Z);
+      ++s_ncom;
       if (index_ok(s_nact < acap, err, SITE_SYN_ACTIVE, s_nact, blockIdx.x)) active[s_nact++] = static_cast<uint16_t>(ridx);
       break;
     }
@@ -230,12 +235,10 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* 
     }
     // One Bridson step per warp on a random active point (poisson.rs:59-129): 30 candidates in
     // the shell [r, 2r], one per lane; the lowest valid lane is the step's winner.
-    if (lane == 0) {
-      const P4 r = philox(static_cast<uint32_t>(iter), static_cast<uint32_t>(warp), colkey, TAG_PICK, t.k0, t.k1);
-      s_pick[warp] = static_cast<int>((static_cast<unsigned long long>(r.x) * static_cast<unsigned>(nact)) >> 32);
-    }
-    __syncwarp();
-    const int pick = s_pick[warp];
+    // Every lane draws the pick (no shared-memory round trip); lane 0 records it for the retirement.
+    const P4 rp = philox(static_cast<uint32_t>(iter), static_cast<uint32_t>(warp), colkey, TAG_PICK, t.k0, t.k1);
+    const int pick = static_cast<int>((static_cast<unsigned long long>(rp.x) * static_cast<unsigned>(nact)) >> 32);
+    if (lane == 0) s_pick[warp] = pick;
     const int pr = active[pick];
     const uint32_t pw = grid[pr];
     const int prx = pr % SYN_R, pry = (pr / SYN_R) % SYN_R, prz = pr / (SYN_R * SYN_R);
@@ -328,7 +331,7 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* 
         acc |= 1u << w;
       }
       // Commit the accepted winners, appending to the active list in warp order.
-      bool inside = false;
+      bool inside = false, committed = false;
       int cridx = 0;
       if (lane < SYN_WARPS && ((acc >> lane) & 1u)) {
         const int slot = __popc(acc & ((1u << lane) - 1u));
@@ -341,6 +344,7 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* 
                      static_cast<uint32_t>(rx | (ry << 8) | (rz << 16)), blockIdx.x)) {
           cridx = (rz * SYN_R + ry) * SYN_R + rx;
           grid[cridx] = syn_word(WX, WY, WZ);
+          committed = true;
           inside = ccx >= x0 && ccx < x1 && ccy >= y0 && ccy < y1;
         }
       }
@@ -350,8 +354,12 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* 
         const int pos = nbase + __popc(im & ((1u << lane) - 1u));
         if (index_ok(pos < acap, err, SITE_SYN_ACTIVE, pos, blockIdx.x)) active[pos] = static_cast<uint16_t>(cridx);
       }
+      const unsigned cmm = __ballot_sync(0xffffffffu, committed);
       __syncwarp();
-      if (lane == 0) s_nact = min(nbase + __popc(im), acap);
+      if (lane == 0) {
+        s_nact = min(nbase + __popc(im), acap);
+        s_ncom += __popc(cmm);
+      }
       __syncwarp();
       // Serial path from the first conflicting warp on.  One lane per candidate.
       int ncom = __popc(acc);
@@ -387,6 +395,7 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* 
                        static_cast<uint32_t>(rx | (ry << 8) | (rz << 16)), blockIdx.x)) {
             const int ridx = (rz * SYN_R + ry) * SYN_R + rx;
             grid[ridx] = syn_word(X, Y, Z);
+            ++s_ncom;
             if (ccx >= x0 && ccx < x1 && ccy >= y0 && ccy < y1 &&
                 index_ok(s_nact < acap, err, SITE_SYN_ACTIVE, s_nact, blockIdx.x))
               active[s_nact++] = static_cast<uint16_t>(ridx);
@@ -427,108 +436,96 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* 
     if (gx >= 0 && gy >= 0 && gz >= 0 && gx < static_cast<int>(t.gw) && gy < static_cast<int>(t.gh) && gz < gd)
       tc[(static_cast<size_t>(gz) * t.gh + gy) * t.gw + gx] = grid[i];
   }
-}
-
-// Points per tile.
-__global__ void k_count_points(const SynthTile* __restrict__ tiles, int ntiles, unsigned long long ncells,
-                               const uint32_t* __restrict__ cells, uint32_t* npts) {
-  const unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
-  const bool occ = i < ncells && (cells[i] & OCC);
-  const unsigned act = __activemask();
-  int tile = -1;
-  if (occ) tile = find_tile_ull(tiles, ntiles, i, 0);
-  const unsigned grp = __match_any_sync(act, tile);
-  if (occ && (threadIdx.x & 31) == static_cast<unsigned>(__ffs(grp) - 1)) atomicAdd(&npts[tile], __popc(grp));
+  if (tid == 0 && s_ncom) atomicAdd(npts + lo, static_cast<uint32_t>(s_ncom));
 }
 
 // Independent deletion down to the Bridson-expected count.
-__global__ void k_thin(const SynthTile* __restrict__ tiles, int ntiles, unsigned long long ncells,
-                       uint32_t* __restrict__ cells, const uint32_t* npts) {
-  const unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
-  if (i >= ncells || !(cells[i] & OCC)) return;
-  const int tile = find_tile_ull(tiles, ntiles, i, 0);
-  const SynthTile& t = tiles[tile];
-  const uint32_t n = npts[tile];
+// blockIdx.y is the tile (the points per tile were counted by k_bridson).
+__global__ void k_thin(const SynthTile* __restrict__ tiles, uint32_t* __restrict__ cells, const uint32_t* npts) {
+  const SynthTile& t = tiles[blockIdx.y];
+  const uint32_t n = npts[blockIdx.y];
   if (n <= t.target) return;
   const float p = 1.0f - static_cast<float>(t.target) / static_cast<float>(n);
-  const uint32_t lin = static_cast<uint32_t>(i - t.cell_base);
-  if (uf(philox(lin, 0, 0, TAG_THIN, t.k0, t.k1).x) < p) cells[i] = 0;
+  const uint32_t nc = t.gw * t.gh * t.gd;
+  uint32_t* tc = cells + t.cell_base;
+  for (uint32_t lin = blockIdx.x * blockDim.x + threadIdx.x; lin < nc; lin += gridDim.x * blockDim.x)
+    if ((tc[lin] & OCC) && uf(philox(lin, 0, 0, TAG_THIN, t.k0, t.k1).x) < p) tc[lin] = 0;
 }
 
 // Occupancy of each compaction slot: slot = morton2(x, y) * gd + z.
-__global__ void k_slot_flags(const SynthTile* __restrict__ tiles, int ntiles, unsigned long long nslots,
-                             const uint32_t* __restrict__ cells, uint32_t* flags) {
-  const unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
-  if (i >= nslots) return;
-  const SynthTile& t = tiles[find_tile_ull(tiles, ntiles, i, 1)];
-  const uint32_t sl = static_cast<uint32_t>(i - t.slot_base);
-  uint32_t f = 0;
-  if (sl < t.slots) {
+// blockIdx.y is the tile.
+__global__ void k_slot_flags(const SynthTile* __restrict__ tiles, const uint32_t* __restrict__ cells,
+                             uint32_t* flags) {
+  const SynthTile& t = tiles[blockIdx.y];
+  const uint32_t* tc = cells + t.cell_base;
+  for (uint32_t sl = blockIdx.x * blockDim.x + threadIdx.x; sl < t.slots; sl += gridDim.x * blockDim.x) {
     const uint32_t m2 = sl / t.gd, z = sl % t.gd;
     const uint32_t x = morton2_compact(m2), y = morton2_compact(m2 >> 1);
-    if (x < t.gw && y < t.gh) f = (cells[t.cell_base + (static_cast<size_t>(z) * t.gh + y) * t.gw + x] & OCC) ? 1u : 0u;
+    uint32_t f = 0;
+    if (x < t.gw && y < t.gh) f = (tc[(static_cast<size_t>(z) * t.gh + y) * t.gw + x] & OCC) ? 1u : 0u;
+    flags[t.slot_base + sl] = f;
   }
-  flags[i] = f;
 }
 
 // Crystal k of a tile from its slot: position from the fixed-point cell word, attributes from the
 // tile's Philox stream keyed by the cell (emulsion.rs:162-200).
-__global__ void k_emit(const SynthTile* __restrict__ tiles, int ntiles, unsigned long long nslots,
-                       const uint32_t* __restrict__ cells, const uint32_t* __restrict__ scan,
-                       float4* A, float4* Q, float4* D, uint64_t* keys, uint32_t* err) {
-  const unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
-  if (i >= nslots) return;
-  const SynthTile& t = tiles[find_tile_ull(tiles, ntiles, i, 1)];
-  const uint32_t sl = static_cast<uint32_t>(i - t.slot_base);
-  if (sl >= t.slots || scan[i + 1] == scan[i]) return;
-  const uint32_t k = scan[i] - scan[t.slot_base];
-  if (k >= t.ccap) {
-    atomicOr(err, ERR_LIST_OVERFLOW);
-    return;
+// blockIdx.y is the tile.
+__global__ void k_emit(const SynthTile* __restrict__ tiles, const uint32_t* __restrict__ cells,
+                       const uint32_t* __restrict__ scan, float4* A, float4* Q, float4* D, uint64_t* keys,
+                       uint32_t* err) {
+  const SynthTile& t = tiles[blockIdx.y];
+  for (uint32_t sl = blockIdx.x * blockDim.x + threadIdx.x; sl < t.slots; sl += gridDim.x * blockDim.x) {
+    const unsigned long long i = t.slot_base + sl;
+    if (scan[i + 1] == scan[i]) continue;
+    const uint32_t k = scan[i] - scan[t.slot_base];
+    if (k >= t.ccap) {
+      atomicOr(err, ERR_LIST_OVERFLOW);
+      continue;
+    }
+    const uint32_t m2 = sl / t.gd, z = sl % t.gd;
+    const uint32_t x = morton2_compact(m2), y = morton2_compact(m2 >> 1);
+    const uint32_t lin = (z * t.gh + y) * t.gw + x;
+    const uint32_t w = cells[t.cell_base + lin];
+    const float px = static_cast<float>(static_cast<int>(x) * SYN_Q + static_cast<int>(w & 1023u)) * (t.cell / SYN_Q);
+    const float py = static_cast<float>(static_cast<int>(y) * SYN_Q + static_cast<int>((w >> 10) & 1023u)) * (t.cell / SYN_Q);
+    const float pz = static_cast<float>(static_cast<int>(z) * SYN_Q + static_cast<int>((w >> 20) & 1023u)) * (t.cell / SYN_Q);
+    const P4 r0 = philox(lin, 0, 0, TAG_ATTR, t.k0, t.k1);
+    const P4 r1 = philox(lin, 1, 0, TAG_ATTR, t.k0, t.k1);
+    // Two normals from one Box-Muller pair: radius (log-normal) and sensitivity.
+    const float bm = sqrtf(-2.0f * logf(1.0f - uf(r0.x)));
+    float s2, c2;
+    sincospif(2.0f * uf(r0.y), &s2, &c2);
+    const float radius = fminf(fmaxf(expf(t.mu + t.sg * bm * c2), 0.15f), t.rmax);
+    const float sens = fmaxf(t.base_sens + 0.15f * bm * s2, 0.1f);
+    float4 q, d;
+    if (t.morph == 1) {
+      // Tabular: thickness r / AR (>= 0.05), tilt +-0.17 rad about a random in-plane axis.
+      const float ht = fmaxf(radius / t.aspect, 0.05f);
+      const float tilt = uf(r0.z) * 0.34f - 0.17f;
+      float ax = uf(r0.w) * 2.0f - 1.0f, ay = uf(r1.x) * 2.0f - 1.0f;
+      const float n = rsqrtf(fmaxf(ax * ax + ay * ay, 1e-30f));
+      ax *= n;
+      ay *= n;
+      float sh, ch;
+      sincosf(0.5f * tilt, &sh, &ch);
+      q = make_float4(ax * sh, ay * sh, 0.0f, ch);
+      d = make_float4(radius, radius, ht, __int_as_float(1));
+    } else {
+      // Cubic / octahedral: UnitQuaternion::from_euler_angles(2 pi u1, pi u2, 2 pi u3).
+      float sr, cr, sp, cp, sy, cy;
+      sincospif(uf(r0.z), &sr, &cr);        // roll / 2 = pi u1
+      sincospif(0.5f * uf(r0.w), &sp, &cp); // pitch / 2 = pi u2 / 2
+      sincospif(uf(r1.x), &sy, &cy);        // yaw / 2 = pi u3
+      q = make_float4(sr * cp * cy - cr * sp * sy, cr * sp * cy + sr * cp * sy, cr * cp * sy - sr * sp * cy,
+                      cr * cp * cy + sr * sp * sy);
+      d = make_float4(radius, radius, radius, __int_as_float(t.morph));
+    }
+    const unsigned long long o = t.cbase + k;
+    A[o] = make_float4(px, py, pz, sens);
+    Q[o] = q;
+    D[o] = d;
+    keys[o] = sl;
   }
-  const uint32_t m2 = sl / t.gd, z = sl % t.gd;
-  const uint32_t x = morton2_compact(m2), y = morton2_compact(m2 >> 1);
-  const uint32_t lin = (z * t.gh + y) * t.gw + x;
-  const uint32_t w = cells[t.cell_base + lin];
-  const float px = static_cast<float>(static_cast<int>(x) * SYN_Q + static_cast<int>(w & 1023u)) * (t.cell / SYN_Q);
-  const float py = static_cast<float>(static_cast<int>(y) * SYN_Q + static_cast<int>((w >> 10) & 1023u)) * (t.cell / SYN_Q);
-  const float pz = static_cast<float>(static_cast<int>(z) * SYN_Q + static_cast<int>((w >> 20) & 1023u)) * (t.cell / SYN_Q);
-  const P4 r0 = philox(lin, 0, 0, TAG_ATTR, t.k0, t.k1);
-  const P4 r1 = philox(lin, 1, 0, TAG_ATTR, t.k0, t.k1);
-  // Two normals from one Box-Muller pair: radius (log-normal) and sensitivity.
-  const float bm = sqrtf(-2.0f * logf(1.0f - uf(r0.x)));
-  float s2, c2;
-  sincospif(2.0f * uf(r0.y), &s2, &c2);
-  const float radius = fminf(fmaxf(expf(t.mu + t.sg * bm * c2), 0.15f), t.rmax);
-  const float sens = fmaxf(t.base_sens + 0.15f * bm * s2, 0.1f);
-  float4 q, d;
-  if (t.morph == 1) {
-    // Tabular: thickness r / AR (>= 0.05), tilt +-0.17 rad about a random in-plane axis.
-    const float ht = fmaxf(radius / t.aspect, 0.05f);
-    const float tilt = uf(r0.z) * 0.34f - 0.17f;
-    float ax = uf(r0.w) * 2.0f - 1.0f, ay = uf(r1.x) * 2.0f - 1.0f;
-    const float n = rsqrtf(fmaxf(ax * ax + ay * ay, 1e-30f));
-    ax *= n;
-    ay *= n;
-    float sh, ch;
-    sincosf(0.5f * tilt, &sh, &ch);
-    q = make_float4(ax * sh, ay * sh, 0.0f, ch);
-    d = make_float4(radius, radius, ht, __int_as_float(1));
-  } else {
-    // Cubic / octahedral: UnitQuaternion::from_euler_angles(2 pi u1, pi u2, 2 pi u3).
-    float sr, cr, sp, cp, sy, cy;
-    sincospif(uf(r0.z), &sr, &cr);        // roll / 2 = pi u1
-    sincospif(0.5f * uf(r0.w), &sp, &cp); // pitch / 2 = pi u2 / 2
-    sincospif(uf(r1.x), &sy, &cy);        // yaw / 2 = pi u3
-    q = make_float4(sr * cp * cy - cr * sp * sy, cr * sp * cy + sr * cp * sy, cr * cp * sy - sr * sp * cy,
-                    cr * cp * cy + sr * sp * sy);
-    d = make_float4(radius, radius, radius, __int_as_float(t.morph));
-  }
-  const unsigned long long o = t.cbase + k;
-  A[o] = make_float4(px, py, pz, sens);
-  Q[o] = q;
-  D[o] = d;
-  keys[o] = sl;
 }
 
 }  // namespace fg
@@ -539,12 +536,12 @@ size_t bridson_smem(int gdmax);
 
 // Host wrappers (launch on `st`; all buffers preallocated so the sequence can be graph-captured).
 void launch_bridson(const SynthTile* tiles, int ntiles, int color, unsigned ncols, int gdmax,
-                    uint32_t* cells, uint32_t* err, cudaStream_t st) {
+                    uint32_t* cells, uint32_t* npts, uint32_t* err, cudaStream_t st) {
   if (ncols == 0) return;
   const int nz = gdmax + 4;
   const size_t smem = bridson_smem(gdmax);
   FG_CUDA(cudaFuncSetAttribute(k_bridson, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-  k_bridson<<<ncols, SYN_WARPS * 32, smem, st>>>(tiles, ntiles, color, nz, cells, err);
+  k_bridson<<<ncols, SYN_WARPS * 32, smem, st>>>(tiles, ntiles, color, nz, cells, npts, err);
   FG_CUDA(cudaGetLastError());
 }
 
@@ -553,18 +550,25 @@ size_t bridson_smem(int gdmax) {
          static_cast<size_t>(SYN_B) * SYN_B * gdmax * sizeof(uint16_t);
 }
 
-void launch_synth_post(const SynthTile* tiles, int ntiles, unsigned long long ncells, unsigned long long nslots,
+// Per-tile grids (blockIdx.y is the tile): max_cells and max_slots are the largest tile's.
+void launch_synth_post(const SynthTile* tiles, int ntiles, unsigned long long max_cells, unsigned long long max_slots,
                        uint32_t* cells, uint32_t* npts, uint32_t* flags, cudaStream_t st) {
-  k_count_points<<<grid_for(ncells, 256), 256, 0, st>>>(tiles, ntiles, ncells, cells, npts);
-  k_thin<<<grid_for(ncells, 256), 256, 0, st>>>(tiles, ntiles, ncells, cells, npts);
-  k_slot_flags<<<grid_for(nslots, 256), 256, 0, st>>>(tiles, ntiles, nslots, cells, flags);
+  if (ntiles == 0) return;
+  FG_REQUIRE(ntiles <= 65535, "too many tiles for one launch");
+  const unsigned bc = static_cast<unsigned>(std::min<unsigned long long>(std::max(grid_for(max_cells, 256), 1u), 1024));
+  const unsigned bs = static_cast<unsigned>(std::min<unsigned long long>(std::max(grid_for(max_slots, 256), 1u), 1024));
+  k_thin<<<dim3(bc, ntiles), 256, 0, st>>>(tiles, cells, npts);
+  k_slot_flags<<<dim3(bs, ntiles), 256, 0, st>>>(tiles, cells, flags);
   FG_CUDA(cudaGetLastError());
 }
 
-void launch_emit(const SynthTile* tiles, int ntiles, unsigned long long nslots, const uint32_t* cells,
+void launch_emit(const SynthTile* tiles, int ntiles, unsigned long long max_slots, const uint32_t* cells,
                  const uint32_t* scan, float4* A, float4* Q, float4* D, uint64_t* keys, uint32_t* err,
                  cudaStream_t st) {
-  k_emit<<<grid_for(nslots, 256), 256, 0, st>>>(tiles, ntiles, nslots, cells, scan, A, Q, D, keys, err);
+  if (ntiles == 0) return;
+  FG_REQUIRE(ntiles <= 65535, "too many tiles for one launch");
+  const unsigned bs = static_cast<unsigned>(std::min<unsigned long long>(std::max(grid_for(max_slots, 256), 1u), 1024));
+  k_emit<<<dim3(bs, ntiles), 256, 0, st>>>(tiles, cells, scan, A, Q, D, keys, err);
   FG_CUDA(cudaGetLastError());
 }
 
