@@ -91,18 +91,27 @@ __device__ __forceinline__ void walk_bvh4_deferred(const Node4* __restrict__ nod
   int stack[64];
   int sp = 0;
   int cur = n ? 0 : EMPTY;
-  uint32_t leaf = NONE, leaf2 = NONE;  // a pending leaf and one found speculatively
+  uint32_t leaf = NONE, leaf2 = NONE, leaf3 = NONE, leaf4 = NONE;  // pending leaf, three found speculatively
   const float3 oi = make_float3(o.x * inv.x, o.y * inv.y, o.z * inv.z);
   for (;;) {
     for (;;) {
       // Visit while some lane still has no leaf; a lane that holds one goes on walking until it
-      // finds a second (speculative traversal) instead of idling.
+      // holds four (speculative traversal) instead of idling.
       const bool need = cur != EMPTY && leaf == NONE;
       if (!__any_sync(amask, need)) break;
-      const bool want = cur != EMPTY && leaf2 == NONE;
+      const bool want = cur != EMPTY && leaf4 == NONE;
       if (!want) continue;
       if (cur < 0) {
-        if (leaf == NONE) leaf = static_cast<uint32_t>(~cur); else leaf2 = static_cast<uint32_t>(~cur);
+        const uint32_t lf = static_cast<uint32_t>(~cur);
+        if (leaf == NONE) {
+          leaf = lf;
+        } else if (leaf2 == NONE) {
+          leaf2 = lf;
+        } else if (leaf3 == NONE) {
+          leaf3 = lf;
+        } else {
+          leaf4 = lf;
+        }
         cur = sp > 0 ? stack[--sp] : EMPTY;
         continue;
       }
@@ -144,7 +153,9 @@ __device__ __forceinline__ void walk_bvh4_deferred(const Node4* __restrict__ nod
     if (leaf != NONE) {
       if (index_ok(leaf < n, err, SITE_LEAF, leaf, n)) fn(leaf);
       leaf = leaf2;
-      leaf2 = NONE;
+      leaf2 = leaf3;
+      leaf3 = leaf4;
+      leaf4 = NONE;
     }
   }
 }
