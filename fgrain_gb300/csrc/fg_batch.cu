@@ -23,8 +23,8 @@
 
 namespace fg {
 
-void launch_bridson(const SynthTile* tiles, int ntiles, int color, unsigned ncols, int gdmax, uint32_t* cells,
-                    uint32_t* npts, uint32_t* err, cudaStream_t st);
+void launch_bridson(const SynthTile* tiles, int ntiles, const unsigned cols[4], int gdmax, uint32_t* cells,
+                    uint32_t* npts, uint32_t* done, uint32_t* err, cudaStream_t st);
 size_t bridson_smem(int gdmax);
 void launch_synth_post(const SynthTile* tiles, int ntiles, unsigned long long max_cells, unsigned long long max_slots,
                        uint32_t* cells, uint32_t* npts, uint32_t* flags, cudaStream_t st);
@@ -454,6 +454,7 @@ struct fg_batch {
   DBuf<ScanTile> d_sc;
   DBuf<BTile> d_bt;
   DBuf<uint32_t> cells, npts, flags, slot_scan, ncrys;
+  DBuf<uint32_t> coldone;  // one flag per synthesis column
   unsigned long long maxcells = 0, maxslots = 0;  // the largest tile's cells and Morton slots
   DBuf<float4> A, Q, D;
   DBuf<uint64_t> keys;
@@ -665,8 +666,7 @@ static void stage_synth(fg_batch* B, cudaStream_t st) {
   FG_CUDA(cudaMemsetAsync(B->dstats.p, 0, 4 * sizeof(unsigned long long), st));
   FG_CUDA(cudaMemsetAsync(B->cells.p, 0, B->ncells * sizeof(uint32_t), st));
   FG_CUDA(cudaMemsetAsync(B->npts.p, 0, B->ntiles * sizeof(uint32_t), st));
-  for (int c = 0; c < 4; ++c)
-    launch_bridson(B->d_syn.p, nt, c, B->cols[c], B->gdmax, B->cells.p, B->npts.p, e->d_err, st);
+  launch_bridson(B->d_syn.p, nt, B->cols, B->gdmax, B->cells.p, B->npts.p, B->coldone.p, e->d_err, st);
   FG_CUDA(cudaMemsetAsync(B->flags.p + B->nslots, 0, sizeof(uint32_t), st));
   launch_synth_post(B->d_syn.p, nt, B->maxcells, B->maxslots, B->cells.p, B->npts.p, B->flags.p, st);
   cub_scan(B, B->flags.p, B->slot_scan.p, B->nslots + 1, st);
@@ -884,6 +884,7 @@ static void plan(fg_batch* B, const fg_batch_options* opt) {
   B->d_bt.alloc(n, st);
   B->cells.alloc(std::max<unsigned long long>(cb, 1), st);
   B->npts.alloc(n, st);
+  B->coldone.alloc(std::max(B->cols[0] + B->cols[1] + B->cols[2] + B->cols[3], 1u), st);
   B->ncrys.alloc(n, st);
   B->flags.alloc(sb + 1, st);
   B->slot_scan.alloc(sb + 1, st);
@@ -1018,7 +1019,8 @@ fg_status fg_emulsion_synthesize(fg_engine* e, const fg_emulsion_cfg* cfg, uint6
     DBuf<uint64_t> keys(s.ccap, st);
     FG_CUDA(cudaMemsetAsync(cells.p, 0, ncells * sizeof(uint32_t), st));
     FG_CUDA(cudaMemsetAsync(npts.p, 0, sizeof(uint32_t), st));
-    for (int c = 0; c < 4; ++c) launch_bridson(d_syn.p, 1, c, cols[c], gdmax, cells.p, npts.p, e->d_err, st);
+    DBuf<uint32_t> coldone(std::max(cols[0] + cols[1] + cols[2] + cols[3], 1u), st);
+    launch_bridson(d_syn.p, 1, cols, gdmax, cells.p, npts.p, coldone.p, e->d_err, st);
     FG_CUDA(cudaMemsetAsync(flags.p + s.slots, 0, sizeof(uint32_t), st));
     launch_synth_post(d_syn.p, 1, ncells, s.slots, cells.p, npts.p, flags.p, st);
     exclusive_scan_u32(flags.p, scan.p, s.slots + 1ull, st);
@@ -1206,10 +1208,10 @@ fg_status fg_batch_wait(fg_batch* b, fg_batch_stats* stats) {
     s.transport_blocks = b->tr_blocks;
     s.scan_bin_px = b->bin_px;
     s.graph = b->exec ? 1u : 0u;
-    // Own kernels per run: Bridson x4 (which also count the points), thin + flags, emit, set_n, Karras + fit +
-    // four-wide collapse, photon order x2, transport, maxdim + threshold + developed list + link + roots +
-    // finalize, scan prep, two bin passes, scan (CUB scans not counted).
-    s.kernel_launches = 4 + 2 + 1 + 1 + 3 + 2 + 1 + 6 + 1 + 2 + 1;
+    // Own kernels per run: Bridson (all colour classes in one launch; it also counts the points), thin +
+    // flags, emit, set_n, Karras + fit + four-wide collapse, photon order x2, transport, maxdim + threshold +
+    // developed list + link + roots + finalize, scan prep, two bin passes, scan (CUB scans not counted).
+    s.kernel_launches = 1 + 2 + 1 + 1 + 3 + 2 + 1 + 6 + 1 + 2 + 1;
     b->stats = s;
     if (stats) *stats = s;
   });

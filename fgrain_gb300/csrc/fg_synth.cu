@@ -133,10 +133,17 @@ __device__ __forceinline__ uint32_t syn_word(int X, int Y, int Z) {
 
 // Launch bounds of 7 CTAs per SM (at most 36 registers): more columns in flight hide the round's
 // barriers; measured 11 % faster than the 45-register default on C2.
+// All columns of all four colour classes in one launch, class after class in block order.  A column
+// starts once the columns of lower classes next to it have written their cells back (their done
+// flags), which gives every column the cell state it would see if the classes ran one launch
+// after another: only the eight neighbouring columns share cells with it, and a neighbour of a
+// higher class waits for it in turn.  The flags are waited on by lower block indices only, so
+// the wait ends as the earlier blocks finish; it is bounded all the same (ERR_SPIN_LIMIT).
 __global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* __restrict__ tiles,
-                                                            int ntiles, int color, int nz,
+                                                            int ntiles, uint4 class_base, int nz,
                                                             uint32_t* __restrict__ cells,
-                                                            uint32_t* __restrict__ npts, uint32_t* err) {
+                                                            uint32_t* __restrict__ npts, uint32_t* done,
+                                                            uint32_t* err) {
   extern __shared__ uint32_t syn_sm[];
   uint32_t* grid = syn_sm;                                   // SYN_R^2 * nz cell words
   uint16_t* active = reinterpret_cast<uint16_t*>(grid + SYN_R * SYN_R * nz);  // SYN_B^2 * (nz - 4)
@@ -148,14 +155,17 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* 
   __shared__ int s_wx[SYN_WARPS], s_wy[SYN_WARPS], s_wz[SYN_WARPS];             // accepted this round
   __shared__ int s_outer[SYN_OUTER];
 
-  // Column of this CTA: tile, then the j-th column of this colour class in that tile.
+  // Column of this CTA: colour class, tile, then the j-th column of this class in that tile.
+  const uint32_t cb[4] = {class_base.x, class_base.y, class_base.z, class_base.w};
+  const int color = blockIdx.x >= cb[3] ? 3 : (blockIdx.x >= cb[2] ? 2 : (blockIdx.x >= cb[1] ? 1 : 0));
+  const uint32_t bidx = blockIdx.x - cb[color];
   int lo = 0, hi = ntiles - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (tiles[mid].col_base[color] <= blockIdx.x) lo = mid; else hi = mid - 1;
+    if (tiles[mid].col_base[color] <= bidx) lo = mid; else hi = mid - 1;
   }
   const SynthTile& t = tiles[lo];
-  const uint32_t j = blockIdx.x - t.col_base[color];
+  const uint32_t j = bidx - t.col_base[color];
   const uint32_t cxn = (t.nbx - (color & 1) + 1) / 2;
   const uint32_t bx = 2 * (j % cxn) + (color & 1), by = 2 * (j / cxn) + (color >> 1);
   const int x0 = static_cast<int>(bx) * SYN_B, y0 = static_cast<int>(by) * SYN_B;
@@ -168,13 +178,38 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* 
   const int acap = SYN_B * SYN_B * (nz - 4);  // active list capacity: one entry per column cell
   uint32_t* tc = cells + t.cell_base;
 
-  // Stage the region (column + halo) of the cell grid.
+  // Wait for the neighbouring columns of lower classes.
+  if (tid == 0 && color > 0) {
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int nx = static_cast<int>(bx) + dx, ny = static_cast<int>(by) + dy;
+        if ((dx == 0 && dy == 0) || nx < 0 || ny < 0 || nx >= static_cast<int>(t.nbx) || ny >= static_cast<int>(t.nby))
+          continue;
+        const int nc = (nx & 1) | ((ny & 1) << 1);
+        if (nc >= color) continue;
+        const uint32_t ncxn = (t.nbx - (nc & 1) + 1) / 2;
+        const uint32_t id = cb[nc] + t.col_base[nc] + static_cast<uint32_t>(ny >> 1) * ncxn + static_cast<uint32_t>(nx >> 1);
+        const volatile uint32_t* f = done + id;
+        uint32_t spins = 0;
+        while (*f == 0u) {
+          if (++spins > (1u << 22)) {
+            atomicOr(err, ERR_SPIN_LIMIT);
+            break;
+          }
+          __nanosleep(64);
+        }
+      }
+    __threadfence();
+  }
+  __syncthreads();
+
+  // Stage the region (column + halo) of the cell grid (through L2: neighbours wrote it).
   for (int i = tid; i < ncell; i += blockDim.x) {
     const int rx = i % SYN_R, ry = (i / SYN_R) % SYN_R, rz = i / (SYN_R * SYN_R);
     const int gx = ox + rx, gy = oy + ry, gz = rz - 2;
     uint32_t w = 0;
     if (gx >= 0 && gy >= 0 && gz >= 0 && gx < static_cast<int>(t.gw) && gy < static_cast<int>(t.gh) && gz < gd)
-      w = tc[(static_cast<size_t>(gz) * t.gh + gy) * t.gw + gx];
+      w = __ldcg(tc + (static_cast<size_t>(gz) * t.gh + gy) * t.gw + gx);
     grid[i] = w;
   }
   if (tid == 0) {
@@ -436,7 +471,12 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* 
     if (gx >= 0 && gy >= 0 && gz >= 0 && gx < static_cast<int>(t.gw) && gy < static_cast<int>(t.gh) && gz < gd)
       tc[(static_cast<size_t>(gz) * t.gh + gy) * t.gw + gx] = grid[i];
   }
-  if (tid == 0 && s_ncom) atomicAdd(npts + lo, static_cast<uint32_t>(s_ncom));
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) {
+    if (s_ncom) atomicAdd(npts + lo, static_cast<uint32_t>(s_ncom));
+    atomicExch(done + blockIdx.x, 1u);
+  }
 }
 
 // Independent deletion down to the Bridson-expected count.
@@ -535,13 +575,17 @@ namespace fg {
 size_t bridson_smem(int gdmax);
 
 // Host wrappers (launch on `st`; all buffers preallocated so the sequence can be graph-captured).
-void launch_bridson(const SynthTile* tiles, int ntiles, int color, unsigned ncols, int gdmax,
-                    uint32_t* cells, uint32_t* npts, uint32_t* err, cudaStream_t st) {
-  if (ncols == 0) return;
+// cols[c] columns of class c; done holds one flag per column (zeroed here).
+void launch_bridson(const SynthTile* tiles, int ntiles, const unsigned cols[4], int gdmax, uint32_t* cells,
+                    uint32_t* npts, uint32_t* done, uint32_t* err, cudaStream_t st) {
+  const unsigned total = cols[0] + cols[1] + cols[2] + cols[3];
+  if (total == 0) return;
   const int nz = gdmax + 4;
   const size_t smem = bridson_smem(gdmax);
+  FG_CUDA(cudaMemsetAsync(done, 0, total * sizeof(uint32_t), st));
   FG_CUDA(cudaFuncSetAttribute(k_bridson, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-  k_bridson<<<ncols, SYN_WARPS * 32, smem, st>>>(tiles, ntiles, color, nz, cells, npts, err);
+  const uint4 cb = make_uint4(0u, cols[0], cols[0] + cols[1], cols[0] + cols[1] + cols[2]);
+  k_bridson<<<total, SYN_WARPS * 32, smem, st>>>(tiles, ntiles, cb, nz, cells, npts, done, err);
   FG_CUDA(cudaGetLastError());
 }
 
