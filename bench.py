@@ -425,6 +425,45 @@ def run_c4(args):
             "clocks": ck.summary()}))
 
 
+def run_fast(args):
+    """The C2 tiles through the fast-approximation mode (the reference's wgpu tile model, with the
+    GPU branch's tile parameters): one fg_render_tiles_fast call per step, host tiles in and host
+    densities out.  Reported next to the headline, not instead of it."""
+    import fgrain_gb300 as fg
+    from fgrain_gb300 import fast
+    from fgrain_gb300.image import tile_grid, tile_seed
+
+    rank, world, local, td = dist()
+    exposure = c2_inputs()
+    H, W = exposure.shape
+    grid, _, _ = tile_grid(W, H, GRAIN)
+    params = [fast.tile_params_fast("tri-x", 1.0 / GRAIN, t.tw, t.th, 1.0, 0.0, tile_seed(SEED, t)) for t in grid]
+    tiles = [np.ascontiguousarray(exposure[t.y_start:t.y_start + t.th, t.x_start:t.x_start + t.tw]) for t in grid]
+    engine = fg.GpuEngine(local)
+    for _ in range(max(args.warmup, 0)):
+        fast.render_tiles_fast(params, tiles, engine)
+    if td:
+        td.barrier()
+    with Clocks(local) as ck:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            fast.render_tiles_fast(params, tiles, engine)
+        t = (time.perf_counter() - t0) / args.steps
+    t = reduce_max(td, t)
+    if rank == 0:
+        value = OUT_W * OUT_H * world / t / 1e6
+        h2d = sum(x.nbytes for x in tiles)
+        print(json.dumps({
+            "metric": METRIC, "value": value, "unit": "Mpx/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "C2 tiles through the fast approximation (the reference's wgpu tile model: "
+                                   "jittered grid, per-crystal Poisson counts, column scan), host to host",
+                       "tiles": len(grid), "output_px": OUT_W * OUT_H, "parallelism": f"replicas x{world}"},
+            "e2e": {"value": value, "unit": "Mpx/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d},
+            "gpu_launches": 5 * args.steps, "clocks": ck.summary()}))
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -463,9 +502,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--tiles", type=int, default=0, help="render only the first N tiles of C2 (profiling)")
-    ap.add_argument("--workload", choices=["c2", "c3", "c4"], default="c2",
+    ap.add_argument("--workload", choices=["c2", "c3", "c4", "fast"], default="c2",
                     help="c2: the headline configuration; c3: the mixed batch; c4: a 4096^2 RGB photograph at "
-                         "supersample 4 through the film renderer (c3 and c4 are reported, not the headline)")
+                         "supersample 4 through the film renderer; fast: the C2 tiles through the fast "
+                         "approximation (c3, c4 and fast are reported, not the headline)")
     ap.add_argument("--film-side", type=int, default=4096, help="c4: side of the RGB photograph (4096 for C4)")
     ap.add_argument("--batch-gb", type=float, default=0.0,
                     help="c4: device GiB one batch of tiles may use (0: 70 %% of the free memory)")
@@ -480,6 +520,8 @@ def main():
         run_reference(args)
     elif args.workload == "c4":
         run_c4(args)
+    elif args.workload == "fast":
+        run_fast(args)
     else:
         run_ours(args)
 

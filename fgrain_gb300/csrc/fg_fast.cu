@@ -35,10 +35,10 @@ struct __align__(16) FastCell {
 static_assert(sizeof(FastCell) == 64, "grid cell layout");
 
 struct FastTile {
-  unsigned long long cell_base, px_base;
+  unsigned long long cell_base, px_base, col_base;  // col_base: first (x, y) column of the tile
   const float* tile;  // exposure, width x height
   uint32_t gw, gh, gd, W, H, g;  // grid, pixels, strata per axis
-  float cs, film_w, film_h, film_d, r_min, mean_r, var, ar, sens, exposure, fexp, clump, opacity;
+  float cs, film_w, film_h, film_d, r_min, log_mean_r, var, ar, sens, exposure, fexp, clump, opacity;
   uint32_t morph, seed, scan_seed;
 };
 
@@ -102,7 +102,7 @@ __global__ void k_fast_generate(const FastTile* __restrict__ tiles, FastCell* __
     const float u1 = fmaxf(rand_f32(rng), 1e-6f);
     const float u2 = rand_f32(rng);
     const float nz = fm(__fsqrt_rn(fm(-2.0f, flog_(u1))), fcos_(fm(fm(2.0f, PI_F), u2)));
-    const float radius = clampf_(fexp_(fa(flog_(t.mean_r), fm(t.var, nz))), 0.15f, fm(t.cs, 0.65f));
+    const float radius = clampf_(fexp_(fa(t.log_mean_r, fm(t.var, nz))), 0.15f, fm(t.cs, 0.65f));
     if (t.morph == 1u) {
       const float aspect = fmaxf(t.ar, 1.0f);
       const float rp = fm(radius, __fsqrt_rn(aspect)), rt = fd(radius, __fsqrt_rn(aspect));
@@ -264,6 +264,24 @@ __global__ void k_fast_clump(const FastTile* __restrict__ tiles, FastCell* __res
   }
 }
 
+// Bitmask over depth of the developed crystals of each (x, y) column (the grid is at most 32 deep),
+// so the scan visits developed cells only, in the same depth order.
+__global__ void k_fast_colmask(const FastTile* __restrict__ tiles, const FastCell* __restrict__ cells,
+                               uint32_t* __restrict__ colmask) {
+  const FastTile t = tiles[blockIdx.y];
+  const unsigned long long ncol = static_cast<unsigned long long>(t.gw) * t.gh;
+  const FastCell* C = cells + t.cell_base;
+  for (unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; i < ncol;
+       i += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+    uint32_t m = 0;
+    for (uint32_t z = 0; z < t.gd; ++z) {
+      const uint4 fl = C[static_cast<size_t>(z) * ncol + i].flags;
+      if (fl.x != 0u && fl.z != 0u) m |= 1u << z;
+    }
+    colmask[t.col_base + i] = m;
+  }
+}
+
 __device__ __forceinline__ void cross3(float ax, float ay, float az, float bx, float by, float bz, float& ox, float& oy,
                                        float& oz) {
   ox = fs(fm(ay, bz), fm(az, by));
@@ -286,7 +304,7 @@ __device__ __forceinline__ void quat_inv_rot(float4 q, float vx, float vy, float
 
 // scan.wgsl:55-178: per pixel, g x g jittered vertical rays through the 5 x 5 cell columns.
 __global__ void k_fast_scan(const FastTile* __restrict__ tiles, const FastCell* __restrict__ cells,
-                            float* __restrict__ d_neg) {
+                            const uint32_t* __restrict__ colmask, float* __restrict__ d_neg) {
   const FastTile t = tiles[blockIdx.y];
   const unsigned long long npx = static_cast<unsigned long long>(t.W) * t.H;
   const FastCell* C = cells + t.cell_base;
@@ -311,10 +329,10 @@ __global__ void k_fast_scan(const FastTile* __restrict__ tiles, const FastCell* 
           for (int dx = -2; dx <= 2; ++dx) {
             const int gx = cx + dx;
             if (gx < 0 || gx >= static_cast<int>(t.gw)) continue;
-            for (int gz = 0; gz < static_cast<int>(t.gd); ++gz) {
+            for (uint32_t m = __ldg(colmask + t.col_base + static_cast<size_t>(gy) * t.gw + gx); m; m &= m - 1) {
+              const int gz = __ffs(m) - 1;
               const FastCell* c = C + (static_cast<size_t>(gz) * t.gh + gy) * t.gw + gx;
               const uint4 fl = __ldg(&c->flags);
-              if (fl.x == 0u || fl.z == 0u) continue;
               const float4 cp = __ldg(&c->pos), de = __ldg(&c->dims_exp), q = __ldg(&c->rot);
               float lox, loy, loz, ldx, ldy, ldz;
               quat_inv_rot(q, fs(ox, cp.x), fs(oy, cp.y), fs(oz, cp.z), lox, loy, loz);
@@ -400,7 +418,8 @@ FastTile fast_tile(const fg_tile_params& p) {
   t.film_h = static_cast<float>(p.film_h);
   t.film_d = static_cast<float>(p.film_d);
   t.r_min = static_cast<float>(p.r_min);
-  t.mean_r = static_cast<float>(p.mean_crystal_radius);
+  // log(mean radius) once per tile, in double and rounded once, as every cell would form it.
+  t.log_mean_r = static_cast<float>(std::log(static_cast<double>(static_cast<float>(p.mean_crystal_radius))));
   t.var = static_cast<float>(p.size_variance);
   t.ar = static_cast<float>(p.tabular_aspect_ratio);
   t.sens = static_cast<float>(p.base_sensitivity);
@@ -436,7 +455,7 @@ fg_status fg_render_tiles_fast(fg_engine* e, const fg_tile_params* params, uint3
     FG_REQUIRE(params && tiles && d_neg && ntiles > 0 && ntiles <= 65535, "null argument or bad tile count");
     cudaStream_t st = e->stream;
     std::vector<FastTile> ft(ntiles);
-    unsigned long long nc = 0, npx = 0, maxc = 0, maxp = 0;
+    unsigned long long nc = 0, npx = 0, maxc = 0, maxp = 0, ncols = 0;
     for (uint32_t i = 0; i < ntiles; ++i) {
       const fg_tile_params& p = params[i];
       FG_REQUIRE(tiles[i] && d_neg[i], "null tile or output");
@@ -446,6 +465,8 @@ fg_status fg_render_tiles_fast(fg_engine* e, const fg_tile_params* params, uint3
       ft[i] = fast_tile(p);
       ft[i].cell_base = nc;
       ft[i].px_base = npx;
+      ft[i].col_base = ncols;
+      ncols += static_cast<unsigned long long>(ft[i].gw) * ft[i].gh;
       const unsigned long long c = static_cast<unsigned long long>(ft[i].gw) * ft[i].gh * ft[i].gd;
       const unsigned long long q = static_cast<unsigned long long>(p.width_px) * p.height_px;
       nc += c;
@@ -456,6 +477,7 @@ fg_status fg_render_tiles_fast(fg_engine* e, const fg_tile_params* params, uint3
     DBuf<float> img(npx, st), out(npx, st);
     DBuf<FastCell> dc(nc, st);
     DBuf<float4> pos0(nc, st);
+    DBuf<uint32_t> colmask(ncols, st);
     for (uint32_t i = 0; i < ntiles; ++i) {
       ft[i].tile = img.p + ft[i].px_base;
       FG_CUDA(cudaMemcpyAsync(img.p + ft[i].px_base, tiles[i],
@@ -470,7 +492,8 @@ fg_status fg_render_tiles_fast(fg_engine* e, const fg_tile_params* params, uint3
     k_fast_resolve<<<dim3(bc, ntiles), 256, 0, st>>>(dt.p, dc.p, pos0.p);
     k_fast_expose<<<dim3(bc, ntiles), 256, 0, st>>>(dt.p, dc.p);
     k_fast_clump<<<dim3(bc, ntiles), 256, 0, st>>>(dt.p, dc.p);
-    k_fast_scan<<<dim3(bp, ntiles), 128, 0, st>>>(dt.p, dc.p, out.p);
+    k_fast_colmask<<<dim3(bc, ntiles), 256, 0, st>>>(dt.p, dc.p, colmask.p);
+    k_fast_scan<<<dim3(bp, ntiles), 128, 0, st>>>(dt.p, dc.p, colmask.p, out.p);
     FG_CUDA(cudaGetLastError());
     for (uint32_t i = 0; i < ntiles; ++i) {
       FG_CUDA(cudaMemcpyAsync(d_neg[i], out.p + ft[i].px_base,
