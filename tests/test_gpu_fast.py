@@ -54,3 +54,13 @@ def test_dark_tile_is_base_density(engine):
     p = fast.tile_params_fast("hp5", 1 / 1.8, 33, 21, 1.0, 0.0, 1)
     d = fast.render_tile_fast(np.zeros((21, 33), np.float32), p, engine)
     assert (d == np.float32(0.05)).all()
+
+
+@pytest.mark.parametrize("tw,th", [(1, 1), (1, 9), (13, 2)])
+def test_tiny_tiles_bit_exact(engine, tw, th):
+    p = fast.tile_params_fast("hp5", 1 / 1.8, tw, th, 1.0, 0.0, 4)
+    tile = np.full((th, tw), 0.8, np.float32)
+    d, cells = fast.render_tile_fast(tile, p, engine, cells=True)
+    do, co = orc.fast_tile(p, tile)
+    np.testing.assert_array_equal(d, do)
+    np.testing.assert_array_equal(cells["flags"], co["flags"])

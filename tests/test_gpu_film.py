@@ -185,3 +185,21 @@ def test_render_in_several_batches_equals_one_batch(engine):
         rep, many = film.render_film(rgb, small, engine)
         np.testing.assert_array_equal(one, many)
         assert rep.total_crystals == rep1.total_crystals and rep.total_tiles == rep1.total_tiles
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (1, 7), (5, 3), (49, 1)])
+def test_tiny_and_ragged_images_render(engine, shape):
+    """Images smaller than a tile, one pixel wide or one pixel high: one clipped tile each; the
+    device renderer agrees with the composition of its stages and keeps the output size."""
+    gray = np.random.default_rng(sum(shape)).integers(40, 256, shape, dtype=np.uint8)
+    opts = film.FilmRenderOptions(preset="tri-x", grain_size_px=2.4, tile_size=64, seed=1)
+    rep, out = film.render_film(gray, opts, engine)
+    assert out.shape == shape and rep.total_tiles == 1
+    np.testing.assert_array_equal(out, compose_bw(gray, opts, engine))
+
+
+def test_all_black_photograph_stays_black(engine):
+    """Zero exposure everywhere: the camera gate is empty, no grain, every output pixel 0
+    (image_pipeline.rs:137-155 and the output gates, 866-882)."""
+    _, out = film.render_film(np.zeros((70, 90, 3), np.uint8), film.FilmRenderOptions(color=True, tile_size=64), engine)
+    assert (out == 0).all()
