@@ -131,15 +131,16 @@ __device__ __forceinline__ uint32_t syn_word(int X, int Y, int Z) {
          static_cast<uint32_t>(X & 1023);
 }
 
-// Launch bounds of 7 CTAs per SM (at most 36 registers): more columns in flight hide the round's
-// barriers; measured 11 % faster than the 45-register default on C2.
+// Launch bounds of 8 CTAs per SM (32 registers): more columns in flight hide the round's barriers.
+// A column with its one-cell spill and the halo stages 14 x 14 cells per layer, so eight CTAs fit
+// in the SM's 228 KB of shared memory for depths up to 23 cells.
 // All columns of all four colour classes in one launch, class after class in block order.  A column
 // starts once the columns of lower classes next to it have written their cells back (their done
 // flags), which gives every column the cell state it would see if the classes ran one launch
 // after another: only the eight neighbouring columns share cells with it, and a neighbour of a
 // higher class waits for it in turn.  The flags are waited on by lower block indices only, so
 // the wait ends as the earlier blocks finish; it is bounded all the same (ERR_SPIN_LIMIT).
-__global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* __restrict__ tiles,
+__global__ void __launch_bounds__(SYN_WARPS * 32, 8) k_bridson(const SynthTile* __restrict__ tiles,
                                                             int ntiles, uint4 class_base, int nz,
                                                             uint32_t* __restrict__ cells,
                                                             uint32_t* __restrict__ npts, uint32_t* done,
@@ -152,7 +153,6 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* 
   __shared__ int s_pick[SYN_WARPS];
   __shared__ unsigned s_vmask[SYN_WARPS];
   __shared__ int s_cx[SYN_WARPS][32], s_cy[SYN_WARPS][32], s_cz[SYN_WARPS][32];  // valid candidates
-  __shared__ int s_wx[SYN_WARPS], s_wy[SYN_WARPS], s_wz[SYN_WARPS];             // accepted this round
   __shared__ int s_outer[SYN_OUTER];
 
   // Column of this CTA: colour class, tile, then the j-th column of this class in that tile.
@@ -326,59 +326,91 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* 
       // first candidate (lane order) that is free in the grid and at least r from the points
       // accepted for warps < w; with none left, its point retires.
       //
-      // Fast path: a warp's first grid-free candidate (its winner) is what that order keeps unless
-      // it lies within r of a point accepted for an earlier warp.  Lane w holds warp w's winner;
-      // the winners' pairwise conflicts come from shuffles, and warps are accepted in order, in
-      // registers, up to the first one whose winner conflicts with an accepted winner.
-      int fw = -1, WX = 0, WY = 0, WZ = 0;
+      // Lane w speaks for warp w and holds its winner (first grid-free candidate).  That order keeps
+      // a winner unless it lies within r of a point accepted for an earlier warp, so the warps keep
+      // their winners in runs up to the next warp whose winner conflicts; only that warp searches
+      // its other candidates against the points accepted so far.  Conflicts between winners come
+      // from shuffles; a point kept instead of a winner is tested against the later winners once.
+      int fw = -1, PX = 0, PY = 0, PZ = 0;
       if (lane < SYN_WARPS) {
         const unsigned m = s_vmask[lane];
         if (m) {
           fw = __ffs(m) - 1;
-          WX = s_cx[lane][fw];
-          WY = s_cy[lane][fw];
-          WZ = s_cz[lane][fw];
+          PX = s_cx[lane][fw];
+          PY = s_cy[lane][fw];
+          PZ = s_cz[lane][fw];
         }
       }
       unsigned cm = 0;  // bit u: this lane's winner conflicts with warp u's (u < lane)
 #pragma unroll
       for (int u = 0; u < SYN_WARPS - 1; ++u) {
-        const int ux = __shfl_sync(0xffffffffu, WX, u), uy = __shfl_sync(0xffffffffu, WY, u);
-        const int uz = __shfl_sync(0xffffffffu, WZ, u), uf = __shfl_sync(0xffffffffu, fw, u);
+        const int ux = __shfl_sync(0xffffffffu, PX, u), uy = __shfl_sync(0xffffffffu, PY, u);
+        const int uz = __shfl_sync(0xffffffffu, PZ, u), uf = __shfl_sync(0xffffffffu, fw, u);
         if (u < lane && fw >= 0 && uf >= 0) {
-          const int ex = WX - ux, ey = WY - uy, ez = WZ - uz;
+          const int ex = PX - ux, ey = PY - uy, ez = PZ - uz;
           if (ex * ex + ey * ey + ez * ez < SYN_R2X) cm |= 1u << u;
         }
       }
-      unsigned acc = 0, retire = 0;
-      int wslow = SYN_WARPS;
-      for (int w = 0; w < SYN_WARPS; ++w) {
-        const int f = __shfl_sync(0xffffffffu, fw, w);
-        const unsigned c = __shfl_sync(0xffffffffu, cm, w);
-        if (f < 0) {
-          retire |= 1u << w;
-          continue;
+      const unsigned has = __ballot_sync(0xffffffffu, fw >= 0);  // warps with a winner
+      unsigned accw = 0, acc = 0;  // warps that keep their winner; warps that keep a point
+      bool near = false;           // this lane's winner lies within r of a point kept instead of a winner
+      for (int cur = 0; cur < SYN_WARPS;) {
+        // A warp from cur on keeps its winner unless it conflicts with a kept point; up to the first
+        // such warp, every warp with a winner keeps it.
+        const unsigned from = ~((1u << cur) - 1u);
+        const bool bad = lane >= cur && fw >= 0 &&
+                         (near || (cm & (accw | (has & from & ((1u << lane) - 1u)))) != 0u);
+        const unsigned bm = __ballot_sync(0xffffffffu, bad);
+        const int wb = bm ? __ffs(bm) - 1 : SYN_WARPS;
+        const unsigned run = has & from & ((1u << wb) - 1u);
+        accw |= run;
+        acc |= run;
+        if (wb == SYN_WARPS) break;
+        // Warp wb: its first candidate at least r from every point kept for warps < wb.
+        const unsigned m = s_vmask[wb];
+        bool ok = (m >> lane) & 1u;
+        int X = 0, Y = 0, Z = 0;
+        if (ok) {
+          X = s_cx[wb][lane];
+          Y = s_cy[wb][lane];
+          Z = s_cz[wb][lane];
         }
-        if (c & acc) {
-          wslow = w;
-          break;
+#pragma unroll
+        for (int u = 0; u < SYN_WARPS - 1; ++u) {
+          const int ux = __shfl_sync(0xffffffffu, PX, u), uy = __shfl_sync(0xffffffffu, PY, u);
+          const int uz = __shfl_sync(0xffffffffu, PZ, u);
+          if ((acc >> u) & 1u) {
+            const int ex = X - ux, ey = Y - uy, ez = Z - uz;
+            if (ex * ex + ey * ey + ez * ez < SYN_R2X) ok = false;
+          }
         }
-        acc |= 1u << w;
+        const unsigned okm = __ballot_sync(0xffffffffu, ok);
+        if (okm) {
+          const int c = __ffs(okm) - 1;
+          const int qx = __shfl_sync(0xffffffffu, X, c), qy = __shfl_sync(0xffffffffu, Y, c);
+          const int qz = __shfl_sync(0xffffffffu, Z, c);
+          acc |= 1u << wb;
+          if (lane == wb) {
+            PX = qx;
+            PY = qy;
+            PZ = qz;
+          } else if (lane > wb && fw >= 0) {
+            const int ex = PX - qx, ey = PY - qy, ez = PZ - qz;
+            if (ex * ex + ey * ey + ez * ez < SYN_R2X) near = true;
+          }
+        }
+        cur = wb + 1;
       }
-      // Commit the accepted winners, appending to the active list in warp order.
+      // Commit the kept points, appending to the active list in warp order.
       bool inside = false, committed = false;
       int cridx = 0;
       if (lane < SYN_WARPS && ((acc >> lane) & 1u)) {
-        const int slot = __popc(acc & ((1u << lane) - 1u));
-        s_wx[slot] = WX;
-        s_wy[slot] = WY;
-        s_wz[slot] = WZ;
-        const int ccx = WX >> 10, ccy = WY >> 10, ccz = WZ >> 10;
+        const int ccx = PX >> 10, ccy = PY >> 10, ccz = PZ >> 10;
         const int rx = ccx - ox, ry = ccy - oy, rz = ccz + 2;
         if (index_ok(rx >= 0 && rx < SYN_R && ry >= 0 && ry < SYN_R && rz >= 0 && rz < nz, err, SITE_SYN_COMMIT,
                      static_cast<uint32_t>(rx | (ry << 8) | (rz << 16)), blockIdx.x)) {
           cridx = (rz * SYN_R + ry) * SYN_R + rx;
-          grid[cridx] = syn_word(WX, WY, WZ);
+          grid[cridx] = syn_word(PX, PY, PZ);
           committed = true;
           inside = ccx >= x0 && ccx < x1 && ccy >= y0 && ccy < y1;
         }
@@ -390,75 +422,47 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 7) k_bridson(const SynthTile* 
         if (index_ok(pos < acap, err, SITE_SYN_ACTIVE, pos, blockIdx.x)) active[pos] = static_cast<uint16_t>(cridx);
       }
       const unsigned cmm = __ballot_sync(0xffffffffu, committed);
-      __syncwarp();
-      if (lane == 0) {
-        s_nact = min(nbase + __popc(im), acap);
-        s_ncom += __popc(cmm);
-      }
-      __syncwarp();
-      // Serial path from the first conflicting warp on.  One lane per candidate.
-      int ncom = __popc(acc);
-      for (int w = wslow; w < SYN_WARPS; ++w) {
-        const unsigned m = s_vmask[w];
-        bool ok = false;
-        int X = 0, Y = 0, Z = 0;
-        if ((m >> lane) & 1u) {
-          X = s_cx[w][lane];
-          Y = s_cy[w][lane];
-          Z = s_cz[w][lane];
-          ok = true;
-          for (int j = 0; j < ncom; ++j) {
-            const int ex = X - s_wx[j], ey = Y - s_wy[j], ez = Z - s_wz[j];
-            if (ex * ex + ey * ey + ez * ez < SYN_R2X) {
-              ok = false;
-              break;
-            }
-          }
-        }
-        const unsigned okm = __ballot_sync(0xffffffffu, ok);
-        if (okm == 0) {
-          retire |= 1u << w;
-          continue;
-        }
-        if (lane == __ffs(okm) - 1) {
-          s_wx[ncom] = X;
-          s_wy[ncom] = Y;
-          s_wz[ncom] = Z;
-          const int ccx = X >> 10, ccy = Y >> 10, ccz = Z >> 10;
-          const int rx = ccx - ox, ry = ccy - oy, rz = ccz + 2;
-          if (index_ok(rx >= 0 && rx < SYN_R && ry >= 0 && ry < SYN_R && rz >= 0 && rz < nz, err, SITE_SYN_COMMIT,
-                       static_cast<uint32_t>(rx | (ry << 8) | (rz << 16)), blockIdx.x)) {
-            const int ridx = (rz * SYN_R + ry) * SYN_R + rx;
-            grid[ridx] = syn_word(X, Y, Z);
-            ++s_ncom;
-            if (ccx >= x0 && ccx < x1 && ccy >= y0 && ccy < y1 &&
-                index_ok(s_nact < acap, err, SITE_SYN_ACTIVE, s_nact, blockIdx.x))
-              active[s_nact++] = static_cast<uint16_t>(ridx);
-          }
-        }
-        ++ncom;
-        __syncwarp();
-      }
-      // Retire the points of failed steps, each once, in descending list order (swap-remove keeps
-      // the lower indices valid): lane w speaks for warp w.
-      const bool mine = lane < SYN_WARPS && ((retire >> lane) & 1u);
-      const int mypick = mine ? s_pick[lane] : -1;
-      bool first = mine;
-      for (int w2 = 0; w2 < lane && first; ++w2)
-        if (((retire >> w2) & 1u) && s_pick[w2] == mypick) first = false;
+      const int n0 = min(nbase + __popc(im), acap);
+      __syncwarp();  // the appended entries are visible to the retirement below
+      // Retire the points of failed steps, each once, as if removed one after another in descending
+      // list order, each by moving the list's current last entry into its place (a swap-remove).
+      // The removal of rank k takes the entry then at n0 - 1 - k; when that position was itself
+      // refilled by an earlier removal, its entry is the one that removal took, so each removal
+      // follows that chain (pointer jumping over the ranks) to an original position.
+      const bool mine = lane < SYN_WARPS && !((acc >> lane) & 1u);
+      const int mypick = lane < SYN_WARPS ? s_pick[lane] : -1;
+      const unsigned peers = __match_any_sync(0xffffffffu, mine ? mypick : -1 - lane);
+      const bool first = mine && lane == __ffs(peers) - 1;
       const unsigned dm = __ballot_sync(0xffffffffu, first);
       int rank = 0;
-      if (first)
-        for (int w2 = 0; w2 < SYN_WARPS; ++w2)
-          if (((dm >> w2) & 1u) && s_pick[w2] > mypick) ++rank;
-      const int K = __popc(dm);
-      for (int k = 0; k < K; ++k) {
-        if (first && rank == k) {
-          const int last = s_nact - 1;
-          active[mypick] = active[last];
-          s_nact = last;
+#pragma unroll
+      for (int w2 = 0; w2 < SYN_WARPS; ++w2) {
+        const int p2 = __shfl_sync(0xffffffffu, mypick, w2);
+        if (((dm >> w2) & 1u) && p2 > mypick) ++rank;
+      }
+      int src = n0 - 1 - rank, ptr = -1;
+#pragma unroll
+      for (int w2 = 0; w2 < SYN_WARPS; ++w2) {
+        const int p2 = __shfl_sync(0xffffffffu, mypick, w2);
+        if (((dm >> w2) & 1u) && w2 != lane && p2 == src) ptr = w2;
+      }
+      if (!first) ptr = -1;
+#pragma unroll
+      for (int hop = 1; hop < SYN_WARPS; hop <<= 1) {  // chains are shorter than SYN_WARPS
+        const int at = ptr < 0 ? lane : ptr;
+        const int ps = __shfl_sync(0xffffffffu, src, at), pp = __shfl_sync(0xffffffffu, ptr, at);
+        if (ptr >= 0) {
+          src = ps;
+          ptr = pp;
         }
-        __syncwarp();
+      }
+      uint16_t moved = 0;
+      if (first && index_ok(src >= 0 && src < n0, err, SITE_SYN_ACTIVE, src, blockIdx.x)) moved = active[src];
+      __syncwarp();
+      if (first && src >= 0 && src < n0) active[mypick] = moved;
+      if (lane == 0) {
+        s_nact = n0 - __popc(dm);
+        s_ncom += __popc(cmm);
       }
     }
   }

@@ -13,8 +13,10 @@
 // also at least r from the points accepted for earlier warps, else its point retires).
 // Positions are fixed point (1/1024 of a cell) so every distance test is exact integer arithmetic.
 //
-// Bridson started from many seeds packs ~0.3-0.6 % denser than from one, so each tile is then
-// thinned (independent deletion) to the count Bridson yields on the same box:
+// Bridson started from many seeds packs denser than from one (0.3-0.9 % per tile on a 1024^2
+// tri-x image at supersample 2; 1.2-1.7 % with a spill of two cells, -1.3 % with none: the
+// columns' walls then leave gaps), so each tile is then thinned (independent deletion) to the
+// count Bridson yields on the same box:
 // rho r^3 = 0.57793 + 0.11307 r (2/W + 2/H + 2/D), fitted to the reference sampler over box
 // sizes 27-160 um and depths 6-20 um (residuals within 0.12 %).
 #pragma once
@@ -23,7 +25,7 @@
 namespace fg {
 
 constexpr int SYN_B = 8;         // column edge in cells
-constexpr int SYN_SPILL = 2;     // cells an accepted point may lie outside its column
+constexpr int SYN_SPILL = 1;     // cells an accepted point may lie outside its column
 constexpr int SYN_HALO = SYN_SPILL + 2;      // + the reach of the neighbourhood test
 constexpr int SYN_R = SYN_B + 2 * SYN_HALO;  // staged region edge
 // Columns of one colour class are one column apart: what one writes (its spill zone) must not
