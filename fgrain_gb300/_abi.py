@@ -120,7 +120,8 @@ class fg_batch_stats(C.Structure):
                 ("pixels", C.c_uint64), ("hits", C.c_uint64), ("scan_hits", C.c_uint64),
                 ("scan_fallbacks", C.c_uint64), ("transport_threads", C.c_uint32),
                 ("transport_blocks", C.c_uint32), ("scan_bin_px", C.c_uint32), ("graph", C.c_uint32),
-                ("kernel_launches", C.c_uint32), ("_pad", C.c_uint32)]
+                ("kernel_launches", C.c_uint32), ("_pad", C.c_uint32), ("developed", C.c_uint64),
+                ("clumps", C.c_uint64)]
 
 
 class fg_device_crystals(C.Structure):
@@ -141,7 +142,8 @@ class fg_film_options(C.Structure):
 class fg_film_report(C.Structure):
     _fields_ = [("in_w", C.c_uint32), ("in_h", C.c_uint32), ("out_w", C.c_uint32), ("out_h", C.c_uint32),
                 ("total_tiles", C.c_uint64), ("total_crystals", C.c_uint64), ("photons", C.c_uint64),
-                ("elapsed_seconds", C.c_double), ("prep_ms", C.c_double), ("tiles_ms", C.c_double),
+                ("elapsed_seconds", C.c_double), ("developed_crystals", C.c_uint64),
+                ("total_clumps", C.c_uint64), ("prep_ms", C.c_double), ("tiles_ms", C.c_double),
                 ("finish_ms", C.c_double)]
 
 
@@ -231,6 +233,7 @@ PROTOTYPES = {
     "fg_scan_crystals_static": (_st, [C.POINTER(fg_device_crystals), C.POINTER(fg_emulsion_cfg),
                                       C.POINTER(fg_scan_cfg), C.c_uint64, _vp, _vp, _vp, C.c_char_p,
                                       C.c_size_t]),
+    "fg_png_unfilter": (_st, [_vp, C.c_uint32, C.c_uint32, C.c_uint32]),
 }
 
 _lib = None

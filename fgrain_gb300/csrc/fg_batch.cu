@@ -387,19 +387,29 @@ __global__ void k_roots_b(unsigned long long ncap, const uint8_t* developed, int
   atomicAdd(&size[r], 1u);
 }
 
+// Also counts the clumps (development.rs:107-108: one per connected component of developed
+// crystals, singletons included), one warp-aggregated add per warp.
 __global__ void k_finalize_b(const BTile* __restrict__ bt, int ntiles, unsigned long long ncap,
-                             const uint8_t* developed, const int* parent, const uint32_t* size, double* exp64) {
+                             const uint8_t* developed, const int* parent, const uint32_t* size, double* exp64,
+                             unsigned long long* clumps) {
   const unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
-  if (g >= ncap) return;
-  if (!developed[g]) {
-    exp64[g] = 0.0;
-    return;
+  bool root = false;
+  if (g < ncap) {
+    if (!developed[g]) {
+      exp64[g] = 0.0;
+    } else {
+      const BTile& t = bt[btile_of(bt, ntiles, g)];
+      const int p = parent[g];
+      const uint32_t sz = size[p];
+      double e = t.fe;
+      if (sz > 1)
+        e = __dmul_rn(t.fe, __dadd_rn(1.15, __dmul_rn(0.18, static_cast<double>((sz < 6 ? sz : 6) - 1))));
+      exp64[g] = e;
+      root = p == static_cast<int>(g);
+    }
   }
-  const BTile& t = bt[btile_of(bt, ntiles, g)];
-  const uint32_t sz = size[parent[g]];
-  double e = t.fe;
-  if (sz > 1) e = __dmul_rn(t.fe, __dadd_rn(1.15, __dmul_rn(0.18, static_cast<double>((sz < 6 ? sz : 6) - 1))));
-  exp64[g] = e;
+  const unsigned m = __ballot_sync(0xffffffffu, root);
+  if ((threadIdx.x & 31) == 0 && m) atomicAdd(clumps, static_cast<unsigned long long>(__popc(m)));
 }
 
 // ---- scan bins (per tile grid of bin_px x bin_px pixels) ----
@@ -471,7 +481,7 @@ struct fg_batch {
   unsigned long long npcells = 0;
   DBuf<float> exposure, d_neg;
   DBuf<unsigned long long> counter;
-  DBuf<unsigned long long> dstats;  // [0] transport hits, [1] scan FP64 fallbacks, [2] scan hits
+  DBuf<unsigned long long> dstats;  // [0] transport hits, [1] scan FP64 fallbacks, [2] scan hits, [3] clumps
   DBuf<unsigned char> cub_tmp;
   size_t cub_bytes = 0;
   unsigned long long ncells = 0, nslots = 0, ncap = 0, nbins = 0, item_cap = 0, photons = 0, rays = 0;
@@ -718,7 +728,8 @@ static void stage_develop(fg_batch* B, cudaStream_t st) {
                               B->devlist.p, B->devscan.p + B->ncap, e->d_err);
   FG_CUDA(cudaMemsetAsync(B->size.p, 0, B->ncap * sizeof(uint32_t), st));
   k_roots_b<<<G, 256, 0, st>>>(B->ncap, B->developed.p, B->parent.p, B->size.p, e->d_err);
-  k_finalize_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->developed.p, B->parent.p, B->size.p, B->exp64.p);
+  k_finalize_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->developed.p, B->parent.p, B->size.p, B->exp64.p,
+                                  B->dstats.p + 3);
   FG_CUDA(cudaGetLastError());
 }
 
@@ -1202,6 +1213,10 @@ fg_status fg_batch_wait(fg_batch* b, fg_batch_stats* stats) {
     s.hits = ds[0];
     s.scan_fallbacks = ds[1];
     s.scan_hits = ds[2];
+    s.clumps = ds[3];
+    uint32_t ndev = 0;  // the exclusive scan of the developed flags ends with their total
+    FG_CUDA(cudaMemcpy(&ndev, b->devscan.p + b->ncap, sizeof(ndev), cudaMemcpyDeviceToHost));
+    s.developed = ndev;
     s.rays = b->rays;
     s.pixels = b->out_total;
     s.transport_threads = b->tr_threads;

@@ -748,6 +748,8 @@ void render_layers(fg_engine* e, std::vector<Layer>& layers, const std::vector<c
     ok(e, fg_batch_wait(b, &bs));
     if (rep) {
       rep->total_crystals += bs.crystals;
+      rep->developed_crystals += bs.developed;
+      rep->total_clumps += bs.clumps;
       rep->photons += bs.photons;
     }
     first = last;

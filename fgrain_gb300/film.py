@@ -63,12 +63,17 @@ class FilmRenderOptions:
 
 @dataclass
 class ImageProcessReport:
+    """image_pipeline.rs:97-105, plus the photons launched and the device stage times (``extra``).
+    Totals are summed over all tiles of all layers (the reference reports a colour render as its
+    red layer's totals times three)."""
     input_resolution: tuple
     output_resolution: tuple
     total_tiles: int
     total_crystals: int
-    photons: int
+    developed_crystals: int
+    total_clumps: int
     elapsed_seconds: float
+    photons: int = 0
     extra: dict = field(default_factory=dict)
 
 
@@ -111,7 +116,7 @@ def render_film(image, options: FilmRenderOptions | None = None, engine=None):
     rep = _abi.fg_film_report()
     _run(engine, "fg_render_film", _u8(img), w, h, ch, C.byref(co), _u8(out), C.byref(rep))
     return ImageProcessReport((rep.in_w, rep.in_h), (rep.out_w, rep.out_h), rep.total_tiles, rep.total_crystals,
-                              rep.photons, rep.elapsed_seconds,
+                              rep.developed_crystals, rep.total_clumps, rep.elapsed_seconds, rep.photons,
                               {"prep_ms": rep.prep_ms, "tiles_ms": rep.tiles_ms, "finish_ms": rep.finish_ms}), out
 
 

@@ -257,10 +257,11 @@ typedef struct fg_film_options {
                               Larger images run as several batches, with identical results. */
 } fg_film_options;
 
-typedef struct fg_film_report {  /* ImageProcessReport (src/image_pipeline.rs:103-113) */
+typedef struct fg_film_report {  /* ImageProcessReport (src/image_pipeline.rs:97-105) */
   uint32_t in_w, in_h, out_w, out_h;
   uint64_t total_tiles, total_crystals, photons;
   double elapsed_seconds;
+  uint64_t developed_crystals, total_clumps;
   /* device time (CUDA events) of the image stages before the tiles (resize, gate, PSF), of the
    * tile batches (gather, run, density copy) and of the finish (blend to u8, downscale) */
   double prep_ms, tiles_ms, finish_ms;
@@ -378,6 +379,8 @@ typedef struct fg_batch_stats {
   uint64_t scan_hits;       /* scanner ray-crystal hits */
   uint64_t scan_fallbacks;  /* scanner decisions taken in FP64 */
   uint32_t transport_threads, transport_blocks, scan_bin_px, graph, kernel_launches, _pad;
+  uint64_t developed;       /* developed crystals (development.rs:79-84) */
+  uint64_t clumps;          /* clumps: connected components of developed crystals (development.rs:107-108) */
 } fg_batch_stats;
 
 fg_status fg_batch_create(fg_engine* e, const fg_tile_params* tiles, uint32_t ntiles,
@@ -465,6 +468,16 @@ typedef struct fg_device_crystals {
 fg_status fg_scan_crystals_static(const fg_device_crystals* crystals, const fg_emulsion_cfg* film,
                                   const fg_scan_cfg* cfg, uint64_t seed, float* out, uint8_t* image8,
                                   void* stream, char* message, size_t message_len);
+
+/* ---- Host helper of the command-line tool (no GPU involved) ---- */
+
+/* Reverses the PNG row filters (ISO/IEC 15948:2003 section 9) in place, for the tool that reads
+ * photographs the way image::open does (src/image_pipeline.rs:1141, the image crate's PNG codec):
+ * rows holds h scanlines of 1 + stride bytes (the filter-type byte, then the filtered bytes); bpp
+ * is the bytes per complete pixel (1 for bit depths below 8).  On return every filter byte is 0
+ * and the scanlines hold the reconstructed bytes.  An unknown filter type gives
+ * FG_ERR_INVALID_ARG (rows before it are already reconstructed). */
+fg_status fg_png_unfilter(uint8_t* rows, uint32_t h, uint32_t stride, uint32_t bpp);
 
 #ifdef __cplusplus
 }

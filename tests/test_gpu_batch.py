@@ -100,11 +100,17 @@ def test_pipeline_matches_oracle_on_the_same_crystals(engine):
     b = fg.Batch([p], engine)
     b.set_exposure([tile])
     b.run()
-    b.wait()
+    st = b.wait()
     d_dev = b.density()[0]
     c = b.tile_crystals(0)
     cfg = reference_cfg("tri-x", p.film_w, p.film_h)
     cr = orc.Crystals(c["pos"], c["dims"], c["quat"], c["sensitivity"], c["morphology"])
+    # The batch's development totals against the oracle's development of the device's own counts.
+    crd = cr.copy()
+    crd.latent[:] = c["counts"]
+    rd = orc.develop(crd, fg.DevelopmentConfig(4, p.filament_expansion, p.clumping_proximity_factor, 0.85))
+    assert st["developed"] == int(c["developed"].sum()) == rd["developed_crystals"] > 100
+    assert st["clumps"] == rd["total_clumps"]
     orc.expose(cr, cfg, tile, fg.ExposureConfig(6.0, 0.12, 1.3, 48), p.seed + 1, orc.CANONICAL)
     same = (cr.latent == c["counts"]).mean()
     assert same > 0.99, same

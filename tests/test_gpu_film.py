@@ -185,6 +185,8 @@ def test_render_in_several_batches_equals_one_batch(engine):
         rep, many = film.render_film(rgb, small, engine)
         np.testing.assert_array_equal(one, many)
         assert rep.total_crystals == rep1.total_crystals and rep.total_tiles == rep1.total_tiles
+        assert (rep.developed_crystals, rep.total_clumps) == (rep1.developed_crystals, rep1.total_clumps)
+    assert 0 < rep1.total_clumps <= rep1.developed_crystals < rep1.total_crystals
 
 
 @pytest.mark.parametrize("shape", [(1, 1), (1, 7), (5, 3), (49, 1)])
