@@ -361,7 +361,7 @@ def run_ours(args):
             "gpu_launches": stats["kernel_launches"] * args.steps,
             "roofline": {"bound": "hbm", "kernel": "k_transport", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                         "traffic": profile_traffic() if args.workload == "c2" else None,
+                         "traffic": profile_traffic() if args.workload == "c2" and full else None,
                          "alg_bytes_per_launch": alg_bytes},
             "clocks": clocks,
         }
