@@ -116,6 +116,35 @@ __device__ __forceinline__ void collapse_node4(const Node* __restrict__ nodes, i
   };
   expand(nd.d.x, nd.a.x, nd.a.y, nd.a.z, nd.a.w, nd.b.x, nd.b.y);
   expand(nd.d.y, nd.b.z, nd.b.w, nd.c.x, nd.c.y, nd.c.z, nd.c.w);
+  // A slot left free by a leaf child takes the two children of the internal grandchild with the
+  // largest box surface: every internal entry stays at least two levels down, so the walk still
+  // descends two levels per four-wide node and its stack bound is unchanged.
+  while (k < 4) {
+    int best = -1;
+    float barea = -1.0f;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (j < k && r[j] >= 0) {
+        const float ex = v[j][3] - v[j][0], ey = v[j][4] - v[j][1], ez = v[j][5] - v[j][2];
+        const float area = ex * ey + ey * ez + ez * ex;
+        if (area > barea) {
+          barea = area;
+          best = j;
+        }
+      }
+    }
+    if (best < 0) break;
+    const Node ch = nodes[r[best]];
+    if (ch.d.y == INT32_MIN) break;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (j == best) {
+        v[j][0] = ch.a.x; v[j][1] = ch.a.y; v[j][2] = ch.a.z; v[j][3] = ch.a.w; v[j][4] = ch.b.x; v[j][5] = ch.b.y;
+        r[j] = ch.d.x;
+      }
+    }
+    add(ch.d.y, ch.b.z, ch.b.w, ch.c.x, ch.c.y, ch.c.z, ch.c.w);
+  }
   for (; k < 4; ++k) {
     for (int j = 0; j < 6; ++j) v[k][j] = 0.0f;
     r[k] = INT32_MIN;
