@@ -8,7 +8,6 @@
 namespace fg {
 
 enum : uint32_t {
-  TAG_PICK = 0x50490000u,
   TAG_CAND = 0x43410000u,
   TAG_SEED = 0x53450000u,
   TAG_THIN = 0x54480000u,
@@ -269,10 +268,15 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 8) k_bridson(const SynthTile* 
       break;
     }
     // One Bridson step per warp on a random active point (poisson.rs:59-129): 30 candidates in
-    // the shell [r, 2r], one per lane; the lowest valid lane is the step's winner.
-    // Every lane draws the pick (no shared-memory round trip); lane 0 records it for the retirement.
-    const P4 rp = philox(static_cast<uint32_t>(iter), static_cast<uint32_t>(warp), colkey, TAG_PICK, t.k0, t.k1);
-    const int pick = static_cast<int>((static_cast<unsigned long long>(rp.x) * static_cast<unsigned>(nact)) >> 32);
+    // the shell [r, 2r], one per lane; the lowest valid lane is the step's winner.  Every lane
+    // draws one Philox block of the warp's stream: lanes 0-29 place the candidates and lane 31's
+    // draw picks the active point (shuffled to the warp); lane 0 records the pick for the
+    // retirement.
+    static_assert(SYN_K < 32, "lane 31 draws the pick");
+    const P4 r = philox(static_cast<uint32_t>(iter), static_cast<uint32_t>(warp * 32 + lane), colkey, TAG_CAND,
+                        t.k0, t.k1);
+    const uint32_t rpick = __shfl_sync(0xffffffffu, r.x, 31);
+    const int pick = static_cast<int>((static_cast<unsigned long long>(rpick) * static_cast<unsigned>(nact)) >> 32);
     if (lane == 0) s_pick[warp] = pick;
     const int pr = active[pick];
     const uint32_t pw = grid[pr];
@@ -283,8 +287,6 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 8) k_bridson(const SynthTile* 
     bool valid = false;
     int X = 0, Y = 0, Z = 0, rb = 0;
     if (lane < SYN_K) {
-      const P4 r = philox(static_cast<uint32_t>(iter), static_cast<uint32_t>(warp * 32 + lane), colkey, TAG_CAND,
-                          t.k0, t.k1);
       const float u = uf(r.x);
       const float ct = uf(r.y) * 2.0f - 1.0f;
       const float st = sqrtf(fmaxf(1.0f - ct * ct, 0.0f));
