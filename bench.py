@@ -337,10 +337,8 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": "Mpx/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": (("" if full else f"first {len(params)} tiles of ") +
-                                    "C2: 1024x1024 blurred-noise luminance (sigma 16, seed 1, gamma 2.2), tri-x, "
-                                    "grain 2.4 px, push 0, supersample 2 (2048^2 internal, 49 tiles), batched "
-                                    "graph path") if args.workload == "c2" else
+            "config": {"workload": (("" if full else f"first {len(params)} tiles of ") + C2_WORKLOAD +
+                                    ", batched graph path") if args.workload == "c2" else
                                    "C3: 64 square images, sides log-uniform 64-512 px, tri-x / t-max / hp5, push "
                                    "0-3, supersample 1-4 (master seed 0), all tiles in one autotuned batch",
                        "tiles": len(params),
@@ -464,6 +462,10 @@ def run_fast(args):
             "gpu_launches": 5 * args.steps, "clocks": ck.summary()}))
 
 
+C2_WORKLOAD = ("C2: 1024x1024 blurred-noise luminance (sigma 16, seed 1, gamma 2.2), tri-x, grain 2.4 px, push 0, "
+               "supersample 2 (2048^2 internal, 49 tiles)")
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -485,10 +487,10 @@ def run_reference(args):
               f"(faithful hit rule; the Rust reference cannot be built here), tiles in parallel on {threads} "
               f"threads; output Mpx/s scaled by tile pixels")
     print(json.dumps({
-        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mpx/s", "n_gpus": 0, "steps": args.steps,
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mpx/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "C2 (see ours)", "tiles_per_step": n},
+        "config": {"workload": C2_WORKLOAD + ", reference CPU path (no GPU used)", "tiles_per_step": n},
         "cpu_baseline": {"value": value, "unit": "Mpx/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "Mpx/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
