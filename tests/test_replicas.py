@@ -68,10 +68,11 @@ def test_reference_arm_line_shape(monkeypatch):
     monkeypatch.setattr("builtins.print", lambda s, *a, **k: lines.append(s))
 
     class A:
-        steps, warmup = 2, 1
+        steps, warmup, gpus = 2, 1, 2
 
     monkeypatch.setenv("RANK", "0")
     bench.run_reference(A())
     d = json.loads(lines[-1])
     assert d["impl"] == "reference" and d["unit"] == "Mpx/s" and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
+    assert d["n_gpus"] == 2 and d["config"]["workload"].startswith(bench.C2_WORKLOAD)
