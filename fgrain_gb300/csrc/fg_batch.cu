@@ -526,10 +526,14 @@ static void derive_tile(const fg_tile_params& p, SynthTile& s, TileDesc& t, Scan
   s.XW = static_cast<uint32_t>(std::ceil(W * SYN_Q / cell));
   s.YW = static_cast<uint32_t>(std::ceil(H * SYN_Q / cell));
   s.ZW = static_cast<uint32_t>(std::ceil(Dd * SYN_Q / cell));
-  uint32_t bits = 0;
+  uint32_t bits = 0, zb = 0;
   while ((1u << bits) < std::max(s.gw, s.gh)) ++bits;
-  s.slot_bits = bits;
-  s.slots = (1u << (2 * bits)) * s.gd;
+  while ((1u << zb) < s.gd) ++zb;
+  s.brick_bits = zb;
+  s.slot_bits = bits > zb ? bits - zb : 0;
+  const unsigned long long slots = (1ull << (2 * s.slot_bits)) << (3 * zb);
+  FG_REQUIRE(slots < (1ull << 31), "tile too large for the synthesis grid");
+  s.slots = static_cast<uint32_t>(slots);
   const double vol = W * H * Dd;
   const double cap = std::min(0.8 * vol / (r * r * r) + 64.0, static_cast<double>(s.gw) * s.gh * s.gd);
   s.ccap = static_cast<uint32_t>(cap);

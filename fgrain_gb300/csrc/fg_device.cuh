@@ -364,6 +364,15 @@ __host__ __device__ inline uint32_t morton2_compact(uint32_t v) {
   v = (v | (v >> 8)) & 0x0000ffffu;
   return v;
 }
+// Every third bit of v from bit 0 (the inverse of a 3D Morton interleave, 10 bits out).
+__host__ __device__ inline uint32_t morton3_compact(uint32_t v) {
+  v &= 0x09249249u;
+  v = (v | (v >> 2)) & 0x030c30c3u;
+  v = (v | (v >> 4)) & 0x0300f00fu;
+  v = (v | (v >> 8)) & 0x030000ffu;
+  v = (v | (v >> 16)) & 0x000003ffu;
+  return v;
+}
 
 // Error word bits written by kernels (read back by the host after each call).  The error record
 // is four words: the bits, then (for ERR_BAD_INDEX) the site and two values of the first failed

@@ -498,17 +498,27 @@ __global__ void k_thin(const SynthTile* __restrict__ tiles, uint32_t* __restrict
     if ((tc[lin] & OCC) && uf(philox(lin, 0, 0, TAG_THIN, t.k0, t.k1).x) < p) tc[lin] = 0;
 }
 
-// Occupancy of each compaction slot: slot = morton2(x, y) * gd + z.
+// Cell of compaction slot sl: the brick (2D Morton over the high x, y bits) in the bits above
+// 3 * brick_bits, the cell inside it (3D Morton, x lowest) below.
+__device__ __forceinline__ void slot_cell(const SynthTile& t, uint32_t sl, uint32_t& x, uint32_t& y, uint32_t& z) {
+  const uint32_t L = t.brick_bits;
+  const uint32_t lo = sl & ((1u << (3 * L)) - 1u), hi = sl >> (3 * L);
+  x = (morton2_compact(hi) << L) | morton3_compact(lo);
+  y = (morton2_compact(hi >> 1) << L) | morton3_compact(lo >> 1);
+  z = morton3_compact(lo >> 2);
+}
+
+// Occupancy of each compaction slot (slot_cell).
 // blockIdx.y is the tile.
 __global__ void k_slot_flags(const SynthTile* __restrict__ tiles, const uint32_t* __restrict__ cells,
                              uint32_t* flags) {
   const SynthTile& t = tiles[blockIdx.y];
   const uint32_t* tc = cells + t.cell_base;
   for (uint32_t sl = blockIdx.x * blockDim.x + threadIdx.x; sl < t.slots; sl += gridDim.x * blockDim.x) {
-    const uint32_t m2 = sl / t.gd, z = sl % t.gd;
-    const uint32_t x = morton2_compact(m2), y = morton2_compact(m2 >> 1);
+    uint32_t x, y, z;
+    slot_cell(t, sl, x, y, z);
     uint32_t f = 0;
-    if (x < t.gw && y < t.gh) f = (tc[(static_cast<size_t>(z) * t.gh + y) * t.gw + x] & OCC) ? 1u : 0u;
+    if (x < t.gw && y < t.gh && z < t.gd) f = (tc[(static_cast<size_t>(z) * t.gh + y) * t.gw + x] & OCC) ? 1u : 0u;
     flags[t.slot_base + sl] = f;
   }
 }
@@ -528,8 +538,8 @@ __global__ void k_emit(const SynthTile* __restrict__ tiles, const uint32_t* __re
       atomicOr(err, ERR_LIST_OVERFLOW);
       continue;
     }
-    const uint32_t m2 = sl / t.gd, z = sl % t.gd;
-    const uint32_t x = morton2_compact(m2), y = morton2_compact(m2 >> 1);
+    uint32_t x, y, z;
+    slot_cell(t, sl, x, y, z);
     const uint32_t lin = (z * t.gh + y) * t.gw + x;
     const uint32_t w = cells[t.cell_base + lin];
     const float px = static_cast<float>(static_cast<int>(x) * SYN_Q + static_cast<int>(w & 1023u)) * (t.cell / SYN_Q);

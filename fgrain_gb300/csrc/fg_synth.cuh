@@ -52,7 +52,12 @@ struct __align__(16) SynthTile {
   uint32_t gw, gh, gd;           // cell grid
   uint32_t nbx, nby;             // columns per axis
   uint32_t XW, YW, ZW;           // exclusive bounds of fixed-point coordinates
-  uint32_t slot_bits, slots;     // 2D Morton bits per axis, slots = 4^bits * gd
+  // Compaction slots in brick order: bricks of 2^brick_bits cells per axis (brick_bits covers the
+  // depth), bricks in 2D Morton order (slot_bits per axis), cells in 3D Morton order inside a
+  // brick.  Slot order is crystal order and the LBVH key, so the tree's lower levels group
+  // compact 3D blocks of crystals, not full-depth columns.
+  uint32_t slot_bits, slots;     // slots = 4^slot_bits * 8^brick_bits
+  uint32_t brick_bits;
   uint32_t ccap;                 // crystal capacity
   uint32_t target;               // Bridson-expected crystal count
   uint32_t k0, k1;               // synthesis key (tile seed)
