@@ -121,7 +121,7 @@ class fg_batch_stats(C.Structure):
                 ("scan_fallbacks", C.c_uint64), ("transport_threads", C.c_uint32),
                 ("transport_blocks", C.c_uint32), ("scan_bin_px", C.c_uint32), ("graph", C.c_uint32),
                 ("kernel_launches", C.c_uint32), ("_pad", C.c_uint32), ("developed", C.c_uint64),
-                ("clumps", C.c_uint64)]
+                ("clumps", C.c_uint64), ("cells", C.c_uint64), ("bridson_ms", C.c_double)]
 
 
 class fg_device_crystals(C.Structure):

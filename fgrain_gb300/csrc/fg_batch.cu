@@ -494,7 +494,7 @@ struct fg_batch {
   bool tune_pending = false;  // autotune (and capture) at the first run, once exposure is set
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  cudaEvent_t ev[7] = {};
+  cudaEvent_t ev[9] = {};  // stage marks 0-5, the timing start 6, k_bridson's end 7 and start 8
   fg_batch_stats stats{};
 
   ~fg_batch() {
@@ -674,13 +674,17 @@ static void cub_scan(fg_batch* B, const uint32_t* in, uint32_t* out, unsigned lo
 }
 
 // Stages; each only enqueues work on `st`.
-static void stage_synth(fg_batch* B, cudaStream_t st) {
+static void mark(cudaEvent_t ev, cudaStream_t st, bool capturing);
+
+static void stage_synth(fg_batch* B, cudaStream_t st, bool capturing = false) {
   fg_engine* e = B->e;
   const int nt = static_cast<int>(B->ntiles);
   FG_CUDA(cudaMemsetAsync(B->dstats.p, 0, 4 * sizeof(unsigned long long), st));
   FG_CUDA(cudaMemsetAsync(B->cells.p, 0, B->ncells * sizeof(uint32_t), st));
   FG_CUDA(cudaMemsetAsync(B->npts.p, 0, B->ntiles * sizeof(uint32_t), st));
+  mark(B->ev[8], st, capturing);
   launch_bridson(B->d_syn.p, nt, B->cols, B->gdmax, B->cells.p, B->npts.p, B->coldone.p, e->d_err, st);
+  mark(B->ev[7], st, capturing);
   FG_CUDA(cudaMemsetAsync(B->flags.p + B->nslots, 0, sizeof(uint32_t), st));
   launch_synth_post(B->d_syn.p, nt, B->maxcells, B->maxslots, B->cells.p, B->npts.p, B->flags.p, st);
   cub_scan(B, B->flags.p, B->slot_scan.p, B->nslots + 1, st);
@@ -761,7 +765,7 @@ static void mark(cudaEvent_t ev, cudaStream_t st, bool capturing) {
 
 static void enqueue_all(fg_batch* B, cudaStream_t st, bool capturing = false) {
   mark(B->ev[0], st, capturing);
-  stage_synth(B, st);
+  stage_synth(B, st, capturing);
   stage_photon_order(B, st);
   mark(B->ev[1], st, capturing);
   stage_bvh(B, st);
@@ -1203,6 +1207,7 @@ fg_status fg_batch_wait(fg_batch* b, fg_batch_stats* stats) {
     check_error_word(b->e);
     fg_batch_stats s{};
     s.synth_ms = ev_ms(b->ev[0], b->ev[1]);
+    s.bridson_ms = ev_ms(b->ev[8], b->ev[7]);
     s.bvh_ms = ev_ms(b->ev[1], b->ev[2]);
     s.transport_ms = ev_ms(b->ev[2], b->ev[3]);
     s.develop_ms = ev_ms(b->ev[3], b->ev[4]);
@@ -1221,6 +1226,7 @@ fg_status fg_batch_wait(fg_batch* b, fg_batch_stats* stats) {
     uint32_t ndev = 0;  // the exclusive scan of the developed flags ends with their total
     FG_CUDA(cudaMemcpy(&ndev, b->devscan.p + b->ncap, sizeof(ndev), cudaMemcpyDeviceToHost));
     s.developed = ndev;
+    s.cells = b->ncells;
     s.rays = b->rays;
     s.pixels = b->out_total;
     s.transport_threads = b->tr_threads;

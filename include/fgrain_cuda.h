@@ -381,6 +381,8 @@ typedef struct fg_batch_stats {
   uint32_t transport_threads, transport_blocks, scan_bin_px, graph, kernel_launches, _pad;
   uint64_t developed;       /* developed crystals (development.rs:79-84) */
   uint64_t clumps;          /* clumps: connected components of developed crystals (development.rs:107-108) */
+  uint64_t cells;           /* synthesis grid cells of all tiles (r_min / sqrt(3) edge, poisson.rs:25-31) */
+  double bridson_ms;        /* the Bridson kernel alone (the done-flag clear and its launch; CUDA events) */
 } fg_batch_stats;
 
 fg_status fg_batch_create(fg_engine* e, const fg_tile_params* tiles, uint32_t ntiles,
