@@ -20,10 +20,10 @@ namespace fg {
 // Production kernel with lane refill: each loop turn every lane with a live packet runs one bounce
 // (its LBVH walk, then absorption and the move or scatter); lanes whose packet died take the next
 // photon of the position-ordered queue, so the warp stays full until the queue is empty.
-// Launch bounds of 5 blocks of 256 per SM (48 registers, the rest spilled to L1): the walk is
-// latency-bound; with the four-wide tree and speculative traversal 40 resident warps beat 48
-// (15.4 against 16.4 ms on the 1024x1024 ss2 workload).
-__global__ void __launch_bounds__(256, 5) k_transport(const TileDesc* __restrict__ tiles, int ntiles,
+// Launch bounds of 4 blocks of 256 per SM (64 registers): the walk is latency-bound, and with
+// the brick-ordered tree 32 resident warps with fewer spills beat 40 at 48 registers and 48 at
+// 40 (10.9 against 11.1 and 13.1 ms on the 1024x1024 ss2 workload).
+__global__ void __launch_bounds__(256, 4) k_transport(const TileDesc* __restrict__ tiles, int ntiles,
                                                      unsigned long long total, const uint32_t* __restrict__ order,
                                                      unsigned long long* next, uint32_t* err,
                                                      unsigned long long* stats) {
