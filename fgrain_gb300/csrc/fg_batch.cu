@@ -70,7 +70,7 @@ __global__ void k_set_n(const SynthTile* syn, int ntiles, const uint32_t* slot_s
                         ScanTile* sc, uint32_t* ncrys) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntiles) return;
-  const uint32_t n = slot_scan[syn[t].slot_base + syn[t].slots] - slot_scan[syn[t].slot_base];
+  const uint32_t n = slot_scan[syn[t].slot_base + (1ull << (2 * syn[t].slot_bits))] - slot_scan[syn[t].slot_base];
   const uint32_t nn = min(n, syn[t].ccap);
   bt[t].n = nn;
   bt[t].max_base = 0.0;
@@ -463,9 +463,9 @@ struct fg_batch {
   DBuf<TileDesc> d_td;
   DBuf<ScanTile> d_sc;
   DBuf<BTile> d_bt;
-  DBuf<uint32_t> cells, npts, flags, slot_scan, ncrys;
+  DBuf<uint32_t> cells, npts, flags, slot_scan, ncrys;  // flags: points per brick, slot_scan: their exclusive sum
   DBuf<uint32_t> coldone;  // one flag per synthesis column
-  unsigned long long maxcells = 0, maxslots = 0;  // the largest tile's cells and Morton slots
+  unsigned long long maxcells = 0, maxslots = 0;  // the largest tile's cells and bricks
   DBuf<float4> A, Q, D;
   DBuf<uint64_t> keys;
   DBuf<Node> nodes;
@@ -484,7 +484,7 @@ struct fg_batch {
   DBuf<unsigned long long> dstats;  // [0] transport hits, [1] scan FP64 fallbacks, [2] scan hits, [3] clumps
   DBuf<unsigned char> cub_tmp;
   size_t cub_bytes = 0;
-  unsigned long long ncells = 0, nslots = 0, ncap = 0, nbins = 0, item_cap = 0, photons = 0, rays = 0;
+  unsigned long long ncells = 0, nslots = 0, ncap = 0, nbins = 0, item_cap = 0, photons = 0, rays = 0;  // nslots: bricks
   unsigned long long exp_total = 0, out_total = 0;
   int gdmax = 0;
   unsigned cols[4] = {0, 0, 0, 0};
@@ -860,9 +860,9 @@ static void plan(fg_batch* B, const fg_batch_options* opt) {
       colc[c] += cxn * cyn;
     }
     cb += static_cast<unsigned long long>(s.gw) * s.gh * s.gd;
-    sb += s.slots;
+    sb += 1ull << (2 * s.slot_bits);  // bricks
     B->maxcells = std::max<unsigned long long>(B->maxcells, static_cast<unsigned long long>(s.gw) * s.gh * s.gd);
-    B->maxslots = std::max<unsigned long long>(B->maxslots, s.slots);
+    B->maxslots = std::max<unsigned long long>(B->maxslots, 1ull << (2 * s.slot_bits));
     cap += s.ccap;
     B->td[i].photon_base = pb;
     pb += B->td[i].P;
@@ -982,9 +982,9 @@ unsigned long long tile_footprint(const fg_tile_params& p, unsigned long long* s
   while ((1u << bits) < static_cast<uint32_t>(std::ceil(side))) ++bits;
   const unsigned long long px = static_cast<unsigned long long>(p.width_px) * p.height_px;
   // Per crystal slot: records 48, key 8, nodes 64 + 128, links and flags 36, expansion 8, scan
-  // prep 128, bin entries 32 (plus slack); cells 4 B; Morton slots 8 B; photon order; images.
+  // prep 128, bin entries 32 (plus slack); cells 4 B; bricks 8 B; photon order; images.
   return static_cast<unsigned long long>(s.ccap) * 480ull + static_cast<unsigned long long>(s.gw) * s.gh * s.gd * 4ull +
-         static_cast<unsigned long long>(s.slots) * 8ull + static_cast<unsigned long long>(t.P) * 4ull +
+         (8ull << (2 * s.slot_bits)) + static_cast<unsigned long long>(t.P) * 4ull +
          (1ull << (2 * bits)) * 12ull + px * 8ull + 4096ull;
 }
 
@@ -1033,19 +1033,20 @@ fg_status fg_emulsion_synthesize(fg_engine* e, const fg_emulsion_cfg* cfg, uint6
     FG_CUDA(cudaEventRecord(e->timer.ev[0], st));
     DBuf<SynthTile> d_syn(1, st);
     FG_CUDA(cudaMemcpyAsync(d_syn.p, &s, sizeof(SynthTile), cudaMemcpyHostToDevice, st));
-    DBuf<uint32_t> cells(ncells, st), npts(1, st), flags(s.slots + 1ull, st), scan(s.slots + 1ull, st);
+    const unsigned long long nbr = 1ull << (2 * s.slot_bits);  // bricks
+    DBuf<uint32_t> cells(ncells, st), npts(1, st), flags(nbr + 1ull, st), scan(nbr + 1ull, st);
     DBuf<float4> A(s.ccap, st), Q(s.ccap, st), D(s.ccap, st);
     DBuf<uint64_t> keys(s.ccap, st);
     FG_CUDA(cudaMemsetAsync(cells.p, 0, ncells * sizeof(uint32_t), st));
     FG_CUDA(cudaMemsetAsync(npts.p, 0, sizeof(uint32_t), st));
     DBuf<uint32_t> coldone(std::max(cols[0] + cols[1] + cols[2] + cols[3], 1u), st);
     launch_bridson(d_syn.p, 1, cols, gdmax, cells.p, npts.p, coldone.p, e->d_err, st);
-    FG_CUDA(cudaMemsetAsync(flags.p + s.slots, 0, sizeof(uint32_t), st));
-    launch_synth_post(d_syn.p, 1, ncells, s.slots, cells.p, npts.p, flags.p, st);
-    exclusive_scan_u32(flags.p, scan.p, s.slots + 1ull, st);
-    launch_emit(d_syn.p, 1, s.slots, cells.p, scan.p, A.p, Q.p, D.p, keys.p, e->d_err, st);
+    FG_CUDA(cudaMemsetAsync(flags.p + nbr, 0, sizeof(uint32_t), st));
+    launch_synth_post(d_syn.p, 1, ncells, nbr, cells.p, npts.p, flags.p, st);
+    exclusive_scan_u32(flags.p, scan.p, nbr + 1ull, st);
+    launch_emit(d_syn.p, 1, nbr, cells.p, scan.p, A.p, Q.p, D.p, keys.p, e->d_err, st);
     uint32_t n = 0;
-    FG_CUDA(cudaMemcpyAsync(&n, scan.p + s.slots, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    FG_CUDA(cudaMemcpyAsync(&n, scan.p + nbr, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     FG_CUDA(cudaStreamSynchronize(st));
     check_error_word(e);
     n = std::min(n, s.ccap);

@@ -13,17 +13,6 @@ enum : uint32_t {
   TAG_THIN = 0x54480000u,
 };
 
-__device__ __forceinline__ int find_tile_ull(const SynthTile* tiles, int ntiles, unsigned long long v,
-                                             int which) {
-  int lo = 0, hi = ntiles - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    const unsigned long long b = which == 0 ? tiles[mid].cell_base : (which == 1 ? tiles[mid].slot_base : tiles[mid].cbase);
-    if (b <= v) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
-
 // True when the cell word w holds a point closer than r to the candidate at (lx, ly, lz) (fixed
 // point, relative to the candidate's cell) from the cell at offset (dx, dy, dz).
 __device__ __forceinline__ bool syn_conflict(uint32_t w, int dx, int dy, int dz, int lx, int ly, int lz) {
@@ -508,79 +497,126 @@ __device__ __forceinline__ void slot_cell(const SynthTile& t, uint32_t sl, uint3
   z = morton3_compact(lo >> 2);
 }
 
-// Occupancy of each compaction slot (slot_cell).
-// blockIdx.y is the tile.
-__global__ void k_slot_flags(const SynthTile* __restrict__ tiles, const uint32_t* __restrict__ cells,
-                             uint32_t* flags) {
+// Points per brick (the compaction unit): one block per brick counts the occupied cells of its
+// region, read row by row.  blockIdx.y is the tile.
+__global__ void k_brick_count(const SynthTile* __restrict__ tiles, const uint32_t* __restrict__ cells,
+                              uint32_t* counts) {
   const SynthTile& t = tiles[blockIdx.y];
+  const uint32_t L = t.brick_bits, E = 1u << L;
+  const uint32_t nbricks = 1u << (2 * t.slot_bits);
   const uint32_t* tc = cells + t.cell_base;
-  for (uint32_t sl = blockIdx.x * blockDim.x + threadIdx.x; sl < t.slots; sl += gridDim.x * blockDim.x) {
-    uint32_t x, y, z;
-    slot_cell(t, sl, x, y, z);
-    uint32_t f = 0;
-    if (x < t.gw && y < t.gh && z < t.gd) f = (tc[(static_cast<size_t>(z) * t.gh + y) * t.gw + x] & OCC) ? 1u : 0u;
-    flags[t.slot_base + sl] = f;
+  __shared__ uint32_t s_sum[32];
+  for (uint32_t b = blockIdx.x; b < nbricks; b += gridDim.x) {
+    const uint32_t xb = morton2_compact(b) << L, yb = morton2_compact(b >> 1) << L;
+    const uint32_t ex = xb < t.gw ? min(E, t.gw - xb) : 0u, ey = yb < t.gh ? min(E, t.gh - yb) : 0u;
+    const uint32_t ez = min(E, t.gd), n = ex * ey * ez;
+    uint32_t c = 0;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+      const uint32_t x = xb + i % ex, y = yb + (i / ex) % ey, z = i / (ex * ey);
+      c += (tc[(static_cast<size_t>(z) * t.gh + y) * t.gw + x] & OCC) ? 1u : 0u;
+    }
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) s_sum[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t tot = 0;
+      for (uint32_t w = 0; w < (blockDim.x + 31) / 32; ++w) tot += s_sum[w];
+      counts[t.slot_base + b] = tot;
+    }
+    __syncthreads();
   }
 }
 
-// Crystal k of a tile from its slot: position from the fixed-point cell word, attributes from the
-// tile's Philox stream keyed by the cell (emulsion.rs:162-200).
-// blockIdx.y is the tile.
+// Crystal k of a tile at compaction slot sl (cell x, y, z): position from the fixed-point cell
+// word, attributes from the tile's Philox stream keyed by the cell (emulsion.rs:162-200).
+__device__ __forceinline__ void emit_crystal(const SynthTile& t, const uint32_t* __restrict__ cells, uint32_t sl,
+                                             uint32_t x, uint32_t y, uint32_t z, uint32_t k, float4* A, float4* Q,
+                                             float4* D, uint64_t* keys) {
+  const uint32_t lin = (z * t.gh + y) * t.gw + x;
+  const uint32_t w = cells[t.cell_base + lin];
+  const float px = static_cast<float>(static_cast<int>(x) * SYN_Q + static_cast<int>(w & 1023u)) * (t.cell / SYN_Q);
+  const float py = static_cast<float>(static_cast<int>(y) * SYN_Q + static_cast<int>((w >> 10) & 1023u)) * (t.cell / SYN_Q);
+  const float pz = static_cast<float>(static_cast<int>(z) * SYN_Q + static_cast<int>((w >> 20) & 1023u)) * (t.cell / SYN_Q);
+  const P4 r0 = philox(lin, 0, 0, TAG_ATTR, t.k0, t.k1);
+  const P4 r1 = philox(lin, 1, 0, TAG_ATTR, t.k0, t.k1);
+  // Two normals from one Box-Muller pair: radius (log-normal) and sensitivity.
+  const float bm = sqrtf(-2.0f * logf(1.0f - uf(r0.x)));
+  float s2, c2;
+  sincospif(2.0f * uf(r0.y), &s2, &c2);
+  const float radius = fminf(fmaxf(expf(t.mu + t.sg * bm * c2), 0.15f), t.rmax);
+  const float sens = fmaxf(t.base_sens + 0.15f * bm * s2, 0.1f);
+  float4 q, d;
+  if (t.morph == 1) {
+    // Tabular: thickness r / AR (>= 0.05), tilt +-0.17 rad about a random in-plane axis.
+    const float ht = fmaxf(radius / t.aspect, 0.05f);
+    const float tilt = uf(r0.z) * 0.34f - 0.17f;
+    float ax = uf(r0.w) * 2.0f - 1.0f, ay = uf(r1.x) * 2.0f - 1.0f;
+    const float n = rsqrtf(fmaxf(ax * ax + ay * ay, 1e-30f));
+    ax *= n;
+    ay *= n;
+    float sh, ch;
+    sincosf(0.5f * tilt, &sh, &ch);
+    q = make_float4(ax * sh, ay * sh, 0.0f, ch);
+    d = make_float4(radius, radius, ht, __int_as_float(1));
+  } else {
+    // Cubic / octahedral: UnitQuaternion::from_euler_angles(2 pi u1, pi u2, 2 pi u3).
+    float sr, cr, sp, cp, sy, cy;
+    sincospif(uf(r0.z), &sr, &cr);        // roll / 2 = pi u1
+    sincospif(0.5f * uf(r0.w), &sp, &cp); // pitch / 2 = pi u2 / 2
+    sincospif(uf(r1.x), &sy, &cy);        // yaw / 2 = pi u3
+    q = make_float4(sr * cp * cy - cr * sp * sy, cr * sp * cy + sr * cp * sy, cr * cp * sy - sr * sp * cy,
+                    cr * cp * cy + sr * sp * sy);
+    d = make_float4(radius, radius, radius, __int_as_float(t.morph));
+  }
+  const unsigned long long o = t.cbase + k;
+  A[o] = make_float4(px, py, pz, sens);
+  Q[o] = q;
+  D[o] = d;
+  keys[o] = sl;
+}
+
+// The crystals of each brick in slot order (slot_cell): the brick's slots are walked in chunks of
+// the block, a block-wide prefix sum of the occupied ones numbers them after the points of the
+// earlier bricks (scan: exclusive sum of k_brick_count).  blockIdx.y is the tile.
 __global__ void k_emit(const SynthTile* __restrict__ tiles, const uint32_t* __restrict__ cells,
                        const uint32_t* __restrict__ scan, float4* A, float4* Q, float4* D, uint64_t* keys,
                        uint32_t* err) {
   const SynthTile& t = tiles[blockIdx.y];
-  for (uint32_t sl = blockIdx.x * blockDim.x + threadIdx.x; sl < t.slots; sl += gridDim.x * blockDim.x) {
-    const unsigned long long i = t.slot_base + sl;
-    if (scan[i + 1] == scan[i]) continue;
-    const uint32_t k = scan[i] - scan[t.slot_base];
-    if (k >= t.ccap) {
-      atomicOr(err, ERR_LIST_OVERFLOW);
-      continue;
+  const uint32_t L = t.brick_bits;
+  const uint32_t nbricks = 1u << (2 * t.slot_bits), per = 1u << (3 * L);
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) / 32;
+  __shared__ uint32_t s_w[33];
+  for (uint32_t b = blockIdx.x; b < nbricks; b += gridDim.x) {
+    const unsigned long long bi = t.slot_base + b;
+    if (scan[bi + 1] == scan[bi]) continue;  // block-uniform
+    uint32_t k0 = scan[bi] - scan[t.slot_base];
+    const uint32_t xb = morton2_compact(b) << L, yb = morton2_compact(b >> 1) << L;
+    for (uint32_t c0 = 0; c0 < per; c0 += blockDim.x) {
+      const uint32_t lo = c0 + threadIdx.x;
+      const uint32_t x = xb | morton3_compact(lo), y = yb | morton3_compact(lo >> 1), z = morton3_compact(lo >> 2);
+      const bool occ = lo < per && x < t.gw && y < t.gh && z < t.gd &&
+                       (cells[t.cell_base + (static_cast<size_t>(z) * t.gh + y) * t.gw + x] & OCC);
+      const unsigned m = __ballot_sync(0xffffffffu, occ);
+      if (lane == 0) s_w[warp] = __popc(m);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        for (uint32_t w = 0; w < nw; ++w) {
+          const uint32_t v = s_w[w];
+          s_w[w] = acc;
+          acc += v;
+        }
+        s_w[32] = acc;
+      }
+      __syncthreads();
+      if (occ) {
+        const uint32_t k = k0 + s_w[warp] + __popc(m & ((1u << lane) - 1u));
+        if (k < t.ccap) emit_crystal(t, cells, (b << (3 * L)) | lo, x, y, z, k, A, Q, D, keys);
+        else atomicOr(err, ERR_LIST_OVERFLOW);
+      }
+      k0 += s_w[32];
+      __syncthreads();
     }
-    uint32_t x, y, z;
-    slot_cell(t, sl, x, y, z);
-    const uint32_t lin = (z * t.gh + y) * t.gw + x;
-    const uint32_t w = cells[t.cell_base + lin];
-    const float px = static_cast<float>(static_cast<int>(x) * SYN_Q + static_cast<int>(w & 1023u)) * (t.cell / SYN_Q);
-    const float py = static_cast<float>(static_cast<int>(y) * SYN_Q + static_cast<int>((w >> 10) & 1023u)) * (t.cell / SYN_Q);
-    const float pz = static_cast<float>(static_cast<int>(z) * SYN_Q + static_cast<int>((w >> 20) & 1023u)) * (t.cell / SYN_Q);
-    const P4 r0 = philox(lin, 0, 0, TAG_ATTR, t.k0, t.k1);
-    const P4 r1 = philox(lin, 1, 0, TAG_ATTR, t.k0, t.k1);
-    // Two normals from one Box-Muller pair: radius (log-normal) and sensitivity.
-    const float bm = sqrtf(-2.0f * logf(1.0f - uf(r0.x)));
-    float s2, c2;
-    sincospif(2.0f * uf(r0.y), &s2, &c2);
-    const float radius = fminf(fmaxf(expf(t.mu + t.sg * bm * c2), 0.15f), t.rmax);
-    const float sens = fmaxf(t.base_sens + 0.15f * bm * s2, 0.1f);
-    float4 q, d;
-    if (t.morph == 1) {
-      // Tabular: thickness r / AR (>= 0.05), tilt +-0.17 rad about a random in-plane axis.
-      const float ht = fmaxf(radius / t.aspect, 0.05f);
-      const float tilt = uf(r0.z) * 0.34f - 0.17f;
-      float ax = uf(r0.w) * 2.0f - 1.0f, ay = uf(r1.x) * 2.0f - 1.0f;
-      const float n = rsqrtf(fmaxf(ax * ax + ay * ay, 1e-30f));
-      ax *= n;
-      ay *= n;
-      float sh, ch;
-      sincosf(0.5f * tilt, &sh, &ch);
-      q = make_float4(ax * sh, ay * sh, 0.0f, ch);
-      d = make_float4(radius, radius, ht, __int_as_float(1));
-    } else {
-      // Cubic / octahedral: UnitQuaternion::from_euler_angles(2 pi u1, pi u2, 2 pi u3).
-      float sr, cr, sp, cp, sy, cy;
-      sincospif(uf(r0.z), &sr, &cr);        // roll / 2 = pi u1
-      sincospif(0.5f * uf(r0.w), &sp, &cp); // pitch / 2 = pi u2 / 2
-      sincospif(uf(r1.x), &sy, &cy);        // yaw / 2 = pi u3
-      q = make_float4(sr * cp * cy - cr * sp * sy, cr * sp * cy + sr * cp * sy, cr * cp * sy - sr * sp * cy,
-                      cr * cp * cy + sr * sp * sy);
-      d = make_float4(radius, radius, radius, __int_as_float(t.morph));
-    }
-    const unsigned long long o = t.cbase + k;
-    A[o] = make_float4(px, py, pz, sens);
-    Q[o] = q;
-    D[o] = d;
-    keys[o] = sl;
   }
 }
 
@@ -610,25 +646,25 @@ size_t bridson_smem(int gdmax) {
          static_cast<size_t>(SYN_B) * SYN_B * gdmax * sizeof(uint16_t);
 }
 
-// Per-tile grids (blockIdx.y is the tile): max_cells and max_slots are the largest tile's.
-void launch_synth_post(const SynthTile* tiles, int ntiles, unsigned long long max_cells, unsigned long long max_slots,
-                       uint32_t* cells, uint32_t* npts, uint32_t* flags, cudaStream_t st) {
+// Per-tile grids (blockIdx.y is the tile): max_cells and max_bricks are the largest tile's.
+void launch_synth_post(const SynthTile* tiles, int ntiles, unsigned long long max_cells, unsigned long long max_bricks,
+                       uint32_t* cells, uint32_t* npts, uint32_t* counts, cudaStream_t st) {
   if (ntiles == 0) return;
   FG_REQUIRE(ntiles <= 65535, "too many tiles for one launch");
   const unsigned bc = static_cast<unsigned>(std::min<unsigned long long>(std::max(grid_for(max_cells, 256), 1u), 1024));
-  const unsigned bs = static_cast<unsigned>(std::min<unsigned long long>(std::max(grid_for(max_slots, 256), 1u), 1024));
+  const unsigned bb = static_cast<unsigned>(std::min<unsigned long long>(std::max(max_bricks, 1ull), 4096));
   k_thin<<<dim3(bc, ntiles), 256, 0, st>>>(tiles, cells, npts);
-  k_slot_flags<<<dim3(bs, ntiles), 256, 0, st>>>(tiles, cells, flags);
+  k_brick_count<<<dim3(bb, ntiles), 256, 0, st>>>(tiles, cells, counts);
   FG_CUDA(cudaGetLastError());
 }
 
-void launch_emit(const SynthTile* tiles, int ntiles, unsigned long long max_slots, const uint32_t* cells,
+void launch_emit(const SynthTile* tiles, int ntiles, unsigned long long max_bricks, const uint32_t* cells,
                  const uint32_t* scan, float4* A, float4* Q, float4* D, uint64_t* keys, uint32_t* err,
                  cudaStream_t st) {
   if (ntiles == 0) return;
   FG_REQUIRE(ntiles <= 65535, "too many tiles for one launch");
-  const unsigned bs = static_cast<unsigned>(std::min<unsigned long long>(std::max(grid_for(max_slots, 256), 1u), 1024));
-  k_emit<<<dim3(bs, ntiles), 256, 0, st>>>(tiles, cells, scan, A, Q, D, keys, err);
+  const unsigned bb = static_cast<unsigned>(std::min<unsigned long long>(std::max(max_bricks, 1ull), 4096));
+  k_emit<<<dim3(bb, ntiles), 256, 0, st>>>(tiles, cells, scan, A, Q, D, keys, err);
   FG_CUDA(cudaGetLastError());
 }
 

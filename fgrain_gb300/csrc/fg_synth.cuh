@@ -47,7 +47,7 @@ __host__ __device__ inline double bridson_density(double W, double H, double D, 
 
 struct __align__(16) SynthTile {
   unsigned long long cell_base;  // first cell of this tile in the batch grid
-  unsigned long long slot_base;  // first compaction slot
+  unsigned long long slot_base;  // first brick of this tile in the batch's brick counts
   unsigned long long cbase;      // first crystal slot
   uint32_t gw, gh, gd;           // cell grid
   uint32_t nbx, nby;             // columns per axis
