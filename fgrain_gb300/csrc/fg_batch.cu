@@ -1,6 +1,6 @@
 // Batched tile pipeline: many exposure tiles (uneven sizes, stocks, push, seeds) rendered to
 // negative density in one sequence of launches:
-//   synthesis (column Bridson, 4 colour classes) -> thinning -> Morton compaction -> LBVH
+//   synthesis (column Bridson, 4 colour classes) -> thinning -> compaction in brick order -> LBVH
 //   -> persistent transport over all tiles' photons -> development -> bins -> binned scan.
 // Every kernel covers all tiles at once (per-tile descriptors in HBM, tile found by binary search
 // on a prefix of work items), every buffer is allocated when the plan is made, and nothing waits
@@ -1235,7 +1235,7 @@ fg_status fg_batch_wait(fg_batch* b, fg_batch_stats* stats) {
     s.scan_bin_px = b->bin_px;
     s.graph = b->exec ? 1u : 0u;
     // Own kernels per run: Bridson (all colour classes in one launch; it also counts the points), thin +
-    // flags, emit, set_n, Karras + fit + four-wide collapse, photon order x2, transport, maxdim + threshold +
+    // brick counts, emit, set_n, Karras + fit + four-wide collapse, photon order x2, transport, maxdim + threshold +
     // developed list + link + roots + finalize, scan prep, two bin passes, scan (CUB scans not counted).
     s.kernel_launches = 1 + 2 + 1 + 1 + 3 + 2 + 1 + 6 + 1 + 2 + 1;
     b->stats = s;
