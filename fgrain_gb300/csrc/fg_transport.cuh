@@ -6,6 +6,7 @@
 namespace fg {
 
 constexpr int HMAX = 48;  // hits kept per segment (a 21 um segment meets ~10 crystals)
+constexpr int WALK_LEAVES = 6;  // leaves a lane may hold while its warp still walks (speculative traversal)
 
 // Everything one tile's transport needs, 16-byte aligned for vector loads.
 struct __align__(16) TileDesc {
@@ -91,26 +92,29 @@ __device__ __forceinline__ void walk_bvh4_deferred(const Node4* __restrict__ nod
   int stack[64];
   int sp = 0;
   int cur = n ? 0 : EMPTY;
-  uint32_t leaf = NONE, leaf2 = NONE, leaf3 = NONE, leaf4 = NONE;  // pending leaf, three found speculatively
+  // lv[0] is the pending leaf, the others were found speculatively (registers: every index below
+  // is a constant after unrolling).
+  uint32_t lv[WALK_LEAVES];
+#pragma unroll
+  for (int j = 0; j < WALK_LEAVES; ++j) lv[j] = NONE;
   const float3 oi = make_float3(o.x * inv.x, o.y * inv.y, o.z * inv.z);
   for (;;) {
     for (;;) {
       // Visit while some lane still has no leaf; a lane that holds one goes on walking until it
-      // holds four (speculative traversal) instead of idling.
-      const bool need = cur != EMPTY && leaf == NONE;
+      // holds WALK_LEAVES (speculative traversal) instead of idling.
+      const bool need = cur != EMPTY && lv[0] == NONE;
       if (!__any_sync(amask, need)) break;
-      const bool want = cur != EMPTY && leaf4 == NONE;
+      const bool want = cur != EMPTY && lv[WALK_LEAVES - 1] == NONE;
       if (!want) continue;
       if (cur < 0) {
         const uint32_t lf = static_cast<uint32_t>(~cur);
-        if (leaf == NONE) {
-          leaf = lf;
-        } else if (leaf2 == NONE) {
-          leaf2 = lf;
-        } else if (leaf3 == NONE) {
-          leaf3 = lf;
-        } else {
-          leaf4 = lf;
+        bool placed = false;
+#pragma unroll
+        for (int j = 0; j < WALK_LEAVES; ++j) {
+          if (!placed && lv[j] == NONE) {
+            lv[j] = lf;
+            placed = true;
+          }
         }
         cur = sp > 0 ? stack[--sp] : EMPTY;
         continue;
@@ -149,13 +153,12 @@ __device__ __forceinline__ void walk_bvh4_deferred(const Node4* __restrict__ nod
       child(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, rf.w);
       cur = next != EMPTY ? next : (sp > 0 ? stack[--sp] : EMPTY);
     }
-    if (!__any_sync(amask, leaf != NONE)) break;
-    if (leaf != NONE) {
-      if (index_ok(leaf < n, err, SITE_LEAF, leaf, n)) fn(leaf);
-      leaf = leaf2;
-      leaf2 = leaf3;
-      leaf3 = leaf4;
-      leaf4 = NONE;
+    if (!__any_sync(amask, lv[0] != NONE)) break;
+    if (lv[0] != NONE) {
+      if (index_ok(lv[0] < n, err, SITE_LEAF, lv[0], n)) fn(lv[0]);
+#pragma unroll
+      for (int j = 0; j + 1 < WALK_LEAVES; ++j) lv[j] = lv[j + 1];
+      lv[WALK_LEAVES - 1] = NONE;
     }
   }
 }
