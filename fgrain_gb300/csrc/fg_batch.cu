@@ -144,6 +144,7 @@ __global__ void k_karras_b(const BTile* __restrict__ bt, int ntiles, unsigned lo
   }
   nodes[i].d.x = left;
   nodes[i].d.y = right;
+  nodes[i].d.w = static_cast<int>(hi);
   if (i == 0) nodes[0].d.z = -1;
 }
 
@@ -350,10 +351,11 @@ __global__ void k_link_b(const BTile* __restrict__ bt, int ntiles, unsigned long
     const Node4* nd = nodes + cur;
     const float4 lx = __ldg(&nd->lox), ly = __ldg(&nd->loy), lz = __ldg(&nd->loz);
     const float4 hx = __ldg(&nd->hix), hy = __ldg(&nd->hiy), hz = __ldg(&nd->hiz);
-    const int4 rf = __ldg(&nd->ref);
+    const int4 rf = __ldg(&nd->ref), ls = __ldg(&nd->last);
     int next = -1;
-    auto child = [&](float a0, float a1, float a2, float a3, float a4, float a5, int r) {
-      if (r == INT32_MIN) return;
+    // Only pairs (s, j > s) are tested, so a child whose crystals all lie at or below s is skipped.
+    auto child = [&](float a0, float a1, float a2, float a3, float a4, float a5, int r, int last) {
+      if (r == INT32_MIN || last <= static_cast<int>(s)) return;
       if (!(a0 <= hi.x && a3 >= lo.x && a1 <= hi.y && a4 >= lo.y && a2 <= hi.z && a5 >= lo.z)) return;
       if (r < 0) {
         leaf(static_cast<uint32_t>(~r));
@@ -365,10 +367,10 @@ __global__ void k_link_b(const BTile* __restrict__ bt, int ntiles, unsigned long
         atomicOr(err, ERR_STACK_OVERFLOW);
       }
     };
-    child(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, rf.x);
-    child(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, rf.y);
-    child(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, rf.z);
-    child(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, rf.w);
+    child(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, rf.x, ls.x);
+    child(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, rf.y, ls.y);
+    child(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, rf.z, ls.z);
+    child(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, rf.w, ls.w);
     if (next >= 0) {
       cur = next;
     } else {

@@ -103,6 +103,7 @@ __global__ void k_karras(const uint64_t* keys, uint32_t n, Node* nodes, int* lea
   }
   nodes[i].d.x = left;
   nodes[i].d.y = right;
+  nodes[i].d.w = static_cast<int>(hi);
   if (i == 0) nodes[0].d.z = -1;
 }
 

@@ -78,44 +78,55 @@ struct __align__(16) Node {
   float4 a;  // l.lo.x l.lo.y l.lo.z l.hi.x
   float4 b;  // l.hi.y l.hi.z r.lo.x r.lo.y
   float4 c;  // r.lo.z r.hi.x r.hi.y r.hi.z
-  int4 d;    // left, right, parent, unused
+  int4 d;    // left, right, parent, last leaf of the node's range (leaves are in key order)
 };
 
 // Four-wide node collapsed from the binary LBVH (the transport walk): binary internal node i keeps
 // its grandchildren (or a child leaf in place of an internal child), so one step of a walk covers
 // two binary levels.  Child k's box is (lox[k], loy[k], loz[k]) - (hix[k], hiy[k], hiz[k]); ref[k]
-// is a collapsed node (the binary index, >= 0), a leaf (~crystal, < 0) or empty (INT32_MIN).
+// is a collapsed node (the binary index, >= 0), a leaf (~crystal, < 0) or empty (INT32_MIN);
+// last[k] is the highest crystal index under child k (-1 when empty).
 struct __align__(16) Node4 {
   float4 lox, loy, loz, hix, hiy, hiz;
   int4 ref;
-  int4 pad;
+  int4 last;
 };
+
+// Highest leaf under the left child of a binary node whose right child is ref_right (a Karras
+// node's range splits between its children, and an internal node's index is the first leaf of a
+// right child's range), given the node's own last leaf.
+__device__ __forceinline__ int left_last(int ref_right, int node_last) {
+  if (ref_right == INT32_MIN) return node_last;
+  return (ref_right < 0 ? ~ref_right : ref_right) - 1;
+}
 
 // Node4 of binary internal node i.  Every child box is the same box its binary parent holds, so
 // the leaves a walk reaches are those of the binary walk: an ancestor box contains its
 // descendants' boxes, and the slab test is monotone in the box.
 __device__ __forceinline__ void collapse_node4(const Node* __restrict__ nodes, int i, Node4* __restrict__ out) {
   float v[4][6];
-  int r[4];
+  int r[4], lst[4];
   int k = 0;
-  auto add = [&](int ref, float a0, float a1, float a2, float a3, float a4, float a5) {
+  auto add = [&](int ref, int last, float a0, float a1, float a2, float a3, float a4, float a5) {
     v[k][0] = a0; v[k][1] = a1; v[k][2] = a2; v[k][3] = a3; v[k][4] = a4; v[k][5] = a5;
     r[k] = ref;
+    lst[k] = last;
     ++k;
   };
   const Node nd = nodes[i];
-  auto expand = [&](int ref, float a0, float a1, float a2, float a3, float a4, float a5) {
+  auto expand = [&](int ref, int last, float a0, float a1, float a2, float a3, float a4, float a5) {
     if (ref == INT32_MIN) return;
     if (ref < 0) {
-      add(ref, a0, a1, a2, a3, a4, a5);
+      add(ref, ~ref, a0, a1, a2, a3, a4, a5);
       return;
     }
     const Node ch = nodes[ref];
-    add(ch.d.x, ch.a.x, ch.a.y, ch.a.z, ch.a.w, ch.b.x, ch.b.y);
-    if (ch.d.y != INT32_MIN) add(ch.d.y, ch.b.z, ch.b.w, ch.c.x, ch.c.y, ch.c.z, ch.c.w);
+    add(ch.d.x, left_last(ch.d.y, ch.d.w), ch.a.x, ch.a.y, ch.a.z, ch.a.w, ch.b.x, ch.b.y);
+    if (ch.d.y != INT32_MIN) add(ch.d.y, ch.d.w, ch.b.z, ch.b.w, ch.c.x, ch.c.y, ch.c.z, ch.c.w);
+    (void)last;
   };
-  expand(nd.d.x, nd.a.x, nd.a.y, nd.a.z, nd.a.w, nd.b.x, nd.b.y);
-  expand(nd.d.y, nd.b.z, nd.b.w, nd.c.x, nd.c.y, nd.c.z, nd.c.w);
+  expand(nd.d.x, left_last(nd.d.y, nd.d.w), nd.a.x, nd.a.y, nd.a.z, nd.a.w, nd.b.x, nd.b.y);
+  expand(nd.d.y, nd.d.w, nd.b.z, nd.b.w, nd.c.x, nd.c.y, nd.c.z, nd.c.w);
   // A slot left free by a leaf child takes the two children of the internal grandchild with the
   // largest box surface: every internal entry stays at least two levels down, so the walk still
   // descends two levels per four-wide node and its stack bound is unchanged.
@@ -141,13 +152,15 @@ __device__ __forceinline__ void collapse_node4(const Node* __restrict__ nodes, i
       if (j == best) {
         v[j][0] = ch.a.x; v[j][1] = ch.a.y; v[j][2] = ch.a.z; v[j][3] = ch.a.w; v[j][4] = ch.b.x; v[j][5] = ch.b.y;
         r[j] = ch.d.x;
+        lst[j] = left_last(ch.d.y, ch.d.w);
       }
     }
-    add(ch.d.y, ch.b.z, ch.b.w, ch.c.x, ch.c.y, ch.c.z, ch.c.w);
+    add(ch.d.y, ch.d.w, ch.b.z, ch.b.w, ch.c.x, ch.c.y, ch.c.z, ch.c.w);
   }
   for (; k < 4; ++k) {
     for (int j = 0; j < 6; ++j) v[k][j] = 0.0f;
     r[k] = INT32_MIN;
+    lst[k] = -1;
   }
   out->lox = make_float4(v[0][0], v[1][0], v[2][0], v[3][0]);
   out->loy = make_float4(v[0][1], v[1][1], v[2][1], v[3][1]);
@@ -156,7 +169,7 @@ __device__ __forceinline__ void collapse_node4(const Node* __restrict__ nodes, i
   out->hiy = make_float4(v[0][4], v[1][4], v[2][4], v[3][4]);
   out->hiz = make_float4(v[0][5], v[1][5], v[2][5], v[3][5]);
   out->ref = make_int4(r[0], r[1], r[2], r[3]);
-  out->pad = make_int4(0, 0, 0, 0);
+  out->last = make_int4(lst[0], lst[1], lst[2], lst[3]);
 }
 
 __device__ __forceinline__ int morph_of(const float4& d) { return __float_as_int(d.w); }
