@@ -25,6 +25,7 @@ STATUS_NAMES = {
     18: "FG_ERR_DEVICE_TIMEOUT",
     19: "FG_ERR_DEVICE_OVERFLOW",
 }
+globals().update({name: code for code, name in STATUS_NAMES.items()})  # FG_ERR_INVALID_ARG = 16, ...
 
 
 class fg_optics(C.Structure):

@@ -15,14 +15,19 @@
 //
 // All calls on a device share the one array, and it keeps whatever the last call left in it:
 // each call clears the parts that must start at zero (bin counts, cursors, error word) on the
-// caller's stream.  Calls whose GPU work overlaps (two host threads, or two streams) race on the
-// array and give wrong results; callers serialise them.
+// caller's stream.  Two calls whose GPU work overlapped (two host threads, or two streams) would
+// race on the array and give wrong images.  The library prevents that within a process: a call
+// holds a per-device lock from its first enqueue until its GPU work has finished (it synchronises
+// the stream before it returns, also on failure), so concurrent callers wait for each other.
+// Other processes load their own copy of the array.
 //
 // The bins, the binned scan kernel and the result are those of fg_scan_emulsion (same kernels,
 // same descriptor), so both entry points give the same image for the same crystals.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <mutex>
 
 #include "fg_internal.h"
 #include "fg_scan.cuh"
@@ -63,12 +68,18 @@ namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mu;
 void* g_scratch_addr[kMaxDevices] = {};
+std::mutex g_call_mu[kMaxDevices];  // one per device: held for the whole of a call on that device
 
-// Device address of the scratch on the current device; the first call on a device looks it up.
-unsigned char* scratch_for_current_device() {
+int current_device() {
   int dev = -1;
   FG_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) throw Error{FG_ERR_ADAPTER_NOT_FOUND, "device ordinal out of range"};
+  return dev;
+}
+
+// Device address of the scratch on device `dev` (the current device); the first call on a device
+// looks it up.
+unsigned char* scratch_for_device(int dev) {
   std::lock_guard<std::mutex> lock(g_scratch_mu);
   if (!g_scratch_addr[dev]) {
     void* p = nullptr;
@@ -136,6 +147,10 @@ void static_scan(const fg_device_crystals* c, const fg_emulsion_cfg* film, const
   const bool has64 = c->pos64 != nullptr;
   FG_REQUIRE((c->dims64 != nullptr) == has64 && (c->quat64 != nullptr) == has64,
              "pos64, dims64 and quat64 must be given together or not at all");
+  FG_REQUIRE(((reinterpret_cast<uintptr_t>(c->pos64) | reinterpret_cast<uintptr_t>(c->dims64) |
+               reinterpret_cast<uintptr_t>(c->quat64) | reinterpret_cast<uintptr_t>(c->expansion)) & 7u) == 0,
+             "FP64 arrays pos64, dims64, quat64 and expansion must be 8-byte aligned");
+  FG_REQUIRE((reinterpret_cast<uintptr_t>(out) & 3u) == 0, "out must be 4-byte aligned");
   FG_REQUIRE(film->width > 0 && film->height > 0, "film dimensions must be positive");
   FG_REQUIRE(cfg->width_px > 0 && cfg->height_px > 0, "scan size must be positive");
   const uint32_t spp_req = std::max<uint32_t>(cfg->samples_per_pixel, 1);
@@ -181,7 +196,9 @@ void static_scan(const fg_device_crystals* c, const fg_emulsion_cfg* film, const
                                         " px; the static scratch holds at most " +
                                         std::to_string(FG_STATIC_SCAN_MAX_BINS)};
 
-  unsigned char* base = scratch_for_current_device();
+  const int dev = current_device();
+  std::lock_guard<std::mutex> call_lock(g_call_mu[dev]);
+  unsigned char* base = scratch_for_device(dev);
   auto* desc = reinterpret_cast<ScanTile*>(base + kDescOff);
   auto* err = reinterpret_cast<uint32_t*>(base + kErrOff);
   auto* cnt = reinterpret_cast<uint32_t*>(base + kCntOff);
@@ -192,6 +209,14 @@ void static_scan(const fg_device_crystals* c, const fg_emulsion_cfg* film, const
   t.bin_items = items;
 
   (void)cudaGetLastError();  // a stale launch error of the caller's is not ours to report
+  // From here on work is queued on the scratch: a failure waits for it before the lock is released.
+  struct DrainOnThrow {
+    cudaStream_t st;
+    bool armed = true;
+    ~DrainOnThrow() {
+      if (armed) (void)cudaStreamSynchronize(st);
+    }
+  } drain{st};
   // What must start at zero: counts (and the total slot), cursors, the error word.
   FG_CUDA(cudaMemsetAsync(cnt, 0, (nbins + 1) * sizeof(uint32_t), st));
   FG_CUDA(cudaMemsetAsync(cur, 0, (nbins + 1) * sizeof(uint32_t), st));
@@ -215,7 +240,12 @@ void static_scan(const fg_device_crystals* c, const fg_emulsion_cfg* film, const
   uint32_t w = 0;
   FG_CUDA(cudaMemcpyAsync(&w, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   FG_CUDA(cudaStreamSynchronize(st));
-  if (w) throw Error{FG_ERR_DEVICE_OVERFLOW, "scan kernel error word 0x" + std::to_string(w)};
+  drain.armed = false;  // the stream is drained
+  if (w) {
+    char hex[16];
+    std::snprintf(hex, sizeof(hex), "%08x", w);
+    throw Error{FG_ERR_DEVICE_OVERFLOW, std::string("scan kernel error word 0x") + hex};
+  }
 }
 
 }  // namespace

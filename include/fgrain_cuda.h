@@ -466,7 +466,11 @@ typedef struct fg_device_crystals {
  * may be NULL).  The first call on a device looks up the scratch's device address
  * (cudaGetSymbolAddress); make that first call before any stream capture.  Every call on a device
  * shares the scratch, which keeps the last call's contents; each call clears what must start at
- * zero.  Calls whose GPU work overlaps race on the scratch: serialise them. */
+ * zero.  Calls whose GPU work overlapped would race on the scratch and give wrong images, so the
+ * library serialises them: a call holds a per-device lock until its GPU work has finished (also
+ * when it fails), and concurrent calls from other host threads wait.  a, q, d must be 16-byte
+ * aligned, pos64, dims64, quat64 and expansion 8-byte aligned and out 4-byte aligned; anything
+ * else fails with FG_ERR_INVALID_ARG before the GPU is touched. */
 fg_status fg_scan_crystals_static(const fg_device_crystals* crystals, const fg_emulsion_cfg* film,
                                   const fg_scan_cfg* cfg, uint64_t seed, float* out, uint8_t* image8,
                                   void* stream, char* message, size_t message_len);

@@ -115,3 +115,28 @@ def test_tile_params_follow_the_cpu_tile_worker(preset, push):
     assert (p.samples_per_pixel, p.silver_opacity, p.seed) == (4, 0.25, 99)
     assert (p.photons_per_sq_um, p.illumination_angle_rad, p.crystal_absorption_coeff, p.max_bounces) == (6.0, 0.12, 1.3, 48)
     assert p.exposure == 0.7
+
+
+def test_static_scan_rejects_misaligned_device_pointers_before_any_gpu_call():
+    """fg_scan_crystals_static checks the alignment of every device array before it touches the
+    GPU (so this runs without one): float4 arrays 16 bytes, FP64 arrays 8 bytes, out 4 bytes."""
+    lib = _abi.load()
+    cfg = fg.EmulsionConfig.preset("tri-x", 10.0, 10.0).to_c()
+    scan = fg.ScanConfig(16, 16, 4, 0, 0.25).to_c()
+    ok = 0x10000  # aligned stand-in addresses: never dereferenced, the checks fail first
+    cases = [
+        (dict(a=ok + 8), b"16-byte aligned"),
+        (dict(pos64=ok + 4, dims64=ok, quat64=ok), b"8-byte aligned"),
+        (dict(pos64=ok, dims64=ok, quat64=ok + 12), b"8-byte aligned"),
+        (dict(expansion=ok + 2), b"8-byte aligned"),
+        (dict(out=ok + 2), b"4-byte aligned"),
+    ]
+    for over, what in cases:
+        f = dict(a=ok, q=ok, d=ok, pos64=None, dims64=None, quat64=None, developed=ok, expansion=ok, out=ok)
+        f.update(over)
+        dc = _abi.fg_device_crystals(f["a"], f["q"], f["d"], f["pos64"], f["dims64"], f["quat64"],
+                                     f["developed"], f["expansion"], 1)
+        msg = C.create_string_buffer(256)
+        st = lib.fg_scan_crystals_static(C.byref(dc), C.byref(cfg), C.byref(scan), 1, f["out"], None, None,
+                                         msg, len(msg))
+        assert st == _abi.FG_ERR_INVALID_ARG and what in msg.value, (over, msg.value)

@@ -1,9 +1,12 @@
 """GPU test of fg_scan_crystals_static, the scan entry point that allocates no device memory.
 
-The caller owns every device buffer (here torch tensors stand in for a host application's own
-pool).  Two calls in a row, with different crystal sets, image sizes, strata and modes, must each
-reproduce fg_scan_emulsion on the same crystals: the second call starts from the scratch contents
-the first one left behind.  The file name makes pytest collect it last; it also passes alone.
+Some callers cannot let a library allocate device memory: a host that owns a fixed device-memory
+budget or its own pool allocator, or a plugin inside one.  They hand over the crystals and the
+output image in device memory they already hold (here torch tensors stand in for such a pool).
+Two calls in a row, with different crystal sets, image sizes, strata and modes, must each give
+exactly the image of fg_scan_emulsion on the same crystals (same kernels, same staging, fixed-point
+chord sums): the second call starts from the scratch contents the first one left behind.  The
+file name makes pytest collect it last; it also passes alone.
 """
 import ctypes as C
 
@@ -78,8 +81,9 @@ def test_static_scan_matches_scan_emulsion_twice(engine):
         ref_out, ref_img = reference_scan(engine, cfg, cr, scan, seed)
         out, img = static_scan(torch, cfg, cr, scan, seed, with64)
         assert (out >= 0).all()
-        np.testing.assert_allclose(out, ref_out, rtol=T_RTOL, atol=0)
-        assert np.abs(img.astype(int) - ref_img.astype(int)).max() <= 1
+        # The same image bit for bit (the scan tolerance would allow T_RTOL).
+        np.testing.assert_array_equal(out, ref_out)
+        np.testing.assert_array_equal(img, ref_img)
         assert (ref_out < 0.999).mean() > 0.05  # the developed crystals do shade the image
 
 
@@ -94,5 +98,32 @@ def test_static_scan_rejects_requests_beyond_its_scratch(engine):
     msg = C.create_string_buffer(512)
     st = _abi.load().fg_scan_crystals_static(C.byref(dc), C.byref(cfg.to_c()), C.byref(scan.to_c()), 1,
                                              out.data_ptr(), None, None, msg, len(msg))
-    assert st == 16 and b"at most 16384" in msg.value, msg.value
+    assert st == _abi.FG_ERR_INVALID_ARG and b"at most 16384" in msg.value, msg.value
+    assert (out.cpu().numpy() == -1.0).all()
+
+
+def test_static_scan_rejects_more_bin_entries_than_its_scratch(engine):
+    """100 developed cubes that each cover the whole film make 100 x 16384 (crystal, bin) entries,
+    more than the scratch's 1,048,576: the call fails after counting and leaves out untouched."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("torch without CUDA")
+    cfg = reference_cfg("tri-x", 20.0, 20.0)
+    n = 100
+    rng = np.random.default_rng(3)
+    pos = np.column_stack([10.0 + rng.random(n), 10.0 + rng.random(n), np.full(n, 7.0)])
+    dev = lambda x: torch.from_numpy(np.ascontiguousarray(x)).to("cuda")  # noqa: E731
+    a = dev(np.column_stack([pos, np.ones(n)]).astype(np.float32))
+    q = dev(np.tile(np.array([0.0, 0.0, 0.0, 1.0], np.float32), (n, 1)))
+    d = dev(np.column_stack([np.full((n, 3), 11.0, np.float32), np.zeros(n, np.int32).view(np.float32)]))
+    developed = dev(np.ones(n, np.uint8))
+    expansion = dev(np.ones(n))
+    dc = _abi.fg_device_crystals(a.data_ptr(), q.data_ptr(), d.data_ptr(), None, None, None,
+                                 developed.data_ptr(), expansion.data_ptr(), n)
+    scan = fg.ScanConfig(1024, 1024, 4, 0, 0.25)  # 128 x 128 bins of 8 px: exactly the bin limit
+    out = torch.full((1024, 1024), -1.0, dtype=torch.float32, device="cuda")
+    msg = C.create_string_buffer(512)
+    st = _abi.load().fg_scan_crystals_static(C.byref(dc), C.byref(cfg.to_c()), C.byref(scan.to_c()), 1,
+                                             out.data_ptr(), None, None, msg, len(msg))
+    assert st == _abi.FG_ERR_INVALID_ARG and b"at most 1048576" in msg.value, msg.value
     assert (out.cpu().numpy() == -1.0).all()
