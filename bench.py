@@ -1,24 +1,33 @@
 #!/usr/bin/env python
 """Benchmark of the fgrain photon-transport and transmittance-scan path on GB300.
 
-Workload (one "step"): the 1024 x 1024 black-and-white image of configuration C2 rendered at
-supersample 2 (2048 x 2048 internal, tri-x cubic grains, grain 2.4 px, push 0, seed 42): 49
-overlapping tiles of up to 384 x 384 px, each synthesized, exposed, developed and scanned to
-negative density by the batched graph path.  Inputs: blurred uniform noise (sigma 16 px, seed 1,
-gamma 2.2) upsampled x2 by linear interpolation (synthetic; no dataset is involved).
+Headline workload (configuration C4, the largest that fits one GPU): a 4096 x 4096 RGB photograph
+(per channel, uniform noise from seed 3 Gaussian-blurred with sigma 32 px, as 8-bit), t-max tabular
+grains at 1.1 px, three dye layers, supersample 4 (16384^2 per layer), seed 42.  Its 8,112
+overlapping tiles (52 x 52 per layer, up to 384 x 384 px) are rendered from exposure tile to
+negative density by the batched graph path.  One step is one batch of 254 of those tiles (every
+32nd tile of the photograph in layer-major grid order), so the step fits the timing budget; the
+whole photograph is about 32 such batches.
 
-Reported:
-  value      output Mpx/s (1024^2 output pixels per step / device time per step), inputs resident
-             in HBM; the working set (crystals, LBVH, grids) is several GB, far larger than L2.
-  e2e        the same through the public API with page-locked host buffers: host->device copy of
-             the exposure tiles, run, device->host copy of the density tiles, every step.
-  roofline   the transport kernel against the measured HBM copy bandwidth.
-  cpu_baseline  the CPU oracle (a C++ restatement of the reference's Rayon CPU path, faithful
-             hit rule) on a bounded sample of the same tiles, all host threads.
+Reported on one JSON line:
+  value      output pixel-channels per second that the batch stands for (4096^2 x 3 x the batch's
+             share of all tile pixels) over the device time per step, inputs resident in HBM.  The
+             working set (crystals, trees, grids: tens of GB) is far larger than L2; no flush.
+  e2e        the whole photograph through fg_render_film, host u8 pixels in, host u8 pixels out
+             (luma split, upscale, PSF, every tile, blend and finish), one timed call.
+  e2e_batch  the step's batch through the public batch API with page-locked host buffers: exposure
+             tiles copied in and densities copied out every step.
+  plain / batched_over_plain  the plain per-tile path (fg_render_tile: plan, copy, run, free per
+             tile) against a batch of the same tiles, both host to host, on a 32-tile sample.
+  roofline   the dominant kernel of the step against the measured HBM copy bandwidth.
+  cpu_baseline  the CPU oracle (a C++ restatement of the reference's Rayon CPU path with the
+             reference's own hit rule) on 16 of the batch's tiles, one tile per host thread;
+             mean_T_rel_err_vs_oracle compares those tiles' mean transmittance with the device's.
+  c2, c3     the same quantities on configurations C2 and C3 (extra keys).
 
 `--impl reference` times that CPU restatement alone (the reference itself is Rust and cannot be
-built here) on the same workload, metric and unit.  With torchrun (N > 1) every rank renders its
-own replica of the image (replicas only: no collective is involved), and rank 0 reports the sum.
+built here; this arm imports nothing of the product) on C4 tiles from the same sample.  With
+torchrun (N > 1) every rank renders its own replica (replicas only: no collective is involved).
 """
 from __future__ import annotations
 
@@ -29,7 +38,6 @@ import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 from concurrent.futures import ThreadPoolExecutor
 from pathlib import Path
@@ -40,51 +48,78 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "Mpx/s and photons/s on 1 GB300, batched vs plain at <=0.5% mean-T error"
-OUT_W = OUT_H = 1024
-SS = 2
-GRAIN = 2.4
 SEED = 42
+M64 = 0xFFFFFFFFFFFFFFFF
+COLOR_SEED_OFFSETS = (0, 10007, 20011)  # image_pipeline.rs:1048-1061
+
+# C4
+C4_SIDE = 4096
+C4_SS = 4
+C4_GRAIN = 1.1
+C4_TILE = 320
+C4_STRIDE = 32        # every 32nd tile of the photograph forms the step's batch
+C4_PLAIN_EVERY = 8    # the plain-path sample: every 8th tile of the batch (32 tiles)
+C4_CPU_EVERY = 16     # the CPU-oracle sample: every 16th tile of the batch (16 tiles)
+C4_WORKLOAD = ("C4: 4096x4096 RGB blurred-noise photograph (sigma 32 px, seed 3, 8-bit), t-max tabular grains "
+               "1.1 px, colour (three dye layers), supersample 4 (16384^2 per layer, 8112 tiles)")
+
+# C2
+C2_OUT = 1024
+C2_SS = 2
+C2_GRAIN = 2.4
+C2_WORKLOAD = ("C2: 1024x1024 blurred-noise luminance (sigma 16, seed 1, gamma 2.2), tri-x, grain 2.4 px, push 0, "
+               "supersample 2 (2048^2 internal, 49 tiles)")
+C3_STOCKS = ("tri-x", "t-max", "hp5")
+
+
+# ------------------------------------------------------------------------------------------------
+# Inputs (synthetic: no dataset is involved)
+
+def c4_image(side=C4_SIDE):
+    """Per channel: uniform [0, 1) noise (numpy PCG64, seed 3, channels drawn in turn), Gaussian
+    blur sigma 32 px (reflect), as 8-bit."""
+    from scipy.ndimage import gaussian_filter
+
+    rng = np.random.default_rng(3)
+    planes = [np.clip(gaussian_filter(rng.random((side, side)), 32.0, mode="reflect"), 0.0, 1.0) for _ in range(3)]
+    return np.ascontiguousarray(np.round(np.stack(planes, -1) * 255.0).astype(np.uint8))
+
+
+def c4_sample(ntiles_per_layer, stride=C4_STRIDE):
+    """(layer, tile index) of every `stride`-th tile of the photograph in layer-major grid order."""
+    return [(k // ntiles_per_layer, k % ntiles_per_layer) for k in range(0, 3 * ntiles_per_layer, stride)]
 
 
 def c2_inputs():
     from scipy.ndimage import gaussian_filter, zoom
 
-    a = np.random.default_rng(1).random((OUT_H, OUT_W))
+    a = np.random.default_rng(1).random((C2_OUT, C2_OUT))
     lum = np.clip(gaussian_filter(a, 16.0, mode="reflect"), 0.0, None) ** 2.2
-    exposure = zoom(lum, SS, order=1, mode="nearest").astype(np.float32)
-    return exposure
+    return zoom(lum, C2_SS, order=1, mode="nearest").astype(np.float32)
 
 
-def c2_tiles(exposure, ntiles=None):
+def c2_tiles(exposure):
     import fgrain_gb300 as fg
     from fgrain_gb300.image import tile_grid, tile_seed
 
     H, W = exposure.shape
-    grid, step, pad = tile_grid(W, H, GRAIN)
-    if ntiles:
-        grid = grid[:ntiles]
-    params, tiles = [], []
-    for t in grid:
-        params.append(fg.tile_params("tri-x", 1.0 / GRAIN, t.tw, t.th, 1.0, 0.0, tile_seed(SEED, t)))
-        tiles.append(np.ascontiguousarray(exposure[t.y_start:t.y_start + t.th, t.x_start:t.x_start + t.tw]))
+    grid, _, _ = tile_grid(W, H, C2_GRAIN)
+    params = [fg.tile_params("tri-x", 1.0 / C2_GRAIN, t.tw, t.th, 1.0, 0.0, tile_seed(SEED, t)) for t in grid]
+    tiles = [np.ascontiguousarray(exposure[t.y_start:t.y_start + t.th, t.x_start:t.x_start + t.tw]) for t in grid]
     return grid, params, tiles
-
-
-C3_STOCKS = ("tri-x", "t-max", "hp5")
 
 
 def c3_tiles():
     """Configuration C3: 64 square images, sides exp(U[ln 64, ln 512]) rounded, stock uniform over
     tri-x / t-max / hp5, push U[0, 3] stops, supersample uniform over 1-4 (master seed 0); image k
     is blurred uniform noise (seed k, sigma side / 32 px, gamma 2.2) zoomed by its supersample
-    factor.  All tiles of all images form one batch.  Returns (params, tiles, output px, internal
-    px)."""
+    factor.  All tiles of all images form one batch.  Returns (params, tiles, output px)."""
     import fgrain_gb300 as fg
     from scipy.ndimage import gaussian_filter, zoom
     from fgrain_gb300.image import default_grain_px, effective_push, tile_grid, tile_seed
 
     rng = np.random.default_rng(0)
-    params, tiles, out_px, int_px = [], [], 0, 0
+    params, tiles, out_px = [], [], 0
     for k in range(64):
         side = int(round(float(np.exp(rng.uniform(np.log(64.0), np.log(512.0))))))
         stock = C3_STOCKS[int(rng.integers(0, 3))]
@@ -101,15 +136,11 @@ def c3_tiles():
                                          tile_seed(k, t)))
             tiles.append(np.ascontiguousarray(exposure[t.y_start:t.y_start + t.th, t.x_start:t.x_start + t.tw]))
         out_px += side * side
-        int_px += W * H
-    return params, tiles, out_px, int_px
+    return params, tiles, out_px
 
 
-def c2_tiles_grid(exposure):
-    from fgrain_gb300.image import tile_grid
-
-    return tile_grid(exposure.shape[1], exposure.shape[0], GRAIN)[0]
-
+# ------------------------------------------------------------------------------------------------
+# Measurement helpers
 
 class Clocks:
     """nvidia-smi samples during the timed region."""
@@ -195,23 +226,9 @@ def reduce_max(td, v):
     return float(t.item())
 
 
-def oracle_sample(params, tiles, ntiles, threads):
-    """Renders `ntiles` tiles with the CPU oracle (faithful hit rule), tiles in parallel the way the
-    reference's rayon map does (image_pipeline.rs:427); returns (seconds, tile pixels)."""
-    from oracle import oracle as orc
-
-    idx = list(range(min(ntiles, len(params))))
-
-    def one(i):
-        p = params[i]
-        orc.render_tile("tri-x", 1.0 / GRAIN, tiles[i], p.exposure, 0.0, p.seed, orc.FAITHFUL, 1)
-        return p.width_px * p.height_px
-
-    orc.lib()
-    t0 = time.perf_counter()
-    with ThreadPoolExecutor(max_workers=threads) as ex:
-        px = sum(ex.map(one, idx))
-    return time.perf_counter() - t0, px
+def barrier(td):
+    if td is not None:
+        td.barrier()
 
 
 def measured_peak():
@@ -222,11 +239,10 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def profile_traffic(name="k_transport_c2.md"):
-    """dram bytes per launch of the full C2 workload from a committed ncu summary, or None."""
-    f = ROOT / "profiles" / name
+def profile_traffic(name):
+    """DRAM bytes per launch of the benchmark's batch from a committed ncu summary, or None."""
     try:
-        for line in f.read_text().splitlines():
+        for line in (ROOT / "profiles" / name).read_text().splitlines():
             if line.strip().startswith("traffic_bytes_per_launch:"):
                 return float(line.split(":", 1)[1].strip().split()[0])
     except (OSError, ValueError):
@@ -234,207 +250,300 @@ def profile_traffic(name="k_transport_c2.md"):
     return None
 
 
-def run_ours(args):
-    import fgrain_gb300 as fg
+def rooflines(stats, workload_key):
+    """The transport and Bridson kernels against the measured HBM bandwidth (algorithmic bytes:
+    transport 4 B exposure per photon + 8 B count read-modify-write per hit + 116 B per crystal
+    read once; Bridson 4 B read + 4 B written per synthesis cell)."""
+    peak, kind = measured_peak()
+    P, H, N = stats["photons"], stats["hits"], stats["crystals"]
+    t_alg = 4.0 * P + 8.0 * H + 116.0 * N
+    t_ach = t_alg / (stats["transport_ms"] / 1e3) / 1e9 if stats["transport_ms"] > 0 else 0.0
+    b_alg = 8.0 * stats["cells"]
+    b_ach = b_alg / (stats["bridson_ms"] / 1e3) / 1e9 if stats["bridson_ms"] > 0 else 0.0
+    rt = {"bound": "hbm", "kernel": "k_transport", "achieved": t_ach, "peak": peak, "unit": "GB/s",
+          "frac": t_ach / peak, "peak_source": kind, "traffic": profile_traffic(f"k_transport_{workload_key}.md"),
+          "alg_bytes_per_launch": t_alg, "ms_per_launch": stats["transport_ms"]}
+    rb = {"bound": "hbm", "kernel": "k_bridson", "achieved": b_ach, "peak": peak, "unit": "GB/s",
+          "frac": b_ach / peak, "peak_source": kind, "traffic": profile_traffic(f"k_bridson_{workload_key}.md"),
+          "alg_bytes_per_launch": b_alg, "ms_per_launch": stats["bridson_ms"],
+          "note": "issue- and barrier-bound (shared-memory Bridson rounds), not memory-bound"}
+    dominant = rb if stats["bridson_ms"] > stats["transport_ms"] else rt
+    return dominant, {"k_bridson": rb, "k_transport": rt}
 
-    rank, world, local, td = dist()
-    if args.workload == "c3":
-        params, tiles, c3_out_px, c3_int_px = c3_tiles()
-        exposure = None
-    else:
-        exposure = c2_inputs()
-        grid, params, tiles = c2_tiles(exposure, args.tiles)
-    engine = fg.GpuEngine(local)
-    batch = fg.Batch(params, engine, use_graph=True, autotune=True)
-    batch.set_exposure(tiles)
-    for _ in range(max(args.warmup, 0)):
-        batch.run()
-        stats = batch.wait()
-    batch.run()
-    stats = batch.wait()
-    d_batched = batch.density()
-    if td:
-        td.barrier()
-    prof = None
-    if args.profile_region:  # limits an `ncu --profile-from-start off` capture to the timed replays
-        import torch.cuda.profiler as prof
-        prof.start()
-    with Clocks(local) as clk:
-        ms = batch.time(args.steps)
-    if prof:
-        prof.stop()
-    stats = batch.wait()  # stage times of the last timed replay (CUDA events on the engine stream)
-    if td:
-        td.barrier()
-    clocks = clk.summary()
-    ms_max = reduce_max(td, ms)
-    per_step = ms_max / args.steps
-    full = not args.tiles or args.tiles >= 49
-    if args.workload == "c3":
-        out_px = c3_out_px
-    else:
-        out_px = OUT_W * OUT_H if full else int(round(OUT_W * OUT_H * sum(p.width_px * p.height_px for p in params)
-                                                      / sum(t.tw * t.th for t in c2_tiles_grid(exposure))))
-    value = world * out_px / (per_step / 1e3) / 1e6
 
-    # End to end through the public API: pinned host exposure in, pinned density out, per step.
+def mean_T(d):
+    return float((10.0 ** (-(np.asarray(d, np.float64) - 0.05))).mean())
+
+
+def host_to_host(fg, batch, tiles, steps):
+    """Seconds per step of the batch API with page-locked host buffers: exposure in, density out."""
     pin_in = [fg.PinnedArray(t.shape) for t in tiles]
     pin_out = [fg.PinnedArray(t.shape) for t in tiles]
     for pi, t in zip(pin_in, tiles):
         pi.array[...] = t
-    def e2e_step():
+
+    def step():
         batch.set_exposure([p.array for p in pin_in])
         batch.run()
         batch.wait()
-        ptrs = [p.array for p in pin_out]
-        import ctypes as C
-        arr = (C.POINTER(C.c_float) * len(ptrs))(*[a.ctypes.data_as(C.POINTER(C.c_float)) for a in ptrs])
-        st = engine._lib.fg_batch_get_density(batch._h, arr)
-        if st != 0:
-            raise RuntimeError("density copy failed")
-    e2e_step()
-    if td:
-        td.barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_step()
-    e2e_s = reduce_max(td, time.perf_counter() - t0) / args.steps
-    h2d = sum(t.nbytes for t in tiles)
-    d2h = h2d
-    e2e_value = world * out_px / e2e_s / 1e6
+        batch.density_into([p.array for p in pin_out])
 
-    # Plain per-tile path (one render_tile call per tile, each making and freeing its buffers).
+    step()
     t0 = time.perf_counter()
-    d_plain = [fg.render_tile(t, p, engine) for t, p in zip(tiles, params)]
+    for _ in range(steps):
+        step()
+    secs = (time.perf_counter() - t0) / steps
+    for p in pin_in + pin_out:
+        p.free()
+    return secs, sum(t.nbytes for t in tiles)
+
+
+def oracle_tiles(jobs, threads):
+    """Renders (stock, pixel um, exposure tile, seed) jobs with the CPU oracle (the reference's hit
+    rule), one tile per host thread as the reference's rayon tile map does (image_pipeline.rs:427).
+    Returns (seconds, densities)."""
+    from oracle import oracle as orc
+
+    orc.lib()
+
+    def one(j):
+        stock, px, tile, seed = j
+        return orc.render_tile(stock, px, tile, 1.0, 0.0, seed, orc.FAITHFUL, 1)[0]
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        dens = list(ex.map(one, jobs))
+    return time.perf_counter() - t0, dens
+
+
+# ------------------------------------------------------------------------------------------------
+# C4 (headline)
+
+def c4_batch_inputs(fg, film, im, img, engine):
+    """Exposure tiles of the C4 sample from the renderer's own stages (per layer: the channel
+    upscaled to the render size with Lanczos3, then the camera gate and gelatin PSF)."""
+    side = img.shape[0]
+    R = side * C4_SS
+    grid, _, _ = im.tile_grid(R, R, C4_GRAIN, C4_TILE)
+    nt = len(grid)
+    sample = c4_sample(nt)
+    params, tiles = [], []
+    for c in range(3):
+        src = film.resize_u8(np.ascontiguousarray(img[..., c]), R, R, film.LANCZOS3, engine)
+        heff, _ = film.gelatin_psf(src, engine)
+        del src
+        for cc, i in sample:
+            if cc != c:
+                continue
+            t = grid[i]
+            params.append(fg.tile_params("t-max", 1.0 / C4_GRAIN, t.tw, t.th, 1.0, 0.0,
+                                         im.tile_seed((SEED + COLOR_SEED_OFFSETS[c]) & M64, t)))
+            tiles.append(np.ascontiguousarray(heff[t.y_start:t.y_start + t.th, t.x_start:t.x_start + t.tw]))
+        del heff
+    all_px = 3 * sum(t.tw * t.th for t in grid)
+    return params, tiles, all_px, len(grid)
+
+
+def run_c4(args):
+    import fgrain_gb300 as fg
+    from fgrain_gb300 import film
+    from fgrain_gb300 import image as im
+
+    rank, world, local, td = dist()
+    side = args.film_side
+    img = c4_image(side)
+    out_pxc = side * side * 3
+    engine = fg.GpuEngine(local)
+    params, tiles, all_px, nt = c4_batch_inputs(fg, film, im, img, engine)
+    sample_px = sum(p.width_px * p.height_px for p in params)
+    rep_pxc = out_pxc * sample_px / all_px  # output pixel-channels the batch stands for
+
+    batch = fg.Batch(params, engine, use_graph=True, autotune=True)
+    batch.set_exposure(tiles)
+    for _ in range(max(args.warmup, 0)):
+        batch.run()
+        batch.wait()
+    barrier(td)
+    with Clocks(local) as clk:
+        ms = batch.time(args.steps)
+    stats = batch.wait()
+    barrier(td)
+    clocks = clk.summary()
+    per_step = reduce_max(td, ms) / args.steps
+    value = world * rep_pxc / (per_step / 1e3) / 1e6
+    d_batched = batch.density()
+    e2e_steps = max(3, args.steps // 4)
+    e2e_s, e2e_bytes = host_to_host(fg, batch, tiles, e2e_steps)
+    e2e_s = reduce_max(td, e2e_s)
+    batch.close()
+
+    # Plain per-tile path against a batch of the same tiles, both host to host.
+    sub = list(range(0, len(params), C4_PLAIN_EVERY))
+    sp = [params[i] for i in sub]
+    st_ = [tiles[i] for i in sub]
+    fg.render_tile(st_[0], sp[0], engine)  # warm-up
+    t0 = time.perf_counter()
+    d_plain = [fg.render_tile(t, p, engine) for t, p in zip(st_, sp)]
     plain_s = time.perf_counter() - t0
-    plain_value = out_px / plain_s / 1e6
-    Tb = np.concatenate([(10.0 ** -(d.astype(np.float64) - 0.05)).ravel() for d in d_batched])
-    Tp = np.concatenate([(10.0 ** -(d.astype(np.float64) - 0.05)).ravel() for d in d_plain])
-    mean_t_err = abs(Tb.mean() - Tp.mean()) / Tp.mean()
-    bit_identical = all(np.array_equal(a, b) for a, b in zip(d_batched, d_plain))
+    sub_pxc = out_pxc * sum(p.width_px * p.height_px for p in sp) / all_px
+    b2 = fg.Batch(sp, engine, use_graph=True, autotune=True)
+    b2_s, _ = host_to_host(fg, b2, st_, 3)
+    b2.close()
+    plain_identical = all(np.array_equal(d_batched[i], d) for i, d in zip(sub, d_plain))
 
-    # Roofline of the transport kernel: algorithmic bytes per launch = 4 B exposure gather per
-    # photon + 8 B count read-modify-write per hit + 116 B per crystal (48 B record, 64 B node,
-    # 4 B count zero) read once.
-    P, H, N = stats["photons"], stats["hits"], stats["crystals"]
-    alg_bytes = 4.0 * P + 8.0 * H + 116.0 * N
-    peak, peak_kind = measured_peak()
-    achieved = alg_bytes / (stats["transport_ms"] / 1e3) / 1e9
-    photons_per_s = P / (stats["transport_ms"] / 1e3)
-    c2_full = args.workload == "c2" and full
-    rl_transport = {"bound": "hbm", "kernel": "k_transport", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                    "frac": achieved / peak, "peak_source": peak_kind,
-                    "traffic": profile_traffic() if c2_full else None, "alg_bytes_per_launch": alg_bytes,
-                    "ms_per_launch": stats["transport_ms"]}
-    # Roofline of the Bridson kernel: it stages every synthesis cell of its column and halo from the
-    # tile's cell grid and writes the column back, so 4 B read + 4 B written per cell at least.
-    b_alg = 8.0 * stats["cells"]
-    b_ach = b_alg / (stats["bridson_ms"] / 1e3) / 1e9
-    rl_bridson = {"bound": "hbm", "kernel": "k_bridson", "achieved": b_ach, "peak": peak, "unit": "GB/s",
-                  "frac": b_ach / peak, "peak_source": peak_kind,
-                  "traffic": profile_traffic("k_bridson_c2.md") if c2_full else None, "alg_bytes_per_launch": b_alg,
-                  "ms_per_launch": stats["bridson_ms"],
-                  "note": "issue- and barrier-bound (shared-memory Bridson rounds), not memory-bound"}
-    dominant = rl_bridson if stats["bridson_ms"] > stats["transport_ms"] else rl_transport
+    dominant, rls = rooflines(stats, "c4")
+    res = {}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        # CPU oracle on 16 tiles of the batch, one tile per thread; mean T against the device's.
+        threads = min(os.cpu_count() or 1, 16)
+        csub = list(range(0, len(params), C4_CPU_EVERY))[:16]
+        jobs = [("t-max", 1.0 / C4_GRAIN, tiles[i], params[i].seed) for i in csub]
+        secs, dens = oracle_tiles(jobs, threads)
+        cpu_pxc = out_pxc * sum(params[i].width_px * params[i].height_px for i in csub) / all_px
+        res["cpu_baseline"] = {
+            "value": cpu_pxc / secs / 1e6, "unit": "Mpx/s", "cores": threads, "kind": "port",
+            "sample": f"{len(csub)} of the C4 batch's tiles (every {C4_STRIDE * C4_CPU_EVERY}th tile of the photograph), "
+                      f"one tile per thread on {threads} threads, C++ restatement of the reference CPU path with the "
+                      f"reference's hit rule; output pixel-channels scaled by tile pixels"}
+        Td = np.array([mean_T(d_batched[i]) for i in csub])
+        To = np.array([mean_T(d) for d in dens])
+        res["mean_T_rel_err_vs_oracle"] = float(abs(Td.mean() - To.mean()) / To.mean())
+        res["mean_T_vs_oracle"] = {"device": float(Td.mean()), "oracle": float(To.mean()), "tiles": len(csub),
+                                   "per_tile_rel_sd": float(np.std(To) / To.mean())}
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu and args.workload == "c2":
-        threads = os.cpu_count() or 1
-        secs, px = oracle_sample(params, tiles, max(threads, 4), threads)
-        total_px = sum(p.width_px * p.height_px for p in params)
-        cpu_value = out_px * (px / total_px) / secs / 1e6
-        cpu = {"value": cpu_value, "unit": "Mpx/s", "cores": threads, "kind": "port",
-               "sample": f"{max(threads, 4)} of the 49 C2 tiles rendered by the C++ restatement of the "
-                         f"reference CPU path (faithful hit rule), tiles in parallel; scaled by tile pixels"}
+    # The whole photograph through fg_render_film, host pixels to host pixels.
+    opts = film.FilmRenderOptions(preset="t-max", grain_size_px=C4_GRAIN, supersample=C4_SS, color=True, seed=SEED,
+                                  eberhard=0.5, batch_bytes=int(args.batch_gb * 2**30))
+    film.render_film(img[:512, :512], opts, engine)  # warm-up on a corner
+    barrier(td)
+    t0 = time.perf_counter()
+    rep, out = film.render_film(img, opts, engine)
+    film_s = reduce_max(td, time.perf_counter() - t0)
+
+    extras = {}
+    if not args.no_extras:
+        extras["c2"] = c2_extra(fg, engine, min(args.steps, 10))
+        extras["c3"] = c3_extra(fg, engine, min(args.steps, 3))
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "Mpx/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": (("" if full else f"first {len(params)} tiles of ") + C2_WORKLOAD +
-                                    ", batched graph path") if args.workload == "c2" else
-                                   "C3: 64 square images, sides log-uniform 64-512 px, tri-x / t-max / hp5, push "
-                                   "0-3, supersample 1-4 (master seed 0), all tiles in one autotuned batch",
-                       "tiles": len(params),
-                       "internal_px": int(exposure.size) if exposure is not None else int(c3_int_px),
-                       "output_px": out_px, "l2": "working set (crystals, LBVH, grids) exceeds L2; no flush",
+            "config": {"workload": C4_WORKLOAD + (" (reduced size)" if side != C4_SIDE else "") +
+                       f"; one step = one batch of {len(params)} of its {3 * nt} tiles (every {C4_STRIDE}th), "
+                       "device-resident, batched graph path",
+                       "tiles_per_step": len(params), "tiles_total": 3 * nt,
+                       "output_px_channels_per_step": rep_pxc, "output_px_channels_total": out_pxc,
+                       "l2": "working set (crystals, trees, grids) exceeds L2; no flush",
                        "parallelism": f"replicas x{world}"},
-            "photons_per_s": photons_per_s,
-            "plain_mpx_s": plain_value,
-            "batched_over_plain": value / world / plain_value,
-            "mean_T_rel_err_batched_vs_plain": mean_t_err,
-            "batched_equals_plain_bitwise": bit_identical,
+            "photons_per_s": stats["photons"] / (stats["transport_ms"] / 1e3),
             "stage_ms": {k: stats[k] for k in ("synth_ms", "bridson_ms", "bvh_ms", "transport_ms", "develop_ms",
                                                "scan_ms", "total_ms")},
             "work": {k: stats[k] for k in ("crystals", "photons", "hits", "rays", "scan_hits", "scan_fallbacks",
                                            "cells", "developed", "clumps")},
             "launch_shape": {"transport_threads": stats["transport_threads"],
                              "transport_blocks": stats["transport_blocks"], "scan_bin_px": stats["scan_bin_px"]},
-            "e2e": {"value": e2e_value, "unit": "Mpx/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "e2e": {"value": out_pxc * world / film_s / 1e6, "unit": "Mpx/s", "h2d_bytes_per_step": int(img.nbytes),
+                    "d2h_bytes_per_step": int(out.nbytes), "steps": 1,
+                    "what": "the whole photograph per fg_render_film call, host u8 pixels to host u8 pixels",
+                    "seconds": film_s, "tiles": rep.total_tiles, "crystals": rep.total_crystals,
+                    "photons": rep.photons, "stage_ms": rep.extra},
+            "e2e_batch": {"value": world * rep_pxc / e2e_s / 1e6, "unit": "Mpx/s", "h2d_bytes_per_step": e2e_bytes,
+                          "d2h_bytes_per_step": e2e_bytes, "steps": e2e_steps,
+                          "what": "the step's batch through the batch API, page-locked host buffers"},
+            "plain_mpx_s": sub_pxc / plain_s / 1e6,
+            "batched_host_mpx_s": sub_pxc / b2_s / 1e6,
+            "batched_over_plain": plain_s / b2_s,
+            "batched_over_plain_basis": f"{len(sp)} tiles of the batch, both host to host: fg_render_tile per tile "
+                                        "against one batch of the same tiles (exposure in, density out)",
+            "batched_equals_plain_bitwise": plain_identical,
             "gpu_launches": stats["kernel_launches"] * args.steps,
             "roofline": dominant,
-            "rooflines": {"k_bridson": rl_bridson, "k_transport": rl_transport},
+            "rooflines": rls,
             "clocks": clocks,
         }
-        if cpu:
-            line["cpu_baseline"] = cpu
+        line.update(res)
+        line.update(extras)
         print(json.dumps(line))
-    for p in pin_in + pin_out:
-        p.free()
-    batch.close()
     if td:
         td.destroy_process_group()
 
 
-def run_c4(args):
-    """C4: a 4096 x 4096 RGB photograph (three dye layers), t-max, grain 1.1 px, supersample 4, so
-    16384^2 per channel and 2704 tiles per channel, rendered whole by fg_render_film from host
-    pixels to host pixels (image stages, tiles in consecutive batches within the device budget,
-    finish).  Inputs: per channel, blurred uniform noise (sigma 16 px) to the power 2.2, as u8.
-    Reported next to the headline, not instead of it: value and e2e are the same host-to-host
-    number, output pixel-channels per second."""
+def c2_extra(fg, engine, steps):
+    exposure = c2_inputs()
+    grid, params, tiles = c2_tiles(exposure)
+    b = fg.Batch(params, engine, use_graph=True, autotune=True)
+    b.set_exposure(tiles)
+    for _ in range(2):
+        b.run()
+        b.wait()
+    ms = b.time(steps) / steps
+    stats = b.wait()
+    d_b = b.density()
+    h_s, h_bytes = host_to_host(fg, b, tiles, 3)
+    b.close()
+    t0 = time.perf_counter()
+    d_p = [fg.render_tile(t, p, engine) for t, p in zip(tiles, params)]
+    plain_s = time.perf_counter() - t0
+    px = C2_OUT * C2_OUT
+    dominant, _ = rooflines(stats, "c2")
+    return {"workload": C2_WORKLOAD, "value": px / (ms / 1e3) / 1e6, "ms_per_step": ms, "steps": steps,
+            "e2e_batch": {"value": px / h_s / 1e6, "h2d_bytes_per_step": h_bytes, "d2h_bytes_per_step": h_bytes},
+            "plain_mpx_s": px / plain_s / 1e6, "batched_over_plain": plain_s / h_s,
+            "batched_over_plain_device": plain_s / (ms / 1e3),
+            "batched_equals_plain_bitwise": all(np.array_equal(x, y) for x, y in zip(d_b, d_p)),
+            "photons_per_s": stats["photons"] / (stats["transport_ms"] / 1e3),
+            "stage_ms": {k: stats[k] for k in ("synth_ms", "bridson_ms", "bvh_ms", "transport_ms", "develop_ms",
+                                               "scan_ms", "total_ms")},
+            "roofline": dominant}
+
+
+def c3_extra(fg, engine, steps):
+    params, tiles, out_px = c3_tiles()
+    b = fg.Batch(params, engine, use_graph=True, autotune=True)
+    b.set_exposure(tiles)
+    b.run()
+    b.wait()
+    ms = b.time(steps) / steps
+    stats = b.wait()
+    d_b = b.density()
+    h_s, h_bytes = host_to_host(fg, b, tiles, 1)
+    b.close()
+    t0 = time.perf_counter()
+    d_p = [fg.render_tile(t, p, engine) for t, p in zip(tiles, params)]
+    plain_s = time.perf_counter() - t0
+    return {"workload": "C3: 64 square images, sides log-uniform 64-512 px, tri-x / t-max / hp5, push 0-3, "
+                        "supersample 1-4 (master seed 0), all tiles in one autotuned batch",
+            "tiles": len(params), "value": out_px / (ms / 1e3) / 1e6, "ms_per_step": ms, "steps": steps,
+            "e2e_batch": {"value": out_px / h_s / 1e6, "h2d_bytes_per_step": h_bytes, "d2h_bytes_per_step": h_bytes},
+            "plain_mpx_s": out_px / plain_s / 1e6, "batched_over_plain": plain_s / h_s,
+            "batched_over_plain_device": plain_s / (ms / 1e3),
+            "batched_equals_plain_bitwise": all(np.array_equal(x, y) for x, y in zip(d_b, d_p)),
+            "stage_ms": {k: stats[k] for k in ("synth_ms", "bridson_ms", "bvh_ms", "transport_ms", "develop_ms",
+                                               "scan_ms", "total_ms")}}
+
+
+# ------------------------------------------------------------------------------------------------
+# C2 / C3 / fast as lines of their own (not the headline)
+
+def run_single(args):
     import fgrain_gb300 as fg
-    from fgrain_gb300 import film
-    from scipy.ndimage import gaussian_filter
 
     rank, world, local, td = dist()
-    rng = np.random.default_rng(1)
-    side = args.film_side
-    img = np.stack([np.clip(gaussian_filter(rng.random((side, side)), 16.0, mode="reflect"), 0.0, 1.0) ** 2.2
-                    for _ in range(3)], -1)
-    img = np.ascontiguousarray(np.round(img * 255.0).astype(np.uint8))
-    opts = film.FilmRenderOptions(preset="t-max", grain_size_px=1.1, supersample=4, color=True, seed=SEED,
-                                  batch_bytes=int(args.batch_gb * 2**30))
     engine = fg.GpuEngine(local)
-    for _ in range(max(args.warmup, 0)):
-        film.render_film(img, opts, engine)
-    if td:
-        td.barrier()
-    times, reps = [], []
-    with Clocks(local) as ck:
-        for _ in range(args.steps):
-            t0 = time.perf_counter()
-            rep, out = film.render_film(img, opts, engine)
-            times.append(time.perf_counter() - t0)
-            reps.append(rep)
-    t = reduce_max(td, sum(times) / len(times))
-    px = side * side * 3
+    d = c2_extra(fg, engine, args.steps) if args.workload == "c2" else c3_extra(fg, engine, args.steps)
     if rank == 0:
-        value = px * world / t / 1e6
-        rep = reps[-1]
+        px_step = d["value"] * d["ms_per_step"] / 1e3
         print(json.dumps({
-            "metric": METRIC, "value": value, "unit": "Mpx/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": (f"C4: {side}x{side} RGB blurred-noise photograph, t-max, grain 1.1 px, supersample 4 "
-                                    f"({4 * side}^2 per channel), colour, whole photograph per fg_render_film call"
-                                    + ("" if side == 4096 else " (reduced size)")),
-                       "tiles": rep.total_tiles, "output_px_channels": px, "crystals": rep.total_crystals,
-                       "photons": rep.photons, "parallelism": f"replicas x{world}",
-                       "stage_ms": rep.extra},
-            "e2e": {"value": value, "unit": "Mpx/s", "h2d_bytes_per_step": img.nbytes, "d2h_bytes_per_step": out.nbytes},
-            "clocks": ck.summary()}))
+            "metric": METRIC, "value": d["value"] * world, "unit": "Mpx/s", "n_gpus": world, "steps": d["steps"],
+            "warmup": 2 if args.workload == "c2" else 1, "ms_per_step": d["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": d["workload"], "output_px_per_step": px_step, "parallelism": f"replicas x{world}"},
+            "e2e": {"value": d["e2e_batch"]["value"], "unit": "Mpx/s",
+                    "h2d_bytes_per_step": d["e2e_batch"]["h2d_bytes_per_step"],
+                    "d2h_bytes_per_step": d["e2e_batch"]["d2h_bytes_per_step"]},
+            "details": d}))
 
 
 def run_fast(args):
@@ -448,14 +557,13 @@ def run_fast(args):
     rank, world, local, td = dist()
     exposure = c2_inputs()
     H, W = exposure.shape
-    grid, _, _ = tile_grid(W, H, GRAIN)
-    params = [fast.tile_params_fast("tri-x", 1.0 / GRAIN, t.tw, t.th, 1.0, 0.0, tile_seed(SEED, t)) for t in grid]
+    grid, _, _ = tile_grid(W, H, C2_GRAIN)
+    params = [fast.tile_params_fast("tri-x", 1.0 / C2_GRAIN, t.tw, t.th, 1.0, 0.0, tile_seed(SEED, t)) for t in grid]
     tiles = [np.ascontiguousarray(exposure[t.y_start:t.y_start + t.th, t.x_start:t.x_start + t.tw]) for t in grid]
     engine = fg.GpuEngine(local)
     for _ in range(max(args.warmup, 0)):
         fast.render_tiles_fast(params, tiles, engine)
-    if td:
-        td.barrier()
+    barrier(td)
     with Clocks(local) as ck:
         t0 = time.perf_counter()
         for _ in range(args.steps):
@@ -463,7 +571,7 @@ def run_fast(args):
         t = (time.perf_counter() - t0) / args.steps
     t = reduce_max(td, t)
     if rank == 0:
-        value = OUT_W * OUT_H * world / t / 1e6
+        value = C2_OUT * C2_OUT * world / t / 1e6
         h2d = sum(x.nbytes for x in tiles)
         print(json.dumps({
             "metric": METRIC, "value": value, "unit": "Mpx/s", "n_gpus": world, "steps": args.steps,
@@ -471,41 +579,59 @@ def run_fast(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "C2 tiles through the fast approximation (the reference's wgpu tile model: "
                                    "jittered grid, per-crystal Poisson counts, column scan), host to host",
-                       "tiles": len(grid), "output_px": OUT_W * OUT_H, "parallelism": f"replicas x{world}"},
+                       "tiles": len(grid), "output_px": C2_OUT * C2_OUT, "parallelism": f"replicas x{world}"},
             "e2e": {"value": value, "unit": "Mpx/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d},
             "gpu_launches": 5 * args.steps, "clocks": ck.summary()}))
 
 
-C2_WORKLOAD = ("C2: 1024x1024 blurred-noise luminance (sigma 16, seed 1, gamma 2.2), tri-x, grain 2.4 px, push 0, "
-               "supersample 2 (2048^2 internal, 49 tiles)")
-
+# ------------------------------------------------------------------------------------------------
+# Reference arm: the CPU restatement of the reference path, oracle only
 
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    exposure = c2_inputs()
-    grid, params, tiles = c2_tiles(exposure)
+    from oracle import oracle as orc
+
+    side = args.film_side
+    img = c4_image(side)
+    out_pxc = side * side * 3
+    R = side * C4_SS
+    grid, _, _ = orc.film_grid(R, R, C4_GRAIN, C4_TILE)
+    nt = len(grid)
+    sample = c4_sample(nt)
+    warm_n, timed_n = max(args.warmup, 0), 4 * args.steps
+    picks = [sample[k % len(sample)] for k in range(warm_n + timed_n)]
+    heffs = {}
+    for c in sorted({c for c, _ in picks}):  # the oracle's own exposure stages (upscale, PSF)
+        src = orc.resize_u8(np.ascontiguousarray(img[..., c]), R, R, orc.LANCZOS3)
+        heffs[c] = orc.gelatin_psf(src)[0]
+        del src
+    jobs = []
+    for c, i in picks:
+        t = grid[i]
+        jobs.append(("t-max", 1.0 / C4_GRAIN,
+                     np.ascontiguousarray(heffs[c][t.y_start:t.y_start + t.th, t.x_start:t.x_start + t.tw]),
+                     orc.film_tile_seed((SEED + COLOR_SEED_OFFSETS[c]) & M64, t)))
+    heffs.clear()
     threads = os.cpu_count() or 1
-    n = max(threads, 4)
-    for _ in range(max(args.warmup, 0) and 1):
-        oracle_sample(params, tiles, min(n, 4), threads)
-    secs, px = 0.0, 0
-    for _ in range(args.steps):
-        s, p = oracle_sample(params, tiles, n, threads)
-        secs += s
-        px += p
-    total_px = sum(p.width_px * p.height_px for p in params)
-    value = OUT_W * OUT_H * (px / args.steps / total_px) / (secs / args.steps) / 1e6
-    sample = (f"each step renders {n} of the 49 C2 tiles with the C++ restatement of the reference CPU path "
-              f"(faithful hit rule; the Rust reference cannot be built here), tiles in parallel on {threads} "
-              f"threads; output Mpx/s scaled by tile pixels")
+    if warm_n:
+        oracle_tiles(jobs[:warm_n], threads)
+    secs, _ = oracle_tiles(jobs[warm_n:], threads)
+    all_px = 3 * sum(t.tw * t.th for t in grid)
+    px = sum(j[2].size for j in jobs[warm_n:])
+    value = out_pxc * px / all_px / secs / 1e6
+    sample_txt = (f"each step renders 4 C4 tiles (the first {timed_n} tiles of the benchmark's every-{C4_STRIDE}th-tile "
+                  f"sample, rendered together by a {threads}-thread tile map as the reference's rayon map renders "
+                  f"tiles); C++ restatement of the reference CPU path with the reference's hit rule (the Rust "
+                  f"reference cannot be built here); output pixel-channels scaled by tile pixels; each warm-up step "
+                  f"renders one tile")
     print(json.dumps({
-        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mpx/s", "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": C2_WORKLOAD + ", reference CPU path (no GPU used)", "tiles_per_step": n},
-        "cpu_baseline": {"value": value, "unit": "Mpx/s", "cores": threads, "kind": "port", "sample": sample},
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mpx/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": C4_WORKLOAD + ", reference CPU path (no GPU used)", "tiles_per_step": 4},
+        "cpu_baseline": {"value": value, "unit": "Mpx/s", "cores": threads, "kind": "port", "sample": sample_txt},
         "e2e": {"value": value, "unit": "Mpx/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
 
@@ -513,25 +639,18 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=None, help="timed steps (default 10; 1 for c4)")
-    ap.add_argument("--warmup", type=int, default=None, help="untimed steps (default 3; 1 for c4)")
+    ap.add_argument("--steps", type=int, default=10, help="timed steps")
+    ap.add_argument("--warmup", type=int, default=3, help="untimed steps")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--tiles", type=int, default=0, help="render only the first N tiles of C2 (profiling)")
-    ap.add_argument("--workload", choices=["c2", "c3", "c4", "fast"], default="c2",
-                    help="c2: the headline configuration; c3: the mixed batch; c4: a 4096^2 RGB photograph at "
-                         "supersample 4 through the film renderer; fast: the C2 tiles through the fast "
-                         "approximation (c3, c4 and fast are reported, not the headline)")
-    ap.add_argument("--film-side", type=int, default=4096, help="c4: side of the RGB photograph (4096 for C4)")
+    ap.add_argument("--no-extras", action="store_true", help="skip the C2 and C3 keys of the C4 line")
+    ap.add_argument("--workload", choices=["c4", "c2", "c3", "fast"], default="c4",
+                    help="c4: the headline (C4 with C2 and C3 as extra keys); c2, c3: those configurations alone; "
+                         "fast: the C2 tiles through the fast approximation")
+    ap.add_argument("--film-side", type=int, default=C4_SIDE, help="side of the C4 photograph (4096 for C4)")
     ap.add_argument("--batch-gb", type=float, default=0.0,
-                    help="c4: device GiB one batch of tiles may use (0: 70 %% of the free memory)")
-    ap.add_argument("--profile-region", action="store_true",
-                    help="bracket the timed replays with cudaProfilerStart/Stop")
+                    help="device GiB one batch of the whole-photograph render may use (0: 70 %% of the free memory)")
     args = ap.parse_args()
-    if args.steps is None:
-        args.steps = 1 if args.workload == "c4" else 10
-    if args.warmup is None:
-        args.warmup = 1 if args.workload == "c4" else 3
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "c4":
@@ -539,7 +658,7 @@ def main():
     elif args.workload == "fast":
         run_fast(args)
     else:
-        run_ours(args)
+        run_single(args)
 
 
 if __name__ == "__main__":

@@ -7,7 +7,7 @@ that ABI, used by the tests and the benchmark.
 from .api import (  # noqa: F401
     DevelopmentConfig, DevelopmentReport, EmulsionConfig, ExposureConfig, GelatinOptics,
     GpuEngine, GpuError, Morphology, ScanConfig, ScanMode, VirtualEmulsionLayer,
-    develop_emulsion, expose_emulsion, get_gpu_engine, replay_rays, replay_segments,
+    develop_emulsion, expose_emulsion, get_gpu_engine, reference_tree, replay_rays, replay_segments,
     scan_emulsion, scan_ray_hits, SEGMENT_DTYPE, Batch, render_tile, tile_params,
     PinnedArray, scan_signal, scan_backward, OTF_SIGMA_REFERENCE,
 )

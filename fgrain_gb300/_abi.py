@@ -191,6 +191,7 @@ PROTOTYPES = {
     "fg_replay_rays": (_st, [_vp, _vp, _dp, _dp, C.c_size_t, C.c_int, _u32p, _u32p,
                              C.c_size_t, _szp, _dp]),
     "fg_scan_ray_hits": (_st, [_vp, _vp, C.POINTER(fg_scan_cfg), C.c_uint64, _u16p]),
+    "fg_emulsion_reference_tree": (_st, [_vp, _vp, C.c_int, _u32p, _u32p, _dp, C.c_size_t, _szp, _szp]),
     "fg_blend_tiles": (_st, [_vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _u32p,
                              C.POINTER(_fp), _fp]),
     "fg_scanner_otf": (_st, [_vp, _fp, C.c_uint32, C.c_uint32, _fp, _fp]),

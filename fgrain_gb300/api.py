@@ -383,17 +383,17 @@ SEGMENT_DTYPE = np.dtype([("origin", "<f8", 3), ("dir", "<f8", 3), ("step", "<f8
                           ("energy", "<f8"), ("photon", "<u4"), ("bounce", "<u4")])
 
 
-HMAX = 48  # most hits the device keeps per segment (larger lists raise FG_ERR_DEVICE_OVERFLOW)
+REPLAY_IDS_PER_SEGMENT = 64  # room for hit ids per segment in replay_segments' output
 
 
 def replay_segments(emulsion: VirtualEmulsionLayer, config: ExposureConfig, seed: int, segments):
-    """Exact replay of recorded photon segments (hit rule and per-hit arithmetic of
-    transport.rs:353-384 in FP64).  Latent counts are added to the emulsion.  Returns
-    (offsets[n+1], hit ids in canonical order)."""
+    """Exact replay of recorded photon segments: the reference's tree walk and hit rule
+    (bvh.rs:300-347, crystal.rs:140-217) and its per-hit arithmetic (transport.rs:108-138) in FP64.
+    Latent counts are added to the emulsion.  Returns (offsets[n+1], hit ids in absorption order)."""
     segs = np.ascontiguousarray(segments, dtype=SEGMENT_DTYPE)
     n = segs.shape[0]
     offsets = np.zeros(n + 1, np.uint32)
-    cap = max(n * HMAX, 1)
+    cap = max(n * REPLAY_IDS_PER_SEGMENT, 1)
     ids = np.zeros(cap, np.uint32)
     nh = C.c_size_t()
     e = emulsion.engine
@@ -402,7 +402,25 @@ def replay_segments(emulsion: VirtualEmulsionLayer, config: ExposureConfig, seed
                                         segs.ctypes.data_as(C.POINTER(_abi.fg_segment)), n,
                                         _ptr(offsets, C.c_uint32), _ptr(ids, C.c_uint32), cap,
                                         C.byref(nh)))
+    if nh.value > cap:
+        raise ValueError(f"{nh.value} hits exceed the {cap} ids replay_segments keeps")
     return offsets, ids[: nh.value].copy()
+
+
+def reference_tree(emulsion: VirtualEmulsionLayer, developed_only=False):
+    """The device's copy of the reference tree (bvh.rs:157-295) over the crystals, or over the
+    developed ones (the scan's tree): (crystal ids in the tree's index order, leaves as rows of
+    (first index, count) sorted by first index, leaf boxes as rows of lo xyz, hi xyz)."""
+    e = emulsion.engine
+    cap = max(len(emulsion), 1)
+    order = np.zeros(cap, np.uint32)
+    leaves = np.zeros((cap, 2), np.uint32)
+    boxes = np.zeros((cap, 6))
+    ne, nl = C.c_size_t(), C.c_size_t()
+    _check(e, e._lib.fg_emulsion_reference_tree(e._h, emulsion._h, int(developed_only), _ptr(order, C.c_uint32),
+                                                _ptr(leaves, C.c_uint32), _ptr(boxes, C.c_double), cap,
+                                                C.byref(ne), C.byref(nl)))
+    return order[: ne.value].copy(), leaves[: nl.value].copy(), boxes[: nl.value].copy()
 
 
 def replay_rays(emulsion: VirtualEmulsionLayer, origins, dirs, developed_only=True):
@@ -506,6 +524,12 @@ class Batch:
         e = self.engine
         _check(e, e._lib.fg_batch_get_density(self._h, ptrs))
         return outs
+
+    def density_into(self, outs):
+        """Copies every tile's density into the given float32 arrays (e.g. page-locked ones)."""
+        ptrs = (C.POINTER(C.c_float) * len(outs))(*[_ptr(o, C.c_float) for o in outs])
+        e = self.engine
+        _check(e, e._lib.fg_batch_get_density(self._h, ptrs))
 
     def tile_crystals(self, tile: int) -> dict:
         e = self.engine

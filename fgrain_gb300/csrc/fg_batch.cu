@@ -1,7 +1,8 @@
 // Batched tile pipeline: many exposure tiles (uneven sizes, stocks, push, seeds) rendered to
 // negative density in one sequence of launches:
-//   synthesis (column Bridson, 4 colour classes) -> thinning -> compaction in brick order -> LBVH
-//   -> persistent transport over all tiles' photons -> development -> bins -> binned scan.
+//   synthesis (column Bridson, 4 colour classes) -> thinning -> compaction in brick order -> the
+//   reference tree (fg_rtree.cuh) -> persistent transport over all tiles' photons -> development ->
+//   the reference tree over the developed crystals -> bins -> binned scan.
 // Every kernel covers all tiles at once (per-tile descriptors in HBM, tile found by binary search
 // on a prefix of work items), every buffer is allocated when the plan is made, and nothing waits
 // on the host, so the sequence is captured once into a CUDA graph and replayed.  An autotuner
@@ -43,9 +44,14 @@ void launch_scan_prep(const ScanTile* tiles, int ntiles, unsigned long long nslo
                       cudaStream_t st);
 uint32_t scan_bin_px(uint32_t spp);
 
-// Per-tile state for the batched LBVH, development and binning kernels.
+// Nodes per crystal slot of the tile trees: the reference tree has about 0.67 nodes per crystal and
+// a tile holds about 0.72 crystals per slot, so 0.8 leaves a wide margin (an overflow fails the run).
+constexpr double RT_NODE_FRAC = 0.8;
+
+// Per-tile state for the batched trees, development and binning kernels.
 struct __align__(16) BTile {
-  unsigned long long cbase;   // first crystal slot
+  unsigned long long cbase;   // first crystal slot (also the tile's first element of its trees)
+  unsigned long long nbase;   // first node of the tile's trees
   unsigned long long bin_base;
   double fe, prox;            // filament expansion, clumping proximity (development.rs:12-27)
   double max_base;            // largest undeveloped max_dim (device-written)
@@ -54,7 +60,7 @@ struct __align__(16) BTile {
   uint32_t nbx, nby;
   float binw_x, binw_y;
   float pad;                  // leaf box padding
-  uint32_t _pad;
+  uint32_t ncap;              // node capacity of the tile's trees
 };
 
 __device__ __forceinline__ int btile_of(const BTile* tiles, int ntiles, unsigned long long g) {
@@ -67,7 +73,7 @@ __device__ __forceinline__ int btile_of(const BTile* tiles, int ntiles, unsigned
 }
 
 __global__ void k_set_n(const SynthTile* syn, int ntiles, const uint32_t* slot_scan, BTile* bt, TileDesc* td,
-                        ScanTile* sc, uint32_t* ncrys) {
+                        ScanTile* sc, uint32_t* ncrys, RTile* rt) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntiles) return;
   const uint32_t n = slot_scan[syn[t].slot_base + (1ull << (2 * syn[t].slot_bits))] - slot_scan[syn[t].slot_base];
@@ -77,150 +83,19 @@ __global__ void k_set_n(const SynthTile* syn, int ntiles, const uint32_t* slot_s
   td[t].n = nn;
   sc[t].n = nn;
   ncrys[t] = nn;
+  rt[t].n = nn;
 }
 
-__device__ __forceinline__ int kdelta_b(const uint64_t* keys, long long n, long long i, long long j) {
-  if (j < 0 || j >= n) return -1;
-  const uint64_t ki = keys[i], kj = keys[j];
-  if (ki == kj) return 64 + __clz(static_cast<uint32_t>(i ^ j));
-  return __clzll(ki ^ kj);
-}
-
-// Karras internal nodes of every tile (node array and keys offset by the tile's crystal base).
-__global__ void k_karras_b(const BTile* __restrict__ bt, int ntiles, unsigned long long ncap,
-                           const uint64_t* __restrict__ keys_all, Node* nodes_all, int* leaf_parent_all,
-                           int* visit_all) {
-  const unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
-  if (g >= ncap) return;
-  const BTile& t = bt[btile_of(bt, ntiles, g)];
-  const long long i = static_cast<long long>(g - t.cbase);
-  const long long n = t.n;
-  Node* nodes = nodes_all + t.cbase;
-  int* leaf_parent = leaf_parent_all + t.cbase;
-  if (n == 1) {
-    if (i == 0) {
-      const float q = __int_as_float(0x7fc00000);
-      nodes[0].a = make_float4(q, q, q, q);
-      nodes[0].b = make_float4(q, q, q, q);
-      nodes[0].c = make_float4(q, q, q, q);
-      nodes[0].d = make_int4(~0, INT32_MIN, -1, 0);
-      leaf_parent[0] = 0;
-      visit_all[t.cbase] = 1;  // the lone leaf must climb past its root
-    }
-    return;
-  }
-  if (i >= n - 1) return;
-  const uint64_t* keys = keys_all + t.cbase;
-  const int dir = (kdelta_b(keys, n, i, i + 1) - kdelta_b(keys, n, i, i - 1)) >= 0 ? 1 : -1;
-  const int dmin = kdelta_b(keys, n, i, i - dir);
-  long long lmax = 2;
-  while (kdelta_b(keys, n, i, i + lmax * dir) > dmin) lmax <<= 1;
-  long long l = 0;
-  for (long long s = lmax >> 1; s >= 1; s >>= 1)
-    if (kdelta_b(keys, n, i, i + (l + s) * dir) > dmin) l += s;
-  const long long j = i + l * dir;
-  const int dnode = kdelta_b(keys, n, i, j);
-  long long s = 0, st = l;
-  do {
-    st = (st + 1) >> 1;
-    if (kdelta_b(keys, n, i, i + (s + st) * dir) > dnode) s += st;
-  } while (st > 1);
-  const long long gamma = i + s * dir + (dir < 0 ? -1 : 0);
-  const long long lo = i < j ? i : j, hi = i < j ? j : i;
-  int left, right;
-  if (lo == gamma) {
-    left = ~static_cast<int>(gamma);
-    leaf_parent[gamma] = static_cast<int>(i);
-  } else {
-    left = static_cast<int>(gamma);
-    nodes[gamma].d.z = static_cast<int>(i);
-  }
-  if (hi == gamma + 1) {
-    right = ~static_cast<int>(gamma + 1);
-    leaf_parent[gamma + 1] = static_cast<int>(i);
-  } else {
-    right = static_cast<int>(gamma + 1);
-    nodes[gamma + 1].d.z = static_cast<int>(i);
-  }
-  nodes[i].d.x = left;
-  nodes[i].d.y = right;
-  nodes[i].d.w = static_cast<int>(hi);
-  if (i == 0) nodes[0].d.z = -1;
-}
-
-// Bottom-up fit of every tile's tree (leaf boxes bound the whole crystal shape, padded).
-__global__ void k_fit_b(const BTile* __restrict__ bt, int ntiles, unsigned long long ncap,
-                        const float4* __restrict__ A, const float4* __restrict__ Q, const float4* __restrict__ D,
-                        Node* nodes_all, const int* leaf_parent_all, int* visit_all) {
-  const unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
-  if (g >= ncap) return;
-  const BTile& t = bt[btile_of(bt, ntiles, g)];
-  const uint32_t s = static_cast<uint32_t>(g - t.cbase);
-  if (s >= t.n) return;
-  Node* nodes = nodes_all + t.cbase;
-  int* visit = visit_all + t.cbase;
-  const float4 a = A[g], q = Q[g], d = D[g];
-  float lo[3], hi[3];
-  {
-    const float x = q.x, y = q.y, z = q.z, w = q.w;
-    const float R[3][3] = {{1.f - 2.f * (y * y + z * z), 2.f * (x * y - z * w), 2.f * (x * z + y * w)},
-                           {2.f * (x * y + z * w), 1.f - 2.f * (x * x + z * z), 2.f * (y * z - x * w)},
-                           {2.f * (x * z - y * w), 2.f * (y * z + x * w), 1.f - 2.f * (x * x + y * y)}};
-    const float dm[3] = {d.x, d.y, d.z};
-    const bool cubic = __float_as_int(d.w) == 0;
-    const float p[3] = {a.x, a.y, a.z};
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      float ext;
-      if (cubic) {
-        ext = fabsf(R[i][0]) * dm[0] + fabsf(R[i][1]) * dm[1] + fabsf(R[i][2]) * dm[2];
-      } else {
-        const float u = R[i][0] * dm[0], v = R[i][1] * dm[1], tt = R[i][2] * dm[2];
-        ext = sqrtf(u * u + v * v + tt * tt);
-      }
-      const float h = ext * 1.0001f + t.pad;
-      lo[i] = p[i] - h;
-      hi[i] = p[i] + h;
-    }
-  }
-  int code = ~static_cast<int>(s);
-  int p = leaf_parent_all[g];
-  while (p >= 0) {
-    float* f = reinterpret_cast<float*>(&nodes[p]);
-    const int off = (nodes[p].d.x == code) ? 0 : 6;
-    __stcg(f + off + 0, lo[0]);
-    __stcg(f + off + 1, lo[1]);
-    __stcg(f + off + 2, lo[2]);
-    __stcg(f + off + 3, hi[0]);
-    __stcg(f + off + 4, hi[1]);
-    __stcg(f + off + 5, hi[2]);
-    __threadfence();
-    if (atomicAdd(&visit[p], 1) == 0) return;
-    __threadfence();
-    float v[12];
-#pragma unroll
-    for (int k = 0; k < 12; ++k) v[k] = __ldcg(f + k);
-    lo[0] = fminf(v[0], v[6]);
-    lo[1] = fminf(v[1], v[7]);
-    lo[2] = fminf(v[2], v[8]);
-    hi[0] = fmaxf(v[3], v[9]);
-    hi[1] = fmaxf(v[4], v[10]);
-    hi[2] = fmaxf(v[5], v[11]);
-    code = p;
-    p = __ldcg(&nodes[p].d.z);
-  }
-}
-
-// Four-wide collapse of every tile's tree (the transport walk).
-__global__ void k_collapse4_b(const BTile* __restrict__ bt, int ntiles, unsigned long long ncap,
-                              const Node* __restrict__ nodes_all, Node4* __restrict__ out_all) {
-  const unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
-  if (g >= ncap) return;
-  const BTile& t = bt[btile_of(bt, ntiles, g)];
-  const unsigned long long i = g - t.cbase;
-  const unsigned long long nint = t.n > 1 ? t.n - 1 : (t.n ? 1 : 0);
-  if (i >= nint) return;
-  collapse_node4(nodes_all + t.cbase, static_cast<int>(i), out_all + g);
+// Inputs of the scan's tree per tile: the tile's developed crystals in slot order (transmittance.rs:
+// 86-89 keeps them in crystal order), from the exclusive sum of the developed flags.
+__global__ void k_scan_tree_tiles(const BTile* bt, int ntiles, const uint32_t* devscan, const uint32_t* devlist,
+                                  RTile* rt) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  const uint32_t first = devscan[bt[t].cbase], last = devscan[bt[t].cbase + bt[t].n];
+  rt[t].order = devlist + first;
+  rt[t].obase = bt[t].cbase;
+  rt[t].n = last - first;
 }
 
 // ---- development (development.rs:59-188), batched; see fg_develop.cu for the reasoning ----
@@ -294,11 +169,13 @@ __device__ __forceinline__ void uf_unite_b(int* parent, int a, int b, uint32_t* 
 }
 
 // Links each developed crystal to the developed crystals it touches (union-find), walking the
-// four-wide tree with the query box: a leaf is reached iff its box and its ancestors' boxes overlap
-// the query, as in the binary walk (ancestor boxes contain their descendants'), and the union-find
-// roots do not depend on the order of the unions.
+// tile's reference tree with the query box: a leaf is reached iff its box and its ancestors' boxes
+// overlap the query (ancestor boxes contain their descendants'), and a crystal within the touch
+// distance lies inside its own leaf box, so the query finds it whatever the tree (bvh.rs:350-402);
+// the union-find roots do not depend on the order of the unions.
 __global__ void k_link_b(const BTile* __restrict__ bt, int ntiles, unsigned long long ncap,
-                         const float4* __restrict__ A, const float4* __restrict__ D, const Node4* __restrict__ nodes_all,
+                         const float4* __restrict__ A, const float4* __restrict__ D, const Node* __restrict__ rnode_all,
+                         const uint2* __restrict__ rleaf_all, const uint32_t* __restrict__ ridx_all,
                          const uint8_t* __restrict__ developed, int* parent, const uint32_t* __restrict__ list,
                          const uint32_t* __restrict__ ndev, uint32_t* err) {
   const unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
@@ -306,7 +183,9 @@ __global__ void k_link_b(const BTile* __restrict__ bt, int ntiles, unsigned long
   const unsigned long long g = list[i];
   const BTile& t = bt[btile_of(bt, ntiles, g)];
   const uint32_t s = static_cast<uint32_t>(g - t.cbase);
-  const Node4* nodes = nodes_all + t.cbase;
+  const Node* nodes = rnode_all + t.nbase;
+  const uint2* leaves = rleaf_all + t.nbase;
+  const uint32_t* ridx = ridx_all + t.cbase;
   const float4* Ab = A + t.cbase;
   const float4* Db = D + t.cbase;
   const uint8_t* dev = developed + t.cbase;
@@ -320,8 +199,8 @@ __global__ void k_link_b(const BTile* __restrict__ bt, int ntiles, unsigned long
   const float fef = static_cast<float>(t.fe), proxf = static_cast<float>(t.prox);
   const float rcf = fmaxf(fmaxf(d.x, d.y), d.z) * fef;
   if (t.n < 2) return;
-  const int nint = static_cast<int>(t.n) - 1;
-  auto leaf = [&](uint32_t j) {
+  const uint32_t nmax = t.ncap;
+  auto test = [&](uint32_t j) {
     if (j <= s || j >= t.n || !dev[j]) return;
     const float4 aj = Ab[j], dj = Db[j];
     const float dx = aj.x - a.x, dy = aj.y - a.y, dz = aj.z - a.z;
@@ -344,35 +223,42 @@ __global__ void k_link_b(const BTile* __restrict__ bt, int ntiles, unsigned long
     }
     if (hit) uf_unite_b(parent, static_cast<int>(g), static_cast<int>(t.cbase + j), err);
   };
-  int stack[64];
+  auto leaf = [&](uint32_t id) {
+    if (!index_ok(id < nmax, err, SITE_LEAF, id, nmax)) return;
+    const uint2 L = leaves[id];
+    if (!index_ok(L.x + L.y <= t.n, err, SITE_LEAF, L.x, L.y)) return;
+    for (uint32_t k = 0; k < L.y; ++k) test(ridx[L.x + k]);
+  };
+  int stack[RT_MAX_DEPTH + 1];
   int sp = 0, cur = 0;
   for (;;) {
-    if (!index_ok(cur >= 0 && cur < nint, err, SITE_NODE, static_cast<uint32_t>(cur), t.n)) break;
-    const Node4* nd = nodes + cur;
-    const float4 lx = __ldg(&nd->lox), ly = __ldg(&nd->loy), lz = __ldg(&nd->loz);
-    const float4 hx = __ldg(&nd->hix), hy = __ldg(&nd->hiy), hz = __ldg(&nd->hiz);
-    const int4 rf = __ldg(&nd->ref), ls = __ldg(&nd->last);
-    int next = -1;
-    // Only pairs (s, j > s) are tested, so a child whose crystals all lie at or below s is skipped.
-    auto child = [&](float a0, float a1, float a2, float a3, float a4, float a5, int r, int last) {
-      if (r == INT32_MIN || last <= static_cast<int>(s)) return;
-      if (!(a0 <= hi.x && a3 >= lo.x && a1 <= hi.y && a4 >= lo.y && a2 <= hi.z && a5 >= lo.z)) return;
-      if (r < 0) {
-        leaf(static_cast<uint32_t>(~r));
-      } else if (next < 0) {
-        next = r;
-      } else if (sp < 64) {
-        stack[sp++] = r;
+    if (!index_ok(static_cast<uint32_t>(cur) < nmax, err, SITE_NODE, static_cast<uint32_t>(cur), nmax)) break;
+    const Node* nd = nodes + cur;
+    const float4 na = __ldg(&nd->a), nb = __ldg(&nd->b), nc = __ldg(&nd->c);
+    const int4 rf = __ldg(&nd->d);
+    bool hl = rf.x != INT32_MIN && na.x <= hi.x && na.w >= lo.x && na.y <= hi.y && nb.x >= lo.y && na.z <= hi.z &&
+              nb.y >= lo.z;
+    bool hr = rf.y != INT32_MIN && nb.z <= hi.x && nc.y >= lo.x && nb.w <= hi.y && nc.z >= lo.y && nc.x <= hi.z &&
+              nc.w >= lo.z;
+    if (hl && rf.x < 0) {
+      leaf(static_cast<uint32_t>(~rf.x));
+      hl = false;
+    }
+    if (hr && rf.y < 0) {
+      leaf(static_cast<uint32_t>(~rf.y));
+      hr = false;
+    }
+    if (hl && hr) {
+      if (sp <= RT_MAX_DEPTH) {
+        stack[sp++] = rf.y;
       } else {
         atomicOr(err, ERR_STACK_OVERFLOW);
       }
-    };
-    child(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, rf.x, ls.x);
-    child(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, rf.y, ls.y);
-    child(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, rf.z, ls.z);
-    child(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, rf.w, ls.w);
-    if (next >= 0) {
-      cur = next;
+      cur = rf.x;
+    } else if (hl) {
+      cur = rf.x;
+    } else if (hr) {
+      cur = rf.y;
     } else {
       if (sp == 0) break;
       cur = stack[--sp];
@@ -416,24 +302,24 @@ __global__ void k_finalize_b(const BTile* __restrict__ bt, int ntiles, unsigned 
 
 // ---- scan bins (per tile grid of bin_px x bin_px pixels) ----
 
-__device__ __forceinline__ void bin_span(float c, float m, float binw, uint32_t nb, uint32_t& b0, uint32_t& b1) {
-  const float lo = (c - m - 1e-3f) / binw, hi = (c + m + 1e-3f) / binw;
+__device__ __forceinline__ void bin_span(float l, float h, float binw, uint32_t nb, uint32_t& b0, uint32_t& b1) {
+  const float lo = (l - 1e-3f) / binw, hi = (h + 1e-3f) / binw;
   b0 = static_cast<uint32_t>(fminf(fmaxf(floorf(lo), 0.0f), static_cast<float>(nb - 1)));
   b1 = static_cast<uint32_t>(fminf(fmaxf(floorf(hi), 0.0f), static_cast<float>(nb - 1)));
 }
 
-__global__ void k_bin_b(const BTile* __restrict__ bt, int ntiles, unsigned long long ncap, const float4* __restrict__ A,
-                        const float4* __restrict__ D, const uint8_t* __restrict__ developed,
-                        const double* __restrict__ exp64, uint32_t* cnt, const uint32_t* off, uint32_t* cursor,
+// A developed crystal goes to every bin its leaf box (in the scan's tree) overlaps.
+__global__ void k_bin_b(const BTile* __restrict__ bt, int ntiles, unsigned long long ncap,
+                        const uint8_t* __restrict__ developed, const double* __restrict__ box64,
+                        const uint32_t* __restrict__ leafof, uint32_t* cnt, const uint32_t* off, uint32_t* cursor,
                         uint32_t* items, unsigned long long item_cap, uint32_t* err) {
   const unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
   if (g >= ncap || !developed[g]) return;
   const BTile& t = bt[btile_of(bt, ntiles, g)];
-  const float4 a = A[g], d = D[g];
-  const float m = fmaxf(fmaxf(d.x, d.y), d.z) * static_cast<float>(exp64[g]) * 1.0001f;
+  const double* lb = box64 + 6ull * (t.nbase + leafof[g]);
   uint32_t x0, x1, y0, y1;
-  bin_span(a.x, m, t.binw_x, t.nbx, x0, x1);
-  bin_span(a.y, m, t.binw_y, t.nby, y0, y1);
+  bin_span(static_cast<float>(lb[0]), static_cast<float>(lb[3]), t.binw_x, t.nbx, x0, x1);
+  bin_span(static_cast<float>(lb[1]), static_cast<float>(lb[4]), t.binw_y, t.nby, y0, y1);
   const uint32_t s = static_cast<uint32_t>(g - t.cbase);
   for (uint32_t by = y0; by <= y1; ++by)
     for (uint32_t bx = x0; bx <= x1; ++bx) {
@@ -470,9 +356,9 @@ struct fg_batch {
   unsigned long long maxcells = 0, maxslots = 0;  // the largest tile's cells and bricks
   DBuf<float4> A, Q, D;
   DBuf<uint64_t> keys;
-  DBuf<Node> nodes;
-  DBuf<Node4> nodes4;
-  DBuf<int> leaf_parent, visit, parent;
+  RTreeBufs rt;             // the reference tree of every tile: over its crystals, then its developed ones
+  DBuf<RTile> rt_scan;      // the tree tiles of the scan's build (developed crystals, their expansion)
+  DBuf<int> parent;
   DBuf<uint32_t> counts, size;
   DBuf<uint8_t> developed;
   DBuf<double> exp64;
@@ -637,8 +523,10 @@ static void upload_descriptors(fg_batch* B, cudaStream_t st) {
     t.a = B->A.p + cb;
     t.q = B->Q.p + cb;
     t.d = B->D.p + cb;
-    t.nodes = B->nodes.p + cb;
-    t.nodes4 = B->nodes4.p + cb;
+    const unsigned long long nb = B->bt[i].nbase;
+    t.rnode = B->rt.rnode.p + nb;
+    t.rleaf = B->rt.rleaf.p + nb;
+    t.ridx = B->rt.ridx.p + cb;
     t.s2id = nullptr;
     t.counts = B->counts.p + cb;
     t.tile = B->exposure.p + B->exp_off[i];
@@ -651,6 +539,8 @@ static void upload_descriptors(fg_batch* B, cudaStream_t st) {
     c.pos64 = c.dims64 = c.quat64 = nullptr;
     c.developed = B->developed.p + cb;
     c.exp64 = B->exp64.p + cb;
+    c.lbox64 = B->rt.box64.p + 6 * nb;
+    c.leafof = B->rt.leafof.p + cb;
     c.sigma_c = nullptr;
     c.bin_off = B->bin_off.p + c.bin_base;
     c.bin_items = B->bin_items.p;
@@ -666,7 +556,7 @@ static void upload_descriptors(fg_batch* B, cudaStream_t st) {
   FG_CUDA(cudaMemcpyAsync(B->d_sc.p, B->sc.data(), B->ntiles * sizeof(ScanTile), cudaMemcpyHostToDevice, st));
   FG_CUDA(cudaMemcpyAsync(B->d_bt.p, B->bt.data(), B->ntiles * sizeof(BTile), cudaMemcpyHostToDevice, st));
   k_set_n<<<grid_for(B->ntiles, 128), 128, 0, st>>>(B->d_syn.p, static_cast<int>(B->ntiles), B->slot_scan.p, B->d_bt.p,
-                                                    B->d_td.p, B->d_sc.p, B->ncrys.p);
+                                                    B->d_td.p, B->d_sc.p, B->ncrys.p, B->rt.tiles.p);
   FG_CUDA(cudaGetLastError());
 }
 
@@ -693,20 +583,13 @@ static void stage_synth(fg_batch* B, cudaStream_t st, bool capturing = false) {
   launch_emit(B->d_syn.p, nt, B->maxslots, B->cells.p, B->slot_scan.p, B->A.p, B->Q.p, B->D.p, B->keys.p, e->d_err,
               st);
   k_set_n<<<grid_for(B->ntiles, 128), 128, 0, st>>>(B->d_syn.p, nt, B->slot_scan.p, B->d_bt.p, B->d_td.p, B->d_sc.p,
-                                                    B->ncrys.p);
+                                                    B->ncrys.p, B->rt.tiles.p);
   FG_CUDA(cudaGetLastError());
 }
 
-static void stage_bvh(fg_batch* B, cudaStream_t st) {
-  const int nt = static_cast<int>(B->ntiles);
-  FG_CUDA(cudaMemsetAsync(B->visit.p, 0, B->ncap * sizeof(int), st));
-  k_karras_b<<<grid_for(B->ncap, 256), 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->keys.p, B->nodes.p, B->leaf_parent.p,
-                                                     B->visit.p);
-  k_fit_b<<<grid_for(B->ncap, 256), 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->A.p, B->Q.p, B->D.p, B->nodes.p,
-                                                  B->leaf_parent.p, B->visit.p);
-  k_collapse4_b<<<grid_for(B->ncap, 256), 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->nodes.p, B->nodes4.p);
-  FG_CUDA(cudaGetLastError());
-}
+// The reference tree of every tile over its crystals (in slot order), for the transport and the
+// development's touch queries.
+static void stage_bvh(fg_batch* B, cudaStream_t st) { rtree_build(B->rt, B->e->d_err, st); }
 
 static void stage_transport(fg_batch* B, cudaStream_t st) {
   FG_CUDA(cudaMemsetAsync(B->counts.p, 0, B->ncap * sizeof(uint32_t), st));
@@ -734,8 +617,8 @@ static void stage_develop(fg_batch* B, cudaStream_t st) {
   FG_CUDA(cudaMemsetAsync(B->devflag.p + B->ncap, 0, sizeof(uint32_t), st));
   cub_scan(B, B->devflag.p, B->devscan.p, B->ncap + 1, st);
   k_devlist_b<<<G, 256, 0, st>>>(B->ncap, B->devflag.p, B->devscan.p, B->devlist.p);
-  k_link_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->A.p, B->D.p, B->nodes4.p, B->developed.p, B->parent.p,
-                              B->devlist.p, B->devscan.p + B->ncap, e->d_err);
+  k_link_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->A.p, B->D.p, B->rt.rnode.p, B->rt.rleaf.p, B->rt.ridx.p,
+                              B->developed.p, B->parent.p, B->devlist.p, B->devscan.p + B->ncap, e->d_err);
   FG_CUDA(cudaMemsetAsync(B->size.p, 0, B->ncap * sizeof(uint32_t), st));
   k_roots_b<<<G, 256, 0, st>>>(B->ncap, B->developed.p, B->parent.p, B->size.p, e->d_err);
   k_finalize_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->developed.p, B->parent.p, B->size.p, B->exp64.p,
@@ -747,13 +630,17 @@ static void stage_scan(fg_batch* B, cudaStream_t st) {
   const int nt = static_cast<int>(B->ntiles);
   fg_engine* e = B->e;
   const unsigned G = grid_for(B->ncap, 256);
+  // The scan's tree: the same buffers, rebuilt over each tile's developed crystals (the transport
+  // and the touch queries are done with the first tree by now).
+  k_scan_tree_tiles<<<grid_for(B->ntiles, 128), 128, 0, st>>>(B->d_bt.p, nt, B->devscan.p, B->devlist.p, B->rt_scan.p);
+  rtree_build(B->rt, e->d_err, st, B->rt_scan.p);
   launch_scan_prep(B->d_sc.p, nt, B->ncap, B->prep.p, st);
   FG_CUDA(cudaMemsetAsync(B->bin_cnt.p, 0, (B->nbins + 1) * sizeof(uint32_t), st));
   FG_CUDA(cudaMemsetAsync(B->bin_cur.p, 0, (B->nbins + 1) * sizeof(uint32_t), st));
-  k_bin_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->A.p, B->D.p, B->developed.p, B->exp64.p, B->bin_cnt.p, nullptr,
-                             nullptr, nullptr, 0, e->d_err);
+  k_bin_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->developed.p, B->rt.box64.p, B->rt.leafof.p, B->bin_cnt.p,
+                             nullptr, nullptr, nullptr, 0, e->d_err);
   cub_scan(B, B->bin_cnt.p, B->bin_off.p, B->nbins + 1, st);
-  k_bin_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->A.p, B->D.p, B->developed.p, B->exp64.p, nullptr,
+  k_bin_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->developed.p, B->rt.box64.p, B->rt.leafof.p, nullptr,
                              B->bin_off.p, B->bin_cur.p, B->bin_items.p, B->item_cap, e->d_err);
   FG_CUDA(cudaGetLastError());
   launch_scan(B->d_sc.p, nt, B->nbins, B->scan_threads, e->d_err, B->dstats.p, st);
@@ -792,6 +679,7 @@ static void autotune(fg_batch* B, cudaStream_t st) {
   enqueue_all(B, st);  // warm-up; leaves a developed emulsion for the scan trials
   FG_CUDA(cudaStreamSynchronize(st));
   check_error_word(e);
+  stage_bvh(B, st);  // the run ended with the scan's tree in the shared tree buffers
   float best = 1e30f;
   unsigned bb = B->tr_blocks, bt_ = B->tr_threads;
   for (unsigned threads : {128u, 256u}) {
@@ -914,15 +802,34 @@ static void plan(fg_batch* B, const fg_batch_options* opt) {
   B->Q.alloc(std::max<unsigned long long>(cap, 1), st);
   B->D.alloc(std::max<unsigned long long>(cap, 1), st);
   B->keys.alloc(std::max<unsigned long long>(cap, 1), st);
-  B->nodes.alloc(std::max<unsigned long long>(cap, 1), st);
-  B->nodes4.alloc(std::max<unsigned long long>(cap, 1), st);
-  B->leaf_parent.alloc(std::max<unsigned long long>(cap, 1), st);
-  B->visit.alloc(std::max<unsigned long long>(cap, 1), st);
   B->parent.alloc(std::max<unsigned long long>(cap, 1), st);
   B->counts.alloc(std::max<unsigned long long>(cap, 1), st);
   B->size.alloc(std::max<unsigned long long>(cap, 1), st);
   B->developed.alloc(std::max<unsigned long long>(cap, 1), st);
   B->exp64.alloc(std::max<unsigned long long>(cap, 1), st);
+  {
+    // Tree tiles: elements in the crystal-slot space (ebase = cbase), about 0.67 nodes per crystal.
+    std::vector<RTile> rt(n), rs(n);
+    for (uint32_t i = 0; i < n; ++i) {
+      RTile& t = rt[i];
+      t = RTile{};
+      t.a = B->A.p + B->syn[i].cbase;
+      t.d = B->D.p + B->syn[i].cbase;
+      t.ecap = B->syn[i].ccap;
+      t.pad = B->bt[i].pad;
+    }
+    rtree_alloc(B->rt, rt, true, st, RT_NODE_FRAC);
+    for (uint32_t i = 0; i < n; ++i) {
+      FG_REQUIRE(rt[i].ebase == B->syn[i].cbase, "tree layout differs from the crystal slots");
+      B->bt[i].nbase = rt[i].nbase;
+      B->bt[i].ncap = rt[i].ncap;
+      B->td[i].nnodes = rt[i].ncap;
+      rs[i] = rt[i];
+      rs[i].exp64 = B->exp64.p + B->syn[i].cbase;
+    }
+    B->rt_scan.alloc(n, st);
+    FG_CUDA(cudaMemcpyAsync(B->rt_scan.p, rs.data(), n * sizeof(RTile), cudaMemcpyHostToDevice, st));
+  }
   B->prep.alloc(std::max<unsigned long long>(cap, 1), st);
   B->devflag.alloc(cap + 1, st);
   B->devscan.alloc(cap + 1, st);
@@ -983,9 +890,10 @@ unsigned long long tile_footprint(const fg_tile_params& p, unsigned long long* s
   uint32_t bits = 0;
   while ((1u << bits) < static_cast<uint32_t>(std::ceil(side))) ++bits;
   const unsigned long long px = static_cast<unsigned long long>(p.width_px) * p.height_px;
-  // Per crystal slot: records 48, key 8, nodes 64 + 128, links and flags 36, expansion 8, scan
-  // prep 128, bin entries 32 (plus slack); cells 4 B; bricks 8 B; photon order; images.
-  return static_cast<unsigned long long>(s.ccap) * 480ull + static_cast<unsigned long long>(s.gw) * s.gh * s.gd * 4ull +
+  // Per crystal slot: records 48, key 8, links and flags 36, expansion 8, scan prep 160, bin
+  // entries 32, tree elements 40 and 0.8 nodes of 276 B (plus slack); cells 4 B; bricks 8 B;
+  // photon order; images.
+  return static_cast<unsigned long long>(s.ccap) * 580ull + static_cast<unsigned long long>(s.gw) * s.gh * s.gd * 4ull +
          (8ull << (2 * s.slot_bits)) + static_cast<unsigned long long>(t.P) * 4ull +
          (1ull << (2 * bits)) * 12ull + px * 8ull + 4096ull;
 }
@@ -1065,6 +973,8 @@ fg_status fg_emulsion_synthesize(fg_engine* e, const fg_emulsion_cfg* cfg, uint6
     em->leaf_parent.alloc(std::max<uint32_t>(n, 1), st);
     alloc_state(em.get(), st);
     if (n) build_lbvh(em.get(), keys.p, em->nodes.p, em->leaf_parent.p, false, st);
+    DBuf<uint32_t> none;
+    build_emulsion_tree(e, em.get(), false, em->rt, none);
     FG_CUDA(cudaEventRecord(e->timer.ev[1], st));
     FG_CUDA(cudaStreamSynchronize(st));
     e->timings.synth_ms = elapsed(e->timer.ev[0], e->timer.ev[1]);
@@ -1237,9 +1147,10 @@ fg_status fg_batch_wait(fg_batch* b, fg_batch_stats* stats) {
     s.scan_bin_px = b->bin_px;
     s.graph = b->exec ? 1u : 0u;
     // Own kernels per run: Bridson (all colour classes in one launch; it also counts the points), thin +
-    // brick counts, emit, set_n, Karras + fit + four-wide collapse, photon order x2, transport, maxdim + threshold +
-    // developed list + link + roots + finalize, scan prep, two bin passes, scan (CUB scans not counted).
-    s.kernel_launches = 1 + 2 + 1 + 1 + 3 + 2 + 1 + 6 + 1 + 2 + 1;
+    // brick counts, emit, set_n, photon order x2, transport, maxdim + threshold + developed list + link +
+    // roots + finalize, scan-tree inputs, scan prep, two bin passes, scan, and the two tree builds (each
+    // level's launches included, also those that find no work; CUB scans not counted).
+    s.kernel_launches = 1 + 2 + 1 + 1 + 2 + 1 + 6 + 1 + 1 + 2 + 1 + 2 * rtree_kernel_launches(b->rt);
     b->stats = s;
     if (stats) *stats = s;
   });

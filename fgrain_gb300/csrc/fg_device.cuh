@@ -319,13 +319,10 @@ __device__ __forceinline__ void slab(float3 o, float3 inv, float lx, float ly, f
   tx = fminf(fminf(fmaxf(t1x, t2x), fmaxf(t1y, t2y)), fmaxf(t1z, t2z));
 }
 
-// FP32 canonical hit of a general ray (production transport): own box and geometry.
-__device__ __forceinline__ bool fcanonical_hit(float4 a, float4 q, float4 d, float e, float3 o,
-                                               float3 dir, float3 inv, float& t0, float& t1) {
-  const float m = fmaxf(fmaxf(d.x, d.y), d.z) * e;
-  float be, bx;
-  slab(o, inv, a.x - m, a.y - m, a.z - m, a.x + m, a.y + m, a.z + m, be, bx);
-  if (!(bx >= be && bx > 0.0f)) return false;
+// FP32 crystal geometry of a general ray (production transport), HalideCrystal::intersect_ray
+// (crystal.rs:140-217): the oriented cube's slabs or the ellipsoid's quadratic, nothing else.
+__device__ __forceinline__ bool fintersect(float4 a, float4 q, float4 d, float e, float3 o, float3 dir, float& t0,
+                                           float& t1) {
   const float3 lo = quat_inv_rotate(q, make_float3(o.x - a.x, o.y - a.y, o.z - a.z));
   const float3 ld = quat_inv_rotate(q, dir);
   const float dx = d.x * e, dy = d.y * e, dz = d.z * e;
@@ -358,6 +355,16 @@ __device__ __forceinline__ bool fcanonical_hit(float4 a, float4 q, float4 d, flo
     return true;
   }
   return false;
+}
+
+// FP32 canonical hit: the crystal's own max_dim box and its geometry.
+__device__ __forceinline__ bool fcanonical_hit(float4 a, float4 q, float4 d, float e, float3 o,
+                                               float3 dir, float3 inv, float& t0, float& t1) {
+  const float m = fmaxf(fmaxf(d.x, d.y), d.z) * e;
+  float be, bx;
+  slab(o, inv, a.x - m, a.y - m, a.z - m, a.x + m, a.y + m, a.z + m, be, bx);
+  if (!(bx >= be && bx > 0.0f)) return false;
+  return fintersect(a, q, d, e, o, dir, t0, t1);
 }
 
 // 2D Morton interleave of 16-bit coordinates.

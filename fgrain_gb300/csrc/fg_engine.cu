@@ -238,6 +238,9 @@ fg_status fg_emulsion_upload(fg_engine* e, const fg_emulsion_cfg* cfg, const fg_
       build_lbvh(em.get(), keys.p, em->nodes.p, em->leaf_parent.p, false, st);
       em->h_s2id.resize(n);
       FG_CUDA(cudaMemcpyAsync(em->h_s2id.data(), em->sorted_to_id.p, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+      FG_CUDA(cudaStreamSynchronize(st));
+      DBuf<uint32_t> none;
+      build_emulsion_tree(e, em.get(), false, em->rt, none);
     } else {
       alloc_state(em.get(), st);
     }

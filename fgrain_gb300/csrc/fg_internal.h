@@ -10,6 +10,7 @@
 
 #include "../../include/fgrain_cuda.h"
 #include "fg_device.cuh"
+#include "fg_rtree.cuh"
 
 namespace fg {
 
@@ -42,31 +43,41 @@ inline fg_status status_of(cudaError_t e) {
   }
 }
 
-// Device buffer owned by RAII; stream-ordered allocation on the engine stream.
+// Device buffer owned by RAII; stream-ordered allocation on the engine stream.  view() makes it a
+// non-owning window onto memory that someone else holds (nothing is freed then).
 template <class T>
 struct DBuf {
   T* p = nullptr;
   size_t n = 0;
   cudaStream_t s = nullptr;
+  bool own = true;
   DBuf() = default;
   DBuf(size_t count, cudaStream_t st) { alloc(count, st); }
   void alloc(size_t count, cudaStream_t st) {
     release();
     s = st;
     n = count;
+    own = true;
     if (count) FG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&p), count * sizeof(T), st));
   }
+  void view(T* ptr, size_t count) {
+    release();
+    p = ptr;
+    n = count;
+    own = false;
+  }
   void release() {
-    if (p) cudaFreeAsync(p, s);
+    if (p && own) cudaFreeAsync(p, s);
     p = nullptr;
     n = 0;
+    own = true;
   }
   ~DBuf() { release(); }
   DBuf(const DBuf&) = delete;
   DBuf& operator=(const DBuf&) = delete;
-  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n), s(o.s) { o.p = nullptr; o.n = 0; }
+  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n), s(o.s), own(o.own) { o.p = nullptr; o.n = 0; }
   DBuf& operator=(DBuf&& o) noexcept {
-    if (this != &o) { release(); p = o.p; n = o.n; s = o.s; o.p = nullptr; o.n = 0; }
+    if (this != &o) { release(); p = o.p; n = o.n; s = o.s; own = o.own; o.p = nullptr; o.n = 0; }
     return *this;
   }
 };
@@ -88,6 +99,27 @@ struct StageTimer {
   }
 };
 
+// fg_rtree.cu: device buffers of reference-tree builds over the tiles of a batch (or one
+// emulsion).  Element positions and nodes are laid out tile after tile (RTile::ebase, nbase).
+struct RTreeBufs {
+  int ntiles = 0;
+  int levels = 0;                 // global split levels before the per-warp finish
+  unsigned long long E = 0, N = 0, nblk = 0;
+  uint32_t count = 0;             // elements of a one-tile tree built on the host's request
+  DBuf<RTile> tiles;
+  DBuf<uint32_t> idx0, idx1, nof0, nof1, flag, bb, blk, P, Q;
+  DBuf<uint32_t> ridx;            // final element order (slots): a leaf's crystals in reference order
+  DBuf<unsigned long long> acc;   // per node: 6 ordered minima, 6 ordered maxima
+  DBuf<double> box64;             // per node: lo xyz, hi xyz (FP64, exact)
+  DBuf<uint32_t> nstart, ncount, nK, nS, ntile, ndepth;
+  DBuf<int> nsplit;               // split axis, -1 for a leaf
+  DBuf<double> nmid;
+  DBuf<int2> nchild;              // global ids of the children
+  DBuf<uint32_t> wl0, wl1, wq, wqpar, cnt;
+  DBuf<Node> rnode;               // walk records (tile-local refs)
+  DBuf<uint2> rleaf;              // leaf: first element (tile-local position), count
+  DBuf<uint32_t> leafof;          // optional: leaf id of each element slot
+};
 }  // namespace fg
 
 struct fg_engine {
@@ -112,9 +144,11 @@ struct fg_emulsion {
   // FP64 copies (uploaded sets only).
   fg::DBuf<double> pos64, dims64, quat64, sens64;
   fg::DBuf<uint32_t> sorted_to_id, id_to_sorted;
-  // LBVH over undeveloped geometry.
+  // LBVH over undeveloped geometry (the development's radius queries).
   fg::DBuf<fg::Node> nodes;
   fg::DBuf<int> leaf_parent;
+  // The reference tree over all crystals in id order (the transport walks).
+  fg::RTreeBufs rt;
   // Mutable per-crystal state (Morton order).
   fg::DBuf<uint32_t> counts;
   fg::DBuf<uint8_t> developed;
@@ -154,6 +188,32 @@ void morton_order(fg_emulsion* em, const double* pos_host, const double* pos_dev
 void gather_sorted(fg_emulsion* em, const uint32_t* order, const double* pos, const double* dims,
                    const double* quat, const double* sens, const int32_t* morph, int32_t morph_all,
                    cudaStream_t st);
+
+// Sets RTile::ebase / nbase / ncap from ecap, copies the tiles to the device and allocates.  The
+// caller fills the source pointers and ecap of each tile, and RTile::n (and order) on the device
+// before each build.
+// Each tile gets min(ecap + 2, node_frac * ecap + 64) nodes (the reference tree has about 0.67
+// nodes per element; running out fails the build with the list-overflow error bit).
+// leafof (when wanted) gets max(elements, leafof_slots) words: it is indexed by element slot.
+void rtree_alloc(RTreeBufs& B, std::vector<RTile>& tiles, bool want_leafof, cudaStream_t st, double node_frac = 1.0,
+                 size_t leafof_slots = 0);
+// Enqueues a build (capturable: no host synchronisation).  tiles_dev (optional) replaces the tile
+// array of the allocation by one with the same layout (ebase, nbase, ecap, ncap) but other element
+// sources, so that one set of buffers serves several trees in turn.
+void rtree_build(RTreeBufs& B, uint32_t* err, cudaStream_t st, RTile* tiles_dev = nullptr);
+unsigned rtree_kernel_launches(const RTreeBufs& B);
+// One tile's build in memory the caller holds (nothing allocated): bytes needed for a tile of ecap
+// elements, and the attach that carves every buffer (the tile descriptor too) from `base`
+// (256-byte aligned).  The tile's source pointers are set by the caller; tile.n may be written on
+// the device later (RTreeBufs::tiles.p).
+size_t rtree_scratch_bytes(uint32_t ecap, bool want_leafof, uint32_t leafof_slots);
+void rtree_attach(RTreeBufs& B, RTile tile, bool want_leafof, uint32_t leafof_slots, unsigned char* base,
+                  size_t bytes, cudaStream_t st);
+// The tree of an emulsion over all its crystals, or over its developed crystals with their
+// expansion (the scan's tree, transmittance.rs:86-89), elements in crystal-id order.  list keeps
+// the developed element list alive for the build.
+void build_emulsion_tree(fg_engine* e, const fg_emulsion* em, bool developed_only, RTreeBufs& B,
+                         DBuf<uint32_t>& list);
 
 // fg_develop.cu
 void develop(fg_engine* e, fg_emulsion* em, const fg_dev_cfg& cfg, fg_dev_report* rep);

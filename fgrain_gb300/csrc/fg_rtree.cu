@@ -1,0 +1,991 @@
+// Device builder of the reference tree (BVH::build / subdivide, bvh.rs:157-295); see fg_rtree.cuh.
+//
+// The tree is built top-down, one level at a time over all tiles of a batch:
+//   reduce  each pending node's box and centroid box (FP64 min / max as ordered 64-bit atomics,
+//           exact whatever the order);
+//   decide  leaf or split (largest centroid extent, midpoint 0.5 (lo + hi)), children ids;
+//   flag    every element of a splitting node: centroid >= mid ("big");
+//   scan    exclusive prefix sum of the flags (ranks of bigs inside each node's contiguous range);
+//   pq      P_m = position of the m-th big from the left, Q_m = of the m-th small from the right;
+//   K       the number of m with P_m < Q_m (bigs and smalls the swaps exchange);
+//   place   every element moves to where the reference's swap partition puts it (below).
+// Nodes of at most 32 elements are then finished by one warp each with the same arithmetic on
+// ballots.
+//
+// The swap partition (bvh.rs:244-258: i from the left, j from the right; a small at i stays and i
+// advances, a big at i is swapped with j and j retreats) examines the range as two streams: the
+// left stream runs while it sees smalls, the right stream while it sees bigs.  With P_m, Q_m and
+// K as above (Q_0 = n), the left stream covers [0, li) where li = P_{K+1} + 1 if a (K+1)-th big
+// exists before Q_K, else li = Q_K; and the element at relative position r goes to
+//   r < li, small:            r                      (stays)
+//   r < li, the m-th big:     Q_{m-1} - 1            (bigs fill the right end in examination order)
+//   r >= li, the m-th small from the right:  P_m     (takes the place of the m-th big)
+//   r >= li, big:             r - 1                  (shifts one place towards the middle)
+// The number of smalls is the left child's size; a simulation of the reference loop confirms the
+// rule on random ranges.
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <type_traits>
+
+#include "fg_internal.h"
+#include "fg_rtree.cuh"
+
+namespace fg {
+
+namespace {
+
+constexpr unsigned RT_BLOCK = 256;
+
+// Global split levels for trees of up to emax elements: halving down to the per-warp size, plus a
+// wide margin for uneven splits (unused levels cost only launches that find no work).
+int levels_for(uint32_t emax) {
+  int lv = 1;
+  while ((static_cast<unsigned long long>(RT_WARP_MAX) << lv) < std::max<unsigned long long>(emax, 1)) ++lv;
+  return std::min(lv + 12, 44);
+}
+
+constexpr unsigned SCAN_ITEMS = 2048;  // entries per block of the prefix sum (256 threads x 8)
+
+__device__ __forceinline__ unsigned long long ord64(double v) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+  return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double unord64(unsigned long long u) {
+  const unsigned long long b = (u & 0x8000000000000000ull) ? (u & 0x7fffffffffffffffull) : ~u;
+  return __longlong_as_double(static_cast<long long>(b));
+}
+
+__device__ __forceinline__ int rt_tile_of(const RTile* tiles, int ntiles, unsigned long long x) {
+  int lo = 0, hi = ntiles - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tiles[mid].ebase <= x) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Position of the k-th (0-based) set bit of m, counting from bit 0 (k < popc(m)).
+__device__ __forceinline__ int nth_bit(unsigned m, int k) {
+  int pos = 0;
+#pragma unroll
+  for (int w = 16; w >= 1; w >>= 1) {
+    const unsigned lo = m & ((1u << w) - 1u);
+    const int c = __popc(lo);
+    if (k >= c) {
+      k -= c;
+      m >>= w;
+      pos += w;
+    } else {
+      m = lo;
+    }
+  }
+  return pos;
+}
+
+struct RtArgs {
+  RTile* tiles;
+  int ntiles;
+  unsigned long long E, N;
+  uint32_t* idx[2];
+  uint32_t* nof[2];
+  uint32_t* flag;
+  uint32_t* bb;
+  uint32_t* blk;
+  uint32_t* P;
+  uint32_t* Q;
+  uint32_t* ridx;
+  unsigned long long* acc;
+  double* box64;
+  uint32_t *nstart, *ncount, *nK, *nS, *ntile, *ndepth;
+  int* nsplit;
+  double* nmid;
+  int2* nchild;
+  uint32_t* wl[2];
+  uint32_t* wq;     // warp queue: node ids
+  uint32_t* wqpar;  // and the buffer parity holding their elements
+  uint32_t* cnt;    // [0], [1] worklist counts, [2] warp queue count
+  uint32_t* err;
+};
+
+// Node allocation: two tile-local ids, or none when the tile's node capacity is spent.
+__device__ __forceinline__ bool alloc_pair(const RtArgs& A, int t, uint32_t& l) {
+  l = atomicAdd(&A.tiles[t].nodes, 2u);
+  if (l + 2 > A.tiles[t].ncap) {
+    atomicOr(A.err, ERR_LIST_OVERFLOW);
+    return false;
+  }
+  return true;
+}
+
+__global__ void k_rt_clear(RtArgs A) {
+  for (unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; i < A.N;
+       i += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) A.acc[12 * i + k] = ~0ull;        // minima
+#pragma unroll
+    for (int k = 6; k < 12; ++k) A.acc[12 * i + k] = 0ull;        // maxima
+    A.nsplit[i] = -1;
+    A.nK[i] = 0;
+  }
+}
+
+// Element order and roots.  Thread x < E fills position x; one thread per tile sets up its root.
+__global__ void k_rt_init(RtArgs A) {
+  const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+  const unsigned long long g0 = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+  for (unsigned long long x = g0; x < A.E; x += stride) {
+    const int t = rt_tile_of(A.tiles, A.ntiles, x);
+    const RTile& T = A.tiles[t];
+    const unsigned long long k = x - T.ebase;
+    uint32_t v = RT_DONE;
+    if (k < T.n) {
+      const uint32_t slot = T.order ? static_cast<uint32_t>(T.order[k] - T.obase) : static_cast<uint32_t>(k);
+      A.idx[0][x] = slot;
+      v = T.n > static_cast<uint32_t>(RT_WARP_MAX) ? static_cast<uint32_t>(T.nbase + 1) : RT_DONE;
+    }
+    A.nof[0][x] = v;
+  }
+  for (unsigned long long t = g0; t < static_cast<unsigned long long>(A.ntiles); t += stride) {
+    RTile& T = A.tiles[t];
+    T.nodes = 2;
+    T.depth = T.n ? 1 : 0;
+    const unsigned long long root = T.nbase + 1;
+    A.nstart[root] = static_cast<uint32_t>(T.ebase);
+    A.ncount[root] = T.n;
+    A.ntile[root] = static_cast<uint32_t>(t);
+    A.ndepth[root] = 1;
+    if (T.n > static_cast<uint32_t>(RT_WARP_MAX)) {
+      A.wl[0][atomicAdd(&A.cnt[0], 1u)] = static_cast<uint32_t>(root);
+    } else if (T.n > 0) {
+      const uint32_t q = atomicAdd(&A.cnt[2], 1u);
+      A.wq[q] = static_cast<uint32_t>(root);
+      A.wqpar[q] = 0;
+    }
+  }
+}
+
+// Box and centroid box of every pending node (12 ordered atomics per warp and node).
+__global__ void k_rt_reduce(RtArgs A, int c) {
+  if (A.cnt[c] == 0) return;
+  const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+  for (unsigned long long base = blockIdx.x * static_cast<unsigned long long>(blockDim.x); base < A.E; base += stride) {
+    const unsigned long long x = base + threadIdx.x;
+    uint32_t node = RT_DONE;
+    double v[12];
+    if (x < A.E) {
+      node = A.nof[c][x];
+      if (!(node & RT_DONE)) {
+        const RTile& T = A.tiles[A.ntile[node]];
+        // v[0..2] box lo, v[3..5] centroid (its minimum), v[6..8] box hi, v[9..11] centroid
+        // (its maximum): six minima, then six maxima.
+        rt_box(T, A.idx[c][x], v, v + 6, v + 3);
+        v[9] = v[3];
+        v[10] = v[4];
+        v[11] = v[5];
+      }
+    }
+    const bool act = !(node & RT_DONE);
+    const unsigned m = __ballot_sync(0xffffffffu, act);
+    if (!act) continue;
+    const unsigned grp = __match_any_sync(m, node);
+    const int leader = __ffs(grp) - 1;
+    // mins: v[0..2] box lo, v[3..5] centroid lo; maxima: v[6..8] box hi, v[9..11] centroid hi
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      double r = v[k];
+      for (unsigned q = grp; q; q &= q - 1) {
+        const double o = __shfl_sync(grp, v[k], __ffs(q) - 1);
+        r = k < 6 ? fmin(r, o) : fmax(r, o);
+      }
+      v[k] = r;
+    }
+    if (static_cast<int>(threadIdx.x & 31) == leader) {
+      unsigned long long* a = A.acc + 12ull * node;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) atomicMin(a + k, ord64(v[k]));
+#pragma unroll
+      for (int k = 6; k < 12; ++k) atomicMax(a + k, ord64(v[k]));
+    }
+  }
+}
+
+// Leaf or split for every pending node of this level (subdivide, bvh.rs:200-270).
+__global__ void k_rt_decide(RtArgs A, int c) {
+  const uint32_t nw = A.cnt[c];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nw; i += gridDim.x * blockDim.x) {
+    const uint32_t node = A.wl[c][i];
+    const int t = static_cast<int>(A.ntile[node]);
+    const unsigned long long* a = A.acc + 12ull * node;
+    double lo[3], hi[3], clo[3], chi[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = unord64(a[k]);
+      clo[k] = unord64(a[3 + k]);
+      hi[k] = unord64(a[6 + k]);
+      chi[k] = unord64(a[9 + k]);
+      A.box64[6ull * node + k] = lo[k];
+      A.box64[6ull * node + 3 + k] = hi[k];
+    }
+    const double ex = __dsub_rn(chi[0], clo[0]), ey = __dsub_rn(chi[1], clo[1]), ez = __dsub_rn(chi[2], clo[2]);
+    const int axis = (ex >= ey && ex >= ez) ? 0 : (ey >= ez ? 1 : 2);
+    const double ext = axis == 0 ? ex : (axis == 1 ? ey : ez);
+    uint32_t l = 0;
+    if (A.ncount[node] <= 4 || ext <= 1e-7 || !alloc_pair(A, t, l)) {
+      A.nsplit[node] = -1;  // leaf (degenerate centroids, or no node capacity left)
+      continue;
+    }
+    A.nsplit[node] = axis;
+    A.nmid[node] = __dmul_rn(0.5, __dadd_rn(clo[axis], chi[axis]));
+    const unsigned long long nb = A.tiles[t].nbase;
+    A.nchild[node] = make_int2(static_cast<int>(nb + l), static_cast<int>(nb + l + 1));
+  }
+}
+
+__device__ __forceinline__ double axis_centroid(const RTile& T, uint32_t s, int axis) {
+  double lo[3], hi[3], cc[3];
+  rt_box(T, s, lo, hi, cc);
+  return cc[axis];
+}
+
+__global__ void k_rt_flags(RtArgs A, int c) {
+  if (A.cnt[c] == 0) return;
+  const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+  for (unsigned long long x = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; x <= A.E;
+       x += stride) {
+    uint32_t f = 0;
+    if (x < A.E) {
+      const uint32_t node = A.nof[c][x];
+      if (!(node & RT_DONE)) {
+        const int axis = A.nsplit[node];
+        if (axis >= 0) f = (axis_centroid(A.tiles[A.ntile[node]], A.idx[c][x], axis) < A.nmid[node]) ? 0u : 1u;
+      }
+    }
+    A.flag[x] = f;
+  }
+}
+
+// Exclusive prefix sum of flag[0..E] into bb, in blocks of SCAN_ITEMS: block sums, one block
+// scanning the block sums, then each block's own scan.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* sh, uint32_t& total) {
+  const unsigned lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= static_cast<unsigned>(o)) incl += y;
+  }
+  if (lane == 31) sh[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    uint32_t s = lane < blockDim.x / 32 ? sh[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= static_cast<unsigned>(o)) s += y;
+    }
+    sh[lane] = s;
+  }
+  __syncthreads();
+  total = sh[blockDim.x / 32 - 1];
+  const uint32_t r = incl - v + (w ? sh[w - 1] : 0u);
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(RT_BLOCK) k_rt_scan_blocks(RtArgs A, int c, unsigned long long nb) {
+  if (A.cnt[c] == 0) return;
+  __shared__ uint32_t sh[32];
+  for (unsigned long long b = blockIdx.x; b < nb; b += gridDim.x) {
+    const unsigned long long x0 = b * SCAN_ITEMS + threadIdx.x * 8ull;
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if (x0 + k <= A.E) s += A.flag[x0 + k];
+    uint32_t tot;
+    block_excl_scan(s, sh, tot);
+    if (threadIdx.x == 0) A.blk[b] = tot;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_rt_scan_top(RtArgs A, int c, unsigned long long nb) {
+  if (A.cnt[c] == 0) return;
+  __shared__ uint32_t sh[32];
+  uint32_t carry = 0;
+  for (unsigned long long base = 0; base < nb; base += 1024) {
+    const unsigned long long i = base + threadIdx.x;
+    const uint32_t v = i < nb ? A.blk[i] : 0u;
+    uint32_t tot;
+    const uint32_t e = block_excl_scan(v, sh, tot);
+    if (i < nb) A.blk[i] = carry + e;
+    carry += tot;
+  }
+}
+
+__global__ void __launch_bounds__(RT_BLOCK) k_rt_scan_final(RtArgs A, int c, unsigned long long nb) {
+  if (A.cnt[c] == 0) return;
+  __shared__ uint32_t sh[32];
+  for (unsigned long long b = blockIdx.x; b < nb; b += gridDim.x) {
+    const unsigned long long x0 = b * SCAN_ITEMS + threadIdx.x * 8ull;
+    uint32_t f[8], s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      f[k] = x0 + k <= A.E ? A.flag[x0 + k] : 0u;
+      s += f[k];
+    }
+    uint32_t tot;
+    uint32_t acc = A.blk[b] + block_excl_scan(s, sh, tot);
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if (x0 + k <= A.E) {
+        A.bb[x0 + k] = acc;
+        acc += f[k];
+      }
+  }
+}
+
+// Ranks: P_m (m-th big from the left) and Q_m (m-th small from the right), relative positions.
+__global__ void k_rt_pq(RtArgs A, int c) {
+  if (A.cnt[c] == 0) return;
+  const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+  for (unsigned long long x = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; x < A.E;
+       x += stride) {
+    const uint32_t node = A.nof[c][x];
+    if ((node & RT_DONE) || A.nsplit[node] < 0) continue;
+    const uint32_t s = A.nstart[node], n = A.ncount[node];
+    const uint32_t r = static_cast<uint32_t>(x - s);
+    const uint32_t bs = A.bb[s];
+    const uint32_t Bb = A.bb[x] - bs, Bt = A.bb[s + n] - bs, St = n - Bt;
+    if (A.flag[x]) {
+      A.P[s + Bb] = r;  // m = Bb + 1
+    } else {
+      const uint32_t mr = St - (r - Bb);  // right rank, 1-based
+      A.Q[s + mr - 1] = r;
+    }
+    if (r == 0) A.nS[node] = St;
+  }
+}
+
+// K: the number of bigs m with P_m < Q_m (they form a prefix of the bigs).
+__global__ void k_rt_K(RtArgs A, int c) {
+  if (A.cnt[c] == 0) return;
+  const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+  for (unsigned long long base = blockIdx.x * static_cast<unsigned long long>(blockDim.x); base < A.E; base += stride) {
+    const unsigned long long x = base + threadIdx.x;
+    uint32_t node = RT_DONE;
+    bool pred = false;
+    if (x < A.E) {
+      node = A.nof[c][x];
+      if (!(node & RT_DONE) && A.nsplit[node] >= 0 && A.flag[x]) {
+        const uint32_t s = A.nstart[node], n = A.ncount[node];
+        const uint32_t r = static_cast<uint32_t>(x - s);
+        const uint32_t bs = A.bb[s];
+        const uint32_t m = A.bb[x] - bs + 1, St = n - (A.bb[s + n] - bs);
+        pred = m <= St && r < A.Q[s + m - 1];
+      }
+    }
+    const unsigned pm = __ballot_sync(0xffffffffu, pred);
+    if (!pred) continue;
+    const unsigned grp = __match_any_sync(pm, node);
+    if (static_cast<int>(threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&A.nK[node], static_cast<uint32_t>(__popc(grp)));
+  }
+}
+
+// Moves every element of a splitting node to its place after the reference's swap partition;
+// finishes the elements of new leaves; sets up the children.
+__global__ void k_rt_place(RtArgs A, int c) {
+  if (A.cnt[c] == 0) return;
+  const int o = c ^ 1;
+  const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+  for (unsigned long long x = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; x < A.E;
+       x += stride) {
+    const uint32_t node = A.nof[c][x];
+    if (node & RT_DONE) {
+      A.nof[o][x] = RT_DONE;
+      continue;
+    }
+    const uint32_t el = A.idx[c][x];
+    if (A.nsplit[node] < 0) {  // a leaf of this level: its order is final
+      A.ridx[x] = el;
+      A.nof[o][x] = RT_DONE;
+      continue;
+    }
+    const uint32_t s = A.nstart[node], n = A.ncount[node];
+    const uint32_t r = static_cast<uint32_t>(x - s);
+    const uint32_t bs = A.bb[s];
+    const uint32_t Bb = A.bb[x] - bs, Bt = A.bb[s + n] - bs, St = n - Bt;
+    const uint32_t K = A.nK[node];
+    const uint32_t QK = K >= 1 ? A.Q[s + K - 1] : n;
+    const bool hasP = K + 1 <= Bt;
+    const uint32_t PK1 = hasP ? A.P[s + K] : n;
+    const uint32_t li = (hasP && PK1 < QK) ? PK1 + 1 : QK;
+    const bool big = A.flag[x] != 0;
+    uint32_t dest;
+    if (r < li) {
+      dest = big ? ((Bb == 0 ? n : A.Q[s + Bb - 1]) - 1) : r;
+    } else {
+      dest = big ? r - 1 : A.P[s + (St - (r - Bb)) - 1];
+    }
+    // The reference splits at count / 2 when every centroid fell on one side (bvh.rs:260-265).
+    const uint32_t Sp = (St == 0 || St == n) ? n / 2 : St;
+    const int2 ch = A.nchild[node];
+    const bool left = dest < Sp;
+    const uint32_t child = static_cast<uint32_t>(left ? ch.x : ch.y);
+    const uint32_t csize = left ? Sp : n - Sp;
+    A.idx[o][s + dest] = el;
+    A.nof[o][s + dest] = csize > static_cast<uint32_t>(RT_WARP_MAX) ? child : RT_DONE;
+    if (r == 0) {
+      const uint32_t t = A.ntile[node], dep = A.ndepth[node] + 1;
+      const uint32_t cs[2] = {Sp, n - Sp};
+      const uint32_t cid[2] = {static_cast<uint32_t>(ch.x), static_cast<uint32_t>(ch.y)};
+      for (int k = 0; k < 2; ++k) {
+        const uint32_t id = cid[k];
+        A.nstart[id] = s + (k ? Sp : 0u);
+        A.ncount[id] = cs[k];
+        A.ntile[id] = t;
+        A.ndepth[id] = dep;
+        if (cs[k] > static_cast<uint32_t>(RT_WARP_MAX)) {
+          A.wl[o][atomicAdd(&A.cnt[o], 1u)] = id;
+        } else {
+          const uint32_t q = atomicAdd(&A.cnt[2], 1u);
+          A.wq[q] = id;
+          A.wqpar[q] = static_cast<uint32_t>(o);
+        }
+      }
+      atomicMax(&A.tiles[t].depth, dep);
+    }
+  }
+}
+
+__global__ void k_rt_level_end(RtArgs A, int c) {
+  // The worklist of this level has been consumed; the next level's count was filled by place.
+  A.cnt[c] = 0;
+}
+
+__global__ void k_rt_check(RtArgs A, int c) {
+  if (A.cnt[c] != 0) atomicOr(A.err, ERR_LIST_OVERFLOW);  // nodes left after the last level
+}
+
+// One warp finishes one node of at most 32 elements: the same splits, with the swap partition
+// evaluated on ballots, children processed from a per-warp stack.
+constexpr int RT_WARPS = 4;
+__global__ void __launch_bounds__(32 * RT_WARPS) k_rt_warp(RtArgs A) {
+  __shared__ int stk[RT_WARPS][32][4];
+  __shared__ int src[RT_WARPS][32];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t nq = A.cnt[2];
+  for (uint32_t q = blockIdx.x * RT_WARPS + w; q < nq; q += gridDim.x * RT_WARPS) {
+    const uint32_t root = A.wq[q], par = A.wqpar[q];
+    const uint32_t s = A.nstart[root], n = A.ncount[root];
+    const uint32_t t = A.ntile[root];
+    const RTile& T = A.tiles[t];
+    uint32_t el = 0;
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0}, cc[3] = {0, 0, 0};
+    if (static_cast<uint32_t>(lane) < n) {
+      el = A.idx[par][s + lane];
+      rt_box(T, el, lo, hi, cc);
+    }
+    int sp = 0;
+    if (lane == 0) {
+      stk[w][0][0] = 0;
+      stk[w][0][1] = static_cast<int>(n);
+      stk[w][0][2] = static_cast<int>(root);
+      stk[w][0][3] = static_cast<int>(A.ndepth[root]);
+    }
+    sp = 1;
+    __syncwarp();
+    uint32_t maxdep = 0;
+    while (sp > 0) {
+      --sp;
+      const int off = stk[w][sp][0], cnt = stk[w][sp][1], id = stk[w][sp][2], dep = stk[w][sp][3];
+      __syncwarp();
+      maxdep = max(maxdep, static_cast<uint32_t>(dep));
+      const bool in = lane >= off && lane < off + cnt;
+      double v[12];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        v[k] = in ? lo[k] : INFINITY;
+        v[3 + k] = in ? cc[k] : INFINITY;
+        v[6 + k] = in ? hi[k] : -INFINITY;
+        v[9 + k] = in ? cc[k] : -INFINITY;
+      }
+#pragma unroll
+      for (int k = 0; k < 12; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const double y = __shfl_xor_sync(0xffffffffu, v[k], o);
+          v[k] = k < 6 ? fmin(v[k], y) : fmax(v[k], y);
+        }
+      if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          A.box64[6ull * id + k] = v[k];
+          A.box64[6ull * id + 3 + k] = v[6 + k];
+        }
+        A.nstart[id] = s + static_cast<uint32_t>(off);
+        A.ncount[id] = static_cast<uint32_t>(cnt);
+      }
+      const double ex = __dsub_rn(v[9], v[3]), ey = __dsub_rn(v[10], v[4]), ez = __dsub_rn(v[11], v[5]);
+      const int axis = (ex >= ey && ex >= ez) ? 0 : (ey >= ez ? 1 : 2);
+      const double ext = axis == 0 ? ex : (axis == 1 ? ey : ez);
+      uint32_t l = 0;
+      bool split = cnt > 4 && ext > 1e-7;
+      if (split) {
+        if (lane == 0) split = alloc_pair(A, static_cast<int>(t), l);
+        split = __shfl_sync(0xffffffffu, split ? 1 : 0, 0) != 0;
+        l = __shfl_sync(0xffffffffu, l, 0);
+      }
+      if (!split) {
+        if (lane == 0) A.nsplit[id] = -1;
+        continue;
+      }
+      const double mid = __dmul_rn(0.5, __dadd_rn(axis == 0 ? v[3] : (axis == 1 ? v[4] : v[5]),
+                                                  axis == 0 ? v[9] : (axis == 1 ? v[10] : v[11])));
+      const double ca = axis == 0 ? cc[0] : (axis == 1 ? cc[1] : cc[2]);
+      const bool big = in && !(ca < mid);
+      const unsigned rng = (cnt == 32 ? 0xffffffffu : ((1u << cnt) - 1u)) << off;
+      const unsigned bm = __ballot_sync(0xffffffffu, big) & rng;
+      const unsigned sm_ = rng & ~bm;
+      const int Bt = __popc(bm), St = cnt - Bt;
+      const int r = lane - off;
+      const int Bb = __popc(bm & ((1u << lane) - 1u));
+      // P_m = nth_bit(bm, m - 1) - off; Q_m = nth_bit(sm_, St - m) - off.
+      bool pred = false;
+      if (big) {
+        const int m = Bb + 1;
+        pred = m <= St && r < nth_bit(sm_, St - m) - off;
+      }
+      const int K = __popc(__ballot_sync(0xffffffffu, pred));
+      const int QK = K >= 1 ? nth_bit(sm_, St - K) - off : cnt;
+      const bool hasP = K + 1 <= Bt;
+      const int PK1 = hasP ? nth_bit(bm, K) - off : cnt;
+      const int li = (hasP && PK1 < QK) ? PK1 + 1 : QK;
+      int dest = r;
+      if (in) {
+        if (r < li) {
+          dest = big ? ((Bb == 0 ? cnt : nth_bit(sm_, St - Bb) - off) - 1) : r;
+        } else {
+          dest = big ? r - 1 : nth_bit(bm, St - (r - Bb) - 1) - off;
+        }
+        src[w][off + dest] = lane;
+      }
+      __syncwarp();
+      const int from = in ? src[w][lane] : lane;
+      __syncwarp();
+      el = __shfl_sync(0xffffffffu, el, from);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        lo[k] = __shfl_sync(0xffffffffu, lo[k], from);
+        hi[k] = __shfl_sync(0xffffffffu, hi[k], from);
+        cc[k] = __shfl_sync(0xffffffffu, cc[k], from);
+      }
+      const unsigned long long nb = T.nbase;
+      const int Sp = (St == 0 || St == cnt) ? cnt / 2 : St;  // bvh.rs:260-265
+      if (lane == 0) {
+        A.nsplit[id] = axis;
+        A.nmid[id] = mid;
+        A.nchild[id] = make_int2(static_cast<int>(nb + l), static_cast<int>(nb + l + 1));
+        A.ndepth[nb + l] = static_cast<uint32_t>(dep + 1);
+        A.ndepth[nb + l + 1] = static_cast<uint32_t>(dep + 1);
+        stk[w][sp][0] = off;
+        stk[w][sp][1] = Sp;
+        stk[w][sp][2] = static_cast<int>(nb + l);
+        stk[w][sp][3] = dep + 1;
+        stk[w][sp + 1][0] = off + Sp;
+        stk[w][sp + 1][1] = cnt - Sp;
+        stk[w][sp + 1][2] = static_cast<int>(nb + l + 1);
+        stk[w][sp + 1][3] = dep + 1;
+      }
+      sp += 2;
+      __syncwarp();
+    }
+    if (static_cast<uint32_t>(lane) < n) A.ridx[s + lane] = el;
+    if (lane == 0) atomicMax(&A.tiles[t].depth, maxdep);
+  }
+}
+
+// Walk records: internal node k gets both child boxes in FP32 (an internal child's box rounded
+// outward and padded, a leaf child's box rounded to nearest), child refs (tile-local id, ~id for a
+// leaf); the super-root (id 0) holds the root as its right child.  leafof[slot] = leaf id.
+__global__ void k_rt_records(RtArgs A, Node* rnode, uint2* rleaf, uint32_t* leafof, unsigned long long leafof_n) {
+  const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+  for (unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; g < A.N;
+       g += stride) {
+    int lo_ = 0, hi_ = A.ntiles - 1;
+    while (lo_ < hi_) {
+      const int mid = (lo_ + hi_ + 1) >> 1;
+      if (A.tiles[mid].nbase <= g) lo_ = mid; else hi_ = mid - 1;
+    }
+    const RTile& T = A.tiles[lo_];
+    const uint32_t id = static_cast<uint32_t>(g - T.nbase);
+    // (After a failed node allocation, ids below the capacity may never have been set up; the
+    // build has flagged the error, and the checks below keep this pass inside its buffers.)
+    if (id >= min(T.nodes, T.ncap) || (id == 1 && T.n == 0)) continue;
+    auto child_box = [&](unsigned long long c, bool leaf, float* f) {
+      const double* b = A.box64 + 6ull * c;
+      if (leaf) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) f[k] = __double2float_rn(b[k]);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          f[k] = __double2float_rd(b[k]) - T.pad;
+          f[3 + k] = __double2float_ru(b[3 + k]) + T.pad;
+        }
+      }
+    };
+    auto ref_of = [&](unsigned long long c, bool& leaf) {
+      leaf = A.nsplit[c] < 0;
+      const int local = static_cast<int>(c - T.nbase);
+      return leaf ? ~local : local;
+    };
+    Node nd;
+    float l[6] = {0, 0, 0, 0, 0, 0}, r[6] = {0, 0, 0, 0, 0, 0};
+    int lref = INT32_MIN, rref = INT32_MIN;
+    if (id == 0) {
+      if (T.n > 0) {
+        bool leaf;
+        rref = ref_of(T.nbase + 1, leaf);
+        child_box(T.nbase + 1, leaf, r);
+      }
+    } else if (A.nsplit[g] >= 0) {
+      const int2 ch = A.nchild[g];
+      if (static_cast<unsigned long long>(ch.x) < T.nbase || static_cast<unsigned long long>(ch.y) >= T.nbase + T.ncap ||
+          static_cast<unsigned long long>(ch.y) < T.nbase || static_cast<unsigned long long>(ch.x) >= T.nbase + T.ncap) {
+        atomicOr(A.err, ERR_BAD_INDEX);
+        continue;
+      }
+      bool ll, rl;
+      lref = ref_of(static_cast<unsigned long long>(ch.x), ll);
+      rref = ref_of(static_cast<unsigned long long>(ch.y), rl);
+      child_box(static_cast<unsigned long long>(ch.x), ll, l);
+      child_box(static_cast<unsigned long long>(ch.y), rl, r);
+    } else {
+      const uint32_t st = A.nstart[g], cn = A.ncount[g];
+      if (st < T.ebase || st - T.ebase + static_cast<unsigned long long>(cn) > T.n) {
+        atomicOr(A.err, ERR_BAD_INDEX);
+        continue;
+      }
+      rleaf[g] = make_uint2(static_cast<uint32_t>(st - T.ebase), cn);
+      if (leafof)
+        for (uint32_t k = 0; k < cn; ++k) {
+          const uint32_t slot = A.ridx[st + k];
+          if (T.ebase + slot < leafof_n) leafof[T.ebase + slot] = id; else atomicOr(A.err, ERR_BAD_INDEX);
+        }
+    }
+    nd.a = make_float4(l[0], l[1], l[2], l[3]);
+    nd.b = make_float4(l[4], l[5], r[0], r[1]);
+    nd.c = make_float4(r[2], r[3], r[4], r[5]);
+    nd.d = make_int4(lref, rref, 0, 0);
+    rnode[g] = nd;
+  }
+}
+
+__global__ void k_rt_depth_check(RtArgs A) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < A.ntiles && A.tiles[t].depth > static_cast<uint32_t>(RT_MAX_DEPTH)) atomicOr(A.err, ERR_STACK_OVERFLOW);
+}
+
+}  // namespace
+
+RtArgs rt_args(RTreeBufs& B, uint32_t* err) {
+  RtArgs A;
+  A.tiles = B.tiles.p;
+  A.ntiles = B.ntiles;
+  A.E = B.E;
+  A.N = B.N;
+  A.idx[0] = B.idx0.p;
+  A.idx[1] = B.idx1.p;
+  A.nof[0] = B.nof0.p;
+  A.nof[1] = B.nof1.p;
+  A.flag = B.flag.p;
+  A.bb = B.bb.p;
+  A.blk = B.blk.p;
+  A.P = B.P.p;
+  A.Q = B.Q.p;
+  A.ridx = B.ridx.p;
+  A.acc = B.acc.p;
+  A.box64 = B.box64.p;
+  A.nstart = B.nstart.p;
+  A.ncount = B.ncount.p;
+  A.nK = B.nK.p;
+  A.nS = B.nS.p;
+  A.ntile = B.ntile.p;
+  A.ndepth = B.ndepth.p;
+  A.nsplit = B.nsplit.p;
+  A.nmid = B.nmid.p;
+  A.nchild = B.nchild.p;
+  A.wl[0] = B.wl0.p;
+  A.wl[1] = B.wl1.p;
+  A.wq = B.wq.p;
+  A.wqpar = B.wqpar.p;
+  A.cnt = B.cnt.p;
+  A.err = err;
+  return A;
+}
+
+void rtree_alloc(RTreeBufs& B, std::vector<RTile>& tiles, bool want_leafof, cudaStream_t st, double node_frac,
+                 size_t leafof_slots) {
+  B.ntiles = static_cast<int>(tiles.size());
+  unsigned long long e = 0, nn = 0;
+  uint32_t emax = 0;
+  for (auto& t : tiles) {
+    t.ebase = e;
+    t.ncap = static_cast<uint32_t>(std::min<double>(t.ecap + 2.0, std::ceil(t.ecap * node_frac) + 64.0));
+    t.nbase = nn;
+    e += t.ecap;
+    nn += t.ncap;
+    emax = std::max(emax, t.ecap);
+  }
+  FG_REQUIRE(e < 0x7fffffffull && nn < 0x7fffffffull, "too many elements for one reference-tree build");
+  B.E = e;
+  B.N = nn;
+  B.levels = levels_for(emax);
+  const size_t E1 = static_cast<size_t>(std::max<unsigned long long>(e, 1));
+  const size_t N1 = static_cast<size_t>(std::max<unsigned long long>(nn, 1));
+  B.tiles.alloc(tiles.size(), st);
+  FG_CUDA(cudaMemcpyAsync(B.tiles.p, tiles.data(), tiles.size() * sizeof(RTile), cudaMemcpyHostToDevice, st));
+  B.idx0.alloc(E1, st);
+  B.idx1.alloc(E1, st);
+  B.nof0.alloc(E1, st);
+  B.nof1.alloc(E1, st);
+  B.flag.alloc(E1 + 1, st);
+  B.bb.alloc(E1 + 1, st);
+  B.nblk = (E1 + 1 + SCAN_ITEMS - 1) / SCAN_ITEMS;
+  B.blk.alloc(B.nblk, st);
+  B.P.alloc(E1, st);
+  B.Q.alloc(E1, st);
+  B.ridx.alloc(E1, st);
+  B.acc.alloc(12 * N1, st);
+  B.box64.alloc(6 * N1, st);
+  B.nstart.alloc(N1, st);
+  B.ncount.alloc(N1, st);
+  B.nK.alloc(N1, st);
+  B.nS.alloc(N1, st);
+  B.ntile.alloc(N1, st);
+  B.ndepth.alloc(N1, st);
+  B.nsplit.alloc(N1, st);
+  B.nmid.alloc(N1, st);
+  B.nchild.alloc(N1, st);
+  B.wl0.alloc(N1, st);
+  B.wl1.alloc(N1, st);
+  B.wq.alloc(N1, st);
+  B.wqpar.alloc(N1, st);
+  B.cnt.alloc(4, st);
+  B.rnode.alloc(N1, st);
+  B.rleaf.alloc(N1, st);
+  if (want_leafof) B.leafof.alloc(std::max(E1, leafof_slots), st);
+  FG_CUDA(cudaMemsetAsync(B.ridx.p, 0, E1 * sizeof(uint32_t), st));
+}
+
+namespace {
+
+// Carves the buffers of a one-tile tree from `base` (or only counts the bytes when base is null).
+size_t carve(RTreeBufs* B, uint32_t ecap, bool want_leafof, uint32_t leafof_slots, unsigned char* base) {
+  const size_t E1 = std::max<uint32_t>(ecap, 1);
+  const size_t N1 = rt_attach_nodes(E1);
+  const size_t nblk = rt_attach_blocks(E1);
+  static_assert(SCAN_ITEMS == 2048, "rt_attach_blocks assumes 2048 entries per prefix-sum block");
+  size_t off = 0;
+  auto take = [&](auto& buf, size_t count) {
+    using T = typename std::remove_reference<decltype(*buf.p)>::type;
+    off = (off + 255) / 256 * 256;
+    if (base) buf.view(reinterpret_cast<T*>(base + off), count);
+    off += count * sizeof(T);
+  };
+  RTreeBufs dummy;
+  RTreeBufs& b = B ? *B : dummy;
+  take(b.tiles, 1);
+  take(b.idx0, E1);
+  take(b.idx1, E1);
+  take(b.nof0, E1);
+  take(b.nof1, E1);
+  take(b.flag, E1 + 1);
+  take(b.bb, E1 + 1);
+  take(b.blk, nblk);
+  take(b.P, E1);
+  take(b.Q, E1);
+  take(b.ridx, E1);
+  take(b.acc, 12 * N1);
+  take(b.box64, 6 * N1);
+  take(b.nstart, N1);
+  take(b.ncount, N1);
+  take(b.nK, N1);
+  take(b.nS, N1);
+  take(b.ntile, N1);
+  take(b.ndepth, N1);
+  take(b.nsplit, N1);
+  take(b.nmid, N1);
+  take(b.nchild, N1);
+  take(b.wl0, N1);
+  take(b.wl1, N1);
+  take(b.wq, N1);
+  take(b.wqpar, N1);
+  take(b.cnt, 4);
+  take(b.rnode, N1);
+  take(b.rleaf, N1);
+  if (want_leafof) take(b.leafof, std::max<uint32_t>(leafof_slots, 1));
+  if (B) {
+    B->ntiles = 1;
+    B->E = E1;
+    B->N = N1;
+    B->nblk = nblk;
+    B->levels = levels_for(ecap);
+  }
+  return (off + 255) / 256 * 256;
+}
+
+}  // namespace
+
+size_t rtree_scratch_bytes(uint32_t ecap, bool want_leafof, uint32_t leafof_slots) {
+  return carve(nullptr, ecap, want_leafof, leafof_slots, nullptr);
+}
+
+void rtree_attach(RTreeBufs& B, RTile tile, bool want_leafof, uint32_t leafof_slots, unsigned char* base,
+                  size_t bytes, cudaStream_t st) {
+  const size_t need = carve(nullptr, tile.ecap, want_leafof, leafof_slots, nullptr);
+  FG_REQUIRE(need == rtree_attach_bytes(tile.ecap, want_leafof, leafof_slots), "tree scratch layout mismatch");
+  FG_REQUIRE(need <= bytes, "tree scratch too small");
+  carve(&B, tile.ecap, want_leafof, leafof_slots, base);
+  tile.ebase = 0;
+  tile.nbase = 0;
+  tile.ncap = static_cast<uint32_t>(B.N);
+  FG_CUDA(cudaMemcpyAsync(B.tiles.p, &tile, sizeof(RTile), cudaMemcpyHostToDevice, st));
+}
+
+void rtree_build(RTreeBufs& B, uint32_t* err, cudaStream_t st, RTile* tiles_dev) {
+  if (B.ntiles == 0) return;
+  RtArgs A = rt_args(B, err);
+  if (tiles_dev) A.tiles = tiles_dev;
+  const unsigned G = static_cast<unsigned>(std::min<unsigned long long>((B.E + RT_BLOCK) / RT_BLOCK, 152ull * 16));
+  const unsigned GN = static_cast<unsigned>(std::min<unsigned long long>((B.N + RT_BLOCK - 1) / RT_BLOCK, 152ull * 16));
+  const unsigned GS = static_cast<unsigned>(std::min<unsigned long long>(B.nblk, 152ull * 16));
+  FG_CUDA(cudaMemsetAsync(B.cnt.p, 0, 4 * sizeof(uint32_t), st));
+  k_rt_clear<<<GN, RT_BLOCK, 0, st>>>(A);
+  k_rt_init<<<G, RT_BLOCK, 0, st>>>(A);
+  for (int L = 0; L < B.levels; ++L) {
+    const int c = L & 1;
+    k_rt_reduce<<<G, RT_BLOCK, 0, st>>>(A, c);
+    k_rt_decide<<<GN, RT_BLOCK, 0, st>>>(A, c);
+    k_rt_flags<<<G, RT_BLOCK, 0, st>>>(A, c);
+    k_rt_scan_blocks<<<GS, RT_BLOCK, 0, st>>>(A, c, B.nblk);
+    k_rt_scan_top<<<1, 1024, 0, st>>>(A, c, B.nblk);
+    k_rt_scan_final<<<GS, RT_BLOCK, 0, st>>>(A, c, B.nblk);
+    k_rt_pq<<<G, RT_BLOCK, 0, st>>>(A, c);
+    k_rt_K<<<G, RT_BLOCK, 0, st>>>(A, c);
+    k_rt_place<<<G, RT_BLOCK, 0, st>>>(A, c);
+    k_rt_level_end<<<1, 1, 0, st>>>(A, c);
+  }
+  k_rt_check<<<1, 1, 0, st>>>(A, B.levels & 1);
+  const unsigned GW = static_cast<unsigned>(std::min<unsigned long long>((B.N + RT_WARPS - 1) / RT_WARPS, 152ull * 32));
+  k_rt_warp<<<GW, 32 * RT_WARPS, 0, st>>>(A);
+  k_rt_records<<<GN, RT_BLOCK, 0, st>>>(A, B.rnode.p, B.rleaf.p, B.leafof.p, B.leafof.n);
+  k_rt_depth_check<<<grid_for(static_cast<size_t>(B.ntiles), 128), 128, 0, st>>>(A);
+  FG_CUDA(cudaGetLastError());
+}
+
+// Element lists of an emulsion in crystal-id order: all crystals (their slots), or the developed
+// ones (flag, exclusive sum, scatter).
+__global__ void k_rt_id_slots(const uint32_t* id2s, uint32_t n, const uint8_t* developed, uint32_t* flag) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const uint32_t s = id2s ? id2s[k] : k;
+  flag[k] = developed[s] ? 1u : 0u;
+}
+__global__ void k_rt_id_scatter(const uint32_t* id2s, uint32_t n, const uint32_t* flag, const uint32_t* pos,
+                                uint32_t* list) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n || !flag[k]) return;
+  list[pos[k]] = id2s ? id2s[k] : k;
+}
+
+void build_emulsion_tree(fg_engine* e, const fg_emulsion* em, bool developed_only, RTreeBufs& B,
+                         DBuf<uint32_t>& list) {
+  cudaStream_t st = e->stream;
+  const uint32_t n = em->n;
+  RTile t{};
+  t.a = em->a.p;
+  t.d = em->d.p;
+  t.pos64 = em->has64 ? em->pos64.p : nullptr;
+  t.dims64 = em->has64 ? em->dims64.p : nullptr;
+  t.exp64 = developed_only ? em->exp64.p : nullptr;
+  t.pad = static_cast<float>(std::max(em->extent, std::max(em->cfg.width, em->cfg.height)) * 2e-6 + 1e-5);
+  const uint32_t* id2s = em->h_s2id.empty() ? nullptr : em->id_to_sorted.p;
+  uint32_t m = n;
+  if (developed_only && n) {
+    DBuf<uint32_t> flag(n + 1, st), pos(n + 1, st);
+    FG_CUDA(cudaMemsetAsync(flag.p + n, 0, sizeof(uint32_t), st));
+    k_rt_id_slots<<<grid_for(n, 256), 256, 0, st>>>(id2s, n, em->developed.p, flag.p);
+    exclusive_scan_u32(flag.p, pos.p, n + 1, st);
+    FG_CUDA(cudaMemcpyAsync(&m, pos.p + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    FG_CUDA(cudaStreamSynchronize(st));
+    list.alloc(std::max<uint32_t>(m, 1), st);
+    k_rt_id_scatter<<<grid_for(n, 256), 256, 0, st>>>(id2s, n, flag.p, pos.p, list.p);
+    FG_CUDA(cudaGetLastError());
+    t.order = list.p;
+  } else {
+    t.order = id2s;
+  }
+  t.ecap = developed_only ? std::max<uint32_t>(m, 1) : std::max<uint32_t>(n, 1);
+  t.n = developed_only ? m : n;
+  std::vector<RTile> v{t};
+  rtree_alloc(B, v, developed_only, st, 1.0, n);
+  rtree_build(B, e->d_err, st);
+  B.count = t.n;
+}
+
+unsigned rtree_kernel_launches(const RTreeBufs& B) {
+  return B.ntiles ? 2u + 10u * static_cast<unsigned>(B.levels) + 4u : 0u;
+}
+
+}  // namespace fg
+
+extern "C" fg_status fg_emulsion_reference_tree(fg_engine* e, const fg_emulsion* em, int developed_only,
+                                                uint32_t* order, uint32_t* leaves, double* leaf_boxes, size_t cap,
+                                                size_t* nelem, size_t* nleaves) {
+  using namespace fg;
+  return guard(e, [&] {
+    FG_REQUIRE(em, "null emulsion");
+    cudaStream_t st = e->stream;
+    begin_call(e);
+    RTreeBufs local;
+    DBuf<uint32_t> list;
+    const RTreeBufs* T = &em->rt;
+    if (developed_only) {
+      build_emulsion_tree(e, em, true, local, list);
+      T = &local;
+    }
+    RTile tile{};
+    if (T->ntiles) FG_CUDA(cudaMemcpyAsync(&tile, T->tiles.p, sizeof(RTile), cudaMemcpyDeviceToHost, st));
+    FG_CUDA(cudaStreamSynchronize(st));
+    end_call(e);  // raises a build error first
+    const uint32_t n = T->ntiles ? tile.n : 0, nn = T->ntiles ? std::min(tile.nodes, tile.ncap) : 0;
+    std::vector<uint32_t> ridx(n), nstart(nn), ncount(nn);
+    std::vector<int> nsplit(nn);
+    std::vector<double> box(6ull * nn);
+    if (n) FG_CUDA(cudaMemcpyAsync(ridx.data(), T->ridx.p, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    if (nn) {
+      FG_CUDA(cudaMemcpyAsync(nstart.data(), T->nstart.p, nn * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+      FG_CUDA(cudaMemcpyAsync(ncount.data(), T->ncount.p, nn * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+      FG_CUDA(cudaMemcpyAsync(nsplit.data(), T->nsplit.p, nn * sizeof(int), cudaMemcpyDeviceToHost, st));
+      FG_CUDA(cudaMemcpyAsync(box.data(), T->box64.p, 6ull * nn * sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
+    FG_CUDA(cudaStreamSynchronize(st));
+    if (nelem) *nelem = n;
+    if (order)
+      for (uint32_t k = 0; k < n && k < cap; ++k) order[k] = em->h_s2id.empty() ? ridx[k] : em->h_s2id[ridx[k]];
+    std::vector<uint32_t> lf;
+    for (uint32_t id = 1; id < nn && n; ++id)
+      if (nsplit[id] < 0) lf.push_back(id);
+    std::sort(lf.begin(), lf.end(), [&](uint32_t a, uint32_t b) { return nstart[a] < nstart[b]; });
+    if (nleaves) *nleaves = lf.size();
+    for (size_t k = 0; k < lf.size() && k < cap; ++k) {
+      if (leaves) {
+        leaves[2 * k] = nstart[lf[k]];
+        leaves[2 * k + 1] = ncount[lf[k]];
+      }
+      if (leaf_boxes)
+        for (int j = 0; j < 6; ++j) leaf_boxes[6 * k + j] = box[6ull * lf[k] + j];
+    }
+  });
+}

@@ -1,0 +1,123 @@
+// The reference's crystal BVH rebuilt on the device ("reference tree"): the same tree that
+// BVH::build (bvh.rs:157-295) makes on the CPU, so that ray walks reach the same leaves and
+// report crystals in the same order as BVH::intersect_ray_all (bvh.rs:300-347).
+//
+// The reference tree is a top-down spatial-median tree over the crystals' max_dim boxes
+// (crystal.rs:106-133): a node of more than four crystals splits on the largest axis of its
+// centroid box at the box's midpoint, unless that extent is at most 1e-7 (then it is a leaf).
+// Which crystals a leaf holds, the boxes and the child order depend only on these sets; the order
+// of the crystals inside a leaf is the result of the reference's in-place swap partition applied
+// level after level, which the builder reproduces exactly (fg_rtree.cu).
+//
+// Why it matters: a leaf box is the union of its crystals' boxes, and the reference tests every
+// crystal of every leaf whose box a ray hits by its geometry alone.  A rotated cube's corner
+// sticks out of its own max_dim box by up to (sqrt(3) - 1) max_dim; the reference finds such a
+// hit whenever the corner lies inside the leaf box.  And the transport absorbs hits in traversal
+// order (right subtree first, leaf crystals in index order), which sets how the packet energy is
+// shared between the crystals along a segment.
+//
+// Walk records.  Node ids are tile-local; id 0 is a super-root whose only (right) child is the
+// real root (id 1), so every walk starts by testing the root's box as the reference does.
+#pragma once
+#include "fg_device.cuh"
+
+namespace fg {
+
+constexpr int RT_WARP_MAX = 32;    // nodes of at most this many crystals are finished by one warp
+constexpr int RT_MAX_DEPTH = 47;   // deeper trees are rejected (the walks keep 48-entry stacks)
+constexpr uint32_t RT_DONE = 0x80000000u;
+
+// Per-tree input and bookkeeping of one tile (or one emulsion).  Element slots are tile-relative.
+struct __align__(16) RTile {
+  const float4* a;         // crystal records: position (xyz)
+  const float4* d;         // half-dimensions (xyz)
+  const double* pos64;     // FP64 copies (3 per slot) or null: then the FP32 records are exact
+  const double* dims64;
+  const double* exp64;     // expansion per slot (developed geometry) or null (1.0)
+  const uint32_t* order;   // initial element order: order[k] - obase is element k's slot (null: k)
+  unsigned long long obase;
+  unsigned long long ebase;  // first element position of the tile
+  unsigned long long nbase;  // first node of the tile
+  uint32_t ecap, ncap;       // element and node capacity
+  uint32_t n;                // elements (device-written before the build)
+  uint32_t nodes;            // nodes made (written by the build)
+  uint32_t depth;            // deepest level (written by the build)
+  float pad;                 // outward padding of internal boxes in the FP32 walk records
+};
+static_assert(sizeof(RTile) == 96, "RTile layout");
+
+// Sizes of a one-tile build in caller-held memory (rtree_attach): nodes for ecap elements (at most
+// 0.8 per element plus 64; the reference tree needs about 0.67), prefix-sum blocks, and the bytes
+// of all buffers, each started on a 256-byte boundary (leafof: one word per crystal slot).
+constexpr size_t rt_attach_nodes(size_t e1) {
+  return e1 + 2 < (e1 * 4 + 4) / 5 + 64 ? e1 + 2 : (e1 * 4 + 4) / 5 + 64;
+}
+constexpr size_t rt_attach_blocks(size_t e1) { return (e1 + 1 + 2047) / 2048; }
+constexpr size_t rt_al(size_t v) { return (v + 255) / 256 * 256; }
+constexpr size_t rtree_attach_bytes(size_t ecap, bool want_leafof, size_t slots) {
+  const size_t e1 = ecap > 0 ? ecap : 1, n1 = rt_attach_nodes(e1);
+  return rt_al(96) + 4 * rt_al(4 * e1) + 2 * rt_al(4 * (e1 + 1)) + rt_al(4 * rt_attach_blocks(e1)) +
+         3 * rt_al(4 * e1) + rt_al(96 * n1) + rt_al(48 * n1) + 6 * rt_al(4 * n1) + rt_al(4 * n1) + rt_al(8 * n1) +
+         rt_al(8 * n1) + 4 * rt_al(4 * n1) + rt_al(16) + rt_al(64 * n1) + rt_al(8 * n1) +
+         (want_leafof ? rt_al(4 * (slots > 0 ? slots : 1)) : 0);
+}
+
+// Max_dim box of element slot s (crystal.rs:106-133) in FP64, and its centroid (bvh.rs:74-80).
+__device__ __forceinline__ void rt_box(const RTile& t, uint32_t s, double lo[3], double hi[3], double c[3]) {
+  double p[3], dm;
+  if (t.pos64) {
+    p[0] = t.pos64[3 * s];
+    p[1] = t.pos64[3 * s + 1];
+    p[2] = t.pos64[3 * s + 2];
+    dm = fmax(fmax(t.dims64[3 * s], t.dims64[3 * s + 1]), t.dims64[3 * s + 2]);
+  } else {
+    const float4 a = t.a[s], d = t.d[s];
+    p[0] = a.x;
+    p[1] = a.y;
+    p[2] = a.z;
+    dm = fmax(fmax(static_cast<double>(d.x), static_cast<double>(d.y)), static_cast<double>(d.z));
+  }
+  const double m = __dmul_rn(dm, t.exp64 ? t.exp64[s] : 1.0);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    lo[i] = __dsub_rn(p[i], m);
+    hi[i] = __dadd_rn(p[i], m);
+    c[i] = __dmul_rn(0.5, __dadd_rn(lo[i], hi[i]));
+  }
+}
+
+// AABB::intersect_ray (bvh.rs:96-124) in FP64 with Rust's NaN-ignoring min / max.
+__device__ __forceinline__ bool rt_box_hit64(const double* b, D3 o, D3 inv) {
+  const double t1x = __dmul_rn(__dsub_rn(b[0], o.x), inv.x), t2x = __dmul_rn(__dsub_rn(b[3], o.x), inv.x);
+  const double t1y = __dmul_rn(__dsub_rn(b[1], o.y), inv.y), t2y = __dmul_rn(__dsub_rn(b[4], o.y), inv.y);
+  const double t1z = __dmul_rn(__dsub_rn(b[2], o.z), inv.z), t2z = __dmul_rn(__dsub_rn(b[5], o.z), inv.z);
+  const double te = fmax(fmax(fmin(t1x, t2x), fmin(t1y, t2y)), fmin(t1z, t2z));
+  const double tx = fmin(fmin(fmax(t1x, t2x), fmax(t1y, t2y)), fmax(t1z, t2z));
+  return tx >= te && tx > 0.0;
+}
+
+// The reference walk, exactly (bvh.rs:300-347): pop a node, test its box on the whole ray in
+// FP64, call fn(leaf id) for a leaf, else push left then right when fewer than 62 entries are on
+// the stack (more are dropped, as the reference drops them).  nodes / box64 / nchild are the
+// tile's build arrays (global ids, nbase applied by the caller).
+template <class F>
+__device__ __forceinline__ void rt_walk64(const double* __restrict__ box64, const int2* __restrict__ nchild,
+                                          const int* __restrict__ nsplit, uint32_t root, D3 o, D3 inv, F&& fn) {
+  uint32_t stack[64];
+  int sp = 0;
+  stack[sp++] = root;
+  while (sp > 0) {
+    const uint32_t id = stack[--sp];
+    if (!rt_box_hit64(box64 + 6 * static_cast<size_t>(id), o, inv)) continue;
+    if (nsplit[id] < 0) {
+      fn(id);
+    } else if (sp + 2 < 64) {
+      const int2 ch = nchild[id];
+      stack[sp] = static_cast<uint32_t>(ch.x);
+      stack[sp + 1] = static_cast<uint32_t>(ch.y);
+      sp += 2;
+    }
+  }
+}
+
+}  // namespace fg

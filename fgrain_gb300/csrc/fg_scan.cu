@@ -4,29 +4,28 @@
 
 namespace fg {
 
-// Bin range of crystal s's own box (max_dim * expansion) in one axis.
-__device__ __forceinline__ void bin_range(float c, float m, float binw, uint32_t nb, uint32_t& b0,
-                                          uint32_t& b1) {
-  const float lo = (c - m - 1e-3f) / binw, hi = (c + m + 1e-3f) / binw;
-  const float fl = fminf(fmaxf(floorf(lo), 0.0f), (float)(nb - 1));
-  const float fh = fminf(fmaxf(floorf(hi), 0.0f), (float)(nb - 1));
+// Bin range [lo, hi] (um, padded by 1e-3) in one axis.
+__device__ __forceinline__ void bin_span(double lo, double hi, float binw, uint32_t nb, uint32_t& b0, uint32_t& b1) {
+  const float l = (static_cast<float>(lo) - 1e-3f) / binw, h = (static_cast<float>(hi) + 1e-3f) / binw;
+  const float fl = fminf(fmaxf(floorf(l), 0.0f), (float)(nb - 1));
+  const float fh = fminf(fmaxf(floorf(h), 0.0f), (float)(nb - 1));
   b0 = static_cast<uint32_t>(fl);
   b1 = static_cast<uint32_t>(fh);
 }
 
-__device__ __forceinline__ float own_half(const ScanTile& t, uint32_t s) {
-  const float4 d = t.d[s];
-  return fmaxf(fmaxf(d.x, d.y), d.z) * (float)t.exp64[s];
+// Bins of developed crystal s: those its leaf box overlaps (a ray outside the leaf box misses s).
+__device__ __forceinline__ void leaf_bins(const ScanTile& t, uint32_t s, uint32_t& x0, uint32_t& x1, uint32_t& y0,
+                                          uint32_t& y1) {
+  const double* b = t.lbox64 + 6ull * t.leafof[s];
+  bin_span(b[0], b[3], (float)(t.bin_px * t.pw), t.nbx, x0, x1);
+  bin_span(b[1], b[4], (float)(t.bin_px * t.ph), t.nby, y0, y1);
 }
 
 __global__ void k_bin_count(ScanTile t, uint32_t* cnt) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= t.n || !t.developed[s]) return;
-  const float4 a = t.a[s];
-  const float m = own_half(t, s) * 1.0001f;
   uint32_t x0, x1, y0, y1;
-  bin_range(a.x, m, (float)(t.bin_px * t.pw), t.nbx, x0, x1);
-  bin_range(a.y, m, (float)(t.bin_px * t.ph), t.nby, y0, y1);
+  leaf_bins(t, s, x0, x1, y0, y1);
   for (uint32_t by = y0; by <= y1; ++by)
     for (uint32_t bx = x0; bx <= x1; ++bx) atomicAdd(&cnt[by * t.nbx + bx], 1u);
 }
@@ -34,11 +33,8 @@ __global__ void k_bin_count(ScanTile t, uint32_t* cnt) {
 __global__ void k_bin_fill(ScanTile t, const uint32_t* off, uint32_t* cursor, uint32_t* items) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= t.n || !t.developed[s]) return;
-  const float4 a = t.a[s];
-  const float m = own_half(t, s) * 1.0001f;
   uint32_t x0, x1, y0, y1;
-  bin_range(a.x, m, (float)(t.bin_px * t.pw), t.nbx, x0, x1);
-  bin_range(a.y, m, (float)(t.bin_px * t.ph), t.nby, y0, y1);
+  leaf_bins(t, s, x0, x1, y0, y1);
   for (uint32_t by = y0; by <= y1; ++by)
     for (uint32_t bx = x0; bx <= x1; ++bx) {
       const uint32_t b = by * t.nbx + bx;
@@ -73,6 +69,8 @@ enum : int { K_CUBE = 0, K_CUBE_DF = 1, K_ELLIPSOID = 2, K_FP64 = 3 };
 // offsets are accurate to ~1e-8 um.
 struct ScanSmem {
   float cxh[SCAN_CH], cxl[SCAN_CH], cyh[SCAN_CH], cyl[SCAN_CH];
+  // Leaf box x / y extent relative to the corner, float pairs: x0, x1, y0, y1.
+  float lbh[4][SCAN_CH], lbl[4][SCAN_CH];
   float m[SCAN_CH], delta[SCAN_CH], err[SCAN_CH], sig[SCAN_CH];
   float g[21][SCAN_CH];
   int s[SCAN_CH];
@@ -96,6 +94,11 @@ __device__ __forceinline__ void prep_crystal(const ScanTile& t, uint32_t s, Scan
   const float m = static_cast<float>(m64);
   P.px = k.pos.x;
   P.py = k.pos.y;
+  const double* lb = t.lbox64 + 6ull * t.leafof[s];
+  P.lx0 = lb[0];
+  P.lx1 = lb[3];
+  P.ly0 = lb[1];
+  P.ly1 = lb[4];
   P.m = m;
   P.delta = static_cast<float>(t.z0 - k.pos.z);
   P.sig = t.sigma_c ? t.sigma_c[s] : t.sigma;
@@ -127,9 +130,12 @@ __device__ __forceinline__ void prep_crystal(const ScanTile& t, uint32_t s, Scan
       P.err = 0.0f;  // bounds are formed per ray from the t values
     } else {
       P.kind = K_CUBE;
-      // |d local| <= 4e-7 m + 1e-7 (rounded rows, offsets); |d D| <= eps D; each t = (+-D - lo)
-      // * inv carries (d lo + d D) |inv| + 2 eps |t|, with |t| <= (D + 2m) invmax.
-      P.err = 4.0f * ((4e-7f * m + 1e-7f + EPS32 * Dmax) * invmax + 2.0f * EPS32 * (Dmax + 2.0f * m) * invmax);
+      // A cube lies within sqrt(3) m of its centre, so rays that can hit it are within mr of the
+      // centre in x and y.  |d local| <= 4e-7 mr + 1e-7 (rounded rows, offsets); |d D| <= eps D;
+      // each t = (+-D - lo) * inv carries (d lo + d D) |inv| + 2 eps |t|, with |t| <= (D + 2 mr)
+      // invmax.
+      const float mr = 1.7320509f * m;
+      P.err = 4.0f * ((4e-7f * mr + 1e-7f + EPS32 * Dmax) * invmax + 2.0f * EPS32 * (Dmax + 2.0f * mr) * invmax);
     }
   } else {
     P.kind = K_ELLIPSOID;
@@ -164,6 +170,10 @@ __device__ __forceinline__ void stage_crystal(const ScanTile& t, ScanSmem& sm, i
   }
   split64(P.px - bx0, sm.cxh[c], sm.cxl[c]);
   split64(P.py - by0, sm.cyh[c], sm.cyl[c]);
+  split64(P.lx0 - bx0, sm.lbh[0][c], sm.lbl[0][c]);
+  split64(P.lx1 - bx0, sm.lbh[1][c], sm.lbl[1][c]);
+  split64(P.ly0 - by0, sm.lbh[2][c], sm.lbl[2][c]);
+  split64(P.ly1 - by0, sm.lbh[3][c], sm.lbl[3][c]);
   sm.m[c] = P.m;
   sm.delta[c] = P.delta;
   sm.err[c] = P.err;
@@ -212,13 +222,27 @@ __device__ __forceinline__ bool scan_pair(const ScanTile& t, const ScanSmem& sm,
   two_sum(oyh, -sm.cyh[c], dh, dl);
   fast_two_sum(dh, dl + (oyl - sm.cyl[c]), dy, dyl);
   const float m = sm.m[c], delta = sm.delta[c];
-  // Own box (strict containment in x and y, entry below the origin in z): exact margins
-  // up to ~2 eps m.
-  const float mx = m - fabsf(dx), my = m - fabsf(dy), mz = delta + m;
-  const float EB = 7.2e-7f * m + 1e-9f, EBz = 1e-6f + 2.4e-7f * m;
-  if (mx < -EB || my < -EB || mz < -EBz) return false;
   const int kind = sm.kind[c];
-  bool amb = mx <= EB || my <= EB || mz <= EBz || kind == K_FP64;
+  // Geometry reach: a cube lies within sqrt(3) m of its centre, an ellipsoid within its own box.
+  const float reach = (kind == K_ELLIPSOID ? m : 1.7320509f * m) * 1.00001f + 1e-9f;
+  if (fabsf(dx) > reach || fabsf(dy) > reach) return false;
+  // The leaf box (strict containment in x and y; the origin lies above every box in z): margins
+  // of float-pair differences, exact to ~1e-12 um.
+  float lm = INFINITY;
+  {
+    float h, l;
+    two_sum(oxh, -sm.lbh[0][c], h, l);
+    lm = fminf(lm, h + (l + (oxl - sm.lbl[0][c])));
+    two_sum(sm.lbh[1][c], -oxh, h, l);
+    lm = fminf(lm, h + (l + (sm.lbl[1][c] - oxl)));
+    two_sum(oyh, -sm.lbh[2][c], h, l);
+    lm = fminf(lm, h + (l + (oyl - sm.lbl[2][c])));
+    two_sum(sm.lbh[3][c], -oyh, h, l);
+    lm = fminf(lm, h + (l + (sm.lbl[3][c] - oyl)));
+  }
+  const float EBL = 1e-9f;
+  if (lm < -EBL) return false;
+  bool amb = lm <= EBL || kind == K_FP64;
   bool hit = false;
   chord = 0.0f;
   if (!amb) {
@@ -526,6 +550,8 @@ uint32_t scan_bin_px(uint32_t spp) {
 // device (shared by the forward scan and its adjoint).
 struct ScanPlan {
   ScanTile t{};
+  RTreeBufs tree;             // the reference tree over the developed crystals
+  DBuf<uint32_t> tree_list;
   DBuf<ScanPrep> prep;
   DBuf<uint32_t> cnt, off, cur, items;
   DBuf<ScanTile> td;
@@ -540,8 +566,11 @@ static void plan_scan(fg_engine* e, const fg_emulsion* em, const fg_scan_cfg& cf
   const uint32_t a = std::max<uint32_t>(g * g, 1);
   FG_REQUIRE(a <= SCAN_THREADS, "samples_per_pixel too large (at most 256 strata)");
   FG_REQUIRE(cfg.width_px > 0 && cfg.height_px > 0, "scan size must be positive");
+  build_emulsion_tree(e, em, true, P.tree, P.tree_list);
   ScanTile& t = P.t;
   t = ScanTile{};
+  t.lbox64 = P.tree.box64.p;
+  t.leafof = P.tree.leafof.p;
   t.a = em->a.p;
   t.q = em->q.p;
   t.d = em->d.p;

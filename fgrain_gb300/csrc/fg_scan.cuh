@@ -1,11 +1,15 @@
 // Device code of the transmittance scan (transmittance.rs:65-171).
 //
 // Scanner rays are vertical (origin (x, y, depth + 0.1), direction -z), so the scan is a 2D
-// problem: a ray can only hit developed crystals whose own max_dim box contains its (x, y)
-// strictly (bvh.rs:96-124 with inv_dir = (inf, inf, -1)).  The image is cut into bins of
-// bin_px x bin_px pixels; every developed crystal is listed in the bins its box overlaps; one CTA
-// scans one bin: it stages the bin's crystals in shared memory, pre-transformed for vertical rays
-// and relative to the bin corner, then each thread traces one stratum ray against them.
+// problem.  The reference walks a tree over the developed crystals (transmittance.rs:86-89,
+// bvh.rs:300-347) and counts every crystal of every leaf whose box the ray hits by its geometry
+// alone; a leaf box is hit by a vertical ray iff it contains the ray's (x, y) strictly
+// (bvh.rs:96-124 with inv_dir = (inf, inf, -1)).  So a ray hits crystal s iff its geometry is hit
+// and (x, y) lies strictly inside the box of s's leaf in that tree (built on the device, see
+// fg_rtree.cuh).  The image is cut into bins of bin_px x bin_px pixels; every developed crystal is
+// listed in the bins its leaf box overlaps; one CTA scans one bin: it stages the bin's crystals in
+// shared memory, pre-transformed for vertical rays and relative to the bin corner, then each
+// thread traces one stratum ray against them.
 //
 // Hit decisions are exact: each FP32 decision quantity carries a per-crystal error bound; when
 // a margin falls inside it the ray/crystal pair is re-evaluated with the reference's FP64
@@ -14,6 +18,7 @@
 // the density conversion are FP64.
 #pragma once
 #include "fg_device.cuh"
+#include "fg_rtree.cuh"
 
 namespace fg {
 
@@ -22,15 +27,16 @@ constexpr int SCAN_THREADS = 256;   // rays per CTA (bin_px^2 * strata)
 
 // Bin-independent part of a developed crystal's staging, derived once per crystal in FP64 and
 // rounded (k_scan_prep): each bin that lists the crystal only adds its centre relative to the
-// bin's corner.  128 bytes, read with vector loads.
+// bin's corner.  160 bytes, read with vector loads.
 struct __align__(16) ScanPrep {
   double px, py;   // centre x, y (um) as the scan sees it
+  double lx0, lx1, ly0, ly1;  // the x and y extent of the crystal's leaf box in the scan's tree
   float g[21];     // per-kind terms (see stage_crystal)
   float m, delta, err, sig;
   int kind;
   int pad_[2];
 };
-static_assert(sizeof(ScanPrep) == 128, "ScanPrep layout");
+static_assert(sizeof(ScanPrep) == 160, "ScanPrep layout");
 
 struct ScanTile {
   const ScanPrep* prep;  // staging of developed crystals (null: derived in each bin)
@@ -43,6 +49,8 @@ struct ScanTile {
   const double* quat64;
   const uint8_t* developed;
   const double* exp64;
+  const double* lbox64;    // the scan tree's node boxes (lo xyz, hi xyz; tile-local node ids)
+  const uint32_t* leafof;  // per crystal slot: its leaf in the scan tree
   const float* sigma_c;  // per crystal (Morton order) or null
   const uint32_t* bin_off;
   const uint32_t* bin_items;
@@ -102,7 +110,8 @@ __device__ __forceinline__ Crystal64 load64_parts(const ScanTile& t, uint32_t s)
   return k;
 }
 
-// Exact FP64 chord of a vertical scan ray through crystal s (0 when it misses).
+// Exact FP64 chord of a vertical scan ray through crystal s (0 when it misses): the reference's
+// geometry with the crystal's expansion, and the ray inside the box of the crystal's leaf.
 static __device__ __noinline__ double scan_chord64(const ScanTile& t, uint32_t s, double ox, double oy,
                                             bool& hit) {
   const Crystal64 k = load64_parts(t, s);
@@ -111,7 +120,7 @@ static __device__ __noinline__ double scan_chord64(const ScanTile& t, uint32_t s
   const D3 dir = d3(0.0, 0.0, -1.0);
   const D3 inv = d3(__ddiv_rn(1.0, 0.0), __ddiv_rn(1.0, 0.0), -1.0);
   double t0, t1;
-  hit = dcanonical_hit(k, e, o, dir, inv, t0, t1);
+  hit = rt_box_hit64(t.lbox64 + 6ull * t.leafof[s], o, inv) && dintersect(k, e, o, dir, t0, t1);
   return hit ? fmax(__dsub_rn(t1, t0), 0.0) : 0.0;
 }
 

@@ -7,11 +7,13 @@
 // device-wide synchronisation of cudaMalloc / cudaFree.  Such a caller hands over the crystal set
 // and the output image in device memory it already holds.
 //
-// The scan's own scratch (bin lists, the kernel descriptor, the error word) lives in one
-// file-scope __device__ array of FG_STATIC_SCAN_SCRATCH_BYTES (about 4.4 MB).  Every GPU on
-// which this library is loaded holds that array until the process exits.  It bounds the work of
-// one call: at most FG_STATIC_SCAN_MAX_BINS scan bins and FG_STATIC_SCAN_MAX_ITEMS
-// (crystal, bin) entries; larger requests are rejected before any output is written.
+// The scan's own scratch (the reference tree over the developed crystals, bin lists, the kernel
+// descriptor, the error word) lives in one file-scope __device__ array of
+// FG_STATIC_SCAN_SCRATCH_BYTES (about 17 MB).  Every GPU on which this library is loaded holds that
+// array until the process exits.  It bounds the work of one call: at most
+// FG_STATIC_SCAN_MAX_CRYSTALS crystals of which FG_STATIC_SCAN_MAX_DEVELOPED developed,
+// FG_STATIC_SCAN_MAX_BINS scan bins and FG_STATIC_SCAN_MAX_ITEMS (crystal, bin) entries; larger
+// requests are rejected before any output is written.
 //
 // All calls on a device share the one array, and it keeps whatever the last call left in it:
 // each call clears the parts that must start at zero (bin counts, cursors, error word) on the
@@ -21,8 +23,10 @@
 // the stream before it returns, also on failure), so concurrent callers wait for each other.
 // Other processes load their own copy of the array.
 //
-// The bins, the binned scan kernel and the result are those of fg_scan_emulsion (same kernels,
-// same descriptor), so both entry points give the same image for the same crystals.
+// The tree, the bins, the binned scan kernel and the result are those of fg_scan_emulsion (same
+// kernels, same descriptor), so both entry points give the same image for the same crystals.  The
+// developed crystals enter the tree in whatever order the device lists them: the leaves' crystal
+// sets and boxes, which are all the scan uses, do not depend on that order.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -53,7 +57,11 @@ constexpr size_t kCntOff = 512;                                  // per-bin coun
 constexpr size_t kOffOff = kCntOff + kBinBytes;                  // exclusive prefix sums
 constexpr size_t kCurOff = kOffOff + kBinBytes;                  // fill cursors
 constexpr size_t kItemsOff = kCurOff + kBinBytes;                // bin lists (crystal indices)
-constexpr size_t kScratchBytes = kItemsOff + FG_STATIC_SCAN_MAX_ITEMS * sizeof(uint32_t);
+constexpr size_t kDevListOff = round256(kItemsOff + FG_STATIC_SCAN_MAX_ITEMS * sizeof(uint32_t));  // developed
+constexpr size_t kDevCountOff = round256(kDevListOff + FG_STATIC_SCAN_MAX_DEVELOPED * sizeof(uint32_t));
+constexpr size_t kTreeOff = kDevCountOff + 256;                  // the scan's reference tree
+constexpr size_t kTreeBytes = rtree_attach_bytes(FG_STATIC_SCAN_MAX_DEVELOPED, true, FG_STATIC_SCAN_MAX_CRYSTALS);
+constexpr size_t kScratchBytes = kTreeOff + kTreeBytes;
 static_assert(sizeof(ScanTile) <= kErrOff - kDescOff, "scan descriptor does not fit its slot");
 static_assert(kScratchBytes == FG_STATIC_SCAN_SCRATCH_BYTES, "header and scratch layout disagree");
 
@@ -128,6 +136,14 @@ __global__ void __launch_bounds__(kScanThreads) k_exclusive_scan_small(const uin
   }
 }
 
+// Lists the developed crystals (any order) and counts them; entries past `cap` are only counted.
+__global__ void k_static_devlist(const uint8_t* developed, uint32_t n, uint32_t* list, uint32_t* count, uint32_t cap) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n || !developed[s]) return;
+  const uint32_t k = atomicAdd(count, 1u);
+  if (k < cap) list[k] = s;
+}
+
 void write_message(char* msg, size_t len, const std::string& s) {
   if (!msg || len == 0) return;
   const size_t k = std::min(len - 1, s.size());
@@ -139,7 +155,8 @@ void static_scan(const fg_device_crystals* c, const fg_emulsion_cfg* film, const
                  uint64_t seed, float* out, uint8_t* image8, cudaStream_t st) {
   FG_REQUIRE(c && film && cfg, "null argument");
   FG_REQUIRE(out || image8, "no output: pass out and/or image8 (device pointers)");
-  FG_REQUIRE(c->n <= 0xffffffffull, "too many crystals (at most 2^32 - 1)");
+  FG_REQUIRE(c->n <= FG_STATIC_SCAN_MAX_CRYSTALS,
+             "too many crystals: the static scratch holds at most " + std::to_string(FG_STATIC_SCAN_MAX_CRYSTALS));
   if (c->n) FG_REQUIRE(c->a && c->q && c->d && c->developed && c->expansion, "null crystal array");
   FG_REQUIRE(((reinterpret_cast<uintptr_t>(c->a) | reinterpret_cast<uintptr_t>(c->q) |
                reinterpret_cast<uintptr_t>(c->d)) & 15u) == 0,
@@ -205,6 +222,8 @@ void static_scan(const fg_device_crystals* c, const fg_emulsion_cfg* film, const
   auto* off = reinterpret_cast<uint32_t*>(base + kOffOff);
   auto* cur = reinterpret_cast<uint32_t*>(base + kCurOff);
   auto* items = reinterpret_cast<uint32_t*>(base + kItemsOff);
+  auto* devlist = reinterpret_cast<uint32_t*>(base + kDevListOff);
+  auto* devcount = reinterpret_cast<uint32_t*>(base + kDevCountOff);
   t.bin_off = off;
   t.bin_items = items;
 
@@ -217,10 +236,39 @@ void static_scan(const fg_device_crystals* c, const fg_emulsion_cfg* film, const
       if (armed) (void)cudaStreamSynchronize(st);
     }
   } drain{st};
-  // What must start at zero: counts (and the total slot), cursors, the error word.
+  // What must start at zero: counts (and the total slot), cursors, the error word, the developed count.
   FG_CUDA(cudaMemsetAsync(cnt, 0, (nbins + 1) * sizeof(uint32_t), st));
   FG_CUDA(cudaMemsetAsync(cur, 0, (nbins + 1) * sizeof(uint32_t), st));
   FG_CUDA(cudaMemsetAsync(err, 0, 4 * sizeof(uint32_t), st));
+  FG_CUDA(cudaMemsetAsync(devcount, 0, sizeof(uint32_t), st));
+  // The scan's tree over the developed crystals (transmittance.rs:86-89).
+  if (t.n)
+    k_static_devlist<<<grid_for(t.n, 256), 256, 0, st>>>(c->developed, t.n, devlist, devcount,
+                                                          FG_STATIC_SCAN_MAX_DEVELOPED);
+  FG_CUDA(cudaGetLastError());
+  uint32_t ndev = 0;
+  FG_CUDA(cudaMemcpyAsync(&ndev, devcount, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  FG_CUDA(cudaStreamSynchronize(st));
+  if (ndev > FG_STATIC_SCAN_MAX_DEVELOPED)
+    throw Error{FG_ERR_INVALID_ARG, std::to_string(ndev) + " developed crystals; the static scratch holds at most " +
+                                        std::to_string(FG_STATIC_SCAN_MAX_DEVELOPED)};
+  RTreeBufs tree;
+  {
+    RTile rt{};
+    rt.a = t.a;
+    rt.d = t.d;
+    rt.pos64 = t.pos64;
+    rt.dims64 = t.dims64;
+    rt.exp64 = t.exp64;
+    rt.order = devlist;
+    rt.ecap = FG_STATIC_SCAN_MAX_DEVELOPED;
+    rt.n = ndev;
+    rt.pad = static_cast<float>(std::max(film->width, film->height) * 2e-6 + 1e-5);
+    rtree_attach(tree, rt, true, FG_STATIC_SCAN_MAX_CRYSTALS, base + kTreeOff, kTreeBytes, st);
+    rtree_build(tree, err, st);
+  }
+  t.lbox64 = tree.box64.p;
+  t.leafof = tree.leafof.p;
   if (t.n) k_bin_count<<<grid_for(t.n, 256), 256, 0, st>>>(t, cnt);
   k_exclusive_scan_small<<<1, kScanThreads, 0, st>>>(cnt, off, static_cast<uint32_t>(nbins + 1));
   FG_CUDA(cudaGetLastError());

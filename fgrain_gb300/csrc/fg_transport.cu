@@ -3,10 +3,10 @@
 //
 // Work: photon ids of all tiles form one index space; each warp takes 32 ids at a time from a
 // global counter.  Every draw is a Philox block named by (photon, bounce, slot, tag), so results
-// do not depend on which warp or SM traces a photon.  Hits of one segment are collected, ordered
-// by (t_enter, crystal id) and absorbed in that order (Beer-Lambert, Bernoulli rounding of
-// 5 E p s latent photons, energy *= max(1 - 0.9 p, 0.05)).  Counts reach HBM as warp-aggregated
-// atomics.
+// do not depend on which warp or SM traces a photon.  Each segment walks the tile's reference tree
+// (fg_rtree.cuh) and absorbs its hits in the reference's traversal order as they are found
+// (Beer-Lambert, Bernoulli rounding of 5 E p s latent photons, energy *= max(1 - 0.9 p, 0.05)).
+// Counts reach HBM as warp-aggregated atomics.
 #include "fg_internal.h"
 #include "fg_transport.cuh"
 
@@ -18,7 +18,7 @@ namespace fg {
 
 // ---------------------------------------------------------------------------------------------
 // Production kernel with lane refill: each loop turn every lane with a live packet runs one bounce
-// (its LBVH walk, then absorption and the move or scatter); lanes whose packet died take the next
+// (its tree walk with absorption, then the move or scatter); lanes whose packet died take the next
 // photon of the position-ordered queue, so the warp stays full until the queue is empty.
 // Launch bounds of 4 blocks of 256 per SM (64 registers): the walk is latency-bound, and with
 // the brick-ordered tree 32 resident warps with fewer spills beat 40 at 48 registers and 48 at
@@ -29,7 +29,6 @@ __global__ void __launch_bounds__(256, 4) k_transport(const TileDesc* __restrict
                                                      unsigned long long* stats) {
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
-  HitS hits[HMAX];
   Photon ph;
   int tile = 0;
   bool alive = false, done = false;
@@ -68,7 +67,7 @@ __global__ void __launch_bounds__(256, 4) k_transport(const TileDesc* __restrict
         alive = false;
       } else {
         uint32_t nh = 0;
-        alive = photon_bounce(tiles[tile], ph, hits, err, nh, FG_DEFERRED_LEAVES ? amask : 0u);
+        alive = photon_bounce(tiles[tile], ph, err, nh, FG_DEFERRED_LEAVES ? amask : 0u);
         my_hits += nh;
       }
     }
@@ -117,116 +116,111 @@ void launch_photon_sort(const TileDesc* tiles_dev, int ntiles, unsigned long lon
 }
 
 // ---------------------------------------------------------------------------------------------
-// Exact replay of recorded segments: FP32 LBVH walk for candidates, the reference predicate and
-// per-hit arithmetic in FP64.  pass 0 counts hits per segment; pass 1 writes hit ids and adds the
-// latent photons.
-struct Hit64 {
-  double t0, t1;
-  uint32_t id, s;
+// Exact replay of recorded segments: the reference walk in FP64 (rt_walk64 over the reference
+// tree, whole ray, the reference's stack rule), each leaf crystal tested with the reference's
+// geometry in FP64, hits inside the step absorbed in walk order (transport.rs:108-138).  pass 0
+// counts hits per segment; pass 1 writes hit ids and adds the latent photons.
+struct RtView {
+  const double* box64;
+  const int2* nchild;
+  const int* nsplit;
+  const uint32_t* nstart;
+  const uint32_t* ncount;
+  const uint32_t* ridx;
+  uint32_t root;
+  uint32_t count;  // elements of the tree (none: nothing to walk)
 };
 
-__global__ void k_replay_segments(const fg_segment* __restrict__ segs, uint32_t nseg,
-                                  CrystalsView cv, const Node* __restrict__ nodes,
-                                  const uint32_t* __restrict__ s2id, uint32_t n, double alpha,
-                                  uint32_t k0, uint32_t k1, int pass, uint32_t* seg_count,
-                                  const uint32_t* offsets, uint32_t* ids, uint32_t id_cap,
-                                  uint32_t* counts, uint32_t* err) {
+RtView rt_view(const RTreeBufs& B) {
+  RtView v;
+  v.box64 = B.box64.p;
+  v.nchild = B.nchild.p;
+  v.nsplit = B.nsplit.p;
+  v.nstart = B.nstart.p;
+  v.ncount = B.ncount.p;
+  v.ridx = B.ridx.p;
+  v.root = 1;
+  v.count = B.count;
+  return v;
+}
+
+template <class F>
+__device__ __forceinline__ void rt_crystals64(const RtView& rv, D3 o, D3 inv, uint32_t n, uint32_t* err, F&& fn) {
+  if (n == 0 || rv.count == 0) return;
+  rt_walk64(rv.box64, rv.nchild, rv.nsplit, rv.root, o, inv, [&](uint32_t leaf) {
+    const uint32_t st = rv.nstart[leaf], cn = rv.ncount[leaf];
+    for (uint32_t k = 0; k < cn; ++k) {
+      const uint32_t s = rv.ridx[st + k];
+      if (index_ok(s < n, err, SITE_LEAF, s, n)) fn(s);
+    }
+  });
+}
+
+__global__ void k_replay_segments(const fg_segment* __restrict__ segs, uint32_t nseg, CrystalsView cv, RtView rv,
+                                  const uint32_t* __restrict__ s2id, uint32_t n, double alpha, uint32_t k0,
+                                  uint32_t k1, int pass, uint32_t* seg_count, const uint32_t* offsets, uint32_t* ids,
+                                  uint32_t id_cap, uint32_t* counts, uint32_t* err) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nseg || n == 0) return;
   const fg_segment g = segs[i];
   const D3 o = d3(g.origin[0], g.origin[1], g.origin[2]);
   const D3 d = d3(g.dir[0], g.dir[1], g.dir[2]);
   const D3 inv = d3(__ddiv_rn(1.0, d.x), __ddiv_rn(1.0, d.y), __ddiv_rn(1.0, d.z));
-  const float3 of = make_float3((float)o.x, (float)o.y, (float)o.z);
-  const float3 invf = make_float3(1.0f / (float)d.x, 1.0f / (float)d.y, 1.0f / (float)d.z);
-  const float tlim = (float)g.step * 1.00001f + 1e-3f;
-  Hit64 hits[HMAX];
-  int nh = 0;
-  walk_lbvh(nodes, of, invf, tlim, err, [&](uint32_t s) {
+  double E = g.energy;
+  const uint32_t base = pass ? offsets[i] : 0u;
+  uint32_t nh = 0;
+  P4 r{};
+  rt_crystals64(rv, o, inv, n, err, [&](uint32_t s) {
     const Crystal64 k = load64(cv, s);
     double t0, t1;
-    if (!dcanonical_hit(k, 1.0, o, d, inv, t0, t1)) return;
+    if (!dintersect(k, 1.0, o, d, t0, t1)) return;
     if (!(t0 < g.step)) return;
     const double path = fmax(__dsub_rn(fmin(t1, g.step), t0), 0.0);
     if (!(path > 0.0)) return;
-    const uint32_t id = s2id ? s2id[s] : s;
-    if (nh == HMAX) { atomicOr(err, ERR_HIT_OVERFLOW); return; }
-    int j = nh++;
-    while (j > 0 && (hits[j - 1].t0 > t0 || (hits[j - 1].t0 == t0 && hits[j - 1].id > id))) {
-      hits[j] = hits[j - 1];
-      --j;
+    if (pass) {
+      if ((nh & 3) == 0) r = philox(g.photon, g.bounce, nh >> 2, TAG_HIT, k0, k1);
+      const double u = ud(word(r, nh & 3));
+      uint32_t cnt;
+      E = absorb64(E, path, alpha, cv.sens64 ? cv.sens64[s] : static_cast<double>(cv.a[s].w), u, &cnt);
+      if (cnt) atomicAdd(&counts[s], cnt);
+      if (base + nh < id_cap) ids[base + nh] = s2id ? s2id[s] : s;
     }
-    hits[j] = Hit64{t0, t1, id, s};
+    ++nh;
   });
-  if (pass == 0) {
-    seg_count[i] = static_cast<uint32_t>(nh);
-    return;
-  }
-  double E = g.energy;
-  const uint32_t base = offsets[i];
-  P4 r{};
-  for (int h = 0; h < nh; ++h) {
-    if ((h & 3) == 0) r = philox(g.photon, g.bounce, static_cast<uint32_t>(h) >> 2, TAG_HIT, k0, k1);
-    const double u = ud(word(r, h & 3));
-    const double path = fmax(__dsub_rn(fmin(hits[h].t1, g.step), hits[h].t0), 0.0);
-    const double sens = cv.sens64 ? cv.sens64[hits[h].s] : (double)cv.a[hits[h].s].w;
-    uint32_t cnt;
-    E = absorb64(E, path, alpha, sens, u, &cnt);
-    if (cnt) atomicAdd(&counts[hits[h].s], cnt);
-    if (base + h < id_cap) ids[base + h] = hits[h].id;
-  }
+  if (pass == 0) seg_count[i] = nh;
 }
 
-// Hits of arbitrary rays (no step limit), exact rule; e is the expansion of developed crystals.
-__global__ void k_replay_rays(const double* __restrict__ org, const double* __restrict__ dir,
-                              uint32_t nrays, CrystalsView cv, const Node* __restrict__ nodes,
-                              const uint32_t* __restrict__ s2id, uint32_t n,
-                              const uint8_t* developed, const double* exp64, int developed_only,
-                              int pass, uint32_t* ray_count, const uint32_t* offsets,
-                              uint32_t* ids, uint32_t id_cap, double* chord_sum, uint32_t* err) {
+// Hits of arbitrary rays (whole ray, reference walk, exact geometry): over all crystals of the
+// emulsion's tree, or over the developed ones (the scan's tree) with their expansion.
+__global__ void k_replay_rays(const double* __restrict__ org, const double* __restrict__ dir, uint32_t nrays,
+                              CrystalsView cv, RtView rv, const uint32_t* __restrict__ s2id, uint32_t n,
+                              const double* exp64, int developed_only, int pass, uint32_t* ray_count,
+                              const uint32_t* offsets, uint32_t* ids, uint32_t id_cap, double* chord_sum,
+                              uint32_t* err) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nrays) return;
   const D3 o = d3(org[3 * i], org[3 * i + 1], org[3 * i + 2]);
   const D3 d = d3(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]);
   const D3 inv = d3(__ddiv_rn(1.0, d.x), __ddiv_rn(1.0, d.y), __ddiv_rn(1.0, d.z));
-  const float3 of = make_float3((float)o.x, (float)o.y, (float)o.z);
-  const float3 invf = make_float3(1.0f / (float)d.x, 1.0f / (float)d.y, 1.0f / (float)d.z);
-  Hit64 hits[HMAX];
-  int nh = 0;
-  if (n > 0) {
-    walk_lbvh(nodes, of, invf, INFINITY, err, [&](uint32_t s) {
-      if (developed_only && !developed[s]) return;
-      const double e = developed_only ? exp64[s] : 1.0;
-      const Crystal64 k = load64(cv, s);
-      double t0, t1;
-      if (!dcanonical_hit(k, e, o, d, inv, t0, t1)) return;
-      const uint32_t id = s2id ? s2id[s] : s;
-      if (nh == HMAX) { atomicOr(err, ERR_HIT_OVERFLOW); return; }
-      int j = nh++;
-      while (j > 0 && (hits[j - 1].t0 > t0 || (hits[j - 1].t0 == t0 && hits[j - 1].id > id))) {
-        hits[j] = hits[j - 1];
-        --j;
-      }
-      hits[j] = Hit64{t0, t1, id, s};
-    });
-  }
-  if (pass == 0) {
-    ray_count[i] = static_cast<uint32_t>(nh);
-    return;
-  }
-  const uint32_t base = offsets[i];
+  const uint32_t base = pass ? offsets[i] : 0u;
+  uint32_t nh = 0;
   double L = 0.0;
-  for (int h = 0; h < nh; ++h) {
-    L = __dadd_rn(L, fmax(__dsub_rn(hits[h].t1, hits[h].t0), 0.0));
-    if (base + h < id_cap) ids[base + h] = hits[h].id;
+  rt_crystals64(rv, o, inv, n, err, [&](uint32_t s) {
+    const double e = developed_only ? exp64[s] : 1.0;
+    const Crystal64 k = load64(cv, s);
+    double t0, t1;
+    if (!dintersect(k, e, o, d, t0, t1)) return;
+    if (pass) {
+      L = __dadd_rn(L, fmax(__dsub_rn(t1, t0), 0.0));
+      if (base + nh < id_cap) ids[base + nh] = s2id ? s2id[s] : s;
+    }
+    ++nh;
+  });
+  if (pass == 0) {
+    ray_count[i] = nh;
+  } else if (chord_sum) {
+    chord_sum[i] = L;
   }
-  if (chord_sum) chord_sum[i] = L;
-}
-
-// Four-wide collapse of a binary LBVH with n crystals (its max(n - 1, 1) internal nodes).
-__global__ void k_collapse4(const Node* __restrict__ nodes, uint32_t nint, Node4* __restrict__ out) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < nint) collapse_node4(nodes, static_cast<int>(i), out + i);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -236,7 +230,10 @@ TileDesc make_tile_desc(const fg_emulsion* em, const float* tile_dev, uint32_t t
   t.a = em->a.p;
   t.q = em->q.p;
   t.d = em->d.p;
-  t.nodes = em->nodes.p;
+  t.rnode = em->rt.rnode.p;
+  t.rleaf = em->rt.rleaf.p;
+  t.ridx = em->rt.ridx.p;
+  t.nnodes = static_cast<uint32_t>(em->rt.N);
   t.s2id = em->sorted_to_id.p;
   t.n = em->n;
   t.counts = counts;
@@ -283,11 +280,6 @@ void expose(fg_engine* e, fg_emulsion* em, const float* tile_dev, uint32_t tw, u
   TileDesc t = make_tile_desc(em, tile_dev, tw, th, cfg, seed, em->counts.p);
   if (photons_out) *photons_out = t.P;
   if (t.P == 0 || em->n == 0) return;
-  const uint32_t nint = em->n > 1 ? em->n - 1 : 1;
-  DBuf<Node4> n4(nint, st);
-  k_collapse4<<<grid_for(nint, 256), 256, 0, st>>>(em->nodes.p, nint, n4.p);
-  FG_CUDA(cudaGetLastError());
-  t.nodes4 = n4.p;
   DBuf<TileDesc> td(1, st);
   DBuf<unsigned long long> ctr(1, st);
   FG_CUDA(cudaMemcpyAsync(td.p, &t, sizeof(TileDesc), cudaMemcpyHostToDevice, st));
@@ -305,10 +297,10 @@ void replay_segments(fg_engine* e, fg_emulsion* em, const fg_exposure_cfg& cfg, 
   if (nseg) FG_CUDA(cudaMemcpyAsync(segs.p, segs_host, nseg * sizeof(fg_segment), cudaMemcpyHostToDevice, st));
   const uint32_t k0 = static_cast<uint32_t>(seed), k1 = static_cast<uint32_t>(seed >> 32);
   const unsigned grid = grid_for(std::max<size_t>(nseg, 1), 128);
-  k_replay_segments<<<grid, 128, 0, st>>>(segs.p, (uint32_t)nseg, em->view(), em->nodes.p,
-                                          em->sorted_to_id.p, em->n, cfg.crystal_absorption_coeff,
-                                          k0, k1, 0, cnt.p, nullptr, nullptr, 0, em->counts.p,
-                                          e->d_err);
+  const RtView rv = rt_view(em->rt);
+  k_replay_segments<<<grid, 128, 0, st>>>(segs.p, (uint32_t)nseg, em->view(), rv, em->sorted_to_id.p, em->n,
+                                          cfg.crystal_absorption_coeff, k0, k1, 0, cnt.p, nullptr, nullptr, 0,
+                                          em->counts.p, e->d_err);
   FG_CUDA(cudaGetLastError());
   std::vector<uint32_t> hc(nseg + 1, 0);
   if (nseg) FG_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, nseg * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
@@ -324,11 +316,10 @@ void replay_segments(fg_engine* e, fg_emulsion* em, const fg_exposure_cfg& cfg, 
   if (nhits) *nhits = acc;
   FG_CUDA(cudaMemcpyAsync(off.p, ho.data(), (nseg + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
   DBuf<uint32_t> ids(std::max<uint64_t>(std::min<uint64_t>(acc, id_cap), 1), st);
-  k_replay_segments<<<grid, 128, 0, st>>>(segs.p, (uint32_t)nseg, em->view(), em->nodes.p,
-                                          em->sorted_to_id.p, em->n, cfg.crystal_absorption_coeff,
-                                          k0, k1, 1, nullptr, off.p, ids.p,
-                                          static_cast<uint32_t>(std::min<uint64_t>(acc, id_cap)),
-                                          em->counts.p, e->d_err);
+  k_replay_segments<<<grid, 128, 0, st>>>(segs.p, (uint32_t)nseg, em->view(), rv, em->sorted_to_id.p, em->n,
+                                          cfg.crystal_absorption_coeff, k0, k1, 1, nullptr, off.p, ids.p,
+                                          static_cast<uint32_t>(std::min<uint64_t>(acc, id_cap)), em->counts.p,
+                                          e->d_err);
   FG_CUDA(cudaGetLastError());
   if (ids_host && acc) {
     FG_CUDA(cudaMemcpyAsync(ids_host, ids.p, std::min<uint64_t>(acc, id_cap) * sizeof(uint32_t),
@@ -350,20 +341,15 @@ void replay_rays(fg_engine* e, const fg_emulsion* em, const double* org_host,
     FG_CUDA(cudaMemcpyAsync(org.p, org_host, 3 * nrays * sizeof(double), cudaMemcpyHostToDevice, st));
     FG_CUDA(cudaMemcpyAsync(dir.p, dir_host, 3 * nrays * sizeof(double), cudaMemcpyHostToDevice, st));
   }
-  // Developed crystals are tested with their expansion: walk a refitted copy of the tree.
-  const Node* nodes = em->nodes.p;
-  DBuf<Node> dev_nodes;
-  if (developed_only && em->n > 0) {
-    dev_nodes.alloc(em->nodes.n, st);
-    FG_CUDA(cudaMemcpyAsync(dev_nodes.p, em->nodes.p, em->nodes.n * sizeof(Node), cudaMemcpyDeviceToDevice, st));
-    refit_lbvh(const_cast<fg_emulsion*>(em), dev_nodes.p, em->leaf_parent.p, true, st);
-    nodes = dev_nodes.p;
-  }
+  // Developed crystals are tested with their expansion over the scan's tree (developed crystals
+  // only, transmittance.rs:86-89).
+  RTreeBufs dev_tree;
+  DBuf<uint32_t> dev_list;
+  if (developed_only && em->n > 0) build_emulsion_tree(e, em, true, dev_tree, dev_list);
+  const RtView rv = rt_view(developed_only ? dev_tree : em->rt);
   const unsigned grid = grid_for(std::max<size_t>(nrays, 1), 128);
-  k_replay_rays<<<grid, 128, 0, st>>>(org.p, dir.p, (uint32_t)nrays, em->view(), nodes,
-                                      em->sorted_to_id.p, em->n, em->developed.p, em->exp64.p,
-                                      developed_only, 0, cnt.p, nullptr, nullptr, 0, nullptr,
-                                      e->d_err);
+  k_replay_rays<<<grid, 128, 0, st>>>(org.p, dir.p, (uint32_t)nrays, em->view(), rv, em->sorted_to_id.p, em->n,
+                                      em->exp64.p, developed_only, 0, cnt.p, nullptr, nullptr, 0, nullptr, e->d_err);
   FG_CUDA(cudaGetLastError());
   std::vector<uint32_t> hc(nrays + 1, 0);
   if (nrays) FG_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, nrays * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
@@ -379,11 +365,9 @@ void replay_rays(fg_engine* e, const fg_emulsion* em, const double* org_host,
   if (nhits) *nhits = acc;
   FG_CUDA(cudaMemcpyAsync(off.p, ho.data(), (nrays + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
   DBuf<uint32_t> ids(std::max<uint64_t>(std::min<uint64_t>(acc, id_cap), 1), st);
-  k_replay_rays<<<grid, 128, 0, st>>>(org.p, dir.p, (uint32_t)nrays, em->view(), nodes,
-                                      em->sorted_to_id.p, em->n, em->developed.p, em->exp64.p,
-                                      developed_only, 1, nullptr, off.p, ids.p,
-                                      static_cast<uint32_t>(std::min<uint64_t>(acc, id_cap)),
-                                      chord.p, e->d_err);
+  k_replay_rays<<<grid, 128, 0, st>>>(org.p, dir.p, (uint32_t)nrays, em->view(), rv, em->sorted_to_id.p, em->n,
+                                      em->exp64.p, developed_only, 1, nullptr, off.p, ids.p,
+                                      static_cast<uint32_t>(std::min<uint64_t>(acc, id_cap)), chord.p, e->d_err);
   FG_CUDA(cudaGetLastError());
   if (ids_host && acc)
     FG_CUDA(cudaMemcpyAsync(ids_host, ids.p, std::min<uint64_t>(acc, id_cap) * sizeof(uint32_t),

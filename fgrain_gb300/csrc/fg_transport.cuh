@@ -1,25 +1,29 @@
-// Device code of the photon transport: tile descriptors, the LBVH walk and the per-photon
-// bounce loop (transport.rs:101-185, optics.rs:100-196).
+// Device code of the photon transport: tile descriptors, the reference-tree walk and the
+// per-photon bounce loop (transport.rs:101-185, optics.rs:100-196).
 #pragma once
 #include "fg_device.cuh"
+#include "fg_rtree.cuh"
 
 namespace fg {
 
-constexpr int HMAX = 48;  // hits kept per segment (a 21 um segment meets ~10 crystals)
 constexpr int WALK_LEAVES = 6;  // leaves a lane may hold while its warp still walks (speculative traversal)
 
-// Everything one tile's transport needs, 16-byte aligned for vector loads.
+// Everything one tile's transport needs, 16-byte aligned for vector loads.  The walk runs over the
+// tile's reference tree (fg_rtree.cuh): rnode / rleaf indexed by tile-local node id, ridx by
+// tile-local element position (a leaf's crystals in the reference's order).
 struct __align__(16) TileDesc {
   const float4* a;
   const float4* q;
   const float4* d;
-  const Node* nodes;
-  const Node4* nodes4;  // the same tree collapsed four-wide (the transport walk)
+  const Node* rnode;
+  const uint2* rleaf;
+  const uint32_t* ridx;
   const uint32_t* s2id;
   uint32_t* counts;
   const float* tile;
   unsigned long long photon_base;
   uint32_t n, tw, th, P;
+  uint32_t nnodes;  // node capacity of the tile's tree (bounds the node ids the walk reads)
   uint32_t stride;  // exposure row stride (floats); tiles may be windows of one image
   uint32_t pcell_base;  // first photon-sort cell of this tile
   uint32_t pcell_bits;  // photon-sort cells per axis = 2^bits (Morton order)
@@ -29,79 +33,27 @@ struct __align__(16) TileDesc {
   uint32_t max_bounces;
 };
 
-// Stack walk of the LBVH: fn(s) is called for every crystal whose padded leaf box the ray
-// enters before tlim.  Both child boxes come with the parent, so each step is one node load.
-// With n > 0 the node and crystal indices read from the tree are checked against the n - 1
-// internal nodes and n crystals of an n-crystal tree (n = 0: unchecked).
+// Walk of a reference tree in the reference's order (BVH::intersect_ray_all, bvh.rs:300-347: push
+// left then right, pop right first), deferred: a hit leaf is queued until every lane of `amask`
+// holds one or has finished, then the lanes run fn(leaf) together; a lane that holds a leaf walks on
+// (speculatively) until it holds WALK_LEAVES.  The queue keeps each lane's leaves in walk order.
+// Child boxes are tested in FP32 against [0, tlim] of the ray (the caller's step, padded): internal
+// boxes are stored rounded outward, leaf boxes rounded to nearest.  nmax bounds the node ids (index
+// checks).  With amask = the lane's own bit it is a plain walk.
 template <class F>
-__device__ __forceinline__ void walk_lbvh(const Node* __restrict__ nodes, float3 o, float3 inv,
-                                          float tlim, uint32_t* err, F&& fn, uint32_t n = 0) {
-  const int nint = n > 1 ? static_cast<int>(n - 1) : 1;
-  int stack[64];
-  int sp = 0;
-  int cur = 0;
-  for (;;) {
-    if (n && !index_ok(cur >= 0 && cur < nint, err, SITE_NODE, static_cast<uint32_t>(cur), n)) break;
-    const float4 na = __ldg(&nodes[cur].a);
-    const float4 nb = __ldg(&nodes[cur].b);
-    const float4 nc = __ldg(&nodes[cur].c);
-    const int4 nd = __ldg(&nodes[cur].d);
-    float te, tx;
-    slab(o, inv, na.x, na.y, na.z, na.w, nb.x, nb.y, te, tx);
-    bool hl = tx >= te && tx >= 0.0f && te <= tlim;
-    slab(o, inv, nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, te, tx);
-    bool hr = tx >= te && tx >= 0.0f && te <= tlim && nd.y != INT32_MIN;
-    if (hl && nd.x < 0) {
-      const uint32_t s = static_cast<uint32_t>(~nd.x);
-      if (!n || index_ok(s < n, err, SITE_LEAF, s, n)) fn(s);
-      hl = false;
-    }
-    if (hr && nd.y < 0) {
-      const uint32_t s = static_cast<uint32_t>(~nd.y);
-      if (!n || index_ok(s < n, err, SITE_LEAF, s, n)) fn(s);
-      hr = false;
-    }
-    if (hl && hr) {
-      if (sp < 64) {
-        stack[sp++] = nd.y;
-      } else {
-        atomicOr(err, ERR_STACK_OVERFLOW);
-      }
-      cur = nd.x;
-    } else if (hl) {
-      cur = nd.x;
-    } else if (hr) {
-      cur = nd.y;
-    } else {
-      if (sp == 0) break;
-      cur = stack[--sp];
-    }
-  }
-}
-
-// The deferred walk over the four-wide tree: a hit child becomes the next node (the first one) or
-// goes on the stack; a leaf taken from the stack (or as the next node) is held until every lane of
-// `amask` holds one or has finished, then the lanes test one leaf each together.  The leaves tested
-// are those of walk_lbvh on the binary tree.  With amask = the lane's own bit it is a plain walk.
-template <class F>
-__device__ __forceinline__ void walk_bvh4_deferred(const Node4* __restrict__ nodes, float3 o, float3 inv, float tlim,
-                                                   uint32_t* err, F&& fn, uint32_t n, unsigned amask) {
-  const int nint = n > 1 ? static_cast<int>(n - 1) : 1;
+__device__ __forceinline__ void rt_walk_deferred(const Node* __restrict__ nodes, float3 o, float3 inv, float tlim,
+                                                 uint32_t* err, F&& fn, uint32_t nmax, unsigned amask) {
   constexpr int EMPTY = INT32_MIN;
   constexpr uint32_t NONE = 0xffffffffu;
-  int stack[64];
+  int stack[RT_MAX_DEPTH + 1];
   int sp = 0;
-  int cur = n ? 0 : EMPTY;
-  // lv[0] is the pending leaf, the others were found speculatively (registers: every index below
-  // is a constant after unrolling).
+  int cur = 0;  // the super-root
   uint32_t lv[WALK_LEAVES];
 #pragma unroll
   for (int j = 0; j < WALK_LEAVES; ++j) lv[j] = NONE;
   const float3 oi = make_float3(o.x * inv.x, o.y * inv.y, o.z * inv.z);
   for (;;) {
     for (;;) {
-      // Visit while some lane still has no leaf; a lane that holds one goes on walking until it
-      // holds WALK_LEAVES (speculative traversal) instead of idling.
       const bool need = cur != EMPTY && lv[0] == NONE;
       if (!__any_sync(amask, need)) break;
       const bool want = cur != EMPTY && lv[WALK_LEAVES - 1] == NONE;
@@ -119,43 +71,42 @@ __device__ __forceinline__ void walk_bvh4_deferred(const Node4* __restrict__ nod
         cur = sp > 0 ? stack[--sp] : EMPTY;
         continue;
       }
-      if (!index_ok(cur < nint, err, SITE_NODE, static_cast<uint32_t>(cur), n)) {
+      if (!index_ok(static_cast<uint32_t>(cur) < nmax, err, SITE_NODE, static_cast<uint32_t>(cur), nmax)) {
         cur = EMPTY;
         continue;
       }
-      const Node4* nd = nodes + cur;
-      const float4 lx = __ldg(&nd->lox), ly = __ldg(&nd->loy), lz = __ldg(&nd->loz);
-      const float4 hx = __ldg(&nd->hix), hy = __ldg(&nd->hiy), hz = __ldg(&nd->hiz);
-      const int4 rf = __ldg(&nd->ref);
-      int next = EMPTY;
-      // Slab test as lo * inv - o * inv (one FMA per plane).  Its rounding differs from the exact
-      // walk's (lo - o) * inv by about |o| * 2^-24 in box units, far inside the leaf padding, so
-      // every crystal the ray meets is still reached; the crystal test itself is unchanged.
-      auto child = [&](float a0, float a1, float a2, float a3, float a4, float a5, int r) {
+      const Node* nd = nodes + cur;
+      const float4 na = __ldg(&nd->a), nb = __ldg(&nd->b), nc = __ldg(&nd->c);
+      const int4 rf = __ldg(&nd->d);
+      // Slab test as lo * inv - o * inv (one FMA per plane), clipped to [0, tlim].
+      auto hit = [&](float a0, float a1, float a2, float a3, float a4, float a5) {
         const float t1x = fmaf(a0, inv.x, -oi.x), t2x = fmaf(a3, inv.x, -oi.x);
         const float t1y = fmaf(a1, inv.y, -oi.y), t2y = fmaf(a4, inv.y, -oi.y);
         const float t1z = fmaf(a2, inv.z, -oi.z), t2z = fmaf(a5, inv.z, -oi.z);
         const float te = fmaxf(fmaxf(fminf(t1x, t2x), fminf(t1y, t2y)), fmaxf(fminf(t1z, t2z), 0.0f));
         const float tx = fminf(fminf(fmaxf(t1x, t2x), fmaxf(t1y, t2y)), fminf(fmaxf(t1z, t2z), tlim));
-        if (r != EMPTY && te <= tx) {
-          if (next == EMPTY) {
-            next = r;
-          } else if (sp < 64) {
-            stack[sp++] = r;
+        return te <= tx;
+      };
+      const bool hl = rf.x != EMPTY && hit(na.x, na.y, na.z, na.w, nb.x, nb.y);
+      const bool hr = rf.y != EMPTY && hit(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w);
+      if (hr) {
+        if (hl) {
+          if (sp <= RT_MAX_DEPTH) {
+            stack[sp++] = rf.x;
           } else {
             atomicOr(err, ERR_STACK_OVERFLOW);
           }
         }
-      };
-      child(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, rf.x);
-      child(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, rf.y);
-      child(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, rf.z);
-      child(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, rf.w);
-      cur = next != EMPTY ? next : (sp > 0 ? stack[--sp] : EMPTY);
+        cur = rf.y;
+      } else if (hl) {
+        cur = rf.x;
+      } else {
+        cur = sp > 0 ? stack[--sp] : EMPTY;
+      }
     }
     if (!__any_sync(amask, lv[0] != NONE)) break;
     if (lv[0] != NONE) {
-      if (index_ok(lv[0] < n, err, SITE_LEAF, lv[0], n)) fn(lv[0]);
+      if (index_ok(lv[0] < nmax, err, SITE_LEAF, lv[0], nmax)) fn(lv[0]);
 #pragma unroll
       for (int j = 0; j + 1 < WALK_LEAVES; ++j) lv[j] = lv[j + 1];
       lv[WALK_LEAVES - 1] = NONE;
@@ -231,22 +182,13 @@ __device__ __forceinline__ bool emit_photon(const TileDesc& t, uint32_t id, Phot
   return true;
 }
 
-struct HitS {
-  float t0, t1;
-  uint32_t s;
-};
-
-// Canonical hit order (t_enter, crystal index); the index is the crystal id, which for crystal
-// sets without an id map is the Morton slot itself.
-__device__ __forceinline__ bool hit_before(const TileDesc& t, float ta, uint32_t sa, float tb, uint32_t sb) {
-  if (ta != tb) return ta < tb;
-  const uint32_t ia = t.s2id ? __ldg(&t.s2id[sa]) : sa, ib = t.s2id ? __ldg(&t.s2id[sb]) : sb;
-  return ia < ib;
-}
-
-// One bounce (transport.rs:101-185).  Returns whether the packet is still alive.
-__device__ __forceinline__ bool photon_bounce(const TileDesc& t, Photon& ph, HitS* hits, uint32_t* err,
-                                              uint32_t& nhit, unsigned amask = 0) {
+// One bounce (transport.rs:101-185).  Returns whether the packet is still alive.  The crystals of
+// every leaf the walk reaches are tested by their geometry (crystal.rs:140-217) in the reference's
+// order, and each hit inside the step is absorbed at once (transport.rs:108-138): Beer-Lambert,
+// Bernoulli rounding of 5 E p s latent photons, E *= max(1 - 0.9 p, 0.05); the n-th absorbing hit
+// of the bounce draws word n % 4 of Philox block n / 4.
+__device__ __forceinline__ bool photon_bounce(const TileDesc& t, Photon& ph, uint32_t* err, uint32_t& nhit,
+                                              unsigned amask = 0) {
   const float PI2 = 6.283185307179586f;
   nhit = 0;
   if (ph.b >= t.max_bounces) return false;
@@ -256,36 +198,35 @@ __device__ __forceinline__ bool photon_bounce(const TileDesc& t, Photon& ph, Hit
   const float step = fminf(fp, t.D * 1.5f);
   const float3 pos = ph.pos, dir = ph.dir;
   const float3 inv = make_float3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
-  int nh = 0;
-  auto leaf = [&](uint32_t s) {
+  float E = ph.E;
+  uint32_t nh = 0;
+  P4 r{};
+  auto leaf = [&](uint32_t id) {
+    const uint2 L = __ldg(&t.rleaf[id]);
+    if (!index_ok(L.x + L.y <= t.n, err, SITE_LEAF, L.x, L.y)) return;
+    for (uint32_t k = 0; k < L.y; ++k) {
+      const uint32_t s = __ldg(&t.ridx[L.x + k]);
+      if (!index_ok(s < t.n, err, SITE_LEAF, s, t.n)) continue;
       const float4 a = __ldg(&t.a[s]), q = __ldg(&t.q[s]), d = __ldg(&t.d[s]);
       float t0, t1;
-      if (!fcanonical_hit(a, q, d, 1.0f, pos, dir, inv, t0, t1)) return;
-      if (!(t0 < step)) return;
-      if (!(fmaxf(fminf(t1, step) - t0, 0.0f) > 0.0f)) return;
-      if (nh == HMAX) { atomicOr(err, ERR_HIT_OVERFLOW); return; }
-      int j = nh++;
-      while (j > 0 && hit_before(t, t0, s, hits[j - 1].t0, hits[j - 1].s)) {
-        hits[j] = hits[j - 1];
-        --j;
-      }
-      hits[j] = HitS{t0, t1, s};
+      if (!fintersect(a, q, d, 1.0f, pos, dir, t0, t1)) continue;
+      if (!(t0 < step)) continue;
+      const float path = fmaxf(fminf(t1, step) - t0, 0.0f);
+      if (!(path > 0.0f)) continue;
+      if ((nh & 3) == 0) r = philox(ph.id, b, nh >> 2, TAG_HIT, t.k0, t.k1);
+      // 1 - exp(-alpha L) without the cancellation of a short chord (corner hits are common).
+      const float p = -expm1f(-t.alpha * path);
+      const float expected = E * p * a.w * 5.0f;
+      const float fl = floorf(expected);
+      const uint32_t cnt = static_cast<uint32_t>(fl) + (uf(word(r, nh & 3)) < expected - fl ? 1u : 0u);
+      if (cnt) add_counts(t.counts, s, cnt);
+      E *= fmaxf(1.0f - p * 0.9f, 0.05f);
+      ++nh;
+    }
   };
-  walk_bvh4_deferred(t.nodes4, pos, inv, step * 1.00001f + 1e-3f, err, leaf, t.n,
-                     amask ? amask : (1u << (threadIdx.x & 31)));
-  float E = ph.E;
-  P4 r{};
-  for (int h = 0; h < nh; ++h) {
-    if ((h & 3) == 0) r = philox(ph.id, b, static_cast<uint32_t>(h) >> 2, TAG_HIT, t.k0, t.k1);
-    const float path = fmaxf(fminf(hits[h].t1, step) - hits[h].t0, 0.0f);
-    const float p = 1.0f - __expf(-t.alpha * path);
-    const float expected = E * p * __ldg(&t.a[hits[h].s].w) * 5.0f;
-    const float fl = floorf(expected);
-    const uint32_t cnt = static_cast<uint32_t>(fl) + (uf(word(r, h & 3)) < expected - fl ? 1u : 0u);
-    if (cnt) add_counts(t.counts, hits[h].s, cnt);
-    E *= fmaxf(1.0f - p * 0.9f, 0.05f);
-  }
-  nhit = static_cast<uint32_t>(nh);
+  rt_walk_deferred(t.rnode, pos, inv, step * 1.00001f + 1e-3f, err, leaf, t.nnodes,
+                   amask ? amask : (1u << (threadIdx.x & 31)));
+  nhit = nh;
   const float3 np = make_float3(pos.x + dir.x * step, pos.y + dir.y * step, pos.z + dir.z * step);
   if (np.x < 0.0f || np.x >= t.W || np.y < 0.0f || np.y >= t.H) return false;
   if (np.z <= 0.0f) return false;

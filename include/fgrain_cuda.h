@@ -320,6 +320,15 @@ fg_status fg_replay_segments(fg_engine* e, fg_emulsion* em, const fg_exposure_cf
 fg_status fg_replay_rays(fg_engine* e, const fg_emulsion* em, const double* origins,
                          const double* dirs, size_t nrays, int developed_only, uint32_t* offsets,
                          uint32_t* ids, size_t id_cap, size_t* nhits, double* chord_sum);
+/* The device's copy of the reference tree (BVH::build, bvh.rs:157-295) over the emulsion's crystals
+ * (developed_only = 0: the transport's tree) or over its developed crystals with their expansion
+ * (developed_only = 1: the scan's tree, transmittance.rs:86-89).  order receives the crystal ids in
+ * the tree's final index order (BVH::indices), leaves 2 words per leaf (first index, count) sorted
+ * by first index, leaf_boxes 6 doubles per leaf (lo xyz, hi xyz); at most cap entries each (any
+ * may be NULL).  *nelem and *nleaves receive the totals. */
+fg_status fg_emulsion_reference_tree(fg_engine* e, const fg_emulsion* em, int developed_only, uint32_t* order,
+                                     uint32_t* leaves, double* leaf_boxes, size_t cap, size_t* nelem,
+                                     size_t* nleaves);
 /* Per-ray hit counts of the production scan kernel (pixel-major, stratum-minor). */
 fg_status fg_scan_ray_hits(fg_engine* e, const fg_emulsion* em, const fg_scan_cfg* cfg,
                            uint64_t seed, uint16_t* ray_hits);
@@ -440,9 +449,11 @@ fg_status fg_render_tile_fast(fg_engine* e, const float* tile, const fg_tile_par
  * already holds in device memory.  It calls no cudaMalloc, cudaFree or allocating library
  * routine; its scratch is one file-scope device array of FG_STATIC_SCAN_SCRATCH_BYTES that every
  * GPU loading this library holds until the process exits, shared by all calls on that device. */
-#define FG_STATIC_SCAN_MAX_BINS 16384u     /* scan bins (bin_px x bin_px pixels each) per call */
-#define FG_STATIC_SCAN_MAX_ITEMS 1048576u  /* (developed crystal, bin) entries per call */
-#define FG_STATIC_SCAN_SCRATCH_BYTES 4392192u
+#define FG_STATIC_SCAN_MAX_CRYSTALS 1048576u /* crystals per call */
+#define FG_STATIC_SCAN_MAX_DEVELOPED 32768u  /* developed crystals per call */
+#define FG_STATIC_SCAN_MAX_BINS 16384u       /* scan bins (bin_px x bin_px pixels each) per call */
+#define FG_STATIC_SCAN_MAX_ITEMS 1048576u    /* (developed crystal, bin) entries per call */
+#define FG_STATIC_SCAN_SCRATCH_BYTES 17153792u
 
 /* A crystal set in device memory, in crystal-index order (any order gives the same image). */
 typedef struct fg_device_crystals {
@@ -460,9 +471,10 @@ typedef struct fg_device_crystals {
 /* Scans `crystals` like fg_scan_emulsion over a film of film->width x film->height x film->depth
  * um (the other fields of film are ignored).  out (width*height floats) and image8 (width*height
  * bytes, may be NULL) are device pointers; work runs on `stream` (a cudaStream_t; NULL is the
- * legacy default stream) and the call returns when it has finished.  Requests needing more than
- * FG_STATIC_SCAN_MAX_BINS bins or FG_STATIC_SCAN_MAX_ITEMS entries fail with FG_ERR_INVALID_ARG
- * before any output is written.  On failure a message is copied to `message` (message_len bytes,
+ * legacy default stream) and the call returns when it has finished.  Requests with more than
+ * FG_STATIC_SCAN_MAX_CRYSTALS crystals or FG_STATIC_SCAN_MAX_DEVELOPED developed ones, or needing
+ * more than FG_STATIC_SCAN_MAX_BINS bins or FG_STATIC_SCAN_MAX_ITEMS entries, fail with
+ * FG_ERR_INVALID_ARG before any output is written.  On failure a message is copied to `message` (message_len bytes,
  * may be NULL).  The first call on a device looks up the scratch's device address
  * (cudaGetSymbolAddress); make that first call before any stream capture.  Every call on a device
  * shares the scratch, which keeps the last call's contents; each call clears what must start at

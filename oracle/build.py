@@ -1,6 +1,6 @@
 """Builds the CPU oracle (TEST INFRASTRUCTURE) into oracle/build/liboracle.so.
 
-g++ with OpenMP; -ffp-contract=off keeps every double operation individually rounded (GCC on
+g++ -O3 with OpenMP; -ffp-contract=off keeps every double operation individually rounded (GCC on
 aarch64 would otherwise fuse multiply-adds), so the oracle rounds exactly like the reference's
 Rust code and like the device's FP64 predicates.
 """
@@ -20,7 +20,7 @@ def build(force: bool = False) -> Path:
     deps = srcs + [HERE / "fg_oracle.h", HERE / "philox.h"]
     if not force and OUT.exists() and all(d.stat().st_mtime <= OUT.stat().st_mtime for d in deps):
         return OUT
-    cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
+    cmd = ["g++", "-O3", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
            "-fPIC", "-shared", *map(str, srcs), "-o", str(OUT)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -505,6 +505,40 @@ int or_bvh_stats(const or_crystals* c, int64_t* nodes, int64_t* depth) {
   return 0;
 }
 
+// The reference tree over all crystals, or over the developed ones only (the scan's tree,
+// transmittance.rs:86-89): the final index order (crystal indices), and per leaf in node order its
+// range in that order and its box.  Returns the number of elements.
+int64_t or_bvh_export(const or_crystals* c, int developed_only, uint32_t* order, int64_t cap,
+                      uint32_t* leaf_start, uint32_t* leaf_count, double* leaf_box, int64_t leaf_cap,
+                      int64_t* nleaves) {
+  std::vector<Crystal> cs;
+  std::vector<size_t> orig;
+  for (size_t i = 0; i < c->n; ++i) {
+    Crystal k = load_crystal(c, i);
+    if (developed_only && !k.developed) continue;
+    if (!developed_only) k.developed = false;
+    cs.push_back(k);
+    orig.push_back(i);
+  }
+  RefBvh bvh;
+  bvh.build(cs);
+  for (size_t k = 0; k < bvh.indices.size() && static_cast<int64_t>(k) < cap; ++k)
+    order[k] = static_cast<uint32_t>(orig[bvh.indices[k]]);
+  int64_t nl = 0;
+  for (const auto& n : bvh.nodes) {
+    if (n.count == 0) continue;
+    if (nl < leaf_cap) {
+      leaf_start[nl] = n.offset;
+      leaf_count[nl] = n.count;
+      const double b[6] = {n.box.lo.x, n.box.lo.y, n.box.lo.z, n.box.hi.x, n.box.hi.y, n.box.hi.z};
+      for (int j = 0; j < 6; ++j) leaf_box[6 * nl + j] = b[j];
+    }
+    ++nl;
+  }
+  *nleaves = nl;
+  return static_cast<int64_t>(cs.size());
+}
+
 double or_free_path(const or_optics* o, double xi) { return Optics{*o}.free_path(xi); }
 
 int or_antihalation(const or_optics* o, double* energy, double dir[3], const double u[4]) {
@@ -807,7 +841,7 @@ int64_t or_expose(or_crystals* c, const or_emulsion_cfg* cfg, const float* tile,
 }
 
 int64_t or_replay_segments(or_crystals* c, const or_exposure_cfg* ecfg, uint64_t seed,
-                           const or_segment* segs, int64_t nseg, uint32_t* offsets,
+                           const or_segment* segs, int64_t nseg, int mode, uint32_t* offsets,
                            uint32_t* ids, int64_t id_cap) {
   const std::vector<Crystal> cs = load_all(c);
   RefBvh bvh;
@@ -819,7 +853,7 @@ int64_t or_replay_segments(or_crystals* c, const or_exposure_cfg* ecfg, uint64_t
     const or_segment& g = segs[s];
     const V3 o = v3(g.origin[0], g.origin[1], g.origin[2]);
     const V3 d = v3(g.dir[0], g.dir[1], g.dir[2]);
-    ray_hits(bvh, cs, o, d, OR_CANONICAL, hits);
+    ray_hits(bvh, cs, o, d, mode, hits);
     if (offsets) offsets[s] = static_cast<uint32_t>(total);
     double E = g.energy;
     uint32_t ordinal = 0;

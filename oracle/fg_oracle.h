@@ -130,6 +130,12 @@ int64_t or_query_radius(const or_crystals* c, const double center[3], double rad
                         uint32_t* out, int64_t cap);
 /* Statistics of the reference BVH over the set: node count, depth, and stack drops. */
 int or_bvh_stats(const or_crystals* c, int64_t* nodes, int64_t* depth);
+/* The reference tree (bvh.rs:157-295) over all crystals, or over the developed ones with their
+ * expansion (the scan's tree): final index order (crystal indices) and the leaves in node order
+ * (range in that order, box lo xyz hi xyz).  Returns the element count. */
+int64_t or_bvh_export(const or_crystals* c, int developed_only, uint32_t* order, int64_t cap,
+                      uint32_t* leaf_start, uint32_t* leaf_count, double* leaf_box, int64_t leaf_cap,
+                      int64_t* nleaves);
 
 /* GelatinOptics::sample_free_path (optics.rs:100-107) for one uniform xi. */
 double or_free_path(const or_optics* o, double xi);
@@ -158,10 +164,12 @@ int64_t or_expose(or_crystals* c, const or_emulsion_cfg* cfg, const float* tile,
                   int threads, or_segment* seg_out, int64_t seg_cap, int64_t* seg_n,
                   uint64_t* hits_out);
 
-/* Replays recorded segments with the per-hit arithmetic of expose (canonical hits only);
- * counts are added to c->latent; hit lists are written CSR-style when offsets != NULL. */
+/* Replays recorded segments with the per-hit arithmetic of expose under hit rule `mode`
+ * (OR_FAITHFUL: the reference's BVH walk and traversal order; OR_CANONICAL: own-box rule, sorted
+ * by (t_enter, index)); counts are added to c->latent; hit lists (in absorption order) are written
+ * CSR-style when offsets != NULL. */
 int64_t or_replay_segments(or_crystals* c, const or_exposure_cfg* ecfg, uint64_t seed,
-                           const or_segment* segs, int64_t nseg, uint32_t* offsets,
+                           const or_segment* segs, int64_t nseg, int mode, uint32_t* offsets,
                            uint32_t* ids, int64_t id_cap);
 
 /* develop_emulsion (development.rs:59-188): fills developed / clump / expansion. */

@@ -108,8 +108,9 @@ float or_film_base_nominal(const char* preset) {
 }
 
 int or_luma(const uint8_t* rgb, uint32_t w, uint32_t h, const float wts[3], uint8_t* out) {
-  const size_t n = static_cast<size_t>(w) * h;
-  for (size_t i = 0; i < n; ++i) {
+  const int64_t n = static_cast<int64_t>(w) * h;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
     const float r = rgb[3 * i], g = rgb[3 * i + 1], b = rgb[3 * i + 2];
     float v = r * wts[0] + g * wts[1] + b * wts[2];
     v = v < 0.0f ? 0.0f : (v > 255.0f ? 255.0f : v);
@@ -129,6 +130,8 @@ int or_resize_u8(const uint8_t* in, uint32_t w, uint32_t h, uint32_t ow, uint32_
   std::vector<std::vector<float>> wt;
   resample_axis(h, oh, filter, left, wt);
   std::vector<float> tmp(static_cast<size_t>(w) * oh);
+  // Rows are independent: OpenMP splits them, each pixel keeps its sequential tap order.
+#pragma omp parallel for schedule(static)
   for (uint32_t y = 0; y < oh; ++y)
     for (uint32_t x = 0; x < w; ++x) {
       float t = 0.0f;
@@ -137,6 +140,7 @@ int or_resize_u8(const uint8_t* in, uint32_t w, uint32_t h, uint32_t ow, uint32_
       tmp[static_cast<size_t>(y) * w + x] = t;
     }
   resample_axis(w, ow, filter, left, wt);
+#pragma omp parallel for schedule(static)
   for (uint32_t y = 0; y < oh; ++y)
     for (uint32_t x = 0; x < ow; ++x) {
       float t = 0.0f;
@@ -185,6 +189,7 @@ int or_gelatin_psf(const uint8_t* src, uint32_t w, uint32_t h, float* heff, uint
   const float wn[3] = {0.15f, 0.70f, 0.15f};
   const float ww[7] = {0.03f, 0.12f, 0.20f, 0.30f, 0.20f, 0.12f, 0.03f};
   auto pass = [&](const std::vector<float>& in, std::vector<float>& out, const float* k, int rad, int axis) {
+#pragma omp parallel for schedule(static)
     for (uint32_t y = top; y < bottom; ++y)
       for (uint32_t x = left; x < right; ++x) {
         float sum = 0.0f, ws = 0.0f;
@@ -212,6 +217,7 @@ int or_gelatin_psf(const uint8_t* src, uint32_t w, uint32_t h, float* heff, uint
   pass(lin, tw, ww, 3, 0);
   pass(tw, ow, ww, 3, 1);
   for (size_t i = 0; i < n; ++i) heff[i] = 0.0f;
+#pragma omp parallel for schedule(static)
   for (uint32_t y = top; y < bottom; ++y)
     for (uint32_t x = left; x < right; ++x) {
       const size_t i = static_cast<size_t>(y) * w + x;

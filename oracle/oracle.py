@@ -168,7 +168,7 @@ def intersect_crystal(pos, dims, quat, morph, expansion, origin, direction):
     return (t0.value, t1.value) if hit else None
 
 
-def ray_hits(cr: Crystals, origin, direction, mode=CANONICAL):
+def ray_hits(cr: Crystals, origin, direction, mode=FAITHFUL):
     L = lib()
     L.or_ray_hits.restype = C.c_int64
     cap = len(cr) + 1
@@ -197,7 +197,7 @@ def antihalation(optics, energy, direction, u):
     return bool(alive), E.value, list(d)
 
 
-def rays_hits(cr: Crystals, origins, dirs, mode=CANONICAL, developed_only=False):
+def rays_hits(cr: Crystals, origins, dirs, mode=FAITHFUL, developed_only=False):
     """Hit lists of many rays: (offsets, ids, chord sums)."""
     o = np.ascontiguousarray(origins, np.float64).reshape(-1, 3)
     d = np.ascontiguousarray(dirs, np.float64).reshape(-1, 3)
@@ -232,6 +232,24 @@ def bvh_stats(cr: Crystals):
     return nodes.value, depth.value
 
 
+def bvh_export(cr: Crystals, developed_only=False):
+    """The reference tree: (final order of crystal indices, leaves as (start, count) rows, leaf boxes
+    (lo xyz, hi xyz) rows), leaves in node order."""
+    L = lib()
+    L.or_bvh_export.restype = C.c_int64
+    n = len(cr)
+    order = np.zeros(max(n, 1), np.uint32)
+    ls = np.zeros(max(n, 1), np.uint32)
+    lc = np.zeros(max(n, 1), np.uint32)
+    lb = np.zeros((max(n, 1), 6))
+    nl = C.c_int64()
+    s = cr.struct()
+    m = L.or_bvh_export(C.byref(s), int(developed_only), _p(order, C.c_uint32), C.c_int64(n), _p(ls, C.c_uint32),
+                        _p(lc, C.c_uint32), _p(lb, C.c_double), C.c_int64(n), C.byref(nl))
+    k = nl.value
+    return order[:m].copy(), np.column_stack([ls[:k], lc[:k]]), lb[:k].copy()
+
+
 def sample_poisson(bounds, r_min, k, seed):
     L = lib()
     L.or_sample_poisson.restype = C.c_int64
@@ -262,7 +280,7 @@ def synthesize(cfg, seed) -> Crystals:
     return out
 
 
-def expose(cr: Crystals, cfg, tile, ecfg, seed, mode=CANONICAL, threads=0, record=False):
+def expose(cr: Crystals, cfg, tile, ecfg, seed, mode=FAITHFUL, threads=0, record=False):
     """Adds counts into cr.latent; returns (photons, segments or None, absorbing hits)."""
     L = lib()
     L.or_expose.restype = C.c_int64
@@ -289,19 +307,72 @@ def expose(cr: Crystals, cfg, tile, ecfg, seed, mode=CANONICAL, threads=0, recor
     return P, segs, hits.value
 
 
-def replay_segments(cr: Crystals, ecfg, seed, segs):
+def replay_segments(cr: Crystals, ecfg, seed, segs, mode=FAITHFUL):
+    """Replays recorded segments under hit rule `mode`; returns CSR (offsets, crystal ids) in
+    absorption order and adds the latent counts to cr.latent."""
     L = lib()
     L.or_replay_segments.restype = C.c_int64
     segs = np.ascontiguousarray(segs, SEGMENT_DTYPE)
     offsets = np.zeros(len(segs) + 1, np.uint32)
-    cap = max(len(segs) * 64, 1)
-    ids = np.zeros(cap, np.uint32)
     xc = exposure_cfg(ecfg)
     s = cr.struct()
+    saved = cr.latent.copy()
     n = L.or_replay_segments(C.byref(s), C.byref(xc), C.c_uint64(seed), segs.ctypes.data_as(C.c_void_p),
-                             C.c_int64(len(segs)), _p(offsets, C.c_uint32), _p(ids, C.c_uint32),
-                             C.c_int64(cap))
+                             C.c_int64(len(segs)), mode, _p(offsets, C.c_uint32), None, C.c_int64(0))
+    cr.latent[:] = saved
+    ids = np.zeros(max(n, 1), np.uint32)
+    s = cr.struct()
+    L.or_replay_segments(C.byref(s), C.byref(xc), C.c_uint64(seed), segs.ctypes.data_as(C.c_void_p),
+                         C.c_int64(len(segs)), mode, _p(offsets, C.c_uint32), _p(ids, C.c_uint32), C.c_int64(n))
     return offsets, ids[:n].copy()
+
+
+def hit_rule_difference(cr: Crystals, cfg, tile, ecfg, seed, threads=0):
+    """How far the canonical hit rule is from the reference's own (FAITHFUL) on one exposure.
+
+    The photon segments of a faithful exposure are replayed under both rules.  Returns the share of
+    segments whose hit sets differ, the share of segments whose absorption order differs (same set),
+    the relative difference of the total hit count, and, from two full exposures with the same seed,
+    the share of crystals whose latent counts differ and the relative difference of the total
+    latent photons."""
+    c0 = cr.copy()
+    c0.latent[:] = 0
+    _, segs, _ = expose(c0, cfg, tile, ecfg, seed, FAITHFUL, threads, record=True)
+    fa, ca = c0.copy(), c0.copy()
+    fa.latent[:] = 0
+    ca.latent[:] = 0
+    of, idf = replay_segments(fa, ecfg, seed, segs, FAITHFUL)
+    oc, idc = replay_segments(ca, ecfg, seed, segs, CANONICAL)
+    nseg = len(segs)
+    set_diff = order_diff = not_subset = 0
+    for k in range(nseg):
+        a = idf[of[k]:of[k + 1]]
+        b = idc[oc[k]:oc[k + 1]]
+        if len(a) != len(b) or not np.array_equal(np.sort(a), np.sort(b)):
+            set_diff += 1
+            if not np.isin(b, a).all():
+                not_subset += 1
+        elif not np.array_equal(a, b):
+            order_diff += 1
+    e_f, e_c = cr.copy(), cr.copy()
+    e_f.latent[:] = 0
+    e_c.latent[:] = 0
+    expose(e_f, cfg, tile, ecfg, seed, FAITHFUL, threads)
+    expose(e_c, cfg, tile, ecfg, seed, CANONICAL, threads)
+    touched = (e_f.latent > 0) | (e_c.latent > 0)
+    return {
+        "segments": nseg,
+        "segments_hit_set_differs": set_diff / max(nseg, 1),
+        "segments_order_differs": order_diff / max(nseg, 1),
+        "segments_canonical_not_subset": not_subset,
+        "hits_faithful": int(len(idf)), "hits_canonical": int(len(idc)),
+        "hits_rel_diff": (len(idf) - len(idc)) / max(len(idc), 1),
+        "crystals": len(cr),
+        "crystals_count_differs": float((e_f.latent != e_c.latent).mean()),
+        "touched_crystals_count_differs": float((e_f.latent != e_c.latent)[touched].mean()) if touched.any() else 0.0,
+        "latent_rel_diff": float(e_f.latent.sum(dtype=np.int64) - e_c.latent.sum(dtype=np.int64))
+        / max(float(e_c.latent.sum(dtype=np.int64)), 1.0),
+    }
 
 
 def develop(cr: Crystals, dcfg):
@@ -312,7 +383,7 @@ def develop(cr: Crystals, dcfg):
     return {k: getattr(rep, k) for k, _ in rep._fields_}
 
 
-def scan(cr: Crystals, cfg, scfg, seed, mode=CANONICAL, threads=0, sigma_c=None, want_hits=False):
+def scan(cr: Crystals, cfg, scfg, seed, mode=FAITHFUL, threads=0, sigma_c=None, want_hits=False):
     """Returns dict(out, image8, T64[, ray_hits])."""
     sc = scan_cfg(scfg)
     ec = emulsion_cfg(cfg)
@@ -345,7 +416,7 @@ def otf_taps(s):
 
 
 def scan_signal(cr: Crystals, cfg, scfg, seed, sigma_c=None, exposure=1.0, otf_sigma=OTF_SIGMA_REFERENCE,
-                mode=CANONICAL, threads=0):
+                mode=FAITHFUL, threads=0):
     """Differentiable scan S = OTF_s(e T) in FP64; returns (S, T)."""
     sc = scan_cfg(scfg)
     ec = emulsion_cfg(cfg)
@@ -359,7 +430,7 @@ def scan_signal(cr: Crystals, cfg, scfg, seed, sigma_c=None, exposure=1.0, otf_s
 
 
 def scan_backward(cr: Crystals, cfg, scfg, seed, dL_dS, sigma_c=None, exposure=1.0,
-                  otf_sigma=OTF_SIGMA_REFERENCE, mode=CANONICAL, threads=0):
+                  otf_sigma=OTF_SIGMA_REFERENCE, mode=FAITHFUL, threads=0):
     """FP64 adjoint of scan_signal: (dL/dsigma per crystal, dL/dexposure, dL/dotf_sigma)."""
     sc = scan_cfg(scfg)
     ec = emulsion_cfg(cfg)
@@ -385,7 +456,7 @@ def scan_ray_origins(cfg, scfg, seed):
     return o
 
 
-def render_tile(preset, pixel_size_um, tile, exposure, push, tile_seed, mode=CANONICAL, threads=0):
+def render_tile(preset, pixel_size_um, tile, exposure, push, tile_seed, mode=FAITHFUL, threads=0):
     tile = np.ascontiguousarray(tile, np.float32)
     th, tw = tile.shape
     d = np.zeros((th, tw), np.float32)
@@ -511,6 +582,11 @@ def film_grid(out_w, out_h, grain_px, tile_size):
     return tiles, step, pad
 
 
+def film_tile_seed(seed, t):
+    """Seed of tile t (image_pipeline.rs:430-434), wrapping at 64 bits."""
+    return (seed + t.idx * 73856093 + t.tx * 19349663 + t.ty * 83492791) & 0xFFFFFFFFFFFFFFFF
+
+
 def film_scaling(opts, out_w, out_h):
     """(grain_size_px, effective_strength, effective_push) of image_pipeline.rs:347-375."""
     user = opts["scale"] if opts["scale"] > 0 else 1.0
@@ -571,7 +647,7 @@ def film_render_bw(image, threads=0, **kw):
     stock = _oracle_stock(opts["preset"], push)
     dens = []
     for t in grid:
-        seed = (opts["seed"] + t.idx * 73856093 + t.tx * 19349663 + t.ty * 83492791) & 0xFFFFFFFFFFFFFFFF
+        seed = film_tile_seed(opts["seed"], t)
         tile = np.ascontiguousarray(heff[t.y_start:t.y_start + t.th, t.x_start:t.x_start + t.tw])
         d, _ = render_tile(stock, 1.0 / grain, tile, opts["exposure"], opts["push"], seed, FAITHFUL, threads)
         dens.append(d)

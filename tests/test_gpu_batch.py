@@ -111,7 +111,7 @@ def test_pipeline_matches_oracle_on_the_same_crystals(engine):
     rd = orc.develop(crd, fg.DevelopmentConfig(4, p.filament_expansion, p.clumping_proximity_factor, 0.85))
     assert st["developed"] == int(c["developed"].sum()) == rd["developed_crystals"] > 100
     assert st["clumps"] == rd["total_clumps"]
-    orc.expose(cr, cfg, tile, fg.ExposureConfig(6.0, 0.12, 1.3, 48), p.seed + 1, orc.CANONICAL)
+    orc.expose(cr, cfg, tile, fg.ExposureConfig(6.0, 0.12, 1.3, 48), p.seed + 1, orc.FAITHFUL)
     same = (cr.latent == c["counts"]).mean()
     assert same > 0.99, same
     orc.develop(cr, fg.DevelopmentConfig(4, p.filament_expansion, p.clumping_proximity_factor, 0.85))
@@ -141,7 +141,7 @@ def test_statistical_parity_with_oracle_renders(engine):
     b.run()
     b.wait()
     for d_dev, s in zip(b.density(), seeds):
-        d_orc, _ = orc.render_tile("tri-x", px, flat, 1.0, 0.0, s, orc.CANONICAL)
+        d_orc, _ = orc.render_tile("tri-x", px, flat, 1.0, 0.0, s, orc.FAITHFUL)
         dev.append(d_dev)
         orcs.append(d_orc)
     dev, orcs = np.array(dev, np.float64), np.array(orcs, np.float64)
@@ -174,7 +174,7 @@ def test_grain_noise_power_spectrum_matches_oracle(engine):
     b.run()
     b.wait()
     dev = np.array([radial_psd_bands(d.astype(np.float64)) for d in b.density()])
-    orcs = np.array([radial_psd_bands(orc.render_tile("tri-x", px, flat, 1.0, 0.0, s, orc.CANONICAL)[0]
+    orcs = np.array([radial_psd_bands(orc.render_tile("tri-x", px, flat, 1.0, 0.0, s, orc.FAITHFUL)[0]
                                       .astype(np.float64)) for s in seeds])
     for j in range(dev.shape[1]):
         diff = dev[:, j].mean() - orcs[:, j].mean()

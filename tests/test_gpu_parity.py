@@ -1,7 +1,9 @@
 """GPU parity of the transport / develop / scan path against the CPU oracle.
 
 Every test runs the CUDA library through the C ABI and checks it against oracle/ on the same
-seeded inputs:
+seeded inputs, with the reference's own hit rule (the oracle's FAITHFUL mode: its spatial-median
+BVH, leaf-box reach and traversal order, bvh.rs:157-347):
+  * the device builds exactly the reference's tree: the same index order, leaves and leaf boxes;
   * recorded photon segments replayed on the device give the oracle's hit index lists and latent
     counts bit for bit;
   * development of identical counts gives the same developed mask, clump ids and expansions;
@@ -95,6 +97,51 @@ def test_device_transmittance_evaluation(engine):
 
 
 # ------------------------------------------------------------------------------------------------
+# The reference tree (bvh.rs:157-295) built on the device
+
+@pytest.mark.parametrize("preset,size,seed", [("tri-x", (40.0, 36.0), 1), ("hp5", (30.0, 24.0), 2),
+                                              ("t-max", (26.0, 22.0), 3), ("tri-x", (200.0, 180.0), 4)])
+def test_device_reference_tree_equals_the_oracle(engine, preset, size, seed):
+    """Index order, leaf ranges and FP64 leaf boxes of the device's tree equal the oracle's
+    restatement of BVH::build, over all crystals and over the developed ones with their expansion."""
+    cfg = reference_cfg(preset, *size)
+    cr = orc.synthesize(cfg, seed)
+    rng = np.random.default_rng(seed)
+    cr.developed[:] = (rng.random(len(cr)) < 0.4).astype(np.uint8)
+    cr.expansion[:] = np.where(cr.developed == 1, 1.2 * (1.0 + 0.18 * rng.integers(0, 4, len(cr))), 0.0)
+    em = upload(cr, cfg, engine)
+    em.set_development(cr.developed, cr.expansion)
+    for dev_only in (False, True):
+        order, leaves, boxes = fg.reference_tree(em, dev_only)
+        ro, rl, rb = orc.bvh_export(cr, dev_only)
+        np.testing.assert_array_equal(order, ro)
+        k = np.argsort(rl[:, 0], kind="stable")
+        np.testing.assert_array_equal(leaves, rl[k])
+        np.testing.assert_array_equal(boxes, rb[k])
+    assert len(cr) > 1000
+
+
+@pytest.mark.parametrize("n", [1, 2, 4, 5, 31, 32, 33, 64, 200])
+def test_device_reference_tree_small_and_degenerate_sets(engine, n):
+    """Sets at the leaf size, at the per-warp finish's edge, and with coincident centroids (the
+    reference's degenerate-extent leaf, bvh.rs:230-239)."""
+    cfg = reference_cfg("tri-x", 20.0, 20.0)
+    rng = np.random.default_rng(n)
+    pos = rng.random((n, 3)) * [20.0, 20.0, 14.0]
+    if n >= 31:
+        pos[: n // 3] = pos[0]  # a third of the crystals share one centre
+    dims = np.full((n, 3), 0.4) * (1.0 + rng.random((n, 1)))
+    cr = orc.Crystals(pos, dims, identity_quats(n), np.ones(n), np.zeros(n, np.int32))
+    em = upload(cr, cfg, engine)
+    order, leaves, boxes = fg.reference_tree(em)
+    ro, rl, rb = orc.bvh_export(cr)
+    np.testing.assert_array_equal(order, ro)
+    k = np.argsort(rl[:, 0], kind="stable")
+    np.testing.assert_array_equal(leaves, rl[k])
+    np.testing.assert_array_equal(boxes, rb[k])
+
+
+# ------------------------------------------------------------------------------------------------
 # Configuration C1: 256 x 256 ramp, tri-x cubic grains, 2.4 px grain (0.41667 um pixels), seed 0.
 
 C1_PX = 1.0 / 2.4
@@ -108,7 +155,7 @@ def c1():
     tile = ramp_tile(th, tw)
     cr = orc.synthesize(cfg, 0)
     ecfg = tile_worker_exposure_cfg(1.0)
-    P, segs, hits = orc.expose(cr, cfg, tile, ecfg, 1, orc.CANONICAL, record=True)
+    P, segs, hits = orc.expose(cr, cfg, tile, ecfg, 1, orc.FAITHFUL, record=True)
     counts = cr.latent.copy()
     dcr = cr.copy()
     rep = orc.develop(dcr, tile_worker_dev_cfg("tri-x"))
@@ -148,7 +195,7 @@ def test_c1_scan_fixed_mask_matches_fp64(engine, c1):
     em.set_development(d.developed, d.expansion)
     sc = fg.ScanConfig(256, 256, 4, fg.ScanMode.NegativeTransmittance, 0.25)
     buf, _ = fg.scan_emulsion(em, sc, 2)
-    ref = orc.scan(d, c1["cfg"], sc, 2, orc.CANONICAL, want_hits=True)
+    ref = orc.scan(d, c1["cfg"], sc, 2, orc.FAITHFUL, want_hits=True)
     rel = np.abs(buf.astype(np.float64) - ref["T64"]) / ref["T64"]
     assert rel.max() <= T_RTOL, rel.max()
     assert abs(buf.mean() - ref["T64"].mean()) / ref["T64"].mean() < 1e-6
@@ -164,7 +211,7 @@ def test_c1_scan_rays_hit_sets_bit_exact(engine, c1):
     o = orc.scan_ray_origins(c1["cfg"], sc, 9)
     dirs = np.tile([0.0, 0.0, -1.0], (len(o), 1))
     off, ids, chord = fg.replay_rays(em, o, dirs, developed_only=True)
-    ro, rids, rchord = orc.rays_hits(d, o, dirs, orc.CANONICAL, developed_only=True)
+    ro, rids, rchord = orc.rays_hits(d, o, dirs, orc.FAITHFUL, developed_only=True)
     np.testing.assert_array_equal(off, ro)
     np.testing.assert_array_equal(ids, rids)
     np.testing.assert_allclose(chord, rchord, rtol=1e-12, atol=1e-12)
@@ -193,7 +240,7 @@ def test_other_stocks_replay_develop_scan(engine, preset):
     cr = orc.synthesize(cfg, 17)
     tile = ramp_tile(th, tw)
     ecfg = tile_worker_exposure_cfg(1.5)
-    P, segs, _ = orc.expose(cr, cfg, tile, ecfg, 18, orc.CANONICAL, record=True)
+    P, segs, _ = orc.expose(cr, cfg, tile, ecfg, 18, orc.FAITHFUL, record=True)
     em = upload(cr, cfg, engine)
     off, ids = fg.replay_segments(em, ecfg, 18, segs)
     ro, rids = orc.replay_segments(cr.copy(), ecfg, 18, segs)
