@@ -111,7 +111,8 @@ class fg_tile_params(C.Structure):
 
 class fg_batch_options(C.Structure):
     _fields_ = [("use_graph", C.c_int32), ("autotune", C.c_int32), ("transport_threads", C.c_uint32),
-                ("transport_blocks", C.c_uint32), ("scan_bin_px", C.c_uint32), ("_pad", C.c_uint32)]
+                ("transport_blocks", C.c_uint32), ("scan_bin_px", C.c_uint32), ("synth_wait_limit", C.c_uint32),
+                ("wait_probe", C.c_int32), ("_pad", C.c_uint32)]
 
 
 class fg_batch_stats(C.Structure):
@@ -191,6 +192,7 @@ PROTOTYPES = {
     "fg_replay_rays": (_st, [_vp, _vp, _dp, _dp, C.c_size_t, C.c_int, _u32p, _u32p,
                              C.c_size_t, _szp, _dp]),
     "fg_scan_ray_hits": (_st, [_vp, _vp, C.POINTER(fg_scan_cfg), C.c_uint64, _u16p]),
+    "fg_set_device_budget": (_st, [C.c_uint64]),
     "fg_emulsion_reference_tree": (_st, [_vp, _vp, C.c_int, _u32p, _u32p, _dp, C.c_size_t, _szp, _szp]),
     "fg_blend_tiles": (_st, [_vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _u32p,
                              C.POINTER(_fp), _fp]),

@@ -481,12 +481,12 @@ class Batch:
     """Many tiles rendered by one graph-captured sequence of launches."""
 
     def __init__(self, params, engine: GpuEngine | None = None, use_graph=True, autotune=False,
-                 transport_threads=0, transport_blocks=0, scan_bin_px=0):
+                 transport_threads=0, transport_blocks=0, scan_bin_px=0, synth_wait_limit=0, wait_probe=False):
         self.engine = _engine(engine)
         self.params = list(params)
         arr = (_abi.fg_tile_params * len(self.params))(*self.params)
         opt = _abi.fg_batch_options(int(use_graph), int(autotune), transport_threads, transport_blocks,
-                                    scan_bin_px, 0)
+                                    scan_bin_px, synth_wait_limit, int(bool(wait_probe)), 0)
         h = C.c_void_p()
         e = self.engine
         _check(e, e._lib.fg_batch_create(e._h, arr, len(self.params), C.byref(opt), C.byref(h)))

@@ -1,7 +1,8 @@
 """Builds libfgrain_cuda.so in-tree for sm_103a (GB300).
 
-Each .cu translation unit is compiled in parallel with nvcc, then linked into one shared
-library next to this file.  Object files go to fgrain_gb300/_build/.
+Each .cu translation unit (csrc/) is compiled in parallel with nvcc and each host-only .cpp
+translation unit (host/) with the host C++ compiler, then all are linked into one shared library
+next to this file.  Object files go to fgrain_gb300/_build/.
 """
 from __future__ import annotations
 
@@ -13,6 +14,8 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
+HOST = HERE / "host"
+INCLUDE = HERE.parent / "include"
 OUT = HERE / "libfgrain_cuda.so"
 BUILD = HERE / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -27,8 +30,15 @@ def nvcc() -> str:
     return cand if Path(cand).exists() else "nvcc"
 
 
+HOST_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-ffp-contract=off"]
+
+
+def cxx() -> str:
+    return os.environ.get("CXX") or "g++"
+
+
 def sources() -> list[Path]:
-    return sorted(CSRC.glob("*.cu"))
+    return sorted(CSRC.glob("*.cu")) + sorted(HOST.glob("*.cpp"))
 
 
 def _stale(out: Path, deps: list[Path]) -> bool:
@@ -40,14 +50,17 @@ def _stale(out: Path, deps: list[Path]) -> bool:
 
 def build(verbose: bool = False, force: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
-    headers = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list((HERE.parent / "include").glob("*.h"))
+    headers = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list(INCLUDE.glob("*.h"))
     objs = []
     jobs = []
     for src in sources():
-        obj = BUILD / (src.stem + ".o")
+        obj = BUILD / (src.stem + (".o" if src.suffix == ".cu" else ".host.o"))
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
-            cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+            if src.suffix == ".cu":
+                cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+            else:
+                cmd = [cxx(), *HOST_FLAGS, "-I", str(INCLUDE), "-c", str(src), "-o", str(obj)]
             jobs.append(cmd)
 
     def run(cmd):
@@ -65,7 +78,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
                 print(r.stderr, file=sys.stderr)
     if failed:
         msg = "\n\n".join(" ".join(c) + "\n" + e for c, e in failed)
-        raise RuntimeError("nvcc failed:\n" + msg)
+        raise RuntimeError("compile failed:\n" + msg)
     if force or jobs or _stale(OUT, objs):
         cmd = [nvcc(), *ARCH, "-shared", "-o", str(OUT), *map(str, objs)]
         r = subprocess.run(cmd, capture_output=True, text=True)

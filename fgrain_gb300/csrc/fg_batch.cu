@@ -25,7 +25,8 @@
 namespace fg {
 
 void launch_bridson(const SynthTile* tiles, int ntiles, const unsigned cols[4], int gdmax, uint32_t* cells,
-                    uint32_t* npts, uint32_t* done, uint32_t* err, cudaStream_t st);
+                    uint32_t* npts, uint32_t* done, uint32_t* err, cudaStream_t st, uint32_t wait_limit = 0,
+                    const uint32_t* probe = nullptr);
 size_t bridson_smem(int gdmax);
 void launch_synth_post(const SynthTile* tiles, int ntiles, unsigned long long max_cells, unsigned long long max_slots,
                        uint32_t* cells, uint32_t* npts, uint32_t* flags, cudaStream_t st);
@@ -353,6 +354,9 @@ struct fg_batch {
   DBuf<BTile> d_bt;
   DBuf<uint32_t> cells, npts, flags, slot_scan, ncrys;  // flags: points per brick, slot_scan: their exclusive sum
   DBuf<uint32_t> coldone;  // one flag per synthesis column
+  DBuf<uint32_t> probe;    // the failure drill's flag (zero, never set)
+  uint32_t wait_limit = 0;
+  bool wait_probe = false;
   unsigned long long maxcells = 0, maxslots = 0;  // the largest tile's cells and bricks
   DBuf<float4> A, Q, D;
   DBuf<uint64_t> keys;
@@ -575,7 +579,8 @@ static void stage_synth(fg_batch* B, cudaStream_t st, bool capturing = false) {
   FG_CUDA(cudaMemsetAsync(B->cells.p, 0, B->ncells * sizeof(uint32_t), st));
   FG_CUDA(cudaMemsetAsync(B->npts.p, 0, B->ntiles * sizeof(uint32_t), st));
   mark(B->ev[8], st, capturing);
-  launch_bridson(B->d_syn.p, nt, B->cols, B->gdmax, B->cells.p, B->npts.p, B->coldone.p, e->d_err, st);
+  launch_bridson(B->d_syn.p, nt, B->cols, B->gdmax, B->cells.p, B->npts.p, B->coldone.p, e->d_err, st,
+                 B->wait_limit, B->wait_probe ? B->probe.p : nullptr);
   mark(B->ev[7], st, capturing);
   FG_CUDA(cudaMemsetAsync(B->flags.p + B->nslots, 0, sizeof(uint32_t), st));
   launch_synth_post(B->d_syn.p, nt, B->maxcells, B->maxslots, B->cells.p, B->npts.p, B->flags.p, st);
@@ -784,6 +789,12 @@ static void plan(fg_batch* B, const fg_batch_options* opt) {
   B->tr_blocks = opt && opt->transport_blocks ? opt->transport_blocks : static_cast<unsigned>(e->sm_count) * 8;
   const uint32_t bin0 = opt && opt->scan_bin_px ? opt->scan_bin_px : 8;
   B->use_graph = !opt || opt->use_graph;
+  B->wait_limit = opt ? opt->synth_wait_limit : 0;
+  B->wait_probe = opt && opt->wait_probe;
+  if (B->wait_probe) {
+    B->probe.alloc(1, st);
+    FG_CUDA(cudaMemsetAsync(B->probe.p, 0, sizeof(uint32_t), st));
+  }
   // Buffers (bins sized for the smallest bin edge the tuner tries).
   layout_bins(B, 4);
   const unsigned long long nbins_max = B->nbins;
@@ -817,6 +828,7 @@ static void plan(fg_batch* B, const fg_batch_options* opt) {
       t.d = B->D.p + B->syn[i].cbase;
       t.ecap = B->syn[i].ccap;
       t.pad = B->bt[i].pad;
+      t.reach = rt_reach(0.48 * B->params[i].r_min);  // the synthesis's radius clamp (emulsion.rs:162-170)
     }
     rtree_alloc(B->rt, rt, true, st, RT_NODE_FRAC);
     for (uint32_t i = 0; i < n; ++i) {
@@ -824,6 +836,7 @@ static void plan(fg_batch* B, const fg_batch_options* opt) {
       B->bt[i].nbase = rt[i].nbase;
       B->bt[i].ncap = rt[i].ncap;
       B->td[i].nnodes = rt[i].ncap;
+      B->td[i].reach = rt[i].reach;
       rs[i] = rt[i];
       rs[i].exp64 = B->exp64.p + B->syn[i].cbase;
     }
@@ -966,6 +979,7 @@ fg_status fg_emulsion_synthesize(fg_engine* e, const fg_emulsion_cfg* cfg, uint6
     em->stream = st;
     em->has64 = false;
     em->extent = std::max(std::max(cfg->width, cfg->height), cfg->depth);
+    em->max_half_dim = 0.48 * cfg->r_min;  // the radius clamp of the synthesis (emulsion.rs:162-170)
     em->a = std::move(A);
     em->q = std::move(Q);
     em->d = std::move(D);

@@ -101,6 +101,11 @@ const char* fg_status_string(fg_status s) {
   return "unknown status";
 }
 
+fg_status fg_set_device_budget(uint64_t bytes) {
+  fg::g_dev_budget.store(bytes);
+  return FG_OK;
+}
+
 fg_status fg_engine_create(int device, fg_engine** out) {
   if (!out) return FG_ERR_INVALID_ARG;
   *out = nullptr;
@@ -214,6 +219,7 @@ fg_status fg_emulsion_upload(fg_engine* e, const fg_emulsion_cfg* cfg, const fg_
     em->stream = st;
     em->has64 = true;
     for (size_t i = 0; i < 3 * n; ++i) em->extent = std::max(em->extent, std::fabs(c->pos[i]));
+    for (size_t i = 0; i < 3 * n; ++i) em->max_half_dim = std::max(em->max_half_dim, c->dims[i]);
     FG_CUDA(cudaEventRecord(e->timer.ev[0], st));
     if (n) {
       DBuf<double> pos, dims, quat, sens;

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <mutex>
 #include <new>
 #include <stdexcept>
@@ -43,6 +44,10 @@ inline fg_status status_of(cudaError_t e) {
   }
 }
 
+// Device bytes held through DBuf and the optional cap on them (fg_set_device_budget).
+inline std::atomic<unsigned long long> g_dev_bytes{0};
+inline std::atomic<unsigned long long> g_dev_budget{0};
+
 // Device buffer owned by RAII; stream-ordered allocation on the engine stream.  view() makes it a
 // non-owning window onto memory that someone else holds (nothing is freed then).
 template <class T>
@@ -56,9 +61,21 @@ struct DBuf {
   void alloc(size_t count, cudaStream_t st) {
     release();
     s = st;
-    n = count;
     own = true;
-    if (count) FG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&p), count * sizeof(T), st));
+    if (!count) return;
+    const unsigned long long bytes = count * sizeof(T), cap = g_dev_budget.load();
+    if (cap && g_dev_bytes.fetch_add(bytes) + bytes > cap) {
+      g_dev_bytes.fetch_sub(bytes);
+      throw Error{FG_ERR_OOM, "device budget of " + std::to_string(cap) + " bytes exceeded (fg_set_device_budget)"};
+    }
+    if (!cap) g_dev_bytes.fetch_add(bytes);
+    const cudaError_t r = cudaMallocAsync(reinterpret_cast<void**>(&p), bytes, st);
+    if (r != cudaSuccess) {
+      g_dev_bytes.fetch_sub(bytes);
+      p = nullptr;
+      throw Error{status_of(r), std::string("cudaMallocAsync: ") + cudaGetErrorString(r)};
+    }
+    n = count;
   }
   void view(T* ptr, size_t count) {
     release();
@@ -67,7 +84,10 @@ struct DBuf {
     own = false;
   }
   void release() {
-    if (p && own) cudaFreeAsync(p, s);
+    if (p && own) {
+      cudaFreeAsync(p, s);
+      g_dev_bytes.fetch_sub(n * sizeof(T));
+    }
     p = nullptr;
     n = 0;
     own = true;
@@ -108,6 +128,7 @@ struct RTreeBufs {
   uint32_t count = 0;             // elements of a one-tile tree built on the host's request
   DBuf<RTile> tiles;
   DBuf<uint32_t> idx0, idx1, nof0, nof1, flag, bb, blk, P, Q;
+  DBuf<double4> pm0, pm1;         // element position and half-size, travelling with the order
   DBuf<uint32_t> ridx;            // final element order (slots): a leaf's crystals in reference order
   DBuf<unsigned long long> acc;   // per node: 6 ordered minima, 6 ordered maxima
   DBuf<double> box64;             // per node: lo xyz, hi xyz (FP64, exact)
@@ -157,6 +178,7 @@ struct fg_emulsion {
   fg::DBuf<int64_t> clump;  // by crystal id
   bool has64 = false;
   double extent = 0.0;             // largest coordinate magnitude (sets the box padding)
+  double max_half_dim = 0.0;       // largest crystal half-dimension (sets the walks' reach)
   std::vector<uint32_t> h_s2id;    // host copy of sorted_to_id (empty: identity)
 
   fg::CrystalsView view() const {

@@ -1,28 +1,29 @@
 // Device builder of the reference tree (BVH::build / subdivide, bvh.rs:157-295); see fg_rtree.cuh.
 //
 // The tree is built top-down, one level at a time over all tiles of a batch:
-//   reduce  each pending node's box and centroid box (FP64 min / max as ordered 64-bit atomics,
-//           exact whatever the order);
+//   reduce  each pending node's box and centroid box (min / max on order-preserving 64-bit keys
+//           of the FP64 values: exact whatever the order, and on the integer pipes);
 //   decide  leaf or split (largest centroid extent, midpoint 0.5 (lo + hi)), children ids;
-//   flag    every element of a splitting node: centroid >= mid ("big");
-//   scan    exclusive prefix sum of the flags (ranks of bigs inside each node's contiguous range);
+//   flag    every element of a splitting node: centroid >= mid ("big"), with the prefix sum of the
+//           flags (ranks of bigs inside each node's contiguous range) in the same passes;
 //   pq      P_m = position of the m-th big from the left, Q_m = of the m-th small from the right;
-//   K       the number of m with P_m < Q_m (bigs and smalls the swaps exchange);
 //   place   every element moves to where the reference's swap partition puts it (below).
+// Each element's position and half-size (FP64) travel with it, so every pass reads them in order.
 // Nodes of at most 32 elements are then finished by one warp each with the same arithmetic on
 // ballots.
 //
 // The swap partition (bvh.rs:244-258: i from the left, j from the right; a small at i stays and i
 // advances, a big at i is swapped with j and j retreats) examines the range as two streams: the
-// left stream runs while it sees smalls, the right stream while it sees bigs.  With P_m, Q_m and
-// K as above (Q_0 = n), the left stream covers [0, li) where li = P_{K+1} + 1 if a (K+1)-th big
-// exists before Q_K, else li = Q_K; and the element at relative position r goes to
+// left stream runs while it sees smalls, the right stream while it sees bigs.  With S the number
+// of smalls, K = the number of bigs among the first S positions (the pairs the swaps exchange) and
+// Q_0 = n, the left stream covers [0, li) where li = S + 1 if position S holds a big, else S; and
+// the element at relative position r goes to
 //   r < li, small:            r                      (stays)
 //   r < li, the m-th big:     Q_{m-1} - 1            (bigs fill the right end in examination order)
 //   r >= li, the m-th small from the right:  P_m     (takes the place of the m-th big)
 //   r >= li, big:             r - 1                  (shifts one place towards the middle)
-// The number of smalls is the left child's size; a simulation of the reference loop confirms the
-// rule on random ranges.
+// S is the left child's size.  A simulation of the reference loop confirms the rule and the closed
+// forms of K and li on random ranges.
 #include <algorithm>
 #include <climits>
 #include <cmath>
@@ -42,7 +43,7 @@ constexpr unsigned RT_BLOCK = 256;
 int levels_for(uint32_t emax) {
   int lv = 1;
   while ((static_cast<unsigned long long>(RT_WARP_MAX) << lv) < std::max<unsigned long long>(emax, 1)) ++lv;
-  return std::min(lv + 12, 44);
+  return std::min(lv + 8, 44);
 }
 
 constexpr unsigned SCAN_ITEMS = 2048;  // entries per block of the prefix sum (256 threads x 8)
@@ -88,6 +89,7 @@ struct RtArgs {
   int ntiles;
   unsigned long long E, N;
   uint32_t* idx[2];
+  double4* pm[2];  // position xyz and half-size (max_dim * expansion) of the element, in FP64
   uint32_t* nof[2];
   uint32_t* flag;
   uint32_t* bb;
@@ -142,6 +144,7 @@ __global__ void k_rt_init(RtArgs A) {
     if (k < T.n) {
       const uint32_t slot = T.order ? static_cast<uint32_t>(T.order[k] - T.obase) : static_cast<uint32_t>(k);
       A.idx[0][x] = slot;
+      A.pm[0][x] = rt_pm(T, slot);
       v = T.n > static_cast<uint32_t>(RT_WARP_MAX) ? static_cast<uint32_t>(T.nbase + 1) : RT_DONE;
     }
     A.nof[0][x] = v;
@@ -165,47 +168,80 @@ __global__ void k_rt_init(RtArgs A) {
   }
 }
 
-// Box and centroid box of every pending node (12 ordered atomics per warp and node).
+// The 12 ordered keys of element slot s: box lo xyz and centroid xyz (minima), box hi xyz and
+// centroid xyz (maxima).  Min and max are exact in any order, and on the ordered 64-bit keys they
+// run on the integer pipes (GB300's FP64 pipe is narrow).
+__device__ __forceinline__ void rt_keys(const double4& v, unsigned long long k[12]) {
+  double lo[3], hi[3], cc[3];
+  rt_box_pm(v, lo, hi, cc);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    k[i] = ord64(lo[i]);
+    k[3 + i] = ord64(cc[i]);
+    k[6 + i] = ord64(hi[i]);
+    k[9 + i] = ord64(cc[i]);
+  }
+}
+
+__device__ __forceinline__ unsigned long long umin64(unsigned long long a, unsigned long long b) { return a < b ? a : b; }
+__device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) { return a > b ? a : b; }
+
+// Box and centroid box of every pending node: a warp whose lanes all hold one node reduces by a
+// butterfly, other warps per group of equal nodes; one set of 12 atomics per warp and node.
 __global__ void k_rt_reduce(RtArgs A, int c) {
   if (A.cnt[c] == 0) return;
   const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
   for (unsigned long long base = blockIdx.x * static_cast<unsigned long long>(blockDim.x); base < A.E; base += stride) {
     const unsigned long long x = base + threadIdx.x;
     uint32_t node = RT_DONE;
-    double v[12];
+    unsigned long long k[12];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      k[i] = ~0ull;
+      k[6 + i] = 0ull;
+    }
     if (x < A.E) {
       node = A.nof[c][x];
-      if (!(node & RT_DONE)) {
-        const RTile& T = A.tiles[A.ntile[node]];
-        // v[0..2] box lo, v[3..5] centroid (its minimum), v[6..8] box hi, v[9..11] centroid
-        // (its maximum): six minima, then six maxima.
-        rt_box(T, A.idx[c][x], v, v + 6, v + 3);
-        v[9] = v[3];
-        v[10] = v[4];
-        v[11] = v[5];
+      if (!(node & RT_DONE)) rt_keys(A.pm[c][x], k);
+    }
+    const uint32_t n0 = __shfl_sync(0xffffffffu, node, 0);
+    if (__all_sync(0xffffffffu, node == n0)) {
+      if (n0 & RT_DONE) continue;
+#pragma unroll
+      for (int i = 0; i < 12; ++i)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const unsigned long long y = __shfl_xor_sync(0xffffffffu, k[i], o);
+          k[i] = i < 6 ? umin64(k[i], y) : umax64(k[i], y);
+        }
+      if ((threadIdx.x & 31) == 0) {
+        unsigned long long* a = A.acc + 12ull * node;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) atomicMin(a + i, k[i]);
+#pragma unroll
+        for (int i = 6; i < 12; ++i) atomicMax(a + i, k[i]);
       }
+      continue;
     }
     const bool act = !(node & RT_DONE);
     const unsigned m = __ballot_sync(0xffffffffu, act);
     if (!act) continue;
     const unsigned grp = __match_any_sync(m, node);
-    const int leader = __ffs(grp) - 1;
-    // mins: v[0..2] box lo, v[3..5] centroid lo; maxima: v[6..8] box hi, v[9..11] centroid hi
 #pragma unroll
-    for (int k = 0; k < 12; ++k) {
-      double r = v[k];
+    for (int i = 0; i < 12; ++i) {
+      unsigned long long r = k[i];
       for (unsigned q = grp; q; q &= q - 1) {
-        const double o = __shfl_sync(grp, v[k], __ffs(q) - 1);
-        r = k < 6 ? fmin(r, o) : fmax(r, o);
+        const unsigned long long y = __shfl_sync(grp, k[i], __ffs(q) - 1);
+        r = i < 6 ? umin64(r, y) : umax64(r, y);
       }
-      v[k] = r;
+      k[i] = r;
     }
-    if (static_cast<int>(threadIdx.x & 31) == leader) {
+    if (static_cast<int>(threadIdx.x & 31) == __ffs(grp) - 1) {
       unsigned long long* a = A.acc + 12ull * node;
 #pragma unroll
-      for (int k = 0; k < 6; ++k) atomicMin(a + k, ord64(v[k]));
+      for (int i = 0; i < 6; ++i) atomicMin(a + i, k[i]);
 #pragma unroll
-      for (int k = 6; k < 12; ++k) atomicMax(a + k, ord64(v[k]));
+      for (int i = 6; i < 12; ++i) atomicMax(a + i, k[i]);
     }
   }
 }
@@ -242,29 +278,6 @@ __global__ void k_rt_decide(RtArgs A, int c) {
   }
 }
 
-__device__ __forceinline__ double axis_centroid(const RTile& T, uint32_t s, int axis) {
-  double lo[3], hi[3], cc[3];
-  rt_box(T, s, lo, hi, cc);
-  return cc[axis];
-}
-
-__global__ void k_rt_flags(RtArgs A, int c) {
-  if (A.cnt[c] == 0) return;
-  const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
-  for (unsigned long long x = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; x <= A.E;
-       x += stride) {
-    uint32_t f = 0;
-    if (x < A.E) {
-      const uint32_t node = A.nof[c][x];
-      if (!(node & RT_DONE)) {
-        const int axis = A.nsplit[node];
-        if (axis >= 0) f = (axis_centroid(A.tiles[A.ntile[node]], A.idx[c][x], axis) < A.nmid[node]) ? 0u : 1u;
-      }
-    }
-    A.flag[x] = f;
-  }
-}
-
 // Exclusive prefix sum of flag[0..E] into bb, in blocks of SCAN_ITEMS: block sums, one block
 // scanning the block sums, then each block's own scan.
 __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* sh, uint32_t& total) {
@@ -293,6 +306,21 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* sh, ui
   return r;
 }
 
+// The flag of position x: its element's centroid >= the split of its node ("big"), 0 when the
+// node does not split (or x is done or past the end).
+__device__ __forceinline__ uint32_t rt_flag(const RtArgs& A, int c, unsigned long long x) {
+  if (x >= A.E) return 0u;
+  const uint32_t node = A.nof[c][x];
+  if (node & RT_DONE) return 0u;
+  const int axis = A.nsplit[node];
+  if (axis < 0) return 0u;
+  const double4 v = A.pm[c][x];
+  const double p = axis == 0 ? v.x : (axis == 1 ? v.y : v.z);
+  const double cc = __dmul_rn(0.5, __dadd_rn(__dsub_rn(p, v.w), __dadd_rn(p, v.w)));
+  return cc < A.nmid[node] ? 0u : 1u;
+}
+
+// Flags and their block sums.
 __global__ void __launch_bounds__(RT_BLOCK) k_rt_scan_blocks(RtArgs A, int c, unsigned long long nb) {
   if (A.cnt[c] == 0) return;
   __shared__ uint32_t sh[32];
@@ -301,7 +329,11 @@ __global__ void __launch_bounds__(RT_BLOCK) k_rt_scan_blocks(RtArgs A, int c, un
     uint32_t s = 0;
 #pragma unroll
     for (int k = 0; k < 8; ++k)
-      if (x0 + k <= A.E) s += A.flag[x0 + k];
+      if (x0 + k <= A.E) {
+        const uint32_t f = rt_flag(A, c, x0 + k);
+        A.flag[x0 + k] = f;
+        s += f;
+      }
     uint32_t tot;
     block_excl_scan(s, sh, tot);
     if (threadIdx.x == 0) A.blk[b] = tot;
@@ -366,31 +398,6 @@ __global__ void k_rt_pq(RtArgs A, int c) {
   }
 }
 
-// K: the number of bigs m with P_m < Q_m (they form a prefix of the bigs).
-__global__ void k_rt_K(RtArgs A, int c) {
-  if (A.cnt[c] == 0) return;
-  const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
-  for (unsigned long long base = blockIdx.x * static_cast<unsigned long long>(blockDim.x); base < A.E; base += stride) {
-    const unsigned long long x = base + threadIdx.x;
-    uint32_t node = RT_DONE;
-    bool pred = false;
-    if (x < A.E) {
-      node = A.nof[c][x];
-      if (!(node & RT_DONE) && A.nsplit[node] >= 0 && A.flag[x]) {
-        const uint32_t s = A.nstart[node], n = A.ncount[node];
-        const uint32_t r = static_cast<uint32_t>(x - s);
-        const uint32_t bs = A.bb[s];
-        const uint32_t m = A.bb[x] - bs + 1, St = n - (A.bb[s + n] - bs);
-        pred = m <= St && r < A.Q[s + m - 1];
-      }
-    }
-    const unsigned pm = __ballot_sync(0xffffffffu, pred);
-    if (!pred) continue;
-    const unsigned grp = __match_any_sync(pm, node);
-    if (static_cast<int>(threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&A.nK[node], static_cast<uint32_t>(__popc(grp)));
-  }
-}
-
 // Moves every element of a splitting node to its place after the reference's swap partition;
 // finishes the elements of new leaves; sets up the children.
 __global__ void k_rt_place(RtArgs A, int c) {
@@ -414,11 +421,7 @@ __global__ void k_rt_place(RtArgs A, int c) {
     const uint32_t r = static_cast<uint32_t>(x - s);
     const uint32_t bs = A.bb[s];
     const uint32_t Bb = A.bb[x] - bs, Bt = A.bb[s + n] - bs, St = n - Bt;
-    const uint32_t K = A.nK[node];
-    const uint32_t QK = K >= 1 ? A.Q[s + K - 1] : n;
-    const bool hasP = K + 1 <= Bt;
-    const uint32_t PK1 = hasP ? A.P[s + K] : n;
-    const uint32_t li = (hasP && PK1 < QK) ? PK1 + 1 : QK;
+    const uint32_t li = St + (St < n ? A.flag[s + St] : 0u);
     const bool big = A.flag[x] != 0;
     uint32_t dest;
     if (r < li) {
@@ -433,6 +436,7 @@ __global__ void k_rt_place(RtArgs A, int c) {
     const uint32_t child = static_cast<uint32_t>(left ? ch.x : ch.y);
     const uint32_t csize = left ? Sp : n - Sp;
     A.idx[o][s + dest] = el;
+    A.pm[o][s + dest] = A.pm[c][x];
     A.nof[o][s + dest] = csize > static_cast<uint32_t>(RT_WARP_MAX) ? child : RT_DONE;
     if (r == 0) {
       const uint32_t t = A.ntile[node], dep = A.ndepth[node] + 1;
@@ -480,10 +484,12 @@ __global__ void __launch_bounds__(32 * RT_WARPS) k_rt_warp(RtArgs A) {
     const uint32_t t = A.ntile[root];
     const RTile& T = A.tiles[t];
     uint32_t el = 0;
-    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0}, cc[3] = {0, 0, 0};
+    unsigned long long key[12];  // the element's ordered keys (rt_keys)
+#pragma unroll
+    for (int i = 0; i < 12; ++i) key[i] = 0;
     if (static_cast<uint32_t>(lane) < n) {
       el = A.idx[par][s + lane];
-      rt_box(T, el, lo, hi, cc);
+      rt_keys(A.pm[par][s + lane], key);
     }
     int sp = 0;
     if (lane == 0) {
@@ -501,21 +507,19 @@ __global__ void __launch_bounds__(32 * RT_WARPS) k_rt_warp(RtArgs A) {
       __syncwarp();
       maxdep = max(maxdep, static_cast<uint32_t>(dep));
       const bool in = lane >= off && lane < off + cnt;
-      double v[12];
+      unsigned long long u[12];
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        v[k] = in ? lo[k] : INFINITY;
-        v[3 + k] = in ? cc[k] : INFINITY;
-        v[6 + k] = in ? hi[k] : -INFINITY;
-        v[9 + k] = in ? cc[k] : -INFINITY;
-      }
+      for (int k = 0; k < 12; ++k) u[k] = in ? key[k] : (k < 6 ? ~0ull : 0ull);
 #pragma unroll
       for (int k = 0; k < 12; ++k)
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-          const double y = __shfl_xor_sync(0xffffffffu, v[k], o);
-          v[k] = k < 6 ? fmin(v[k], y) : fmax(v[k], y);
+          const unsigned long long y = __shfl_xor_sync(0xffffffffu, u[k], o);
+          u[k] = k < 6 ? umin64(u[k], y) : umax64(u[k], y);
         }
+      double v[12];
+#pragma unroll
+      for (int k = 0; k < 12; ++k) v[k] = unord64(u[k]);
       if (lane == 0) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
@@ -541,7 +545,7 @@ __global__ void __launch_bounds__(32 * RT_WARPS) k_rt_warp(RtArgs A) {
       }
       const double mid = __dmul_rn(0.5, __dadd_rn(axis == 0 ? v[3] : (axis == 1 ? v[4] : v[5]),
                                                   axis == 0 ? v[9] : (axis == 1 ? v[10] : v[11])));
-      const double ca = axis == 0 ? cc[0] : (axis == 1 ? cc[1] : cc[2]);
+      const double ca = unord64(axis == 0 ? key[3] : (axis == 1 ? key[4] : key[5]));
       const bool big = in && !(ca < mid);
       const unsigned rng = (cnt == 32 ? 0xffffffffu : ((1u << cnt) - 1u)) << off;
       const unsigned bm = __ballot_sync(0xffffffffu, big) & rng;
@@ -574,11 +578,7 @@ __global__ void __launch_bounds__(32 * RT_WARPS) k_rt_warp(RtArgs A) {
       __syncwarp();
       el = __shfl_sync(0xffffffffu, el, from);
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        lo[k] = __shfl_sync(0xffffffffu, lo[k], from);
-        hi[k] = __shfl_sync(0xffffffffu, hi[k], from);
-        cc[k] = __shfl_sync(0xffffffffu, cc[k], from);
-      }
+      for (int k = 0; k < 12; ++k) key[k] = __shfl_sync(0xffffffffu, key[k], from);
       const unsigned long long nb = T.nbase;
       const int Sp = (St == 0 || St == cnt) ? cnt / 2 : St;  // bvh.rs:260-265
       if (lane == 0) {
@@ -629,8 +629,8 @@ __global__ void k_rt_records(RtArgs A, Node* rnode, uint2* rleaf, uint32_t* leaf
       } else {
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-          f[k] = __double2float_rd(b[k]) - T.pad;
-          f[3 + k] = __double2float_ru(b[3 + k]) + T.pad;
+          f[k] = __double2float_rd(b[k]) - T.pad - T.reach;
+          f[3 + k] = __double2float_ru(b[3 + k]) + T.pad + T.reach;
         }
       }
     };
@@ -696,6 +696,8 @@ RtArgs rt_args(RTreeBufs& B, uint32_t* err) {
   A.N = B.N;
   A.idx[0] = B.idx0.p;
   A.idx[1] = B.idx1.p;
+  A.pm[0] = B.pm0.p;
+  A.pm[1] = B.pm1.p;
   A.nof[0] = B.nof0.p;
   A.nof[1] = B.nof1.p;
   A.flag = B.flag.p;
@@ -747,6 +749,8 @@ void rtree_alloc(RTreeBufs& B, std::vector<RTile>& tiles, bool want_leafof, cuda
   FG_CUDA(cudaMemcpyAsync(B.tiles.p, tiles.data(), tiles.size() * sizeof(RTile), cudaMemcpyHostToDevice, st));
   B.idx0.alloc(E1, st);
   B.idx1.alloc(E1, st);
+  B.pm0.alloc(E1, st);
+  B.pm1.alloc(E1, st);
   B.nof0.alloc(E1, st);
   B.nof1.alloc(E1, st);
   B.flag.alloc(E1 + 1, st);
@@ -798,6 +802,8 @@ size_t carve(RTreeBufs* B, uint32_t ecap, bool want_leafof, uint32_t leafof_slot
   take(b.tiles, 1);
   take(b.idx0, E1);
   take(b.idx1, E1);
+  take(b.pm0, E1);
+  take(b.pm1, E1);
   take(b.nof0, E1);
   take(b.nof1, E1);
   take(b.flag, E1 + 1);
@@ -867,12 +873,10 @@ void rtree_build(RTreeBufs& B, uint32_t* err, cudaStream_t st, RTile* tiles_dev)
     const int c = L & 1;
     k_rt_reduce<<<G, RT_BLOCK, 0, st>>>(A, c);
     k_rt_decide<<<GN, RT_BLOCK, 0, st>>>(A, c);
-    k_rt_flags<<<G, RT_BLOCK, 0, st>>>(A, c);
     k_rt_scan_blocks<<<GS, RT_BLOCK, 0, st>>>(A, c, B.nblk);
     k_rt_scan_top<<<1, 1024, 0, st>>>(A, c, B.nblk);
     k_rt_scan_final<<<GS, RT_BLOCK, 0, st>>>(A, c, B.nblk);
     k_rt_pq<<<G, RT_BLOCK, 0, st>>>(A, c);
-    k_rt_K<<<G, RT_BLOCK, 0, st>>>(A, c);
     k_rt_place<<<G, RT_BLOCK, 0, st>>>(A, c);
     k_rt_level_end<<<1, 1, 0, st>>>(A, c);
   }
@@ -910,6 +914,7 @@ void build_emulsion_tree(fg_engine* e, const fg_emulsion* em, bool developed_onl
   t.dims64 = em->has64 ? em->dims64.p : nullptr;
   t.exp64 = developed_only ? em->exp64.p : nullptr;
   t.pad = static_cast<float>(std::max(em->extent, std::max(em->cfg.width, em->cfg.height)) * 2e-6 + 1e-5);
+  t.reach = developed_only ? 0.0f : rt_reach(em->max_half_dim);
   const uint32_t* id2s = em->h_s2id.empty() ? nullptr : em->id_to_sorted.p;
   uint32_t m = n;
   if (developed_only && n) {
@@ -935,7 +940,7 @@ void build_emulsion_tree(fg_engine* e, const fg_emulsion* em, bool developed_onl
 }
 
 unsigned rtree_kernel_launches(const RTreeBufs& B) {
-  return B.ntiles ? 2u + 10u * static_cast<unsigned>(B.levels) + 4u : 0u;
+  return B.ntiles ? 2u + 8u * static_cast<unsigned>(B.levels) + 4u : 0u;
 }
 
 }  // namespace fg

@@ -17,7 +17,12 @@
 // shared between the crystals along a segment.
 //
 // Walk records.  Node ids are tile-local; id 0 is a super-root whose only (right) child is the
-// real root (id 1), so every walk starts by testing the root's box as the reference does.
+// real root (id 1), so every walk starts by testing the root's box as the reference does.  An
+// internal child's FP32 box is its box rounded outward, padded, and extended by the crystals'
+// reach beyond their own boxes, so that a walk clipped to a segment [0, step] still reaches every
+// leaf holding a crystal the segment hits (the corner of a rotated cube can lie outside its
+// leaf's box, nearer than the box); a leaf child's box is rounded to nearest, for the reference's
+// own leaf test.
 #pragma once
 #include "fg_device.cuh"
 
@@ -43,8 +48,16 @@ struct __align__(16) RTile {
   uint32_t nodes;            // nodes made (written by the build)
   uint32_t depth;            // deepest level (written by the build)
   float pad;                 // outward padding of internal boxes in the FP32 walk records
+  float reach;               // and their extension by the crystals' reach beyond their own boxes
+  uint32_t _pad[3];
 };
-static_assert(sizeof(RTile) == 96, "RTile layout");
+static_assert(sizeof(RTile) == 112, "RTile layout");
+
+// How far a crystal's geometry reaches beyond its own max_dim box (crystal.rs:106-217): a cube of
+// half-size m lies within sqrt(3) m of its centre, an ellipsoid within m; so (sqrt(3) - 1) m.
+inline float rt_reach(double max_half_dim) {
+  return static_cast<float>(0.7320508075688773 * max_half_dim * 1.0001 + 1e-5);
+}
 
 // Sizes of a one-tile build in caller-held memory (rtree_attach): nodes for ecap elements (at most
 // 0.8 per element plus 64; the reference tree needs about 0.67), prefix-sum blocks, and the bytes
@@ -56,7 +69,7 @@ constexpr size_t rt_attach_blocks(size_t e1) { return (e1 + 1 + 2047) / 2048; }
 constexpr size_t rt_al(size_t v) { return (v + 255) / 256 * 256; }
 constexpr size_t rtree_attach_bytes(size_t ecap, bool want_leafof, size_t slots) {
   const size_t e1 = ecap > 0 ? ecap : 1, n1 = rt_attach_nodes(e1);
-  return rt_al(96) + 4 * rt_al(4 * e1) + 2 * rt_al(4 * (e1 + 1)) + rt_al(4 * rt_attach_blocks(e1)) +
+  return rt_al(112) + 4 * rt_al(4 * e1) + 2 * rt_al(32 * e1) + 2 * rt_al(4 * (e1 + 1)) + rt_al(4 * rt_attach_blocks(e1)) +
          3 * rt_al(4 * e1) + rt_al(96 * n1) + rt_al(48 * n1) + 6 * rt_al(4 * n1) + rt_al(4 * n1) + rt_al(8 * n1) +
          rt_al(8 * n1) + 4 * rt_al(4 * n1) + rt_al(16) + rt_al(64 * n1) + rt_al(8 * n1) +
          (want_leafof ? rt_al(4 * (slots > 0 ? slots : 1)) : 0);
@@ -82,6 +95,37 @@ __device__ __forceinline__ void rt_box(const RTile& t, uint32_t s, double lo[3],
   for (int i = 0; i < 3; ++i) {
     lo[i] = __dsub_rn(p[i], m);
     hi[i] = __dadd_rn(p[i], m);
+    c[i] = __dmul_rn(0.5, __dadd_rn(lo[i], hi[i]));
+  }
+}
+
+// Position xyz and half-size m = max_dim * expansion of element slot s, in FP64 (crystal.rs:114-119).
+__device__ __forceinline__ double4 rt_pm(const RTile& t, uint32_t s) {
+  double4 v;
+  double dm;
+  if (t.pos64) {
+    v.x = t.pos64[3 * s];
+    v.y = t.pos64[3 * s + 1];
+    v.z = t.pos64[3 * s + 2];
+    dm = fmax(fmax(t.dims64[3 * s], t.dims64[3 * s + 1]), t.dims64[3 * s + 2]);
+  } else {
+    const float4 a = t.a[s], d = t.d[s];
+    v.x = a.x;
+    v.y = a.y;
+    v.z = a.z;
+    dm = fmax(fmax(static_cast<double>(d.x), static_cast<double>(d.y)), static_cast<double>(d.z));
+  }
+  v.w = __dmul_rn(dm, t.exp64 ? t.exp64[s] : 1.0);
+  return v;
+}
+
+// The box p -+ m and its centroid 0.5 (lo + hi), as rt_box computes them.
+__device__ __forceinline__ void rt_box_pm(const double4& v, double lo[3], double hi[3], double c[3]) {
+  const double p[3] = {v.x, v.y, v.z};
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    lo[i] = __dsub_rn(p[i], v.w);
+    hi[i] = __dadd_rn(p[i], v.w);
     c[i] = __dmul_rn(0.5, __dadd_rn(lo[i], hi[i]));
   }
 }

@@ -132,7 +132,8 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 8) k_bridson(const SynthTile* 
                                                             int ntiles, uint4 class_base, int nz,
                                                             uint32_t* __restrict__ cells,
                                                             uint32_t* __restrict__ npts, uint32_t* done,
-                                                            uint32_t* err) {
+                                                            uint32_t* err, uint32_t wait_limit,
+                                                            const uint32_t* probe) {
   extern __shared__ uint32_t syn_sm[];
   uint32_t* grid = syn_sm;                                   // SYN_R^2 * nz cell words
   uint16_t* active = reinterpret_cast<uint16_t*>(grid + SYN_R * SYN_R * nz);  // SYN_B^2 * (nz - 4)
@@ -180,7 +181,7 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 8) k_bridson(const SynthTile* 
         const volatile uint32_t* f = done + id;
         uint32_t spins = 0;
         while (*f == 0u) {
-          if (++spins > (1u << 22)) {
+          if (++spins > wait_limit) {
             atomicOr(err, ERR_SPIN_LIMIT);
             break;
           }
@@ -188,6 +189,18 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 8) k_bridson(const SynthTile* 
         }
       }
     __threadfence();
+  }
+  // Failure drill: a flag that nothing sets, waited on with the same bound.
+  if (tid == 0 && probe) {
+    const volatile uint32_t* f = probe;
+    uint32_t spins = 0;
+    while (*f == 0u) {
+      if (++spins > wait_limit) {
+        atomicOr(err, ERR_SPIN_LIMIT);
+        break;
+      }
+      __nanosleep(64);
+    }
   }
   __syncthreads();
 
@@ -629,7 +642,8 @@ size_t bridson_smem(int gdmax);
 // Host wrappers (launch on `st`; all buffers preallocated so the sequence can be graph-captured).
 // cols[c] columns of class c; done holds one flag per column (zeroed here).
 void launch_bridson(const SynthTile* tiles, int ntiles, const unsigned cols[4], int gdmax, uint32_t* cells,
-                    uint32_t* npts, uint32_t* done, uint32_t* err, cudaStream_t st) {
+                    uint32_t* npts, uint32_t* done, uint32_t* err, cudaStream_t st, uint32_t wait_limit,
+                    const uint32_t* probe) {
   const unsigned total = cols[0] + cols[1] + cols[2] + cols[3];
   if (total == 0) return;
   const int nz = gdmax + 4;
@@ -637,7 +651,8 @@ void launch_bridson(const SynthTile* tiles, int ntiles, const unsigned cols[4], 
   FG_CUDA(cudaMemsetAsync(done, 0, total * sizeof(uint32_t), st));
   FG_CUDA(cudaFuncSetAttribute(k_bridson, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   const uint4 cb = make_uint4(0u, cols[0], cols[0] + cols[1], cols[0] + cols[1] + cols[2]);
-  k_bridson<<<total, SYN_WARPS * 32, smem, st>>>(tiles, ntiles, cb, nz, cells, npts, done, err);
+  k_bridson<<<total, SYN_WARPS * 32, smem, st>>>(tiles, ntiles, cb, nz, cells, npts, done, err,
+                                                  wait_limit ? wait_limit : (1u << 22), probe);
   FG_CUDA(cudaGetLastError());
 }
 

@@ -24,6 +24,7 @@ struct __align__(16) TileDesc {
   unsigned long long photon_base;
   uint32_t n, tw, th, P;
   uint32_t nnodes;  // node capacity of the tile's tree (bounds the node ids the walk reads)
+  float reach;      // crystals' reach beyond their own boxes (fg_rtree.cuh)
   uint32_t stride;  // exposure row stride (floats); tiles may be windows of one image
   uint32_t pcell_base;  // first photon-sort cell of this tile
   uint32_t pcell_bits;  // photon-sort cells per axis = 2^bits (Morton order)
@@ -37,12 +38,14 @@ struct __align__(16) TileDesc {
 // left then right, pop right first), deferred: a hit leaf is queued until every lane of `amask`
 // holds one or has finished, then the lanes run fn(leaf) together; a lane that holds a leaf walks on
 // (speculatively) until it holds WALK_LEAVES.  The queue keeps each lane's leaves in walk order.
-// Child boxes are tested in FP32 against [0, tlim] of the ray (the caller's step, padded): internal
-// boxes are stored rounded outward, leaf boxes rounded to nearest.  nmax bounds the node ids (index
-// checks).  With amask = the lane's own bit it is a plain walk.
+// An internal child is entered when its (extended) box meets [0, tlim] of the ray (the caller's
+// step, padded); a leaf child when its box extended by `reach` meets [0, tlim] (a crystal hit
+// inside the step lies there) and its own box meets the whole ray (the reference's leaf test,
+// bvh.rs:96-124).  nmax bounds the node ids (index checks).  With amask = the lane's own bit it is
+// a plain walk.
 template <class F>
 __device__ __forceinline__ void rt_walk_deferred(const Node* __restrict__ nodes, float3 o, float3 inv, float tlim,
-                                                 uint32_t* err, F&& fn, uint32_t nmax, unsigned amask) {
+                                                 float reach, uint32_t* err, F&& fn, uint32_t nmax, unsigned amask) {
   constexpr int EMPTY = INT32_MIN;
   constexpr uint32_t NONE = 0xffffffffu;
   int stack[RT_MAX_DEPTH + 1];
@@ -78,17 +81,22 @@ __device__ __forceinline__ void rt_walk_deferred(const Node* __restrict__ nodes,
       const Node* nd = nodes + cur;
       const float4 na = __ldg(&nd->a), nb = __ldg(&nd->b), nc = __ldg(&nd->c);
       const int4 rf = __ldg(&nd->d);
-      // Slab test as lo * inv - o * inv (one FMA per plane), clipped to [0, tlim].
-      auto hit = [&](float a0, float a1, float a2, float a3, float a4, float a5) {
-        const float t1x = fmaf(a0, inv.x, -oi.x), t2x = fmaf(a3, inv.x, -oi.x);
-        const float t1y = fmaf(a1, inv.y, -oi.y), t2y = fmaf(a4, inv.y, -oi.y);
-        const float t1z = fmaf(a2, inv.z, -oi.z), t2z = fmaf(a5, inv.z, -oi.z);
+      // Slab test as lo * inv - o * inv (one FMA per plane), the box grown by g, clipped to [0, t].
+      auto slab_hit = [&](float a0, float a1, float a2, float a3, float a4, float a5, float g, float t) {
+        const float t1x = fmaf(a0 - g, inv.x, -oi.x), t2x = fmaf(a3 + g, inv.x, -oi.x);
+        const float t1y = fmaf(a1 - g, inv.y, -oi.y), t2y = fmaf(a4 + g, inv.y, -oi.y);
+        const float t1z = fmaf(a2 - g, inv.z, -oi.z), t2z = fmaf(a5 + g, inv.z, -oi.z);
         const float te = fmaxf(fmaxf(fminf(t1x, t2x), fminf(t1y, t2y)), fmaxf(fminf(t1z, t2z), 0.0f));
-        const float tx = fminf(fminf(fmaxf(t1x, t2x), fmaxf(t1y, t2y)), fminf(fmaxf(t1z, t2z), tlim));
+        const float tx = fminf(fminf(fmaxf(t1x, t2x), fmaxf(t1y, t2y)), fminf(fmaxf(t1z, t2z), t));
         return te <= tx;
       };
-      const bool hl = rf.x != EMPTY && hit(na.x, na.y, na.z, na.w, nb.x, nb.y);
-      const bool hr = rf.y != EMPTY && hit(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w);
+      auto hit = [&](int ref, float a0, float a1, float a2, float a3, float a4, float a5) {
+        if (ref == EMPTY) return false;
+        if (ref >= 0) return slab_hit(a0, a1, a2, a3, a4, a5, 0.0f, tlim);
+        return slab_hit(a0, a1, a2, a3, a4, a5, reach, tlim) && slab_hit(a0, a1, a2, a3, a4, a5, 0.0f, INFINITY);
+      };
+      const bool hl = hit(rf.x, na.x, na.y, na.z, na.w, nb.x, nb.y);
+      const bool hr = hit(rf.y, nb.z, nb.w, nc.x, nc.y, nc.z, nc.w);
       if (hr) {
         if (hl) {
           if (sp <= RT_MAX_DEPTH) {
@@ -224,7 +232,7 @@ __device__ __forceinline__ bool photon_bounce(const TileDesc& t, Photon& ph, uin
       ++nh;
     }
   };
-  rt_walk_deferred(t.rnode, pos, inv, step * 1.00001f + 1e-3f, err, leaf, t.nnodes,
+  rt_walk_deferred(t.rnode, pos, inv, step * 1.00001f + 1e-3f, t.reach, err, leaf, t.nnodes,
                    amask ? amask : (1u << (threadIdx.x & 31)));
   nhit = nh;
   const float3 np = make_float3(pos.x + dir.x * step, pos.y + dir.y * step, pos.z + dir.z * step);

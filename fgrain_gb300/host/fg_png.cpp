@@ -1,14 +1,16 @@
-// Host helper of the command-line tool's image files: the PNG row filters.
+// Host helper of the command-line tool's image files: the PNG row filters (plain C++, built with
+// the host compiler and linked into the same library as the CUDA translation units).
 //
 // The reference reads and writes its photographs with the image crate (image 0.25, png feature;
 // image::open at src/image_pipeline.rs:1141, GrayImage/RgbImage::save at :1087-1133).  The tool's
 // PNG codec lives in Python (fgrain_gb300/imageio.py: chunks, zlib, Adam7 passes, bit depths);
 // the per-byte recurrences of the Average and Paeth filters are the one part that needs native
-// code to be fast on large scans.  Host code only: nothing here touches the GPU.
+// code to be fast on large scans.  Nothing here touches the GPU.
+#include <cstddef>
 #include <cstdint>
 #include <cstdlib>
 
-#include "fg_internal.h"
+#include "fgrain_cuda.h"
 
 namespace {
 

@@ -9,7 +9,7 @@ u8: alpha dropped, palette looked up, 16-bit samples rounded to 8 bits, gray rep
 Low bit-depth gray is widened to 8 bits by bit replication, as the png crate's ``EXPAND`` does.
 
 PNG chunks, zlib, Adam7 passes and sample unpacking are done here; the row filters are undone by
-the library's ``fg_png_unfilter`` (host code, native for speed on large scans).  JPEG and WebP
+the library's ``fg_png_unfilter`` (host C++ in fgrain_gb300/host/, native for speed on large scans).  JPEG and WebP
 have no codec in this build: reading or writing them raises ``ImageFormatError``.
 """
 from __future__ import annotations

@@ -146,6 +146,12 @@ typedef struct fg_timings {
   uint32_t error_word;
 } fg_timings;
 
+/* Process-wide cap on the device bytes this library holds at once through its own allocations
+ * (0: none, the default).  An allocation past the cap fails with FG_ERR_OOM as a failed cudaMalloc
+ * would, which lets callers and tests exercise the out-of-memory path without exhausting the GPU.
+ * No counterpart in the reference. */
+fg_status fg_set_device_budget(uint64_t bytes);
+
 /* ---- engine (GpuEngine::new / get_gpu_engine, src/gpu.rs:9-14,174) ---- */
 fg_status fg_engine_create(int device, fg_engine** out);
 fg_status fg_engine_destroy(fg_engine* e);
@@ -378,6 +384,11 @@ typedef struct fg_batch_options {
   uint32_t transport_threads;     /* 0: default */
   uint32_t transport_blocks;      /* 0: default */
   uint32_t scan_bin_px;           /* 0: default */
+  uint32_t synth_wait_limit;      /* polls before a synthesis column stops waiting for its
+                                     neighbours (about 64 ns each; 0: 2^22) */
+  int32_t wait_probe;             /* failure drill: nonzero makes every synthesis column also wait
+                                     on a device flag that nothing sets, so the bounded wait runs
+                                     out and the run fails with FG_ERR_DEVICE_TIMEOUT */
   uint32_t _pad;
 } fg_batch_options;
 
@@ -453,7 +464,7 @@ fg_status fg_render_tile_fast(fg_engine* e, const float* tile, const fg_tile_par
 #define FG_STATIC_SCAN_MAX_DEVELOPED 32768u  /* developed crystals per call */
 #define FG_STATIC_SCAN_MAX_BINS 16384u       /* scan bins (bin_px x bin_px pixels each) per call */
 #define FG_STATIC_SCAN_MAX_ITEMS 1048576u    /* (developed crystal, bin) entries per call */
-#define FG_STATIC_SCAN_SCRATCH_BYTES 17153792u
+#define FG_STATIC_SCAN_SCRATCH_BYTES 19250944u
 
 /* A crystal set in device memory, in crystal-index order (any order gives the same image). */
 typedef struct fg_device_crystals {

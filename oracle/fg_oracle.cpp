@@ -1066,6 +1066,73 @@ int or_scan(const or_crystals* c, const or_emulsion_cfg* ecfg, const or_scan_cfg
   return 0;
 }
 
+// FP64 transmittance of pixel windows of a scan, each under +-hstep on one crystal's opacity (the
+// reference's tree over all developed crystals, as or_scan builds it, built once).  Window k is
+// win[4k..4k+3] = (x0, y0, w, h) in absolute pixels and perturbs crystal pidx[k]; T_out receives,
+// window after window, three planes of w*h doubles: base, +hstep, -hstep.
+int64_t or_scan_windows(const or_crystals* c, const or_emulsion_cfg* ecfg, const or_scan_cfg* scfg, uint64_t seed,
+                        int threads, const double* sigma_c, int64_t nwin, const uint32_t* win, const uint32_t* pidx,
+                        double hstep, double* T_out) {
+  const uint32_t W = scfg->width_px, H = scfg->height_px;
+  const uint32_t spp = std::max<uint32_t>(scfg->samples_per_pixel, 1);
+  const double pw = ecfg->width / static_cast<double>(W), ph = ecfg->height / static_cast<double>(H);
+  std::vector<Crystal> dev;
+  std::vector<size_t> orig;
+  for (size_t i = 0; i < c->n; ++i) {
+    Crystal k = load_crystal(c, i);
+    if (k.developed) {
+      dev.push_back(k);
+      orig.push_back(i);
+    }
+  }
+  RefBvh bvh;
+  bvh.build(dev);
+  const uint32_t g = static_cast<uint32_t>(std::round(std::sqrt(static_cast<double>(spp))));
+  const uint32_t a = std::max<uint32_t>(g * g, 1);
+  const int nt = threads > 0 ? threads : omp_get_max_threads();
+  size_t base = 0;
+  for (int64_t k = 0; k < nwin; ++k) {
+    const uint32_t x0 = win[4 * k], y0 = win[4 * k + 1], w = win[4 * k + 2], h = win[4 * k + 3];
+    const size_t np = static_cast<size_t>(w) * h;
+    double* tb = T_out + base;
+    double* tp = tb + np;
+    double* tm = tp + np;
+#pragma omp parallel num_threads(nt)
+    {
+      std::vector<Hit> hits;
+#pragma omp for schedule(dynamic, 1)
+      for (int64_t yy = 0; yy < static_cast<int64_t>(h); ++yy) {
+        for (uint32_t xx = 0; xx < w; ++xx) {
+          const uint32_t px = x0 + xx, py = y0 + static_cast<uint32_t>(yy);
+          double accb = 0.0, accp = 0.0, accm = 0.0;
+          for (uint32_t sy = 0; sy < g; ++sy)
+            for (uint32_t sx = 0; sx < g; ++sx) {
+              double tau = 0.0, lc = 0.0;
+              if (px < W && py < H && !dev.empty()) {
+                const V3 o = scan_origin(seed, px, py, sx, sy, g, pw, ph, ecfg->depth + 0.1);
+                ray_hits(bvh, dev, o, v3(0.0, 0.0, -1.0), OR_FAITHFUL, hits);
+                for (const Hit& hh : hits) {
+                  const double chord = rmax(hh.t1 - hh.t0, 0.0);
+                  tau += (sigma_c ? sigma_c[orig[hh.idx]] : scfg->silver_opacity) * chord;
+                  if (orig[hh.idx] == pidx[k]) lc += chord;
+                }
+              }
+              accb += std::exp(-tau);
+              accp += std::exp(-(tau + hstep * lc));
+              accm += std::exp(-(tau - hstep * lc));
+            }
+          const size_t i = static_cast<size_t>(yy) * w + xx;
+          tb[i] = accb / static_cast<double>(a);
+          tp[i] = accp / static_cast<double>(a);
+          tm[i] = accm / static_cast<double>(a);
+        }
+      }
+    }
+    base += 3 * np;
+  }
+  return static_cast<int64_t>(base);
+}
+
 // ---- differentiable scan and its adjoint (FP64) ----
 
 void or_otf_taps(double s, double taps[3], double dtaps[3]) {

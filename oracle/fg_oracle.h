@@ -130,6 +130,12 @@ int64_t or_query_radius(const or_crystals* c, const double center[3], double rad
                         uint32_t* out, int64_t cap);
 /* Statistics of the reference BVH over the set: node count, depth, and stack drops. */
 int or_bvh_stats(const or_crystals* c, int64_t* nodes, int64_t* depth);
+/* FP64 transmittance of pixel windows (x0, y0, w, h) of a scan with the reference's rule, each
+ * window under +-hstep on the opacity of crystal pidx[k]: three planes (base, plus, minus) per
+ * window.  The tree over the developed crystals is built once.  Returns the doubles written. */
+int64_t or_scan_windows(const or_crystals* c, const or_emulsion_cfg* ecfg, const or_scan_cfg* scfg, uint64_t seed,
+                        int threads, const double* sigma_c, int64_t nwin, const uint32_t* win, const uint32_t* pidx,
+                        double hstep, double* T_out);
 /* The reference tree (bvh.rs:157-295) over all crystals, or over the developed ones with their
  * expansion (the scan's tree): final index order (crystal indices) and the leaves in node order
  * (range in that order, box lo xyz hi xyz).  Returns the element count. */

@@ -446,6 +446,42 @@ def scan_backward(cr: Crystals, cfg, scfg, seed, dL_dS, sigma_c=None, exposure=1
     return gs, ge.value, go.value
 
 
+def scan_windows(cr: Crystals, cfg, scfg, seed, sigma_c, windows, pidx, hstep, threads=0):
+    """FP64 transmittance of pixel windows (x0, y0, w, h) under +-hstep on crystal pidx[k]'s opacity,
+    with the reference's rule and the tree over all developed crystals: a list of (base, plus,
+    minus) arrays of shape (h, w)."""
+    L = lib()
+    L.or_scan_windows.restype = C.c_int64
+    win = np.ascontiguousarray(np.array(windows, np.uint32).reshape(-1, 4))
+    pid = np.ascontiguousarray(np.array(pidx, np.uint32).reshape(-1))
+    total = int(sum(3 * int(w) * int(h) for _, _, w, h in win))
+    out = np.zeros(max(total, 1))
+    sig = None if sigma_c is None else np.ascontiguousarray(sigma_c, np.float64)
+    s = cr.struct()
+    L.or_scan_windows(C.byref(s), C.byref(emulsion_cfg(cfg)), C.byref(scan_cfg(scfg)), C.c_uint64(seed), threads,
+                      _p(sig, C.c_double), C.c_int64(len(win)), _p(win, C.c_uint32), _p(pid, C.c_uint32),
+                      C.c_double(hstep), _p(out, C.c_double))
+    res, base = [], 0
+    for _, _, w, h in win:
+        n = int(w) * int(h)
+        res.append(tuple(out[base + j * n: base + (j + 1) * n].reshape(int(h), int(w)) for j in range(3)))
+        base += 3 * n
+    return res
+
+
+def otf_image(field, s):
+    """The differentiable scan's OTF in FP64 (or_scan_signal's order: x pass, then y pass), taps of
+    otf_taps(s), clamp-to-edge."""
+    k, _ = otf_taps(s)
+    f = np.asarray(field, np.float64)
+    xm = np.concatenate([f[:, :1], f[:, :-1]], axis=1)
+    xp = np.concatenate([f[:, 1:], f[:, -1:]], axis=1)
+    t = xm * k[0] + f * k[1] + xp * k[2]
+    ym = np.concatenate([t[:1], t[:-1]], axis=0)
+    yp = np.concatenate([t[1:], t[-1:]], axis=0)
+    return ym * k[0] + t * k[1] + yp * k[2]
+
+
 def scan_ray_origins(cfg, scfg, seed):
     sc = scan_cfg(scfg)
     ec = emulsion_cfg(cfg)
@@ -619,9 +655,11 @@ def _oracle_stock(preset, push):
     return 0
 
 
-def film_render_bw(image, threads=0, **kw):
+def film_render_bw(image, threads=0, tile_fn=None, **kw):
     """render_film_black_and_white_tiled (image_pipeline.rs:299-891) on the CPU: a u8 gray image
-    (H, W) or an RGB8 image (H, W, 3) to a u8 gray image, every tile through or_render_tile."""
+    (H, W) or an RGB8 image (H, W, 3) to a u8 gray image, every tile through or_render_tile, or
+    through tile_fn(preset, grain_px, exposure, push, [(tile seed, exposure tile), ...]) -> densities
+    when given (a parity check can render the tiles elsewhere and keep this driver)."""
     opts = dict(FILM_DEFAULTS, **kw)
     img = np.ascontiguousarray(image, np.uint8)
     gray = img if img.ndim == 2 else luma(img, opts["preset"])
@@ -638,22 +676,39 @@ def film_render_bw(image, threads=0, **kw):
         out_w, out_h = res
     ss = min(max(opts["supersample"], 1), 4)
     if ss > 1:
-        big = film_render_bw(image, threads, **dict(opts, supersample=1, output_resolution=(out_w * ss, out_h * ss)))
+        big = film_render_bw(image, threads, tile_fn,
+                             **dict(opts, supersample=1, output_resolution=(out_w * ss, out_h * ss)))
         return resize_u8(big, out_w, out_h, TRIANGLE)
     src = gray if (in_w, in_h) == (out_w, out_h) else resize_u8(gray, out_w, out_h, LANCZOS3)
     heff, _ = gelatin_psf(src)
     grain, strength, push = film_scaling(opts, out_w, out_h)
     grid, step, pad = film_grid(out_w, out_h, grain, opts["tile_size"])
     stock = _oracle_stock(opts["preset"], push)
-    dens = []
-    for t in grid:
-        seed = film_tile_seed(opts["seed"], t)
-        tile = np.ascontiguousarray(heff[t.y_start:t.y_start + t.th, t.x_start:t.x_start + t.tw])
-        d, _ = render_tile(stock, 1.0 / grain, tile, opts["exposure"], opts["push"], seed, FAITHFUL, threads)
-        dens.append(d)
+    jobs = [(film_tile_seed(opts["seed"], t),
+             np.ascontiguousarray(heff[t.y_start:t.y_start + t.th, t.x_start:t.x_start + t.tw])) for t in grid]
+    if tile_fn is not None:
+        dens = tile_fn(opts["preset"], grain, opts["exposure"], opts["push"], jobs)
+    else:
+        dens = [render_tile(stock, 1.0 / grain, tile, opts["exposure"], opts["push"], seed, FAITHFUL, threads)[0]
+                for seed, tile in jobs]
     out, _ = film_finish(opts["preset"], grain, strength, push, opts["scanner_otf"], out_w, out_h, grid, step, pad,
                          dens, src, heff)
     return out
+
+
+COLOR_SEED_OFFSETS = (0, 10007, 20011)
+
+
+def film_render_color(rgb, threads=0, tile_fn=None, **kw):
+    """render_film_color_tiled (image_pipeline.rs:1017-1085): the R, G and B channels as three
+    black-and-white runs with seeds seed, seed + 10007, seed + 20011 (wrapping), interleaved."""
+    opts = dict(FILM_DEFAULTS, **kw)
+    img = np.ascontiguousarray(rgb, np.uint8)
+    layers = []
+    for c, off in enumerate(COLOR_SEED_OFFSETS):
+        o = dict(opts, seed=(opts["seed"] + off) & 0xFFFFFFFFFFFFFFFF)
+        layers.append(film_render_bw(np.ascontiguousarray(img[..., c]), threads, tile_fn, **o))
+    return np.stack(layers, -1)
 
 
 # ---- the reference's wgpu tile model (fg_oracle_fast.cpp) ----

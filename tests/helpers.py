@@ -52,3 +52,11 @@ REFERENCE_PRESETS = {
 def reference_cfg(name, w, h):
     d, r, m, v, mo, ar, o, s = REFERENCE_PRESETS[name]
     return fg.EmulsionConfig((w, h, d), r, m, v, fg.Morphology(mo), ar, fg.GelatinOptics(*o), s)
+
+
+def tile_cfg(p):
+    """The emulsion configuration a tile's parameters describe (the stock the tile worker selected
+    for its push, on the tile's film box)."""
+    o = fg.GelatinOptics(*[getattr(p.optics, k) for k, _ in p.optics._fields_])
+    return fg.EmulsionConfig((p.film_w, p.film_h, p.film_d), p.r_min, p.mean_crystal_radius, p.size_variance,
+                             fg.Morphology(p.morphology), p.tabular_aspect_ratio, o, p.base_sensitivity)

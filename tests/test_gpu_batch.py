@@ -5,7 +5,7 @@ import pytest
 
 import fgrain_gb300 as fg
 from oracle import oracle as orc
-from tests.helpers import reference_cfg
+from tests.helpers import reference_cfg, tile_cfg
 
 pytestmark = pytest.mark.gpu
 
@@ -92,10 +92,13 @@ def test_tabular_synthesis(engine):
     assert (c["morphology"] == 1).all()
 
 
-def test_pipeline_matches_oracle_on_the_same_crystals(engine):
+@pytest.mark.parametrize("stock,grain,expo,push", [("tri-x", 2.4, 1.0, 0.0), ("t-max", 1.1, 3.0, 2.0),
+                                                   ("hp5", 1.8, 1.0, 2.0)])
+def test_pipeline_matches_oracle_on_the_same_crystals(engine, stock, grain, expo, push):
     """The device's own synthesized crystals pushed through the oracle's expose / develop / scan
-    reproduce the device tile: counts and the developed mask nearly everywhere, density to 1e-5."""
-    p = fg.tile_params("tri-x", 1 / 2.4, 96, 80, 1.0, 0.0, 21)
+    reproduce the device tile: counts and the developed mask nearly everywhere, density to 1e-5.
+    Each stock with its own tile-worker settings (exposure multiplier, push)."""
+    p = fg.tile_params(stock, 1 / grain, 96, 80, expo, push, 21)
     tile = ramp(80, 96)
     b = fg.Batch([p], engine)
     b.set_exposure([tile])
@@ -103,23 +106,28 @@ def test_pipeline_matches_oracle_on_the_same_crystals(engine):
     st = b.wait()
     d_dev = b.density()[0]
     c = b.tile_crystals(0)
-    cfg = reference_cfg("tri-x", p.film_w, p.film_h)
+    cfg = tile_cfg(p)
+    dcfg = fg.DevelopmentConfig(p.threshold_photons, p.filament_expansion, p.clumping_proximity_factor, 0.85)
     cr = orc.Crystals(c["pos"], c["dims"], c["quat"], c["sensitivity"], c["morphology"])
     # The batch's development totals against the oracle's development of the device's own counts.
     crd = cr.copy()
     crd.latent[:] = c["counts"]
-    rd = orc.develop(crd, fg.DevelopmentConfig(4, p.filament_expansion, p.clumping_proximity_factor, 0.85))
+    rd = orc.develop(crd, dcfg)
     assert st["developed"] == int(c["developed"].sum()) == rd["developed_crystals"] > 100
     assert st["clumps"] == rd["total_clumps"]
-    orc.expose(cr, cfg, tile, fg.ExposureConfig(6.0, 0.12, 1.3, 48), p.seed + 1, orc.FAITHFUL)
+    np.testing.assert_array_equal(crd.developed, c["developed"])
+    np.testing.assert_allclose(crd.expansion, c["expansion"], rtol=1e-6)
+    ecfg = fg.ExposureConfig(p.photons_per_sq_um * max(expo, 0.05), p.illumination_angle_rad,
+                             p.crystal_absorption_coeff, p.max_bounces)
+    orc.expose(cr, cfg, tile, ecfg, p.seed + 1, orc.FAITHFUL)
     same = (cr.latent == c["counts"]).mean()
     assert same > 0.99, same
-    orc.develop(cr, fg.DevelopmentConfig(4, p.filament_expansion, p.clumping_proximity_factor, 0.85))
+    orc.develop(cr, dcfg)
     # Scan the device's developed mask with the oracle: isolates the scan stage.
     cr2 = cr.copy()
     cr2.developed[:] = c["developed"]
     cr2.expansion[:] = c["expansion"]
-    r = orc.scan(cr2, cfg, fg.ScanConfig(96, 80, 4, 0, 0.25), p.seed + 2)
+    r = orc.scan(cr2, cfg, fg.ScanConfig(96, 80, p.samples_per_pixel, 0, p.silver_opacity), p.seed + 2)
     T_orc = np.clip(r["T64"], 1e-4, 1.0)  # the density conversion clamps T (image_pipeline.rs:1009)
     d_orc = (-np.log10(T_orc) + 0.05).astype(np.float32)
     T_dev = 10.0 ** (-(d_dev.astype(np.float64) - 0.05))

@@ -59,20 +59,40 @@ def test_reference_arm_runs_on_rank_zero_only():
 
 
 def test_reference_arm_line_shape(monkeypatch):
-    """The reference arm's JSON line on a tiny sample (the oracle timing itself is patched out)."""
+    """The reference arm's JSON line on a tiny photograph (the oracle's tile renders patched out)."""
     sys.path.insert(0, str(ROOT))
+    import numpy as np
     import bench
 
-    monkeypatch.setattr(bench, "oracle_sample", lambda params, tiles, n, threads: (2.0, 4 * 384 * 384))
+    seen = []
+    monkeypatch.setattr(bench, "oracle_tiles",
+                        lambda jobs, threads: (seen.extend(jobs), (2.0, [np.zeros_like(j[2]) for j in jobs]))[1])
     lines = []
     monkeypatch.setattr("builtins.print", lambda s, *a, **k: lines.append(s))
 
     class A:
-        steps, warmup, gpus = 2, 1, 2
+        steps, warmup, gpus, film_side = 2, 1, 2, 64
 
     monkeypatch.setenv("RANK", "0")
     bench.run_reference(A())
     d = json.loads(lines[-1])
     assert d["impl"] == "reference" and d["unit"] == "Mpx/s" and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
-    assert d["n_gpus"] == 2 and d["config"]["workload"].startswith(bench.C2_WORKLOAD)
+    assert d["n_gpus"] == 2 and d["config"]["workload"].startswith(bench.C4_WORKLOAD)
+    assert d["steps"] == 2 and d["warmup"] == 1 and len(seen) == 1 + 4 * 2  # one tile per warm-up step
+    assert all(j[0] == "t-max" and abs(j[1] - 1 / 1.1) < 1e-15 for j in seen)
+
+
+def test_reference_arm_imports_nothing_of_the_product():
+    """The reference arm runs the oracle only: after a (tiny, patched) run no module of the
+    product package is loaded in the process."""
+    code = (
+        "import sys, numpy as np; sys.path.insert(0, %r); import bench\n"
+        "bench.oracle_tiles = lambda jobs, threads: (1.0, [np.zeros_like(j[2]) for j in jobs])\n"
+        "class A: steps, warmup, gpus, film_side = 1, 0, 1, 64\n"
+        "bench.run_reference(A())\n"
+        "print(sorted(m for m in sys.modules if m.startswith('fgrain_gb300')))\n" % str(ROOT))
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.strip().splitlines()[-1] == "[]"
