@@ -128,15 +128,15 @@ struct RTreeBufs {
   uint32_t count = 0;             // elements of a one-tile tree built on the host's request
   DBuf<RTile> tiles;
   DBuf<uint32_t> idx0, idx1, nof0, nof1, flag, bb, blk, P, Q;
-  DBuf<double4> pm0, pm1;         // element position and half-size, travelling with the order
+  DBuf<double4_32a> pm0, pm1;         // element position and half-size, travelling with the order
   DBuf<uint32_t> ridx;            // final element order (slots): a leaf's crystals in reference order
   DBuf<unsigned long long> acc;   // per node: 6 ordered minima, 6 ordered maxima
   DBuf<double> box64;             // per node: lo xyz, hi xyz (FP64, exact)
-  DBuf<uint32_t> nstart, ncount, nK, nS, ntile, ndepth;
+  DBuf<uint32_t> nstart, ncount, ntile, ndepth;
   DBuf<int> nsplit;               // split axis, -1 for a leaf
   DBuf<double> nmid;
   DBuf<int2> nchild;              // global ids of the children
-  DBuf<uint32_t> wl0, wl1, wq, wqpar, cnt;
+  DBuf<uint32_t> wl0, wl1, bq, bqpar, cnt;  // global worklists, block queue (node, buffer parity), counts
   DBuf<Node> rnode;               // walk records (tile-local refs)
   DBuf<uint2> rleaf;              // leaf: first element (tile-local position), count
   DBuf<uint32_t> leafof;          // optional: leaf id of each element slot

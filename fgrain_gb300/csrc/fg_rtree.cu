@@ -9,8 +9,9 @@
 //   pq      P_m = position of the m-th big from the left, Q_m = of the m-th small from the right;
 //   place   every element moves to where the reference's swap partition puts it (below).
 // Each element's position and half-size (FP64) travel with it, so every pass reads them in order.
-// Nodes of at most 32 elements are then finished by one warp each with the same arithmetic on
-// ballots.
+// Nodes of at most RT_CTA_MAX elements leave the global levels: one thread block each builds
+// their subtree with the elements in shared memory, the same passes per level, all levels down to
+// the leaves.  Node boxes are reduced segment-wise (a node is a contiguous range of positions).
 //
 // The swap partition (bvh.rs:244-258: i from the left, j from the right; a small at i stays and i
 // advances, a big at i is swapped with j and j retreats) examines the range as two streams: the
@@ -38,11 +39,12 @@ namespace {
 
 constexpr unsigned RT_BLOCK = 256;
 
-// Global split levels for trees of up to emax elements: halving down to the per-warp size, plus a
+// Global split levels for trees of up to emax elements: halving down to the per-block size, plus a
 // wide margin for uneven splits (unused levels cost only launches that find no work).
 int levels_for(uint32_t emax) {
-  int lv = 1;
-  while ((static_cast<unsigned long long>(RT_WARP_MAX) << lv) < std::max<unsigned long long>(emax, 1)) ++lv;
+  if (emax <= static_cast<uint32_t>(RT_CTA_MAX)) return 0;
+  int lv = 0;
+  while ((static_cast<unsigned long long>(RT_CTA_MAX) << lv) < emax) ++lv;
   return std::min(lv + 8, 44);
 }
 
@@ -66,30 +68,12 @@ __device__ __forceinline__ int rt_tile_of(const RTile* tiles, int ntiles, unsign
   return lo;
 }
 
-// Position of the k-th (0-based) set bit of m, counting from bit 0 (k < popc(m)).
-__device__ __forceinline__ int nth_bit(unsigned m, int k) {
-  int pos = 0;
-#pragma unroll
-  for (int w = 16; w >= 1; w >>= 1) {
-    const unsigned lo = m & ((1u << w) - 1u);
-    const int c = __popc(lo);
-    if (k >= c) {
-      k -= c;
-      m >>= w;
-      pos += w;
-    } else {
-      m = lo;
-    }
-  }
-  return pos;
-}
-
 struct RtArgs {
   RTile* tiles;
   int ntiles;
   unsigned long long E, N;
   uint32_t* idx[2];
-  double4* pm[2];  // position xyz and half-size (max_dim * expansion) of the element, in FP64
+  double4_32a* pm[2];  // position xyz and half-size (max_dim * expansion) of the element, in FP64
   uint32_t* nof[2];
   uint32_t* flag;
   uint32_t* bb;
@@ -99,14 +83,14 @@ struct RtArgs {
   uint32_t* ridx;
   unsigned long long* acc;
   double* box64;
-  uint32_t *nstart, *ncount, *nK, *nS, *ntile, *ndepth;
+  uint32_t *nstart, *ncount, *ntile, *ndepth;
   int* nsplit;
   double* nmid;
   int2* nchild;
   uint32_t* wl[2];
-  uint32_t* wq;     // warp queue: node ids
-  uint32_t* wqpar;  // and the buffer parity holding their elements
-  uint32_t* cnt;    // [0], [1] worklist counts, [2] warp queue count
+  uint32_t* bq;     // block queue: nodes of at most RT_CTA_MAX elements
+  uint32_t* bqpar;  // and the buffer parity holding their elements
+  uint32_t* cnt;    // [0], [1] worklist counts, [2] block queue count
   uint32_t* err;
 };
 
@@ -120,15 +104,21 @@ __device__ __forceinline__ bool alloc_pair(const RtArgs& A, int t, uint32_t& l) 
   return true;
 }
 
-__global__ void k_rt_clear(RtArgs A) {
-  for (unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; i < A.N;
-       i += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+// Hands a new node of n elements (held in buffer `par`) to the phase that builds it: the global
+// levels (more than RT_CTA_MAX elements; its box accumulators start empty) or one block.
+__device__ __forceinline__ void rt_enqueue(const RtArgs& A, uint32_t id, uint32_t n, int par) {
+  A.nsplit[id] = -1;
+  if (n > static_cast<uint32_t>(RT_CTA_MAX)) {
+    unsigned long long* a = A.acc + 12ull * id;
 #pragma unroll
-    for (int k = 0; k < 6; ++k) A.acc[12 * i + k] = ~0ull;        // minima
+    for (int k = 0; k < 6; ++k) a[k] = ~0ull;  // minima
 #pragma unroll
-    for (int k = 6; k < 12; ++k) A.acc[12 * i + k] = 0ull;        // maxima
-    A.nsplit[i] = -1;
-    A.nK[i] = 0;
+    for (int k = 6; k < 12; ++k) a[k] = 0ull;  // maxima
+    A.wl[par][atomicAdd(&A.cnt[par], 1u)] = id;
+  } else if (n > 0) {
+    const uint32_t q = atomicAdd(&A.cnt[2], 1u);
+    A.bq[q] = id;
+    A.bqpar[q] = static_cast<uint32_t>(par);
   }
 }
 
@@ -145,7 +135,7 @@ __global__ void k_rt_init(RtArgs A) {
       const uint32_t slot = T.order ? static_cast<uint32_t>(T.order[k] - T.obase) : static_cast<uint32_t>(k);
       A.idx[0][x] = slot;
       A.pm[0][x] = rt_pm(T, slot);
-      v = T.n > static_cast<uint32_t>(RT_WARP_MAX) ? static_cast<uint32_t>(T.nbase + 1) : RT_DONE;
+      v = T.n > static_cast<uint32_t>(RT_CTA_MAX) ? static_cast<uint32_t>(T.nbase + 1) : RT_DONE;
     }
     A.nof[0][x] = v;
   }
@@ -158,20 +148,14 @@ __global__ void k_rt_init(RtArgs A) {
     A.ncount[root] = T.n;
     A.ntile[root] = static_cast<uint32_t>(t);
     A.ndepth[root] = 1;
-    if (T.n > static_cast<uint32_t>(RT_WARP_MAX)) {
-      A.wl[0][atomicAdd(&A.cnt[0], 1u)] = static_cast<uint32_t>(root);
-    } else if (T.n > 0) {
-      const uint32_t q = atomicAdd(&A.cnt[2], 1u);
-      A.wq[q] = static_cast<uint32_t>(root);
-      A.wqpar[q] = 0;
-    }
+    rt_enqueue(A, static_cast<uint32_t>(root), T.n, 0);
   }
 }
 
 // The 12 ordered keys of element slot s: box lo xyz and centroid xyz (minima), box hi xyz and
 // centroid xyz (maxima).  Min and max are exact in any order, and on the ordered 64-bit keys they
 // run on the integer pipes (GB300's FP64 pipe is narrow).
-__device__ __forceinline__ void rt_keys(const double4& v, unsigned long long k[12]) {
+__device__ __forceinline__ void rt_keys(const double4_32a& v, unsigned long long k[12]) {
   double lo[3], hi[3], cc[3];
   rt_box_pm(v, lo, hi, cc);
 #pragma unroll
@@ -186,57 +170,49 @@ __device__ __forceinline__ void rt_keys(const double4& v, unsigned long long k[1
 __device__ __forceinline__ unsigned long long umin64(unsigned long long a, unsigned long long b) { return a < b ? a : b; }
 __device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) { return a > b ? a : b; }
 
-// Box and centroid box of every pending node: a warp whose lanes all hold one node reduces by a
-// butterfly, other warps per group of equal nodes; one set of 12 atomics per warp and node.
+// Segment-wise reduction over a warp's 32 consecutive positions: lanes with equal `seg` form
+// contiguous runs (a node is a contiguous range of positions, so equal values at two lanes mean
+// the same node in between).  On return the first lane of each run holds the run's minima
+// (k[0..5]) and maxima (k[6..11]); the return value says whether this lane is a run's first.
+// Lanes without a node pass a seg value no other lane has.
+__device__ __forceinline__ bool rt_seg_reduce(uint32_t seg, unsigned long long k[12]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t ns = __shfl_down_sync(0xffffffffu, seg, o);
+    const bool take = lane + o < 32 && ns == seg;
+#pragma unroll
+    for (int i = 0; i < 12; ++i) {
+      const unsigned long long y = __shfl_down_sync(0xffffffffu, k[i], o);
+      if (take) k[i] = i < 6 ? umin64(k[i], y) : umax64(k[i], y);
+    }
+  }
+  const uint32_t up = __shfl_up_sync(0xffffffffu, seg, 1);
+  return lane == 0 || up != seg;
+}
+
+__device__ __forceinline__ void rt_keys_empty(unsigned long long k[12]) {
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    k[i] = ~0ull;
+    k[6 + i] = 0ull;
+  }
+}
+
+// Box and centroid box of every pending node: segment-wise per warp, then one set of 12 atomics
+// per warp and node.
 __global__ void k_rt_reduce(RtArgs A, int c) {
   if (A.cnt[c] == 0) return;
   const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
   for (unsigned long long base = blockIdx.x * static_cast<unsigned long long>(blockDim.x); base < A.E; base += stride) {
     const unsigned long long x = base + threadIdx.x;
-    uint32_t node = RT_DONE;
-    unsigned long long k[12];
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-      k[i] = ~0ull;
-      k[6 + i] = 0ull;
-    }
-    if (x < A.E) {
-      node = A.nof[c][x];
-      if (!(node & RT_DONE)) rt_keys(A.pm[c][x], k);
-    }
-    const uint32_t n0 = __shfl_sync(0xffffffffu, node, 0);
-    if (__all_sync(0xffffffffu, node == n0)) {
-      if (n0 & RT_DONE) continue;
-#pragma unroll
-      for (int i = 0; i < 12; ++i)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const unsigned long long y = __shfl_xor_sync(0xffffffffu, k[i], o);
-          k[i] = i < 6 ? umin64(k[i], y) : umax64(k[i], y);
-        }
-      if ((threadIdx.x & 31) == 0) {
-        unsigned long long* a = A.acc + 12ull * node;
-#pragma unroll
-        for (int i = 0; i < 6; ++i) atomicMin(a + i, k[i]);
-#pragma unroll
-        for (int i = 6; i < 12; ++i) atomicMax(a + i, k[i]);
-      }
-      continue;
-    }
+    const uint32_t node = x < A.E ? A.nof[c][x] : RT_DONE;
     const bool act = !(node & RT_DONE);
-    const unsigned m = __ballot_sync(0xffffffffu, act);
-    if (!act) continue;
-    const unsigned grp = __match_any_sync(m, node);
-#pragma unroll
-    for (int i = 0; i < 12; ++i) {
-      unsigned long long r = k[i];
-      for (unsigned q = grp; q; q &= q - 1) {
-        const unsigned long long y = __shfl_sync(grp, k[i], __ffs(q) - 1);
-        r = i < 6 ? umin64(r, y) : umax64(r, y);
-      }
-      k[i] = r;
-    }
-    if (static_cast<int>(threadIdx.x & 31) == __ffs(grp) - 1) {
+    if (!__any_sync(0xffffffffu, act)) continue;
+    unsigned long long k[12];
+    if (act) rt_keys(A.pm[c][x], k); else rt_keys_empty(k);
+    const bool head = rt_seg_reduce(act ? node : (RT_DONE | (threadIdx.x & 31)), k);
+    if (act && head) {
       unsigned long long* a = A.acc + 12ull * node;
 #pragma unroll
       for (int i = 0; i < 6; ++i) atomicMin(a + i, k[i]);
@@ -314,7 +290,7 @@ __device__ __forceinline__ uint32_t rt_flag(const RtArgs& A, int c, unsigned lon
   if (node & RT_DONE) return 0u;
   const int axis = A.nsplit[node];
   if (axis < 0) return 0u;
-  const double4 v = A.pm[c][x];
+  const double4_32a v = A.pm[c][x];
   const double p = axis == 0 ? v.x : (axis == 1 ? v.y : v.z);
   const double cc = __dmul_rn(0.5, __dadd_rn(__dsub_rn(p, v.w), __dadd_rn(p, v.w)));
   return cc < A.nmid[node] ? 0u : 1u;
@@ -394,7 +370,6 @@ __global__ void k_rt_pq(RtArgs A, int c) {
       const uint32_t mr = St - (r - Bb);  // right rank, 1-based
       A.Q[s + mr - 1] = r;
     }
-    if (r == 0) A.nS[node] = St;
   }
 }
 
@@ -437,24 +412,19 @@ __global__ void k_rt_place(RtArgs A, int c) {
     const uint32_t csize = left ? Sp : n - Sp;
     A.idx[o][s + dest] = el;
     A.pm[o][s + dest] = A.pm[c][x];
-    A.nof[o][s + dest] = csize > static_cast<uint32_t>(RT_WARP_MAX) ? child : RT_DONE;
+    A.nof[o][s + dest] = csize > static_cast<uint32_t>(RT_CTA_MAX) ? child : RT_DONE;
     if (r == 0) {
       const uint32_t t = A.ntile[node], dep = A.ndepth[node] + 1;
       const uint32_t cs[2] = {Sp, n - Sp};
       const uint32_t cid[2] = {static_cast<uint32_t>(ch.x), static_cast<uint32_t>(ch.y)};
+#pragma unroll
       for (int k = 0; k < 2; ++k) {
         const uint32_t id = cid[k];
         A.nstart[id] = s + (k ? Sp : 0u);
         A.ncount[id] = cs[k];
         A.ntile[id] = t;
         A.ndepth[id] = dep;
-        if (cs[k] > static_cast<uint32_t>(RT_WARP_MAX)) {
-          A.wl[o][atomicAdd(&A.cnt[o], 1u)] = id;
-        } else {
-          const uint32_t q = atomicAdd(&A.cnt[2], 1u);
-          A.wq[q] = id;
-          A.wqpar[q] = static_cast<uint32_t>(o);
-        }
+        rt_enqueue(A, id, cs[k], o);
       }
       atomicMax(&A.tiles[t].depth, dep);
     }
@@ -470,137 +440,305 @@ __global__ void k_rt_check(RtArgs A, int c) {
   if (A.cnt[c] != 0) atomicOr(A.err, ERR_LIST_OVERFLOW);  // nodes left after the last level
 }
 
-// One warp finishes one node of at most 32 elements: the same splits, with the swap partition
-// evaluated on ballots, children processed from a per-warp stack.
-constexpr int RT_WARPS = 4;
-__global__ void __launch_bounds__(32 * RT_WARPS) k_rt_warp(RtArgs A) {
-  __shared__ int stk[RT_WARPS][32][4];
-  __shared__ int src[RT_WARPS][32];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+// The block queue: one block builds the whole subtree of a node of at most RT_CTA_MAX elements
+// with its elements in shared memory.  Each level runs the passes of the global levels over all
+// of the level's nodes of more than RT_LEAF_MAX elements at once (segment-wise reduce, decide,
+// flags and prefix sum, ranks, place); a child of at most RT_LEAF_MAX elements is a leaf
+// (bvh.rs:200-204) whose box one thread takes at the start of the next level.
+constexpr int RT_CTA_T = 256;                                // threads per block
+constexpr int RT_CTA_PER = RT_CTA_MAX / RT_CTA_T;            // positions per thread
+constexpr int RT_LEAF_MAX = 4;                               // subdivide's leaf size
+constexpr int RT_CTA_LV = RT_CTA_MAX / (RT_LEAF_MAX + 1);    // nodes of more than 4 per level (204)
+constexpr int RT_CTA_SL = 2 * RT_CTA_LV;                     // leaves of at most 4 made by one level
+constexpr uint8_t RT_CTA_FREE = 0xff;                        // position of a finished range
+static_assert(RT_CTA_LV < RT_CTA_FREE, "level slots must fit a byte");
+static_assert(RT_CTA_MAX <= 2048, "positions are packed in 11 bits");
+
+struct RtCtaSmem {
+  double4_32a pm[RT_CTA_MAX];                 // element position and half-size
+  unsigned long long acc[RT_CTA_LV][12];  // per level node: ordered minima, maxima
+  double mid[RT_CTA_LV];
+  uint32_t idx[RT_CTA_MAX];               // element slot
+  uint32_t id[2][RT_CTA_LV];              // this level's nodes and the next's
+  uint32_t child[RT_CTA_LV];              // first child id of a splitting node
+  uint32_t sl[RT_CTA_SL];                 // small leaves: position | count << 11 | depth << 14
+  uint32_t slid[RT_CTA_SL];
+  uint32_t scan[RT_CTA_T / 32];
+  uint16_t bb[RT_CTA_MAX + 1];            // exclusive prefix sum of the flags
+  uint16_t P[RT_CTA_MAX], Q[RT_CTA_MAX];
+  uint16_t off[2][RT_CTA_LV], cnt[2][RT_CTA_LV];
+  uint16_t sp[RT_CTA_LV];                 // left child size
+  uint8_t nd[RT_CTA_MAX];                 // level slot of the position's node, RT_CTA_FREE when done
+  uint8_t flag[RT_CTA_MAX];
+  uint8_t dep[2][RT_CTA_LV];
+  uint8_t cslot[RT_CTA_LV][2];            // next-level slot of each child, RT_CTA_FREE for a small leaf
+  int8_t axis[RT_CTA_LV];
+  int nl, nsl, nnext, nslnew;
+  uint32_t maxdep;
+};
+
+__global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
+  extern __shared__ __align__(32) unsigned char rt_cta_raw[];
+  RtCtaSmem& S = *reinterpret_cast<RtCtaSmem*>(rt_cta_raw);
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const uint32_t nq = A.cnt[2];
-  for (uint32_t q = blockIdx.x * RT_WARPS + w; q < nq; q += gridDim.x * RT_WARPS) {
-    const uint32_t root = A.wq[q], par = A.wqpar[q];
-    const uint32_t s = A.nstart[root], n = A.ncount[root];
+  for (uint32_t q = blockIdx.x; q < nq; q += gridDim.x) {
+    const uint32_t root = A.bq[q], par = A.bqpar[q];
+    const uint32_t s = A.nstart[root];
+    const int n = static_cast<int>(min(A.ncount[root], static_cast<uint32_t>(RT_CTA_MAX)));
     const uint32_t t = A.ntile[root];
-    const RTile& T = A.tiles[t];
-    uint32_t el = 0;
-    unsigned long long key[12];  // the element's ordered keys (rt_keys)
-#pragma unroll
-    for (int i = 0; i < 12; ++i) key[i] = 0;
-    if (static_cast<uint32_t>(lane) < n) {
-      el = A.idx[par][s + lane];
-      rt_keys(A.pm[par][s + lane], key);
+    const unsigned long long nb = A.tiles[t].nbase;
+    const uint32_t dep0 = min(A.ndepth[root], 255u);
+    for (int x = tid; x < RT_CTA_MAX; x += RT_CTA_T) {
+      if (x < n) {
+        S.pm[x] = A.pm[par][s + x];
+        S.idx[x] = A.idx[par][s + x];
+        S.nd[x] = n > RT_LEAF_MAX ? 0 : RT_CTA_FREE;
+      } else {
+        S.nd[x] = RT_CTA_FREE;
+      }
     }
-    int sp = 0;
-    if (lane == 0) {
-      stk[w][0][0] = 0;
-      stk[w][0][1] = static_cast<int>(n);
-      stk[w][0][2] = static_cast<int>(root);
-      stk[w][0][3] = static_cast<int>(A.ndepth[root]);
+    if (tid == 0) {
+      S.maxdep = 0;
+      if (n > RT_LEAF_MAX) {
+        S.nl = 1;
+        S.nsl = 0;
+        S.id[0][0] = root;
+        S.off[0][0] = 0;
+        S.cnt[0][0] = static_cast<uint16_t>(n);
+        S.dep[0][0] = static_cast<uint8_t>(dep0);
+      } else {
+        S.nl = 0;
+        S.nsl = 1;
+        S.sl[0] = static_cast<uint32_t>(n) << 11 | dep0 << 14;
+        S.slid[0] = root;
+      }
     }
-    sp = 1;
-    __syncwarp();
-    uint32_t maxdep = 0;
-    while (sp > 0) {
-      --sp;
-      const int off = stk[w][sp][0], cnt = stk[w][sp][1], id = stk[w][sp][2], dep = stk[w][sp][3];
-      __syncwarp();
-      maxdep = max(maxdep, static_cast<uint32_t>(dep));
-      const bool in = lane >= off && lane < off + cnt;
-      unsigned long long u[12];
+    __syncthreads();
+    int cur = 0;
+    for (;;) {
+      const int nl = S.nl, nsl = S.nsl;
+      // Leaves of at most four elements made by the previous level (or a small root).
+      for (int i = tid; i < nsl; i += RT_CTA_T) {
+        const uint32_t e = S.sl[i], id = S.slid[i];
+        const int o0 = static_cast<int>(e & 2047u), cn = static_cast<int>((e >> 11) & 7u);
+        const uint32_t dp = e >> 14;
+        unsigned long long k[12], kk[12];
+        rt_keys_empty(k);
+        for (int j = 0; j < cn; ++j) {
+          rt_keys(S.pm[o0 + j], kk);
 #pragma unroll
-      for (int k = 0; k < 12; ++k) u[k] = in ? key[k] : (k < 6 ? ~0ull : 0ull);
-#pragma unroll
-      for (int k = 0; k < 12; ++k)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const unsigned long long y = __shfl_xor_sync(0xffffffffu, u[k], o);
-          u[k] = k < 6 ? umin64(u[k], y) : umax64(u[k], y);
+          for (int m = 0; m < 6; ++m) {
+            k[m] = umin64(k[m], kk[m]);
+            k[6 + m] = umax64(k[6 + m], kk[6 + m]);
+          }
         }
-      double v[12];
 #pragma unroll
-      for (int k = 0; k < 12; ++k) v[k] = unord64(u[k]);
-      if (lane == 0) {
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          A.box64[6ull * id + k] = v[k];
-          A.box64[6ull * id + 3 + k] = v[6 + k];
+        for (int m = 0; m < 3; ++m) {
+          A.box64[6ull * id + m] = unord64(k[m]);
+          A.box64[6ull * id + 3 + m] = unord64(k[6 + m]);
         }
-        A.nstart[id] = s + static_cast<uint32_t>(off);
-        A.ncount[id] = static_cast<uint32_t>(cnt);
+        A.nstart[id] = s + static_cast<uint32_t>(o0);
+        A.ncount[id] = static_cast<uint32_t>(cn);
+        A.ntile[id] = t;
+        A.ndepth[id] = dp;
+        A.nsplit[id] = -1;
+        atomicMax(&S.maxdep, dp);
       }
-      const double ex = __dsub_rn(v[9], v[3]), ey = __dsub_rn(v[10], v[4]), ez = __dsub_rn(v[11], v[5]);
-      const int axis = (ex >= ey && ex >= ez) ? 0 : (ey >= ez ? 1 : 2);
-      const double ext = axis == 0 ? ex : (axis == 1 ? ey : ez);
-      uint32_t l = 0;
-      bool split = cnt > 4 && ext > 1e-7;
-      if (split) {
-        if (lane == 0) split = alloc_pair(A, static_cast<int>(t), l);
-        split = __shfl_sync(0xffffffffu, split ? 1 : 0, 0) != 0;
-        l = __shfl_sync(0xffffffffu, l, 0);
+      for (int i = tid; i < nl * 12; i += RT_CTA_T) S.acc[i / 12][i % 12] = (i % 12) < 6 ? ~0ull : 0ull;
+      __syncthreads();
+      if (nl == 0) break;
+      if (tid == 0) {
+        S.nnext = 0;
+        S.nslnew = 0;
       }
-      if (!split) {
-        if (lane == 0) A.nsplit[id] = -1;
-        continue;
+      // Reduce: position x = k * RT_CTA_T + tid, so a warp holds 32 consecutive positions.
+#pragma unroll 1
+      for (int k = 0; k < RT_CTA_PER; ++k) {
+        const int x = k * RT_CTA_T + tid;
+        const uint32_t node = S.nd[x];
+        const bool act = node != RT_CTA_FREE;
+        if (!__any_sync(0xffffffffu, act)) continue;
+        unsigned long long kk[12];
+        if (act) rt_keys(S.pm[x], kk); else rt_keys_empty(kk);
+        const bool head = rt_seg_reduce(act ? node : (0x100u | static_cast<uint32_t>(lane)), kk);
+        if (act && head) {
+#pragma unroll
+          for (int i = 0; i < 6; ++i) atomicMin(&S.acc[node][i], kk[i]);
+#pragma unroll
+          for (int i = 6; i < 12; ++i) atomicMax(&S.acc[node][i], kk[i]);
+        }
       }
-      const double mid = __dmul_rn(0.5, __dadd_rn(axis == 0 ? v[3] : (axis == 1 ? v[4] : v[5]),
-                                                  axis == 0 ? v[9] : (axis == 1 ? v[10] : v[11])));
-      const double ca = unord64(axis == 0 ? key[3] : (axis == 1 ? key[4] : key[5]));
-      const bool big = in && !(ca < mid);
-      const unsigned rng = (cnt == 32 ? 0xffffffffu : ((1u << cnt) - 1u)) << off;
-      const unsigned bm = __ballot_sync(0xffffffffu, big) & rng;
-      const unsigned sm_ = rng & ~bm;
-      const int Bt = __popc(bm), St = cnt - Bt;
-      const int r = lane - off;
-      const int Bb = __popc(bm & ((1u << lane) - 1u));
-      // P_m = nth_bit(bm, m - 1) - off; Q_m = nth_bit(sm_, St - m) - off.
-      bool pred = false;
-      if (big) {
-        const int m = Bb + 1;
-        pred = m <= St && r < nth_bit(sm_, St - m) - off;
-      }
-      const int K = __popc(__ballot_sync(0xffffffffu, pred));
-      const int QK = K >= 1 ? nth_bit(sm_, St - K) - off : cnt;
-      const bool hasP = K + 1 <= Bt;
-      const int PK1 = hasP ? nth_bit(bm, K) - off : cnt;
-      const int li = (hasP && PK1 < QK) ? PK1 + 1 : QK;
-      int dest = r;
-      if (in) {
-        if (r < li) {
-          dest = big ? ((Bb == 0 ? cnt : nth_bit(sm_, St - Bb) - off) - 1) : r;
+      __syncthreads();
+      // Decide (subdivide, bvh.rs:200-270), one thread per node of the level.
+      for (int i = tid; i < nl; i += RT_CTA_T) {
+        const uint32_t id = S.id[cur][i];
+        const int cn = S.cnt[cur][i];
+        double lo[3], hi[3], clo[3], chi[3];
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+          lo[m] = unord64(S.acc[i][m]);
+          clo[m] = unord64(S.acc[i][3 + m]);
+          hi[m] = unord64(S.acc[i][6 + m]);
+          chi[m] = unord64(S.acc[i][9 + m]);
+          A.box64[6ull * id + m] = lo[m];
+          A.box64[6ull * id + 3 + m] = hi[m];
+        }
+        A.nstart[id] = s + S.off[cur][i];
+        A.ncount[id] = static_cast<uint32_t>(cn);
+        A.ntile[id] = t;
+        A.ndepth[id] = S.dep[cur][i];
+        atomicMax(&S.maxdep, static_cast<uint32_t>(S.dep[cur][i]));
+        const double ex = __dsub_rn(chi[0], clo[0]), ey = __dsub_rn(chi[1], clo[1]), ez = __dsub_rn(chi[2], clo[2]);
+        const int axis = (ex >= ey && ex >= ez) ? 0 : (ey >= ez ? 1 : 2);
+        const double ext = axis == 0 ? ex : (axis == 1 ? ey : ez);
+        uint32_t l = 0;
+        if (cn <= RT_LEAF_MAX || ext <= 1e-7 || !alloc_pair(A, static_cast<int>(t), l)) {
+          S.axis[i] = -1;  // leaf (degenerate centroids, or no node capacity left)
+          A.nsplit[id] = -1;
         } else {
-          dest = big ? r - 1 : nth_bit(bm, St - (r - Bb) - 1) - off;
+          const double ca = axis == 0 ? clo[0] : (axis == 1 ? clo[1] : clo[2]);
+          const double cb = axis == 0 ? chi[0] : (axis == 1 ? chi[1] : chi[2]);
+          const double mid = __dmul_rn(0.5, __dadd_rn(ca, cb));
+          S.axis[i] = static_cast<int8_t>(axis);
+          S.mid[i] = mid;
+          S.child[i] = static_cast<uint32_t>(nb + l);
+          A.nsplit[id] = axis;
+          A.nmid[id] = mid;
+          A.nchild[id] = make_int2(static_cast<int>(nb + l), static_cast<int>(nb + l + 1));
         }
-        src[w][off + dest] = lane;
       }
-      __syncwarp();
-      const int from = in ? src[w][lane] : lane;
-      __syncwarp();
-      el = __shfl_sync(0xffffffffu, el, from);
+      __syncthreads();
+      // Flags and their exclusive prefix sum: thread tid owns positions RT_CTA_PER * tid + k.
+      {
+        uint32_t f[RT_CTA_PER], sum = 0;
 #pragma unroll
-      for (int k = 0; k < 12; ++k) key[k] = __shfl_sync(0xffffffffu, key[k], from);
-      const unsigned long long nb = T.nbase;
-      const int Sp = (St == 0 || St == cnt) ? cnt / 2 : St;  // bvh.rs:260-265
-      if (lane == 0) {
-        A.nsplit[id] = axis;
-        A.nmid[id] = mid;
-        A.nchild[id] = make_int2(static_cast<int>(nb + l), static_cast<int>(nb + l + 1));
-        A.ndepth[nb + l] = static_cast<uint32_t>(dep + 1);
-        A.ndepth[nb + l + 1] = static_cast<uint32_t>(dep + 1);
-        stk[w][sp][0] = off;
-        stk[w][sp][1] = Sp;
-        stk[w][sp][2] = static_cast<int>(nb + l);
-        stk[w][sp][3] = dep + 1;
-        stk[w][sp + 1][0] = off + Sp;
-        stk[w][sp + 1][1] = cnt - Sp;
-        stk[w][sp + 1][2] = static_cast<int>(nb + l + 1);
-        stk[w][sp + 1][3] = dep + 1;
+        for (int k = 0; k < RT_CTA_PER; ++k) {
+          const int x = RT_CTA_PER * tid + k;
+          const uint32_t node = S.nd[x];
+          f[k] = 0;
+          if (node != RT_CTA_FREE && S.axis[node] >= 0) {
+            const double4_32a v = S.pm[x];
+            const int ax = S.axis[node];
+            const double p = ax == 0 ? v.x : (ax == 1 ? v.y : v.z);
+            const double cc = __dmul_rn(0.5, __dadd_rn(__dsub_rn(p, v.w), __dadd_rn(p, v.w)));
+            f[k] = cc < S.mid[node] ? 0u : 1u;
+          }
+          sum += f[k];
+        }
+        uint32_t incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += y;
+        }
+        if (lane == 31) S.scan[w] = incl;
+        __syncthreads();
+        uint32_t acc = incl - sum;
+        for (int i = 0; i < w; ++i) acc += S.scan[i];
+#pragma unroll
+        for (int k = 0; k < RT_CTA_PER; ++k) {
+          const int x = RT_CTA_PER * tid + k;
+          S.flag[x] = static_cast<uint8_t>(f[k]);
+          S.bb[x] = static_cast<uint16_t>(acc);
+          acc += f[k];
+        }
+        if (tid == RT_CTA_T - 1) S.bb[RT_CTA_MAX] = static_cast<uint16_t>(acc);
       }
-      sp += 2;
-      __syncwarp();
+      __syncthreads();
+      // Ranks P / Q; the children of every splitting node go to the next level (more than four
+      // elements) or become small leaves.
+      for (int x = tid; x < RT_CTA_MAX; x += RT_CTA_T) {
+        const uint32_t node = S.nd[x];
+        if (node == RT_CTA_FREE || S.axis[node] < 0) continue;
+        const int o0 = S.off[cur][node], cn = S.cnt[cur][node];
+        const int r = x - o0;
+        const int bs = S.bb[o0];
+        const int Bb = S.bb[x] - bs, Bt = S.bb[o0 + cn] - bs, St = cn - Bt;
+        if (S.flag[x]) {
+          S.P[o0 + Bb] = static_cast<uint16_t>(r);
+        } else {
+          S.Q[o0 + (St - (r - Bb)) - 1] = static_cast<uint16_t>(r);
+        }
+      }
+      for (int i = tid; i < nl; i += RT_CTA_T) {
+        if (S.axis[i] < 0) continue;
+        const int o0 = S.off[cur][i], cn = S.cnt[cur][i];
+        const int St = cn - (S.bb[o0 + cn] - S.bb[o0]);
+        const int Sp = (St == 0 || St == cn) ? cn / 2 : St;  // bvh.rs:260-265
+        S.sp[i] = static_cast<uint16_t>(Sp);
+        const uint32_t cd = min(static_cast<uint32_t>(S.dep[cur][i]) + 1u, 255u);  // saturates past the depth check
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          const uint32_t cid = S.child[i] + static_cast<uint32_t>(c);
+          const int coff = o0 + (c ? Sp : 0), csz = c ? cn - Sp : Sp;
+          if (csz > RT_LEAF_MAX) {
+            const int slot = atomicAdd(&S.nnext, 1);
+            S.id[cur ^ 1][slot] = cid;
+            S.off[cur ^ 1][slot] = static_cast<uint16_t>(coff);
+            S.cnt[cur ^ 1][slot] = static_cast<uint16_t>(csz);
+            S.dep[cur ^ 1][slot] = static_cast<uint8_t>(cd);
+            S.cslot[i][c] = static_cast<uint8_t>(slot);
+          } else {
+            const int qi = atomicAdd(&S.nslnew, 1);
+            S.sl[qi] = static_cast<uint32_t>(coff) | static_cast<uint32_t>(csz) << 11 | cd << 14;
+            S.slid[qi] = cid;
+            S.cslot[i][c] = RT_CTA_FREE;
+          }
+        }
+      }
+      __syncthreads();
+      // Place: every element of a splitting node moves to its place after the swap partition.
+      double4_32a vp[RT_CTA_PER];
+      uint32_t vi[RT_CTA_PER];
+      int dst[RT_CTA_PER];
+      uint8_t vn[RT_CTA_PER];
+#pragma unroll
+      for (int k = 0; k < RT_CTA_PER; ++k) {
+        const int x = k * RT_CTA_T + tid;
+        const uint32_t node = S.nd[x];
+        dst[k] = -1;
+        vn[k] = RT_CTA_FREE;
+        if (node == RT_CTA_FREE) continue;
+        vp[k] = S.pm[x];
+        vi[k] = S.idx[x];
+        if (S.axis[node] < 0) {  // a leaf of this level: its order is final
+          dst[k] = x;
+          continue;
+        }
+        const int o0 = S.off[cur][node], cn = S.cnt[cur][node];
+        const int r = x - o0;
+        const int bs = S.bb[o0];
+        const int Bb = S.bb[x] - bs, Bt = S.bb[o0 + cn] - bs, St = cn - Bt;
+        const int li = St + (St < cn ? S.flag[o0 + St] : 0);
+        const bool big = S.flag[x] != 0;
+        int d;
+        if (r < li) {
+          d = big ? ((Bb == 0 ? cn : S.Q[o0 + Bb - 1]) - 1) : r;
+        } else {
+          d = big ? r - 1 : S.P[o0 + (St - (r - Bb)) - 1];
+        }
+        dst[k] = o0 + d;
+        vn[k] = S.cslot[node][d < S.sp[node] ? 0 : 1];
+      }
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < RT_CTA_PER; ++k) {
+        if (dst[k] < 0) continue;
+        S.pm[dst[k]] = vp[k];
+        S.idx[dst[k]] = vi[k];
+        S.nd[dst[k]] = vn[k];
+      }
+      if (tid == 0) {
+        S.nl = S.nnext;
+        S.nsl = S.nslnew;
+      }
+      cur ^= 1;
+      __syncthreads();
     }
-    if (static_cast<uint32_t>(lane) < n) A.ridx[s + lane] = el;
-    if (lane == 0) atomicMax(&A.tiles[t].depth, maxdep);
+    for (int x = tid; x < n; x += RT_CTA_T) A.ridx[s + x] = S.idx[x];
+    if (tid == 0) atomicMax(&A.tiles[t].depth, S.maxdep);
+    __syncthreads();
   }
 }
 
@@ -710,8 +848,6 @@ RtArgs rt_args(RTreeBufs& B, uint32_t* err) {
   A.box64 = B.box64.p;
   A.nstart = B.nstart.p;
   A.ncount = B.ncount.p;
-  A.nK = B.nK.p;
-  A.nS = B.nS.p;
   A.ntile = B.ntile.p;
   A.ndepth = B.ndepth.p;
   A.nsplit = B.nsplit.p;
@@ -719,8 +855,8 @@ RtArgs rt_args(RTreeBufs& B, uint32_t* err) {
   A.nchild = B.nchild.p;
   A.wl[0] = B.wl0.p;
   A.wl[1] = B.wl1.p;
-  A.wq = B.wq.p;
-  A.wqpar = B.wqpar.p;
+  A.bq = B.bq.p;
+  A.bqpar = B.bqpar.p;
   A.cnt = B.cnt.p;
   A.err = err;
   return A;
@@ -764,8 +900,6 @@ void rtree_alloc(RTreeBufs& B, std::vector<RTile>& tiles, bool want_leafof, cuda
   B.box64.alloc(6 * N1, st);
   B.nstart.alloc(N1, st);
   B.ncount.alloc(N1, st);
-  B.nK.alloc(N1, st);
-  B.nS.alloc(N1, st);
   B.ntile.alloc(N1, st);
   B.ndepth.alloc(N1, st);
   B.nsplit.alloc(N1, st);
@@ -773,8 +907,8 @@ void rtree_alloc(RTreeBufs& B, std::vector<RTile>& tiles, bool want_leafof, cuda
   B.nchild.alloc(N1, st);
   B.wl0.alloc(N1, st);
   B.wl1.alloc(N1, st);
-  B.wq.alloc(N1, st);
-  B.wqpar.alloc(N1, st);
+  B.bq.alloc(N1, st);
+  B.bqpar.alloc(N1, st);
   B.cnt.alloc(4, st);
   B.rnode.alloc(N1, st);
   B.rleaf.alloc(N1, st);
@@ -816,8 +950,6 @@ size_t carve(RTreeBufs* B, uint32_t ecap, bool want_leafof, uint32_t leafof_slot
   take(b.box64, 6 * N1);
   take(b.nstart, N1);
   take(b.ncount, N1);
-  take(b.nK, N1);
-  take(b.nS, N1);
   take(b.ntile, N1);
   take(b.ndepth, N1);
   take(b.nsplit, N1);
@@ -825,8 +957,8 @@ size_t carve(RTreeBufs* B, uint32_t ecap, bool want_leafof, uint32_t leafof_slot
   take(b.nchild, N1);
   take(b.wl0, N1);
   take(b.wl1, N1);
-  take(b.wq, N1);
-  take(b.wqpar, N1);
+  take(b.bq, N1);
+  take(b.bqpar, N1);
   take(b.cnt, 4);
   take(b.rnode, N1);
   take(b.rleaf, N1);
@@ -867,7 +999,6 @@ void rtree_build(RTreeBufs& B, uint32_t* err, cudaStream_t st, RTile* tiles_dev)
   const unsigned GN = static_cast<unsigned>(std::min<unsigned long long>((B.N + RT_BLOCK - 1) / RT_BLOCK, 152ull * 16));
   const unsigned GS = static_cast<unsigned>(std::min<unsigned long long>(B.nblk, 152ull * 16));
   FG_CUDA(cudaMemsetAsync(B.cnt.p, 0, 4 * sizeof(uint32_t), st));
-  k_rt_clear<<<GN, RT_BLOCK, 0, st>>>(A);
   k_rt_init<<<G, RT_BLOCK, 0, st>>>(A);
   for (int L = 0; L < B.levels; ++L) {
     const int c = L & 1;
@@ -881,8 +1012,11 @@ void rtree_build(RTreeBufs& B, uint32_t* err, cudaStream_t st, RTile* tiles_dev)
     k_rt_level_end<<<1, 1, 0, st>>>(A, c);
   }
   k_rt_check<<<1, 1, 0, st>>>(A, B.levels & 1);
-  const unsigned GW = static_cast<unsigned>(std::min<unsigned long long>((B.N + RT_WARPS - 1) / RT_WARPS, 152ull * 32));
-  k_rt_warp<<<GW, 32 * RT_WARPS, 0, st>>>(A);
+  const unsigned GC = static_cast<unsigned>(
+      std::min<unsigned long long>(B.E / (RT_LEAF_MAX + 1) + static_cast<unsigned long long>(B.ntiles), 152ull * 8));
+  FG_CUDA(cudaFuncSetAttribute(k_rt_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               static_cast<int>(sizeof(RtCtaSmem))));
+  k_rt_cta<<<GC, RT_CTA_T, sizeof(RtCtaSmem), st>>>(A);
   k_rt_records<<<GN, RT_BLOCK, 0, st>>>(A, B.rnode.p, B.rleaf.p, B.leafof.p, B.leafof.n);
   k_rt_depth_check<<<grid_for(static_cast<size_t>(B.ntiles), 128), 128, 0, st>>>(A);
   FG_CUDA(cudaGetLastError());
@@ -940,7 +1074,7 @@ void build_emulsion_tree(fg_engine* e, const fg_emulsion* em, bool developed_onl
 }
 
 unsigned rtree_kernel_launches(const RTreeBufs& B) {
-  return B.ntiles ? 2u + 8u * static_cast<unsigned>(B.levels) + 4u : 0u;
+  return B.ntiles ? 1u + 8u * static_cast<unsigned>(B.levels) + 4u : 0u;
 }
 
 }  // namespace fg

@@ -28,7 +28,7 @@
 
 namespace fg {
 
-constexpr int RT_WARP_MAX = 32;    // nodes of at most this many crystals are finished by one warp
+constexpr int RT_CTA_MAX = 1024;   // nodes of at most this many crystals are finished by one block
 constexpr int RT_MAX_DEPTH = 47;   // deeper trees are rejected (the walks keep 48-entry stacks)
 constexpr uint32_t RT_DONE = 0x80000000u;
 
@@ -70,7 +70,7 @@ constexpr size_t rt_al(size_t v) { return (v + 255) / 256 * 256; }
 constexpr size_t rtree_attach_bytes(size_t ecap, bool want_leafof, size_t slots) {
   const size_t e1 = ecap > 0 ? ecap : 1, n1 = rt_attach_nodes(e1);
   return rt_al(112) + 4 * rt_al(4 * e1) + 2 * rt_al(32 * e1) + 2 * rt_al(4 * (e1 + 1)) + rt_al(4 * rt_attach_blocks(e1)) +
-         3 * rt_al(4 * e1) + rt_al(96 * n1) + rt_al(48 * n1) + 6 * rt_al(4 * n1) + rt_al(4 * n1) + rt_al(8 * n1) +
+         3 * rt_al(4 * e1) + rt_al(96 * n1) + rt_al(48 * n1) + 4 * rt_al(4 * n1) + rt_al(4 * n1) + rt_al(8 * n1) +
          rt_al(8 * n1) + 4 * rt_al(4 * n1) + rt_al(16) + rt_al(64 * n1) + rt_al(8 * n1) +
          (want_leafof ? rt_al(4 * (slots > 0 ? slots : 1)) : 0);
 }
@@ -100,8 +100,8 @@ __device__ __forceinline__ void rt_box(const RTile& t, uint32_t s, double lo[3],
 }
 
 // Position xyz and half-size m = max_dim * expansion of element slot s, in FP64 (crystal.rs:114-119).
-__device__ __forceinline__ double4 rt_pm(const RTile& t, uint32_t s) {
-  double4 v;
+__device__ __forceinline__ double4_32a rt_pm(const RTile& t, uint32_t s) {
+  double4_32a v;
   double dm;
   if (t.pos64) {
     v.x = t.pos64[3 * s];
@@ -120,7 +120,7 @@ __device__ __forceinline__ double4 rt_pm(const RTile& t, uint32_t s) {
 }
 
 // The box p -+ m and its centroid 0.5 (lo + hi), as rt_box computes them.
-__device__ __forceinline__ void rt_box_pm(const double4& v, double lo[3], double hi[3], double c[3]) {
+__device__ __forceinline__ void rt_box_pm(const double4_32a& v, double lo[3], double hi[3], double c[3]) {
   const double p[3] = {v.x, v.y, v.z};
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
