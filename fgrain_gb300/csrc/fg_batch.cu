@@ -39,6 +39,7 @@ void launch_transport_shape(const TileDesc* tiles_dev, int ntiles, unsigned long
 void launch_photon_sort(const TileDesc* tiles_dev, int ntiles, unsigned long long total, unsigned long long ncells,
                         uint32_t* cnt, const uint32_t* off, uint32_t* cur, uint32_t* order, uint32_t* err,
                         cudaStream_t st);
+void launch_density(float* d, unsigned long long n, cudaStream_t st);
 void launch_scan(const ScanTile* tiles, int ntiles, unsigned long long nbins, unsigned threads, uint32_t* err,
                  unsigned long long* stats, cudaStream_t st);
 void launch_scan_prep(const ScanTile* tiles, int ntiles, unsigned long long nslots, ScanPrep* prep,
@@ -649,6 +650,7 @@ static void stage_scan(fg_batch* B, cudaStream_t st) {
                              B->bin_off.p, B->bin_cur.p, B->bin_items.p, B->item_cap, e->d_err);
   FG_CUDA(cudaGetLastError());
   launch_scan(B->d_sc.p, nt, B->nbins, B->scan_threads, e->d_err, B->dstats.p, st);
+  launch_density(B->d_neg.p, B->out_total, st);
 }
 
 // Stage events: inside a graph capture they must be external records so that every replay
@@ -1162,9 +1164,9 @@ fg_status fg_batch_wait(fg_batch* b, fg_batch_stats* stats) {
     s.graph = b->exec ? 1u : 0u;
     // Own kernels per run: Bridson (all colour classes in one launch; it also counts the points), thin +
     // brick counts, emit, set_n, photon order x2, transport, maxdim + threshold + developed list + link +
-    // roots + finalize, scan-tree inputs, scan prep, two bin passes, scan, and the two tree builds (each
+    // roots + finalize, scan-tree inputs, scan prep, two bin passes, scan, density, and the two tree builds (each
     // level's launches included, also those that find no work; CUB scans not counted).
-    s.kernel_launches = 1 + 2 + 1 + 1 + 2 + 1 + 6 + 1 + 1 + 2 + 1 + 2 * rtree_kernel_launches(b->rt);
+    s.kernel_launches = 1 + 2 + 1 + 1 + 2 + 1 + 6 + 1 + 1 + 2 + 1 + 1 + 2 * rtree_kernel_launches(b->rt);
     b->stats = s;
     if (stats) *stats = s;
   });

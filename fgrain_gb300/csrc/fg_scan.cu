@@ -60,6 +60,45 @@ __device__ __forceinline__ void split64(double v, float& hi, float& lo) {
   hi = static_cast<float>(v);
   lo = static_cast<float>(v - static_cast<double>(hi));
 }
+// A float widened to double by moving its bits (integer pipes); zero and subnormals (T below
+// 2^-126, rare) take the conversion instruction.
+__device__ __forceinline__ double f2d_exact(float f) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t e = (b >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return static_cast<double>(f);
+  const unsigned long long d = (static_cast<unsigned long long>(b & 0x80000000u) << 32) |
+                               (static_cast<unsigned long long>(e + (1023u - 127u)) << 52) |
+                               (static_cast<unsigned long long>(b & 0x7fffffu) << 29);
+  return __longlong_as_double(static_cast<long long>(d));
+}
+
+// (ah + al) - (bh + bl) as a float pair, to about 2^-48 of the operands.
+__device__ __forceinline__ void pair_sub(float ah, float al, float bh, float bl, float& h, float& l) {
+  float s, e;
+  two_sum(ah, -bh, s, e);
+  two_sum(s, e + (al - bl), h, l);
+}
+
+// Fixed-point chord sums (units of 2^-40 um) without 64-bit integer / float conversions, which
+// run on GB300's narrow FP64 pipe.  fix40(v) equals __float2ll_rn(v * 2^40) for 0 <= v < 2^15:
+// below 2^31 the 32-bit conversion rounds the same way; above, v * 2^40 is an integer (its ulp is
+// at least 2^8) split exactly into hi * 2^24 + lo.
+__device__ __forceinline__ long long fix40(float v) {
+  const float w = v * 1099511627776.0f;
+  if (w < 2147483648.0f) return static_cast<long long>(__float2int_rn(w));
+  const float hf = truncf(w * 0x1p-24f);
+  const float lf = fmaf(-hf, 16777216.0f, w);  // exact: the low 24 bits of an integer
+  return (static_cast<long long>(__float2int_rz(hf)) << 24) + __float2int_rz(lf);
+}
+// u rounded to the nearest float (ties to even), as __ll2float_rn does, in integer arithmetic.
+__device__ __forceinline__ float u64_to_float_rn(unsigned long long u) {
+  if (u < (1ull << 24)) return static_cast<float>(static_cast<uint32_t>(u));
+  const int sh = 63 - __clzll(static_cast<long long>(u)) - 23;  // >= 1
+  unsigned long long m = u >> sh;                                // 24 bits
+  const unsigned long long rem = u & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+  if (rem > half || (rem == half && (m & 1ull))) ++m;            // m <= 2^24: exact as a float
+  return static_cast<float>(static_cast<uint32_t>(m)) * __int_as_float((127 + sh) << 23);
+}
 
 // Crystal kinds in shared memory.
 enum : int { K_CUBE = 0, K_CUBE_DF = 1, K_ELLIPSOID = 2, K_FP64 = 3 };
@@ -92,13 +131,13 @@ __device__ __forceinline__ void prep_crystal(const ScanTile& t, uint32_t s, Scan
   const double mdim = fmax(fmax(k.dims.x, k.dims.y), k.dims.z);
   const double m64 = __dmul_rn(mdim, e64);
   const float m = static_cast<float>(m64);
-  P.px = k.pos.x;
-  P.py = k.pos.y;
+  split64(k.pos.x, P.ch[0], P.cl[0]);
+  split64(k.pos.y, P.ch[1], P.cl[1]);
   const double* lb = t.lbox64 + 6ull * t.leafof[s];
-  P.lx0 = lb[0];
-  P.lx1 = lb[3];
-  P.ly0 = lb[1];
-  P.ly1 = lb[4];
+  split64(lb[0], P.ch[2], P.cl[2]);
+  split64(lb[3], P.ch[3], P.cl[3]);
+  split64(lb[1], P.ch[4], P.cl[4]);
+  split64(lb[4], P.ch[5], P.cl[5]);
   P.m = m;
   P.delta = static_cast<float>(t.z0 - k.pos.z);
   P.sig = t.sigma_c ? t.sigma_c[s] : t.sigma;
@@ -158,22 +197,23 @@ __device__ __forceinline__ void prep_crystal(const ScanTile& t, uint32_t s, Scan
   }
 }
 
-// Stages crystal s for the bin whose 16-px-square corner is (bx0, by0): the bin-independent terms
-// (from t.prep, or derived here), and the centre relative to the corner as float pairs.
-__device__ __forceinline__ void stage_crystal(const ScanTile& t, ScanSmem& sm, int c, uint32_t s,
-                                              double bx0, double by0) {
+// Stages crystal s for the bin whose 16-px-square corner is (bxh + bxl, byh + byl): the
+// bin-independent terms (from t.prep, or derived here), and the centre and leaf box relative to
+// the corner as float pairs (float arithmetic only).
+__device__ __forceinline__ void stage_crystal(const ScanTile& t, ScanSmem& sm, int c, uint32_t s, float bxh,
+                                              float bxl, float byh, float byl) {
   ScanPrep P;
   if (t.prep) {
     P = t.prep[s];
   } else {
     prep_crystal(t, s, P);
   }
-  split64(P.px - bx0, sm.cxh[c], sm.cxl[c]);
-  split64(P.py - by0, sm.cyh[c], sm.cyl[c]);
-  split64(P.lx0 - bx0, sm.lbh[0][c], sm.lbl[0][c]);
-  split64(P.lx1 - bx0, sm.lbh[1][c], sm.lbl[1][c]);
-  split64(P.ly0 - by0, sm.lbh[2][c], sm.lbl[2][c]);
-  split64(P.ly1 - by0, sm.lbh[3][c], sm.lbl[3][c]);
+  pair_sub(P.ch[0], P.cl[0], bxh, bxl, sm.cxh[c], sm.cxl[c]);
+  pair_sub(P.ch[1], P.cl[1], byh, byl, sm.cyh[c], sm.cyl[c]);
+  pair_sub(P.ch[2], P.cl[2], bxh, bxl, sm.lbh[0][c], sm.lbl[0][c]);
+  pair_sub(P.ch[3], P.cl[3], bxh, bxl, sm.lbh[1][c], sm.lbl[1][c]);
+  pair_sub(P.ch[4], P.cl[4], byh, byl, sm.lbh[2][c], sm.lbl[2][c]);
+  pair_sub(P.ch[5], P.cl[5], byh, byl, sm.lbh[3][c], sm.lbl[3][c]);
   sm.m[c] = P.m;
   sm.delta[c] = P.delta;
   sm.err[c] = P.err;
@@ -328,7 +368,7 @@ __device__ __forceinline__ bool scan_pair(const ScanTile& t, const ScanSmem& sm,
 struct ScanRay {
   uint32_t px, py, sx, sy, st;
   bool active;
-  double bx0, by0;
+  float bxh, bxl, byh, byl;  // corner of the 16-pixel square holding the bin (um, float pairs)
   float oxh, oxl, oyh, oyl;
 };
 
@@ -345,8 +385,16 @@ __device__ __forceinline__ ScanRay scan_ray(const ScanTile& t, uint32_t bin, uin
   // the bin itself, so that every bin edge rounds identically and results do not depend on the
   // launch shape.
   const uint32_t ox_px = (bx * t.bin_px) & ~15u, oy_px = (by * t.bin_px) & ~15u;
-  R.bx0 = __dmul_rn(static_cast<double>(ox_px), t.pw);
-  R.by0 = __dmul_rn(static_cast<double>(oy_px), t.ph);
+  {
+    // The corner as a whole number of jitter units, (ox_px g 2^24) (pw / (g 2^24)), in float pairs:
+    // the ray offsets below are counted in the same units, so the two agree to about 2^-48.
+    const float fx = static_cast<float>(ox_px * t.g) * 16777216.0f, fy = static_cast<float>(oy_px * t.g) * 16777216.0f;
+    float p, e;
+    two_prod(fx, t.jxh, p, e);
+    fast_two_sum(p, fmaf(fx, t.jxl, e), R.bxh, R.bxl);
+    two_prod(fy, t.jyh, p, e);
+    fast_two_sum(p, fmaf(fy, t.jyl, e), R.byh, R.byl);
+  }
   const uint32_t rlx = px - ox_px, rly = py - oy_px;  // < 16 + bin_px
   // Ray position relative to that corner as a float pair.  The offset in units of the 24-bit
   // jitter is an exact integer X = (l g + s) 2^24 + u, so x = X * pw / (g 2^24).
@@ -358,9 +406,11 @@ __device__ __forceinline__ ScanRay scan_ray(const ScanTile& t, uint32_t bin, uin
     const float cxh = t.jxh, cxl = t.jxl, cyh = t.jyh, cyl = t.jyl;
     const uint32_t X = ((rlx * t.g + sx) << 24) + (r.x >> 8);
     const uint32_t Y = ((rly * t.g + sy) << 24) + (r.y >> 8);
-    const float Xh = static_cast<float>(X), Yh = static_cast<float>(Y);
-    const float Xl = static_cast<float>(static_cast<long long>(X) - static_cast<long long>(Xh));
-    const float Yl = static_cast<float>(static_cast<long long>(Y) - static_cast<long long>(Yh));
+    // X, Y < 2^31 as a float pair: Xh rounded, Xl = X - Xh exact (32-bit conversions only; the
+    // 64-bit ones run on the FP64 pipe).
+    const float Xh = __uint2float_rn(X), Yh = __uint2float_rn(Y);
+    const float Xl = __int2float_rn(static_cast<int>(X - __float2uint_rn(Xh)));
+    const float Yl = __int2float_rn(static_cast<int>(Y - __float2uint_rn(Yh)));
     float p, e;
     two_prod(Xh, cxh, p, e);
     fast_two_sum(p, e + (Xh * cxl + Xl * cxh), oxh, oxl);
@@ -404,7 +454,6 @@ __global__ void __launch_bounds__(SCAN_THREADS, 4) k_scan(const ScanTile* __rest
   const ScanRay R = scan_ray(t, bin, tid);
   const uint32_t px = R.px, py = R.py, sx = R.sx, sy = R.sy, st = R.st;
   const bool active = R.active;
-  const double bx0 = R.bx0, by0 = R.by0;
   const float oxh = R.oxh, oxl = R.oxl, oyh = R.oyh, oyl = R.oyl;
   long long Lfix = 0;  // chord sum (sigma-weighted when per crystal), 2^-40 um units
   uint32_t nh = 0, nfb = 0;
@@ -413,7 +462,8 @@ __global__ void __launch_bounds__(SCAN_THREADS, 4) k_scan(const ScanTile* __rest
   for (uint32_t base = b0; base < b1; base += SCAN_CH) {
     const uint32_t cnt = min(static_cast<uint32_t>(SCAN_CH), b1 - base);
     __syncthreads();
-    for (uint32_t c = tid; c < cnt; c += blockDim.x) stage_crystal(t, sm, c, t.bin_items[base + c], bx0, by0);
+    for (uint32_t c = tid; c < cnt; c += blockDim.x)
+      stage_crystal(t, sm, c, t.bin_items[base + c], R.bxh, R.bxl, R.byh, R.byl);
     __syncthreads();
     if (!active) continue;
     for (uint32_t c = 0; c < cnt; ++c) {
@@ -422,27 +472,33 @@ __global__ void __launch_bounds__(SCAN_THREADS, 4) k_scan(const ScanTile* __rest
       if (hit) {
         ++nh;
         const float v = per_crystal ? sm.sig[c] * fmaxf(chord, 0.0f) : fmaxf(chord, 0.0f);
-        Lfix += __float2ll_rn(v * 1099511627776.0f);
+        Lfix += fix40(v);
       }
     }
   }
   float T = 1.0f;
   if (active) {
     // Lfix * 2^-40 rounded once to float (the conversion rounds, the power-of-two scale is exact).
-    const float L = __ll2float_rn(Lfix) * 0x1p-40f;
+    const float L = u64_to_float_rn(static_cast<unsigned long long>(Lfix)) * 0x1p-40f;
     T = per_crystal ? expf(-L) : expf(-t.sigma * L);
     if (t.ray_hits) t.ray_hits[(static_cast<size_t>(py) * t.w + px) * a + st] = static_cast<uint16_t>(min(nh, 65535u));
   }
-  sm.T[tid] = (double)T;
+  sm.T[tid] = f2d_exact(T);
   __syncthreads();
-  if (active && st == 0) {
+  // Per pixel: thread p finishes the bin's p-th pixel, so the FP64 work runs on consecutive lanes
+  // (a pixel's strata are a consecutive threads; one thread in a per pixel would leave most lanes
+  // of each FP64 instruction idle on GB300's narrow FP64 pipe).
+  for (uint32_t p = tid; p * a < blockDim.x; p += blockDim.x) {
+    const uint32_t bx = bin % t.nbx, by = bin / t.nbx;
+    const uint32_t qx = bx * t.bin_px + p % t.bin_px, qy = by * t.bin_px + p / t.bin_px;
+    if (p >= t.bin_px * t.bin_px || qx >= t.w || qy >= t.h) continue;
     // FP64 mean over strata in the reference's order (sy, sx), then f32 (transmittance.rs:142).
     double acc = 0.0;
-    for (uint32_t k = 0; k < a; ++k) acc = __dadd_rn(acc, sm.T[tid + k]);
+    for (uint32_t k = 0; k < a; ++k) acc = __dadd_rn(acc, sm.T[p * a + k]);
     // Division by a power of two is the multiplication by its exact reciprocal.
     const float mean = (float)((a & (a - 1)) == 0 ? __dmul_rn(acc, 1.0 / static_cast<double>(a))
                                                    : __ddiv_rn(acc, static_cast<double>(a)));
-    const size_t idx = static_cast<size_t>(py) * t.w + px;
+    const size_t idx = static_cast<size_t>(qy) * t.w + qx;
     float v;
     if (t.mode == 0) {
       v = mean;
@@ -454,11 +510,8 @@ __global__ void __launch_bounds__(SCAN_THREADS, 4) k_scan(const ScanTile* __rest
     }
     if (t.out) t.out[idx] = v;
     if (t.image8) t.image8[idx] = static_cast<uint8_t>(rintf(fminf(fmaxf(v, 0.0f), 1.0f) * 255.0f));
-    if (t.d_neg) {
-      // d = -log10(clamp(T, 1e-4, 1)) + 0.05 in FP64 (image_pipeline.rs:1007-1011).
-      const double tc = fmin(fmax((double)mean, 1e-4), 1.0);
-      t.d_neg[idx] = (float)(-log10(tc) + 0.05);
-    }
+    // The mean transmittance; launch_density turns it into the density in a pass of its own.
+    if (t.d_neg) t.d_neg[idx] = mean;
   }
   if (stats) {
     unsigned long long f = nfb, hsum = nh;
@@ -494,20 +547,21 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_adjoint(const ScanTile* _
   for (uint32_t base = b0; base < b1; base += SCAN_CH) {
     const uint32_t cnt = min(static_cast<uint32_t>(SCAN_CH), b1 - base);
     __syncthreads();
-    for (uint32_t c = tid; c < cnt; c += blockDim.x) stage_crystal(t, sm, c, t.bin_items[base + c], R.bx0, R.by0);
+    for (uint32_t c = tid; c < cnt; c += blockDim.x)
+      stage_crystal(t, sm, c, t.bin_items[base + c], R.bxh, R.bxl, R.byh, R.byl);
     __syncthreads();
     if (!R.active) continue;
     for (uint32_t c = 0; c < cnt; ++c) {
       float chord;
       if (scan_pair(t, sm, c, R.oxh, R.oxl, R.oyh, R.oyl, R.px, R.py, R.sx, R.sy, chord, nfb)) {
         const float v = per_crystal ? sm.sig[c] * fmaxf(chord, 0.0f) : fmaxf(chord, 0.0f);
-        Lfix += __float2ll_rn(v * 1099511627776.0f);
+        Lfix += fix40(v);
       }
     }
   }
   float coef = 0.0f;
   if (R.active) {
-    const float L = __ll2float_rn(Lfix) * 0x1p-40f;  // rounded once, as in k_scan
+    const float L = u64_to_float_rn(static_cast<unsigned long long>(Lfix)) * 0x1p-40f;  // as in k_scan
     const float T = per_crystal ? expf(-L) : expf(-t.sigma * L);
     coef = wpx[static_cast<size_t>(R.py) * t.w + R.px] / static_cast<float>(a) * T;
   }
@@ -515,7 +569,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_adjoint(const ScanTile* _
     const uint32_t cnt = min(static_cast<uint32_t>(SCAN_CH), b1 - base);
     __syncthreads();
     for (uint32_t c = tid; c < cnt; c += blockDim.x) {
-      stage_crystal(t, sm, c, t.bin_items[base + c], R.bx0, R.by0);
+      stage_crystal(t, sm, c, t.bin_items[base + c], R.bxh, R.bxl, R.byh, R.byl);
       gsum[c] = 0.0;
     }
     __syncthreads();
@@ -530,6 +584,25 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_adjoint(const ScanTile* _
     for (uint32_t c = tid; c < cnt; c += blockDim.x)
       if (gsum[c] != 0.0) atomicAdd(&g[sm.s[c]], gsum[c]);
   }
+}
+
+// d = -log10(clamp(T, 1e-4, 1)) + 0.05 in FP64 (image_pipeline.rs:1007-1011), in place over the
+// pixels' mean transmittance.  A pass of its own so that every lane of a warp converts a pixel:
+// inside k_scan only one thread per pixel (of spp) would, and each FP64 instruction would occupy
+// GB300's narrow FP64 pipe for a whole warp.
+__global__ void k_density(float* __restrict__ d, unsigned long long n) {
+  const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+  for (unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; i < n;
+       i += stride) {
+    const double tc = fmin(fmax(static_cast<double>(d[i]), 1e-4), 1.0);
+    d[i] = static_cast<float>(-log10(tc) + 0.05);
+  }
+}
+
+void launch_density(float* d, unsigned long long n, cudaStream_t st) {
+  if (n == 0) return;
+  k_density<<<static_cast<unsigned>(std::min<unsigned long long>(grid_for(n, 256), 152ull * 16)), 256, 0, st>>>(d, n);
+  FG_CUDA(cudaGetLastError());
 }
 
 void launch_scan(const ScanTile* tiles, int ntiles, unsigned long long nbins, unsigned threads, uint32_t* err,
@@ -634,6 +707,7 @@ void scan(fg_engine* e, const fg_emulsion* em, const fg_scan_cfg& cfg, uint64_t 
   plan_scan(e, em, cfg, seed, sigma_sorted, out, P);
   k_scan<<<P.nbins, P.threads, 0, e->stream>>>(P.td.p, 1, e->d_err, e->d_stats);
   FG_CUDA(cudaGetLastError());
+  if (out.d_neg) launch_density(out.d_neg, static_cast<unsigned long long>(cfg.width_px) * cfg.height_px, e->stream);
   FG_CUDA(cudaStreamSynchronize(e->stream));
 }
 

@@ -29,8 +29,9 @@ constexpr int SCAN_THREADS = 256;   // rays per CTA (bin_px^2 * strata)
 // rounded (k_scan_prep): each bin that lists the crystal only adds its centre relative to the
 // bin's corner.  160 bytes, read with vector loads.
 struct __align__(16) ScanPrep {
-  double px, py;   // centre x, y (um) as the scan sees it
-  double lx0, lx1, ly0, ly1;  // the x and y extent of the crystal's leaf box in the scan's tree
+  // Centre x, y (um) as the scan sees it, and the x and y extent of the crystal's leaf box in the
+  // scan's tree, as float pairs (hi + lo): x, y, leaf x0, x1, y0, y1.
+  float ch[6], cl[6];
   float g[21];     // per-kind terms (see stage_crystal)
   float m, delta, err, sig;
   int kind;
