@@ -54,12 +54,33 @@ __device__ void syn_outer_table(int* tbl) {
       }
 }
 
+// Whether the candidate at region cell cb, fixed-point offsets (cx, cy, cz) inside it, has a point
+// within r in the 90 outer cells; the warp splits the cells over its lanes.  All 32 lanes call it
+// with the same candidate; the answer is the same in every lane.
+__device__ __forceinline__ bool syn_outer_hit(const uint32_t* grid, const int* tbl, int cb, int cx, int cy, int cz,
+                                              int lane) {
+  bool hit = false;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int j = lane + 32 * k;
+    if (j < SYN_OUTER) {
+      const int e = tbl[j];
+      hit |= syn_conflict(grid[cb + static_cast<int16_t>(e & 0xffff)], ((e >> 16) & 7) - 2, ((e >> 19) & 7) - 2,
+                          ((e >> 22) & 7) - 2, cx, cy, cz);
+    }
+  }
+  return __any_sync(0xffffffffu, hit);
+}
+
 // Second half of the test for the lanes whose candidates passed syn_near_free: the warp takes the
-// survivors one at a time and splits the 90 outer cells over its lanes.  Returns the lane's
-// updated verdict.  All 32 lanes must call it.
+// survivors one at a time, in lane order, until one also passes the outer cells: the step's first
+// valid candidate, the only lane left valid.  The survivors after it stay untested (`rest`, the
+// same in every lane): the round's resolution needs another candidate only when that one
+// conflicts with a point accepted for an earlier warp, and tests them then.  All 32 lanes call it.
 __device__ __forceinline__ bool syn_outer_free(const uint32_t* grid, const int* tbl, bool valid, int rb, int lx,
-                                               int ly, int lz, int lane) {
+                                               int ly, int lz, int lane, unsigned& rest) {
   unsigned sm = __ballot_sync(0xffffffffu, valid);
+  int win = -1;
   while (sm) {
     const int c = __ffs(sm) - 1;
     sm &= sm - 1;
@@ -67,19 +88,13 @@ __device__ __forceinline__ bool syn_outer_free(const uint32_t* grid, const int* 
     const int cx = __shfl_sync(0xffffffffu, lx, c);
     const int cy = __shfl_sync(0xffffffffu, ly, c);
     const int cz = __shfl_sync(0xffffffffu, lz, c);
-    bool hit = false;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const int j = lane + 32 * k;
-      if (j < SYN_OUTER) {
-        const int e = tbl[j];
-        hit |= syn_conflict(grid[cb + static_cast<int16_t>(e & 0xffff)], ((e >> 16) & 7) - 2, ((e >> 19) & 7) - 2,
-                            ((e >> 22) & 7) - 2, cx, cy, cz);
-      }
+    if (!syn_outer_hit(grid, tbl, cb, cx, cy, cz, lane)) {
+      win = c;
+      break;
     }
-    if (__any_sync(0xffffffffu, hit) && lane == c) valid = false;
   }
-  return valid;
+  rest = sm;
+  return lane == win;
 }
 
 // Exact test of a fixed-point candidate against the staged grid: every point within r.  The eight
@@ -140,7 +155,8 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 8) k_bridson(const SynthTile* 
   __shared__ int s_nact, s_wsum[SYN_WARPS];
   __shared__ int s_ncom;  // points this column commits (each fills one empty cell of its tile)
   __shared__ int s_pick[SYN_WARPS];
-  __shared__ unsigned s_vmask[SYN_WARPS];
+  __shared__ unsigned s_vmask[SYN_WARPS];  // the step's first valid candidate (at most one lane)
+  __shared__ unsigned s_rmask[SYN_WARPS];  // later candidates that passed the near cells, untested
   __shared__ int s_cx[SYN_WARPS][32], s_cy[SYN_WARPS][32], s_cz[SYN_WARPS][32];  // valid candidates
   __shared__ int s_outer[SYN_OUTER];
 
@@ -316,14 +332,18 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 8) k_bridson(const SynthTile* 
         }
       }
     }
-    valid = syn_outer_free(grid, s_outer, valid, rb, X & 1023, Y & 1023, Z & 1023, lane);
-    const unsigned vm = __ballot_sync(0xffffffffu, valid);
-    if (valid) {
+    unsigned rest;
+    const bool first = syn_outer_free(grid, s_outer, valid, rb, X & 1023, Y & 1023, Z & 1023, lane, rest);
+    const unsigned vm = __ballot_sync(0xffffffffu, first);
+    if (first || ((rest >> lane) & 1u)) {
       s_cx[warp][lane] = X;
       s_cy[warp][lane] = Y;
       s_cz[warp][lane] = Z;
     }
-    if (lane == 0) s_vmask[warp] = vm;
+    if (lane == 0) {
+      s_vmask[warp] = vm;
+      s_rmask[warp] = rest;
+    }
     __syncthreads();
     if (warp == 0) {
       // The round's steps in warp order, exactly as if they ran one after another: warp w keeps its
@@ -370,9 +390,11 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 8) k_bridson(const SynthTile* 
         accw |= run;
         acc |= run;
         if (wb == SYN_WARPS) break;
-        // Warp wb: its first candidate at least r from every point kept for warps < wb.
-        const unsigned m = s_vmask[wb];
-        bool ok = (m >> lane) & 1u;
+        // Warp wb: its first valid candidate at least r from every point kept for warps < wb.  Its
+        // untested candidates take the outer test here, in lane order, until one passes (the grid
+        // is as the candidate phase saw it: the round commits after it is resolved).
+        const unsigned m = s_vmask[wb], mr = s_rmask[wb];
+        bool ok = ((m | mr) >> lane) & 1u;
         int X = 0, Y = 0, Z = 0;
         if (ok) {
           X = s_cx[wb][lane];
@@ -388,9 +410,24 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 8) k_bridson(const SynthTile* 
             if (ex * ex + ey * ey + ez * ez < SYN_R2X) ok = false;
           }
         }
-        const unsigned okm = __ballot_sync(0xffffffffu, ok);
-        if (okm) {
-          const int c = __ffs(okm) - 1;
+        unsigned okm = __ballot_sync(0xffffffffu, ok);
+        int c = -1;
+        while (okm) {
+          const int l = __ffs(okm) - 1;
+          okm &= okm - 1;
+          if ((m >> l) & 1u) {
+            c = l;
+            break;
+          }
+          const int lx_ = __shfl_sync(0xffffffffu, X, l), ly_ = __shfl_sync(0xffffffffu, Y, l);
+          const int lz_ = __shfl_sync(0xffffffffu, Z, l);
+          const int cb = (((lz_ >> 10) + 2) * SYN_R + ((ly_ >> 10) - oy)) * SYN_R + ((lx_ >> 10) - ox);
+          if (!syn_outer_hit(grid, s_outer, cb, lx_ & 1023, ly_ & 1023, lz_ & 1023, lane)) {
+            c = l;
+            break;
+          }
+        }
+        if (c >= 0) {
           const int qx = __shfl_sync(0xffffffffu, X, c), qy = __shfl_sync(0xffffffffu, Y, c);
           const int qz = __shfl_sync(0xffffffffu, Z, c);
           acc |= 1u << wb;
