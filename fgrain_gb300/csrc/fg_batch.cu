@@ -63,6 +63,7 @@ struct __align__(16) BTile {
   float binw_x, binw_y;
   float pad;                  // leaf box padding
   uint32_t ncap;              // node capacity of the tile's trees
+  uint32_t rbase, rcap;       // first walk record of the tile's tree, and their count
 };
 
 __device__ __forceinline__ int btile_of(const BTile* tiles, int ntiles, unsigned long long g) {
@@ -176,7 +177,7 @@ __device__ __forceinline__ void uf_unite_b(int* parent, int a, int b, uint32_t* 
 // distance lies inside its own leaf box, so the query finds it whatever the tree (bvh.rs:350-402);
 // the union-find roots do not depend on the order of the unions.
 __global__ void k_link_b(const BTile* __restrict__ bt, int ntiles, unsigned long long ncap,
-                         const float4* __restrict__ A, const float4* __restrict__ D, const Node* __restrict__ rnode_all,
+                         const float4* __restrict__ A, const float4* __restrict__ D, const Node4* __restrict__ rnode_all,
                          const uint2* __restrict__ rleaf_all, const uint32_t* __restrict__ ridx_all,
                          const uint8_t* __restrict__ developed, int* parent, const uint32_t* __restrict__ list,
                          const uint32_t* __restrict__ ndev, uint32_t* err) {
@@ -185,7 +186,7 @@ __global__ void k_link_b(const BTile* __restrict__ bt, int ntiles, unsigned long
   const unsigned long long g = list[i];
   const BTile& t = bt[btile_of(bt, ntiles, g)];
   const uint32_t s = static_cast<uint32_t>(g - t.cbase);
-  const Node* nodes = rnode_all + t.nbase;
+  const Node4* nodes = rnode_all + t.rbase;
   const uint2* leaves = rleaf_all + t.nbase;
   const uint32_t* ridx = ridx_all + t.cbase;
   const float4* Ab = A + t.cbase;
@@ -231,41 +232,7 @@ __global__ void k_link_b(const BTile* __restrict__ bt, int ntiles, unsigned long
     if (!index_ok(L.x + L.y <= t.n, err, SITE_LEAF, L.x, L.y)) return;
     for (uint32_t k = 0; k < L.y; ++k) test(ridx[L.x + k]);
   };
-  int stack[RT_MAX_DEPTH + 1];
-  int sp = 0, cur = 0;
-  for (;;) {
-    if (!index_ok(static_cast<uint32_t>(cur) < nmax, err, SITE_NODE, static_cast<uint32_t>(cur), nmax)) break;
-    const Node* nd = nodes + cur;
-    const float4 na = __ldg(&nd->a), nb = __ldg(&nd->b), nc = __ldg(&nd->c);
-    const int4 rf = __ldg(&nd->d);
-    bool hl = rf.x != INT32_MIN && na.x <= hi.x && na.w >= lo.x && na.y <= hi.y && nb.x >= lo.y && na.z <= hi.z &&
-              nb.y >= lo.z;
-    bool hr = rf.y != INT32_MIN && nb.z <= hi.x && nc.y >= lo.x && nb.w <= hi.y && nc.z >= lo.y && nc.x <= hi.z &&
-              nc.w >= lo.z;
-    if (hl && rf.x < 0) {
-      leaf(static_cast<uint32_t>(~rf.x));
-      hl = false;
-    }
-    if (hr && rf.y < 0) {
-      leaf(static_cast<uint32_t>(~rf.y));
-      hr = false;
-    }
-    if (hl && hr) {
-      if (sp <= RT_MAX_DEPTH) {
-        stack[sp++] = rf.y;
-      } else {
-        atomicOr(err, ERR_STACK_OVERFLOW);
-      }
-      cur = rf.x;
-    } else if (hl) {
-      cur = rf.x;
-    } else if (hr) {
-      cur = rf.y;
-    } else {
-      if (sp == 0) break;
-      cur = stack[--sp];
-    }
-  }
+  rt_walk4_box(nodes, lo, hi, t.rcap, err, leaf);
 }
 
 __global__ void k_roots_b(unsigned long long ncap, const uint8_t* developed, int* parent, uint32_t* size,
@@ -529,7 +496,7 @@ static void upload_descriptors(fg_batch* B, cudaStream_t st) {
     t.q = B->Q.p + cb;
     t.d = B->D.p + cb;
     const unsigned long long nb = B->bt[i].nbase;
-    t.rnode = B->rt.rnode.p + nb;
+    t.rnode = B->rt.rnode.p + B->bt[i].rbase;
     t.rleaf = B->rt.rleaf.p + nb;
     t.ridx = B->rt.ridx.p + cb;
     t.s2id = nullptr;
@@ -837,7 +804,10 @@ static void plan(fg_batch* B, const fg_batch_options* opt) {
       FG_REQUIRE(rt[i].ebase == B->syn[i].cbase, "tree layout differs from the crystal slots");
       B->bt[i].nbase = rt[i].nbase;
       B->bt[i].ncap = rt[i].ncap;
+      B->bt[i].rbase = rt[i].rbase;
+      B->bt[i].rcap = rt[i].rcap;
       B->td[i].nnodes = rt[i].ncap;
+      B->td[i].nrec = rt[i].rcap;
       B->td[i].reach = rt[i].reach;
       rs[i] = rt[i];
       rs[i].exp64 = B->exp64.p + B->syn[i].cbase;
@@ -985,10 +955,7 @@ fg_status fg_emulsion_synthesize(fg_engine* e, const fg_emulsion_cfg* cfg, uint6
     em->a = std::move(A);
     em->q = std::move(Q);
     em->d = std::move(D);
-    em->nodes.alloc(std::max<uint32_t>(n > 0 ? n - 1 : 0, 1), st);
-    em->leaf_parent.alloc(std::max<uint32_t>(n, 1), st);
     alloc_state(em.get(), st);
-    if (n) build_lbvh(em.get(), keys.p, em->nodes.p, em->leaf_parent.p, false, st);
     DBuf<uint32_t> none;
     build_emulsion_tree(e, em.get(), false, em->rt, none);
     FG_CUDA(cudaEventRecord(e->timer.ev[1], st));

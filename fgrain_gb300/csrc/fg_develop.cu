@@ -5,7 +5,8 @@
 // index order.  Its clumps are exactly the connected components of the symmetric "touch" graph
 // |p_i - p_j|^2 <= ((r_i fe + r_j fe) prox)^2 over developed crystals (every touch test uses the
 // base expansion fe; the boost is applied after a component is complete).  Here each developed
-// crystal finds its touching neighbours through an LBVH box query and links them with a
+// crystal finds its touching neighbours through a box query on the emulsion's reference tree
+// (the four-wide walk records, fg_rtree.cuh) and links them with a
 // lock-free union-find.  Clump ids follow the reference's numbering: components ranked by their
 // smallest crystal index.  Touch decisions are exact: an FP32 test with an error margin, and the
 // reference's FP64 expression when the margin is too thin to decide.
@@ -61,34 +62,8 @@ __device__ __forceinline__ void uf_unite(int* parent, int a, int b, uint32_t* er
   atomicOr(err, ERR_SPIN_LIMIT);
 }
 
-template <class F>
-__device__ __forceinline__ void walk_box(const Node* __restrict__ nodes, float3 lo, float3 hi,
-                                         uint32_t* err, F&& fn) {
-  int stack[64];
-  int sp = 0, cur = 0;
-  for (;;) {
-    const float4 na = __ldg(&nodes[cur].a), nb = __ldg(&nodes[cur].b), nc = __ldg(&nodes[cur].c);
-    const int4 nd = __ldg(&nodes[cur].d);
-    bool hl = na.x <= hi.x && na.w >= lo.x && na.y <= hi.y && nb.x >= lo.y && na.z <= hi.z && nb.y >= lo.z;
-    bool hr = nb.z <= hi.x && nc.y >= lo.x && nb.w <= hi.y && nc.z >= lo.y && nc.x <= hi.z && nc.w >= lo.z &&
-              nd.y != INT32_MIN;
-    if (hl && nd.x < 0) { fn(static_cast<uint32_t>(~nd.x)); hl = false; }
-    if (hr && nd.y < 0) { fn(static_cast<uint32_t>(~nd.y)); hr = false; }
-    if (hl && hr) {
-      if (sp < 64) stack[sp++] = nd.y; else atomicOr(err, ERR_STACK_OVERFLOW);
-      cur = nd.x;
-    } else if (hl) {
-      cur = nd.x;
-    } else if (hr) {
-      cur = nd.y;
-    } else {
-      if (sp == 0) break;
-      cur = stack[--sp];
-    }
-  }
-}
-
-__global__ void k_link(CrystalsView cv, const Node* __restrict__ nodes, uint32_t n,
+__global__ void k_link(CrystalsView cv, const Node4* __restrict__ rec, uint32_t nrec, const uint2* __restrict__ rleaf,
+                       uint32_t nleaf, const uint32_t* __restrict__ ridx, uint32_t n,
                        const uint8_t* __restrict__ developed, double fe, double prox,
                        double max_base, int* parent, DevCounters* dc, uint32_t* err) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -103,8 +78,8 @@ __global__ void k_link(CrystalsView cv, const Node* __restrict__ nodes, uint32_t
   const float fef = (float)fe, proxf = (float)prox;
   const float rcf = fmaxf(fmaxf(d.x, d.y), d.z) * fef;
   unsigned long long fb = 0;
-  walk_box(nodes, lo, hi, err, [&](uint32_t j) {
-    if (j <= s || !developed[j]) return;
+  auto test = [&](uint32_t j) {
+    if (j <= s || j >= n || !developed[j]) return;
     const float4 aj = cv.a[j], dj = cv.d[j];
     const float dx = aj.x - a.x, dy = aj.y - a.y, dz = aj.z - a.z;
     const float d2 = dx * dx + dy * dy + dz * dz;
@@ -128,6 +103,12 @@ __global__ void k_link(CrystalsView cv, const Node* __restrict__ nodes, uint32_t
       touch_hit = ddot(df, df) <= __dmul_rn(tt, tt);
     }
     if (touch_hit) uf_unite(parent, static_cast<int>(s), static_cast<int>(j), err);
+  };
+  rt_walk4_box(rec, lo, hi, nrec, err, [&](uint32_t leaf) {
+    if (!index_ok(leaf < nleaf, err, SITE_LEAF, leaf, nleaf)) return;
+    const uint2 L = rleaf[leaf];
+    if (!index_ok(L.x + L.y <= n, err, SITE_LEAF, L.x, L.y)) return;
+    for (uint32_t k = 0; k < L.y; ++k) test(ridx[L.x + k]);
   });
   if (fb) atomicAdd(&dc->fallbacks, fb);
 }
@@ -229,7 +210,8 @@ void develop(fg_engine* e, fg_emulsion* em, const fg_dev_cfg& cfg, fg_dev_report
   FG_CUDA(cudaStreamSynchronize(st));
   double max_base;
   std::memcpy(&max_base, &mbits, sizeof(double));
-  k_link<<<G, 256, 0, st>>>(em->view(), em->nodes.p, n, em->developed.p, cfg.filament_expansion,
+  k_link<<<G, 256, 0, st>>>(em->view(), em->rt.rnode.p, static_cast<uint32_t>(em->rt.R), em->rt.rleaf.p,
+                            static_cast<uint32_t>(em->rt.N), em->rt.ridx.p, n, em->developed.p, cfg.filament_expansion,
                             cfg.clumping_proximity_factor, max_base, parent.p, dc.p, e->d_err);
   k_roots<<<G, 256, 0, st>>>(n, em->developed.p, parent.p, s2id, size.p, minid.p, e->d_err);
   k_flags<<<G, 256, 0, st>>>(n, em->developed.p, parent.p, s2id, size.p, minid.p, flag.p, dc.p);

@@ -71,106 +71,14 @@ struct CrystalsView {
   uint32_t n;
 };
 
-// LBVH node, 64 bytes: the boxes of both children plus their indices.  A child index >= 0 is an
-// internal node; a negative index ~s is crystal s.  Leaf boxes bound the crystal's shape (oriented
-// cube or ellipsoid), rounded outward.
-struct __align__(16) Node {
-  float4 a;  // l.lo.x l.lo.y l.lo.z l.hi.x
-  float4 b;  // l.hi.y l.hi.z r.lo.x r.lo.y
-  float4 c;  // r.lo.z r.hi.x r.hi.y r.hi.z
-  int4 d;    // left, right, parent, last leaf of the node's range (leaves are in key order)
-};
-
-// Four-wide node collapsed from the binary LBVH (the transport walk): binary internal node i keeps
-// its grandchildren (or a child leaf in place of an internal child), so one step of a walk covers
-// two binary levels.  Child k's box is (lox[k], loy[k], loz[k]) - (hix[k], hiy[k], hiz[k]); ref[k]
-// is a collapsed node (the binary index, >= 0), a leaf (~crystal, < 0) or empty (INT32_MIN);
-// last[k] is the highest crystal index under child k (-1 when empty).
+// Walk record: a four-wide node of the reference tree, 128 bytes.  Child k's FP32 box is
+// (lox[k], loy[k], loz[k]) - (hix[k], hiy[k], hiz[k]); ref[k] is another record (its index, >= 0),
+// a leaf (~tile-local node id, < 0) or empty (INT32_MIN).  Children are in visiting order.
 struct __align__(16) Node4 {
   float4 lox, loy, loz, hix, hiy, hiz;
   int4 ref;
-  int4 last;
+  int4 _pad;
 };
-
-// Highest leaf under the left child of a binary node whose right child is ref_right (a Karras
-// node's range splits between its children, and an internal node's index is the first leaf of a
-// right child's range), given the node's own last leaf.
-__device__ __forceinline__ int left_last(int ref_right, int node_last) {
-  if (ref_right == INT32_MIN) return node_last;
-  return (ref_right < 0 ? ~ref_right : ref_right) - 1;
-}
-
-// Node4 of binary internal node i.  Every child box is the same box its binary parent holds, so
-// the leaves a walk reaches are those of the binary walk: an ancestor box contains its
-// descendants' boxes, and the slab test is monotone in the box.
-__device__ __forceinline__ void collapse_node4(const Node* __restrict__ nodes, int i, Node4* __restrict__ out) {
-  float v[4][6];
-  int r[4], lst[4];
-  int k = 0;
-  auto add = [&](int ref, int last, float a0, float a1, float a2, float a3, float a4, float a5) {
-    v[k][0] = a0; v[k][1] = a1; v[k][2] = a2; v[k][3] = a3; v[k][4] = a4; v[k][5] = a5;
-    r[k] = ref;
-    lst[k] = last;
-    ++k;
-  };
-  const Node nd = nodes[i];
-  auto expand = [&](int ref, int last, float a0, float a1, float a2, float a3, float a4, float a5) {
-    if (ref == INT32_MIN) return;
-    if (ref < 0) {
-      add(ref, ~ref, a0, a1, a2, a3, a4, a5);
-      return;
-    }
-    const Node ch = nodes[ref];
-    add(ch.d.x, left_last(ch.d.y, ch.d.w), ch.a.x, ch.a.y, ch.a.z, ch.a.w, ch.b.x, ch.b.y);
-    if (ch.d.y != INT32_MIN) add(ch.d.y, ch.d.w, ch.b.z, ch.b.w, ch.c.x, ch.c.y, ch.c.z, ch.c.w);
-    (void)last;
-  };
-  expand(nd.d.x, left_last(nd.d.y, nd.d.w), nd.a.x, nd.a.y, nd.a.z, nd.a.w, nd.b.x, nd.b.y);
-  expand(nd.d.y, nd.d.w, nd.b.z, nd.b.w, nd.c.x, nd.c.y, nd.c.z, nd.c.w);
-  // A slot left free by a leaf child takes the two children of the internal grandchild with the
-  // largest box surface: every internal entry stays at least two levels down, so the walk still
-  // descends two levels per four-wide node and its stack bound is unchanged.
-  while (k < 4) {
-    int best = -1;
-    float barea = -1.0f;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      if (j < k && r[j] >= 0) {
-        const float ex = v[j][3] - v[j][0], ey = v[j][4] - v[j][1], ez = v[j][5] - v[j][2];
-        const float area = ex * ey + ey * ez + ez * ex;
-        if (area > barea) {
-          barea = area;
-          best = j;
-        }
-      }
-    }
-    if (best < 0) break;
-    const Node ch = nodes[r[best]];
-    if (ch.d.y == INT32_MIN) break;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      if (j == best) {
-        v[j][0] = ch.a.x; v[j][1] = ch.a.y; v[j][2] = ch.a.z; v[j][3] = ch.a.w; v[j][4] = ch.b.x; v[j][5] = ch.b.y;
-        r[j] = ch.d.x;
-        lst[j] = left_last(ch.d.y, ch.d.w);
-      }
-    }
-    add(ch.d.y, ch.d.w, ch.b.z, ch.b.w, ch.c.x, ch.c.y, ch.c.z, ch.c.w);
-  }
-  for (; k < 4; ++k) {
-    for (int j = 0; j < 6; ++j) v[k][j] = 0.0f;
-    r[k] = INT32_MIN;
-    lst[k] = -1;
-  }
-  out->lox = make_float4(v[0][0], v[1][0], v[2][0], v[3][0]);
-  out->loy = make_float4(v[0][1], v[1][1], v[2][1], v[3][1]);
-  out->loz = make_float4(v[0][2], v[1][2], v[2][2], v[3][2]);
-  out->hix = make_float4(v[0][3], v[1][3], v[2][3], v[3][3]);
-  out->hiy = make_float4(v[0][4], v[1][4], v[2][4], v[3][4]);
-  out->hiz = make_float4(v[0][5], v[1][5], v[2][5], v[3][5]);
-  out->ref = make_int4(r[0], r[1], r[2], r[3]);
-  out->last = make_int4(lst[0], lst[1], lst[2], lst[3]);
-}
 
 __device__ __forceinline__ int morph_of(const float4& d) { return __float_as_int(d.w); }
 
@@ -415,8 +323,8 @@ enum : uint32_t {
   SITE_PHOTON_CELL = 4,  // photon ordering: emission cell out of range
   SITE_PHOTON_SLOT = 5,  // photon ordering: slot past the photon count
   SITE_PHOTON_ID = 6,    // transport: ordered photon id past the photon count
-  SITE_NODE = 7,         // LBVH walk: internal node index out of range
-  SITE_LEAF = 8,         // LBVH walk: crystal index out of range
+  SITE_NODE = 7,         // tree walk: record index out of range
+  SITE_LEAF = 8,         // tree walk: leaf id or its element range out of range
 };
 
 __device__ __noinline__ static void record_bad_index(uint32_t* err, uint32_t site, uint32_t a, uint32_t b) {

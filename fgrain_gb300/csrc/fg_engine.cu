@@ -238,10 +238,7 @@ fg_status fg_emulsion_upload(fg_engine* e, const fg_emulsion_cfg* cfg, const fg_
       morton_order(em.get(), c->pos, pos.p, st, keys, order);
       gather_sorted(em.get(), order.p, pos.p, dims.p, quat.p, sens.p, c->morphology ? morph.p : nullptr,
                     cfg->morphology, st);
-      em->nodes.alloc(std::max<size_t>(n - 1, 1), st);
-      em->leaf_parent.alloc(n, st);
       alloc_state(em.get(), st);
-      build_lbvh(em.get(), keys.p, em->nodes.p, em->leaf_parent.p, false, st);
       em->h_s2id.resize(n);
       FG_CUDA(cudaMemcpyAsync(em->h_s2id.data(), em->sorted_to_id.p, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
       FG_CUDA(cudaStreamSynchronize(st));

@@ -137,7 +137,8 @@ struct RTreeBufs {
   DBuf<double> nmid;
   DBuf<int2> nchild;              // global ids of the children
   DBuf<uint32_t> wl0, wl1, bq, bqpar, cnt;  // global worklists, block queue (node, buffer parity), counts
-  DBuf<Node> rnode;               // walk records (tile-local refs)
+  unsigned long long R = 0;       // walk records (all tiles)
+  DBuf<Node4> rnode;              // four-wide walk records (tile-local refs)
   DBuf<uint2> rleaf;              // leaf: first element (tile-local position), count
   DBuf<uint32_t> leafof;          // optional: leaf id of each element slot
 };
@@ -165,10 +166,8 @@ struct fg_emulsion {
   // FP64 copies (uploaded sets only).
   fg::DBuf<double> pos64, dims64, quat64, sens64;
   fg::DBuf<uint32_t> sorted_to_id, id_to_sorted;
-  // LBVH over undeveloped geometry (the development's radius queries).
-  fg::DBuf<fg::Node> nodes;
-  fg::DBuf<int> leaf_parent;
-  // The reference tree over all crystals in id order (the transport walks).
+  // The reference tree over all crystals in id order (the transport walks, the development's
+  // radius queries).
   fg::RTreeBufs rt;
   // Mutable per-crystal state (Morton order).
   fg::DBuf<uint32_t> counts;
@@ -196,13 +195,6 @@ struct fg_emulsion {
 namespace fg {
 
 // fg_bvh.cu
-// Builds (or refits) the LBVH of an emulsion whose crystals are already in Morton order.
-// keys: sorted 64-bit Morton keys (device).  developed_geometry: leaf boxes of developed crystals
-// with their expansion (undeveloped leaves get empty boxes) instead of the raw geometry.
-void build_lbvh(fg_emulsion* em, const uint64_t* keys, Node* nodes, int* leaf_parent,
-                bool developed_geometry, cudaStream_t st);
-void refit_lbvh(fg_emulsion* em, Node* nodes, const int* leaf_parent, bool developed_geometry,
-                cudaStream_t st);
 // Sorts crystals by Morton code and fills the hot arrays; returns the sorted keys.
 // pos_host / pos_dev: id-ordered FP64 positions on the host and on the device.
 void morton_order(fg_emulsion* em, const double* pos_host, const double* pos_dev, cudaStream_t st,

@@ -742,10 +742,12 @@ __global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
   }
 }
 
-// Walk records: internal node k gets both child boxes in FP32 (an internal child's box rounded
-// outward and padded, a leaf child's box rounded to nearest), child refs (tile-local id, ~id for a
-// leaf); the super-root (id 0) holds the root as its right child.  leafof[slot] = leaf id.
-__global__ void k_rt_records(RtArgs A, Node* rnode, uint2* rleaf, uint32_t* leafof, unsigned long long leafof_n) {
+// Walk records (fg_rtree.cuh): one thread per node.  A leaf fills its element range and the
+// leaf-of map; the root and every internal node at odd depth write their four-wide record, the
+// grandchildren in the reference's visiting order (right before left, a leaf child in one slot).
+// An internal slot's box is rounded outward, padded and extended by the reach; a leaf slot's box
+// is rounded to nearest.
+__global__ void k_rt_records(RtArgs A, Node4* rec, uint2* rleaf, uint32_t* leafof, unsigned long long leafof_n) {
   const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
   for (unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; g < A.N;
        g += stride) {
@@ -758,47 +760,33 @@ __global__ void k_rt_records(RtArgs A, Node* rnode, uint2* rleaf, uint32_t* leaf
     const uint32_t id = static_cast<uint32_t>(g - T.nbase);
     // (After a failed node allocation, ids below the capacity may never have been set up; the
     // build has flagged the error, and the checks below keep this pass inside its buffers.)
-    if (id >= min(T.nodes, T.ncap) || (id == 1 && T.n == 0)) continue;
-    auto child_box = [&](unsigned long long c, bool leaf, float* f) {
-      const double* b = A.box64 + 6ull * c;
-      if (leaf) {
+    if (id >= min(T.nodes, T.ncap)) continue;
+    Node4* R = rec + T.rbase;
+    float bx[6][4];
+    int ref[4] = {INT32_MIN, INT32_MIN, INT32_MIN, INT32_MIN};
 #pragma unroll
-        for (int k = 0; k < 6; ++k) f[k] = __double2float_rn(b[k]);
-      } else {
+    for (int k = 0; k < 4; ++k)
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          f[k] = __double2float_rd(b[k]) - T.pad - T.reach;
-          f[3 + k] = __double2float_ru(b[3 + k]) + T.pad + T.reach;
-        }
-      }
+      for (int c = 0; c < 6; ++c) bx[c][k] = 0.0f;
+    auto put = [&](int k, Node4* out) {
+      Node4 nd;
+      nd.lox = make_float4(bx[0][0], bx[0][1], bx[0][2], bx[0][3]);
+      nd.loy = make_float4(bx[1][0], bx[1][1], bx[1][2], bx[1][3]);
+      nd.loz = make_float4(bx[2][0], bx[2][1], bx[2][2], bx[2][3]);
+      nd.hix = make_float4(bx[3][0], bx[3][1], bx[3][2], bx[3][3]);
+      nd.hiy = make_float4(bx[4][0], bx[4][1], bx[4][2], bx[4][3]);
+      nd.hiz = make_float4(bx[5][0], bx[5][1], bx[5][2], bx[5][3]);
+      nd.ref = make_int4(ref[0], ref[1], ref[2], ref[3]);
+      nd._pad = make_int4(k, 0, 0, 0);
+      *out = nd;
     };
-    auto ref_of = [&](unsigned long long c, bool& leaf) {
-      leaf = A.nsplit[c] < 0;
-      const int local = static_cast<int>(c - T.nbase);
-      return leaf ? ~local : local;
-    };
-    Node nd;
-    float l[6] = {0, 0, 0, 0, 0, 0}, r[6] = {0, 0, 0, 0, 0, 0};
-    int lref = INT32_MIN, rref = INT32_MIN;
-    if (id == 0) {
-      if (T.n > 0) {
-        bool leaf;
-        rref = ref_of(T.nbase + 1, leaf);
-        child_box(T.nbase + 1, leaf, r);
-      }
-    } else if (A.nsplit[g] >= 0) {
-      const int2 ch = A.nchild[g];
-      if (static_cast<unsigned long long>(ch.x) < T.nbase || static_cast<unsigned long long>(ch.y) >= T.nbase + T.ncap ||
-          static_cast<unsigned long long>(ch.y) < T.nbase || static_cast<unsigned long long>(ch.x) >= T.nbase + T.ncap) {
-        atomicOr(A.err, ERR_BAD_INDEX);
-        continue;
-      }
-      bool ll, rl;
-      lref = ref_of(static_cast<unsigned long long>(ch.x), ll);
-      rref = ref_of(static_cast<unsigned long long>(ch.y), rl);
-      child_box(static_cast<unsigned long long>(ch.x), ll, l);
-      child_box(static_cast<unsigned long long>(ch.y), rl, r);
-    } else {
+    if (id == 0) {  // the super-root slot: an empty tree's record 0
+      if (T.n == 0 && T.rcap > 0) put(0, R);
+      continue;
+    }
+    if (id == 1 && T.n == 0) continue;
+    const bool leaf = A.nsplit[g] < 0;
+    if (leaf) {
       const uint32_t st = A.nstart[g], cn = A.ncount[g];
       if (st < T.ebase || st - T.ebase + static_cast<unsigned long long>(cn) > T.n) {
         atomicOr(A.err, ERR_BAD_INDEX);
@@ -811,11 +799,68 @@ __global__ void k_rt_records(RtArgs A, Node* rnode, uint2* rleaf, uint32_t* leaf
           if (T.ebase + slot < leafof_n) leafof[T.ebase + slot] = id; else atomicOr(A.err, ERR_BAD_INDEX);
         }
     }
-    nd.a = make_float4(l[0], l[1], l[2], l[3]);
-    nd.b = make_float4(l[4], l[5], r[0], r[1]);
-    nd.c = make_float4(r[2], r[3], r[4], r[5]);
-    nd.d = make_int4(lref, rref, 0, 0);
-    rnode[g] = nd;
+    if (id != 1 && (leaf || !(A.ndepth[g] & 1u))) continue;
+    // Slot k takes node c (a global id inside the tile): its box and reference.
+    int k = 0;
+    bool bad = false;
+    auto add = [&](unsigned long long c) {
+      if (c < T.nbase || c >= T.nbase + T.ncap || k >= 4) {
+        bad = true;
+        return;
+      }
+      const double* b = A.box64 + 6ull * c;
+      const int local = static_cast<int>(c - T.nbase);
+      float f[6];
+      if (A.nsplit[c] < 0) {
+#pragma unroll
+        for (int m = 0; m < 6; ++m) f[m] = __double2float_rn(b[m]);
+        ref[k] = ~local;
+      } else {
+        const int2 ch = A.nchild[c];
+        const long long r = (static_cast<long long>(ch.x) - static_cast<long long>(T.nbase)) >> 1;
+        if (r < 1 || r >= static_cast<long long>(T.rcap)) {
+          bad = true;
+          return;
+        }
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+          f[m] = __double2float_rd(b[m]) - T.pad - T.reach;
+          f[3 + m] = __double2float_ru(b[3 + m]) + T.pad + T.reach;
+        }
+        ref[k] = static_cast<int>(r);
+      }
+#pragma unroll
+      for (int m = 0; m < 6; ++m) bx[m][k] = f[m];
+      ++k;
+    };
+    unsigned long long at = 0;  // record index
+    if (leaf) {  // a root leaf
+      add(g);
+    } else {
+      const int2 ch = A.nchild[g];
+      if (id != 1) at = (static_cast<unsigned long long>(ch.x) - T.nbase) >> 1;
+      const unsigned long long cs[2] = {static_cast<unsigned long long>(ch.y), static_cast<unsigned long long>(ch.x)};
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {  // right child first
+        const unsigned long long c = cs[q];
+        if (c < T.nbase || c >= T.nbase + T.ncap) {
+          bad = true;
+          break;
+        }
+        if (A.nsplit[c] < 0) {
+          add(c);
+        } else {
+          const int2 gc = A.nchild[c];
+          add(static_cast<unsigned long long>(gc.y));
+          add(static_cast<unsigned long long>(gc.x));
+        }
+      }
+    }
+    if (bad || at >= T.rcap) {
+      atomicOr(A.err, ERR_BAD_INDEX);
+      continue;
+    }
+    put(k, R + at);
   }
 }
 
@@ -867,17 +912,22 @@ void rtree_alloc(RTreeBufs& B, std::vector<RTile>& tiles, bool want_leafof, cuda
   B.ntiles = static_cast<int>(tiles.size());
   unsigned long long e = 0, nn = 0;
   uint32_t emax = 0;
+  unsigned long long rr = 0;
   for (auto& t : tiles) {
     t.ebase = e;
     t.ncap = static_cast<uint32_t>(std::min<double>(t.ecap + 2.0, std::ceil(t.ecap * node_frac) + 64.0));
     t.nbase = nn;
+    t.rcap = t.ncap / 2 + 1;
+    t.rbase = static_cast<uint32_t>(rr);
     e += t.ecap;
     nn += t.ncap;
+    rr += t.rcap;
     emax = std::max(emax, t.ecap);
   }
   FG_REQUIRE(e < 0x7fffffffull && nn < 0x7fffffffull, "too many elements for one reference-tree build");
   B.E = e;
   B.N = nn;
+  B.R = rr;
   B.levels = levels_for(emax);
   const size_t E1 = static_cast<size_t>(std::max<unsigned long long>(e, 1));
   const size_t N1 = static_cast<size_t>(std::max<unsigned long long>(nn, 1));
@@ -910,7 +960,7 @@ void rtree_alloc(RTreeBufs& B, std::vector<RTile>& tiles, bool want_leafof, cuda
   B.bq.alloc(N1, st);
   B.bqpar.alloc(N1, st);
   B.cnt.alloc(4, st);
-  B.rnode.alloc(N1, st);
+  B.rnode.alloc(std::max<unsigned long long>(rr, 1), st);
   B.rleaf.alloc(N1, st);
   if (want_leafof) B.leafof.alloc(std::max(E1, leafof_slots), st);
   FG_CUDA(cudaMemsetAsync(B.ridx.p, 0, E1 * sizeof(uint32_t), st));
@@ -960,13 +1010,14 @@ size_t carve(RTreeBufs* B, uint32_t ecap, bool want_leafof, uint32_t leafof_slot
   take(b.bq, N1);
   take(b.bqpar, N1);
   take(b.cnt, 4);
-  take(b.rnode, N1);
+  take(b.rnode, N1 / 2 + 1);
   take(b.rleaf, N1);
   if (want_leafof) take(b.leafof, std::max<uint32_t>(leafof_slots, 1));
   if (B) {
     B->ntiles = 1;
     B->E = E1;
     B->N = N1;
+    B->R = N1 / 2 + 1;
     B->nblk = nblk;
     B->levels = levels_for(ecap);
   }
@@ -988,6 +1039,8 @@ void rtree_attach(RTreeBufs& B, RTile tile, bool want_leafof, uint32_t leafof_sl
   tile.ebase = 0;
   tile.nbase = 0;
   tile.ncap = static_cast<uint32_t>(B.N);
+  tile.rbase = 0;
+  tile.rcap = static_cast<uint32_t>(B.R);
   FG_CUDA(cudaMemcpyAsync(B.tiles.p, &tile, sizeof(RTile), cudaMemcpyHostToDevice, st));
 }
 

@@ -16,20 +16,25 @@
 // order (right subtree first, leaf crystals in index order), which sets how the packet energy is
 // shared between the crystals along a segment.
 //
-// Walk records.  Node ids are tile-local; id 0 is a super-root whose only (right) child is the
-// real root (id 1), so every walk starts by testing the root's box as the reference does.  An
-// internal child's FP32 box is its box rounded outward, padded, and extended by the crystals'
-// reach beyond their own boxes, so that a walk clipped to a segment [0, step] still reaches every
-// leaf holding a crystal the segment hits (the corner of a rotated cube can lie outside its
-// leaf's box, nearer than the box); a leaf child's box is rounded to nearest, for the reference's
-// own leaf test.
+// Walk records.  Node ids are tile-local; the root is id 1, children come in pairs (l, l + 1) =
+// (left, right).  The walks run over four-wide records: the record of an internal node at odd depth
+// (the root's is record 0, any other's is record l / 2 of its children's pair l) holds that node's
+// grandchildren, a leaf child taking one slot itself, in the order the reference's walk visits
+// them (right subtree before left: RR, RL, LR, LL).  A child box contains its descendants' boxes,
+// and the slab test is monotone in the box, so testing a grandchild alone reaches exactly the
+// leaves the binary walk reaches, in the same order.  An internal child's FP32 box is its box
+// rounded outward, padded, and extended by the crystals' reach beyond their own boxes, so that a
+// walk clipped to a segment [0, step] still reaches every leaf holding a crystal the segment hits
+// (the corner of a rotated cube can lie outside its leaf's box, nearer than the box); a leaf
+// child's box is rounded to nearest, for the reference's own leaf test.
 #pragma once
 #include "fg_device.cuh"
 
 namespace fg {
 
 constexpr int RT_CTA_MAX = 1024;   // nodes of at most this many crystals are finished by one block
-constexpr int RT_MAX_DEPTH = 47;   // deeper trees are rejected (the walks keep 48-entry stacks)
+constexpr int RT_MAX_DEPTH = 47;   // deeper trees are rejected (bounds the walks' stacks)
+constexpr int RT_STACK4 = 3 * ((RT_MAX_DEPTH + 1) / 2);  // four-wide walk: three pushes per record level
 constexpr uint32_t RT_DONE = 0x80000000u;
 
 // Per-tree input and bookkeeping of one tile (or one emulsion).  Element slots are tile-relative.
@@ -49,7 +54,8 @@ struct __align__(16) RTile {
   uint32_t depth;            // deepest level (written by the build)
   float pad;                 // outward padding of internal boxes in the FP32 walk records
   float reach;               // and their extension by the crystals' reach beyond their own boxes
-  uint32_t _pad[3];
+  uint32_t rbase, rcap;      // first walk record of the tile, and the tile's record capacity
+  uint32_t _pad;
 };
 static_assert(sizeof(RTile) == 112, "RTile layout");
 
@@ -71,7 +77,7 @@ constexpr size_t rtree_attach_bytes(size_t ecap, bool want_leafof, size_t slots)
   const size_t e1 = ecap > 0 ? ecap : 1, n1 = rt_attach_nodes(e1);
   return rt_al(112) + 4 * rt_al(4 * e1) + 2 * rt_al(32 * e1) + 2 * rt_al(4 * (e1 + 1)) + rt_al(4 * rt_attach_blocks(e1)) +
          3 * rt_al(4 * e1) + rt_al(96 * n1) + rt_al(48 * n1) + 4 * rt_al(4 * n1) + rt_al(4 * n1) + rt_al(8 * n1) +
-         rt_al(8 * n1) + 4 * rt_al(4 * n1) + rt_al(16) + rt_al(64 * n1) + rt_al(8 * n1) +
+         rt_al(8 * n1) + 4 * rt_al(4 * n1) + rt_al(16) + rt_al(128 * (n1 / 2 + 1)) + rt_al(8 * n1) +
          (want_leafof ? rt_al(4 * (slots > 0 ? slots : 1)) : 0);
 }
 
@@ -127,6 +133,42 @@ __device__ __forceinline__ void rt_box_pm(const double4_32a& v, double lo[3], do
     lo[i] = __dsub_rn(p[i], v.w);
     hi[i] = __dadd_rn(p[i], v.w);
     c[i] = __dmul_rn(0.5, __dadd_rn(lo[i], hi[i]));
+  }
+}
+
+// Every leaf of a tree whose box overlaps the query box [lo, hi], through the four-wide records
+// (fn(local leaf id); the order of the calls is not the reference's, for order-free queries such
+// as BVH::query_radius, bvh.rs:350-402).  A leaf is reached iff its box and its ancestors' boxes
+// overlap the query, and ancestor boxes contain their descendants'.  nrec bounds the records.
+template <class F>
+__device__ __forceinline__ void rt_walk4_box(const Node4* __restrict__ rec, float3 lo, float3 hi, uint32_t nrec,
+                                             uint32_t* err, F&& fn) {
+  int stack[RT_STACK4];
+  int sp = 0, cur = 0;
+  for (;;) {
+    if (!index_ok(static_cast<uint32_t>(cur) < nrec, err, SITE_NODE, static_cast<uint32_t>(cur), nrec)) break;
+    const Node4* nd = rec + cur;
+    const float4 lx = __ldg(&nd->lox), ly = __ldg(&nd->loy), lz = __ldg(&nd->loz);
+    const float4 hx = __ldg(&nd->hix), hy = __ldg(&nd->hiy), hz = __ldg(&nd->hiz);
+    const int4 rf = __ldg(&nd->ref);
+    const float ax[4] = {lx.x, lx.y, lx.z, lx.w}, ay[4] = {ly.x, ly.y, ly.z, ly.w}, az[4] = {lz.x, lz.y, lz.z, lz.w};
+    const float bx[4] = {hx.x, hx.y, hx.z, hx.w}, by[4] = {hy.x, hy.y, hy.z, hy.w}, bz[4] = {hz.x, hz.y, hz.z, hz.w};
+    const int r[4] = {rf.x, rf.y, rf.z, rf.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (r[k] == INT32_MIN) continue;
+      if (ax[k] <= hi.x && bx[k] >= lo.x && ay[k] <= hi.y && by[k] >= lo.y && az[k] <= hi.z && bz[k] >= lo.z) {
+        if (r[k] < 0) {
+          fn(static_cast<uint32_t>(~r[k]));
+        } else if (sp < RT_STACK4) {
+          stack[sp++] = r[k];
+        } else {
+          atomicOr(err, ERR_STACK_OVERFLOW);
+        }
+      }
+    }
+    if (sp == 0) break;
+    cur = stack[--sp];
   }
 }
 

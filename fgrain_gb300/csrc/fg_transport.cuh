@@ -15,7 +15,7 @@ struct __align__(16) TileDesc {
   const float4* a;
   const float4* q;
   const float4* d;
-  const Node* rnode;
+  const Node4* rnode;     // four-wide walk records of the tile's tree
   const uint2* rleaf;
   const uint32_t* ridx;
   const uint32_t* s2id;
@@ -23,7 +23,8 @@ struct __align__(16) TileDesc {
   const float* tile;
   unsigned long long photon_base;
   uint32_t n, tw, th, P;
-  uint32_t nnodes;  // node capacity of the tile's tree (bounds the node ids the walk reads)
+  uint32_t nnodes;  // node capacity of the tile's tree (bounds the leaf ids the walk reads)
+  uint32_t nrec;    // walk records of the tile's tree (bounds the record indices)
   float reach;      // crystals' reach beyond their own boxes (fg_rtree.cuh)
   uint32_t stride;  // exposure row stride (floats); tiles may be windows of one image
   uint32_t pcell_base;  // first photon-sort cell of this tile
@@ -35,22 +36,25 @@ struct __align__(16) TileDesc {
 };
 
 // Walk of a reference tree in the reference's order (BVH::intersect_ray_all, bvh.rs:300-347: push
-// left then right, pop right first), deferred: a hit leaf is queued until every lane of `amask`
-// holds one or has finished, then the lanes run fn(leaf) together; a lane that holds a leaf walks on
-// (speculatively) until it holds WALK_LEAVES.  The queue keeps each lane's leaves in walk order.
-// An internal child is entered when its (extended) box meets [0, tlim] of the ray (the caller's
-// step, padded); a leaf child when its box extended by `reach` meets [0, tlim] (a crystal hit
-// inside the step lies there) and its own box meets the whole ray (the reference's leaf test,
-// bvh.rs:96-124).  nmax bounds the node ids (index checks).  With amask = the lane's own bit it is
-// a plain walk.
+// left then right, pop right first) over its four-wide records (fg_rtree.cuh), whose children
+// are stored in that visiting order: the first hit child is entered, the other hit children are
+// pushed so that they come off the stack in order.  Deferred: a hit leaf is queued until every
+// lane of `amask` holds one or has finished, then the lanes run fn(leaf) together; a lane that
+// holds a leaf walks on (speculatively) until it holds WALK_LEAVES.  The queue keeps each lane's
+// leaves in walk order.  An internal child is entered when its (extended) box meets [0, tlim] of
+// the ray (the caller's step, padded); a leaf child when its box extended by `reach` meets
+// [0, tlim] (a crystal hit inside the step lies there) and its own box meets the whole ray (the
+// reference's leaf test, bvh.rs:96-124).  nrec and nleaf bound the record indices and leaf ids
+// (index checks).  With amask = the lane's own bit it is a plain walk.
 template <class F>
-__device__ __forceinline__ void rt_walk_deferred(const Node* __restrict__ nodes, float3 o, float3 inv, float tlim,
-                                                 float reach, uint32_t* err, F&& fn, uint32_t nmax, unsigned amask) {
+__device__ __forceinline__ void rt_walk_deferred(const Node4* __restrict__ rec, float3 o, float3 inv, float tlim,
+                                                 float reach, uint32_t* err, F&& fn, uint32_t nrec, uint32_t nleaf,
+                                                 unsigned amask) {
   constexpr int EMPTY = INT32_MIN;
   constexpr uint32_t NONE = 0xffffffffu;
-  int stack[RT_MAX_DEPTH + 1];
+  int stack[RT_STACK4];
   int sp = 0;
-  int cur = 0;  // the super-root
+  int cur = 0;  // record 0: the root's
   uint32_t lv[WALK_LEAVES];
 #pragma unroll
   for (int j = 0; j < WALK_LEAVES; ++j) lv[j] = NONE;
@@ -74,13 +78,14 @@ __device__ __forceinline__ void rt_walk_deferred(const Node* __restrict__ nodes,
         cur = sp > 0 ? stack[--sp] : EMPTY;
         continue;
       }
-      if (!index_ok(static_cast<uint32_t>(cur) < nmax, err, SITE_NODE, static_cast<uint32_t>(cur), nmax)) {
+      if (!index_ok(static_cast<uint32_t>(cur) < nrec, err, SITE_NODE, static_cast<uint32_t>(cur), nrec)) {
         cur = EMPTY;
         continue;
       }
-      const Node* nd = nodes + cur;
-      const float4 na = __ldg(&nd->a), nb = __ldg(&nd->b), nc = __ldg(&nd->c);
-      const int4 rf = __ldg(&nd->d);
+      const Node4* nd = rec + cur;
+      const float4 lx = __ldg(&nd->lox), ly = __ldg(&nd->loy), lz = __ldg(&nd->loz);
+      const float4 hx = __ldg(&nd->hix), hy = __ldg(&nd->hiy), hz = __ldg(&nd->hiz);
+      const int4 rf = __ldg(&nd->ref);
       // Slab test as lo * inv - o * inv (one FMA per plane), the box grown by g, clipped to [0, t].
       auto slab_hit = [&](float a0, float a1, float a2, float a3, float a4, float a5, float g, float t) {
         const float t1x = fmaf(a0 - g, inv.x, -oi.x), t2x = fmaf(a3 + g, inv.x, -oi.x);
@@ -95,31 +100,48 @@ __device__ __forceinline__ void rt_walk_deferred(const Node* __restrict__ nodes,
         if (ref >= 0) return slab_hit(a0, a1, a2, a3, a4, a5, 0.0f, tlim);
         return slab_hit(a0, a1, a2, a3, a4, a5, reach, tlim) && slab_hit(a0, a1, a2, a3, a4, a5, 0.0f, INFINITY);
       };
-      const bool hl = hit(rf.x, na.x, na.y, na.z, na.w, nb.x, nb.y);
-      const bool hr = hit(rf.y, nb.z, nb.w, nc.x, nc.y, nc.z, nc.w);
-      if (hr) {
-        if (hl) {
-          if (sp <= RT_MAX_DEPTH) {
-            stack[sp++] = rf.x;
+      const bool h0 = hit(rf.x, lx.x, ly.x, lz.x, hx.x, hy.x, hz.x);
+      const bool h1 = hit(rf.y, lx.y, ly.y, lz.y, hx.y, hy.y, hz.y);
+      const bool h2 = hit(rf.z, lx.z, ly.z, lz.z, hx.z, hy.z, hz.z);
+      const bool h3 = hit(rf.w, lx.w, ly.w, lz.w, hx.w, hy.w, hz.w);
+      // Enter the first hit child; push the later ones, last first.
+      int next = EMPTY;
+      auto take = [&](bool h, int r) {
+        if (!h) return;
+        if (next != EMPTY) {
+          if (sp < RT_STACK4) {
+            stack[sp++] = next;
           } else {
             atomicOr(err, ERR_STACK_OVERFLOW);
           }
         }
-        cur = rf.y;
-      } else if (hl) {
-        cur = rf.x;
-      } else {
-        cur = sp > 0 ? stack[--sp] : EMPTY;
-      }
+        next = r;
+      };
+      take(h3, rf.w);
+      take(h2, rf.z);
+      take(h1, rf.y);
+      take(h0, rf.x);
+      cur = next != EMPTY ? next : (sp > 0 ? stack[--sp] : EMPTY);
     }
     if (!__any_sync(amask, lv[0] != NONE)) break;
     if (lv[0] != NONE) {
-      if (index_ok(lv[0] < nmax, err, SITE_LEAF, lv[0], nmax)) fn(lv[0]);
+      if (index_ok(lv[0] < nleaf, err, SITE_LEAF, lv[0], nleaf)) fn(lv[0]);
 #pragma unroll
       for (int j = 0; j + 1 < WALK_LEAVES; ++j) lv[j] = lv[j + 1];
       lv[WALK_LEAVES - 1] = NONE;
     }
   }
+}
+
+// 1 / d for the walk's slab tests, kept finite: the test forms lo * inv - o * inv with one FMA, and
+// an infinite inv (a direction component of 0, or below 1e-30) would turn that into inf - inf =
+// NaN, which fminf / fmaxf drop, so the axis would not constrain the box at all (a parent box
+// could fail while its child passes).  With |inv| capped at 1e30 the products stay finite
+// (coordinates are below 1e4 um) and the slab is (-huge, huge) or empty as for the reference's
+// infinite inv (bvh.rs:96-124); only a box face within about 1e-7 relative of the ray's
+// coordinate can be judged either way.
+__device__ __forceinline__ float slab_inv(float d) {
+  return fabsf(d) < 1e-30f ? copysignf(1e30f, d) : 1.0f / d;
 }
 
 // Beer-Lambert absorption of one hit and Bernoulli rounding of the latent photons
@@ -205,7 +227,7 @@ __device__ __forceinline__ bool photon_bounce(const TileDesc& t, Photon& ph, uin
   const float fp = t.mu_t > 0.0f ? -__logf(fmaxf(1.0f - uf(rb.x), 1.17549435e-38f)) / t.mu_t : 1e6f;
   const float step = fminf(fp, t.D * 1.5f);
   const float3 pos = ph.pos, dir = ph.dir;
-  const float3 inv = make_float3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
+  const float3 inv = make_float3(slab_inv(dir.x), slab_inv(dir.y), slab_inv(dir.z));
   float E = ph.E;
   uint32_t nh = 0;
   P4 r{};
@@ -232,7 +254,7 @@ __device__ __forceinline__ bool photon_bounce(const TileDesc& t, Photon& ph, uin
       ++nh;
     }
   };
-  rt_walk_deferred(t.rnode, pos, inv, step * 1.00001f + 1e-3f, t.reach, err, leaf, t.nnodes,
+  rt_walk_deferred(t.rnode, pos, inv, step * 1.00001f + 1e-3f, t.reach, err, leaf, t.nrec, t.nnodes,
                    amask ? amask : (1u << (threadIdx.x & 31)));
   nhit = nh;
   const float3 np = make_float3(pos.x + dir.x * step, pos.y + dir.y * step, pos.z + dir.z * step);
