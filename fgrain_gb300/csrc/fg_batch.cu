@@ -797,7 +797,8 @@ static void plan(fg_batch* B, const fg_batch_options* opt) {
       t.d = B->D.p + B->syn[i].cbase;
       t.ecap = B->syn[i].ccap;
       t.pad = B->bt[i].pad;
-      t.reach = rt_reach(0.48 * B->params[i].r_min);  // the synthesis's radius clamp (emulsion.rs:162-170)
+      // The synthesis's radius clamp (emulsion.rs:162-170) for cubes; the other shapes lie in their boxes.
+      t.reach = rt_reach(B->params[i].morphology == FG_CUBIC ? 0.48 * B->params[i].r_min : 0.0);
     }
     rtree_alloc(B->rt, rt, true, st, RT_NODE_FRAC);
     for (uint32_t i = 0; i < n; ++i) {
@@ -952,6 +953,7 @@ fg_status fg_emulsion_synthesize(fg_engine* e, const fg_emulsion_cfg* cfg, uint6
     em->has64 = false;
     em->extent = std::max(std::max(cfg->width, cfg->height), cfg->depth);
     em->max_half_dim = 0.48 * cfg->r_min;  // the radius clamp of the synthesis (emulsion.rs:162-170)
+    em->any_cubic = cfg->morphology == FG_CUBIC;
     em->a = std::move(A);
     em->q = std::move(Q);
     em->d = std::move(D);

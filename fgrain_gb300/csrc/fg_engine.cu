@@ -220,6 +220,8 @@ fg_status fg_emulsion_upload(fg_engine* e, const fg_emulsion_cfg* cfg, const fg_
     em->has64 = true;
     for (size_t i = 0; i < 3 * n; ++i) em->extent = std::max(em->extent, std::fabs(c->pos[i]));
     for (size_t i = 0; i < 3 * n; ++i) em->max_half_dim = std::max(em->max_half_dim, c->dims[i]);
+    em->any_cubic = c->morphology ? std::any_of(c->morphology, c->morphology + n, [](int32_t m) { return m == FG_CUBIC; })
+                                  : cfg->morphology == FG_CUBIC;
     FG_CUDA(cudaEventRecord(e->timer.ev[0], st));
     if (n) {
       DBuf<double> pos, dims, quat, sens;

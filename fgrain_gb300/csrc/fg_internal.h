@@ -178,6 +178,7 @@ struct fg_emulsion {
   bool has64 = false;
   double extent = 0.0;             // largest coordinate magnitude (sets the box padding)
   double max_half_dim = 0.0;       // largest crystal half-dimension (sets the walks' reach)
+  bool any_cubic = true;           // some crystal is a cube (only a cube reaches out of its box)
   std::vector<uint32_t> h_s2id;    // host copy of sorted_to_id (empty: identity)
 
   fg::CrystalsView view() const {

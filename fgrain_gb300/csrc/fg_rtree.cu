@@ -1101,7 +1101,7 @@ void build_emulsion_tree(fg_engine* e, const fg_emulsion* em, bool developed_onl
   t.dims64 = em->has64 ? em->dims64.p : nullptr;
   t.exp64 = developed_only ? em->exp64.p : nullptr;
   t.pad = static_cast<float>(std::max(em->extent, std::max(em->cfg.width, em->cfg.height)) * 2e-6 + 1e-5);
-  t.reach = developed_only ? 0.0f : rt_reach(em->max_half_dim);
+  t.reach = developed_only ? 0.0f : rt_reach(em->any_cubic ? em->max_half_dim : 0.0);
   const uint32_t* id2s = em->h_s2id.empty() ? nullptr : em->id_to_sorted.p;
   uint32_t m = n;
   if (developed_only && n) {

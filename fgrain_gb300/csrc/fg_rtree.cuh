@@ -60,7 +60,9 @@ struct __align__(16) RTile {
 static_assert(sizeof(RTile) == 112, "RTile layout");
 
 // How far a crystal's geometry reaches beyond its own max_dim box (crystal.rs:106-217): a cube of
-// half-size m lies within sqrt(3) m of its centre, an ellipsoid within m; so (sqrt(3) - 1) m.
+// half-size m lies within sqrt(3) m of its centre, an ellipsoid (the tabular and octahedral
+// shapes) within m; so (sqrt(3) - 1) m for a set with cubes (m its largest half-size), else 0,
+// plus a margin for FP32 rounding.
 inline float rt_reach(double max_half_dim) {
   return static_cast<float>(0.7320508075688773 * max_half_dim * 1.0001 + 1e-5);
 }

@@ -235,7 +235,7 @@ TileDesc make_tile_desc(const fg_emulsion* em, const float* tile_dev, uint32_t t
   t.ridx = em->rt.ridx.p;
   t.nnodes = static_cast<uint32_t>(em->rt.N);
   t.nrec = static_cast<uint32_t>(em->rt.R);
-  t.reach = rt_reach(em->max_half_dim);
+  t.reach = rt_reach(em->any_cubic ? em->max_half_dim : 0.0);
   t.s2id = em->sorted_to_id.p;
   t.n = em->n;
   t.counts = counts;
