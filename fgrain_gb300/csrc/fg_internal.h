@@ -128,7 +128,7 @@ struct RTreeBufs {
   uint32_t count = 0;             // elements of a one-tile tree built on the host's request
   DBuf<RTile> tiles;
   DBuf<uint32_t> idx0, idx1, nof0, nof1, flag, bb, blk, P, Q;
-  DBuf<double4_32a> pm0, pm1;         // element position and half-size, travelling with the order
+  DBuf<unsigned long long> key0, key1;  // nine ordered keys per element (SoA), travelling with the order
   DBuf<uint32_t> ridx;            // final element order (slots): a leaf's crystals in reference order
   DBuf<unsigned long long> acc;   // per node: 6 ordered minima, 6 ordered maxima
   DBuf<double> box64;             // per node: lo xyz, hi xyz (FP64, exact)

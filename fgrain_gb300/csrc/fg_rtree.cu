@@ -8,7 +8,8 @@
 //           flags (ranks of bigs inside each node's contiguous range) in the same passes;
 //   pq      P_m = position of the m-th big from the left, Q_m = of the m-th small from the right;
 //   place   every element moves to where the reference's swap partition puts it (below).
-// Each element's position and half-size (FP64) travel with it, so every pass reads them in order.
+// Each element's nine order-preserving 64-bit keys (box lo, hi and centroid of its FP64 max_dim
+// box, computed once) travel with it, so every pass reads them in order and none does FP64 work.
 // Nodes of at most RT_CTA_MAX elements leave the global levels: one thread block each builds
 // their subtree with the elements in shared memory, the same passes per level, all levels down to
 // the leaves.  Node boxes are reduced segment-wise (a node is a contiguous range of positions).
@@ -73,7 +74,9 @@ struct RtArgs {
   int ntiles;
   unsigned long long E, N;
   uint32_t* idx[2];
-  double4_32a* pm[2];  // position xyz and half-size (max_dim * expansion) of the element, in FP64
+  // Keys of the element at position x, field f at key[c][f * E + x]: ord64 of the box lo xyz (f
+  // 0-2), hi xyz (3-5) and centroid xyz (6-8).
+  unsigned long long* key[2];
   uint32_t* nof[2];
   uint32_t* flag;
   uint32_t* bb;
@@ -122,6 +125,35 @@ __device__ __forceinline__ void rt_enqueue(const RtArgs& A, uint32_t id, uint32_
   }
 }
 
+// The 12 reduction keys of the element at position x of a key array (field f at key[f * stride +
+// x]): box lo xyz and centroid xyz (minima), box hi xyz and centroid xyz (maxima).  Min and max
+// are exact in any order, and on the ordered 64-bit keys they run on the integer pipes (GB300's
+// FP64 pipe is narrow).
+__device__ __forceinline__ void rt_keys(const unsigned long long* key, unsigned long long stride, unsigned long long x,
+                                        unsigned long long k[12]) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    k[i] = key[i * stride + x];
+    k[6 + i] = key[(3 + i) * stride + x];
+    k[3 + i] = key[(6 + i) * stride + x];
+    k[9 + i] = k[3 + i];
+  }
+}
+
+// The nine keys of element slot s of tile T, written to position x of key[f * stride + x]
+// (centroids normalised so that -0 orders as +0, as the FP64 comparisons see them).
+__device__ __forceinline__ void rt_key9(const RTile& T, uint32_t s, unsigned long long* key, unsigned long long stride,
+                                        unsigned long long x) {
+  double lo[3], hi[3], cc[3];
+  rt_box_pm(rt_pm(T, s), lo, hi, cc);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    key[i * stride + x] = ord64(lo[i]);
+    key[(3 + i) * stride + x] = ord64(hi[i]);
+    key[(6 + i) * stride + x] = ord64(__dadd_rn(cc[i], 0.0));
+  }
+}
+
 // Element order and roots.  Thread x < E fills position x; one thread per tile sets up its root.
 __global__ void k_rt_init(RtArgs A) {
   const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
@@ -134,7 +166,7 @@ __global__ void k_rt_init(RtArgs A) {
     if (k < T.n) {
       const uint32_t slot = T.order ? static_cast<uint32_t>(T.order[k] - T.obase) : static_cast<uint32_t>(k);
       A.idx[0][x] = slot;
-      A.pm[0][x] = rt_pm(T, slot);
+      rt_key9(T, slot, A.key[0], A.E, x);
       v = T.n > static_cast<uint32_t>(RT_CTA_MAX) ? static_cast<uint32_t>(T.nbase + 1) : RT_DONE;
     }
     A.nof[0][x] = v;
@@ -149,21 +181,6 @@ __global__ void k_rt_init(RtArgs A) {
     A.ntile[root] = static_cast<uint32_t>(t);
     A.ndepth[root] = 1;
     rt_enqueue(A, static_cast<uint32_t>(root), T.n, 0);
-  }
-}
-
-// The 12 ordered keys of element slot s: box lo xyz and centroid xyz (minima), box hi xyz and
-// centroid xyz (maxima).  Min and max are exact in any order, and on the ordered 64-bit keys they
-// run on the integer pipes (GB300's FP64 pipe is narrow).
-__device__ __forceinline__ void rt_keys(const double4_32a& v, unsigned long long k[12]) {
-  double lo[3], hi[3], cc[3];
-  rt_box_pm(v, lo, hi, cc);
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    k[i] = ord64(lo[i]);
-    k[3 + i] = ord64(cc[i]);
-    k[6 + i] = ord64(hi[i]);
-    k[9 + i] = ord64(cc[i]);
   }
 }
 
@@ -210,7 +227,7 @@ __global__ void k_rt_reduce(RtArgs A, int c) {
     const bool act = !(node & RT_DONE);
     if (!__any_sync(0xffffffffu, act)) continue;
     unsigned long long k[12];
-    if (act) rt_keys(A.pm[c][x], k); else rt_keys_empty(k);
+    if (act) rt_keys(A.key[c], A.E, x, k); else rt_keys_empty(k);
     const bool head = rt_seg_reduce(act ? node : (RT_DONE | (threadIdx.x & 31)), k);
     if (act && head) {
       unsigned long long* a = A.acc + 12ull * node;
@@ -290,10 +307,7 @@ __device__ __forceinline__ uint32_t rt_flag(const RtArgs& A, int c, unsigned lon
   if (node & RT_DONE) return 0u;
   const int axis = A.nsplit[node];
   if (axis < 0) return 0u;
-  const double4_32a v = A.pm[c][x];
-  const double p = axis == 0 ? v.x : (axis == 1 ? v.y : v.z);
-  const double cc = __dmul_rn(0.5, __dadd_rn(__dsub_rn(p, v.w), __dadd_rn(p, v.w)));
-  return cc < A.nmid[node] ? 0u : 1u;
+  return A.key[c][(6 + axis) * A.E + x] < ord64(A.nmid[node]) ? 0u : 1u;
 }
 
 // Flags and their block sums.
@@ -411,7 +425,8 @@ __global__ void k_rt_place(RtArgs A, int c) {
     const uint32_t child = static_cast<uint32_t>(left ? ch.x : ch.y);
     const uint32_t csize = left ? Sp : n - Sp;
     A.idx[o][s + dest] = el;
-    A.pm[o][s + dest] = A.pm[c][x];
+#pragma unroll
+    for (int f = 0; f < 9; ++f) A.key[o][f * A.E + s + dest] = A.key[c][f * A.E + x];
     A.nof[o][s + dest] = csize > static_cast<uint32_t>(RT_CTA_MAX) ? child : RT_DONE;
     if (r == 0) {
       const uint32_t t = A.ntile[node], dep = A.ndepth[node] + 1;
@@ -455,17 +470,24 @@ static_assert(RT_CTA_LV < RT_CTA_FREE, "level slots must fit a byte");
 static_assert(RT_CTA_MAX <= 2048, "positions are packed in 11 bits");
 
 struct RtCtaSmem {
-  double4_32a pm[RT_CTA_MAX];                 // element position and half-size
-  unsigned long long acc[RT_CTA_LV][12];  // per level node: ordered minima, maxima
+  unsigned long long key[9][RT_CTA_MAX];  // the job's element keys, at their load position (home)
+  // Per level: the nodes' box accumulators (reduce to decide), then the flags' prefix sum and the
+  // ranks (flags to place); the two uses do not overlap.
+  union {
+    unsigned long long acc[RT_CTA_LV][12];  // per level node: ordered minima, maxima
+    struct {
+      uint16_t bb[RT_CTA_MAX + 1];          // exclusive prefix sum of the flags
+      uint16_t P[RT_CTA_MAX], Q[RT_CTA_MAX];
+    } r;
+  } u;
   double mid[RT_CTA_LV];
   uint32_t idx[RT_CTA_MAX];               // element slot
+  uint16_t home[RT_CTA_MAX];              // element's load position (its keys)
   uint32_t id[2][RT_CTA_LV];              // this level's nodes and the next's
   uint32_t child[RT_CTA_LV];              // first child id of a splitting node
   uint32_t sl[RT_CTA_SL];                 // small leaves: position | count << 11 | depth << 14
   uint32_t slid[RT_CTA_SL];
   uint32_t scan[RT_CTA_T / 32];
-  uint16_t bb[RT_CTA_MAX + 1];            // exclusive prefix sum of the flags
-  uint16_t P[RT_CTA_MAX], Q[RT_CTA_MAX];
   uint16_t off[2][RT_CTA_LV], cnt[2][RT_CTA_LV];
   uint16_t sp[RT_CTA_LV];                 // left child size
   uint8_t nd[RT_CTA_MAX];                 // level slot of the position's node, RT_CTA_FREE when done
@@ -491,7 +513,9 @@ __global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
     const uint32_t dep0 = min(A.ndepth[root], 255u);
     for (int x = tid; x < RT_CTA_MAX; x += RT_CTA_T) {
       if (x < n) {
-        S.pm[x] = A.pm[par][s + x];
+#pragma unroll
+        for (int f = 0; f < 9; ++f) S.key[f][x] = A.key[par][f * A.E + s + x];
+        S.home[x] = static_cast<uint16_t>(x);
         S.idx[x] = A.idx[par][s + x];
         S.nd[x] = n > RT_LEAF_MAX ? 0 : RT_CTA_FREE;
       } else {
@@ -526,7 +550,7 @@ __global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
         unsigned long long k[12], kk[12];
         rt_keys_empty(k);
         for (int j = 0; j < cn; ++j) {
-          rt_keys(S.pm[o0 + j], kk);
+          rt_keys(&S.key[0][0], RT_CTA_MAX, S.home[o0 + j], kk);
 #pragma unroll
           for (int m = 0; m < 6; ++m) {
             k[m] = umin64(k[m], kk[m]);
@@ -545,7 +569,7 @@ __global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
         A.nsplit[id] = -1;
         atomicMax(&S.maxdep, dp);
       }
-      for (int i = tid; i < nl * 12; i += RT_CTA_T) S.acc[i / 12][i % 12] = (i % 12) < 6 ? ~0ull : 0ull;
+      for (int i = tid; i < nl * 12; i += RT_CTA_T) S.u.acc[i / 12][i % 12] = (i % 12) < 6 ? ~0ull : 0ull;
       __syncthreads();
       if (nl == 0) break;
       if (tid == 0) {
@@ -560,13 +584,13 @@ __global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
         const bool act = node != RT_CTA_FREE;
         if (!__any_sync(0xffffffffu, act)) continue;
         unsigned long long kk[12];
-        if (act) rt_keys(S.pm[x], kk); else rt_keys_empty(kk);
+        if (act) rt_keys(&S.key[0][0], RT_CTA_MAX, S.home[x], kk); else rt_keys_empty(kk);
         const bool head = rt_seg_reduce(act ? node : (0x100u | static_cast<uint32_t>(lane)), kk);
         if (act && head) {
 #pragma unroll
-          for (int i = 0; i < 6; ++i) atomicMin(&S.acc[node][i], kk[i]);
+          for (int i = 0; i < 6; ++i) atomicMin(&S.u.acc[node][i], kk[i]);
 #pragma unroll
-          for (int i = 6; i < 12; ++i) atomicMax(&S.acc[node][i], kk[i]);
+          for (int i = 6; i < 12; ++i) atomicMax(&S.u.acc[node][i], kk[i]);
         }
       }
       __syncthreads();
@@ -577,10 +601,10 @@ __global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
         double lo[3], hi[3], clo[3], chi[3];
 #pragma unroll
         for (int m = 0; m < 3; ++m) {
-          lo[m] = unord64(S.acc[i][m]);
-          clo[m] = unord64(S.acc[i][3 + m]);
-          hi[m] = unord64(S.acc[i][6 + m]);
-          chi[m] = unord64(S.acc[i][9 + m]);
+          lo[m] = unord64(S.u.acc[i][m]);
+          clo[m] = unord64(S.u.acc[i][3 + m]);
+          hi[m] = unord64(S.u.acc[i][6 + m]);
+          chi[m] = unord64(S.u.acc[i][9 + m]);
           A.box64[6ull * id + m] = lo[m];
           A.box64[6ull * id + 3 + m] = hi[m];
         }
@@ -617,13 +641,8 @@ __global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
           const int x = RT_CTA_PER * tid + k;
           const uint32_t node = S.nd[x];
           f[k] = 0;
-          if (node != RT_CTA_FREE && S.axis[node] >= 0) {
-            const double4_32a v = S.pm[x];
-            const int ax = S.axis[node];
-            const double p = ax == 0 ? v.x : (ax == 1 ? v.y : v.z);
-            const double cc = __dmul_rn(0.5, __dadd_rn(__dsub_rn(p, v.w), __dadd_rn(p, v.w)));
-            f[k] = cc < S.mid[node] ? 0u : 1u;
-          }
+          if (node != RT_CTA_FREE && S.axis[node] >= 0)
+            f[k] = S.key[6 + S.axis[node]][S.home[x]] < ord64(S.mid[node]) ? 0u : 1u;
           sum += f[k];
         }
         uint32_t incl = sum;
@@ -640,10 +659,10 @@ __global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
         for (int k = 0; k < RT_CTA_PER; ++k) {
           const int x = RT_CTA_PER * tid + k;
           S.flag[x] = static_cast<uint8_t>(f[k]);
-          S.bb[x] = static_cast<uint16_t>(acc);
+          S.u.r.bb[x] = static_cast<uint16_t>(acc);
           acc += f[k];
         }
-        if (tid == RT_CTA_T - 1) S.bb[RT_CTA_MAX] = static_cast<uint16_t>(acc);
+        if (tid == RT_CTA_T - 1) S.u.r.bb[RT_CTA_MAX] = static_cast<uint16_t>(acc);
       }
       __syncthreads();
       // Ranks P / Q; the children of every splitting node go to the next level (more than four
@@ -653,18 +672,18 @@ __global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
         if (node == RT_CTA_FREE || S.axis[node] < 0) continue;
         const int o0 = S.off[cur][node], cn = S.cnt[cur][node];
         const int r = x - o0;
-        const int bs = S.bb[o0];
-        const int Bb = S.bb[x] - bs, Bt = S.bb[o0 + cn] - bs, St = cn - Bt;
+        const int bs = S.u.r.bb[o0];
+        const int Bb = S.u.r.bb[x] - bs, Bt = S.u.r.bb[o0 + cn] - bs, St = cn - Bt;
         if (S.flag[x]) {
-          S.P[o0 + Bb] = static_cast<uint16_t>(r);
+          S.u.r.P[o0 + Bb] = static_cast<uint16_t>(r);
         } else {
-          S.Q[o0 + (St - (r - Bb)) - 1] = static_cast<uint16_t>(r);
+          S.u.r.Q[o0 + (St - (r - Bb)) - 1] = static_cast<uint16_t>(r);
         }
       }
       for (int i = tid; i < nl; i += RT_CTA_T) {
         if (S.axis[i] < 0) continue;
         const int o0 = S.off[cur][i], cn = S.cnt[cur][i];
-        const int St = cn - (S.bb[o0 + cn] - S.bb[o0]);
+        const int St = cn - (S.u.r.bb[o0 + cn] - S.u.r.bb[o0]);
         const int Sp = (St == 0 || St == cn) ? cn / 2 : St;  // bvh.rs:260-265
         S.sp[i] = static_cast<uint16_t>(Sp);
         const uint32_t cd = min(static_cast<uint32_t>(S.dep[cur][i]) + 1u, 255u);  // saturates past the depth check
@@ -689,7 +708,7 @@ __global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
       }
       __syncthreads();
       // Place: every element of a splitting node moves to its place after the swap partition.
-      double4_32a vp[RT_CTA_PER];
+      uint16_t vp[RT_CTA_PER];
       uint32_t vi[RT_CTA_PER];
       int dst[RT_CTA_PER];
       uint8_t vn[RT_CTA_PER];
@@ -700,7 +719,7 @@ __global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
         dst[k] = -1;
         vn[k] = RT_CTA_FREE;
         if (node == RT_CTA_FREE) continue;
-        vp[k] = S.pm[x];
+        vp[k] = S.home[x];
         vi[k] = S.idx[x];
         if (S.axis[node] < 0) {  // a leaf of this level: its order is final
           dst[k] = x;
@@ -708,15 +727,15 @@ __global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
         }
         const int o0 = S.off[cur][node], cn = S.cnt[cur][node];
         const int r = x - o0;
-        const int bs = S.bb[o0];
-        const int Bb = S.bb[x] - bs, Bt = S.bb[o0 + cn] - bs, St = cn - Bt;
+        const int bs = S.u.r.bb[o0];
+        const int Bb = S.u.r.bb[x] - bs, Bt = S.u.r.bb[o0 + cn] - bs, St = cn - Bt;
         const int li = St + (St < cn ? S.flag[o0 + St] : 0);
         const bool big = S.flag[x] != 0;
         int d;
         if (r < li) {
-          d = big ? ((Bb == 0 ? cn : S.Q[o0 + Bb - 1]) - 1) : r;
+          d = big ? ((Bb == 0 ? cn : S.u.r.Q[o0 + Bb - 1]) - 1) : r;
         } else {
-          d = big ? r - 1 : S.P[o0 + (St - (r - Bb)) - 1];
+          d = big ? r - 1 : S.u.r.P[o0 + (St - (r - Bb)) - 1];
         }
         dst[k] = o0 + d;
         vn[k] = S.cslot[node][d < S.sp[node] ? 0 : 1];
@@ -725,7 +744,7 @@ __global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
 #pragma unroll
       for (int k = 0; k < RT_CTA_PER; ++k) {
         if (dst[k] < 0) continue;
-        S.pm[dst[k]] = vp[k];
+        S.home[dst[k]] = vp[k];
         S.idx[dst[k]] = vi[k];
         S.nd[dst[k]] = vn[k];
       }
@@ -879,8 +898,8 @@ RtArgs rt_args(RTreeBufs& B, uint32_t* err) {
   A.N = B.N;
   A.idx[0] = B.idx0.p;
   A.idx[1] = B.idx1.p;
-  A.pm[0] = B.pm0.p;
-  A.pm[1] = B.pm1.p;
+  A.key[0] = B.key0.p;
+  A.key[1] = B.key1.p;
   A.nof[0] = B.nof0.p;
   A.nof[1] = B.nof1.p;
   A.flag = B.flag.p;
@@ -935,8 +954,8 @@ void rtree_alloc(RTreeBufs& B, std::vector<RTile>& tiles, bool want_leafof, cuda
   FG_CUDA(cudaMemcpyAsync(B.tiles.p, tiles.data(), tiles.size() * sizeof(RTile), cudaMemcpyHostToDevice, st));
   B.idx0.alloc(E1, st);
   B.idx1.alloc(E1, st);
-  B.pm0.alloc(E1, st);
-  B.pm1.alloc(E1, st);
+  B.key0.alloc(9 * E1, st);
+  B.key1.alloc(9 * E1, st);
   B.nof0.alloc(E1, st);
   B.nof1.alloc(E1, st);
   B.flag.alloc(E1 + 1, st);
@@ -986,8 +1005,8 @@ size_t carve(RTreeBufs* B, uint32_t ecap, bool want_leafof, uint32_t leafof_slot
   take(b.tiles, 1);
   take(b.idx0, E1);
   take(b.idx1, E1);
-  take(b.pm0, E1);
-  take(b.pm1, E1);
+  take(b.key0, 9 * E1);
+  take(b.key1, 9 * E1);
   take(b.nof0, E1);
   take(b.nof1, E1);
   take(b.flag, E1 + 1);
@@ -1067,6 +1086,7 @@ void rtree_build(RTreeBufs& B, uint32_t* err, cudaStream_t st, RTile* tiles_dev)
   k_rt_check<<<1, 1, 0, st>>>(A, B.levels & 1);
   const unsigned GC = static_cast<unsigned>(
       std::min<unsigned long long>(B.E / (RT_LEAF_MAX + 1) + static_cast<unsigned long long>(B.ntiles), 152ull * 8));
+  static_assert(sizeof(RtCtaSmem) <= 112 * 1024, "two blocks of the block phase must fit an SM");
   FG_CUDA(cudaFuncSetAttribute(k_rt_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                static_cast<int>(sizeof(RtCtaSmem))));
   k_rt_cta<<<GC, RT_CTA_T, sizeof(RtCtaSmem), st>>>(A);
