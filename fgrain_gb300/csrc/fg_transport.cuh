@@ -237,7 +237,20 @@ __device__ __forceinline__ bool photon_bounce(const TileDesc& t, Photon& ph, uin
     for (uint32_t k = 0; k < L.y; ++k) {
       const uint32_t s = __ldg(&t.ridx[L.x + k]);
       if (!index_ok(s < t.n, err, SITE_LEAF, s, t.n)) continue;
-      const float4 a = __ldg(&t.a[s]), q = __ldg(&t.q[s]), d = __ldg(&t.d[s]);
+      const float4 a = __ldg(&t.a[s]), d = __ldg(&t.d[s]);
+      // The crystal lies in the ball of radius sqrt(3) m (a cube) or m (the ellipsoid shapes)
+      // around its centre; a ball the step's segment misses, with a margin well above FP32
+      // rounding, cannot give a hit inside the step, so the geometry test is skipped (the hits
+      // and their order are those of testing every crystal).
+      {
+        const float m = fmaxf(fmaxf(d.x, d.y), d.z);
+        const float R = (morph_of(d) == 0 ? 1.7320509f * m : m) * 1.001f + 1e-3f;
+        const float wx = a.x - pos.x, wy = a.y - pos.y, wz = a.z - pos.z;
+        const float tc = fminf(fmaxf(wx * dir.x + wy * dir.y + wz * dir.z, 0.0f), step);
+        const float ex = wx - tc * dir.x, ey = wy - tc * dir.y, ez = wz - tc * dir.z;
+        if (ex * ex + ey * ey + ez * ez > R * R) continue;
+      }
+      const float4 q = __ldg(&t.q[s]);
       float t0, t1;
       if (!fintersect(a, q, d, 1.0f, pos, dir, t0, t1)) continue;
       if (!(t0 < step)) continue;
