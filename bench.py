@@ -600,7 +600,11 @@ def run_reference(args):
     grid, _, _ = orc.film_grid(R, R, C4_GRAIN, C4_TILE)
     nt = len(grid)
     sample = c4_sample(nt)
-    warm_n, timed_n = max(args.warmup, 0), 4 * args.steps
+    threads = os.cpu_count() or 1
+    # 4 tiles per step, rounded up to whole waves of the thread pool: the reference's rayon tile map
+    # over a photograph's thousands of tiles keeps every core busy.
+    warm_n = max(args.warmup, 0)
+    timed_n = -(-4 * args.steps // threads) * threads
     picks = [sample[k % len(sample)] for k in range(warm_n + timed_n)]
     heffs = {}
     for c in sorted({c for c, _ in picks}):  # the oracle's own exposure stages (upscale, PSF)
@@ -614,26 +618,57 @@ def run_reference(args):
                      np.ascontiguousarray(heffs[c][t.y_start:t.y_start + t.th, t.x_start:t.x_start + t.tw]),
                      orc.film_tile_seed((SEED + COLOR_SEED_OFFSETS[c]) & M64, t)))
     heffs.clear()
-    threads = os.cpu_count() or 1
     if warm_n:
         oracle_tiles(jobs[:warm_n], threads)
     secs, _ = oracle_tiles(jobs[warm_n:], threads)
     all_px = 3 * sum(t.tw * t.th for t in grid)
     px = sum(j[2].size for j in jobs[warm_n:])
     value = out_pxc * px / all_px / secs / 1e6
-    sample_txt = (f"each step renders 4 C4 tiles (the first {timed_n} tiles of the benchmark's every-{C4_STRIDE}th-tile "
-                  f"sample, rendered together by a {threads}-thread tile map as the reference's rayon map renders "
-                  f"tiles); C++ restatement of the reference CPU path with the reference's hit rule (the Rust "
+    sample_txt = (f"{timed_n} C4 tiles for {args.steps} steps (the first of the benchmark's every-{C4_STRIDE}th-tile "
+                  f"sample, 4 per step rounded up to whole waves of the {threads}-thread tile map, rendered together as "
+                  f"the reference's rayon map renders tiles); C++ restatement of the reference CPU path with the reference's hit rule (the Rust "
                   f"reference cannot be built here); output pixel-channels scaled by tile pixels; each warm-up step "
                   f"renders one tile")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mpx/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": C4_WORKLOAD + ", reference CPU path (no GPU used)", "tiles_per_step": 4},
+        "config": {"workload": C4_WORKLOAD + ", reference CPU path (no GPU used)", "tiles_per_step": timed_n / args.steps},
         "cpu_baseline": {"value": value, "unit": "Mpx/s", "cores": threads, "kind": "port", "sample": sample_txt},
         "e2e": {"value": value, "unit": "Mpx/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
+
+
+def run_profile(args):
+    """One batched run of the workload's batch between cudaProfilerStart and cudaProfilerStop, for
+    `ncu --profile-from-start off`: c2, its 49 tiles; c4, the first --profile-region tiles of the C4
+    step's batch.  Warm-up runs (autotune, graph capture) come first and are not profiled."""
+    import torch.cuda.profiler as prof
+    import fgrain_gb300 as fg
+
+    engine = fg.GpuEngine(0)
+    if args.workload == "c2":
+        exposure = c2_inputs()
+        _, params, tiles = c2_tiles(exposure)
+    else:
+        from fgrain_gb300 import film
+        from fgrain_gb300 import image as im
+
+        params, tiles, _, _ = c4_batch_inputs(fg, film, im, c4_image(args.film_side), engine)
+        params, tiles = params[:args.profile_region], tiles[:args.profile_region]
+    batch = fg.Batch(params, engine, use_graph=True, autotune=True)
+    batch.set_exposure(tiles)
+    for _ in range(max(args.warmup, 1)):
+        batch.run()
+        batch.wait()
+    prof.start()
+    batch.run()
+    st = batch.wait()
+    prof.stop()
+    batch.close()
+    print(json.dumps({"profile_region": args.workload, "tiles": len(params),
+                      **{k: st[k] for k in ("synth_ms", "bvh_ms", "transport_ms", "develop_ms", "scan_ms", "total_ms",
+                                            "kernel_launches", "crystals", "photons", "hits")}}))
 
 
 def main():
@@ -650,8 +685,13 @@ def main():
     ap.add_argument("--film-side", type=int, default=C4_SIDE, help="side of the C4 photograph (4096 for C4)")
     ap.add_argument("--batch-gb", type=float, default=0.0,
                     help="device GiB one batch of the whole-photograph render may use (0: 70 %% of the free memory)")
+    ap.add_argument("--profile-region", type=int, default=0, metavar="TILES",
+                    help="run one batch between cudaProfilerStart/Stop and exit (ncu --profile-from-start off): "
+                         "c2, its 49 tiles; c4, the first TILES tiles of the C4 step's batch")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile_region:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.workload == "c4":
         run_c4(args)

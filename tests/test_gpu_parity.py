@@ -121,10 +121,10 @@ def test_device_reference_tree_equals_the_oracle(engine, preset, size, seed):
     assert len(cr) > 1000
 
 
-@pytest.mark.parametrize("n", [1, 2, 4, 5, 31, 32, 33, 64, 200])
+@pytest.mark.parametrize("n", [1, 2, 4, 5, 6, 33, 200, 1024, 1025, 2100])
 def test_device_reference_tree_small_and_degenerate_sets(engine, n):
-    """Sets at the leaf size, at the per-warp finish's edge, and with coincident centroids (the
-    reference's degenerate-extent leaf, bvh.rs:230-239)."""
+    """Sets at the leaf size, at the edge of the per-block finish (1024 crystals), and with
+    coincident centroids (the reference's degenerate-extent leaf, bvh.rs:230-239)."""
     cfg = reference_cfg("tri-x", 20.0, 20.0)
     rng = np.random.default_rng(n)
     pos = rng.random((n, 3)) * [20.0, 20.0, 14.0]
