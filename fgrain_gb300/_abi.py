@@ -238,7 +238,37 @@ PROTOTYPES = {
                                       C.POINTER(fg_scan_cfg), C.c_uint64, _vp, _vp, _vp, C.c_char_p,
                                       C.c_size_t]),
     "fg_png_unfilter": (_st, [_vp, C.c_uint32, C.c_uint32, C.c_uint32]),
+    "fg_jpeg_info": (_st, [_vp, C.c_size_t, _u32p, _u32p, _u32p, C.c_char_p, C.c_size_t]),
+    "fg_jpeg_decode": (_st, [_vp, C.c_size_t, _vp, C.c_size_t, C.c_char_p, C.c_size_t]),
+    "fg_jpeg_encode": (_st, [_vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _vp, C.c_size_t,
+                             C.POINTER(C.c_size_t)]),
+    "fg_webp_info": (_st, [_vp, C.c_size_t, _u32p, _u32p, _u32p, C.c_char_p, C.c_size_t]),
+    "fg_webp_decode": (_st, [_vp, C.c_size_t, _vp, C.c_size_t, C.c_char_p, C.c_size_t]),
+    "fg_webp_encode": (_st, [_vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _vp, C.c_size_t,
+                             C.POINTER(C.c_size_t)]),
 }
+
+# Options of the JPEG encoder (the FG_JPEG_* bits; a restart interval of n MCUs is n << 16).
+FG_JPEG_SUBSAMPLE_420 = 0x0
+FG_JPEG_SUBSAMPLE_422 = 0x1
+FG_JPEG_SUBSAMPLE_444 = 0x2
+FG_JPEG_SEPARATE_SCANS = 0x4
+
+
+def FG_JPEG_RESTART(n: int) -> int:
+    return n << 16
+
+
+# Tools of the lossless WebP encoder (the FG_WEBP_* bits).
+FG_WEBP_SUBTRACT_GREEN = 0x01
+FG_WEBP_PREDICTOR = 0x02
+FG_WEBP_COLOR_TRANSFORM = 0x04
+FG_WEBP_PALETTE = 0x08
+FG_WEBP_COLOR_CACHE = 0x10
+FG_WEBP_BACKREFS = 0x20
+FG_WEBP_META_CODES = 0x40
+FG_WEBP_ALL_MODES = 0x80
+FG_WEBP_DEFAULT = FG_WEBP_SUBTRACT_GREEN | FG_WEBP_PREDICTOR | FG_WEBP_COLOR_CACHE | FG_WEBP_BACKREFS
 
 _lib = None
 

@@ -1,6 +1,7 @@
 """Image files of the command-line tool: what ``image::open`` and ``ImageBuffer::save`` do for
-the reference (the image crate 0.25 with its ``png`` feature; src/image_pipeline.rs:1087-1152),
-restated for PNG, plus the binary netpbm formats (PGM, PPM) as a convenience.
+the reference (the image crate 0.25 with its ``png``, ``jpeg`` and ``webp`` features, Cargo.toml:13;
+src/image_pipeline.rs:1087-1152), restated for PNG, JPEG and WebP, plus the binary netpbm formats
+(PGM, PPM) as a convenience.
 
 ``read_image`` returns what the renderer consumes from a ``DynamicImage``
 (src/image_pipeline.rs:259-296, 1017-1024): an 8-bit gray image without transparency stays gray
@@ -9,8 +10,16 @@ u8: alpha dropped, palette looked up, 16-bit samples rounded to 8 bits, gray rep
 Low bit-depth gray is widened to 8 bits by bit replication, as the png crate's ``EXPAND`` does.
 
 PNG chunks, zlib, Adam7 passes and sample unpacking are done here; the row filters are undone by
-the library's ``fg_png_unfilter`` (host C++ in fgrain_gb300/host/, native for speed on large scans).  JPEG and WebP
-have no codec in this build: reading or writing them raises ``ImageFormatError``.
+the library's ``fg_png_unfilter`` (host C++ in fgrain_gb300/host/, native for speed on large scans).
+JPEG and WebP are coded by the library's host C++ codecs (``fg_jpeg_*``, ``fg_webp_*``):
+
+- JPEG: sequential Huffman-coded files are read (gray stays gray, as the crate's ``ImageLuma8``;
+  colour gives RGB); progressive, arithmetic-coded, 12-bit and CMYK files raise
+  ``ImageFormatError``.  Writing is baseline JFIF at quality 75, the crate's ``JpegEncoder``
+  default (gray as one component, colour as YCbCr with 2x2 chroma subsampling).
+- WebP: lossless files are read (the crate's decoder gives ``Rgb8``/``Rgba8``, which the renderer
+  takes through ``to_rgb8``: RGB, alpha dropped); lossy (VP8) and animated files raise
+  ``ImageFormatError``.  Writing is lossless, as the crate's WebP encoder writes.
 """
 from __future__ import annotations
 
@@ -41,10 +50,42 @@ def read_image(path) -> np.ndarray:
         return decode_png(data)
     if data[:2] in (b"P5", b"P6"):
         return decode_pnm(data)
-    kind = _kind_of(path)
-    if kind in ("jpeg", "webp"):
-        raise ImageFormatError(f"decoding {kind.upper()} is not available in this build (PNG, PGM and PPM are)")
-    raise ImageFormatError(f"'{path}' is not a PNG, PGM or PPM file")
+    if data[:3] == b"\xff\xd8\xff":
+        return decode_jpeg(data)
+    if data[:4] == b"RIFF" and data[8:12] == b"WEBP":
+        return decode_webp(data)
+    raise ImageFormatError(f"'{path}' is not a PNG, JPEG, WebP, PGM or PPM file")
+
+
+def _codec_call(fn, *args) -> None:
+    msg = C.create_string_buffer(256)
+    if fn(*args, msg, len(msg)) != 0:
+        raise ImageFormatError(msg.value.decode(errors="replace") or "corrupt image file")
+
+
+def decode_jpeg(data: bytes) -> np.ndarray:
+    """(H, W) u8 for a gray JPEG, (H, W, 3) u8 RGB otherwise."""
+    lib = _abi.load()
+    w, h, ch = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    _codec_call(lib.fg_jpeg_info, data, len(data), C.byref(w), C.byref(h), C.byref(ch))
+    out = np.empty(h.value * w.value * ch.value, np.uint8)
+    _codec_call(lib.fg_jpeg_decode, data, len(data), out.ctypes.data, out.nbytes)
+    return out.reshape(h.value, w.value) if ch.value == 1 else out.reshape(h.value, w.value, 3)
+
+
+def decode_webp_rgba(data: bytes) -> np.ndarray:
+    """(H, W, 4) u8 RGBA pixels of a lossless WebP file."""
+    lib = _abi.load()
+    w, h, alpha = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    _codec_call(lib.fg_webp_info, data, len(data), C.byref(w), C.byref(h), C.byref(alpha))
+    out = np.empty((h.value, w.value, 4), np.uint8)
+    _codec_call(lib.fg_webp_decode, data, len(data), out.ctypes.data, out.nbytes)
+    return out
+
+
+def decode_webp(data: bytes) -> np.ndarray:
+    """(H, W, 3) u8: the RGB of a lossless WebP file (``to_rgb8``)."""
+    return np.ascontiguousarray(decode_webp_rgba(data)[:, :, :3])
 
 
 def _chunks(data: bytes):
@@ -209,6 +250,39 @@ def encode_png(img: np.ndarray, level: int = 6) -> bytes:
             chunk(b"IDAT", zlib.compress(rows.tobytes(), level)) + chunk(b"IEND", b""))
 
 
+def _encode(fn, a: np.ndarray, *settings: int) -> bytes:
+    h, w = a.shape[:2]
+    ch = 1 if a.ndim == 2 else a.shape[2]
+    cap = C.c_size_t(0)
+    size = max(1 << 16, a.nbytes + a.nbytes // 2 + 4096)
+    for _ in range(2):  # the second pass with the size the first reported
+        out = np.empty(size, np.uint8)
+        if fn(a.ctypes.data, w, h, ch, *settings, out.ctypes.data, out.nbytes, C.byref(cap)) == 0:
+            return out[:cap.value].tobytes()
+        if cap.value <= size:
+            break
+        size = cap.value
+    raise ImageFormatError("image could not be encoded")
+
+
+def encode_jpeg(img: np.ndarray, quality: int = 75, options: int = 0) -> bytes:
+    """Baseline JFIF of a u8 gray ((H, W)) or RGB ((H, W, 3)) image; quality 1..100; options are
+    the encoder's FG_JPEG_* settings (0: 4:2:0, one interleaved scan, no restart markers)."""
+    a = np.ascontiguousarray(img, np.uint8)
+    if not 1 <= quality <= 100:
+        raise ValueError("JPEG quality must be within 1..100")
+    return _encode(_abi.load().fg_jpeg_encode, a, quality, options)
+
+
+def encode_webp(img: np.ndarray, options: int = _abi.FG_WEBP_DEFAULT) -> bytes:
+    """Lossless WebP of a u8 gray ((H, W)), RGB ((H, W, 3)) or RGBA ((H, W, 4)) image; options are
+    the encoder's FG_WEBP_* tools."""
+    a = np.ascontiguousarray(img, np.uint8)
+    if a.shape[0] > 16384 or a.shape[1] > 16384:
+        raise ImageFormatError("a WebP image is at most 16384 pixels on a side")
+    return _encode(_abi.load().fg_webp_encode, a, options)
+
+
 def write_image(path, img: np.ndarray) -> None:
     """Saves a u8 gray ((H, W)) or RGB ((H, W, 3)) image in the format its extension names."""
     a = np.ascontiguousarray(img, np.uint8)
@@ -222,8 +296,10 @@ def write_image(path, img: np.ndarray) -> None:
             raise ImageFormatError("a PGM file holds gray images only")
         magic = b"P5" if a.ndim == 2 else b"P6"
         data = magic + f"\n{a.shape[1]} {a.shape[0]}\n255\n".encode() + a.tobytes()
-    elif kind in ("jpeg", "webp"):
-        raise ImageFormatError(f"encoding {kind.upper()} is not available in this build (PNG, PGM and PPM are)")
+    elif kind == "jpeg":
+        data = encode_jpeg(a)
+    elif kind == "webp":
+        data = encode_webp(a)
     else:
         raise ImageFormatError(f"unsupported output format '.{kind}'")
     Path(path).write_bytes(data)

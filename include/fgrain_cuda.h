@@ -508,6 +508,56 @@ fg_status fg_scan_crystals_static(const fg_device_crystals* crystals, const fg_e
  * FG_ERR_INVALID_ARG (rows before it are already reconstructed). */
 fg_status fg_png_unfilter(uint8_t* rows, uint32_t h, uint32_t stride, uint32_t bpp);
 
+/* JPEG files as image::open and ImageBuffer::save handle them (src/image_pipeline.rs:1141, 1091,
+ * 1114; the image crate's `jpeg` feature, Cargo.toml:13).  Reading: sequential Huffman-coded DCT
+ * (SOF0, SOF1), 8-bit samples, one component (gray) or three (YCbCr; RGB when an Adobe marker
+ * says so), any sampling factors and restart intervals; progressive, arithmetic-coded, lossless,
+ * 12-bit and CMYK files give FG_ERR_INVALID_ARG with the reason in msg.  fg_jpeg_info reads the
+ * header only: width, height and channels (1 or 3, what fg_jpeg_decode writes per pixel).
+ * fg_jpeg_decode writes h rows of w * channels bytes (gray, or R, G, B) into out, cap bytes.
+ * fg_jpeg_encode writes baseline JFIF at quality 1..100 (the example tables of ITU T.81 Annex K
+ * scaled as the IJG library does; the image crate's default is 75): channels 1 (gray) or 3 (RGB,
+ * stored as YCbCr).  options: the chroma subsampling (FG_JPEG_SUBSAMPLE_*, 4:2:0 when 0, what
+ * writing an image file uses), FG_JPEG_SEPARATE_SCANS for one scan per component instead of one
+ * interleaved scan, and FG_JPEG_RESTART(n) for a restart marker every n MCUs (n < 65536).  *len
+ * receives the file's size; when it exceeds cap nothing useful is written and FG_ERR_INVALID_ARG
+ * is returned (call again with *len bytes).  No GPU counterpart: host code of the command-line
+ * tool. */
+#define FG_JPEG_SUBSAMPLE_420 0x0u
+#define FG_JPEG_SUBSAMPLE_422 0x1u
+#define FG_JPEG_SUBSAMPLE_444 0x2u
+#define FG_JPEG_SEPARATE_SCANS 0x4u
+#define FG_JPEG_RESTART(n) ((uint32_t)(n) << 16)
+fg_status fg_jpeg_info(const uint8_t* data, size_t n, uint32_t* w, uint32_t* h, uint32_t* channels, char* msg,
+                       size_t msg_cap);
+fg_status fg_jpeg_decode(const uint8_t* data, size_t n, uint8_t* out, size_t cap, char* msg, size_t msg_cap);
+fg_status fg_jpeg_encode(const uint8_t* px, uint32_t w, uint32_t h, uint32_t channels, uint32_t quality,
+                         uint32_t options, uint8_t* out, size_t cap, size_t* len);
+
+/* WebP files (the image crate's `webp` feature, Cargo.toml:13; its encoder writes lossless
+ * WebP): the lossless format (VP8L) in a RIFF container.  Reading covers the whole lossless
+ * format (predictor, colour and subtract-green transforms, colour indexing with pixel bundling,
+ * colour cache, meta prefix codes, backward references); lossy (VP8) and animated files give
+ * FG_ERR_INVALID_ARG with the reason in msg.  fg_webp_info: width, height and the header's alpha
+ * hint.  fg_webp_decode writes h rows of w RGBA pixels (4 bytes each) into rgba, cap bytes.
+ * fg_webp_encode takes channels 1 (gray, stored as R = G = B), 3 (RGB) or 4 (RGBA) and the tools
+ * of the format to use (FG_WEBP_* bits; FG_WEBP_DEFAULT is what writing an image file uses; the
+ * others exist to exercise every decoding path).  *len as for fg_jpeg_encode. */
+#define FG_WEBP_SUBTRACT_GREEN 0x01u
+#define FG_WEBP_PREDICTOR 0x02u
+#define FG_WEBP_COLOR_TRANSFORM 0x04u
+#define FG_WEBP_PALETTE 0x08u /* colour indexing when the image has at most 256 colours */
+#define FG_WEBP_COLOR_CACHE 0x10u
+#define FG_WEBP_BACKREFS 0x20u
+#define FG_WEBP_META_CODES 0x40u
+#define FG_WEBP_ALL_MODES 0x80u /* predictor modes assigned in turn rather than chosen */
+#define FG_WEBP_DEFAULT (FG_WEBP_SUBTRACT_GREEN | FG_WEBP_PREDICTOR | FG_WEBP_COLOR_CACHE | FG_WEBP_BACKREFS)
+fg_status fg_webp_info(const uint8_t* data, size_t n, uint32_t* w, uint32_t* h, uint32_t* has_alpha, char* msg,
+                       size_t msg_cap);
+fg_status fg_webp_decode(const uint8_t* data, size_t n, uint8_t* rgba, size_t cap, char* msg, size_t msg_cap);
+fg_status fg_webp_encode(const uint8_t* px, uint32_t w, uint32_t h, uint32_t channels, uint32_t options,
+                         uint8_t* out, size_t cap, size_t* len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -235,11 +235,15 @@ def test_writers_round_trip(tmp_path):
     for name, img in (("a.png", g), ("b.png", rgb), ("c.pgm", g), ("d.ppm", rgb)):
         imageio.write_image(tmp_path / name, img)
         np.testing.assert_array_equal(imageio.read_image(tmp_path / name), img)
-    for name in ("e.jpg", "f.webp"):
-        with pytest.raises(imageio.ImageFormatError):
-            imageio.write_image(tmp_path / name, g)
+    imageio.write_image(tmp_path / "f.webp", rgb)  # lossless
+    np.testing.assert_array_equal(imageio.read_image(tmp_path / "f.webp"), rgb)
+    imageio.write_image(tmp_path / "e.jpg", g)  # lossy: same shape, gray stays gray
+    assert imageio.read_image(tmp_path / "e.jpg").shape == g.shape
     (tmp_path / "g.jpg").write_bytes(b"\xff\xd8\xff\xe0")
-    with pytest.raises(imageio.ImageFormatError, match="JPEG"):
+    with pytest.raises(imageio.ImageFormatError):
         imageio.read_image(tmp_path / "g.jpg")
+    (tmp_path / "i.gif").write_bytes(b"GIF89a")
+    with pytest.raises(imageio.ImageFormatError, match="not a PNG, JPEG, WebP"):
+        imageio.read_image(tmp_path / "i.gif")
     (tmp_path / "h.pgm").write_bytes(b"P5\n# comment\n2 2\n65535\n" + np.array([0, 65535, 257, 32896], ">u2").tobytes())
     np.testing.assert_array_equal(imageio.read_image(tmp_path / "h.pgm"), [[0, 255], [1, 128]])

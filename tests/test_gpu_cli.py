@@ -59,3 +59,38 @@ def test_demos(tmp_path, engine, name):
         assert c > img[:32, :32].mean()
     else:
         assert 0 < img.std()
+
+
+@pytest.mark.parametrize("color", [False, True])
+def test_webp_file_to_webp_file(tmp_path, engine, color):
+    """src/image_pipeline.rs:1159-1229 (test_webp_read_write_pipeline, test_webp_color_pipeline):
+    a WebP photograph (64 x 64 gray ramp, or 48 x 48 colour ramps) rendered with grain size 2 px
+    and one tile to a WebP file, which loads back with the input's size.  WebP is lossless, so
+    the file holds exactly the renderer's pixels (a gray render replicated into RGB)."""
+    n = 48 if color else 64
+    y, x = np.mgrid[0:n, 0:n]
+    img = (np.stack([x * 5, y * 5, np.full_like(x, 128)], -1) if color else (x + y) * 2).astype(np.uint8)
+    src, dst = tmp_path / "in.webp", tmp_path / "out.webp"
+    imageio.write_image(src, img)
+    args = ["--tile-size", str(n), "-s", "2.0"] + (["-c"] if color else [])
+    run(str(src), str(dst), *args)
+    got = imageio.read_image(dst)
+    assert got.shape == (n, n, 3)
+    opts = cli.apply_options(cli.parse_apply_args(["x", *args]), lambda *_: None)
+    rep, want = film.render_film(imageio.read_image(src), opts, engine)
+    assert rep.input_resolution == (n, n) and rep.output_resolution == (n, n)
+    np.testing.assert_array_equal(got, want if color else np.repeat(want[:, :, None], 3, axis=2))
+
+
+def test_jpeg_file_to_jpeg_file(tmp_path, engine):
+    """A gray JPEG photograph rendered to a JPEG file: the output is the renderer's image of the
+    decoded input, written at quality 75 (the image crate's default)."""
+    y, x = np.mgrid[0:72, 0:88]
+    img = (40 + x + y).astype(np.uint8)
+    src, dst = tmp_path / "in.jpg", tmp_path / "out.jpg"
+    imageio.write_image(src, img)
+    run(str(src), str(dst), "--tile-size", "64", "-p", "t-max")
+    opts = cli.apply_options(cli.parse_apply_args(["x", "--tile-size", "64", "-p", "t-max"]), lambda *_: None)
+    _, want = film.render_film(imageio.read_image(src), opts, engine)
+    assert dst.read_bytes() == imageio.encode_jpeg(want, 75)
+    assert imageio.read_image(dst).shape == (72, 88)
