@@ -877,10 +877,10 @@ unsigned long long tile_footprint(const fg_tile_params& p, unsigned long long* s
   while ((1u << bits) < static_cast<uint32_t>(std::ceil(side))) ++bits;
   const unsigned long long px = static_cast<unsigned long long>(p.width_px) * p.height_px;
   // Per crystal slot: records 48, key 8, links and flags 36, expansion 8, scan prep 160, bin
-  // entries 32, tree elements 184 (order, node of, two copies of nine 8-byte keys, flags, prefix
-  // sums, ranks, final order, leaf of) and 0.8 nodes of 268 B (plus slack); cells 4 B; bricks
+  // entries 32, tree elements 88 (order, node of, two copies of three 8-byte keys, flags, prefix
+  // sums, ranks, final order, leaf of) and 0.8 nodes of 224 B (plus slack); cells 4 B; bricks
   // 8 B; photon order; images.
-  return static_cast<unsigned long long>(s.ccap) * 700ull + static_cast<unsigned long long>(s.gw) * s.gh * s.gd * 4ull +
+  return static_cast<unsigned long long>(s.ccap) * 580ull + static_cast<unsigned long long>(s.gw) * s.gh * s.gd * 4ull +
          (8ull << (2 * s.slot_bits)) + static_cast<unsigned long long>(t.P) * 4ull +
          (1ull << (2 * bits)) * 12ull + px * 8ull + 4096ull;
 }

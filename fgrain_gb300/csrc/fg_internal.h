@@ -128,15 +128,17 @@ struct RTreeBufs {
   uint32_t count = 0;             // elements of a one-tile tree built on the host's request
   DBuf<RTile> tiles;
   DBuf<uint32_t> idx0, idx1, nof0, nof1, flag, bb, blk, P, Q;
-  DBuf<unsigned long long> key0, key1;  // nine ordered keys per element (SoA), travelling with the order
+  DBuf<unsigned long long> key0, key1;  // three ordered centroid keys per element (SoA), travelling with the order
   DBuf<uint32_t> ridx;            // final element order (slots): a leaf's crystals in reference order
-  DBuf<unsigned long long> acc;   // per node: 6 ordered minima, 6 ordered maxima
+  DBuf<unsigned long long> acc;   // per node: ordered centroid minima, maxima (3 each)
   DBuf<double> box64;             // per node: lo xyz, hi xyz (FP64, exact)
+  DBuf<uint32_t> parent;          // per node: parent id (0xffffffff for a root)
   DBuf<uint32_t> nstart, ncount, ntile, ndepth;
   DBuf<int> nsplit;               // split axis, -1 for a leaf
   DBuf<double> nmid;
   DBuf<int2> nchild;              // global ids of the children
-  DBuf<uint32_t> wl0, wl1, bq, bqpar, cnt;  // global worklists, block queue (node, buffer parity), counts
+  DBuf<uint32_t> wl0, wl1, bq, bqpar, cnt;  // global worklists (wl0 then the refit's arrival counts),
+                                            // block queue (node, buffer parity), counts
   unsigned long long R = 0;       // walk records (all tiles)
   DBuf<Node4> rnode;              // four-wide walk records (tile-local refs)
   DBuf<uint2> rleaf;              // leaf: first element (tile-local position), count

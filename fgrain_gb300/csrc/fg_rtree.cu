@@ -1,18 +1,21 @@
 // Device builder of the reference tree (BVH::build / subdivide, bvh.rs:157-295); see fg_rtree.cuh.
 //
-// The tree is built top-down, one level at a time over all tiles of a batch:
-//   reduce  each pending node's box and centroid box (min / max on order-preserving 64-bit keys
-//           of the FP64 values: exact whatever the order, and on the integer pipes);
+// The tree's topology is built top-down, one level at a time over all tiles of a batch:
+//   reduce  each pending node's centroid box (min / max on order-preserving 64-bit keys of the
+//           FP64 values: exact whatever the order, and on the integer pipes);
 //   decide  leaf or split (largest centroid extent, midpoint 0.5 (lo + hi)), children ids;
 //   flag    every element of a splitting node: centroid >= mid ("big"), with the prefix sum of the
 //           flags (ranks of bigs inside each node's contiguous range) in the same passes;
 //   pq      P_m = position of the m-th big from the left, Q_m = of the m-th small from the right;
 //   place   every element moves to where the reference's swap partition puts it (below).
-// Each element's nine order-preserving 64-bit keys (box lo, hi and centroid of its FP64 max_dim
-// box, computed once) travel with it, so every pass reads them in order and none does FP64 work.
-// Nodes of at most RT_CTA_MAX elements leave the global levels: one thread block each builds
-// their subtree with the elements in shared memory, the same passes per level, all levels down to
-// the leaves.  Node boxes are reduced segment-wise (a node is a contiguous range of positions).
+// The splits read only the centroids (bvh.rs:196-258), so each element's three order-preserving
+// 64-bit centroid keys (of its FP64 max_dim box, computed once) travel with it, and every pass
+// reads them in order and does no FP64 work.  Nodes of at most RT_CTA_MAX elements leave the
+// global levels: one thread block each builds their subtree with the elements in shared memory,
+// the same passes per level, all levels down to the leaves.  Centroid boxes are reduced
+// segment-wise (a node is a contiguous range of positions).  The node boxes (the union of the
+// elements' boxes, which the reference stores but never splits on) are formed bottom up once the
+// topology is final (k_rt_refit); min and max are exact, so the order does not matter.
 //
 // The swap partition (bvh.rs:244-258: i from the left, j from the right; a small at i stays and i
 // advances, a big at i is swapped with j and j retreats) examines the range as two streams: the
@@ -74,8 +77,7 @@ struct RtArgs {
   int ntiles;
   unsigned long long E, N;
   uint32_t* idx[2];
-  // Keys of the element at position x, field f at key[c][f * E + x]: ord64 of the box lo xyz (f
-  // 0-2), hi xyz (3-5) and centroid xyz (6-8).
+  // Keys of the element at position x, field f at key[c][f * E + x]: ord64 of the centroid xyz.
   unsigned long long* key[2];
   uint32_t* nof[2];
   uint32_t* flag;
@@ -86,6 +88,7 @@ struct RtArgs {
   uint32_t* ridx;
   unsigned long long* acc;
   double* box64;
+  uint32_t* parent;  // parent id of each node (RT_NONE for a root)
   uint32_t *nstart, *ncount, *ntile, *ndepth;
   int* nsplit;
   double* nmid;
@@ -107,16 +110,18 @@ __device__ __forceinline__ bool alloc_pair(const RtArgs& A, int t, uint32_t& l) 
   return true;
 }
 
+constexpr uint32_t RT_NONE = 0xffffffffu;
+
 // Hands a new node of n elements (held in buffer `par`) to the phase that builds it: the global
-// levels (more than RT_CTA_MAX elements; its box accumulators start empty) or one block.
+// levels (more than RT_CTA_MAX elements; its centroid accumulators start empty) or one block.
 __device__ __forceinline__ void rt_enqueue(const RtArgs& A, uint32_t id, uint32_t n, int par) {
   A.nsplit[id] = -1;
   if (n > static_cast<uint32_t>(RT_CTA_MAX)) {
-    unsigned long long* a = A.acc + 12ull * id;
+    unsigned long long* a = A.acc + 6ull * id;
 #pragma unroll
-    for (int k = 0; k < 6; ++k) a[k] = ~0ull;  // minima
+    for (int k = 0; k < 3; ++k) a[k] = ~0ull;  // minima
 #pragma unroll
-    for (int k = 6; k < 12; ++k) a[k] = 0ull;  // maxima
+    for (int k = 3; k < 6; ++k) a[k] = 0ull;  // maxima
     A.wl[par][atomicAdd(&A.cnt[par], 1u)] = id;
   } else if (n > 0) {
     const uint32_t q = atomicAdd(&A.cnt[2], 1u);
@@ -125,33 +130,26 @@ __device__ __forceinline__ void rt_enqueue(const RtArgs& A, uint32_t id, uint32_
   }
 }
 
-// The 12 reduction keys of the element at position x of a key array (field f at key[f * stride +
-// x]): box lo xyz and centroid xyz (minima), box hi xyz and centroid xyz (maxima).  Min and max
-// are exact in any order, and on the ordered 64-bit keys they run on the integer pipes (GB300's
-// FP64 pipe is narrow).
+// The 6 reduction keys of the element at position x of a key array (field f at key[f * stride +
+// x]): centroid xyz as minima, then as maxima.  Min and max are exact in any order, and on the
+// ordered 64-bit keys they run on the integer pipes (GB300's FP64 pipe is narrow).
 __device__ __forceinline__ void rt_keys(const unsigned long long* key, unsigned long long stride, unsigned long long x,
-                                        unsigned long long k[12]) {
+                                        unsigned long long k[6]) {
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     k[i] = key[i * stride + x];
-    k[6 + i] = key[(3 + i) * stride + x];
-    k[3 + i] = key[(6 + i) * stride + x];
-    k[9 + i] = k[3 + i];
+    k[3 + i] = k[i];
   }
 }
 
-// The nine keys of element slot s of tile T, written to position x of key[f * stride + x]
-// (centroids normalised so that -0 orders as +0, as the FP64 comparisons see them).
-__device__ __forceinline__ void rt_key9(const RTile& T, uint32_t s, unsigned long long* key, unsigned long long stride,
+// The three centroid keys of element slot s of tile T, written to position x of key[f * stride +
+// x] (normalised so that -0 orders as +0, as the FP64 comparisons see them).
+__device__ __forceinline__ void rt_key3(const RTile& T, uint32_t s, unsigned long long* key, unsigned long long stride,
                                         unsigned long long x) {
   double lo[3], hi[3], cc[3];
   rt_box_pm(rt_pm(T, s), lo, hi, cc);
 #pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    key[i * stride + x] = ord64(lo[i]);
-    key[(3 + i) * stride + x] = ord64(hi[i]);
-    key[(6 + i) * stride + x] = ord64(__dadd_rn(cc[i], 0.0));
-  }
+  for (int i = 0; i < 3; ++i) key[i * stride + x] = ord64(__dadd_rn(cc[i], 0.0));
 }
 
 // Element order and roots.  Thread x < E fills position x; one thread per tile sets up its root.
@@ -166,7 +164,7 @@ __global__ void k_rt_init(RtArgs A) {
     if (k < T.n) {
       const uint32_t slot = T.order ? static_cast<uint32_t>(T.order[k] - T.obase) : static_cast<uint32_t>(k);
       A.idx[0][x] = slot;
-      rt_key9(T, slot, A.key[0], A.E, x);
+      rt_key3(T, slot, A.key[0], A.E, x);
       v = T.n > static_cast<uint32_t>(RT_CTA_MAX) ? static_cast<uint32_t>(T.nbase + 1) : RT_DONE;
     }
     A.nof[0][x] = v;
@@ -180,6 +178,7 @@ __global__ void k_rt_init(RtArgs A) {
     A.ncount[root] = T.n;
     A.ntile[root] = static_cast<uint32_t>(t);
     A.ndepth[root] = 1;
+    A.parent[root] = RT_NONE;
     rt_enqueue(A, static_cast<uint32_t>(root), T.n, 0);
   }
 }
@@ -190,34 +189,34 @@ __device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsig
 // Segment-wise reduction over a warp's 32 consecutive positions: lanes with equal `seg` form
 // contiguous runs (a node is a contiguous range of positions, so equal values at two lanes mean
 // the same node in between).  On return the first lane of each run holds the run's minima
-// (k[0..5]) and maxima (k[6..11]); the return value says whether this lane is a run's first.
+// (k[0..2]) and maxima (k[3..5]); the return value says whether this lane is a run's first.
 // Lanes without a node pass a seg value no other lane has.
-__device__ __forceinline__ bool rt_seg_reduce(uint32_t seg, unsigned long long k[12]) {
+__device__ __forceinline__ bool rt_seg_reduce(uint32_t seg, unsigned long long k[6]) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
     const uint32_t ns = __shfl_down_sync(0xffffffffu, seg, o);
     const bool take = lane + o < 32 && ns == seg;
 #pragma unroll
-    for (int i = 0; i < 12; ++i) {
+    for (int i = 0; i < 6; ++i) {
       const unsigned long long y = __shfl_down_sync(0xffffffffu, k[i], o);
-      if (take) k[i] = i < 6 ? umin64(k[i], y) : umax64(k[i], y);
+      if (take) k[i] = i < 3 ? umin64(k[i], y) : umax64(k[i], y);
     }
   }
   const uint32_t up = __shfl_up_sync(0xffffffffu, seg, 1);
   return lane == 0 || up != seg;
 }
 
-__device__ __forceinline__ void rt_keys_empty(unsigned long long k[12]) {
+__device__ __forceinline__ void rt_keys_empty(unsigned long long k[6]) {
 #pragma unroll
-  for (int i = 0; i < 6; ++i) {
+  for (int i = 0; i < 3; ++i) {
     k[i] = ~0ull;
-    k[6 + i] = 0ull;
+    k[3 + i] = 0ull;
   }
 }
 
-// Box and centroid box of every pending node: segment-wise per warp, then one set of 12 atomics
-// per warp and node.
+// Centroid box of every pending node: segment-wise per warp, then one set of 6 atomics per warp
+// and node.
 __global__ void k_rt_reduce(RtArgs A, int c) {
   if (A.cnt[c] == 0) return;
   const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
@@ -226,15 +225,15 @@ __global__ void k_rt_reduce(RtArgs A, int c) {
     const uint32_t node = x < A.E ? A.nof[c][x] : RT_DONE;
     const bool act = !(node & RT_DONE);
     if (!__any_sync(0xffffffffu, act)) continue;
-    unsigned long long k[12];
+    unsigned long long k[6];
     if (act) rt_keys(A.key[c], A.E, x, k); else rt_keys_empty(k);
     const bool head = rt_seg_reduce(act ? node : (RT_DONE | (threadIdx.x & 31)), k);
     if (act && head) {
-      unsigned long long* a = A.acc + 12ull * node;
+      unsigned long long* a = A.acc + 6ull * node;
 #pragma unroll
-      for (int i = 0; i < 6; ++i) atomicMin(a + i, k[i]);
+      for (int i = 0; i < 3; ++i) atomicMin(a + i, k[i]);
 #pragma unroll
-      for (int i = 6; i < 12; ++i) atomicMax(a + i, k[i]);
+      for (int i = 3; i < 6; ++i) atomicMax(a + i, k[i]);
     }
   }
 }
@@ -245,16 +244,12 @@ __global__ void k_rt_decide(RtArgs A, int c) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nw; i += gridDim.x * blockDim.x) {
     const uint32_t node = A.wl[c][i];
     const int t = static_cast<int>(A.ntile[node]);
-    const unsigned long long* a = A.acc + 12ull * node;
-    double lo[3], hi[3], clo[3], chi[3];
+    const unsigned long long* a = A.acc + 6ull * node;
+    double clo[3], chi[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      lo[k] = unord64(a[k]);
-      clo[k] = unord64(a[3 + k]);
-      hi[k] = unord64(a[6 + k]);
-      chi[k] = unord64(a[9 + k]);
-      A.box64[6ull * node + k] = lo[k];
-      A.box64[6ull * node + 3 + k] = hi[k];
+      clo[k] = unord64(a[k]);
+      chi[k] = unord64(a[3 + k]);
     }
     const double ex = __dsub_rn(chi[0], clo[0]), ey = __dsub_rn(chi[1], clo[1]), ez = __dsub_rn(chi[2], clo[2]);
     const int axis = (ex >= ey && ex >= ez) ? 0 : (ey >= ez ? 1 : 2);
@@ -268,6 +263,8 @@ __global__ void k_rt_decide(RtArgs A, int c) {
     A.nmid[node] = __dmul_rn(0.5, __dadd_rn(clo[axis], chi[axis]));
     const unsigned long long nb = A.tiles[t].nbase;
     A.nchild[node] = make_int2(static_cast<int>(nb + l), static_cast<int>(nb + l + 1));
+    A.parent[nb + l] = node;
+    A.parent[nb + l + 1] = node;
   }
 }
 
@@ -307,7 +304,7 @@ __device__ __forceinline__ uint32_t rt_flag(const RtArgs& A, int c, unsigned lon
   if (node & RT_DONE) return 0u;
   const int axis = A.nsplit[node];
   if (axis < 0) return 0u;
-  return A.key[c][(6 + axis) * A.E + x] < ord64(A.nmid[node]) ? 0u : 1u;
+  return A.key[c][axis * A.E + x] < ord64(A.nmid[node]) ? 0u : 1u;
 }
 
 // Flags and their block sums.
@@ -426,7 +423,7 @@ __global__ void k_rt_place(RtArgs A, int c) {
     const uint32_t csize = left ? Sp : n - Sp;
     A.idx[o][s + dest] = el;
 #pragma unroll
-    for (int f = 0; f < 9; ++f) A.key[o][f * A.E + s + dest] = A.key[c][f * A.E + x];
+    for (int f = 0; f < 3; ++f) A.key[o][f * A.E + s + dest] = A.key[c][f * A.E + x];
     A.nof[o][s + dest] = csize > static_cast<uint32_t>(RT_CTA_MAX) ? child : RT_DONE;
     if (r == 0) {
       const uint32_t t = A.ntile[node], dep = A.ndepth[node] + 1;
@@ -459,7 +456,7 @@ __global__ void k_rt_check(RtArgs A, int c) {
 // with its elements in shared memory.  Each level runs the passes of the global levels over all
 // of the level's nodes of more than RT_LEAF_MAX elements at once (segment-wise reduce, decide,
 // flags and prefix sum, ranks, place); a child of at most RT_LEAF_MAX elements is a leaf
-// (bvh.rs:200-204) whose box one thread takes at the start of the next level.
+// (bvh.rs:200-204), whose fields one thread writes at the start of the next level.
 constexpr int RT_CTA_T = 256;                                // threads per block
 constexpr int RT_CTA_PER = RT_CTA_MAX / RT_CTA_T;            // positions per thread
 constexpr int RT_LEAF_MAX = 4;                               // subdivide's leaf size
@@ -470,11 +467,11 @@ static_assert(RT_CTA_LV < RT_CTA_FREE, "level slots must fit a byte");
 static_assert(RT_CTA_MAX <= 2048, "positions are packed in 11 bits");
 
 struct RtCtaSmem {
-  unsigned long long key[9][RT_CTA_MAX];  // the job's element keys, at their load position (home)
-  // Per level: the nodes' box accumulators (reduce to decide), then the flags' prefix sum and the
-  // ranks (flags to place); the two uses do not overlap.
+  unsigned long long key[3][RT_CTA_MAX];  // the job's centroid keys, at their load position (home)
+  // Per level: the nodes' centroid accumulators (reduce to decide), then the flags' prefix sum and
+  // the ranks (flags to place); the two uses do not overlap.
   union {
-    unsigned long long acc[RT_CTA_LV][12];  // per level node: ordered minima, maxima
+    unsigned long long acc[RT_CTA_LV][6];   // per level node: ordered minima, maxima
     struct {
       uint16_t bb[RT_CTA_MAX + 1];          // exclusive prefix sum of the flags
       uint16_t P[RT_CTA_MAX], Q[RT_CTA_MAX];
@@ -514,7 +511,7 @@ __global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
     for (int x = tid; x < RT_CTA_MAX; x += RT_CTA_T) {
       if (x < n) {
 #pragma unroll
-        for (int f = 0; f < 9; ++f) S.key[f][x] = A.key[par][f * A.E + s + x];
+        for (int f = 0; f < 3; ++f) S.key[f][x] = A.key[par][f * A.E + s + x];
         S.home[x] = static_cast<uint16_t>(x);
         S.idx[x] = A.idx[par][s + x];
         S.nd[x] = n > RT_LEAF_MAX ? 0 : RT_CTA_FREE;
@@ -547,21 +544,6 @@ __global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
         const uint32_t e = S.sl[i], id = S.slid[i];
         const int o0 = static_cast<int>(e & 2047u), cn = static_cast<int>((e >> 11) & 7u);
         const uint32_t dp = e >> 14;
-        unsigned long long k[12], kk[12];
-        rt_keys_empty(k);
-        for (int j = 0; j < cn; ++j) {
-          rt_keys(&S.key[0][0], RT_CTA_MAX, S.home[o0 + j], kk);
-#pragma unroll
-          for (int m = 0; m < 6; ++m) {
-            k[m] = umin64(k[m], kk[m]);
-            k[6 + m] = umax64(k[6 + m], kk[6 + m]);
-          }
-        }
-#pragma unroll
-        for (int m = 0; m < 3; ++m) {
-          A.box64[6ull * id + m] = unord64(k[m]);
-          A.box64[6ull * id + 3 + m] = unord64(k[6 + m]);
-        }
         A.nstart[id] = s + static_cast<uint32_t>(o0);
         A.ncount[id] = static_cast<uint32_t>(cn);
         A.ntile[id] = t;
@@ -569,7 +551,7 @@ __global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
         A.nsplit[id] = -1;
         atomicMax(&S.maxdep, dp);
       }
-      for (int i = tid; i < nl * 12; i += RT_CTA_T) S.u.acc[i / 12][i % 12] = (i % 12) < 6 ? ~0ull : 0ull;
+      for (int i = tid; i < nl * 6; i += RT_CTA_T) S.u.acc[i / 6][i % 6] = (i % 6) < 3 ? ~0ull : 0ull;
       __syncthreads();
       if (nl == 0) break;
       if (tid == 0) {
@@ -583,14 +565,14 @@ __global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
         const uint32_t node = S.nd[x];
         const bool act = node != RT_CTA_FREE;
         if (!__any_sync(0xffffffffu, act)) continue;
-        unsigned long long kk[12];
+        unsigned long long kk[6];
         if (act) rt_keys(&S.key[0][0], RT_CTA_MAX, S.home[x], kk); else rt_keys_empty(kk);
         const bool head = rt_seg_reduce(act ? node : (0x100u | static_cast<uint32_t>(lane)), kk);
         if (act && head) {
 #pragma unroll
-          for (int i = 0; i < 6; ++i) atomicMin(&S.u.acc[node][i], kk[i]);
+          for (int i = 0; i < 3; ++i) atomicMin(&S.u.acc[node][i], kk[i]);
 #pragma unroll
-          for (int i = 6; i < 12; ++i) atomicMax(&S.u.acc[node][i], kk[i]);
+          for (int i = 3; i < 6; ++i) atomicMax(&S.u.acc[node][i], kk[i]);
         }
       }
       __syncthreads();
@@ -598,15 +580,11 @@ __global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
       for (int i = tid; i < nl; i += RT_CTA_T) {
         const uint32_t id = S.id[cur][i];
         const int cn = S.cnt[cur][i];
-        double lo[3], hi[3], clo[3], chi[3];
+        double clo[3], chi[3];
 #pragma unroll
         for (int m = 0; m < 3; ++m) {
-          lo[m] = unord64(S.u.acc[i][m]);
-          clo[m] = unord64(S.u.acc[i][3 + m]);
-          hi[m] = unord64(S.u.acc[i][6 + m]);
-          chi[m] = unord64(S.u.acc[i][9 + m]);
-          A.box64[6ull * id + m] = lo[m];
-          A.box64[6ull * id + 3 + m] = hi[m];
+          clo[m] = unord64(S.u.acc[i][m]);
+          chi[m] = unord64(S.u.acc[i][3 + m]);
         }
         A.nstart[id] = s + S.off[cur][i];
         A.ncount[id] = static_cast<uint32_t>(cn);
@@ -630,6 +608,8 @@ __global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
           A.nsplit[id] = axis;
           A.nmid[id] = mid;
           A.nchild[id] = make_int2(static_cast<int>(nb + l), static_cast<int>(nb + l + 1));
+          A.parent[nb + l] = id;
+          A.parent[nb + l + 1] = id;
         }
       }
       __syncthreads();
@@ -642,7 +622,7 @@ __global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
           const uint32_t node = S.nd[x];
           f[k] = 0;
           if (node != RT_CTA_FREE && S.axis[node] >= 0)
-            f[k] = S.key[6 + S.axis[node]][S.home[x]] < ord64(S.mid[node]) ? 0u : 1u;
+            f[k] = S.key[S.axis[node]][S.home[x]] < ord64(S.mid[node]) ? 0u : 1u;
           sum += f[k];
         }
         uint32_t incl = sum;
@@ -758,6 +738,74 @@ __global__ void __launch_bounds__(RT_CTA_T, 2) k_rt_cta(RtArgs A) {
     for (int x = tid; x < n; x += RT_CTA_T) A.ridx[s + x] = S.idx[x];
     if (tid == 0) atomicMax(&A.tiles[t].depth, S.maxdep);
     __syncthreads();
+  }
+}
+
+// Node boxes (the BVHNode aabb: the union of the node's elements' max_dim boxes, bvh.rs:196-204),
+// bottom up over the final topology, one thread per node: a leaf forms its box from its elements
+// (in the order-preserving key domain, as a union of the elements' boxes compares them), then
+// climbs: at each parent the first child to arrive stops and the second forms the parent's box as
+// the union of both children's.  Boxes are published with a fence before the arrival count and
+// read through L2.  `arrive` holds one zeroed counter per node.
+__global__ void k_rt_refit(RtArgs A, uint32_t* arrive) {
+  const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+  for (unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; g < A.N;
+       g += stride) {
+    int lo_ = 0, hi_ = A.ntiles - 1;
+    while (lo_ < hi_) {
+      const int mid = (lo_ + hi_ + 1) >> 1;
+      if (A.tiles[mid].nbase <= g) lo_ = mid; else hi_ = mid - 1;
+    }
+    const RTile& T = A.tiles[lo_];
+    const uint32_t id = static_cast<uint32_t>(g - T.nbase);
+    if (id == 0 || id >= min(T.nodes, T.ncap) || (id == 1 && T.n == 0) || A.nsplit[g] >= 0) continue;
+    const uint32_t st = A.nstart[g], cn = A.ncount[g];
+    if (st < T.ebase || st - T.ebase + static_cast<unsigned long long>(cn) > T.n) {
+      atomicOr(A.err, ERR_BAD_INDEX);
+      continue;
+    }
+    unsigned long long k[6];
+    rt_keys_empty(k);
+    for (uint32_t j = 0; j < cn; ++j) {
+      const uint32_t slot = A.ridx[st + j];  // a slot k_rt_init read the keys of
+      double lo[3], hi[3], cc[3];
+      rt_box_pm(rt_pm(T, slot), lo, hi, cc);
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        k[m] = umin64(k[m], ord64(lo[m]));
+        k[3 + m] = umax64(k[3 + m], ord64(hi[m]));
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < 6; ++m) A.box64[6ull * g + m] = unord64(k[m]);
+    const unsigned long long nlo = T.nbase, nhi = T.nbase + T.ncap;
+    unsigned long long node = g;
+    for (int up = 0; up <= RT_MAX_DEPTH; ++up) {
+      const uint32_t p = A.parent[node];
+      if (p == RT_NONE) break;
+      if (p < nlo || p >= nhi) {
+        atomicOr(A.err, ERR_BAD_INDEX);
+        break;
+      }
+      __threadfence();
+      if (atomicAdd(&arrive[p], 1u) == 0u) break;  // the other child forms the parent's box
+      __threadfence();
+      const int2 ch = A.nchild[p];
+      if (static_cast<unsigned long long>(ch.x) < nlo || static_cast<unsigned long long>(ch.y) >= nhi) {
+        atomicOr(A.err, ERR_BAD_INDEX);
+        break;
+      }
+      const double* a = A.box64 + 6ull * static_cast<unsigned long long>(ch.x);
+      const double* b = A.box64 + 6ull * static_cast<unsigned long long>(ch.y);
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        const unsigned long long l = umin64(ord64(__ldcg(a + m)), ord64(__ldcg(b + m)));
+        const unsigned long long h = umax64(ord64(__ldcg(a + 3 + m)), ord64(__ldcg(b + 3 + m)));
+        A.box64[6ull * p + m] = unord64(l);
+        A.box64[6ull * p + 3 + m] = unord64(h);
+      }
+      node = p;
+    }
   }
 }
 
@@ -910,6 +958,7 @@ RtArgs rt_args(RTreeBufs& B, uint32_t* err) {
   A.ridx = B.ridx.p;
   A.acc = B.acc.p;
   A.box64 = B.box64.p;
+  A.parent = B.parent.p;
   A.nstart = B.nstart.p;
   A.ncount = B.ncount.p;
   A.ntile = B.ntile.p;
@@ -954,8 +1003,8 @@ void rtree_alloc(RTreeBufs& B, std::vector<RTile>& tiles, bool want_leafof, cuda
   FG_CUDA(cudaMemcpyAsync(B.tiles.p, tiles.data(), tiles.size() * sizeof(RTile), cudaMemcpyHostToDevice, st));
   B.idx0.alloc(E1, st);
   B.idx1.alloc(E1, st);
-  B.key0.alloc(9 * E1, st);
-  B.key1.alloc(9 * E1, st);
+  B.key0.alloc(3 * E1, st);
+  B.key1.alloc(3 * E1, st);
   B.nof0.alloc(E1, st);
   B.nof1.alloc(E1, st);
   B.flag.alloc(E1 + 1, st);
@@ -965,8 +1014,9 @@ void rtree_alloc(RTreeBufs& B, std::vector<RTile>& tiles, bool want_leafof, cuda
   B.P.alloc(E1, st);
   B.Q.alloc(E1, st);
   B.ridx.alloc(E1, st);
-  B.acc.alloc(12 * N1, st);
+  B.acc.alloc(6 * N1, st);
   B.box64.alloc(6 * N1, st);
+  B.parent.alloc(N1, st);
   B.nstart.alloc(N1, st);
   B.ncount.alloc(N1, st);
   B.ntile.alloc(N1, st);
@@ -1005,8 +1055,8 @@ size_t carve(RTreeBufs* B, uint32_t ecap, bool want_leafof, uint32_t leafof_slot
   take(b.tiles, 1);
   take(b.idx0, E1);
   take(b.idx1, E1);
-  take(b.key0, 9 * E1);
-  take(b.key1, 9 * E1);
+  take(b.key0, 3 * E1);
+  take(b.key1, 3 * E1);
   take(b.nof0, E1);
   take(b.nof1, E1);
   take(b.flag, E1 + 1);
@@ -1015,8 +1065,9 @@ size_t carve(RTreeBufs* B, uint32_t ecap, bool want_leafof, uint32_t leafof_slot
   take(b.P, E1);
   take(b.Q, E1);
   take(b.ridx, E1);
-  take(b.acc, 12 * N1);
+  take(b.acc, 6 * N1);
   take(b.box64, 6 * N1);
+  take(b.parent, N1);
   take(b.nstart, N1);
   take(b.ncount, N1);
   take(b.ntile, N1);
@@ -1090,6 +1141,9 @@ void rtree_build(RTreeBufs& B, uint32_t* err, cudaStream_t st, RTile* tiles_dev)
   FG_CUDA(cudaFuncSetAttribute(k_rt_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                static_cast<int>(sizeof(RtCtaSmem))));
   k_rt_cta<<<GC, RT_CTA_T, sizeof(RtCtaSmem), st>>>(A);
+  // The global worklist is spent: its words count the children that reached each node.
+  FG_CUDA(cudaMemsetAsync(B.wl0.p, 0, static_cast<size_t>(B.N) * sizeof(uint32_t), st));
+  k_rt_refit<<<GN, RT_BLOCK, 0, st>>>(A, B.wl0.p);
   k_rt_records<<<GN, RT_BLOCK, 0, st>>>(A, B.rnode.p, B.rleaf.p, B.leafof.p, B.leafof.n);
   k_rt_depth_check<<<grid_for(static_cast<size_t>(B.ntiles), 128), 128, 0, st>>>(A);
   FG_CUDA(cudaGetLastError());
@@ -1147,7 +1201,7 @@ void build_emulsion_tree(fg_engine* e, const fg_emulsion* em, bool developed_onl
 }
 
 unsigned rtree_kernel_launches(const RTreeBufs& B) {
-  return B.ntiles ? 1u + 8u * static_cast<unsigned>(B.levels) + 4u : 0u;
+  return B.ntiles ? 1u + 8u * static_cast<unsigned>(B.levels) + 5u : 0u;
 }
 
 }  // namespace fg

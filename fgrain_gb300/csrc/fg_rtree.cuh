@@ -77,8 +77,8 @@ constexpr size_t rt_attach_blocks(size_t e1) { return (e1 + 1 + 2047) / 2048; }
 constexpr size_t rt_al(size_t v) { return (v + 255) / 256 * 256; }
 constexpr size_t rtree_attach_bytes(size_t ecap, bool want_leafof, size_t slots) {
   const size_t e1 = ecap > 0 ? ecap : 1, n1 = rt_attach_nodes(e1);
-  return rt_al(112) + 4 * rt_al(4 * e1) + 2 * rt_al(72 * e1) + 2 * rt_al(4 * (e1 + 1)) + rt_al(4 * rt_attach_blocks(e1)) +
-         3 * rt_al(4 * e1) + rt_al(96 * n1) + rt_al(48 * n1) + 4 * rt_al(4 * n1) + rt_al(4 * n1) + rt_al(8 * n1) +
+  return rt_al(112) + 4 * rt_al(4 * e1) + 2 * rt_al(24 * e1) + 2 * rt_al(4 * (e1 + 1)) + rt_al(4 * rt_attach_blocks(e1)) +
+         3 * rt_al(4 * e1) + rt_al(48 * n1) + rt_al(48 * n1) + rt_al(4 * n1) + 4 * rt_al(4 * n1) + rt_al(4 * n1) + rt_al(8 * n1) +
          rt_al(8 * n1) + 4 * rt_al(4 * n1) + rt_al(16) + rt_al(128 * (n1 / 2 + 1)) + rt_al(8 * n1) +
          (want_leafof ? rt_al(4 * (slots > 0 ? slots : 1)) : 0);
 }

@@ -464,7 +464,7 @@ fg_status fg_render_tile_fast(fg_engine* e, const float* tile, const fg_tile_par
 #define FG_STATIC_SCAN_MAX_DEVELOPED 32768u  /* developed crystals per call */
 #define FG_STATIC_SCAN_MAX_BINS 16384u       /* scan bins (bin_px x bin_px pixels each) per call */
 #define FG_STATIC_SCAN_MAX_ITEMS 1048576u    /* (developed crystal, bin) entries per call */
-#define FG_STATIC_SCAN_SCRATCH_BYTES 21661952u
+#define FG_STATIC_SCAN_SCRATCH_BYTES 17360128u
 
 /* A crystal set in device memory, in crystal-index order (any order gives the same image). */
 typedef struct fg_device_crystals {
