@@ -10,70 +10,97 @@
 #include "fg_internal.h"
 #include "fg_transport.cuh"
 
-#ifndef FG_DEFERRED_LEAVES
-#define FG_DEFERRED_LEAVES 1
-#endif
-
 namespace fg {
 
 // ---------------------------------------------------------------------------------------------
-// Production kernel with lane refill: each loop turn every lane with a live packet runs one bounce
-// (its tree walk with absorption, then the move or scatter); lanes whose packet died take the next
-// photon of the position-ordered queue, so the warp stays full until the queue is empty.
-// Launch bounds of 4 blocks of 256 per SM (64 registers): the walk is latency-bound, and with
-// the brick-ordered tree 32 resident warps with fewer spills beat 40 at 48 registers and 48 at
-// 40 (10.9 against 11.1 and 13.1 ms on the 1024x1024 ss2 workload).
+// Production kernel.  Every lane carries one photon through its bounces; a lane is in one of five
+// states: no photon, a photon between bounces, a bounce walking (fg_transport.cuh: Bounce), a
+// walked bounce whose end is pending, or done (the photon queue is spent).  Each loop turn the warp
+// does one of two kinds of work:
+//   - restart: once WALK_RESTART lanes are idle (or none walks), the walked lanes end their
+//     bounces, lanes between bounces begin the next one, and empty lanes take the next photons of
+//     the position-ordered queue (which begin their first bounce at once);
+//   - otherwise walk: while a walking lane still needs a leaf, walk steps for every walking lane
+//     whose leaf queue has room; then every walking lane tests its oldest queued leaf.
+// So lanes whose walk ended early wait for a group of restarts, not for the warp's longest walk,
+// and the ends and beginnings of bounces still run with many lanes.  Which lane traces a photon,
+// and when, never changes its result: its draws are named by (photon, bounce, slot, tag), and its
+// leaves are tested in walk order.
+// Launch bounds of 4 blocks of 256 per SM (64 registers): the walk is latency-bound.
 __global__ void __launch_bounds__(256, 4) k_transport(const TileDesc* __restrict__ tiles, int ntiles,
                                                      unsigned long long total, const uint32_t* __restrict__ order,
                                                      unsigned long long* next, uint32_t* err,
                                                      unsigned long long* stats) {
+  constexpr unsigned FULL = 0xffffffffu;
+  enum : int { EMPTY_LANE = 0, READY = 1, WALKING = 2, WALKED = 3, DONE = 4 };
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
-  Photon ph;
+  Photon ph{};
+  Bounce w;
+  int stack[RT_STACK4];
   int tile = 0;
-  bool alive = false, done = false;
+  int state = EMPTY_LANE;
   unsigned long long my_hits = 0;
+  w.cur = WALK_EMPTY;
+#pragma unroll
+  for (int j = 0; j < WALK_LEAVES; ++j) w.lv[j] = WALK_NONE;
   for (;;) {
-    unsigned need = __ballot_sync(0xffffffffu, !alive && !done);
-    while (need) {
-      unsigned long long base = 0;
-      if (lane == 0) base = atomicAdd(next, static_cast<unsigned long long>(__popc(need)));
-      base = __shfl_sync(0xffffffffu, base, 0);
-      if (!alive && !done) {
-        const unsigned long long g = base + __popc(need & lt);
-        if (g >= total) {
-          done = true;
+    if (state == WALKING && w.cur == WALK_EMPTY && w.lv[0] == WALK_NONE) state = WALKED;
+    const unsigned walkm = __ballot_sync(FULL, state == WALKING);
+    const unsigned idlem = __ballot_sync(FULL, state != WALKING && state != DONE);
+    if (!(walkm | idlem)) break;
+    if (!walkm || __popc(idlem) >= WALK_RESTART) {
+      if (state == WALKED) {
+        my_hits += w.nh;
+        state = bounce_end(tiles[tile], ph, w) ? READY : EMPTY_LANE;
+      }
+      if (state == READY) {
+        if (ph.b < tiles[tile].max_bounces) {
+          bounce_begin(tiles[tile], ph, w);
+          state = WALKING;
         } else {
-          unsigned long long gid = order ? order[g] : g;
-          if (!index_ok(gid < total, err, SITE_PHOTON_ID, static_cast<uint32_t>(gid), static_cast<uint32_t>(g)))
-            gid = g;
-          int lo = 0, hi = ntiles - 1;
-          while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (tiles[mid].photon_base <= gid) lo = mid; else hi = mid - 1;
-          }
-          tile = lo;
-          alive = emit_photon(tiles[lo], static_cast<uint32_t>(gid - tiles[lo].photon_base), ph);
+          state = EMPTY_LANE;
         }
       }
-      need = __ballot_sync(0xffffffffu, !alive && !done);
-    }
-    if (!__any_sync(0xffffffffu, alive)) break;
-    // The lanes with a bounce to run walk together (deferred leaf tests need the full set).
-    const bool go = alive && ph.b < tiles[tile].max_bounces;
-    const unsigned amask = __ballot_sync(0xffffffffu, go);
-    if (alive) {
-      if (!go) {
-        alive = false;
-      } else {
-        uint32_t nh = 0;
-        alive = photon_bounce(tiles[tile], ph, err, nh, FG_DEFERRED_LEAVES ? amask : 0u);
-        my_hits += nh;
+      unsigned need = __ballot_sync(FULL, state == EMPTY_LANE);
+      while (need) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(next, static_cast<unsigned long long>(__popc(need)));
+        base = __shfl_sync(FULL, base, 0);
+        if (state == EMPTY_LANE) {
+          const unsigned long long g = base + __popc(need & lt);
+          if (g >= total) {
+            state = DONE;
+          } else {
+            unsigned long long gid = order ? order[g] : g;
+            if (!index_ok(gid < total, err, SITE_PHOTON_ID, static_cast<uint32_t>(gid), static_cast<uint32_t>(g)))
+              gid = g;
+            int lo = 0, hi = ntiles - 1;
+            while (lo < hi) {
+              const int mid = (lo + hi + 1) >> 1;
+              if (tiles[mid].photon_base <= gid) lo = mid; else hi = mid - 1;
+            }
+            tile = lo;
+            if (emit_photon(tiles[lo], static_cast<uint32_t>(gid - tiles[lo].photon_base), ph) &&
+                ph.b < tiles[lo].max_bounces) {
+              bounce_begin(tiles[lo], ph, w);
+              state = WALKING;
+            }
+          }
+        }
+        need = __ballot_sync(FULL, state == EMPTY_LANE);
       }
+      continue;
     }
+    for (;;) {
+      if (!__any_sync(FULL, state == WALKING && w.cur != WALK_EMPTY && w.lv[0] == WALK_NONE)) break;
+      if (state == WALKING && w.cur != WALK_EMPTY && w.lv[WALK_LEAVES - 1] == WALK_NONE)
+        walk_step(tiles[tile], w, stack, err);
+    }
+    if (state == WALKING && w.lv[0] != WALK_NONE) leaf_step(tiles[tile], ph, w, err);
   }
   if (stats) {
-    for (int o = 16; o > 0; o >>= 1) my_hits += __shfl_down_sync(0xffffffffu, my_hits, o);
+    for (int o = 16; o > 0; o >>= 1) my_hits += __shfl_down_sync(FULL, my_hits, o);
     if (lane == 0 && my_hits) atomicAdd(&stats[0], my_hits);
   }
 }

@@ -6,7 +6,10 @@
 
 namespace fg {
 
-constexpr int WALK_LEAVES = 6;  // leaves a lane may hold while its warp still walks (speculative traversal)
+constexpr int WALK_LEAVES = 6;    // leaves a lane may hold while its warp still walks (speculative traversal)
+constexpr int WALK_RESTART = 24;  // idle lanes of a warp that end and start their bounces together
+constexpr int WALK_EMPTY = INT32_MIN;
+constexpr uint32_t WALK_NONE = 0xffffffffu;
 
 // Everything one tile's transport needs, 16-byte aligned for vector loads.  The walk runs over the
 // tile's reference tree (fg_rtree.cuh): rnode / rleaf indexed by tile-local node id, ridx by
@@ -34,104 +37,6 @@ struct __align__(16) TileDesc {
   float mu_t, albedo, g, r0, eff_r, theta_max, alpha;
   uint32_t max_bounces;
 };
-
-// Walk of a reference tree in the reference's order (BVH::intersect_ray_all, bvh.rs:300-347: push
-// left then right, pop right first) over its four-wide records (fg_rtree.cuh), whose children
-// are stored in that visiting order: the first hit child is entered, the other hit children are
-// pushed so that they come off the stack in order.  Deferred: a hit leaf is queued until every
-// lane of `amask` holds one or has finished, then the lanes run fn(leaf) together; a lane that
-// holds a leaf walks on (speculatively) until it holds WALK_LEAVES.  The queue keeps each lane's
-// leaves in walk order.  An internal child is entered when its (extended) box meets [0, tlim] of
-// the ray (the caller's step, padded); a leaf child when its box extended by `reach` meets
-// [0, tlim] (a crystal hit inside the step lies there) and its own box meets the whole ray (the
-// reference's leaf test, bvh.rs:96-124).  nrec and nleaf bound the record indices and leaf ids
-// (index checks).  With amask = the lane's own bit it is a plain walk.
-template <class F>
-__device__ __forceinline__ void rt_walk_deferred(const Node4* __restrict__ rec, float3 o, float3 inv, float tlim,
-                                                 float reach, uint32_t* err, F&& fn, uint32_t nrec, uint32_t nleaf,
-                                                 unsigned amask) {
-  constexpr int EMPTY = INT32_MIN;
-  constexpr uint32_t NONE = 0xffffffffu;
-  int stack[RT_STACK4];
-  int sp = 0;
-  int cur = 0;  // record 0: the root's
-  uint32_t lv[WALK_LEAVES];
-#pragma unroll
-  for (int j = 0; j < WALK_LEAVES; ++j) lv[j] = NONE;
-  const float3 oi = make_float3(o.x * inv.x, o.y * inv.y, o.z * inv.z);
-  for (;;) {
-    for (;;) {
-      const bool need = cur != EMPTY && lv[0] == NONE;
-      if (!__any_sync(amask, need)) break;
-      const bool want = cur != EMPTY && lv[WALK_LEAVES - 1] == NONE;
-      if (!want) continue;
-      if (cur < 0) {
-        const uint32_t lf = static_cast<uint32_t>(~cur);
-        bool placed = false;
-#pragma unroll
-        for (int j = 0; j < WALK_LEAVES; ++j) {
-          if (!placed && lv[j] == NONE) {
-            lv[j] = lf;
-            placed = true;
-          }
-        }
-        cur = sp > 0 ? stack[--sp] : EMPTY;
-        continue;
-      }
-      if (!index_ok(static_cast<uint32_t>(cur) < nrec, err, SITE_NODE, static_cast<uint32_t>(cur), nrec)) {
-        cur = EMPTY;
-        continue;
-      }
-      const Node4* nd = rec + cur;
-      const float4 lx = __ldg(&nd->lox), ly = __ldg(&nd->loy), lz = __ldg(&nd->loz);
-      const float4 hx = __ldg(&nd->hix), hy = __ldg(&nd->hiy), hz = __ldg(&nd->hiz);
-      const int4 rf = __ldg(&nd->ref);
-      // Slab test as lo * inv - o * inv (one FMA per plane), the box grown by g, clipped to [0, t].
-      auto slab_hit = [&](float a0, float a1, float a2, float a3, float a4, float a5, float g, float t) {
-        const float t1x = fmaf(a0 - g, inv.x, -oi.x), t2x = fmaf(a3 + g, inv.x, -oi.x);
-        const float t1y = fmaf(a1 - g, inv.y, -oi.y), t2y = fmaf(a4 + g, inv.y, -oi.y);
-        const float t1z = fmaf(a2 - g, inv.z, -oi.z), t2z = fmaf(a5 + g, inv.z, -oi.z);
-        const float te = fmaxf(fmaxf(fminf(t1x, t2x), fminf(t1y, t2y)), fmaxf(fminf(t1z, t2z), 0.0f));
-        const float tx = fminf(fminf(fmaxf(t1x, t2x), fmaxf(t1y, t2y)), fminf(fmaxf(t1z, t2z), t));
-        return te <= tx;
-      };
-      auto hit = [&](int ref, float a0, float a1, float a2, float a3, float a4, float a5) {
-        if (ref == EMPTY) return false;
-        if (ref >= 0) return slab_hit(a0, a1, a2, a3, a4, a5, 0.0f, tlim);
-        return slab_hit(a0, a1, a2, a3, a4, a5, reach, tlim) && slab_hit(a0, a1, a2, a3, a4, a5, 0.0f, INFINITY);
-      };
-      const bool h0 = hit(rf.x, lx.x, ly.x, lz.x, hx.x, hy.x, hz.x);
-      const bool h1 = hit(rf.y, lx.y, ly.y, lz.y, hx.y, hy.y, hz.y);
-      const bool h2 = hit(rf.z, lx.z, ly.z, lz.z, hx.z, hy.z, hz.z);
-      const bool h3 = hit(rf.w, lx.w, ly.w, lz.w, hx.w, hy.w, hz.w);
-      // Enter the first hit child; push the later ones, last first.
-      int next = EMPTY;
-      auto take = [&](bool h, int r) {
-        if (!h) return;
-        if (next != EMPTY) {
-          if (sp < RT_STACK4) {
-            stack[sp++] = next;
-          } else {
-            atomicOr(err, ERR_STACK_OVERFLOW);
-          }
-        }
-        next = r;
-      };
-      take(h3, rf.w);
-      take(h2, rf.z);
-      take(h1, rf.y);
-      take(h0, rf.x);
-      cur = next != EMPTY ? next : (sp > 0 ? stack[--sp] : EMPTY);
-    }
-    if (!__any_sync(amask, lv[0] != NONE)) break;
-    if (lv[0] != NONE) {
-      if (index_ok(lv[0] < nleaf, err, SITE_LEAF, lv[0], nleaf)) fn(lv[0]);
-#pragma unroll
-      for (int j = 0; j + 1 < WALK_LEAVES; ++j) lv[j] = lv[j + 1];
-      lv[WALK_LEAVES - 1] = NONE;
-    }
-  }
-}
 
 // 1 / d for the walk's slab tests, kept finite: the test forms lo * inv - o * inv with one FMA, and
 // an infinite inv (a direction component of 0, or below 1e-30) would turn that into inf - inf =
@@ -172,8 +77,9 @@ __device__ __forceinline__ void add_counts(uint32_t* counts, uint32_t s, uint32_
 }
 
 // ---------------------------------------------------------------------------------------------
-// Photon state for the lane-refilling transport kernel: one bounce of the reference's loop per
-// call, so a lane whose packet dies takes a new photon while the rest of the warp carries on.
+// A packet between bounces (transport.rs:72-185): position, direction, energy, photon id and the
+// number of bounces begun.  The transport kernel keeps one per lane and refills a lane whose packet
+// died with the next photon while the rest of the warp carries on.
 struct Photon {
   float3 pos, dir;
   float E;
@@ -212,64 +118,171 @@ __device__ __forceinline__ bool emit_photon(const TileDesc& t, uint32_t id, Phot
   return true;
 }
 
-// One bounce (transport.rs:101-185).  Returns whether the packet is still alive.  The crystals of
-// every leaf the walk reaches are tested by their geometry (crystal.rs:140-217) in the reference's
-// order, and each hit inside the step is absorbed at once (transport.rs:108-138): Beer-Lambert,
-// Bernoulli rounding of 5 E p s latent photons, E *= max(1 - 0.9 p, 0.05); the n-th absorbing hit
-// of the bounce draws word n % 4 of Philox block n / 4.
-__device__ __forceinline__ bool photon_bounce(const TileDesc& t, Photon& ph, uint32_t* err, uint32_t& nhit,
-                                              unsigned amask = 0) {
-  const float PI2 = 6.283185307179586f;
-  nhit = 0;
-  if (ph.b >= t.max_bounces) return false;
+// One lane's bounce in progress (transport.rs:101-185): its segment, the packet's absorption so
+// far and its walk of the tile's reference tree (the walk stack is the caller's).
+//
+// The walk follows the reference's order (BVH::intersect_ray_all, bvh.rs:300-347: push left then
+// right, pop right first) over the four-wide records (fg_rtree.cuh), whose children are stored in
+// that visiting order: the first hit child is entered, the other hit children are pushed so that
+// they come off the stack in order.  An internal child is entered when its (extended) box meets
+// [0, tlim] of the ray (the step, padded); a leaf child when its box extended by `reach` meets
+// [0, tlim] (a crystal hit inside the step lies there) and its own box meets the whole ray (the
+// reference's leaf test, bvh.rs:96-124).  Leaves are queued in walk order and tested later, so
+// that a warp's lanes test leaves together (deferred, speculative traversal): a lane walks on
+// while its queue has room.
+struct Bounce {
+  float3 inv, oi;     // 1 / dir (slab_inv) and pos * inv, for the slab tests
+  float step, tlim;   // the step and the walk's reach along the ray
+  float E;            // packet energy, as the hits absorb it
+  uint32_t nh;        // absorbing hits so far
+  P4 r;               // the Philox block of hits nh & ~3 .. (nh & ~3) + 3
+  int cur, sp;        // current record (~leaf for a leaf child, WALK_EMPTY when done) and stack depth
+  uint32_t lv[WALK_LEAVES];  // leaves reached and not yet tested, in walk order
+};
+
+// Starts bounce ph.b (transport.rs:101-107): the free path, the segment's step and the walk from
+// the root record.
+__device__ __forceinline__ void bounce_begin(const TileDesc& t, Photon& ph, Bounce& w) {
   const uint32_t b = ph.b++;
   const P4 rb = philox(ph.id, b, 0, TAG_BOUNCE, t.k0, t.k1);
   const float fp = t.mu_t > 0.0f ? -__logf(fmaxf(1.0f - uf(rb.x), 1.17549435e-38f)) / t.mu_t : 1e6f;
-  const float step = fminf(fp, t.D * 1.5f);
-  const float3 pos = ph.pos, dir = ph.dir;
-  const float3 inv = make_float3(slab_inv(dir.x), slab_inv(dir.y), slab_inv(dir.z));
-  float E = ph.E;
-  uint32_t nh = 0;
-  P4 r{};
-  auto leaf = [&](uint32_t id) {
-    const uint2 L = __ldg(&t.rleaf[id]);
-    if (!index_ok(L.x + L.y <= t.n, err, SITE_LEAF, L.x, L.y)) return;
-    for (uint32_t k = 0; k < L.y; ++k) {
-      const uint32_t s = __ldg(&t.ridx[L.x + k]);
-      if (!index_ok(s < t.n, err, SITE_LEAF, s, t.n)) continue;
-      const float4 a = __ldg(&t.a[s]), d = __ldg(&t.d[s]);
-      // The crystal lies in the ball of radius sqrt(3) m (a cube) or m (the ellipsoid shapes)
-      // around its centre; a ball the step's segment misses, with a margin well above FP32
-      // rounding, cannot give a hit inside the step, so the geometry test is skipped (the hits
-      // and their order are those of testing every crystal).
-      {
-        const float m = fmaxf(fmaxf(d.x, d.y), d.z);
-        const float R = (morph_of(d) == 0 ? 1.7320509f * m : m) * 1.001f + 1e-3f;
-        const float wx = a.x - pos.x, wy = a.y - pos.y, wz = a.z - pos.z;
-        const float tc = fminf(fmaxf(wx * dir.x + wy * dir.y + wz * dir.z, 0.0f), step);
-        const float ex = wx - tc * dir.x, ey = wy - tc * dir.y, ez = wz - tc * dir.z;
-        if (ex * ex + ey * ey + ez * ez > R * R) continue;
+  w.step = fminf(fp, t.D * 1.5f);
+  w.inv = make_float3(slab_inv(ph.dir.x), slab_inv(ph.dir.y), slab_inv(ph.dir.z));
+  w.oi = make_float3(ph.pos.x * w.inv.x, ph.pos.y * w.inv.y, ph.pos.z * w.inv.z);
+  w.tlim = w.step * 1.00001f + 1e-3f;
+  w.E = ph.E;
+  w.nh = 0;
+  w.r = P4{};
+  w.cur = 0;  // record 0: the root's
+  w.sp = 0;
+#pragma unroll
+  for (int j = 0; j < WALK_LEAVES; ++j) w.lv[j] = WALK_NONE;
+}
+
+// One step of the walk: queue the leaf child taken last, or test the current record's four
+// children (enter the first hit, push the later ones).  Only for a lane whose walk goes on
+// (cur != WALK_EMPTY) and whose leaf queue has room.
+__device__ __forceinline__ void walk_step(const TileDesc& t, Bounce& w, int* stack, uint32_t* err) {
+  if (w.cur < 0) {
+    const uint32_t lf = static_cast<uint32_t>(~w.cur);
+    bool placed = false;
+#pragma unroll
+    for (int j = 0; j < WALK_LEAVES; ++j) {
+      if (!placed && w.lv[j] == WALK_NONE) {
+        w.lv[j] = lf;
+        placed = true;
       }
-      const float4 q = __ldg(&t.q[s]);
-      float t0, t1;
-      if (!fintersect(a, q, d, 1.0f, pos, dir, t0, t1)) continue;
-      if (!(t0 < step)) continue;
-      const float path = fmaxf(fminf(t1, step) - t0, 0.0f);
-      if (!(path > 0.0f)) continue;
-      if ((nh & 3) == 0) r = philox(ph.id, b, nh >> 2, TAG_HIT, t.k0, t.k1);
-      // 1 - exp(-alpha L) without the cancellation of a short chord (corner hits are common).
-      const float p = -expm1f(-t.alpha * path);
-      const float expected = E * p * a.w * 5.0f;
-      const float fl = floorf(expected);
-      const uint32_t cnt = static_cast<uint32_t>(fl) + (uf(word(r, nh & 3)) < expected - fl ? 1u : 0u);
-      if (cnt) add_counts(t.counts, s, cnt);
-      E *= fmaxf(1.0f - p * 0.9f, 0.05f);
-      ++nh;
     }
+    w.cur = w.sp > 0 ? stack[--w.sp] : WALK_EMPTY;
+    return;
+  }
+  if (!index_ok(static_cast<uint32_t>(w.cur) < t.nrec, err, SITE_NODE, static_cast<uint32_t>(w.cur), t.nrec)) {
+    w.cur = WALK_EMPTY;
+    return;
+  }
+  const Node4* nd = t.rnode + w.cur;
+  const float4 lx = __ldg(&nd->lox), ly = __ldg(&nd->loy), lz = __ldg(&nd->loz);
+  const float4 hx = __ldg(&nd->hix), hy = __ldg(&nd->hiy), hz = __ldg(&nd->hiz);
+  const int4 rf = __ldg(&nd->ref);
+  const float3 inv = w.inv, oi = w.oi;
+  const float tlim = w.tlim, reach = t.reach;
+  // Slab test as lo * inv - o * inv (one FMA per plane), the box grown by g, clipped to [0, tm].
+  auto slab_hit = [&](float a0, float a1, float a2, float a3, float a4, float a5, float g, float tm) {
+    const float t1x = fmaf(a0 - g, inv.x, -oi.x), t2x = fmaf(a3 + g, inv.x, -oi.x);
+    const float t1y = fmaf(a1 - g, inv.y, -oi.y), t2y = fmaf(a4 + g, inv.y, -oi.y);
+    const float t1z = fmaf(a2 - g, inv.z, -oi.z), t2z = fmaf(a5 + g, inv.z, -oi.z);
+    const float te = fmaxf(fmaxf(fminf(t1x, t2x), fminf(t1y, t2y)), fmaxf(fminf(t1z, t2z), 0.0f));
+    const float tx = fminf(fminf(fmaxf(t1x, t2x), fmaxf(t1y, t2y)), fminf(fmaxf(t1z, t2z), tm));
+    return te <= tx;
   };
-  rt_walk_deferred(t.rnode, pos, inv, step * 1.00001f + 1e-3f, t.reach, err, leaf, t.nrec, t.nnodes,
-                   amask ? amask : (1u << (threadIdx.x & 31)));
-  nhit = nh;
+  auto hit = [&](int ref, float a0, float a1, float a2, float a3, float a4, float a5) {
+    if (ref == WALK_EMPTY) return false;
+    if (ref >= 0) return slab_hit(a0, a1, a2, a3, a4, a5, 0.0f, tlim);
+    return slab_hit(a0, a1, a2, a3, a4, a5, reach, tlim) && slab_hit(a0, a1, a2, a3, a4, a5, 0.0f, INFINITY);
+  };
+  const bool h0 = hit(rf.x, lx.x, ly.x, lz.x, hx.x, hy.x, hz.x);
+  const bool h1 = hit(rf.y, lx.y, ly.y, lz.y, hx.y, hy.y, hz.y);
+  const bool h2 = hit(rf.z, lx.z, ly.z, lz.z, hx.z, hy.z, hz.z);
+  const bool h3 = hit(rf.w, lx.w, ly.w, lz.w, hx.w, hy.w, hz.w);
+  // Enter the first hit child; push the later ones, last first.
+  int next = WALK_EMPTY;
+  auto take = [&](bool h, int r) {
+    if (!h) return;
+    if (next != WALK_EMPTY) {
+      if (w.sp < RT_STACK4) {
+        stack[w.sp++] = next;
+      } else {
+        atomicOr(err, ERR_STACK_OVERFLOW);
+      }
+    }
+    next = r;
+  };
+  take(h3, rf.w);
+  take(h2, rf.z);
+  take(h1, rf.y);
+  take(h0, rf.x);
+  w.cur = next != WALK_EMPTY ? next : (w.sp > 0 ? stack[--w.sp] : WALK_EMPTY);
+}
+
+// Tests the crystals of the lane's oldest queued leaf by their geometry (crystal.rs:140-217) in
+// the reference's order, and absorbs each hit inside the step at once (transport.rs:108-138):
+// Beer-Lambert, Bernoulli rounding of 5 E p s latent photons, E *= max(1 - 0.9 p, 0.05); the
+// n-th absorbing hit of the bounce draws word n % 4 of Philox block n / 4.
+__device__ __forceinline__ void leaf_step(const TileDesc& t, const Photon& ph, Bounce& w, uint32_t* err) {
+  const uint32_t id = w.lv[0];
+#pragma unroll
+  for (int j = 0; j + 1 < WALK_LEAVES; ++j) w.lv[j] = w.lv[j + 1];
+  w.lv[WALK_LEAVES - 1] = WALK_NONE;
+  if (!index_ok(id < t.nnodes, err, SITE_LEAF, id, t.nnodes)) return;
+  const uint2 L = __ldg(&t.rleaf[id]);
+  if (!index_ok(L.x + L.y <= t.n, err, SITE_LEAF, L.x, L.y)) return;
+  const float3 pos = ph.pos, dir = ph.dir;
+  const float step = w.step;
+  const uint32_t b = ph.b - 1;
+  for (uint32_t k = 0; k < L.y; ++k) {
+    const uint32_t s = __ldg(&t.ridx[L.x + k]);
+    if (!index_ok(s < t.n, err, SITE_LEAF, s, t.n)) continue;
+    const float4 a = __ldg(&t.a[s]), d = __ldg(&t.d[s]);
+    // The crystal lies in the ball of radius sqrt(3) m (a cube) or m (the ellipsoid shapes)
+    // around its centre; a ball the step's segment misses, with a margin well above FP32
+    // rounding, cannot give a hit inside the step, so the geometry test is skipped (the hits
+    // and their order are those of testing every crystal).
+    {
+      const float m = fmaxf(fmaxf(d.x, d.y), d.z);
+      const float R = (morph_of(d) == 0 ? 1.7320509f * m : m) * 1.001f + 1e-3f;
+      const float wx = a.x - pos.x, wy = a.y - pos.y, wz = a.z - pos.z;
+      const float tc = fminf(fmaxf(wx * dir.x + wy * dir.y + wz * dir.z, 0.0f), step);
+      const float ex = wx - tc * dir.x, ey = wy - tc * dir.y, ez = wz - tc * dir.z;
+      if (ex * ex + ey * ey + ez * ez > R * R) continue;
+    }
+    const float4 q = __ldg(&t.q[s]);
+    float t0, t1;
+    if (!fintersect(a, q, d, 1.0f, pos, dir, t0, t1)) continue;
+    if (!(t0 < step)) continue;
+    const float path = fmaxf(fminf(t1, step) - t0, 0.0f);
+    if (!(path > 0.0f)) continue;
+    if ((w.nh & 3) == 0) w.r = philox(ph.id, b, w.nh >> 2, TAG_HIT, t.k0, t.k1);
+    // 1 - exp(-alpha L) without the cancellation of a short chord (corner hits are common).
+    const float p = -expm1f(-t.alpha * path);
+    const float expected = w.E * p * a.w * 5.0f;
+    const float fl = floorf(expected);
+    const uint32_t cnt = static_cast<uint32_t>(fl) + (uf(word(w.r, w.nh & 3)) < expected - fl ? 1u : 0u);
+    if (cnt) add_counts(t.counts, s, cnt);
+    w.E *= fmaxf(1.0f - p * 0.9f, 0.05f);
+    ++w.nh;
+  }
+}
+
+// Ends the bounce whose walk is done (transport.rs:140-185): the move, the film's faces (escape,
+// or the anti-halation layer's reflection, optics.rs:150-196), Henyey-Greenstein scattering with
+// albedo and Russian roulette.  Returns whether the packet is still alive.
+__device__ __forceinline__ bool bounce_end(const TileDesc& t, Photon& ph, const Bounce& w) {
+  const float PI2 = 6.283185307179586f;
+  const uint32_t b = ph.b - 1;
+  const P4 rb = philox(ph.id, b, 0, TAG_BOUNCE, t.k0, t.k1);
+  const float3 pos = ph.pos, dir = ph.dir;
+  const float step = w.step;
+  float E = w.E;
   const float3 np = make_float3(pos.x + dir.x * step, pos.y + dir.y * step, pos.z + dir.z * step);
   if (np.x < 0.0f || np.x >= t.W || np.y < 0.0f || np.y >= t.H) return false;
   if (np.z <= 0.0f) return false;
