@@ -14,8 +14,9 @@
 // global levels: one thread block each builds their subtree with the elements in shared memory,
 // the same passes per level, all levels down to the leaves.  Centroid boxes are reduced
 // segment-wise (a node is a contiguous range of positions).  The node boxes (the union of the
-// elements' boxes, which the reference stores but never splits on) are formed bottom up once the
-// topology is final (k_rt_refit); min and max are exact, so the order does not matter.
+// elements' boxes, which the reference stores but never splits on) are formed bottom up: a block
+// forms those of its subtree after its last level, k_rt_refit those above the blocks' subtrees;
+// min and max are exact, so the order does not matter.
 //
 // The swap partition (bvh.rs:244-258: i from the left, j from the right; a small at i stays and i
 // advances, a big at i is swapped with j and j retreats) examines the range as two streams: the
@@ -111,6 +112,7 @@ __device__ __forceinline__ bool alloc_pair(const RtArgs& A, int t, uint32_t& l) 
 }
 
 constexpr uint32_t RT_NONE = 0xffffffffu;
+constexpr uint32_t RT_BOX_ONLY = 2;  // block-queue entry of a finished leaf: only its box is formed
 
 // Hands a new node of n elements (held in buffer `par`) to the phase that builds it: the global
 // levels (more than RT_CTA_MAX elements; its centroid accumulators start empty) or one block.
@@ -257,6 +259,9 @@ __global__ void k_rt_decide(RtArgs A, int c) {
     uint32_t l = 0;
     if (A.ncount[node] <= 4 || ext <= 1e-7 || !alloc_pair(A, t, l)) {
       A.nsplit[node] = -1;  // leaf (degenerate centroids, or no node capacity left)
+      const uint32_t q = atomicAdd(&A.cnt[2], 1u);  // a block forms its box
+      A.bq[q] = node;
+      A.bqpar[q] = RT_BOX_ONLY;
       continue;
     }
     A.nsplit[node] = axis;
@@ -463,6 +468,7 @@ constexpr int RT_LEAF_MAX = 4;                               // subdivide's leaf
 constexpr int RT_CTA_LV = RT_CTA_MAX / (RT_LEAF_MAX + 1);    // nodes of more than 4 per level (204)
 constexpr int RT_CTA_SL = 2 * RT_CTA_LV;                     // leaves of at most 4 made by one level
 constexpr uint8_t RT_CTA_FREE = 0xff;                        // position of a finished range
+constexpr int RT_CTA_LVMAX = RT_MAX_DEPTH + 1;               // levels of a job (deeper trees are rejected)
 static_assert(RT_CTA_LV < RT_CTA_FREE, "level slots must fit a byte");
 static_assert(RT_CTA_MAX <= 2048, "positions are packed in 11 bits");
 
@@ -494,7 +500,25 @@ struct RtCtaSmem {
   int8_t axis[RT_CTA_LV];
   int nl, nsl, nnext, nslnew;
   uint32_t maxdep;
+  int nint, nlvl;                         // internal nodes of the job so far, and levels
+  uint16_t lvend[RT_CTA_LVMAX];           // internal nodes listed after each level
 };
+
+// Folds the max_dim box of element slot `slot` into k (minima 0-2, maxima 3-5, ordered keys).
+__device__ __forceinline__ void rt_fold_box(const RTile& T, uint32_t slot, unsigned long long k[6]) {
+  double lo[3], hi[3], cc[3];
+  rt_box_pm(rt_pm(T, slot), lo, hi, cc);
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    k[m] = umin64(k[m], ord64(lo[m]));
+    k[3 + m] = umax64(k[3 + m], ord64(hi[m]));
+  }
+}
+
+__device__ __forceinline__ void rt_store_box(const RtArgs& A, uint32_t id, const unsigned long long k[6]) {
+#pragma unroll
+  for (int m = 0; m < 6; ++m) A.box64[6ull * id + m] = unord64(k[m]);
+}
 
 // Four blocks per SM (64 registers; the block's shared memory is about 53 KB): 9 % faster than two.
 __global__ void __launch_bounds__(RT_CTA_T, 4) k_rt_cta(RtArgs A) {
@@ -505,6 +529,24 @@ __global__ void __launch_bounds__(RT_CTA_T, 4) k_rt_cta(RtArgs A) {
   for (uint32_t q = blockIdx.x; q < nq; q += gridDim.x) {
     const uint32_t root = A.bq[q], par = A.bqpar[q];
     const uint32_t s = A.nstart[root];
+    if (par == RT_BOX_ONLY) {  // a leaf of the global levels: its box, from all its elements
+      const RTile& T = A.tiles[A.ntile[root]];
+      const uint32_t cn = A.ncount[root];
+      if (tid < 6) S.u.acc[0][tid] = tid < 3 ? ~0ull : 0ull;
+      __syncthreads();
+      unsigned long long k[6];
+      rt_keys_empty(k);
+      for (uint32_t j = tid; j < cn; j += RT_CTA_T) rt_fold_box(T, A.ridx[s + j], k);
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        atomicMin(&S.u.acc[0][m], k[m]);
+        atomicMax(&S.u.acc[0][3 + m], k[3 + m]);
+      }
+      __syncthreads();
+      if (tid == 0) rt_store_box(A, root, S.u.acc[0]);
+      __syncthreads();
+      continue;
+    }
     const int n = static_cast<int>(min(A.ncount[root], static_cast<uint32_t>(RT_CTA_MAX)));
     const uint32_t t = A.ntile[root];
     const unsigned long long nb = A.tiles[t].nbase;
@@ -522,6 +564,8 @@ __global__ void __launch_bounds__(RT_CTA_T, 4) k_rt_cta(RtArgs A) {
     }
     if (tid == 0) {
       S.maxdep = 0;
+      S.nint = 0;
+      S.nlvl = 0;
       if (n > RT_LEAF_MAX) {
         S.nl = 1;
         S.nsl = 0;
@@ -545,6 +589,10 @@ __global__ void __launch_bounds__(RT_CTA_T, 4) k_rt_cta(RtArgs A) {
         const uint32_t e = S.sl[i], id = S.slid[i];
         const int o0 = static_cast<int>(e & 2047u), cn = static_cast<int>((e >> 11) & 7u);
         const uint32_t dp = e >> 14;
+        unsigned long long k[6];
+        rt_keys_empty(k);
+        for (int j = 0; j < cn; ++j) rt_fold_box(A.tiles[t], S.idx[o0 + j], k);
+        rt_store_box(A, id, k);
         A.nstart[id] = s + static_cast<uint32_t>(o0);
         A.ncount[id] = static_cast<uint32_t>(cn);
         A.ntile[id] = t;
@@ -599,7 +647,12 @@ __global__ void __launch_bounds__(RT_CTA_T, 4) k_rt_cta(RtArgs A) {
         if (cn <= RT_LEAF_MAX || ext <= 1e-7 || !alloc_pair(A, static_cast<int>(t), l)) {
           S.axis[i] = -1;  // leaf (degenerate centroids, or no node capacity left)
           A.nsplit[id] = -1;
+          unsigned long long k[6];
+          rt_keys_empty(k);
+          for (int j = 0; j < cn; ++j) rt_fold_box(A.tiles[t], S.idx[S.off[cur][i] + j], k);
+          rt_store_box(A, id, k);
         } else {
+          A.P[s + static_cast<uint32_t>(atomicAdd(&S.nint, 1))] = id;  // its box after the last level
           const double ca = axis == 0 ? clo[0] : (axis == 1 ? clo[1] : clo[2]);
           const double cb = axis == 0 ? chi[0] : (axis == 1 ? chi[1] : chi[2]);
           const double mid = __dmul_rn(0.5, __dadd_rn(ca, cb));
@@ -614,6 +667,10 @@ __global__ void __launch_bounds__(RT_CTA_T, 4) k_rt_cta(RtArgs A) {
         }
       }
       __syncthreads();
+      if (tid == 0) {
+        if (S.nlvl < RT_CTA_LVMAX) S.lvend[S.nlvl++] = static_cast<uint16_t>(S.nint);
+        else atomicOr(A.err, ERR_STACK_OVERFLOW);  // deeper than the depth check allows
+      }
       // Flags and their exclusive prefix sum: thread tid owns positions RT_CTA_PER * tid + k.
       {
         uint32_t f[RT_CTA_PER], sum = 0;
@@ -736,51 +793,45 @@ __global__ void __launch_bounds__(RT_CTA_T, 4) k_rt_cta(RtArgs A) {
       cur ^= 1;
       __syncthreads();
     }
+    // The internal nodes' boxes, deepest level first: each the union of its children's, written
+    // by this block before the barrier (leaves at their creation, internal nodes a level below).
+    for (int L = S.nlvl - 1; L >= 0; --L) {
+      const int b0 = L ? S.lvend[L - 1] : 0, b1 = S.lvend[L];
+      for (int k = b0 + tid; k < b1; k += RT_CTA_T) {
+        const uint32_t id = A.P[s + static_cast<uint32_t>(k)];
+        const int2 ch = A.nchild[id];
+        const double* a = A.box64 + 6ull * static_cast<unsigned long long>(ch.x);
+        const double* b = A.box64 + 6ull * static_cast<unsigned long long>(ch.y);
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+          A.box64[6ull * id + m] = unord64(umin64(ord64(a[m]), ord64(b[m])));
+          A.box64[6ull * id + 3 + m] = unord64(umax64(ord64(a[3 + m]), ord64(b[3 + m])));
+        }
+      }
+      __syncthreads();
+    }
     for (int x = tid; x < n; x += RT_CTA_T) A.ridx[s + x] = S.idx[x];
     if (tid == 0) atomicMax(&A.tiles[t].depth, S.maxdep);
     __syncthreads();
   }
 }
 
-// Node boxes (the BVHNode aabb: the union of the node's elements' max_dim boxes, bvh.rs:196-204),
-// bottom up over the final topology, one thread per node: a leaf forms its box from its elements
-// (in the order-preserving key domain, as a union of the elements' boxes compares them), then
-// climbs: at each parent the first child to arrive stops and the second forms the parent's box as
-// the union of both children's.  Boxes are published with a fence before the arrival count and
-// read through L2.  `arrive` holds one zeroed counter per node.
+// Node boxes above the blocks' subtrees (the BVHNode aabb: the union of the node's elements'
+// max_dim boxes, bvh.rs:196-204).  Every block-queue entry (a subtree's root, or a leaf of the
+// global levels) has its box; one thread per entry climbs: at each parent the first child to
+// arrive stops and the second forms the parent's box as the union of both children's.  Boxes are
+// published with a fence before the arrival count and read through L2.  `arrive` holds one zeroed
+// counter per node.
 __global__ void k_rt_refit(RtArgs A, uint32_t* arrive) {
-  const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
-  for (unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; g < A.N;
-       g += stride) {
-    int lo_ = 0, hi_ = A.ntiles - 1;
-    while (lo_ < hi_) {
-      const int mid = (lo_ + hi_ + 1) >> 1;
-      if (A.tiles[mid].nbase <= g) lo_ = mid; else hi_ = mid - 1;
-    }
-    const RTile& T = A.tiles[lo_];
-    const uint32_t id = static_cast<uint32_t>(g - T.nbase);
-    if (id == 0 || id >= min(T.nodes, T.ncap) || (id == 1 && T.n == 0) || A.nsplit[g] >= 0) continue;
-    const uint32_t st = A.nstart[g], cn = A.ncount[g];
-    if (st < T.ebase || st - T.ebase + static_cast<unsigned long long>(cn) > T.n) {
+  const uint32_t nq = A.cnt[2];
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+    unsigned long long node = A.bq[q];
+    if (node >= A.N) {
       atomicOr(A.err, ERR_BAD_INDEX);
       continue;
     }
-    unsigned long long k[6];
-    rt_keys_empty(k);
-    for (uint32_t j = 0; j < cn; ++j) {
-      const uint32_t slot = A.ridx[st + j];  // a slot k_rt_init read the keys of
-      double lo[3], hi[3], cc[3];
-      rt_box_pm(rt_pm(T, slot), lo, hi, cc);
-#pragma unroll
-      for (int m = 0; m < 3; ++m) {
-        k[m] = umin64(k[m], ord64(lo[m]));
-        k[3 + m] = umax64(k[3 + m], ord64(hi[m]));
-      }
-    }
-#pragma unroll
-    for (int m = 0; m < 6; ++m) A.box64[6ull * g + m] = unord64(k[m]);
+    const RTile& T = A.tiles[A.ntile[node]];
     const unsigned long long nlo = T.nbase, nhi = T.nbase + T.ncap;
-    unsigned long long node = g;
     for (int up = 0; up <= RT_MAX_DEPTH; ++up) {
       const uint32_t p = A.parent[node];
       if (p == RT_NONE) break;
