@@ -627,21 +627,39 @@ __device__ __forceinline__ void emit_crystal(const SynthTile& t, const uint32_t*
 
 // The crystals of each brick in slot order (slot_cell): the brick's slots are walked in chunks of
 // the block, a block-wide prefix sum of the occupied ones numbers them after the points of the
-// earlier bricks (scan: exclusive sum of k_brick_count).  blockIdx.y is the tile.
-__global__ void k_emit(const SynthTile* __restrict__ tiles, const uint32_t* __restrict__ cells,
-                       const uint32_t* __restrict__ scan, float4* A, float4* Q, float4* D, uint64_t* keys,
-                       uint32_t* err) {
+// earlier bricks (scan: exclusive sum of k_brick_count).  About one cell in nine holds a point,
+// so the numbered crystals are queued in shared memory and made once the queue holds a block's
+// worth, with every lane busy.  blockIdx.y is the tile.
+constexpr int EMIT_T = 256;
+__global__ void __launch_bounds__(EMIT_T) k_emit(const SynthTile* __restrict__ tiles,
+                                                 const uint32_t* __restrict__ cells,
+                                                 const uint32_t* __restrict__ scan, float4* A, float4* Q,
+                                                 float4* D, uint64_t* keys, uint32_t* err) {
   const SynthTile& t = tiles[blockIdx.y];
   const uint32_t L = t.brick_bits;
   const uint32_t nbricks = 1u << (2 * t.slot_bits), per = 1u << (3 * L);
-  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) / 32;
-  __shared__ uint32_t s_w[33];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr uint32_t NW = EMIT_T / 32;
+  __shared__ uint32_t s_w[NW + 1];
+  __shared__ uint32_t s_k[2 * EMIT_T], s_sl[2 * EMIT_T];  // queued crystals: number and slot
+  uint32_t fill = 0;                                      // queue length (the same in every thread)
+  auto drain = [&]() {
+    for (uint32_t i = threadIdx.x; i < fill; i += EMIT_T) {
+      const uint32_t sl = s_sl[i], k = s_k[i];
+      if (k >= t.ccap) continue;  // past the tile's capacity (flagged when queued)
+      uint32_t x, y, z;
+      slot_cell(t, sl, x, y, z);
+      emit_crystal(t, cells, sl, x, y, z, k, A, Q, D, keys);
+    }
+    fill = 0;
+    __syncthreads();
+  };
   for (uint32_t b = blockIdx.x; b < nbricks; b += gridDim.x) {
     const unsigned long long bi = t.slot_base + b;
     if (scan[bi + 1] == scan[bi]) continue;  // block-uniform
     uint32_t k0 = scan[bi] - scan[t.slot_base];
     const uint32_t xb = morton2_compact(b) << L, yb = morton2_compact(b >> 1) << L;
-    for (uint32_t c0 = 0; c0 < per; c0 += blockDim.x) {
+    for (uint32_t c0 = 0; c0 < per; c0 += EMIT_T) {
       const uint32_t lo = c0 + threadIdx.x;
       const uint32_t x = xb | morton3_compact(lo), y = yb | morton3_compact(lo >> 1), z = morton3_compact(lo >> 2);
       const bool occ = lo < per && x < t.gw && y < t.gh && z < t.gd &&
@@ -651,23 +669,29 @@ __global__ void k_emit(const SynthTile* __restrict__ tiles, const uint32_t* __re
       __syncthreads();
       if (threadIdx.x == 0) {
         uint32_t acc = 0;
-        for (uint32_t w = 0; w < nw; ++w) {
+        for (uint32_t w = 0; w < NW; ++w) {
           const uint32_t v = s_w[w];
           s_w[w] = acc;
           acc += v;
         }
-        s_w[32] = acc;
+        s_w[NW] = acc;
       }
       __syncthreads();
       if (occ) {
-        const uint32_t k = k0 + s_w[warp] + __popc(m & ((1u << lane) - 1u));
-        if (k < t.ccap) emit_crystal(t, cells, (b << (3 * L)) | lo, x, y, z, k, A, Q, D, keys);
-        else atomicOr(err, ERR_LIST_OVERFLOW);
+        const uint32_t r = s_w[warp] + __popc(m & ((1u << lane) - 1u));
+        const uint32_t k = k0 + r;
+        if (k >= t.ccap) atomicOr(err, ERR_LIST_OVERFLOW);
+        s_k[fill + r] = k;
+        s_sl[fill + r] = (b << (3 * L)) | lo;
       }
-      k0 += s_w[32];
+      const uint32_t got = s_w[NW];
+      k0 += got;
+      fill += got;
       __syncthreads();
+      if (fill >= EMIT_T) drain();
     }
   }
+  drain();
 }
 
 }  // namespace fg
@@ -716,7 +740,7 @@ void launch_emit(const SynthTile* tiles, int ntiles, unsigned long long max_bric
   if (ntiles == 0) return;
   FG_REQUIRE(ntiles <= 65535, "too many tiles for one launch");
   const unsigned bb = static_cast<unsigned>(std::min<unsigned long long>(std::max(max_bricks, 1ull), 4096));
-  k_emit<<<dim3(bb, ntiles), 256, 0, st>>>(tiles, cells, scan, A, Q, D, keys, err);
+  k_emit<<<dim3(bb, ntiles), EMIT_T, 0, st>>>(tiles, cells, scan, A, Q, D, keys, err);
   FG_CUDA(cudaGetLastError());
 }
 
