@@ -103,26 +103,21 @@ __global__ void k_scan_tree_tiles(const BTile* bt, int ntiles, const uint32_t* d
 
 // ---- development (development.rs:59-188), batched; see fg_develop.cu for the reasoning ----
 
-__global__ void k_maxdim_b(BTile* bt, int ntiles, unsigned long long ncap, const float4* __restrict__ D) {
-  const unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
-  int tile = -1;
+// Largest max_dim of each tile's crystals (the reach of the development's proximity search):
+// blockIdx.y is the tile, its blocks stride over the tile's crystals; a warp maximum, then one
+// atomic per warp (positive doubles order as their bit patterns).
+__global__ void k_maxdim_b(BTile* bt, const float4* __restrict__ D) {
+  BTile& T = bt[blockIdx.y];
+  const uint32_t n = T.n;
   float m = 0.0f;
-  if (g < ncap) {
-    tile = btile_of(bt, ntiles, g);
-    if (g - bt[tile].cbase < bt[tile].n) {
-      const float4 d = D[g];
-      m = fmaxf(fmaxf(d.x, d.y), d.z);
-    } else {
-      tile = -1;
-    }
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 d = D[T.cbase + i];
+    m = fmaxf(m, fmaxf(fmaxf(d.x, d.y), d.z));
   }
-  const unsigned act = __activemask();
-  const unsigned grp = __match_any_sync(act, tile);
-  float mm = m;
-  for (unsigned k = grp; k; k &= k - 1) mm = fmaxf(mm, __shfl_sync(grp, m, __ffs(k) - 1));
-  if (tile >= 0 && (threadIdx.x & 31) == static_cast<unsigned>(__ffs(grp) - 1))
-    atomicMax(reinterpret_cast<unsigned long long*>(&bt[tile].max_base),
-              static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(mm))));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.0f)
+    atomicMax(reinterpret_cast<unsigned long long*>(&T.max_base),
+              static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(m))));
 }
 
 __global__ void k_threshold_b(const BTile* __restrict__ bt, int ntiles, unsigned long long ncap,
@@ -585,7 +580,13 @@ static void stage_develop(fg_batch* B, cudaStream_t st) {
   const int nt = static_cast<int>(B->ntiles);
   fg_engine* e = B->e;
   const unsigned G = grid_for(B->ncap, 256);
-  k_maxdim_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->D.p);
+  {
+    uint32_t cmax = 1;  // the largest tile's crystal capacity
+    for (int i = 0; i < nt; ++i) cmax = std::max(cmax, B->syn[i].ccap);
+    const unsigned bx = std::min(std::max((cmax + 2047u) / 2048u, 1u), 2048u);
+    FG_REQUIRE(nt <= 65535, "too many tiles for one launch");
+    k_maxdim_b<<<dim3(bx, static_cast<unsigned>(nt)), 256, 0, st>>>(B->d_bt.p, B->D.p);
+  }
   k_threshold_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->counts.p, B->developed.p, B->parent.p, B->devflag.p);
   FG_CUDA(cudaMemsetAsync(B->devflag.p + B->ncap, 0, sizeof(uint32_t), st));
   cub_scan(B, B->devflag.p, B->devscan.p, B->ncap + 1, st);

@@ -524,17 +524,46 @@ __global__ void __launch_bounds__(SYN_WARPS * 32, 8) k_bridson(const SynthTile* 
   }
 }
 
-// Independent deletion down to the Bridson-expected count.
-// blockIdx.y is the tile (the points per tile were counted by k_bridson).
-__global__ void k_thin(const SynthTile* __restrict__ tiles, uint32_t* __restrict__ cells, const uint32_t* npts) {
+// Independent deletion down to the Bridson-expected count: each point goes with probability p,
+// drawn from the Philox block of its cell.  blockIdx.y is the tile (the points per tile were
+// counted by k_bridson).  Each warp reads 32 cells at a time and queues the occupied ones; the
+// draws run once 32 are queued, with every lane busy.
+constexpr int THIN_T = 256;
+__global__ void __launch_bounds__(THIN_T) k_thin(const SynthTile* __restrict__ tiles, uint32_t* __restrict__ cells,
+                                                 const uint32_t* npts) {
   const SynthTile& t = tiles[blockIdx.y];
   const uint32_t n = npts[blockIdx.y];
   if (n <= t.target) return;
   const float p = 1.0f - static_cast<float>(t.target) / static_cast<float>(n);
   const uint32_t nc = t.gw * t.gh * t.gd;
   uint32_t* tc = cells + t.cell_base;
-  for (uint32_t lin = blockIdx.x * blockDim.x + threadIdx.x; lin < nc; lin += gridDim.x * blockDim.x)
-    if ((tc[lin] & OCC) && uf(philox(lin, 0, 0, TAG_THIN, t.k0, t.k1).x) < p) tc[lin] = 0;
+  const uint32_t lane = threadIdx.x & 31, lt = (1u << lane) - 1u;
+  __shared__ uint32_t s_q[THIN_T / 32][64];
+  uint32_t* q = s_q[threadIdx.x >> 5];
+  uint32_t fill = 0;  // the same in every lane of the warp
+  auto thin = [&](uint32_t lin) {
+    if (uf(philox(lin, 0, 0, TAG_THIN, t.k0, t.k1).x) < p) tc[lin] = 0;
+  };
+  const uint32_t warps = gridDim.x * (THIN_T / 32);
+  for (uint32_t base = (blockIdx.x * THIN_T + threadIdx.x - lane); base < nc; base += warps * 32) {
+    const uint32_t lin = base + lane;
+    const bool occ = lin < nc && (tc[lin] & OCC);
+    const unsigned m = __ballot_sync(0xffffffffu, occ);
+    if (occ) q[fill + __popc(m & lt)] = lin;
+    fill += __popc(m);
+    __syncwarp();
+    if (fill >= 32) {
+      const uint32_t mine = q[lane];
+      const uint32_t rest = fill - 32;
+      const uint32_t moved = lane < rest ? q[32 + lane] : 0u;
+      __syncwarp();
+      if (lane < rest) q[lane] = moved;
+      fill = rest;
+      __syncwarp();
+      thin(mine);
+    }
+  }
+  if (lane < fill) thin(q[lane]);
 }
 
 // Cell of compaction slot sl: the brick (2D Morton over the high x, y bits) in the bits above
@@ -729,7 +758,7 @@ void launch_synth_post(const SynthTile* tiles, int ntiles, unsigned long long ma
   FG_REQUIRE(ntiles <= 65535, "too many tiles for one launch");
   const unsigned bc = static_cast<unsigned>(std::min<unsigned long long>(std::max(grid_for(max_cells, 256), 1u), 1024));
   const unsigned bb = static_cast<unsigned>(std::min<unsigned long long>(std::max(max_bricks, 1ull), 4096));
-  k_thin<<<dim3(bc, ntiles), 256, 0, st>>>(tiles, cells, npts);
+  k_thin<<<dim3(bc, ntiles), THIN_T, 0, st>>>(tiles, cells, npts);
   k_brick_count<<<dim3(bb, ntiles), 256, 0, st>>>(tiles, cells, counts);
   FG_CUDA(cudaGetLastError());
 }

@@ -487,7 +487,7 @@ typedef struct fg_device_crystals {
  * more than FG_STATIC_SCAN_MAX_BINS bins or FG_STATIC_SCAN_MAX_ITEMS entries, fail with
  * FG_ERR_INVALID_ARG before any output is written.  On failure a message is copied to `message` (message_len bytes,
  * may be NULL).  The first call on a device looks up the scratch's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.  Every call on a device
+ * (cudaGetSymbolAddress).  Every call on a device
  * shares the scratch, which keeps the last call's contents; each call clears what must start at
  * zero.  Calls whose GPU work overlapped would race on the scratch and give wrong images, so the
  * library serialises them: a call holds a per-device lock until its GPU work has finished (also
