@@ -192,9 +192,27 @@ __device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsig
 // contiguous runs (a node is a contiguous range of positions, so equal values at two lanes mean
 // the same node in between).  On return the first lane of each run holds the run's minima
 // (k[0..2]) and maxima (k[3..5]); the return value says whether this lane is a run's first.
-// Lanes without a node pass a seg value no other lane has.
+// Lanes without a node pass a seg value no other lane has.  All 32 lanes call it.
 __device__ __forceinline__ bool rt_seg_reduce(uint32_t seg, unsigned long long k[6]) {
   const int lane = threadIdx.x & 31;
+  if (__all_sync(0xffffffffu, __shfl_sync(0xffffffffu, seg, 0) == seg)) {
+    // One node across the warp (the common case): each 64-bit minimum or maximum as two 32-bit
+    // warp reductions, the high words, then the low words of the lanes holding that high word.
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      const uint32_t hi = static_cast<uint32_t>(k[i] >> 32), lo = static_cast<uint32_t>(k[i]);
+      uint32_t h, l;
+      if (i < 3) {
+        h = __reduce_min_sync(0xffffffffu, hi);
+        l = __reduce_min_sync(0xffffffffu, hi == h ? lo : 0xffffffffu);
+      } else {
+        h = __reduce_max_sync(0xffffffffu, hi);
+        l = __reduce_max_sync(0xffffffffu, hi == h ? lo : 0u);
+      }
+      k[i] = (static_cast<unsigned long long>(h) << 32) | l;
+    }
+    return lane == 0;
+  }
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
     const uint32_t ns = __shfl_down_sync(0xffffffffu, seg, o);
