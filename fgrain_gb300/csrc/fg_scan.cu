@@ -255,16 +255,23 @@ void launch_scan_prep(const ScanTile* tiles, int ntiles, unsigned long long nslo
 __device__ __forceinline__ bool scan_pair(const ScanTile& t, const ScanSmem& sm, uint32_t c, float oxh, float oxl,
                                           float oyh, float oyl, uint32_t px, uint32_t py, uint32_t sx, uint32_t sy,
                                           float& chord, uint32_t& nfb) {
+  const float m = sm.m[c], delta = sm.delta[c];
+  const int kind = sm.kind[c];
+  // Geometry reach: a cube lies within sqrt(3) m of its centre, an ellipsoid within its own box.
+  const float reach = (kind == K_ELLIPSOID ? m : 1.7320509f * m) * 1.00001f + 1e-9f;
+  {
+    // Quick rejection on the high words alone: they differ from the float pairs by a few units in
+    // the last place, far inside the slack, so a pair rejected here fails the exact test below.
+    const float cxh = sm.cxh[c], cyh = sm.cyh[c];
+    const float slack = 1e-4f + 4.8e-7f * (fabsf(oxh) + fabsf(cxh) + fabsf(oyh) + fabsf(cyh));
+    if (fabsf(oxh - cxh) > reach + slack || fabsf(oyh - cyh) > reach + slack) return false;
+  }
   // Ray minus crystal centre, x and y, as float pairs.
   float dh, dl, dx, dxl, dy, dyl;
   two_sum(oxh, -sm.cxh[c], dh, dl);
   fast_two_sum(dh, dl + (oxl - sm.cxl[c]), dx, dxl);
   two_sum(oyh, -sm.cyh[c], dh, dl);
   fast_two_sum(dh, dl + (oyl - sm.cyl[c]), dy, dyl);
-  const float m = sm.m[c], delta = sm.delta[c];
-  const int kind = sm.kind[c];
-  // Geometry reach: a cube lies within sqrt(3) m of its centre, an ellipsoid within its own box.
-  const float reach = (kind == K_ELLIPSOID ? m : 1.7320509f * m) * 1.00001f + 1e-9f;
   if (fabsf(dx) > reach || fabsf(dy) > reach) return false;
   // The leaf box (strict containment in x and y; the origin lies above every box in z): margins
   // of float-pair differences, exact to ~1e-12 um.
