@@ -101,6 +101,24 @@ __global__ void k_scan_tree_tiles(const BTile* bt, int ntiles, const uint32_t* d
   rt[t].n = last - first;
 }
 
+// Crystal records of every tile in its tree's element order (TileDesc): position p of tile t holds
+// the crystal ridx[p] of that tile, so a leaf's crystals lie next to each other.
+__global__ void k_element_records_b(const BTile* __restrict__ bt, int ntiles, unsigned long long ncap,
+                                    const uint32_t* __restrict__ ridx, const float4* __restrict__ A,
+                                    const float4* __restrict__ Q, const float4* __restrict__ D, float4* EA,
+                                    float4* EQ, float4* ED, uint32_t* err) {
+  const unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+  if (g >= ncap) return;
+  const BTile& t = bt[btile_of(bt, ntiles, g)];
+  const unsigned long long p = g - t.cbase;
+  if (p >= t.n) return;
+  const uint32_t s = ridx[g];
+  if (!index_ok(s < t.n, err, SITE_LEAF, s, t.n)) return;
+  EA[g] = A[t.cbase + s];
+  EQ[g] = Q[t.cbase + s];
+  ED[g] = D[t.cbase + s];
+}
+
 // ---- development (development.rs:59-188), batched; see fg_develop.cu for the reasoning ----
 
 // Largest max_dim of each tile's crystals (the reach of the development's proximity search):
@@ -322,6 +340,7 @@ struct fg_batch {
   bool wait_probe = false;
   unsigned long long maxcells = 0, maxslots = 0;  // the largest tile's cells and bricks
   DBuf<float4> A, Q, D;
+  DBuf<float4> EA, EQ, ED;  // A, Q, D in the transport tree's element order (TileDesc)
   DBuf<uint64_t> keys;
   RTreeBufs rt;             // the reference tree of every tile: over its crystals, then its developed ones
   DBuf<RTile> rt_scan;      // the tree tiles of the scan's build (developed crystals, their expansion)
@@ -487,9 +506,9 @@ static void upload_descriptors(fg_batch* B, cudaStream_t st) {
   for (uint32_t i = 0; i < B->ntiles; ++i) {
     const unsigned long long cb = B->syn[i].cbase;
     TileDesc& t = B->td[i];
-    t.a = B->A.p + cb;
-    t.q = B->Q.p + cb;
-    t.d = B->D.p + cb;
+    t.a = B->EA.p + cb;
+    t.q = B->EQ.p + cb;
+    t.d = B->ED.p + cb;
     const unsigned long long nb = B->bt[i].nbase;
     t.rnode = B->rt.rnode.p + B->bt[i].rbase;
     t.rleaf = B->rt.rleaf.p + nb;
@@ -557,7 +576,13 @@ static void stage_synth(fg_batch* B, cudaStream_t st, bool capturing = false) {
 
 // The reference tree of every tile over its crystals (in slot order), for the transport and the
 // development's touch queries.
-static void stage_bvh(fg_batch* B, cudaStream_t st) { rtree_build(B->rt, B->e->d_err, st); }
+static void stage_bvh(fg_batch* B, cudaStream_t st) {
+  rtree_build(B->rt, B->e->d_err, st);
+  k_element_records_b<<<grid_for(B->ncap, 256), 256, 0, st>>>(B->d_bt.p, static_cast<int>(B->ntiles), B->ncap,
+                                                              B->rt.ridx.p, B->A.p, B->Q.p, B->D.p, B->EA.p,
+                                                              B->EQ.p, B->ED.p, B->e->d_err);
+  FG_CUDA(cudaGetLastError());
+}
 
 static void stage_transport(fg_batch* B, cudaStream_t st) {
   FG_CUDA(cudaMemsetAsync(B->counts.p, 0, B->ncap * sizeof(uint32_t), st));
@@ -782,6 +807,9 @@ static void plan(fg_batch* B, const fg_batch_options* opt) {
   B->A.alloc(std::max<unsigned long long>(cap, 1), st);
   B->Q.alloc(std::max<unsigned long long>(cap, 1), st);
   B->D.alloc(std::max<unsigned long long>(cap, 1), st);
+  B->EA.alloc(std::max<unsigned long long>(cap, 1), st);
+  B->EQ.alloc(std::max<unsigned long long>(cap, 1), st);
+  B->ED.alloc(std::max<unsigned long long>(cap, 1), st);
   B->keys.alloc(std::max<unsigned long long>(cap, 1), st);
   B->parent.alloc(std::max<unsigned long long>(cap, 1), st);
   B->counts.alloc(std::max<unsigned long long>(cap, 1), st);
@@ -877,11 +905,11 @@ unsigned long long tile_footprint(const fg_tile_params& p, unsigned long long* s
   uint32_t bits = 0;
   while ((1u << bits) < static_cast<uint32_t>(std::ceil(side))) ++bits;
   const unsigned long long px = static_cast<unsigned long long>(p.width_px) * p.height_px;
-  // Per crystal slot: records 48, key 8, links and flags 36, expansion 8, scan prep 160, bin
+  // Per crystal slot: records 48 (and 48 in the tree's element order), key 8, links and flags 36, expansion 8, scan prep 160, bin
   // entries 32, tree elements 88 (order, node of, two copies of three 8-byte keys, flags, prefix
   // sums, ranks, final order, leaf of) and 0.8 nodes of 224 B (plus slack); cells 4 B; bricks
   // 8 B; photon order; images.
-  return static_cast<unsigned long long>(s.ccap) * 580ull + static_cast<unsigned long long>(s.gw) * s.gh * s.gd * 4ull +
+  return static_cast<unsigned long long>(s.ccap) * 628ull + static_cast<unsigned long long>(s.gw) * s.gh * s.gd * 4ull +
          (8ull << (2 * s.slot_bits)) + static_cast<unsigned long long>(t.P) * 4ull +
          (1ull << (2 * bits)) * 12ull + px * 8ull + 4096ull;
 }
@@ -1135,9 +1163,10 @@ fg_status fg_batch_wait(fg_batch* b, fg_batch_stats* stats) {
     s.graph = b->exec ? 1u : 0u;
     // Own kernels per run: Bridson (all colour classes in one launch; it also counts the points), thin +
     // brick counts, emit, set_n, photon order x2, transport, maxdim + threshold + developed list + link +
-    // roots + finalize, scan-tree inputs, scan prep, two bin passes, scan, density, and the two tree builds (each
-    // level's launches included, also those that find no work; CUB scans not counted).
-    s.kernel_launches = 1 + 2 + 1 + 1 + 2 + 1 + 6 + 1 + 1 + 2 + 1 + 1 + 2 * rtree_kernel_launches(b->rt);
+    // roots + finalize, scan-tree inputs, scan prep, two bin passes, scan, density, the crystal records in
+    // the transport tree's order, and the two tree builds (each level's launches included, also those that
+    // find no work; CUB scans not counted).
+    s.kernel_launches = 1 + 2 + 1 + 1 + 2 + 1 + 6 + 1 + 1 + 2 + 1 + 1 + 1 + 2 * rtree_kernel_launches(b->rt);
     b->stats = s;
     if (stats) *stats = s;
   });

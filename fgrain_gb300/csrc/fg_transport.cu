@@ -251,12 +251,37 @@ __global__ void k_replay_rays(const double* __restrict__ org, const double* __re
 }
 
 // ---------------------------------------------------------------------------------------------
+// Crystal records in a tree's element order: out[p] = in[ridx[p]] for p < n, so that the crystals
+// of a leaf lie next to each other (TileDesc).
+__global__ void k_element_records(const uint32_t* __restrict__ ridx, uint32_t n, const float4* __restrict__ a,
+                                  const float4* __restrict__ q, const float4* __restrict__ d, float4* oa,
+                                  float4* oq, float4* od, uint32_t* err) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const uint32_t s = ridx[p];
+  if (!index_ok(s < n, err, SITE_LEAF, s, n)) return;
+  oa[p] = a[s];
+  oq[p] = q[s];
+  od[p] = d[s];
+}
+
+// The transport descriptor of an emulsion; a, q, d are its crystal records in the tree's element
+// order (records, 3 n float4 written here).
 TileDesc make_tile_desc(const fg_emulsion* em, const float* tile_dev, uint32_t tw, uint32_t th,
-                        const fg_exposure_cfg& cfg, uint64_t seed, uint32_t* counts) {
+                        const fg_exposure_cfg& cfg, uint64_t seed, uint32_t* counts, float4* records,
+                        uint32_t* err, cudaStream_t st) {
   TileDesc t{};
-  t.a = em->a.p;
-  t.q = em->q.p;
-  t.d = em->d.p;
+  float4* oa = records;
+  float4* oq = records + em->n;
+  float4* od = records + 2ull * em->n;
+  if (em->n) {
+    k_element_records<<<grid_for(em->n, 256), 256, 0, st>>>(em->rt.ridx.p, em->n, em->a.p, em->q.p, em->d.p, oa, oq,
+                                                             od, err);
+    FG_CUDA(cudaGetLastError());
+  }
+  t.a = oa;
+  t.q = oq;
+  t.d = od;
   t.rnode = em->rt.rnode.p;
   t.rleaf = em->rt.rleaf.p;
   t.ridx = em->rt.ridx.p;
@@ -306,7 +331,8 @@ void launch_transport_shape(const TileDesc* tiles_dev, int ntiles, unsigned long
 void expose(fg_engine* e, fg_emulsion* em, const float* tile_dev, uint32_t tw, uint32_t th,
             const fg_exposure_cfg& cfg, uint64_t seed, unsigned long long* photons_out) {
   cudaStream_t st = e->stream;
-  TileDesc t = make_tile_desc(em, tile_dev, tw, th, cfg, seed, em->counts.p);
+  DBuf<float4> records(3ull * std::max<uint32_t>(em->n, 1), st);
+  TileDesc t = make_tile_desc(em, tile_dev, tw, th, cfg, seed, em->counts.p, records.p, e->d_err, st);
   if (photons_out) *photons_out = t.P;
   if (t.P == 0 || em->n == 0) return;
   DBuf<TileDesc> td(1, st);

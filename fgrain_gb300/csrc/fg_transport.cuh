@@ -13,7 +13,9 @@ constexpr uint32_t WALK_NONE = 0xffffffffu;
 
 // Everything one tile's transport needs, 16-byte aligned for vector loads.  The walk runs over the
 // tile's reference tree (fg_rtree.cuh): rnode / rleaf indexed by tile-local node id, ridx by
-// tile-local element position (a leaf's crystals in the reference's order).
+// tile-local element position (a leaf's crystals in the reference's order).  The crystal records
+// a, q, d are in that element order too (position p holds the crystal ridx[p]), so a leaf's
+// crystals lie next to each other and are read without their slots.
 struct __align__(16) TileDesc {
   const float4* a;
   const float4* q;
@@ -240,9 +242,8 @@ __device__ __forceinline__ void leaf_step(const TileDesc& t, const Photon& ph, B
   const float step = w.step;
   const uint32_t b = ph.b - 1;
   for (uint32_t k = 0; k < L.y; ++k) {
-    const uint32_t s = __ldg(&t.ridx[L.x + k]);
-    if (!index_ok(s < t.n, err, SITE_LEAF, s, t.n)) continue;
-    const float4 a = __ldg(&t.a[s]), d = __ldg(&t.d[s]);
+    const uint32_t e = L.x + k;  // element position: the crystal ridx[e]
+    const float4 a = __ldg(&t.a[e]), d = __ldg(&t.d[e]);
     // The crystal lies in the ball of radius sqrt(3) m (a cube) or m (the ellipsoid shapes)
     // around its centre; a ball the step's segment misses, with a margin well above FP32
     // rounding, cannot give a hit inside the step, so the geometry test is skipped (the hits
@@ -255,7 +256,7 @@ __device__ __forceinline__ void leaf_step(const TileDesc& t, const Photon& ph, B
       const float ex = wx - tc * dir.x, ey = wy - tc * dir.y, ez = wz - tc * dir.z;
       if (ex * ex + ey * ey + ez * ez > R * R) continue;
     }
-    const float4 q = __ldg(&t.q[s]);
+    const float4 q = __ldg(&t.q[e]);
     float t0, t1;
     if (!fintersect(a, q, d, 1.0f, pos, dir, t0, t1)) continue;
     if (!(t0 < step)) continue;
@@ -267,7 +268,10 @@ __device__ __forceinline__ void leaf_step(const TileDesc& t, const Photon& ph, B
     const float expected = w.E * p * a.w * 5.0f;
     const float fl = floorf(expected);
     const uint32_t cnt = static_cast<uint32_t>(fl) + (uf(word(w.r, w.nh & 3)) < expected - fl ? 1u : 0u);
-    if (cnt) add_counts(t.counts, s, cnt);
+    if (cnt) {
+      const uint32_t s = __ldg(&t.ridx[e]);
+      if (index_ok(s < t.n, err, SITE_LEAF, s, t.n)) add_counts(t.counts, s, cnt);
+    }
     w.E *= fmaxf(1.0f - p * 0.9f, 0.05f);
     ++w.nh;
   }
