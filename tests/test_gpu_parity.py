@@ -317,6 +317,33 @@ def test_empty_single_and_zero_opacity(engine):
     assert (buf == 1.0).all()
 
 
+@pytest.mark.parametrize("max_bounces", [0, 1, 2, 5])
+def test_production_transport_bounce_limits(engine, max_bounces):
+    """The bounce loop's bound (transport.rs:101): the device ends and begins bounces for groups of
+    idle lanes and refills lanes whose packets died, so short limits stress those paths.  With no
+    bounce nothing is absorbed; with one, two or five the counts follow the oracle's crystal by
+    crystal, as at the stock limit (test_c1_production_transport_matches_oracle)."""
+    cfg = reference_cfg("tri-x", 96 * C1_PX, 96 * C1_PX)
+    cr = orc.synthesize(cfg, 9)
+    tile = ramp_tile(96, 96)
+    base = tile_worker_exposure_cfg(1.0)
+    ecfg = fg.ExposureConfig(base.photons_per_sq_um, base.illumination_angle_rad, base.crystal_absorption_coeff,
+                             max_bounces)
+    ocr = cr.copy()
+    P, _, _ = orc.expose(ocr, cfg, tile, ecfg, 3, orc.FAITHFUL)
+    em = upload(cr, cfg, engine)
+    fg.expose_emulsion(em, tile, ecfg, 3)
+    got = em.latent_counts().astype(np.int64)
+    ref = ocr.latent.astype(np.int64)
+    assert engine.timings()["photons"] == P
+    if max_bounces == 0:
+        assert got.sum() == 0 and ref.sum() == 0
+        return
+    assert ref.sum() > 0
+    assert (got == ref).mean() > 0.99
+    assert abs(got.sum() - ref.sum()) / ref.sum() < 5e-3
+
+
 def test_zero_exposure_leaves_no_latent_image(engine):
     cfg = reference_cfg("tri-x", 20.0, 20.0)
     cr = orc.synthesize(cfg, 2)
