@@ -44,6 +44,8 @@ void launch_scan(const ScanTile* tiles, int ntiles, unsigned long long nbins, un
                  unsigned long long* stats, cudaStream_t st);
 void launch_scan_prep(const ScanTile* tiles, int ntiles, unsigned long long nslots, ScanPrep* prep,
                       cudaStream_t st);
+void launch_scan_prep_list(const ScanTile* tiles, int ntiles, const uint32_t* list, const uint32_t* nlist,
+                           unsigned long long cap, ScanPrep* prep, cudaStream_t st);
 uint32_t scan_bin_px(uint32_t spp);
 
 // Nodes per crystal slot of the tile trees: the reference tree has about 0.67 nodes per crystal and
@@ -633,7 +635,7 @@ static void stage_scan(fg_batch* B, cudaStream_t st) {
   // and the touch queries are done with the first tree by now).
   k_scan_tree_tiles<<<grid_for(B->ntiles, 128), 128, 0, st>>>(B->d_bt.p, nt, B->devscan.p, B->devlist.p, B->rt_scan.p);
   rtree_build(B->rt, e->d_err, st, B->rt_scan.p);
-  launch_scan_prep(B->d_sc.p, nt, B->ncap, B->prep.p, st);
+  launch_scan_prep_list(B->d_sc.p, nt, B->devlist.p, B->devscan.p + B->ncap, B->ncap, B->prep.p, st);
   FG_CUDA(cudaMemsetAsync(B->bin_cnt.p, 0, (B->nbins + 1) * sizeof(uint32_t), st));
   FG_CUDA(cudaMemsetAsync(B->bin_cur.p, 0, (B->nbins + 1) * sizeof(uint32_t), st));
   k_bin_b<<<G, 256, 0, st>>>(B->d_bt.p, nt, B->ncap, B->developed.p, B->rt.box64.p, B->rt.leafof.p, B->bin_cnt.p,

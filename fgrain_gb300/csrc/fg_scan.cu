@@ -242,6 +242,34 @@ __global__ void k_scan_prep(const ScanTile* __restrict__ tiles, int ntiles, unsi
   prep[g] = P;
 }
 
+// k_scan_prep over a list of the developed crystals' slots (*nlist of them, at most cap): one
+// thread per listed crystal, so the FP64 derivation runs with every lane busy.
+__global__ void k_scan_prep_list(const ScanTile* __restrict__ tiles, int ntiles, const uint32_t* __restrict__ list,
+                                 const uint32_t* __restrict__ nlist, unsigned long long cap,
+                                 ScanPrep* __restrict__ prep) {
+  const unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+  if (i >= cap || i >= *nlist) return;
+  const unsigned long long g = list[i];
+  int lo = 0, hi = ntiles - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tiles[mid].slot_base <= g) lo = mid; else hi = mid - 1;
+  }
+  const ScanTile& t = tiles[lo];
+  const unsigned long long s = g - t.slot_base;
+  if (s >= t.n || !t.developed[s]) return;
+  ScanPrep P;
+  prep_crystal(t, static_cast<uint32_t>(s), P);
+  prep[g] = P;
+}
+
+void launch_scan_prep_list(const ScanTile* tiles, int ntiles, const uint32_t* list, const uint32_t* nlist,
+                           unsigned long long cap, ScanPrep* prep, cudaStream_t st) {
+  if (cap == 0) return;
+  k_scan_prep_list<<<grid_for(cap, 128), 128, 0, st>>>(tiles, ntiles, list, nlist, cap, prep);
+  FG_CUDA(cudaGetLastError());
+}
+
 void launch_scan_prep(const ScanTile* tiles, int ntiles, unsigned long long nslots, ScanPrep* prep,
                       cudaStream_t st) {
   if (nslots == 0) return;
