@@ -275,3 +275,36 @@ def test_jpeg_reads_photographs_written_by_another_encoder(path):
     assert edges < 1.25 * inner
     again = imageio.decode_jpeg(imageio.encode_jpeg(img, 95))
     assert psnr(again, img) > 35.0
+
+
+def test_corrupt_files_decode_or_raise():
+    """Bit flips, truncations and overwritten runs in JPEG and WebP files: the decoders return an
+    image or raise ImageFormatError, never crash (a command line reads whatever file it is given)."""
+    rng = np.random.default_rng(7)
+    img = smooth(37, 53, 3)
+    bases = [("j", imageio.encode_jpeg(img, 75)), ("j", imageio.encode_jpeg(img[:, :, 0], 50)),
+             ("j", imageio.encode_jpeg(img, 90, W.FG_JPEG_SUBSAMPLE_422 | W.FG_JPEG_SEPARATE_SCANS | W.FG_JPEG_RESTART(2))),
+             ("w", imageio.encode_webp(img, 0xFF)), ("w", imageio.encode_webp(img, W.FG_WEBP_DEFAULT)),
+             ("w", imageio.encode_webp(img, 0))]
+    decoded = 0
+    for it in range(1200):
+        kind, base = bases[it % len(bases)]
+        b = bytearray(base)
+        m = rng.integers(0, 3)
+        if m == 0:
+            for _ in range(rng.integers(1, 8)):
+                i = rng.integers(0, len(b))
+                b[i] ^= 1 << int(rng.integers(0, 8))
+        elif m == 1:
+            b = b[:rng.integers(0, len(b))]
+        else:
+            i = rng.integers(0, len(b))
+            j = min(len(b), i + int(rng.integers(1, 64)))
+            b[i:j] = rng.integers(0, 256, j - i).astype(np.uint8).tobytes()
+        try:
+            out = imageio.decode_jpeg(bytes(b)) if kind == "j" else imageio.decode_webp_rgba(bytes(b))
+            assert out.dtype == np.uint8 and out.size > 0
+            decoded += 1
+        except imageio.ImageFormatError:
+            pass
+    assert 0 < decoded < 1200
